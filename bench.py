@@ -1,0 +1,305 @@
+"""Benchmark of the XC grid path: E_xc forward + V_xc backward, grid points per second.
+
+Workload (synthetic, seeded): spin 2, n_ao = 512 s/p/d Gaussians with centres
+in a 12 A box, n_grid = 2^20 points in a 20 A box, log-normal weights,
+D_sigma = C diag(1 x 64, 0) C^T, B88 + LYP energy densities (lsda_x + b88
+correction + lyp, unit coefficients).  One step = one E_xc + V_xc evaluation
+(the reference's energy_predictor.xc_energy_and_grads, train.py:86) with the
+molecule resident in HBM.
+
+    python bench.py [--gpus N --steps K --warmup W] [--form tf32x3|fp64] [--impl reference]
+
+Prints one JSON line (rank 0).  Under torchrun each rank evaluates its own
+2^20-point grid slice (weak scaling) and the per-rank partial E_xc and V_xc
+are summed with one all-reduce, as the grid sum shards over points.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "E_xc fwd+bwd grid-pts/s, mixed vs FP64 form on 1 GB300 at |dE|<=1e-6 Ha"
+UNIT = "grid-pts/s"
+N_AO, N_GRID, N_OCC, SEED = 512, 1 << 20, 64, 0
+WORKLOAD = "synthetic XC contraction: spin 2, n_ao 512 (s/p/d Gaussians), n_grid 2^20, B88+LYP, E_xc + V_xc"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], p["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"gdft_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(n_sample: int, threads: int):
+    """The oracle (FP64 CPU restatement) on a bounded sample of the same workload."""
+    import torch
+
+    import oracle
+    from graddft_gb300 import synthetic
+
+    torch.set_num_threads(threads)
+    wl = synthetic.make_workload(N_GRID, N_AO, N_OCC, SEED)
+    idx = slice(0, n_sample)
+    ao, g1, g2 = oracle.eval_ao_planes(wl.basis, wl.coords[idx])
+    w = wl.weights[idx]
+    t0 = time.perf_counter()
+    oracle.xc_energy_and_grads("BLYP", wl.rdm1, ao, g1, g2, w)
+    dt = time.perf_counter() - t0
+    return n_sample / dt, dt
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path (oracle restatement) timed on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n_sample = args.cpu_sample
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, _ = cpu_baseline(n_sample, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n_sample / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_ao": N_AO, "n_grid": N_GRID, "functional": "B88+LYP"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n_sample} of the 2^20 grid points (same basis, D, weights), "
+                                   "FP64 torch-CPU restatement with autograd for V_xc"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--form", default=None, choices=["tf32x3", "fp64"])
+    ap.add_argument("--n-grid", type=int, default=N_GRID)
+    ap.add_argument("--n-ao", type=int, default=N_AO)
+    ap.add_argument("--fp64-grid", type=int, default=1 << 16,
+                    help="grid points of the FP64-form measurement (its rate is per point)")
+    ap.add_argument("--cpu-sample", type=int, default=4096)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from graddft_gb300 import _lib, build, engine, synthetic
+
+    build.build()
+    lib = _lib.load()
+    form = args.form or "fp64"
+    dev = torch.device("cuda", local)
+    fn = engine.make_functional([_lib.COL_LSDA, _lib.COL_B88, _lib.COL_LYP], [1.0])
+
+    def resident(n_grid, precision, seed):
+        wl = synthetic.make_workload(n_grid, args.n_ao, N_OCC, seed)
+        r = engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, precision, dev)
+        return r, torch.as_tensor(wl.rdm1, device=dev)
+
+    # Each rank owns its own grid slice (weak scaling); D and the basis are shared.
+    r, rdm1 = resident(args.n_grid, form, SEED)
+    if world > 1:
+        # same molecule, rank-specific grid slice
+        wl = synthetic.make_workload(args.n_grid, args.n_ao, N_OCC, SEED)
+        coords = wl.coords + 1e-3 * rank
+        r = engine.Resident.from_basis(wl.basis.packed(), coords, wl.weights, form, dev)
+    exc = torch.empty((), dtype=torch.float64, device=dev)
+    vxc = torch.empty((2, args.n_ao, args.n_ao), dtype=torch.float64, device=dev)
+
+    def step():
+        r.xc_energy_and_grads(rdm1, fn, None, True, exc, vxc)
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.all_reduce(vxc)
+            dist.all_reduce(exc)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    lib.gdft_profile_reset()
+    lib.gdft_profile_enable(1)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    lib.gdft_profile_enable(0)
+    ms = e0.elapsed_time(e1)
+    stage = {}
+    for name, sid in (("density", _lib.STAGE_DENSITY), ("point", _lib.STAGE_POINT), ("vxc", _lib.STAGE_VXC),
+                      ("reduce", _lib.STAGE_REDUCE)):
+        import ctypes
+
+        t, n = ctypes.c_double(), ctypes.c_int64()
+        _lib.check(lib.gdft_profile_read(sid, ctypes.byref(t), ctypes.byref(n)))
+        stage[name] = (t.value, n.value)
+    launches = sum(n for _, n in stage.values())
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    ms_step = ms / args.steps
+    value = world * args.n_grid / (ms_step * 1e-3)
+
+    # e2e: the same call with host buffers (pinned rdm1 in, E and V out) per step.
+    h_rdm1 = rdm1.cpu().pin_memory()
+    h_v = torch.empty(vxc.shape, dtype=torch.float64).pin_memory()
+    h_e = torch.empty((), dtype=torch.float64).pin_memory()
+    d_rdm1 = torch.empty_like(rdm1)
+    for _ in range(2):
+        d_rdm1.copy_(h_rdm1, non_blocking=True)
+        r.xc_energy_and_grads(d_rdm1, fn, None, True, exc, vxc)
+        h_v.copy_(vxc, non_blocking=True)
+        h_e.copy_(exc, non_blocking=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        d_rdm1.copy_(h_rdm1, non_blocking=True)
+        r.xc_energy_and_grads(d_rdm1, fn, None, True, exc, vxc)
+        h_v.copy_(vxc, non_blocking=True)
+        h_e.copy_(exc, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e = {"value": args.n_grid / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": rdm1.numel() * 8,
+           "d2h_bytes_per_step": vxc.numel() * 8 + 8,
+           "note": "molecule (grid, AO tables) resident as after to_device_arrays; rdm1 in, E_xc and V_xc out"}
+
+    # Roofline of the dominant kernel.
+    hbm, bf16, src = _peaks()
+    dom = max(("density", "vxc"), key=lambda k: stage[k][0])
+    t_dom, n_dom = stage[dom]
+    flops_launch = 16.0 * args.n_grid * args.n_ao ** 2  # 2 spins x 4 planes x 2 N n^2 per contraction
+    achieved = flops_launch / (t_dom / n_dom * 1e-3) / 1e12
+    if form == "fp64":
+        peak, bound, peak_src = 1.25, "fp64", "nominal GB300 FP64 rate (no measured FP64 peak)"
+    else:
+        peak, bound, peak_src = bf16, "tensor", f"{src} bf16 dense (TF32 pipe nominally runs at half of it)"
+    roof = {"bound": bound, "kernel": f"{dom}_{form}", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+            "flops_per_launch": flops_launch,
+            "stage_ms_per_step": {k: v[0] / args.steps for k, v in stage.items()}}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if form == "fp64" else "tf32x3",
+        "data": "synthetic (seeded Gaussian basis evaluated on the device)",
+        "config": {"workload": WORKLOAD, "n_ao": args.n_ao, "n_grid": args.n_grid, "form": form,
+                   "functional": "B88+LYP", "l2": "inputs larger than L2 (5 FP64 AO planes, "
+                                                 f"{5 * args.n_grid * args.n_ao * 8 / 2**30:.1f} GiB)"},
+        "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        v, dt = cpu_baseline(args.cpu_sample, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{args.cpu_sample} grid points of the same workload ({dt:.1f} s), "
+                                          "FP64 torch-CPU restatement with autograd"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

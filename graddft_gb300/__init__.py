@@ -1,0 +1,41 @@
+"""GB300-native XC grid path of Grad DFT.
+
+The public names mirror ``grad_dft`` (grad_dft/__init__.py) for the XC path:
+containers, density primitives, the Functional plugin API, the classical
+functionals and ``energy_predictor``.  Compute runs in ``libgdft_xc.so``
+(hand-written sm_103a CUDA behind a C ABI); there is no CPU fallback.
+"""
+from .molecule import Grid, Molecule, abs_clip, density, grad_density, lapl_density, kinetic_density
+from .functional import (
+    Functional,
+    canonicalize_inputs,
+    dm21_combine_cinputs,
+    dm21_combine_densities,
+    dm21_densities,
+    stack_densities,
+)
+from .popular_functionals import (
+    B3LYP,
+    B88,
+    BLYP,
+    LSDA,
+    LYP,
+    PW92,
+    VWN,
+    b3lyp_combine,
+    b3lyp_exhf_densities,
+    b88_density,
+    lsda_density,
+    lyp_density,
+    pw92_densities,
+    vwn_density,
+)
+from .train import energy_predictor
+
+__all__ = [
+    "Grid", "Molecule", "abs_clip", "density", "grad_density", "lapl_density", "kinetic_density",
+    "Functional", "canonicalize_inputs", "dm21_combine_cinputs", "dm21_combine_densities", "dm21_densities",
+    "stack_densities", "B3LYP", "B88", "BLYP", "LSDA", "LYP", "PW92", "VWN", "b3lyp_combine",
+    "b3lyp_exhf_densities", "b88_density", "lsda_density", "lyp_density", "pw92_densities", "vwn_density",
+    "energy_predictor",
+]

@@ -1,0 +1,128 @@
+"""ctypes binding of libgdft_xc.so (the C ABI declared in include/gdft.h).
+
+The library is built in-tree by ``graddft_gb300.build``.  There is no CPU or
+eager-PyTorch fallback: if the shared library is missing, importing the
+compute path raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libgdft_xc.so")
+
+GDFT_OK = 0
+GDFT_ERR_INVALID = 1
+GDFT_ERR_ALIGNMENT = 2
+GDFT_ERR_WORKSPACE = 3
+GDFT_ERR_CUDA = 4
+GDFT_ERR_DEVICE = 5
+GDFT_ERR_UNSUPPORTED = 6
+
+GDFT_FP64 = 0
+GDFT_TF32X3 = 1
+
+COL_LSDA, COL_B88, COL_VWN, COL_LYP, COL_PW92, COL_HF, COL_DM21_LDA, COL_HF_W0, COL_HF_W1 = range(9)
+MAX_COLS = 8
+
+# Every symbol include/gdft.h declares.
+EXPORTS = (
+    "gdft_abi_version", "gdft_last_error", "gdft_molecule_bytes", "gdft_molecule_init", "gdft_molecule_load",
+    "gdft_molecule_eval_basis", "gdft_workspace_bytes", "gdft_density", "gdft_xc_energy_and_grads",
+    "gdft_energy_densities", "gdft_integrate", "gdft_integrate_workspace_bytes", "gdft_fock", "gdft_coulomb",
+    "gdft_profile_enable", "gdft_profile_reset", "gdft_profile_read",
+)
+STAGE_AO, STAGE_DENSITY, STAGE_POINT, STAGE_VXC, STAGE_REDUCE, STAGE_MLP = range(6)
+
+
+class GdftFunctional(ctypes.Structure):
+    _fields_ = [
+        ("n_cols", ctypes.c_int32),
+        ("cols", ctypes.c_int32 * MAX_COLS),
+        ("n_coeffs", ctypes.c_int32),
+        ("coeffs", ctypes.c_double * MAX_COLS),
+        ("clip", ctypes.c_double),
+    ]
+
+
+class GdftMolecule(ctypes.Structure):
+    _fields_ = [
+        ("n_grid", ctypes.c_int64),
+        ("n_grid_pad", ctypes.c_int64),
+        ("n_ao", ctypes.c_int32),
+        ("ld", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("buffer", ctypes.c_void_p),
+        ("buffer_bytes", ctypes.c_size_t),
+    ]
+
+
+_lib = None
+_lock = threading.Lock()
+
+P = ctypes.c_void_p
+I32, I64, SZ, D = ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t, ctypes.c_double
+PMOL = ctypes.POINTER(GdftMolecule)
+PFN = ctypes.POINTER(GdftFunctional)
+
+_SIGS = {
+    "gdft_abi_version": ([], ctypes.c_int),
+    "gdft_last_error": ([], ctypes.c_char_p),
+    "gdft_molecule_bytes": ([I64, I32, I32, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_molecule_init": ([PMOL, I64, I32, I32, P, SZ], ctypes.c_int),
+    "gdft_molecule_load": ([PMOL, P, P, P, P, P], ctypes.c_int),
+    "gdft_molecule_eval_basis": ([PMOL, P, P, P, P], ctypes.c_int),
+    "gdft_workspace_bytes": ([PMOL, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_density": ([PMOL, P, P, P, P, P, P, SZ, P], ctypes.c_int),
+    "gdft_xc_energy_and_grads": ([PMOL, P, PFN, P, I32, P, P, P, SZ, P], ctypes.c_int),
+    "gdft_energy_densities": ([PMOL, P, PFN, P, I32, P, P, SZ, P], ctypes.c_int),
+    "gdft_integrate": ([I64, I32, P, I32, P, P, D, P, P, SZ, P], ctypes.c_int),
+    "gdft_integrate_workspace_bytes": ([I64, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_fock": ([I32, P, P, P, D, P, P], ctypes.c_int),
+    "gdft_coulomb": ([I32, P, P, P, D, P, P, P], ctypes.c_int),
+    "gdft_profile_enable": ([I32], ctypes.c_int),
+    "gdft_profile_reset": ([], ctypes.c_int),
+    "gdft_profile_read": ([I32, ctypes.POINTER(D), ctypes.POINTER(I64)], ctypes.c_int),
+}
+
+
+def load(path: str | None = None):
+    """Load libgdft_xc.so and declare the C signatures (raises if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = path or LIB_PATH
+        if not os.path.exists(path):
+            raise ImportError(
+                f"libgdft_xc.so not found at {path}; build it with `python -m graddft_gb300.build` "
+                "(the XC path has no CPU fallback)")
+        lib = ctypes.CDLL(path)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        if lib.gdft_abi_version() != 1:
+            raise ImportError("libgdft_xc.so ABI version mismatch")
+        _lib = lib
+        return lib
+
+
+class GdftError(RuntimeError):
+    pass
+
+
+def check(rc: int) -> None:
+    if rc == GDFT_OK:
+        return
+    msg = load().gdft_last_error().decode(errors="replace")
+    if rc in (GDFT_ERR_INVALID, GDFT_ERR_WORKSPACE):
+        raise ValueError(msg)
+    if rc == GDFT_ERR_ALIGNMENT:
+        raise TypeError(msg)
+    if rc == GDFT_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    raise GdftError(msg)

@@ -1,0 +1,444 @@
+// api.cu - the C ABI (include/gdft.h): validation, layouts, launch order.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace gdft {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int check_cuda(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return GDFT_OK;
+  set_error("%s: %s", what, cudaGetErrorString(e));
+  return GDFT_ERR_CUDA;
+}
+
+static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// ---- stage timing ---------------------------------------------------------
+struct StageRec {
+  cudaEvent_t a, b;
+};
+static bool g_prof = false;
+static StageRec *g_recs[GDFT_STAGE_COUNT] = {nullptr};
+static int g_nrec[GDFT_STAGE_COUNT] = {0}, g_cap[GDFT_STAGE_COUNT] = {0};
+
+struct StageTimer {
+  int stage;
+  cudaStream_t st;
+  StageRec *rec = nullptr;
+  StageTimer(int s, cudaStream_t stream) : stage(s), st(stream) {
+    if (!g_prof) return;
+    if (g_nrec[s] == g_cap[s]) {
+      const int cap = g_cap[s] ? 2 * g_cap[s] : 64;
+      StageRec *n = new StageRec[cap];
+      for (int i = 0; i < g_cap[s]; ++i) n[i] = g_recs[s][i];
+      for (int i = g_cap[s]; i < cap; ++i) {
+        cudaEventCreate(&n[i].a);
+        cudaEventCreate(&n[i].b);
+      }
+      delete[] g_recs[s];
+      g_recs[s] = n;
+      g_cap[s] = cap;
+    }
+    rec = &g_recs[s][g_nrec[s]++];
+    cudaEventRecord(rec->a, st);
+  }
+  ~StageTimer() {
+    if (rec) cudaEventRecord(rec->b, st);
+  }
+};
+
+MolLayout mol_layout(int64_t n_grid, int n_ao, int precision) {
+  MolLayout L;
+  L.np = round_up(n_grid, kPointTile);
+  L.ld = (int)round_up(n_ao, kAoPad);
+  size_t off = 0;
+  L.off_tab = off;
+  off = align256(off + (size_t)kPlanes * L.plane_elems() * sizeof(double));
+  L.off_w = off;
+  off = align256(off + (size_t)L.np * sizeof(double));
+  L.off_tc = off;
+  (void)precision;
+  L.bytes = off;
+  return L;
+}
+
+WsLayout ws_layout(const gdft_molecule *m) {
+  WsLayout W;
+  const int64_t np = m->n_grid_pad;
+  W.n_eblocks = xc_point_blocks(np);
+  W.n_vsplit = vxc_f64_splits(np, m->n_ao);
+  size_t off = 0;
+  W.off_feat = off;
+  off = align256(off + (size_t)2 * kFeat * np * sizeof(double));
+  W.off_coef = off;
+  off = align256(off + (size_t)2 * kFeat * np * sizeof(double));
+  W.off_epart = off;
+  off = align256(off + (size_t)W.n_eblocks * sizeof(double));
+  W.off_vpart = off;
+  off = align256(off + (size_t)W.n_vsplit * 2 * m->n_ao * m->n_ao * sizeof(double));
+  W.off_err = off;
+  off = align256(off + 64);
+  W.off_scratch = off;
+  W.scratch_bytes = 0;
+  W.bytes = off;
+  return W;
+}
+
+static int check_mol(const gdft_molecule *m) {
+  if (m == nullptr || m->buffer == nullptr) {
+    set_error("molecule is not initialised");
+    return GDFT_ERR_INVALID;
+  }
+  if (m->n_grid <= 0 || m->n_ao <= 0) {
+    set_error("molecule has n_grid=%lld n_ao=%d", (long long)m->n_grid, m->n_ao);
+    return GDFT_ERR_INVALID;
+  }
+  const MolLayout L = mol_layout(m->n_grid, m->n_ao, m->precision);
+  if (m->buffer_bytes < L.bytes || m->n_grid_pad != L.np || m->ld != L.ld) {
+    set_error("molecule descriptor does not match its layout");
+    return GDFT_ERR_INVALID;
+  }
+  return GDFT_OK;
+}
+
+static int check_ws(const gdft_molecule *m, void *ws, size_t ws_bytes) {
+  const WsLayout W = ws_layout(m);
+  if (ws == nullptr || ws_bytes < W.bytes) {
+    set_error("workspace of %zu bytes is smaller than the %zu bytes required", ws_bytes, W.bytes);
+    return GDFT_ERR_WORKSPACE;
+  }
+  if (((uintptr_t)ws & 255u) != 0) {
+    set_error("workspace must be 256-byte aligned");
+    return GDFT_ERR_ALIGNMENT;
+  }
+  return GDFT_OK;
+}
+
+static int check_aligned8(const void *p, const char *name) {
+  if (((uintptr_t)p & 7u) != 0) {
+    set_error("%s must be 8-byte aligned", name);
+    return GDFT_ERR_ALIGNMENT;
+  }
+  return GDFT_OK;
+}
+
+static int check_functional(const gdft_functional *fn, const double *ehf, int n_omega) {
+  if (fn == nullptr || fn->n_cols < 1 || fn->n_cols > GDFT_MAX_COLS) {
+    set_error("functional must have 1..%d energy-density columns", GDFT_MAX_COLS);
+    return GDFT_ERR_INVALID;
+  }
+  if (!(fn->n_coeffs == 1 || fn->n_coeffs == fn->n_cols)) {
+    set_error("functional has %d coefficients for %d columns", fn->n_coeffs, fn->n_cols);
+    return GDFT_ERR_INVALID;
+  }
+  for (int i = 0; i < fn->n_cols; ++i) {
+    const int c = fn->cols[i];
+    if (c < GDFT_COL_LSDA || c > GDFT_COL_HF_W1) {
+      set_error("unknown energy-density column %d", c);
+      return GDFT_ERR_INVALID;
+    }
+    const bool needs_hf = c == GDFT_COL_HF || c == GDFT_COL_HF_W0 || c == GDFT_COL_HF_W1;
+    if (needs_hf && (ehf == nullptr || n_omega < (c == GDFT_COL_HF_W1 ? 2 : 1))) {
+      set_error("energy-density column %d needs ehf with enough omegas (got n_omega=%d)", c, n_omega);
+      return GDFT_ERR_INVALID;
+    }
+  }
+  return GDFT_OK;
+}
+
+static const double *mol_tab(const gdft_molecule *m) {
+  return (const double *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_tab);
+}
+static const double *mol_w(const gdft_molecule *m) {
+  return (const double *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_w);
+}
+
+// Density stage into ws.feat.
+static int run_density(const gdft_molecule *m, const double *rdm1, char *ws, cudaStream_t st) {
+  const WsLayout W = ws_layout(m);
+  double *feat = (double *)(ws + W.off_feat);
+  if (m->precision == GDFT_FP64) {
+    StageTimer tm(GDFT_STAGE_DENSITY, st);
+    return check_cuda(launch_dens_f64(mol_tab(m), m->n_grid_pad, m->ld, m->n_ao, rdm1, feat, st), "dens_f64");
+  }
+  set_error("precision %d is not available in this build", m->precision);
+  return GDFT_ERR_UNSUPPORTED;
+}
+
+}  // namespace gdft
+
+using namespace gdft;
+
+extern "C" {
+
+int gdft_abi_version(void) { return GDFT_ABI_VERSION; }
+
+int gdft_profile_enable(int32_t enable) {
+  g_prof = enable != 0;
+  return GDFT_OK;
+}
+
+int gdft_profile_reset(void) {
+  for (int s = 0; s < GDFT_STAGE_COUNT; ++s) g_nrec[s] = 0;
+  return GDFT_OK;
+}
+
+int gdft_profile_read(int32_t stage, double *total_ms, int64_t *launches) {
+  if (stage < 0 || stage >= GDFT_STAGE_COUNT || total_ms == nullptr || launches == nullptr) {
+    set_error("gdft_profile_read: invalid arguments");
+    return GDFT_ERR_INVALID;
+  }
+  double t = 0.0;
+  for (int i = 0; i < g_nrec[stage]; ++i) {
+    float ms = 0.0f;
+    cudaError_t e = cudaEventSynchronize(g_recs[stage][i].b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, g_recs[stage][i].a, g_recs[stage][i].b);
+    if (e != cudaSuccess) return check_cuda(e, "profile_read");
+    t += ms;
+  }
+  *total_ms = t;
+  *launches = g_nrec[stage];
+  return GDFT_OK;
+}
+
+const char *gdft_last_error(void) { return g_err; }
+
+int gdft_molecule_bytes(int64_t n_grid, int32_t n_ao, int32_t precision, size_t *bytes) {
+  if (bytes == nullptr || n_grid <= 0 || n_ao <= 0) {
+    set_error("gdft_molecule_bytes: n_grid and n_ao must be positive");
+    return GDFT_ERR_INVALID;
+  }
+  if (precision != GDFT_FP64 && precision != GDFT_TF32X3) {
+    set_error("unknown precision %d", precision);
+    return GDFT_ERR_INVALID;
+  }
+  *bytes = mol_layout(n_grid, n_ao, precision).bytes;
+  return GDFT_OK;
+}
+
+int gdft_molecule_init(gdft_molecule *mol, int64_t n_grid, int32_t n_ao, int32_t precision, void *d_buffer,
+                       size_t buffer_bytes) {
+  size_t need = 0;
+  int rc = gdft_molecule_bytes(n_grid, n_ao, precision, &need);
+  if (rc) return rc;
+  if (mol == nullptr || d_buffer == nullptr) {
+    set_error("gdft_molecule_init: null descriptor or buffer");
+    return GDFT_ERR_INVALID;
+  }
+  if (buffer_bytes < need) {
+    set_error("molecule buffer of %zu bytes is smaller than the %zu bytes required", buffer_bytes, need);
+    return GDFT_ERR_WORKSPACE;
+  }
+  if (((uintptr_t)d_buffer & 255u) != 0) {
+    set_error("molecule buffer must be 256-byte aligned");
+    return GDFT_ERR_ALIGNMENT;
+  }
+  const MolLayout L = mol_layout(n_grid, n_ao, precision);
+  mol->n_grid = n_grid;
+  mol->n_grid_pad = L.np;
+  mol->n_ao = n_ao;
+  mol->ld = L.ld;
+  mol->precision = precision;
+  mol->reserved = 0;
+  mol->buffer = d_buffer;
+  mol->buffer_bytes = buffer_bytes;
+  return GDFT_OK;
+}
+
+int gdft_molecule_load(const gdft_molecule *mol, const double *d_ao, const double *d_grad_ao,
+                       const double *d_grad2_ao, const double *d_weights, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if (d_ao == nullptr || d_grad_ao == nullptr || d_weights == nullptr) {
+    set_error("gdft_molecule_load: ao, grad_ao and weights are required");
+    return GDFT_ERR_INVALID;
+  }
+  if ((rc = check_aligned8(d_ao, "ao")) || (rc = check_aligned8(d_grad_ao, "grad_ao")) ||
+      (rc = check_aligned8(d_weights, "weights")))
+    return rc;
+  const MolLayout L = mol_layout(mol->n_grid, mol->n_ao, mol->precision);
+  double *tab = (double *)((char *)mol->buffer + L.off_tab);
+  double *w = (double *)((char *)mol->buffer + L.off_w);
+  StageTimer tm(GDFT_STAGE_AO, (cudaStream_t)stream);
+  return check_cuda(launch_load_tables(d_ao, d_grad_ao, d_grad2_ao, d_weights, mol->n_grid, mol->n_ao, L.np, L.ld,
+                                       tab, w, (cudaStream_t)stream),
+                    "load_tables");
+}
+
+int gdft_molecule_eval_basis(const gdft_molecule *mol, const double *d_basis, const double *d_coords,
+                             const double *d_weights, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if (d_basis == nullptr || d_coords == nullptr || d_weights == nullptr) {
+    set_error("gdft_molecule_eval_basis: basis, coords and weights are required");
+    return GDFT_ERR_INVALID;
+  }
+  const MolLayout L = mol_layout(mol->n_grid, mol->n_ao, mol->precision);
+  double *tab = (double *)((char *)mol->buffer + L.off_tab);
+  double *w = (double *)((char *)mol->buffer + L.off_w);
+  StageTimer tm(GDFT_STAGE_AO, (cudaStream_t)stream);
+  return check_cuda(launch_eval_basis(d_basis, d_coords, d_weights, mol->n_grid, mol->n_ao, L.np, L.ld, tab, w,
+                                      (cudaStream_t)stream),
+                    "eval_basis");
+}
+
+int gdft_workspace_bytes(const gdft_molecule *mol, size_t *bytes) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if (bytes == nullptr) {
+    set_error("gdft_workspace_bytes: null output");
+    return GDFT_ERR_INVALID;
+  }
+  *bytes = ws_layout(mol).bytes;
+  return GDFT_OK;
+}
+
+int gdft_density(const gdft_molecule *mol, const double *d_rdm1, double *d_rho, double *d_grad_rho, double *d_lapl,
+                 double *d_tau, void *d_ws, size_t ws_bytes, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_ws(mol, d_ws, ws_bytes))) return rc;
+  if (d_rdm1 == nullptr) {
+    set_error("gdft_density: rdm1 is required");
+    return GDFT_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if ((rc = run_density(mol, d_rdm1, (char *)d_ws, st))) return rc;
+  const WsLayout W = ws_layout(mol);
+  StageTimer tm(GDFT_STAGE_REDUCE, st);
+  return check_cuda(launch_feat_to_reference((const double *)((char *)d_ws + W.off_feat), mol->n_grid,
+                                             mol->n_grid_pad, d_rho, d_grad_rho, d_lapl, d_tau, st),
+                    "feat_to_reference");
+}
+
+int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,
+                             const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc, void *d_ws,
+                             size_t ws_bytes, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_ws(mol, d_ws, ws_bytes))) return rc;
+  if ((rc = check_functional(fn, d_ehf, n_omega))) return rc;
+  if (d_rdm1 == nullptr || d_exc == nullptr) {
+    set_error("gdft_xc_energy_and_grads: rdm1 and exc are required");
+    return GDFT_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  const WsLayout W = ws_layout(mol);
+  if ((rc = run_density(mol, d_rdm1, ws, st))) return rc;
+  double *feat = (double *)(ws + W.off_feat);
+  double *coef = d_vxc ? (double *)(ws + W.off_coef) : nullptr;
+  double *epart = (double *)(ws + W.off_epart);
+  {
+    StageTimer tm(GDFT_STAGE_POINT, st);
+    rc = check_cuda(launch_xc_point(feat, mol_w(mol), mol->n_grid, mol->n_grid_pad, *fn, d_ehf, n_omega, coef, epart,
+                                    nullptr, st),
+                    "xc_point");
+    if (rc) return rc;
+  }
+  {
+    StageTimer tm(GDFT_STAGE_REDUCE, st);
+    if ((rc = check_cuda(launch_energy_reduce(epart, W.n_eblocks, d_exc, st), "energy_reduce"))) return rc;
+  }
+  if (d_vxc == nullptr) return GDFT_OK;
+  double *vpart = (double *)(ws + W.off_vpart);
+  if (mol->precision == GDFT_FP64) {
+    {
+      StageTimer tm(GDFT_STAGE_VXC, st);
+      rc = check_cuda(launch_vxc_f64(mol_tab(mol), mol->n_grid_pad, mol->ld, mol->n_ao, coef, W.n_vsplit, vpart, st),
+                      "vxc_f64");
+      if (rc) return rc;
+    }
+    StageTimer tm(GDFT_STAGE_REDUCE, st);
+    return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
+  }
+  set_error("precision %d is not available in this build", mol->precision);
+  return GDFT_ERR_UNSUPPORTED;
+}
+
+int gdft_energy_densities(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,
+                          const double *d_ehf, int32_t n_omega, double *d_dens, void *d_ws, size_t ws_bytes,
+                          void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_ws(mol, d_ws, ws_bytes))) return rc;
+  if ((rc = check_functional(fn, d_ehf, n_omega))) return rc;
+  if (d_rdm1 == nullptr || d_dens == nullptr) {
+    set_error("gdft_energy_densities: rdm1 and dens are required");
+    return GDFT_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  const WsLayout W = ws_layout(mol);
+  if ((rc = run_density(mol, d_rdm1, ws, st))) return rc;
+  return check_cuda(launch_xc_point((double *)(ws + W.off_feat), mol_w(mol), mol->n_grid, mol->n_grid_pad, *fn,
+                                    d_ehf, n_omega, nullptr, (double *)(ws + W.off_epart), d_dens, st),
+                    "xc_point");
+}
+
+int gdft_integrate_workspace_bytes(int64_t n_grid, size_t *bytes) {
+  if (n_grid <= 0 || bytes == nullptr) {
+    set_error("gdft_integrate_workspace_bytes: invalid arguments");
+    return GDFT_ERR_INVALID;
+  }
+  *bytes = align256((size_t)integrate_blocks(n_grid) * sizeof(double));
+  return GDFT_OK;
+}
+
+int gdft_integrate(int64_t n_grid, int32_t n_cols, const double *h_coeffs, int32_t n_coeffs, const double *d_dens,
+                   const double *d_weights, double clip, double *d_exc, void *d_ws, size_t ws_bytes, void *stream) {
+  if (n_grid <= 0 || n_cols < 1 || !(n_coeffs == 1 || n_coeffs == n_cols) || n_coeffs > GDFT_MAX_COLS ||
+      h_coeffs == nullptr || d_dens == nullptr || d_weights == nullptr || d_exc == nullptr) {
+    set_error("gdft_integrate: invalid arguments (n_cols=%d, n_coeffs=%d)", n_cols, n_coeffs);
+    return GDFT_ERR_INVALID;
+  }
+  const size_t need = align256((size_t)integrate_blocks(n_grid) * sizeof(double));
+  if (d_ws == nullptr || ws_bytes < need) {
+    set_error("gdft_integrate: workspace of %zu bytes is smaller than %zu", ws_bytes, need);
+    return GDFT_ERR_WORKSPACE;
+  }
+  gdft_functional fn;
+  memset(&fn, 0, sizeof(fn));
+  fn.n_cols = n_cols;
+  fn.n_coeffs = n_coeffs;
+  for (int i = 0; i < n_coeffs; ++i) fn.coeffs[i] = h_coeffs[i];
+  fn.clip = clip;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = check_cuda(launch_integrate(n_grid, n_cols, fn, d_dens, d_weights, (double *)d_ws, st), "integrate");
+  if (rc) return rc;
+  return check_cuda(launch_energy_reduce((const double *)d_ws, integrate_blocks(n_grid), d_exc, st), "energy_reduce");
+}
+
+int gdft_fock(int32_t n_ao, const double *d_h1e, const double *d_vj, const double *d_vxc, double clip,
+              double *d_fock, void *stream) {
+  if (n_ao <= 0 || !d_h1e || !d_vj || !d_vxc || !d_fock) {
+    set_error("gdft_fock: invalid arguments");
+    return GDFT_ERR_INVALID;
+  }
+  return check_cuda(launch_fock(n_ao, d_h1e, d_vj, d_vxc, clip, d_fock, (cudaStream_t)stream), "fock");
+}
+
+int gdft_coulomb(int32_t n_ao, const double *d_eri, const double *d_rdm1, const double *d_h1e,
+                 double nuclear_repulsion, double *d_vj, double *d_enonxc, void *stream) {
+  if (n_ao <= 0 || !d_eri || !d_rdm1 || !d_vj || (d_enonxc && !d_h1e)) {
+    set_error("gdft_coulomb: invalid arguments");
+    return GDFT_ERR_INVALID;
+  }
+  return check_cuda(launch_coulomb(n_ao, d_eri, d_rdm1, d_h1e, nuclear_repulsion, d_vj, d_enonxc,
+                                   (cudaStream_t)stream),
+                    "coulomb");
+}
+
+}  // extern "C"

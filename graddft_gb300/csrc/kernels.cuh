@@ -1,0 +1,43 @@
+// kernels.cuh - launchers shared between the translation units.
+#pragma once
+
+#include "common.cuh"
+
+namespace gdft {
+
+// ao.cu
+cudaError_t launch_load_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *w,
+                               int64_t n_grid, int n_ao, int64_t np, int ld, double *tab, double *wout,
+                               cudaStream_t st);
+cudaError_t launch_eval_basis(const double *basis, const double *coords, const double *w, int64_t n_grid, int n_ao,
+                              int64_t np, int ld, double *tab, double *wout, cudaStream_t st);
+
+// dens_f64.cu: FP64 form of the density contraction -> feat[2][6][np].
+cudaError_t launch_dens_f64(const double *tab, int64_t np, int ld, int n_ao, const double *rdm1, double *feat,
+                            cudaStream_t st);
+
+// vxc_f64.cu: FP64 form of the V_xc contraction -> vpart[nsplit][2][n][n].
+int vxc_f64_splits(int64_t np, int n_ao);
+cudaError_t launch_vxc_f64(const double *tab, int64_t np, int ld, int n_ao, const double *coef, int nsplit,
+                           double *vpart, cudaStream_t st);
+
+// xc_point.cu
+int xc_point_blocks(int64_t np);
+cudaError_t launch_xc_point(const double *feat, const double *w, int64_t n_grid, int64_t np,
+                            const gdft_functional &fn, const double *ehf, int n_omega, double *coef,
+                            double *epart, double *dens, cudaStream_t st);
+
+// reduce.cu
+int integrate_blocks(int64_t n_grid);
+cudaError_t launch_integrate(int64_t n_grid, int n_cols, const gdft_functional &fn, const double *dens,
+                             const double *w, double *epart, cudaStream_t st);
+cudaError_t launch_energy_reduce(const double *epart, int n, double *exc, cudaStream_t st);
+cudaError_t launch_vxc_reduce(const double *vpart, int nsplit, int n_ao, double *vxc, cudaStream_t st);
+cudaError_t launch_feat_to_reference(const double *feat, int64_t n_grid, int64_t np, double *rho, double *grad_rho,
+                                     double *lapl, double *tau, cudaStream_t st);
+cudaError_t launch_fock(int n_ao, const double *h1e, const double *vj, const double *vxc, double clip, double *fock,
+                        cudaStream_t st);
+cudaError_t launch_coulomb(int n_ao, const double *eri, const double *rdm1, const double *h1e, double enuc,
+                           double *vj, double *enonxc, cudaStream_t st);
+
+}  // namespace gdft

@@ -1,0 +1,157 @@
+// xc_point.cu - per-grid-point stage of the XC path.
+//
+// For every grid point it evaluates the functional's energy-density columns
+// (compute_densities, functional.py:160-185), contracts them with the
+// coefficients and clips (xc_energy, functional.py:219-253), weights them
+// (_integrate, functional.py:316-342) and writes:
+//   * a per-block partial sum of w_r * e_xc(r) (FP64; the blocks are summed
+//     with Kahan compensation by reduce.cu);
+//   * the adjoint coefficients of V_xc (the pointwise part of the transpose
+//     that jax.value_and_grad builds at train.py:86), per spin:
+//       C_RHO = dE/drho, C_GJ = 2 dE/d(d_j rho), C_LAP = 2 dE/d(lap rho),
+//       C_KIN = 2 dE/d(lap rho) + 1/2 dE/dtau,
+//     so that V_ab = sum_r phi_a (C_RHO phi_b + sum_j C_GJ d_j phi_b + C_LAP lap phi_b)
+//                  + sum_r C_KIN sum_j d_j phi_a d_j phi_b.
+#include "common.cuh"
+#include "xc_functionals.cuh"
+#include "kernels.cuh"
+
+namespace gdft {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+// Dual variable indices for the classical functionals: rho_a, rho_b,
+// |grad rho_a|^2, |grad rho_b|^2, lap_a, lap_b.
+constexpr int KV = 6;
+enum { V_R0 = 0, V_R1 = 1, V_S0 = 2, V_S1 = 3, V_L0 = 4, V_L1 = 5 };
+
+template <int K>
+__device__ __forceinline__ Dual<K> seed(double v, int idx) {
+  Dual<K> r = dconst<K>(v);
+  r.d[idx] = 1.0;
+  return r;
+}
+
+template <class T>
+__device__ __forceinline__ T column(int col, const T rho[2], const T s[2], const T lap[2], double hf,
+                                    double hf0, double hf1, double clip) {
+  switch (col) {
+    case GDFT_COL_LSDA: return lsda_x_e(rho, clip);
+    case GDFT_COL_B88: return b88_x_e(rho, s, clip);
+    case GDFT_COL_VWN: return vwn_c_e(rho, clip);
+    case GDFT_COL_LYP: return lyp_c_e(rho, s, lap, clip);
+    case GDFT_COL_PW92: return pw92_c_e(rho, clip);
+    case GDFT_COL_DM21_LDA: return dm21_lda(rho, clip);
+    case GDFT_COL_HF: return tconst(rho[0], hf);
+    case GDFT_COL_HF_W0: return tconst(rho[0], hf0);
+    case GDFT_COL_HF_W1: return tconst(rho[0], hf1);
+    default: return tconst(rho[0], 0.0);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restrict__ feat, const double *__restrict__ w,
+                                                          int64_t n_grid, int64_t np, gdft_functional fn,
+                                                          const double *__restrict__ ehf, int n_omega,
+                                                          double *__restrict__ coef, double *__restrict__ epart,
+                                                          double *__restrict__ dens) {
+  const int64_t p = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  double e_r = 0.0;
+  if (p < np) {
+    double c[2][kFeat];
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+#pragma unroll
+      for (int k = 0; k < kFeat; ++k) c[s][k] = 0.0;
+    if (p < n_grid) {
+      const double clip = fn.clip;
+      double f[2][kFeat];
+#pragma unroll
+      for (int s = 0; s < 2; ++s)
+#pragma unroll
+        for (int k = 0; k < kFeat; ++k) f[s][k] = feat[((size_t)s * kFeat + k) * np + p];
+      Dual<KV> rho[2], sg[2], lap[2];
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        rho[s] = seed<KV>(f[s][F_RHO], V_R0 + s);
+        // jnp.sum(grad_rho**2, axis=-1)
+        const double sv = (f[s][F_GX] * f[s][F_GX] + f[s][F_GY] * f[s][F_GY]) + f[s][F_GZ] * f[s][F_GZ];
+        sg[s] = seed<KV>(sv, V_S0 + s);
+        lap[s] = seed<KV>(f[s][F_LAP], V_L0 + s);
+      }
+      double hf = 0.0, hf0 = 0.0, hf1 = 0.0;
+      if (ehf != nullptr) {
+        // ehf layout (omega, spin, grid).
+        for (int o = 0; o < n_omega; ++o) {
+          const double a = ehf[((size_t)o * 2 + 0) * n_grid + p];
+          const double b = ehf[((size_t)o * 2 + 1) * n_grid + p];
+          hf = o == 0 ? (a + b) : hf + (a + b);
+          if (o == 0) hf0 = a + b;
+          if (o == 1) hf1 = a + b;
+        }
+      }
+      // Energy density: sum_f c_f * abs_clip(e_f), then abs_clip; weight abs_clip(w).
+      Dual<KV> exc = dconst<KV>(0.0);
+      for (int i = 0; i < fn.n_cols; ++i) {
+        Dual<KV> e = column<Dual<KV>>(fn.cols[i], rho, sg, lap, hf, hf0, hf1, clip);
+        if (dens != nullptr) dens[(size_t)p * fn.n_cols + i] = e.v;
+        if (!(fabs(e.v) > clip)) e = dconst<KV>(0.0);  // abs_clip(densities), functional.py:184
+        const double ci = fn.n_coeffs == 1 ? fn.coeffs[0] : fn.coeffs[i];
+        exc = i == 0 ? ci * e : exc + ci * e;
+      }
+      if (!(fabs(exc.v) > clip)) exc = dconst<KV>(0.0);  // functional.py:252 and :342
+      const double wr = w[p];
+      const double W = fabs(wr) > clip ? wr : 0.0;      // abs_clip(gridweights), functional.py:342
+      e_r = W * exc.v;
+      // dE_r/dvar = W * d exc/dvar.
+      double dv[KV];
+#pragma unroll
+      for (int k = 0; k < KV; ++k) dv[k] = W * exc.d[k];
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        const double dsig = dv[V_S0 + s];  // dE/d|grad rho_s|^2
+        const double dlap = dv[V_L0 + s];
+        c[s][C_RHO] = dv[V_R0 + s];
+        c[s][C_GX] = 2.0 * (2.0 * f[s][F_GX] * dsig);
+        c[s][C_GY] = 2.0 * (2.0 * f[s][F_GY] * dsig);
+        c[s][C_GZ] = 2.0 * (2.0 * f[s][F_GZ] * dsig);
+        c[s][C_LAP] = 2.0 * dlap;
+        c[s][C_KIN] = 2.0 * dlap;  // + 1/2 dE/dtau (no tau dependence in these columns)
+      }
+    }
+    if (coef != nullptr) {
+#pragma unroll
+      for (int s = 0; s < 2; ++s)
+#pragma unroll
+        for (int k = 0; k < kFeat; ++k) coef[((size_t)s * kFeat + k) * np + p] = c[s][k];
+    }
+  }
+  // Block partial sum of the weighted energy density.
+  __shared__ double red[kBlock / 32];
+  double v = e_r;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < kBlock / 32 ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) epart[blockIdx.x] = v;
+  }
+}
+
+}  // namespace
+
+int xc_point_blocks(int64_t np) { return (int)((np + kBlock - 1) / kBlock); }
+
+cudaError_t launch_xc_point(const double *feat, const double *w, int64_t n_grid, int64_t np,
+                            const gdft_functional &fn, const double *ehf, int n_omega, double *coef,
+                            double *epart, double *dens, cudaStream_t st) {
+  const int blocks = xc_point_blocks(np);
+  xc_point_kernel<<<blocks, kBlock, 0, st>>>(feat, w, n_grid, np, fn, ehf, n_omega, coef, epart, dens);
+  return cudaGetLastError();
+}
+
+}  // namespace gdft

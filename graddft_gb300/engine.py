@@ -1,0 +1,188 @@
+"""Device-side engine: resident molecules, workspaces and calls into libgdft_xc.so.
+
+PyTorch is used only for device memory and the current CUDA stream; all
+arithmetic of the XC path runs in the library's kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import torch
+
+from . import _lib
+from ._lib import GdftFunctional, GdftMolecule, check
+
+F64 = torch.float64
+PRECISIONS = {"fp64": _lib.GDFT_FP64, "tf32x3": _lib.GDFT_TF32X3}
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(device: torch.device) -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def as_device_f64(x, device) -> torch.Tensor:
+    """Accept torch tensors, numpy arrays or any DLPack producer (e.g. jax.Array)."""
+    if x is None:
+        return None
+    if not isinstance(x, torch.Tensor):
+        if hasattr(x, "__dlpack__") and not hasattr(x, "__array_interface__"):
+            x = torch.from_dlpack(x)
+        else:
+            x = torch.as_tensor(x)
+    return x.to(device=device, dtype=F64).contiguous()
+
+
+def require_cuda(device=None) -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("the GB300 XC path needs a CUDA device (there is no CPU fallback)")
+    d = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    if d.type != "cuda":
+        raise RuntimeError(f"device {d} is not a CUDA device (there is no CPU fallback)")
+    return d
+
+
+class Resident:
+    """A molecule's grid and AO tables resident in HBM in the library's layout."""
+
+    def __init__(self, n_grid: int, n_ao: int, precision: str = "fp64", device=None):
+        lib = _lib.load()
+        self.device = require_cuda(device)
+        self.n_grid, self.n_ao = int(n_grid), int(n_ao)
+        self.precision = precision
+        prec = PRECISIONS[precision]
+        nbytes = ctypes.c_size_t()
+        check(lib.gdft_molecule_bytes(self.n_grid, self.n_ao, prec, ctypes.byref(nbytes)))
+        self.buffer = torch.empty(nbytes.value, dtype=torch.uint8, device=self.device)
+        self.desc = GdftMolecule()
+        check(lib.gdft_molecule_init(ctypes.byref(self.desc), self.n_grid, self.n_ao, prec,
+                                     _ptr(self.buffer), nbytes.value))
+        wbytes = ctypes.c_size_t()
+        check(lib.gdft_workspace_bytes(ctypes.byref(self.desc), ctypes.byref(wbytes)))
+        self.ws = torch.empty(wbytes.value, dtype=torch.uint8, device=self.device)
+
+    @property
+    def nbytes(self) -> int:
+        return self.buffer.numel() + self.ws.numel()
+
+    @classmethod
+    def from_tables(cls, ao, grad_ao, grad2_ao, weights, precision="fp64", device=None) -> "Resident":
+        dev = require_cuda(device)
+        ao = as_device_f64(ao, dev)
+        r = cls(ao.shape[0], ao.shape[1], precision, dev)
+        r.load(ao, grad_ao, grad2_ao, weights)
+        return r
+
+    def load(self, ao, grad_ao, grad2_ao, weights):
+        ao = as_device_f64(ao, self.device)
+        grad_ao = as_device_f64(grad_ao, self.device)
+        grad2_ao = as_device_f64(grad2_ao, self.device)
+        weights = as_device_f64(weights, self.device)
+        if ao.shape != (self.n_grid, self.n_ao) or grad_ao.shape != (self.n_grid, self.n_ao, 3):
+            raise ValueError(f"ao {tuple(ao.shape)} / grad_ao {tuple(grad_ao.shape)} do not match "
+                             f"({self.n_grid}, {self.n_ao}[, 3])")
+        if grad2_ao is not None and grad2_ao.shape != (self.n_grid, self.n_ao, 3):
+            raise ValueError(f"grad_n_ao[2] {tuple(grad2_ao.shape)} does not match ({self.n_grid}, {self.n_ao}, 3)")
+        if weights.shape != (self.n_grid,):
+            raise ValueError(f"weights {tuple(weights.shape)} do not match ({self.n_grid},)")
+        check(_lib.load().gdft_molecule_load(ctypes.byref(self.desc), _ptr(ao), _ptr(grad_ao), _ptr(grad2_ao),
+                                             _ptr(weights), _stream(self.device)))
+
+    @classmethod
+    def from_basis(cls, basis_rows, coords, weights, precision="fp64", device=None) -> "Resident":
+        """Evaluate a seeded Gaussian basis on the device (see graddft_gb300.synthetic)."""
+        dev = require_cuda(device)
+        basis_rows = as_device_f64(basis_rows, dev)
+        coords = as_device_f64(coords, dev)
+        weights = as_device_f64(weights, dev)
+        r = cls(coords.shape[0], basis_rows.shape[0], precision, dev)
+        check(_lib.load().gdft_molecule_eval_basis(ctypes.byref(r.desc), _ptr(basis_rows), _ptr(coords),
+                                                   _ptr(weights), _stream(dev)))
+        torch.cuda.current_stream(dev).synchronize()
+        return r
+
+    # ------------------------------------------------------------------ calls
+    def density(self, rdm1, want=("rho", "grad_rho", "lapl", "tau")):
+        rdm1 = self._rdm1(rdm1)
+        n = self.n_grid
+        out = {
+            "rho": torch.empty((n, 2), dtype=F64, device=self.device) if "rho" in want else None,
+            "grad_rho": torch.empty((n, 2, 3), dtype=F64, device=self.device) if "grad_rho" in want else None,
+            "lapl": torch.empty((n, 2), dtype=F64, device=self.device) if "lapl" in want else None,
+            "tau": torch.empty((n, 2), dtype=F64, device=self.device) if "tau" in want else None,
+        }
+        check(_lib.load().gdft_density(ctypes.byref(self.desc), _ptr(rdm1), _ptr(out["rho"]), _ptr(out["grad_rho"]),
+                                       _ptr(out["lapl"]), _ptr(out["tau"]), _ptr(self.ws), self.ws.numel(),
+                                       _stream(self.device)))
+        return out
+
+    def xc_energy_and_grads(self, rdm1, fn: GdftFunctional, ehf=None, want_vxc=True, exc_out=None, vxc_out=None):
+        rdm1 = self._rdm1(rdm1)
+        ehf_t = as_device_f64(ehf, self.device)
+        n_omega = 0
+        if ehf_t is not None:
+            if ehf_t.ndim != 3 or ehf_t.shape[1] != 2 or ehf_t.shape[2] != self.n_grid:
+                raise ValueError(f"ehf must be (omega, 2, {self.n_grid}), got {tuple(ehf_t.shape)}")
+            n_omega = ehf_t.shape[0]
+        exc = exc_out if exc_out is not None else torch.empty((), dtype=F64, device=self.device)
+        vxc = None
+        if want_vxc:
+            vxc = vxc_out if vxc_out is not None else torch.empty((2, self.n_ao, self.n_ao), dtype=F64,
+                                                                   device=self.device)
+        check(_lib.load().gdft_xc_energy_and_grads(ctypes.byref(self.desc), _ptr(rdm1), ctypes.byref(fn),
+                                                   _ptr(ehf_t), n_omega, _ptr(exc), _ptr(vxc), _ptr(self.ws),
+                                                   self.ws.numel(), _stream(self.device)))
+        return exc, vxc
+
+    def _rdm1(self, rdm1) -> torch.Tensor:
+        rdm1 = as_device_f64(rdm1, self.device)
+        if rdm1.shape != (2, self.n_ao, self.n_ao):
+            raise ValueError(f"rdm1 must be (2, {self.n_ao}, {self.n_ao}), got {tuple(rdm1.shape)}")
+        return rdm1
+
+
+def make_functional(cols: Sequence[int], coeffs: Sequence[float], clip: float = 1e-30) -> GdftFunctional:
+    cols, coeffs = list(cols), [float(c) for c in coeffs]
+    if not 1 <= len(cols) <= _lib.MAX_COLS:
+        raise ValueError(f"a functional needs 1..{_lib.MAX_COLS} energy-density columns, got {len(cols)}")
+    if len(coeffs) not in (1, len(cols)):
+        raise ValueError(f"{len(coeffs)} coefficients for {len(cols)} energy-density columns")
+    fn = GdftFunctional()
+    fn.n_cols = len(cols)
+    for i, c in enumerate(cols):
+        fn.cols[i] = int(c)
+    fn.n_coeffs = len(coeffs)
+    for i, c in enumerate(coeffs):
+        fn.coeffs[i] = c
+    fn.clip = float(clip)
+    return fn
+
+
+def fock(h1e, vj, vxc, clip=1e-30) -> torch.Tensor:
+    dev = vxc.device
+    n = vxc.shape[-1]
+    h1e = as_device_f64(h1e, dev)
+    vj = as_device_f64(vj, dev)
+    out = torch.empty_like(vxc)
+    check(_lib.load().gdft_fock(n, _ptr(h1e), _ptr(vj), _ptr(vxc.contiguous()), float(clip), _ptr(out),
+                                _stream(dev)))
+    return out
+
+
+def coulomb(eri, rdm1, h1e=None, nuclear_repulsion=0.0, want_energy=False):
+    dev = rdm1.device if isinstance(rdm1, torch.Tensor) and rdm1.is_cuda else require_cuda()
+    rdm1 = as_device_f64(rdm1, dev)
+    eri = as_device_f64(eri, dev)
+    n = rdm1.shape[-1]
+    if eri.shape != (n, n, n, n):
+        raise ValueError(f"rep_tensor must be ({n}, {n}, {n}, {n}), got {tuple(eri.shape)}")
+    vj = torch.empty((n, n), dtype=F64, device=dev)
+    e = torch.empty((), dtype=F64, device=dev) if want_energy else None
+    h = as_device_f64(h1e, dev) if want_energy else None
+    check(_lib.load().gdft_coulomb(n, _ptr(eri), _ptr(rdm1), _ptr(h), float(nuclear_repulsion), _ptr(vj), _ptr(e),
+                                   _stream(dev)))
+    return vj, e

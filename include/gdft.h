@@ -1,0 +1,189 @@
+/*
+ * gdft.h - C ABI of the GB300 XC grid path (libgdft_xc.so).
+ *
+ * The reference (Grad DFT) is pure Python/JAX and has no native interface;
+ * each entry point below replaces one Python/JAX function of the XC path and
+ * keeps its argument meaning.  Citations are file:line in the GradDFT tree.
+ *
+ * Conventions
+ *  - Every pointer argument named d_* is DEVICE memory; h_* is host memory.
+ *  - All floating-point inputs and outputs are IEEE float64 in the
+ *    reference's own layouts (Molecule.ao (grid, ao), grad_ao (grid, ao, 3),
+ *    grad_n_ao[2] (grid, ao, 3), rdm1 (2, ao, ao), row-major).
+ *  - Work is enqueued on the caller's CUDA stream; nothing synchronises the
+ *    host except where a function says so.
+ *  - The library allocates no device memory: molecules live in a
+ *    caller-provided buffer (gdft_molecule_bytes) and every call takes a
+ *    caller-provided workspace (gdft_workspace_bytes).
+ *  - Return value: GDFT_OK or an error code; gdft_last_error() gives the
+ *    message of the calling thread's last failure.
+ */
+#ifndef GDFT_H_
+#define GDFT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GDFT_ABI_VERSION 1
+
+/* Status codes (the Python layer maps them to ValueError/TypeError/RuntimeError,
+ * as the reference raises ValueError at functional.py:583, molecule.py:174-180). */
+enum {
+  GDFT_OK = 0,
+  GDFT_ERR_INVALID = 1,     /* bad shape or argument                          */
+  GDFT_ERR_ALIGNMENT = 2,   /* pointer not aligned as required                */
+  GDFT_ERR_WORKSPACE = 3,   /* workspace or buffer too small                  */
+  GDFT_ERR_CUDA = 4,        /* a CUDA runtime call failed                     */
+  GDFT_ERR_DEVICE = 5,      /* a kernel reported an error word (bounded wait)  */
+  GDFT_ERR_UNSUPPORTED = 6  /* functional/precision combination not built     */
+};
+
+/* Arithmetic forms of the path. */
+enum {
+  GDFT_FP64 = 0,    /* plain FP64 form: FP64 contractions and FP64 point work      */
+  GDFT_TF32X3 = 1   /* mixed form: tcgen05 TF32 3-term split products, FP32
+                       accumulation inside a K-chunk, FP64 across chunks       */
+};
+
+/* Energy-density columns (popular_functionals.py:29-326, functional.py:534-675). */
+enum {
+  GDFT_COL_LSDA = 0,     /* lsda_x_e               popular_functionals.py:29-50   */
+  GDFT_COL_B88 = 1,      /* b88_x_e (correction)   popular_functionals.py:52-103  */
+  GDFT_COL_VWN = 2,      /* vwn_c_e                popular_functionals.py:141-195 */
+  GDFT_COL_LYP = 3,      /* lyp_c_e                popular_functionals.py:197-269 */
+  GDFT_COL_PW92 = 4,     /* pw92_c_e               popular_functionals.py:105-139 */
+  GDFT_COL_HF = 5,       /* sum_{omega,spin} ehf   popular_functionals.py:328-334 */
+  GDFT_COL_DM21_LDA = 6, /* dm21_densities 'LDA'   functional.py:534-626          */
+  GDFT_COL_HF_W0 = 7,    /* sum_spin ehf[0]        functional.py:652-675          */
+  GDFT_COL_HF_W1 = 8     /* sum_spin ehf[1]        functional.py:652-675          */
+};
+
+#define GDFT_MAX_COLS 8
+
+/* A functional with constant coefficients: Functional(coefficients=lambda: c,
+ * energy_densities=stack of columns) (functional.py:128-141, popular_functionals.py:375-393).
+ * A single coefficient broadcasts over all columns, as jnp.einsum("rf,rf->r")
+ * broadcasts the [[1.0]] row in the reference. */
+typedef struct gdft_functional {
+  int32_t n_cols;
+  int32_t cols[GDFT_MAX_COLS];
+  int32_t n_coeffs;                 /* 1 (broadcast) or n_cols */
+  double coeffs[GDFT_MAX_COLS];
+  double clip;                      /* clip_cte, 1e-30 in the reference */
+} gdft_functional;
+
+/* A molecule resident on the device in the library's layout: the Molecule
+ * fields the XC path reads (molecule.py:72-106: grid.weights, ao, grad_ao,
+ * grad_n_ao[2]).  Filled by gdft_molecule_init; opaque beyond these fields. */
+typedef struct gdft_molecule {
+  int64_t n_grid;      /* grid points                                   */
+  int64_t n_grid_pad;  /* grid points rounded up to the tile (128)      */
+  int32_t n_ao;        /* atomic orbitals                               */
+  int32_t ld;          /* AO leading dimension (n_ao rounded up to 32)  */
+  int32_t precision;   /* GDFT_FP64 or GDFT_TF32X3                      */
+  int32_t reserved;
+  void *buffer;        /* device buffer of gdft_molecule_bytes bytes    */
+  size_t buffer_bytes;
+} gdft_molecule;
+
+int gdft_abi_version(void);
+const char *gdft_last_error(void);
+
+/* Size of the device buffer that holds a molecule in the library's layout. */
+int gdft_molecule_bytes(int64_t n_grid, int32_t n_ao, int32_t precision, size_t *bytes);
+
+/* Bind a caller buffer to a molecule descriptor (no device work). */
+int gdft_molecule_init(gdft_molecule *mol, int64_t n_grid, int32_t n_ao, int32_t precision,
+                       void *d_buffer, size_t buffer_bytes);
+
+/* Load Molecule.ao, grad_ao, grad_n_ao[2] and grid.weights (reference layouts,
+ * molecule.py:72-106) into the molecule: the host-side analogue is
+ * interface/pyscf.py:639-654 to_device_arrays.  d_grad2_ao may be NULL when
+ * no functional needs the Laplacian. */
+int gdft_molecule_load(const gdft_molecule *mol, const double *d_ao, const double *d_grad_ao,
+                       const double *d_grad2_ao, const double *d_weights, void *stream);
+
+/* Evaluate a Gaussian basis on the grid directly into the molecule (stands in
+ * for numint.eval_ao, interface/pyscf.py:849-852, and ao_grads(order=2),
+ * :677-705).  d_basis: (n_ao, 8) rows cx, cy, cz, alpha, norm, kind, comp, 0;
+ * d_coords: (n_grid, 3) bohr. */
+int gdft_molecule_eval_basis(const gdft_molecule *mol, const double *d_basis, const double *d_coords,
+                             const double *d_weights, void *stream);
+
+/* Workspace bytes for the calls below on this molecule. */
+int gdft_workspace_bytes(const gdft_molecule *mol, size_t *bytes);
+
+/* density / grad_density / lapl_density / kinetic_density (molecule.py:385-502)
+ * in one pass.  Outputs (any may be NULL): rho (grid, 2), grad_rho (grid, 2, 3),
+ * lapl (grid, 2), tau (grid, 2). */
+int gdft_density(const gdft_molecule *mol, const double *d_rdm1, double *d_rho, double *d_grad_rho,
+                 double *d_lapl, double *d_tau, void *d_ws, size_t ws_bytes, void *stream);
+
+/* energy_predictor.xc_energy_and_grads (train.py:86-121) for a functional
+ * with constant coefficients: E_xc = Functional.xc_energy (functional.py:219-253)
+ * and V_xc = dE_xc/d rdm1 (raw, not symmetrised).
+ * d_ehf: (n_omega, 2, grid) stop-gradient HF energy densities, needed by the
+ * HF columns (NULL otherwise); n_omega its leading extent.
+ * d_exc: one double; d_vxc: (2, ao, ao).  d_vxc may be NULL (energy only). */
+int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,
+                             const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc,
+                             void *d_ws, size_t ws_bytes, void *stream);
+
+/* The functional's energy-density columns before clipping (the stacked output of
+ * the energy_densities plugin, e.g. b88_density popular_functionals.py:277-284,
+ * b3lyp_exhf_densities :306-326 plus the combine step :328-334).
+ * d_dens: (grid, n_cols). */
+int gdft_energy_densities(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,
+                          const double *d_ehf, int32_t n_omega, double *d_dens, void *d_ws, size_t ws_bytes,
+                          void *stream);
+
+/* Functional.xc_energy on given energy densities and constant coefficients
+ * (functional.py:219-253 with _integrate :316-342):
+ * E = sum_r abs_clip(w_r) * abs_clip(abs_clip(sum_f c_f dens_rf)), Kahan-compensated FP64.
+ * d_dens (grid, n_cols); coeffs: n_coeffs (1 broadcasts) host doubles; d_exc one double. */
+int gdft_integrate(int64_t n_grid, int32_t n_cols, const double *h_coeffs, int32_t n_coeffs, const double *d_dens,
+                   const double *d_weights, double clip, double *d_exc, void *d_ws, size_t ws_bytes, void *stream);
+
+/* Workspace bytes of gdft_integrate. */
+int gdft_integrate_workspace_bytes(int64_t n_grid, size_t *bytes);
+
+/* Fock assembly of predict (train.py:147-163):
+ * F = abs_clip(1/2 (G + G^T)) with G = abs_clip(h1e + J + V_xc), both spins.
+ * d_h1e (ao, ao), d_vj (ao, ao) Coulomb potential, d_vxc (2, ao, ao) -> d_fock (2, ao, ao). */
+int gdft_fock(int32_t n_ao, const double *d_h1e, const double *d_vj, const double *d_vxc, double clip,
+              double *d_fock, void *stream);
+
+/* Coulomb potential J_pq = sum_rt (pq|rt) D_rt with D = rdm1 summed over spin
+ * (molecule.py:783-811 coulomb_potential, :117 get_coulomb_potential), and the
+ * non-XC energy E_nuc + tr(D h1e) + 1/2 tr(D J) (molecule.py:694-733 nonXC).
+ * d_eri (ao, ao, ao, ao); d_vj (ao, ao); d_enonxc one double. */
+int gdft_coulomb(int32_t n_ao, const double *d_eri, const double *d_rdm1, const double *d_h1e,
+                 double nuclear_repulsion, double *d_vj, double *d_enonxc, void *stream);
+
+/* Stage timing (observability; no counterpart in the reference, whose only
+ * tracing is jax.profiler.annotate_function at train.py:123).  When enabled,
+ * the library records a CUDA event pair on the launching stream around every
+ * kernel it launches, per stage.  Host-side state is process-wide and not
+ * thread-safe; gdft_profile_read synchronises on the recorded events. */
+enum {
+  GDFT_STAGE_AO = 0,       /* AO table load / evaluation           */
+  GDFT_STAGE_DENSITY = 1,  /* density contraction                  */
+  GDFT_STAGE_POINT = 2,    /* energy densities + adjoint coefficients */
+  GDFT_STAGE_VXC = 3,      /* V_xc contraction                     */
+  GDFT_STAGE_REDUCE = 4,   /* energy / split-K reductions, assembly */
+  GDFT_STAGE_MLP = 5,      /* coefficient network                  */
+  GDFT_STAGE_COUNT = 8
+};
+int gdft_profile_enable(int32_t enable);
+int gdft_profile_reset(void);
+int gdft_profile_read(int32_t stage, double *total_ms, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GDFT_H_ */

@@ -459,11 +459,11 @@ def xc_energy_and_grads(name, rdm1, ao, grad_ao, grad2_ao, weights, params=None,
     grads = torch.autograd.grad(E, inputs, allow_unused=True)
     V = grads[0]
     if not want_param_grads:
-        return float(E), V.numpy()
+        return float(E.detach()), V.numpy()
     dparams = {}
     for ((k, kk), _), g in zip(leaves, grads[1:]):
         dparams.setdefault(k, {})[kk] = (torch.zeros_like(_) if g is None else g).numpy()
-    return float(E), V.numpy(), {"params": dparams}
+    return float(E.detach()), V.numpy(), {"params": dparams}
 
 
 def predict_fock(E_xc, V_xc, h1e, vj, nonxc_energy, clip_cte=CLIP):

@@ -1,0 +1,145 @@
+"""The oracle against fixtures produced by the reference's own grad_dft source.
+
+The fixtures (tests/golden/ref_*.npz) come from tests/golden/make_golden.py,
+which executes the reference's molecule.py, functional.py,
+popular_functionals.py and train.py unchanged.  Everything here is FP64 on
+the CPU, so the agreement is to rounding (1e-12 relative).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from graddft_gb300 import synthetic
+
+RTOL = 1e-12
+FUNCTIONALS = ["LSDA", "B88", "VWN", "LYP", "PW92", "BLYP", "B3LYP"]
+
+
+def _close(a, b, rtol=RTOL):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    m = ~np.isnan(b)
+    scale = max(np.max(np.abs(b[m])), 1e-300) if m.any() else 1.0
+    assert np.max(np.abs(a[m] - b[m])) <= rtol * scale
+
+
+@pytest.mark.parametrize("case", ["compact", "tails"])
+def test_density_primitives(golden, case):
+    g = golden(case)
+    rho, grad_rho, lapl, tau = O.features_numpy(g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"])
+    _close(rho, g["rho"])
+    _close(grad_rho, g["grad_rho"])
+    _close(lapl, g["lapl_rho"])
+    _close(tau, g["tau"])
+
+
+@pytest.mark.parametrize("case", ["compact", "tails"])
+@pytest.mark.parametrize("name", FUNCTIONALS)
+def test_xc_energy_and_grads(golden, case, name):
+    g = golden(case)
+    ehf = g["ehf"][:1] if name == "B3LYP" else None
+    e, v = O.xc_energy_and_grads(name, g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"], ehf=ehf)
+    assert abs(e - float(g[f"exc_{name}"])) <= RTOL * abs(float(g[f"exc_{name}"]))
+    _close(v, g[f"vxc_{name}"])
+
+
+@pytest.mark.parametrize("case", ["compact", "tails"])
+def test_energy_density_columns(golden, case):
+    import torch
+
+    g = golden(case)
+    rho, grad_rho, lapl, tau = (O.t64(x) for x in O.features_numpy(g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"]))
+    _close(O.lsda_x_e(rho)[:, None].numpy(), g["ed_lsda"])
+    _close(torch.stack((O.lsda_x_e(rho), O.b88_x_e(rho, grad_rho)), 1).numpy(), g["ed_b88"])
+    _close(O.vwn_c_e(rho)[:, None].numpy(), g["ed_vwn"])
+    _close(O.lyp_c_e(rho, grad_rho, lapl)[:, None].numpy(), g["ed_lyp"])
+    _close(O.pw92_c_e(rho)[:, None].numpy(), g["ed_pw92"])
+    _close(O.dm21_coefficient_inputs(rho, grad_rho, tau).numpy(), g["dm21_cinputs"])
+    _close(O.dm21_densities(rho, grad_rho, tau, "LDA").numpy(), g["dm21_densities_lda"])
+    _close(O.dm21_densities(rho, grad_rho, tau, "MGGA").numpy(), g["dm21_densities_mgga"])
+    _close(O.densities_generic(rho, grad_rho, tau, "MGGA").numpy(), g["densities_mgga"])
+
+
+@pytest.mark.parametrize("name", ["LSDA", "B88", "BLYP"])
+def test_predict_fock(golden, name):
+    g = golden("compact")
+    e, v = O.xc_energy_and_grads(name, g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"])
+    d = g["rdm1"].sum(0)
+    vj = np.einsum("pqrt,rt->pq", g["eri"], d)
+    enonxc = 1.25 + np.einsum("ij,ij->", d, g["h1e"]) + np.einsum("pq,pq->", d, vj) / 2.0
+    E, F = O.predict_fock(e, v, g["h1e"], vj, enonxc)
+    assert abs(E - float(g[f"predict_E_{name}"])) <= 1e-12 * abs(float(g[f"predict_E_{name}"]))
+    _close(F, g[f"predict_F_{name}"])
+
+
+def test_dm21_energy_and_grads(golden):
+    g = golden("dm21")
+    params = synthetic.glorot_params(seed=int(g["theta_seed"]))
+    e, v, dp = O.xc_energy_and_grads("DM21", g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"],
+                                     params=params, ehf=g["ehf"], want_param_grads=True)
+    assert abs(e - float(g["exc"])) <= RTOL * abs(float(g["exc"]))
+    _close(v, g["vxc"])
+    for k in g.files:
+        if k.startswith("dtheta/") and not k.endswith("/idx"):
+            _, a, b = k.split("/")
+            got = dp["params"][a][b].reshape(-1)
+            if k + "/idx" in g.files:
+                got = got[g[k + "/idx"]]
+            _close(got, g[k].reshape(-1))
+
+
+def test_fzeta_constant():
+    assert abs(O.FZETA_PP0 - 4.0 / (9.0 * (2 ** (1 / 3) - 1.0))) < 1e-13
+
+
+def test_vxc_central_differences():
+    """dE/dD from autodiff against central finite differences (B88+LYP)."""
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "ref_compact.npz"))
+    rdm1 = g["rdm1"]
+    e0, v = O.xc_energy_and_grads("BLYP", rdm1, g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"])
+    rng = np.random.default_rng(3)
+    for _ in range(4):
+        s, a, b = rng.integers(0, 2), rng.integers(0, rdm1.shape[1]), rng.integers(0, rdm1.shape[1])
+        h = 1e-5
+        dp = rdm1.copy()
+        dp[s, a, b] += h
+        dm = rdm1.copy()
+        dm[s, a, b] -= h
+        ep, _ = O.xc_energy_and_grads("BLYP", dp, g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"])
+        em, _ = O.xc_energy_and_grads("BLYP", dm, g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"])
+        fd = (ep - em) / (2 * h)
+        assert abs(fd - v[s, a, b]) <= 1e-6 * max(1.0, np.max(np.abs(v)))
+
+
+def test_ao_oracle_derivatives():
+    """Analytic AO gradients/second derivatives against central differences."""
+    from oracle import eval_ao_planes
+
+    basis = synthetic.make_basis(24, seed=5, centre_box_angstrom=3.0)
+    x = np.random.default_rng(1).uniform(-2, 2, size=(16, 3))
+    ao, g1, g2 = eval_ao_planes(basis, x)
+    h = 1e-5
+    for i in range(3):
+        e = np.zeros(3)
+        e[i] = h
+        ap, g1p, _ = eval_ao_planes(basis, x + e)
+        am, g1m, _ = eval_ao_planes(basis, x - e)
+        np.testing.assert_allclose((ap - am) / (2 * h), g1[..., i], atol=1e-6 * np.abs(g1).max())
+        np.testing.assert_allclose((g1p[..., i] - g1m[..., i]) / (2 * h), g2[..., i], atol=1e-5 * np.abs(g2).max())
+
+
+def test_ao_normalisation():
+    """Each synthetic AO integrates to 1 in L2 (analytic normalisation constants)."""
+    from oracle import eval_ao_planes
+
+    basis = synthetic.make_basis(12, seed=2, centre_box_angstrom=0.0)
+    basis.exponents[:] = 1.3
+    basis.norm[:] = synthetic._norm(basis.kind, basis.comp, basis.exponents)
+    L, n = 5.0, 61
+    t = np.linspace(-L, L, n)
+    X, Y, Z = np.meshgrid(t, t, t, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    ao, _, _ = eval_ao_planes(basis, pts)
+    dv = (t[1] - t[0]) ** 3
+    np.testing.assert_allclose((ao ** 2).sum(0) * dv, 1.0, rtol=1e-6)
