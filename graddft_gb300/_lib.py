@@ -32,7 +32,7 @@ EXPORTS = (
     "gdft_abi_version", "gdft_last_error", "gdft_molecule_bytes", "gdft_molecule_init", "gdft_molecule_load",
     "gdft_molecule_eval_basis", "gdft_workspace_bytes", "gdft_density", "gdft_xc_energy_and_grads",
     "gdft_energy_densities", "gdft_integrate", "gdft_integrate_workspace_bytes", "gdft_fock", "gdft_coulomb",
-    "gdft_profile_enable", "gdft_profile_reset", "gdft_profile_read",
+    "gdft_profile_enable", "gdft_profile_reset", "gdft_profile_read", "gdft_device_status", "gdft_selftest_umma",
 )
 STAGE_AO, STAGE_DENSITY, STAGE_POINT, STAGE_VXC, STAGE_REDUCE, STAGE_MLP = range(6)
 
@@ -83,6 +83,8 @@ _SIGS = {
     "gdft_integrate_workspace_bytes": ([I64, ctypes.POINTER(SZ)], ctypes.c_int),
     "gdft_fock": ([I32, P, P, P, D, P, P], ctypes.c_int),
     "gdft_coulomb": ([I32, P, P, P, D, P, P, P], ctypes.c_int),
+    "gdft_device_status": ([PMOL, P, SZ, ctypes.POINTER(I32), P], ctypes.c_int),
+    "gdft_selftest_umma": ([ctypes.POINTER(D)], ctypes.c_int),
     "gdft_profile_enable": ([I32], ctypes.c_int),
     "gdft_profile_reset": ([], ctypes.c_int),
     "gdft_profile_read": ([I32, ctypes.POINTER(D), ctypes.POINTER(I64)], ctypes.c_int),

@@ -63,13 +63,21 @@ MolLayout mol_layout(int64_t n_grid, int n_ao, int precision) {
   MolLayout L;
   L.np = round_up(n_grid, kPointTile);
   L.ld = (int)round_up(n_ao, kAoPad);
+  L.ldk = (int)round_up(n_ao, 128);
   size_t off = 0;
-  L.off_tab = off;
-  off = align256(off + (size_t)kPlanes * L.plane_elems() * sizeof(double));
   L.off_w = off;
   off = align256(off + (size_t)L.np * sizeof(double));
-  L.off_tc = off;
-  (void)precision;
+  L.off_tab = L.off_pm = L.off_am = off;
+  if (precision == GDFT_FP64) {
+    off = align256(off + (size_t)kPlanes * L.plane_elems() * sizeof(double));
+  } else {
+    // hi/lo TF32 pairs of the five planes in the point-major and AO-major tiles.
+    const size_t tables = (size_t)kPlanes * L.np * L.ldk * 2 * sizeof(float);
+    L.off_pm = off;
+    off = align256(off + tables);
+    L.off_am = off;
+    off = align256(off + tables);
+  }
   L.bytes = off;
   return L;
 }
@@ -78,7 +86,8 @@ WsLayout ws_layout(const gdft_molecule *m) {
   WsLayout W;
   const int64_t np = m->n_grid_pad;
   W.n_eblocks = xc_point_blocks(np);
-  W.n_vsplit = vxc_f64_splits(np, m->n_ao);
+  W.vrange = 0;
+  W.n_vsplit = m->precision == GDFT_FP64 ? vxc_f64_splits(np, m->n_ao) : vxc_tc_splits(np, m->n_ao, &W.vrange);
   size_t off = 0;
   W.off_feat = off;
   off = align256(off + (size_t)2 * kFeat * np * sizeof(double));
@@ -88,10 +97,13 @@ WsLayout ws_layout(const gdft_molecule *m) {
   off = align256(off + (size_t)W.n_eblocks * sizeof(double));
   W.off_vpart = off;
   off = align256(off + (size_t)W.n_vsplit * 2 * m->n_ao * m->n_ao * sizeof(double));
+  W.off_dpk = off;
+  if (m->precision == GDFT_TF32X3) {
+    const size_t ldk = (size_t)round_up(m->n_ao, 128);
+    off = align256(off + 2 * ldk * ldk * 2 * sizeof(float));
+  }
   W.off_err = off;
   off = align256(off + 64);
-  W.off_scratch = off;
-  W.scratch_bytes = 0;
   W.bytes = off;
   return W;
 }
@@ -106,7 +118,8 @@ static int check_mol(const gdft_molecule *m) {
     return GDFT_ERR_INVALID;
   }
   const MolLayout L = mol_layout(m->n_grid, m->n_ao, m->precision);
-  if (m->buffer_bytes < L.bytes || m->n_grid_pad != L.np || m->ld != L.ld) {
+  if (m->buffer_bytes < L.bytes || m->n_grid_pad != L.np || m->ld != L.ld ||
+      (m->precision != GDFT_FP64 && m->precision != GDFT_TF32X3)) {
     set_error("molecule descriptor does not match its layout");
     return GDFT_ERR_INVALID;
   }
@@ -165,6 +178,13 @@ static const double *mol_w(const gdft_molecule *m) {
   return (const double *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_w);
 }
 
+static const float *mol_pm(const gdft_molecule *m) {
+  return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_pm);
+}
+static const float *mol_am(const gdft_molecule *m) {
+  return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_am);
+}
+
 // Density stage into ws.feat.
 static int run_density(const gdft_molecule *m, const double *rdm1, char *ws, cudaStream_t st) {
   const WsLayout W = ws_layout(m);
@@ -173,8 +193,16 @@ static int run_density(const gdft_molecule *m, const double *rdm1, char *ws, cud
     StageTimer tm(GDFT_STAGE_DENSITY, st);
     return check_cuda(launch_dens_f64(mol_tab(m), m->n_grid_pad, m->ld, m->n_ao, rdm1, feat, st), "dens_f64");
   }
-  set_error("precision %d is not available in this build", m->precision);
-  return GDFT_ERR_UNSUPPORTED;
+  const int ldk = (int)round_up(m->n_ao, 128);
+  float *dpk = (float *)(ws + W.off_dpk);
+  int rc;
+  {
+    StageTimer tm(GDFT_STAGE_REDUCE, st);
+    if ((rc = check_cuda(launch_pack_rdm1(rdm1, m->n_ao, ldk, dpk, st), "pack_rdm1"))) return rc;
+  }
+  StageTimer tm(GDFT_STAGE_DENSITY, st);
+  return check_cuda(launch_dens_tc(mol_pm(m), dpk, m->n_grid_pad, ldk, feat, (int *)(ws + W.off_err), st),
+                    "dens_tc");
 }
 
 }  // namespace gdft
@@ -272,6 +300,11 @@ int gdft_molecule_load(const gdft_molecule *mol, const double *d_ao, const doubl
   double *tab = (double *)((char *)mol->buffer + L.off_tab);
   double *w = (double *)((char *)mol->buffer + L.off_w);
   StageTimer tm(GDFT_STAGE_AO, (cudaStream_t)stream);
+  if (mol->precision == GDFT_TF32X3)
+    return check_cuda(launch_pack_tables(d_ao, d_grad_ao, d_grad2_ao, nullptr, nullptr, d_weights, mol->n_grid,
+                                         mol->n_ao, L.np, L.ldk, (float *)((char *)mol->buffer + L.off_pm),
+                                         (float *)((char *)mol->buffer + L.off_am), w, (cudaStream_t)stream),
+                      "pack_tables");
   return check_cuda(launch_load_tables(d_ao, d_grad_ao, d_grad2_ao, d_weights, mol->n_grid, mol->n_ao, L.np, L.ld,
                                        tab, w, (cudaStream_t)stream),
                     "load_tables");
@@ -289,6 +322,11 @@ int gdft_molecule_eval_basis(const gdft_molecule *mol, const double *d_basis, co
   double *tab = (double *)((char *)mol->buffer + L.off_tab);
   double *w = (double *)((char *)mol->buffer + L.off_w);
   StageTimer tm(GDFT_STAGE_AO, (cudaStream_t)stream);
+  if (mol->precision == GDFT_TF32X3)
+    return check_cuda(launch_pack_tables(nullptr, nullptr, nullptr, d_basis, d_coords, d_weights, mol->n_grid,
+                                         mol->n_ao, L.np, L.ldk, (float *)((char *)mol->buffer + L.off_pm),
+                                         (float *)((char *)mol->buffer + L.off_am), w, (cudaStream_t)stream),
+                      "pack_tables");
   return check_cuda(launch_eval_basis(d_basis, d_coords, d_weights, mol->n_grid, mol->n_ao, L.np, L.ld, tab, w,
                                       (cudaStream_t)stream),
                     "eval_basis");
@@ -364,8 +402,38 @@ int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, con
     StageTimer tm(GDFT_STAGE_REDUCE, st);
     return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
   }
-  set_error("precision %d is not available in this build", mol->precision);
-  return GDFT_ERR_UNSUPPORTED;
+  {
+    StageTimer tm(GDFT_STAGE_VXC, st);
+    rc = check_cuda(launch_vxc_tc(mol_am(mol), coef, mol->n_grid_pad, (int)round_up(mol->n_ao, 128), mol->n_ao,
+                                  W.n_vsplit, W.vrange, vpart, (int *)(ws + W.off_err), st),
+                    "vxc_tc");
+    if (rc) return rc;
+  }
+  StageTimer tm(GDFT_STAGE_REDUCE, st);
+  return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
+}
+
+int gdft_device_status(const gdft_molecule *mol, void *d_ws, size_t ws_bytes, int32_t *status, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_ws(mol, d_ws, ws_bytes))) return rc;
+  if (status == nullptr) {
+    set_error("gdft_device_status: null output");
+    return GDFT_ERR_INVALID;
+  }
+  const WsLayout W = ws_layout(mol);
+  int *err = (int *)((char *)d_ws + W.off_err);
+  int h = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  if ((rc = check_cuda(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st), "status read"))) return rc;
+  if ((rc = check_cuda(cudaStreamSynchronize(st), "status sync"))) return rc;
+  if ((rc = check_cuda(cudaMemsetAsync(err, 0, sizeof(int), st), "status clear"))) return rc;
+  *status = h;
+  if (h != 0) {
+    set_error("a device-side wait expired (code %d); results of the last calls are invalid", h);
+    return GDFT_ERR_DEVICE;
+  }
+  return GDFT_OK;
 }
 
 int gdft_energy_densities(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,

@@ -33,8 +33,9 @@ inline int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 // Layout of the molecule buffer.
 struct MolLayout {
   int64_t np;   // padded grid points
-  int ld;       // AO leading dimension
-  size_t off_tab, off_w, off_tc, bytes;
+  int ld;       // AO leading dimension of the FP64 planes
+  int ldk;      // AO extent of the TF32x3 tables (multiple of 128)
+  size_t off_tab, off_w, off_pm, off_am, bytes;
   size_t plane_elems() const { return (size_t)np * ld; }
 };
 
@@ -42,10 +43,10 @@ MolLayout mol_layout(int64_t n_grid, int n_ao, int precision);
 
 // Layout of the per-call workspace.
 struct WsLayout {
-  size_t off_feat, off_coef, off_epart, off_vpart, off_err, off_scratch, bytes;
-  int n_eblocks;  // blocks of the point kernel (energy partial sums)
-  int n_vsplit;   // split-K factor of the V contraction
-  size_t scratch_bytes;
+  size_t off_feat, off_coef, off_epart, off_vpart, off_dpk, off_err, bytes;
+  int n_eblocks;   // blocks of the point kernel (energy partial sums)
+  int n_vsplit;    // split-K factor of the V contraction
+  int64_t vrange;  // grid points per split (TF32x3 form)
 };
 
 WsLayout ws_layout(const gdft_molecule *m);

@@ -1,0 +1,275 @@
+// dens_tc.cu - mixed (TF32x3) form of the density contraction on tcgen05.
+//
+// One CTA owns 128 grid points.  For every AO plane t (phi, d_x, d_y, d_z)
+// and every 128-column block cb of the output it forms, for both spins,
+//   X_t,sigma[:, cb] = T_t D_sigma[:, cb]          (M = 128, N = 128, K = n_ao)
+// in TMEM with three TF32 products per term (hi*hi + hi*lo + lo*hi of the
+// split operands, FP32 accumulation), then the epilogue warps reduce each row
+// against the AO planes exactly as the FP64 form (dens_f64.cu) does:
+//   t = phi : rho, grad rho (x2), and the phi*lap part of the Laplacian
+//   t = d_j : the d_j phi . d_j phi part of the Laplacian and tau.
+// Per-job partial sums are FP32 (128 columns), summed across jobs in FP64.
+//
+// Warp roles (192 threads): warp 0 = TMA producer (one thread issues bulk
+// copies of pre-tiled 32 KB operand images), warp 1 = TMEM owner and MMA
+// issuer (one thread), warps 2-5 = epilogue (TMEM lane quadrant = warp % 4).
+// Two 96 KB smem stages; two TMEM accumulator buffers of 2 x 128 columns so
+// the epilogue of one job overlaps the MMAs of the next.  Every wait is
+// bounded (umma::mbar_wait); on expiry the CTA records an error word, waits
+// for its own copies and MMAs to land and releases TMEM.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "umma.cuh"
+
+namespace gdft {
+
+namespace {
+
+constexpr int kStages = 2;
+constexpr uint32_t kStageBytes = 6 * umma::kBlockBytes;  // A hi|lo, B_a hi|lo, B_b hi|lo
+constexpr int kThreads = 192;
+constexpr uint32_t kTmemCols = 512;
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;
+
+struct DensArgs {
+  const float *pm;   // point-major resident tables
+  const float *dpk;  // packed rdm1
+  int64_t np;
+  int ldk;
+  double *feat;  // [2][6][np]
+  int *err;
+};
+
+__device__ __forceinline__ const float *pm_blk(const DensArgs &A, int64_t tile, int plane, int kc) {
+  const int nkc = A.ldk / 32;
+  return A.pm + ((size_t)(tile * kPlanes + plane) * nkc + kc) * 2 * (umma::kBlockBytes / 4);
+}
+
+__device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, code); }
+
+// The row's 32 values (hi + lo) of a point-major block.
+__device__ __forceinline__ void load_row32(const float *blk, int row, float (&v)[32]) {
+  const float4 *hi = (const float4 *)blk;
+  const float4 *lo = (const float4 *)(blk + umma::kBlockBytes / 4);
+#pragma unroll
+  for (int g = 0; g < 8; ++g) {
+    const int o = (((row >> 3) * 8 + g) * 128 + (row & 7) * 16) / 16;
+    const float4 h = __ldg(hi + o), l = __ldg(lo + o);
+    v[4 * g + 0] = h.x + l.x;
+    v[4 * g + 1] = h.y + l.y;
+    v[4 * g + 2] = h.z + l.z;
+    v[4 * g + 3] = h.w + l.w;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], drain;
+  __shared__ uint32_t tmem_base;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t tile = blockIdx.x;
+  const int nkc = A.ldk / 32, ncb = A.ldk / 128;
+  const int njobs = 4 * ncb;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      umma::mbar_init(&full[s], 1);
+      umma::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      umma::mbar_init(&tfull[b], 1);
+      umma::mbar_init(&tempty[b], 128);
+    }
+    umma::mbar_init(&drain, 1);
+    umma::fence_barrier_init();
+  }
+  if (warp == 1) umma::tmem_alloc(&tmem_base, kTmemCols);
+  umma::tc_fence_before();
+  __syncthreads();
+  umma::tc_fence_after();
+  const uint32_t tbase = tmem_base;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    // The whole warp runs the loop (uniform control flow); lane 0 issues.
+    uint32_t it = 0;
+    bool ok = true;
+    for (int j = 0; j < njobs && ok; ++j) {
+      const int t = j / ncb, cb = j % ncb;
+      for (int kc = 0; kc < nkc; ++kc) {
+        const int s = it % kStages;
+        if (!umma::warp_wait(&empty[s], ((it / kStages) & 1) ^ 1)) {
+          if (lane == 0) flag(A.err, 11);
+          ok = false;
+          break;
+        }
+        if (lane == 0) {
+          unsigned char *st = smem + s * kStageBytes;
+          umma::mbar_arrive_expect_tx(&full[s], kStageBytes);
+          umma::bulk_g2s(st, pm_blk(A, tile, t, kc), 2 * umma::kBlockBytes, &full[s]);
+          for (int sp = 0; sp < 2; ++sp) {
+            const float *b = A.dpk + (((size_t)sp * ncb + cb) * nkc + kc) * 2 * (umma::kBlockBytes / 4);
+            umma::bulk_g2s(st + (2 + 2 * sp) * umma::kBlockBytes, b, 2 * umma::kBlockBytes, &full[s]);
+          }
+        }
+        __syncwarp();
+        ++it;
+      }
+    }
+    // Wait for the copies still in flight before the CTA can retire.
+    for (uint32_t i = it > kStages ? it - kStages : 0; i < it; ++i) {
+      if (!umma::warp_wait(&full[i % kStages], (i / kStages) & 1) && lane == 0) flag(A.err, 12);
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------- MMA issuer
+    const uint32_t idesc = umma::idesc_tf32(128, 128);
+    uint32_t it = 0;
+    bool ok = true;
+    for (int j = 0; j < njobs && ok; ++j) {
+      const int buf = j & 1;
+      if (!umma::warp_wait(&tempty[buf], ((j >> 1) & 1) ^ 1)) {
+        if (lane == 0) flag(A.err, 13);
+        break;
+      }
+      umma::tc_fence_after();
+      for (int kc = 0; kc < nkc; ++kc) {
+        const int s = it % kStages;
+        if (!umma::warp_wait(&full[s], (it / kStages) & 1)) {
+          if (lane == 0) flag(A.err, 14);
+          ok = false;
+          break;
+        }
+        umma::tc_fence_after();
+        if (lane == 0) {
+          const uint32_t sb = umma::smem_u32(smem + s * kStageBytes);
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t ahi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+            const uint64_t alo = umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+#pragma unroll
+            for (int sp = 0; sp < 2; ++sp) {
+              const uint32_t bb = sb + (2 + 2 * sp) * umma::kBlockBytes + kk * 256;
+              const uint64_t bhi = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
+              const uint64_t blo = umma::sdesc(bb + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
+              const uint32_t d = tbase + buf * 256 + sp * 128;
+              umma::mma_tf32(d, ahi, bhi, idesc, (kc > 0 || kk > 0) ? 1u : 0u);
+              umma::mma_tf32(d, ahi, blo, idesc, 1u);
+              umma::mma_tf32(d, alo, bhi, idesc, 1u);
+            }
+          }
+          umma::mma_commit(&empty[s]);
+        }
+        __syncwarp();
+        ++it;
+      }
+      if (!ok) break;
+      if (lane == 0) umma::mma_commit(&tfull[buf]);
+      __syncwarp();
+    }
+    // All issued MMAs complete before TMEM is released.
+    if (lane == 0) umma::mma_commit(&drain);
+    __syncwarp();
+    if (!umma::warp_wait(&drain, 0) && lane == 0) flag(A.err, 15);
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
+    double F[2][6];
+#pragma unroll
+    for (int sp = 0; sp < 2; ++sp)
+#pragma unroll
+      for (int k = 0; k < 6; ++k) F[sp][k] = 0.0;
+    for (int j = 0; j < njobs; ++j) {
+      const int buf = j & 1;
+      const int t = j / ncb, cb = j % ncb;
+      if (!umma::warp_wait(&tfull[buf], (j >> 1) & 1)) {
+        if (lane == 0) flag(A.err, 16);
+        break;
+      }
+      umma::tc_fence_after();
+      float acc[2][5];
+#pragma unroll
+      for (int sp = 0; sp < 2; ++sp)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) acc[sp][k] = 0.0f;
+      for (int c0 = 0; c0 < 128; c0 += 32) {
+        float x0[32], x1[32], pv[32];
+        umma::tmem_ld32(tl + buf * 256 + c0, x0);
+        umma::tmem_ld32(tl + buf * 256 + 128 + c0, x1);
+        const int kc = cb * 4 + c0 / 32;
+        if (t == 0) {
+#pragma unroll 1
+          for (int k = 0; k < kPlanes; ++k) {
+            load_row32(pm_blk(A, tile, k, kc), row, pv);
+            float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              a0 = fmaf(x0[i], pv[i], a0);
+              a1 = fmaf(x1[i], pv[i], a1);
+            }
+            acc[0][k] += a0;
+            acc[1][k] += a1;
+          }
+        } else {
+          load_row32(pm_blk(A, tile, t, kc), row, pv);
+          float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            a0 = fmaf(x0[i], pv[i], a0);
+            a1 = fmaf(x1[i], pv[i], a1);
+          }
+          acc[0][0] += a0;
+          acc[1][0] += a1;
+        }
+      }
+      umma::tc_fence_before();
+      umma::mbar_arrive(&tempty[buf]);
+#pragma unroll
+      for (int sp = 0; sp < 2; ++sp) {
+        if (t == 0) {
+          F[sp][0] += acc[sp][T_PHI];  // rho
+          F[sp][1] += acc[sp][T_DX];
+          F[sp][2] += acc[sp][T_DY];
+          F[sp][3] += acc[sp][T_DZ];
+          F[sp][4] += acc[sp][T_LAP];  // phi . lap phi part
+        } else {
+          F[sp][5] += acc[sp][0];  // sum_j d_j phi . d_j phi part
+        }
+      }
+    }
+    const int64_t p = tile * 128 + row;
+#pragma unroll
+    for (int sp = 0; sp < 2; ++sp) {
+      double *fs = A.feat + (size_t)sp * kFeat * A.np;
+      fs[F_RHO * A.np + p] = F[sp][0];
+      fs[F_GX * A.np + p] = 2.0 * F[sp][1];
+      fs[F_GY * A.np + p] = 2.0 * F[sp][2];
+      fs[F_GZ * A.np + p] = 2.0 * F[sp][3];
+      fs[F_LAP * A.np + p] = 2.0 * F[sp][5] + 2.0 * F[sp][4];
+      fs[F_TAU * A.np + p] = 0.5 * F[sp][5];
+    }
+  }
+  umma::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) umma::tmem_dealloc(tbase, kTmemCols);
+}
+
+}  // namespace
+
+cudaError_t launch_dens_tc(const float *pm, const float *dpk, int64_t np, int ldk, double *feat, int *err,
+                           cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(dens_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  DensArgs a{pm, dpk, np, ldk, feat, err};
+  dens_tc_kernel<<<(unsigned)(np / 128), kThreads, kSmemBytes, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace gdft

@@ -1,0 +1,151 @@
+// tc_pack.cu - operand layouts of the TF32x3 (mixed) form.
+//
+// The AO planes (phi, d_x phi, d_y phi, d_z phi, lap phi) are kept resident as
+// pairs of TF32 values (hi + lo ~= the FP64 value to about 22 bits) in two
+// pre-tiled layouts whose 16 KB blocks are exactly the shared-memory images
+// the tensor cores read (K-major, no swizzle, see umma::kblock_off), so every
+// operand stage is one contiguous bulk copy:
+//   point-major  [point tile (128)][plane][AO chunk (32)][hi|lo] : 128 points x 32 AO
+//     (A operand of the density contraction and its epilogue partners)
+//   AO-major     [AO tile (128)][plane][point chunk (32)][hi|lo] : 128 AO x 32 points
+//     (operands of the V_xc contraction, contracted over points)
+// The density matrix is packed per call as the B operand of the density
+// contraction: [spin][column tile (128)][k chunk (32)][hi|lo], element (c, k) = D[k][c].
+#include "common.cuh"
+#include "kernels.cuh"
+#include "umma.cuh"
+
+namespace gdft {
+
+namespace {
+
+__device__ __forceinline__ size_t pm_block(int64_t tile, int plane, int kc, int nkc) {
+  return ((size_t)(tile * kPlanes + plane) * nkc + kc) * 2;  // in units of 16 KB blocks (hi; lo = +1)
+}
+__device__ __forceinline__ size_t am_block(int atile, int plane, int64_t pc, int64_t npc) {
+  return ((size_t)(atile * kPlanes + plane) * npc + pc) * 2;
+}
+
+__device__ __forceinline__ void store_split(float *base, size_t blk, uint32_t off, double v) {
+  float hi, lo;
+  umma::split_tf32(v, hi, lo);
+  float *b = (float *)((char *)base + blk * umma::kBlockBytes);
+  b[off / 4] = hi;
+  b[umma::kBlockBytes / 4 + off / 4] = lo;
+}
+
+// One thread per (point, AO) of the padded tables: computes the five plane
+// values (from reference layouts or from the synthetic basis) and scatters
+// them, split, into both layouts.
+template <bool kBasis>
+__global__ void pack_tables_kernel(const double *__restrict__ ao, const double *__restrict__ grad_ao,
+                                   const double *__restrict__ grad2_ao, const double *__restrict__ basis,
+                                   const double *__restrict__ coords, const double *__restrict__ w, int64_t n_grid,
+                                   int n_ao, int64_t np, int ldk, float *__restrict__ pm, float *__restrict__ am,
+                                   double *__restrict__ wout) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)np * ldk) return;
+  const int64_t p = (int64_t)(idx / ldk);
+  const int a = (int)(idx % ldk);
+  double v[kPlanes] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if (p < n_grid && a < n_ao) {
+    if (!kBasis) {
+      const size_t r = (size_t)p * n_ao + a;
+      v[T_PHI] = ao[r];
+      v[T_DX] = grad_ao[3 * r + 0];
+      v[T_DY] = grad_ao[3 * r + 1];
+      v[T_DZ] = grad_ao[3 * r + 2];
+      if (grad2_ao != nullptr) v[T_LAP] = (grad2_ao[3 * r + 0] + grad2_ao[3 * r + 1]) + grad2_ao[3 * r + 2];
+    } else {
+      const double *b = basis + 8 * (size_t)a;
+      const double x = coords[3 * p + 0] - b[0];
+      const double y = coords[3 * p + 1] - b[1];
+      const double z = coords[3 * p + 2] - b[2];
+      const double al = b[3];
+      const double ex = b[4] * exp(-al * (x * x + y * y + z * z));
+      const int kind = (int)b[5], comp = (int)b[6];
+      double P = 1.0, dP[3] = {0.0, 0.0, 0.0}, d2P[3] = {0.0, 0.0, 0.0};
+      const double xyz[3] = {x, y, z};
+      if (kind == 1) {
+        P = xyz[comp];
+        dP[comp] = 1.0;
+      } else if (kind == 2) {
+        if (comp <= 2) {
+          const int i0 = comp == 1 ? 1 : 0, i1 = comp == 0 ? 1 : 2;
+          P = xyz[i0] * xyz[i1];
+          dP[i0] = xyz[i1];
+          dP[i1] = xyz[i0];
+        } else if (comp == 3) {
+          P = x * x - y * y;
+          dP[0] = 2 * x;
+          dP[1] = -2 * y;
+          d2P[0] = 2.0;
+          d2P[1] = -2.0;
+        } else {
+          P = 2 * z * z - x * x - y * y;
+          dP[0] = -2 * x;
+          dP[1] = -2 * y;
+          dP[2] = 4 * z;
+          d2P[0] = -2.0;
+          d2P[1] = -2.0;
+          d2P[2] = 4.0;
+        }
+      }
+      v[T_PHI] = P * ex;
+      double lp[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        v[T_DX + i] = (dP[i] - 2 * al * xyz[i] * P) * ex;
+        lp[i] = (d2P[i] - 2 * al * P - 4 * al * xyz[i] * dP[i] + 4 * al * al * xyz[i] * xyz[i] * P) * ex;
+      }
+      v[T_LAP] = (lp[0] + lp[1]) + lp[2];
+    }
+  }
+  const int nkc = ldk / 32;
+  const int64_t npc = np / 32;
+  const int64_t tile = p / 128;
+#pragma unroll
+  for (int t = 0; t < kPlanes; ++t) {
+    store_split(pm, pm_block(tile, t, a / 32, nkc), umma::kblock_off((int)(p % 128), a % 32), v[t]);
+    store_split(am, am_block(a / 128, t, p / 32, npc), umma::kblock_off(a % 128, (int)(p % 32)), v[t]);
+  }
+  if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
+}
+
+// D (2, n, n) -> [spin][column tile][k chunk][hi|lo] blocks with (c, k) = D[k][c].
+__global__ void pack_rdm1_kernel(const double *__restrict__ D, int n, int ldk, float *__restrict__ out) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t per_spin = (size_t)ldk * ldk;
+  if (idx >= 2 * per_spin) return;
+  const int s = (int)(idx / per_spin);
+  const int k = (int)((idx % per_spin) / ldk);
+  const int c = (int)(idx % ldk);
+  const double v = (k < n && c < n) ? D[((size_t)s * n + k) * n + c] : 0.0;
+  const int nkc = ldk / 32, ncb = ldk / 128;
+  const size_t blk = (((size_t)s * ncb + c / 128) * nkc + k / 32) * 2;
+  store_split(out, blk, umma::kblock_off(c % 128, k % 32), v);
+}
+
+}  // namespace
+
+cudaError_t launch_pack_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *basis,
+                               const double *coords, const double *w, int64_t n_grid, int n_ao, int64_t np, int ldk,
+                               float *pm, float *am, double *wout, cudaStream_t st) {
+  const size_t total = (size_t)np * ldk;
+  const unsigned blocks = (unsigned)((total + 255) / 256);
+  if (basis != nullptr)
+    pack_tables_kernel<true><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
+                                                     pm, am, wout);
+  else
+    pack_tables_kernel<false><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
+                                                      pm, am, wout);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_rdm1(const double *D, int n, int ldk, float *out, cudaStream_t st) {
+  const size_t total = (size_t)2 * ldk * ldk;
+  pack_rdm1_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(D, n, ldk, out);
+  return cudaGetLastError();
+}
+
+}  // namespace gdft

@@ -35,12 +35,21 @@ __device__ __forceinline__ T fzeta_log2(const T &z) {
 __device__ __forceinline__ double fzeta_pp0() { return 4.0 / (9.0 * (pow(2.0, 1.0 / 3.0) - 1.0)); }
 
 // correlation_polarization_correction, functional.py:982-1045.
+//
+// `nan_path` is set when the reference's reverse-mode gradient is NaN: with
+// rho_a + rho_b > clip and zeta exactly +-1, the backward of log2(1 -+ zeta)
+// in fzeta divides a (possibly zero) cotangent by zero, and the NaN reaches
+// rho_a and rho_b through the selected branch of the zeta `where`, whatever
+// the masks further down (jax.grad at train.py:86).  Forward-mode partials
+// would stay finite there, so the caller poisons those inputs explicitly.
 template <class T>
-__device__ __forceinline__ T corr_pol(const T &ep0, const T &ep1, const T &r0, const T &r1, double clip) {
+__device__ __forceinline__ T corr_pol(const T &ep0, const T &ep1, const T &r0, const T &r1, double clip,
+                                      bool *nan_path = nullptr) {
   const T rs = r0 + r1;
   const T log_rho = xlog2(xclipmin(rs, clip));
   const T log_rs = log2(pow(3.0 / (4.0 * kPi), 1.0 / 3.0)) - log_rho / 3.0;
   const T zeta = xwhere(val(rs) > clip, (r0 - r1) / rs, tconst(rs, 0.0));
+  if (nan_path != nullptr) *nan_path = val(rs) > clip && (1.0 - val(zeta) == 0.0 || 1.0 + val(zeta) == 0.0);
   const double A_ = 0.016887, alpha1 = 0.11125, beta1 = 10.357, beta2 = 3.6231, beta3 = 0.88026,
                beta4 = 0.49671;
   const T ars = xexp2(log2(alpha1) + log_rs);
@@ -86,7 +95,7 @@ __device__ __forceinline__ T b88_x_e(const T rho_in[2], const T s[2], double cli
 
 // pw92_c_e, popular_functionals.py:105-139.
 template <class T>
-__device__ __forceinline__ T pw92_c_e(const T rho[2], double clip) {
+__device__ __forceinline__ T pw92_c_e(const T rho[2], double clip, unsigned *poison = nullptr) {
   const double A_[2] = {0.031091, 0.015545}, alpha1[2] = {0.21370, 0.20548}, beta1[2] = {7.5957, 14.1189},
                beta2[2] = {3.5876, 6.1977}, beta3[2] = {1.6382, 3.3662}, beta4[2] = {0.49294, 0.62517};
   const T rs_sum = rho[0] + rho[1];
@@ -102,13 +111,15 @@ __device__ __forceinline__ T pw92_c_e(const T rho[2], double clip) {
     const T brs2 = xexp2(2.0 * log_rs + log2(beta4[k]));
     ep[k] = -2.0 * A_[k] * (1.0 + ars) * xlog(1.0 + (1.0 / (2.0 * A_[k])) / (brs_1_2 + brs + brs_3_2 + brs2));
   }
-  const T et = corr_pol(ep[0], ep[1], rho[0], rho[1], clip);
+  bool np = false;
+  const T et = corr_pol(ep[0], ep[1], rho[0], rho[1], clip, &np);
+  if (poison != nullptr && np) *poison |= 3u;  // both spins reach zeta unmasked
   return et * rs_sum;
 }
 
 // vwn_c_e, popular_functionals.py:141-195.
 template <class T>
-__device__ __forceinline__ T vwn_c_e(const T rho_in[2], double clip) {
+__device__ __forceinline__ T vwn_c_e(const T rho_in[2], double clip, unsigned *poison = nullptr) {
   const double A[2] = {0.0621814, 0.0621814 / 2.0}, b[2] = {3.72744, 7.06042}, c[2] = {12.9352, 18.0578},
                x0[2] = {-0.10498, -0.325};
   const T r0 = xwhere(val(rho_in[0]) > clip, rho_in[0], tconst(rho_in[0], 0.0));
@@ -129,7 +140,10 @@ __device__ __forceinline__ T vwn_c_e(const T rho_in[2], double clip) {
             (2.0 * xlog(x) - xlog(X) + 2.0 * b[k] / Q * at -
              b[k] * x0[k] / X0 * (xlog(xsq(x - x0[k]) / X) + 2.0 * (2.0 * x0[k] + b[k]) / Q * at));
   }
-  const T et = corr_pol(ep[0], ep[1], r0, r1, clip);
+  bool np = false;
+  const T et = corr_pol(ep[0], ep[1], r0, r1, clip, &np);
+  // where(rho > clip, rho, 0) routes the NaN only to the spins above the clip.
+  if (poison != nullptr && np) *poison |= (val(rho_in[0]) > clip ? 1u : 0u) | (val(rho_in[1]) > clip ? 2u : 0u);
   return et * rs_sum;
 }
 

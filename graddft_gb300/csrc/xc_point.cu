@@ -36,13 +36,13 @@ __device__ __forceinline__ Dual<K> seed(double v, int idx) {
 
 template <class T>
 __device__ __forceinline__ T column(int col, const T rho[2], const T s[2], const T lap[2], double hf,
-                                    double hf0, double hf1, double clip) {
+                                    double hf0, double hf1, double clip, unsigned *poison) {
   switch (col) {
     case GDFT_COL_LSDA: return lsda_x_e(rho, clip);
     case GDFT_COL_B88: return b88_x_e(rho, s, clip);
-    case GDFT_COL_VWN: return vwn_c_e(rho, clip);
+    case GDFT_COL_VWN: return vwn_c_e(rho, clip, poison);
     case GDFT_COL_LYP: return lyp_c_e(rho, s, lap, clip);
-    case GDFT_COL_PW92: return pw92_c_e(rho, clip);
+    case GDFT_COL_PW92: return pw92_c_e(rho, clip, poison);
     case GDFT_COL_DM21_LDA: return dm21_lda(rho, clip);
     case GDFT_COL_HF: return tconst(rho[0], hf);
     case GDFT_COL_HF_W0: return tconst(rho[0], hf0);
@@ -93,8 +93,9 @@ __global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restri
       }
       // Energy density: sum_f c_f * abs_clip(e_f), then abs_clip; weight abs_clip(w).
       Dual<KV> exc = dconst<KV>(0.0);
+      unsigned poison = 0;  // spins whose rho gradient is NaN in the reference (see corr_pol)
       for (int i = 0; i < fn.n_cols; ++i) {
-        Dual<KV> e = column<Dual<KV>>(fn.cols[i], rho, sg, lap, hf, hf0, hf1, clip);
+        Dual<KV> e = column<Dual<KV>>(fn.cols[i], rho, sg, lap, hf, hf0, hf1, clip, &poison);
         if (dens != nullptr) dens[(size_t)p * fn.n_cols + i] = e.v;
         if (!(fabs(e.v) > clip)) e = dconst<KV>(0.0);  // abs_clip(densities), functional.py:184
         const double ci = fn.n_coeffs == 1 ? fn.coeffs[0] : fn.coeffs[i];
@@ -118,6 +119,7 @@ __global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restri
         c[s][C_GZ] = 2.0 * (2.0 * f[s][F_GZ] * dsig);
         c[s][C_LAP] = 2.0 * dlap;
         c[s][C_KIN] = 2.0 * dlap;  // + 1/2 dE/dtau (no tau dependence in these columns)
+        if (poison & (1u << s)) c[s][C_RHO] = __longlong_as_double(0x7ff8000000000000ll);
       }
     }
     if (coef != nullptr) {

@@ -63,7 +63,7 @@ class Resident:
                                      _ptr(self.buffer), nbytes.value))
         wbytes = ctypes.c_size_t()
         check(lib.gdft_workspace_bytes(ctypes.byref(self.desc), ctypes.byref(wbytes)))
-        self.ws = torch.empty(wbytes.value, dtype=torch.uint8, device=self.device)
+        self.ws = torch.zeros(wbytes.value, dtype=torch.uint8, device=self.device)  # error word starts at 0
 
     @property
     def nbytes(self) -> int:
@@ -138,11 +138,25 @@ class Resident:
                                                    self.ws.numel(), _stream(self.device)))
         return exc, vxc
 
+    def status(self) -> int:
+        """Synchronise and raise if a kernel recorded an expired bounded wait since the last query."""
+        st = ctypes.c_int32()
+        check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(self.ws), self.ws.numel(),
+                                             ctypes.byref(st), _stream(self.device)))
+        return st.value
+
     def _rdm1(self, rdm1) -> torch.Tensor:
         rdm1 = as_device_f64(rdm1, self.device)
         if rdm1.shape != (2, self.n_ao, self.n_ao):
             raise ValueError(f"rdm1 must be (2, {self.n_ao}, {self.n_ao}), got {tuple(rdm1.shape)}")
         return rdm1
+
+
+def selftest_umma() -> float:
+    """Run the tensor-core self-test; returns the max abs error (0 when the device path is right)."""
+    err = ctypes.c_double()
+    check(_lib.load().gdft_selftest_umma(ctypes.byref(err)))
+    return err.value
 
 
 def make_functional(cols: Sequence[int], coeffs: Sequence[float], clip: float = 1e-30) -> GdftFunctional:

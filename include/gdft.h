@@ -164,6 +164,19 @@ int gdft_fock(int32_t n_ao, const double *d_h1e, const double *d_vj, const doubl
 int gdft_coulomb(int32_t n_ao, const double *d_eri, const double *d_rdm1, const double *d_h1e,
                  double nuclear_repulsion, double *d_vj, double *d_enonxc, void *stream);
 
+/* Device-side status of the calls made with this workspace since the last
+ * query: kernels never trap; a bounded wait that expired records a nonzero
+ * code in the workspace.  Synchronises `stream`, returns GDFT_ERR_DEVICE (and
+ * the code in *status) if set, and clears it.  No counterpart in the
+ * reference (its errors are Python exceptions). */
+int gdft_device_status(const gdft_molecule *mol, void *d_ws, size_t ws_bytes, int32_t *status, void *stream);
+
+/* Self-test of the tensor-core building blocks (TMA bulk copy, tcgen05.mma
+ * kind::tf32, TMEM load) on one 128 x 128 x 32 product of small integers;
+ * *max_abs_err is 0 on a correct device path.  Synchronous; allocates its own
+ * small buffers.  No counterpart in the reference. */
+int gdft_selftest_umma(double *max_abs_err);
+
 /* Stage timing (observability; no counterpart in the reference, whose only
  * tracing is jax.profiler.annotate_function at train.py:123).  When enabled,
  * the library records a CUDA event pair on the launching stream around every

@@ -1,0 +1,92 @@
+"""GPU parity of the mixed (TF32x3 tensor-core) form.
+
+The mixed form rounds the AO tables and D to hi + lo TF32 pairs (~22 bits)
+and accumulates in FP32 inside bounded windows, FP64 across them.  It is
+checked against the FP64 oracle on small and ragged shapes with the
+tolerances below (relative to the largest entry), and against the GPU FP64
+form at larger sizes.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from graddft_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+# Mixed-form tolerances, relative to the largest magnitude of the quantity.
+TOL_FEAT = 2e-6
+TOL_E = 2e-7
+TOL_V = 2e-6
+
+
+@pytest.fixture(scope="module")
+def eng(built_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from graddft_gb300 import engine
+
+    return engine
+
+
+def _rel(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def test_umma_selftest(eng):
+    assert eng.selftest_umma() == 0.0
+
+
+@pytest.mark.parametrize("n_ao,n_grid", [(20, 512), (64, 2048), (130, 1000), (200, 4096)])
+def test_mixed_density_vs_oracle(eng, n_ao, n_grid):
+    wl = synthetic.make_workload(n_grid, n_ao, max(1, n_ao // 8), seed=n_ao + 1, box_angstrom=8.0,
+                                 centre_box_angstrom=5.0)
+    ao, g1, g2 = O.eval_ao_planes(wl.basis, wl.coords)
+    r = eng.Resident.from_tables(ao, g1, g2, wl.weights, "tf32x3")
+    got = r.density(wl.rdm1)
+    assert r.status() == 0
+    rho, grad_rho, lapl, tau = O.features_numpy(wl.rdm1, ao, g1, g2)
+    errs = {k: _rel(got[k], v) for k, v in (("rho", rho), ("grad_rho", grad_rho), ("lapl", lapl), ("tau", tau))}
+    print(n_ao, n_grid, errs)
+    assert all(e <= TOL_FEAT for e in errs.values()), errs
+
+
+@pytest.mark.parametrize("n_ao,n_grid", [(20, 512), (64, 2048), (130, 1000), (200, 4096)])
+def test_mixed_xc_vs_oracle(eng, n_ao, n_grid):
+    from graddft_gb300 import _lib
+
+    wl = synthetic.make_workload(n_grid, n_ao, max(1, n_ao // 8), seed=n_ao + 2, box_angstrom=8.0,
+                                 centre_box_angstrom=5.0)
+    ao, g1, g2 = O.eval_ao_planes(wl.basis, wl.coords)
+    r = eng.Resident.from_tables(ao, g1, g2, wl.weights, "tf32x3")
+    fn = eng.make_functional([_lib.COL_LSDA, _lib.COL_B88, _lib.COL_LYP], [1.0])
+    exc, vxc = r.xc_energy_and_grads(wl.rdm1, fn)
+    assert r.status() == 0
+    e_ref, v_ref = O.xc_energy_and_grads("BLYP", wl.rdm1, ao, g1, g2, wl.weights)
+    de = abs(float(exc) - e_ref) / abs(e_ref)
+    dv = _rel(vxc, v_ref)
+    print(n_ao, n_grid, "dE", de, "dV", dv, "E", e_ref, "max|V|", np.abs(v_ref).max())
+    assert de <= TOL_E and dv <= TOL_V
+
+
+def test_mixed_vs_fp64_gpu_large(eng):
+    """n_ao 512 on 2^16 points: mixed vs the FP64 GPU form (itself pinned to the oracle)."""
+    from graddft_gb300 import _lib
+
+    wl = synthetic.make_workload(1 << 16, 512, 64, seed=0)
+    fn = eng.make_functional([_lib.COL_LSDA, _lib.COL_B88, _lib.COL_LYP], [1.0])
+    out = {}
+    for prec in ("fp64", "tf32x3"):
+        r = eng.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, prec)
+        out[prec] = r.xc_energy_and_grads(wl.rdm1, fn)
+        assert r.status() == 0
+        del r
+    (e64, v64), (emx, vmx) = out["fp64"], out["tf32x3"]
+    de = abs(float(emx) - float(e64))
+    dv = float((vmx - v64).abs().max())
+    print("E", float(e64), "|dE|", de, "max|V|", float(v64.abs().max()), "max|dV|", dv)
+    assert de <= TOL_E * abs(float(e64))
+    assert dv <= TOL_V * float(v64.abs().max())
