@@ -152,6 +152,7 @@ def main():
                     help="grid points of the FP64-form measurement (its rate is per point)")
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -170,27 +171,24 @@ def main():
 
     build.build()
     lib = _lib.load()
-    form = args.form or "fp64"
+    form = args.form or "tf32x3"
     dev = torch.device("cuda", local)
     fn = engine.make_functional([_lib.COL_LSDA, _lib.COL_B88, _lib.COL_LYP], [1.0])
 
-    def resident(n_grid, precision, seed):
-        wl = synthetic.make_workload(n_grid, args.n_ao, N_OCC, seed)
-        r = engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, precision, dev)
-        return r, torch.as_tensor(wl.rdm1, device=dev)
+    # Each rank owns its own grid slice of the same molecule (weak scaling).
+    wl = synthetic.make_workload(args.n_grid, args.n_ao, N_OCC, SEED)
+    coords = wl.coords + 1e-3 * rank if world > 1 else wl.coords
+    rdm1 = torch.as_tensor(wl.rdm1, device=dev)
 
-    # Each rank owns its own grid slice (weak scaling); D and the basis are shared.
-    r, rdm1 = resident(args.n_grid, form, SEED)
-    if world > 1:
-        # same molecule, rank-specific grid slice
-        wl = synthetic.make_workload(args.n_grid, args.n_ao, N_OCC, SEED)
-        coords = wl.coords + 1e-3 * rank
-        r = engine.Resident.from_basis(wl.basis.packed(), coords, wl.weights, form, dev)
+    def resident(precision):
+        return engine.Resident.from_basis(wl.basis.packed(), coords, wl.weights, precision, dev)
+
+    r = resident(form)
     exc = torch.empty((), dtype=torch.float64, device=dev)
     vxc = torch.empty((2, args.n_ao, args.n_ao), dtype=torch.float64, device=dev)
 
-    def step():
-        r.xc_energy_and_grads(rdm1, fn, None, True, exc, vxc)
+    def step(res=r):
+        res.xc_energy_and_grads(rdm1, fn, None, True, exc, vxc)
         if world > 1:
             import torch.distributed as dist
 
@@ -206,6 +204,7 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    r.status()
     lib.gdft_profile_reset()
     lib.gdft_profile_enable(1)
     stream = torch.cuda.current_stream(dev)
@@ -220,12 +219,13 @@ def main():
         torch.cuda.synchronize()
         barrier()
     lib.gdft_profile_enable(0)
+    r.status()
     ms = e0.elapsed_time(e1)
+    import ctypes
+
     stage = {}
     for name, sid in (("density", _lib.STAGE_DENSITY), ("point", _lib.STAGE_POINT), ("vxc", _lib.STAGE_VXC),
                       ("reduce", _lib.STAGE_REDUCE)):
-        import ctypes
-
         t, n = ctypes.c_double(), ctypes.c_int64()
         _lib.check(lib.gdft_profile_read(sid, ctypes.byref(t), ctypes.byref(n)))
         stage[name] = (t.value, n.value)
@@ -238,30 +238,55 @@ def main():
         ms = float(t)
     ms_step = ms / args.steps
     value = world * args.n_grid / (ms_step * 1e-3)
+    e_mixed, v_mixed = exc.clone(), vxc.clone()
 
     # e2e: the same call with host buffers (pinned rdm1 in, E and V out) per step.
     h_rdm1 = rdm1.cpu().pin_memory()
     h_v = torch.empty(vxc.shape, dtype=torch.float64).pin_memory()
     h_e = torch.empty((), dtype=torch.float64).pin_memory()
     d_rdm1 = torch.empty_like(rdm1)
-    for _ in range(2):
+
+    def e2e_step():
         d_rdm1.copy_(h_rdm1, non_blocking=True)
         r.xc_energy_and_grads(d_rdm1, fn, None, True, exc, vxc)
         h_v.copy_(vxc, non_blocking=True)
         h_e.copy_(exc, non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(args.steps):
-        d_rdm1.copy_(h_rdm1, non_blocking=True)
-        r.xc_energy_and_grads(d_rdm1, fn, None, True, exc, vxc)
-        h_v.copy_(vxc, non_blocking=True)
-        h_e.copy_(exc, non_blocking=True)
+        e2e_step()
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
-    e2e = {"value": args.n_grid / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": rdm1.numel() * 8,
+    e2e = {"value": world * args.n_grid / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": rdm1.numel() * 8,
            "d2h_bytes_per_step": vxc.numel() * 8 + 8,
            "note": "molecule (grid, AO tables) resident as after to_device_arrays; rdm1 in, E_xc and V_xc out"}
+
+    # The other form on the same full workload: FP64 rate and the accuracy of the mixed form.
+    other = {}
+    if form == "tf32x3" and not args.no_fp64:
+        del r
+        torch.cuda.empty_cache()
+        r64 = resident("fp64")
+        step(r64)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        step(r64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        r64.status()
+        ms64 = e0.elapsed_time(e1)
+        other = {
+            "fp64_form_value": world * args.n_grid / (ms64 * 1e-3), "fp64_form_ms_per_step": ms64,
+            "mixed_over_fp64": (world * args.n_grid / (ms_step * 1e-3)) / (world * args.n_grid / (ms64 * 1e-3)),
+            "accuracy_vs_fp64": {"E_xc": float(exc), "abs_dE": abs(float(e_mixed) - float(exc)),
+                                 "max_abs_V": float(vxc.abs().max()),
+                                 "max_abs_dV": float((v_mixed - vxc).abs().max()),
+                                 "target": {"abs_dE": 1e-6, "max_abs_dV": 1e-7}},
+        }
 
     # Roofline of the dominant kernel.
     hbm, bf16, src = _peaks()
@@ -272,10 +297,11 @@ def main():
     if form == "fp64":
         peak, bound, peak_src = 1.25, "fp64", "nominal GB300 FP64 rate (no measured FP64 peak)"
     else:
-        peak, bound, peak_src = bf16, "tensor", f"{src} bf16 dense (TF32 pipe nominally runs at half of it)"
+        peak, bound, peak_src = bf16, "tensor", f"{src} bf16 dense (the TF32 pipe nominally runs at half of it)"
     roof = {"bound": bound, "kernel": f"{dom}_{form}", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
             "flops_per_launch": flops_launch,
+            "executed_flops_per_launch": flops_launch * (3 if form == "tf32x3" else 1),
             "stage_ms_per_step": {k: v[0] / args.steps for k, v in stage.items()}}
 
     line = {
@@ -284,9 +310,9 @@ def main():
         "vs_baseline": None, "dtype": "f64" if form == "fp64" else "tf32x3",
         "data": "synthetic (seeded Gaussian basis evaluated on the device)",
         "config": {"workload": WORKLOAD, "n_ao": args.n_ao, "n_grid": args.n_grid, "form": form,
-                   "functional": "B88+LYP", "l2": "inputs larger than L2 (5 FP64 AO planes, "
-                                                 f"{5 * args.n_grid * args.n_ao * 8 / 2**30:.1f} GiB)"},
-        "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
+                   "functional": "B88+LYP", "l2": "inputs larger than L2 (AO tables "
+                                                 f"{5 * args.n_grid * args.n_ao * 8 / 2**30:.1f} GiB per layout)"},
+        "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), **other,
     }
     if rank == 0 and not args.no_cpu:
         v, dt = cpu_baseline(args.cpu_sample, os.cpu_count() or 1)

@@ -209,6 +209,32 @@ static int run_density(const gdft_molecule *m, const double *rdm1, char *ws, cud
 
 using namespace gdft;
 
+// V_xc contraction of the adjoint coefficients in ws.coef into d_vxc.
+static int run_vxc(const gdft_molecule *mol, const double *coef, double *d_vxc, char *ws, cudaStream_t st) {
+  const WsLayout W = ws_layout(mol);
+  int rc;
+  double *vpart = (double *)(ws + W.off_vpart);
+  if (mol->precision == GDFT_FP64) {
+    {
+      StageTimer tm(GDFT_STAGE_VXC, st);
+      rc = check_cuda(launch_vxc_f64(mol_tab(mol), mol->n_grid_pad, mol->ld, mol->n_ao, coef, W.n_vsplit, vpart, st),
+                      "vxc_f64");
+      if (rc) return rc;
+    }
+    StageTimer tm(GDFT_STAGE_REDUCE, st);
+    return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
+  }
+  {
+    StageTimer tm(GDFT_STAGE_VXC, st);
+    rc = check_cuda(launch_vxc_tc(mol_am(mol), coef, mol->n_grid_pad, (int)round_up(mol->n_ao, 128), mol->n_ao,
+                                  W.n_vsplit, W.vrange, vpart, (int *)(ws + W.off_err), st),
+                    "vxc_tc");
+    if (rc) return rc;
+  }
+  StageTimer tm(GDFT_STAGE_REDUCE, st);
+  return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
+}
+
 extern "C" {
 
 int gdft_abi_version(void) { return GDFT_ABI_VERSION; }
@@ -391,26 +417,29 @@ int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, con
     if ((rc = check_cuda(launch_energy_reduce(epart, W.n_eblocks, d_exc, st), "energy_reduce"))) return rc;
   }
   if (d_vxc == nullptr) return GDFT_OK;
-  double *vpart = (double *)(ws + W.off_vpart);
-  if (mol->precision == GDFT_FP64) {
-    {
-      StageTimer tm(GDFT_STAGE_VXC, st);
-      rc = check_cuda(launch_vxc_f64(mol_tab(mol), mol->n_grid_pad, mol->ld, mol->n_ao, coef, W.n_vsplit, vpart, st),
-                      "vxc_f64");
-      if (rc) return rc;
-    }
-    StageTimer tm(GDFT_STAGE_REDUCE, st);
-    return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
+  return run_vxc(mol, coef, d_vxc, ws, st);
+}
+
+
+int gdft_vxc_from_potentials(const gdft_molecule *mol, const double *d_pot, double *d_vxc, void *d_ws,
+                             size_t ws_bytes, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_ws(mol, d_ws, ws_bytes))) return rc;
+  if (d_pot == nullptr || d_vxc == nullptr) {
+    set_error("gdft_vxc_from_potentials: potentials and vxc are required");
+    return GDFT_ERR_INVALID;
   }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  const WsLayout W = ws_layout(mol);
+  double *coef = (double *)(ws + W.off_coef);
   {
-    StageTimer tm(GDFT_STAGE_VXC, st);
-    rc = check_cuda(launch_vxc_tc(mol_am(mol), coef, mol->n_grid_pad, (int)round_up(mol->n_ao, 128), mol->n_ao,
-                                  W.n_vsplit, W.vrange, vpart, (int *)(ws + W.off_err), st),
-                    "vxc_tc");
-    if (rc) return rc;
+    StageTimer tm(GDFT_STAGE_REDUCE, st);
+    if ((rc = check_cuda(launch_pad_potentials(d_pot, mol->n_grid, mol->n_grid_pad, coef, st), "pad_potentials")))
+      return rc;
   }
-  StageTimer tm(GDFT_STAGE_REDUCE, st);
-  return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
+  return run_vxc(mol, coef, d_vxc, ws, st);
 }
 
 int gdft_device_status(const gdft_molecule *mol, void *d_ws, size_t ws_bytes, int32_t *status, void *stream) {

@@ -8,7 +8,7 @@
 // against the AO planes exactly as the FP64 form (dens_f64.cu) does:
 //   t = phi : rho, grad rho (x2), and the phi*lap part of the Laplacian
 //   t = d_j : the d_j phi . d_j phi part of the Laplacian and tau.
-// Per-job partial sums are FP32 (128 columns), summed across jobs in FP64.
+// Row reductions use FP32 FMA chains of 8 products summed in FP64.
 //
 // Warp roles (192 threads): warp 0 = TMA producer (one thread issues bulk
 // copies of pre-tiled 32 KB operand images), warp 1 = TMEM owner and MMA
@@ -190,65 +190,39 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
         break;
       }
       umma::tc_fence_after();
-      float acc[2][5];
-#pragma unroll
-      for (int sp = 0; sp < 2; ++sp)
-#pragma unroll
-        for (int k = 0; k < 5; ++k) acc[sp][k] = 0.0f;
+      // Row reductions: FP32 FMA chains of 8 products, summed in FP64.
       for (int c0 = 0; c0 < 128; c0 += 32) {
         float x0[32], x1[32], pv[32];
         umma::tmem_ld32(tl + buf * 256 + c0, x0);
         umma::tmem_ld32(tl + buf * 256 + 128 + c0, x1);
         const int kc = cb * 4 + c0 / 32;
-        if (t == 0) {
+        const int k_lo = t == 0 ? 0 : t, k_hi = t == 0 ? kPlanes : t + 1;
 #pragma unroll 1
-          for (int k = 0; k < kPlanes; ++k) {
-            load_row32(pm_blk(A, tile, k, kc), row, pv);
-            float a0 = 0.0f, a1 = 0.0f;
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-              a0 = fmaf(x0[i], pv[i], a0);
-              a1 = fmaf(x1[i], pv[i], a1);
-            }
-            acc[0][k] += a0;
-            acc[1][k] += a1;
-          }
-        } else {
-          load_row32(pm_blk(A, tile, t, kc), row, pv);
-          float a0 = 0.0f, a1 = 0.0f;
+        for (int k = k_lo; k < k_hi; ++k) {
+          load_row32(pm_blk(A, tile, k, kc), row, pv);
+          float a0[4] = {0.0f, 0.0f, 0.0f, 0.0f}, a1[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
           for (int i = 0; i < 32; ++i) {
-            a0 = fmaf(x0[i], pv[i], a0);
-            a1 = fmaf(x1[i], pv[i], a1);
+            a0[i & 3] = fmaf(x0[i], pv[i], a0[i & 3]);
+            a1[i & 3] = fmaf(x1[i], pv[i], a1[i & 3]);
           }
-          acc[0][0] += a0;
-          acc[1][0] += a1;
+          const int slot = t == 0 ? k : 5;
+          F[0][slot] += ((double)a0[0] + (double)a0[1]) + ((double)a0[2] + (double)a0[3]);
+          F[1][slot] += ((double)a1[0] + (double)a1[1]) + ((double)a1[2] + (double)a1[3]);
         }
       }
       umma::tc_fence_before();
       umma::mbar_arrive(&tempty[buf]);
-#pragma unroll
-      for (int sp = 0; sp < 2; ++sp) {
-        if (t == 0) {
-          F[sp][0] += acc[sp][T_PHI];  // rho
-          F[sp][1] += acc[sp][T_DX];
-          F[sp][2] += acc[sp][T_DY];
-          F[sp][3] += acc[sp][T_DZ];
-          F[sp][4] += acc[sp][T_LAP];  // phi . lap phi part
-        } else {
-          F[sp][5] += acc[sp][0];  // sum_j d_j phi . d_j phi part
-        }
-      }
     }
     const int64_t p = tile * 128 + row;
 #pragma unroll
     for (int sp = 0; sp < 2; ++sp) {
       double *fs = A.feat + (size_t)sp * kFeat * A.np;
-      fs[F_RHO * A.np + p] = F[sp][0];
-      fs[F_GX * A.np + p] = 2.0 * F[sp][1];
-      fs[F_GY * A.np + p] = 2.0 * F[sp][2];
-      fs[F_GZ * A.np + p] = 2.0 * F[sp][3];
-      fs[F_LAP * A.np + p] = 2.0 * F[sp][5] + 2.0 * F[sp][4];
+      fs[F_RHO * A.np + p] = F[sp][T_PHI];
+      fs[F_GX * A.np + p] = 2.0 * F[sp][T_DX];
+      fs[F_GY * A.np + p] = 2.0 * F[sp][T_DY];
+      fs[F_GZ * A.np + p] = 2.0 * F[sp][T_DZ];
+      fs[F_LAP * A.np + p] = 2.0 * F[sp][5] + 2.0 * F[sp][T_LAP];
       fs[F_TAU * A.np + p] = 0.5 * F[sp][5];
     }
   }

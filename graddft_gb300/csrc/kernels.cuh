@@ -40,6 +40,7 @@ cudaError_t launch_xc_point(const double *feat, const double *w, int64_t n_grid,
 
 // reduce.cu
 int integrate_blocks(int64_t n_grid);
+cudaError_t launch_pad_potentials(const double *pot, int64_t n_grid, int64_t np, double *coef, cudaStream_t st);
 cudaError_t launch_integrate(int64_t n_grid, int n_cols, const gdft_functional &fn, const double *dens,
                              const double *w, double *epart, cudaStream_t st);
 cudaError_t launch_energy_reduce(const double *epart, int n, double *exc, cudaStream_t st);

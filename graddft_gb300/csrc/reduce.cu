@@ -134,7 +134,21 @@ __global__ void integrate_kernel(int64_t n_grid, int n_cols, gdft_functional fn,
   }
 }
 
+// (2, 6, n_grid) -> [2][6][np] (padded points get zero potentials).
+__global__ void pad_potentials_kernel(const double *__restrict__ pot, int64_t n_grid, int64_t np,
+                                      double *__restrict__ coef) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+#pragma unroll
+  for (int k = 0; k < 2 * kFeat; ++k) coef[(size_t)k * np + p] = p < n_grid ? pot[(size_t)k * n_grid + p] : 0.0;
+}
+
 }  // namespace
+
+cudaError_t launch_pad_potentials(const double *pot, int64_t n_grid, int64_t np, double *coef, cudaStream_t st) {
+  pad_potentials_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(pot, n_grid, np, coef);
+  return cudaGetLastError();
+}
 
 int integrate_blocks(int64_t n_grid) { return (int)((n_grid + 255) / 256); }
 

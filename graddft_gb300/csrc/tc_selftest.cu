@@ -76,19 +76,12 @@ __global__ void __launch_bounds__(128) umma_selftest_kernel(const float *__restr
 
 using namespace gdft;
 
-extern "C" int gdft_selftest_umma(double *max_abs_err) {
-  if (max_abs_err == nullptr) {
-    set_error("gdft_selftest_umma: null output");
-    return GDFT_ERR_INVALID;
-  }
+// D (128 x 128) = A (128 x 32) B (128 x 32)^T on the tensor cores for caller
+// data (host arrays, row-major, values taken as TF32); used to characterise
+// the accumulation rounding of kind::tf32 against exact products.
+static int run_umma_128x128x32(const float *ha, const float *hb, float *hd) {
   const int M = 128, N = 128, K = 32;
-  float *ha = (float *)malloc(sizeof(float) * M * K), *hb = (float *)malloc(sizeof(float) * N * K);
   float *hpa = (float *)calloc(umma::kBlockBytes / 4, 4), *hpb = (float *)calloc(umma::kBlockBytes / 4, 4);
-  float *hd = (float *)malloc(sizeof(float) * M * N);
-  for (int i = 0; i < M; ++i)
-    for (int k = 0; k < K; ++k) ha[i * K + k] = (float)(((i * 7 + k * 3) % 11) - 5);
-  for (int j = 0; j < N; ++j)
-    for (int k = 0; k < K; ++k) hb[j * K + k] = (float)(((j * 5 + k * 13) % 9) - 4);
   for (int i = 0; i < M; ++i)
     for (int k = 0; k < K; ++k) hpa[umma::kblock_off(i, k) / 4] = ha[i * K + k];
   for (int j = 0; j < N; ++j)
@@ -115,11 +108,42 @@ extern "C" int gdft_selftest_umma(double *max_abs_err) {
   if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(hd, dd, sizeof(float) * M * N, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) {
-    rc = check_cuda(e, "selftest_umma");
+    rc = check_cuda(e, "umma 128x128x32");
   } else if (herr != 0) {
-    set_error("selftest_umma: bounded wait expired (stage %d)", herr);
+    set_error("umma 128x128x32: bounded wait expired (stage %d)", herr);
     rc = GDFT_ERR_DEVICE;
-  } else {
+  }
+  cudaFree(da);
+  cudaFree(db);
+  cudaFree(dd);
+  cudaFree(derr);
+  free(hpa);
+  free(hpb);
+  return rc;
+}
+
+extern "C" int gdft_umma_probe(const float *h_a, const float *h_b, float *h_d) {
+  if (h_a == nullptr || h_b == nullptr || h_d == nullptr) {
+    set_error("gdft_umma_probe: null argument");
+    return GDFT_ERR_INVALID;
+  }
+  return run_umma_128x128x32(h_a, h_b, h_d);
+}
+
+extern "C" int gdft_selftest_umma(double *max_abs_err) {
+  if (max_abs_err == nullptr) {
+    set_error("gdft_selftest_umma: null output");
+    return GDFT_ERR_INVALID;
+  }
+  const int M = 128, N = 128, K = 32;
+  float *ha = (float *)malloc(sizeof(float) * M * K), *hb = (float *)malloc(sizeof(float) * N * K);
+  float *hd = (float *)malloc(sizeof(float) * M * N);
+  for (int i = 0; i < M; ++i)
+    for (int k = 0; k < K; ++k) ha[i * K + k] = (float)(((i * 7 + k * 3) % 11) - 5);
+  for (int j = 0; j < N; ++j)
+    for (int k = 0; k < K; ++k) hb[j * K + k] = (float)(((j * 5 + k * 13) % 9) - 4);
+  const int rc = run_umma_128x128x32(ha, hb, hd);
+  if (rc == GDFT_OK) {
     double mx = 0.0;
     for (int i = 0; i < M; ++i)
       for (int j = 0; j < N; ++j) {
@@ -129,14 +153,8 @@ extern "C" int gdft_selftest_umma(double *max_abs_err) {
       }
     *max_abs_err = mx;
   }
-  cudaFree(da);
-  cudaFree(db);
-  cudaFree(dd);
-  cudaFree(derr);
   free(ha);
   free(hb);
-  free(hpa);
-  free(hpb);
   free(hd);
   return rc;
 }

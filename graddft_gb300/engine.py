@@ -138,6 +138,16 @@ class Resident:
                                                    self.ws.numel(), _stream(self.device)))
         return exc, vxc
 
+    def vxc_from_potentials(self, pot, vxc_out=None):
+        """V_s = sum_r [c0 phi phi + sum_j c_j phi d_j phi + c4 phi lap phi + c5 sum_j d_j phi d_j phi], pot (2, 6, grid)."""
+        pot = as_device_f64(pot, self.device)
+        if pot.shape != (2, 6, self.n_grid):
+            raise ValueError(f"potentials must be (2, 6, {self.n_grid}), got {tuple(pot.shape)}")
+        vxc = vxc_out if vxc_out is not None else torch.empty((2, self.n_ao, self.n_ao), dtype=F64, device=self.device)
+        check(_lib.load().gdft_vxc_from_potentials(ctypes.byref(self.desc), _ptr(pot), _ptr(vxc), _ptr(self.ws),
+                                                   self.ws.numel(), _stream(self.device)))
+        return vxc
+
     def status(self) -> int:
         """Synchronise and raise if a kernel recorded an expired bounded wait since the last query."""
         st = ctypes.c_int32()

@@ -133,6 +133,14 @@ int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, con
                              const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc,
                              void *d_ws, size_t ws_bytes, void *stream);
 
+/* The transposed density contraction on given per-point potentials (the part
+ * of jax.grad at train.py:86 downstream of the pointwise functional):
+ *   V_s[a][b] = sum_r  c[s][0] phi_a phi_b + sum_j c[s][1+j] phi_a d_j phi_b
+ *                    + c[s][4] phi_a lap phi_b + c[s][5] sum_j d_j phi_a d_j phi_b
+ * d_pot: (2, 6, grid) FP64; d_vxc: (2, ao, ao). */
+int gdft_vxc_from_potentials(const gdft_molecule *mol, const double *d_pot, double *d_vxc, void *d_ws,
+                             size_t ws_bytes, void *stream);
+
 /* The functional's energy-density columns before clipping (the stacked output of
  * the energy_densities plugin, e.g. b88_density popular_functionals.py:277-284,
  * b3lyp_exhf_densities :306-326 plus the combine step :328-334).
@@ -176,6 +184,12 @@ int gdft_device_status(const gdft_molecule *mol, void *d_ws, size_t ws_bytes, in
  * *max_abs_err is 0 on a correct device path.  Synchronous; allocates its own
  * small buffers.  No counterpart in the reference. */
 int gdft_selftest_umma(double *max_abs_err);
+
+/* D (128 x 128) = A (128 x 32) B (128 x 32)^T (host arrays, row-major, FP32
+ * containers read as TF32) through the same tensor-core path, for
+ * characterising its accumulation rounding.  Synchronous.  No counterpart in
+ * the reference. */
+int gdft_umma_probe(const float *h_a, const float *h_b, float *h_d);
 
 /* Stage timing (observability; no counterpart in the reference, whose only
  * tracing is jax.profiler.annotate_function at train.py:123).  When enabled,
