@@ -67,16 +67,19 @@ MolLayout mol_layout(int64_t n_grid, int n_ao, int precision) {
   size_t off = 0;
   L.off_w = off;
   off = align256(off + (size_t)L.np * sizeof(double));
-  L.off_tab = L.off_pm = L.off_am = off;
+  L.off_tab = L.off_pm = L.off_am = L.off_af = off;
   if (precision == GDFT_FP64) {
     off = align256(off + (size_t)kPlanes * L.plane_elems() * sizeof(double));
   } else {
-    // hi/lo TF32 pairs of the five planes in the point-major and AO-major tiles.
-    const size_t tables = (size_t)kPlanes * L.np * L.ldk * 2 * sizeof(float);
+    // Point-major hi/lo of the five planes, AO-major hi/lo of four planes and
+    // AO-major FP32 of the five planes.
+    const size_t plane = (size_t)L.np * L.ldk * sizeof(float);
     L.off_pm = off;
-    off = align256(off + tables);
+    off = align256(off + kPlanes * 2 * plane);
     L.off_am = off;
-    off = align256(off + tables);
+    off = align256(off + 4 * 2 * plane);
+    L.off_af = off;
+    off = align256(off + kPlanes * plane);
   }
   L.bytes = off;
   return L;
@@ -184,6 +187,9 @@ static const float *mol_pm(const gdft_molecule *m) {
 static const float *mol_am(const gdft_molecule *m) {
   return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_am);
 }
+static const float *mol_af(const gdft_molecule *m) {
+  return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_af);
+}
 
 // Density stage into ws.feat.
 static int run_density(const gdft_molecule *m, const double *rdm1, char *ws, cudaStream_t st) {
@@ -226,7 +232,7 @@ static int run_vxc(const gdft_molecule *mol, const double *coef, double *d_vxc, 
   }
   {
     StageTimer tm(GDFT_STAGE_VXC, st);
-    rc = check_cuda(launch_vxc_tc(mol_am(mol), coef, mol->n_grid_pad, (int)round_up(mol->n_ao, 128), mol->n_ao,
+    rc = check_cuda(launch_vxc_tc(mol_am(mol), mol_af(mol), coef, mol->n_grid_pad, (int)round_up(mol->n_ao, 128), mol->n_ao,
                                   W.n_vsplit, W.vrange, vpart, (int *)(ws + W.off_err), st),
                     "vxc_tc");
     if (rc) return rc;
@@ -329,7 +335,8 @@ int gdft_molecule_load(const gdft_molecule *mol, const double *d_ao, const doubl
   if (mol->precision == GDFT_TF32X3)
     return check_cuda(launch_pack_tables(d_ao, d_grad_ao, d_grad2_ao, nullptr, nullptr, d_weights, mol->n_grid,
                                          mol->n_ao, L.np, L.ldk, (float *)((char *)mol->buffer + L.off_pm),
-                                         (float *)((char *)mol->buffer + L.off_am), w, (cudaStream_t)stream),
+                                         (float *)((char *)mol->buffer + L.off_am),
+                                         (float *)((char *)mol->buffer + L.off_af), w, (cudaStream_t)stream),
                       "pack_tables");
   return check_cuda(launch_load_tables(d_ao, d_grad_ao, d_grad2_ao, d_weights, mol->n_grid, mol->n_ao, L.np, L.ld,
                                        tab, w, (cudaStream_t)stream),
@@ -351,7 +358,8 @@ int gdft_molecule_eval_basis(const gdft_molecule *mol, const double *d_basis, co
   if (mol->precision == GDFT_TF32X3)
     return check_cuda(launch_pack_tables(nullptr, nullptr, nullptr, d_basis, d_coords, d_weights, mol->n_grid,
                                          mol->n_ao, L.np, L.ldk, (float *)((char *)mol->buffer + L.off_pm),
-                                         (float *)((char *)mol->buffer + L.off_am), w, (cudaStream_t)stream),
+                                         (float *)((char *)mol->buffer + L.off_am),
+                                         (float *)((char *)mol->buffer + L.off_af), w, (cudaStream_t)stream),
                       "pack_tables");
   return check_cuda(launch_eval_basis(d_basis, d_coords, d_weights, mol->n_grid, mol->n_ao, L.np, L.ld, tab, w,
                                       (cudaStream_t)stream),

@@ -10,13 +10,19 @@
 //   t = d_j : the d_j phi . d_j phi part of the Laplacian and tau.
 // Row reductions use FP32 FMA chains of 8 products summed in FP64.
 //
+// Accumulation: the tensor cores truncate every MMA's products to the
+// accumulator's ulp grid, so long FP32 accumulation chains drift towards
+// zero.  Each job's K range is therefore split into sub-jobs of kSubK
+// (24 MMAs per accumulator); a sub-job accumulates in TMEM region W and the
+// epilogue folds W into a second TMEM region S with round-to-nearest FP32
+// adds on the CUDA cores, then reduces S against the AO planes.
+//
 // Warp roles (192 threads): warp 0 = TMA producer (one thread issues bulk
 // copies of pre-tiled 32 KB operand images), warp 1 = TMEM owner and MMA
 // issuer (one thread), warps 2-5 = epilogue (TMEM lane quadrant = warp % 4).
-// Two 96 KB smem stages; two TMEM accumulator buffers of 2 x 128 columns so
-// the epilogue of one job overlaps the MMAs of the next.  Every wait is
-// bounded (umma::mbar_wait); on expiry the CTA records an error word, waits
-// for its own copies and MMAs to land and releases TMEM.
+// Two 96 KB smem stages.  Every wait is bounded (umma::mbar_wait); on expiry
+// the CTA records an error word, waits for its own copies and MMAs to land
+// and releases TMEM.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "umma.cuh"
@@ -28,7 +34,8 @@ namespace {
 constexpr int kStages = 2;
 constexpr uint32_t kStageBytes = 6 * umma::kBlockBytes;  // A hi|lo, B_a hi|lo, B_b hi|lo
 constexpr int kThreads = 192;
-constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kTmemCols = 512;  // W: columns [0, 256), S: [256, 512)
+constexpr int kSubK = 64;             // K extent of one accumulation chain
 constexpr int kSmemBytes = kStages * kStageBytes + 1024;
 
 struct DensArgs {
@@ -65,23 +72,22 @@ __device__ __forceinline__ void load_row32(const float *blk, int row, float (&v)
 __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], drain;
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], wfull, wempty, drain;
   __shared__ uint32_t tmem_base;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t tile = blockIdx.x;
   const int nkc = A.ldk / 32, ncb = A.ldk / 128;
   const int njobs = 4 * ncb;
+  const int nkq = A.ldk / kSubK, kc_per_sub = kSubK / 32;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       umma::mbar_init(&full[s], 1);
       umma::mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
-      umma::mbar_init(&tfull[b], 1);
-      umma::mbar_init(&tempty[b], 128);
-    }
+    umma::mbar_init(&wfull, 1);
+    umma::mbar_init(&wempty, 128);
     umma::mbar_init(&drain, 1);
     umma::fence_barrier_init();
   }
@@ -125,48 +131,51 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
     const uint32_t idesc = umma::idesc_tf32(128, 128);
-    uint32_t it = 0;
+    uint32_t it = 0, sub = 0;
     bool ok = true;
     for (int j = 0; j < njobs && ok; ++j) {
-      const int buf = j & 1;
-      if (!umma::warp_wait(&tempty[buf], ((j >> 1) & 1) ^ 1)) {
-        if (lane == 0) flag(A.err, 13);
-        break;
-      }
-      umma::tc_fence_after();
-      for (int kc = 0; kc < nkc; ++kc) {
-        const int s = it % kStages;
-        if (!umma::warp_wait(&full[s], (it / kStages) & 1)) {
-          if (lane == 0) flag(A.err, 14);
+      for (int kq = 0; kq < nkq && ok; ++kq, ++sub) {
+        if (!umma::warp_wait(&wempty, (sub & 1) ^ 1)) {
+          if (lane == 0) flag(A.err, 13);
           ok = false;
           break;
         }
         umma::tc_fence_after();
-        if (lane == 0) {
-          const uint32_t sb = umma::smem_u32(smem + s * kStageBytes);
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const uint64_t ahi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-            const uint64_t alo = umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-#pragma unroll
-            for (int sp = 0; sp < 2; ++sp) {
-              const uint32_t bb = sb + (2 + 2 * sp) * umma::kBlockBytes + kk * 256;
-              const uint64_t bhi = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
-              const uint64_t blo = umma::sdesc(bb + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
-              const uint32_t d = tbase + buf * 256 + sp * 128;
-              umma::mma_tf32(d, ahi, bhi, idesc, (kc > 0 || kk > 0) ? 1u : 0u);
-              umma::mma_tf32(d, ahi, blo, idesc, 1u);
-              umma::mma_tf32(d, alo, bhi, idesc, 1u);
-            }
+        for (int kc = kq * kc_per_sub; kc < (kq + 1) * kc_per_sub; ++kc) {
+          const int s = it % kStages;
+          if (!umma::warp_wait(&full[s], (it / kStages) & 1)) {
+            if (lane == 0) flag(A.err, 14);
+            ok = false;
+            break;
           }
-          umma::mma_commit(&empty[s]);
+          umma::tc_fence_after();
+          if (lane == 0) {
+            const uint32_t sb = umma::smem_u32(smem + s * kStageBytes);
+            const bool first = kc == kq * kc_per_sub;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t ahi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+              const uint64_t alo = umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+#pragma unroll
+              for (int sp = 0; sp < 2; ++sp) {
+                const uint32_t bb = sb + (2 + 2 * sp) * umma::kBlockBytes + kk * 256;
+                const uint64_t bhi = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
+                const uint64_t blo = umma::sdesc(bb + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
+                const uint32_t d = tbase + sp * 128;
+                umma::mma_tf32(d, ahi, bhi, idesc, (first && kk == 0) ? 0u : 1u);
+                umma::mma_tf32(d, ahi, blo, idesc, 1u);
+                umma::mma_tf32(d, alo, bhi, idesc, 1u);
+              }
+            }
+            umma::mma_commit(&empty[s]);
+          }
+          __syncwarp();
+          ++it;
         }
+        if (!ok) break;
+        if (lane == 0) umma::mma_commit(&wfull);
         __syncwarp();
-        ++it;
       }
-      if (!ok) break;
-      if (lane == 0) umma::mma_commit(&tfull[buf]);
-      __syncwarp();
     }
     // All issued MMAs complete before TMEM is released.
     if (lane == 0) umma::mma_commit(&drain);
@@ -182,19 +191,40 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
     for (int sp = 0; sp < 2; ++sp)
 #pragma unroll
       for (int k = 0; k < 6; ++k) F[sp][k] = 0.0;
-    for (int j = 0; j < njobs; ++j) {
-      const int buf = j & 1;
+    uint32_t sub = 0;
+    bool ok = true;
+    for (int j = 0; j < njobs && ok; ++j) {
       const int t = j / ncb, cb = j % ncb;
-      if (!umma::warp_wait(&tfull[buf], (j >> 1) & 1)) {
-        if (lane == 0) flag(A.err, 16);
-        break;
+      for (int kq = 0; kq < nkq; ++kq, ++sub) {
+        if (!umma::warp_wait(&wfull, sub & 1)) {
+          if (lane == 0) flag(A.err, 16);
+          ok = false;
+          break;
+        }
+        umma::tc_fence_after();
+        // S (+)= W, 32 columns at a time (round-to-nearest FP32 adds).
+#pragma unroll 1
+        for (int c = 0; c < 256; c += 32) {
+          float w[32];
+          umma::tmem_ld32(tl + c, w);
+          if (kq > 0) {
+            float sv[32];
+            umma::tmem_ld32(tl + 256 + c, sv);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) w[i] += sv[i];
+          }
+          umma::tmem_st32(tl + 256 + c, w);
+        }
+        umma::tmem_st_wait();
+        umma::tc_fence_before();
+        umma::mbar_arrive(&wempty);
       }
-      umma::tc_fence_after();
-      // Row reductions: FP32 FMA chains of 8 products, summed in FP64.
+      if (!ok) break;
+      // Row reductions of S: FP32 FMA chains of 8 products, summed in FP64.
       for (int c0 = 0; c0 < 128; c0 += 32) {
         float x0[32], x1[32], pv[32];
-        umma::tmem_ld32(tl + buf * 256 + c0, x0);
-        umma::tmem_ld32(tl + buf * 256 + 128 + c0, x1);
+        umma::tmem_ld32(tl + 256 + c0, x0);
+        umma::tmem_ld32(tl + 256 + 128 + c0, x1);
         const int kc = cb * 4 + c0 / 32;
         const int k_lo = t == 0 ? 0 : t, k_hi = t == 0 ? kPlanes : t + 1;
 #pragma unroll 1
@@ -211,8 +241,6 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
           F[1][slot] += ((double)a1[0] + (double)a1[1]) + ((double)a1[2] + (double)a1[3]);
         }
       }
-      umma::tc_fence_before();
-      umma::mbar_arrive(&tempty[buf]);
     }
     const int64_t p = tile * 128 + row;
 #pragma unroll

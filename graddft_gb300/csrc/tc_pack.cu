@@ -7,8 +7,10 @@
 // operand stage is one contiguous bulk copy:
 //   point-major  [point tile (128)][plane][AO chunk (32)][hi|lo] : 128 points x 32 AO
 //     (A operand of the density contraction and its epilogue partners)
-//   AO-major     [AO tile (128)][plane][point chunk (32)][hi|lo] : 128 AO x 32 points
-//     (operands of the V_xc contraction, contracted over points)
+//   AO-major     [AO tile (128)][plane 0-3][point chunk (32)][hi|lo] : 128 AO x 32 points
+//     (A operand of the V_xc contraction, contracted over points)
+//   AO-major FP32 [AO tile (128)][plane][point chunk (32)] : the same blocks as single
+//     FP32 values (inputs of the B operand that is built per stage)
 // The density matrix is packed per call as the B operand of the density
 // contraction: [spin][column tile (128)][k chunk (32)][hi|lo], element (c, k) = D[k][c].
 #include "common.cuh"
@@ -23,7 +25,10 @@ __device__ __forceinline__ size_t pm_block(int64_t tile, int plane, int kc, int 
   return ((size_t)(tile * kPlanes + plane) * nkc + kc) * 2;  // in units of 16 KB blocks (hi; lo = +1)
 }
 __device__ __forceinline__ size_t am_block(int atile, int plane, int64_t pc, int64_t npc) {
-  return ((size_t)(atile * kPlanes + plane) * npc + pc) * 2;
+  return ((size_t)(atile * 4 + plane) * npc + pc) * 2;
+}
+__device__ __forceinline__ size_t af_block(int atile, int plane, int64_t pc, int64_t npc) {
+  return (size_t)(atile * kPlanes + plane) * npc + pc;
 }
 
 __device__ __forceinline__ void store_split(float *base, size_t blk, uint32_t off, double v) {
@@ -42,7 +47,7 @@ __global__ void pack_tables_kernel(const double *__restrict__ ao, const double *
                                    const double *__restrict__ grad2_ao, const double *__restrict__ basis,
                                    const double *__restrict__ coords, const double *__restrict__ w, int64_t n_grid,
                                    int n_ao, int64_t np, int ldk, float *__restrict__ pm, float *__restrict__ am,
-                                   double *__restrict__ wout) {
+                                   float *__restrict__ af, double *__restrict__ wout) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)np * ldk) return;
   const int64_t p = (int64_t)(idx / ldk);
@@ -107,7 +112,9 @@ __global__ void pack_tables_kernel(const double *__restrict__ ao, const double *
 #pragma unroll
   for (int t = 0; t < kPlanes; ++t) {
     store_split(pm, pm_block(tile, t, a / 32, nkc), umma::kblock_off((int)(p % 128), a % 32), v[t]);
-    store_split(am, am_block(a / 128, t, p / 32, npc), umma::kblock_off(a % 128, (int)(p % 32)), v[t]);
+    if (t < 4) store_split(am, am_block(a / 128, t, p / 32, npc), umma::kblock_off(a % 128, (int)(p % 32)), v[t]);
+    af[af_block(a / 128, t, p / 32, npc) * (umma::kBlockBytes / 4) + umma::kblock_off(a % 128, (int)(p % 32)) / 4] =
+        (float)v[t];
   }
   if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
 }
@@ -130,15 +137,15 @@ __global__ void pack_rdm1_kernel(const double *__restrict__ D, int n, int ldk, f
 
 cudaError_t launch_pack_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *basis,
                                const double *coords, const double *w, int64_t n_grid, int n_ao, int64_t np, int ldk,
-                               float *pm, float *am, double *wout, cudaStream_t st) {
+                               float *pm, float *am, float *af, double *wout, cudaStream_t st) {
   const size_t total = (size_t)np * ldk;
   const unsigned blocks = (unsigned)((total + 255) / 256);
   if (basis != nullptr)
     pack_tables_kernel<true><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
-                                                     pm, am, wout);
+                                                     pm, am, af, wout);
   else
     pack_tables_kernel<false><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
-                                                      pm, am, wout);
+                                                      pm, am, af, wout);
   return cudaGetLastError();
 }
 
