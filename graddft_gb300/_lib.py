@@ -31,7 +31,7 @@ MAX_COLS = 8
 EXPORTS = (
     "gdft_abi_version", "gdft_last_error", "gdft_molecule_bytes", "gdft_molecule_init", "gdft_molecule_load",
     "gdft_molecule_eval_basis", "gdft_workspace_bytes", "gdft_density", "gdft_xc_energy_and_grads",
-    "gdft_energy_densities", "gdft_vxc_from_potentials", "gdft_integrate", "gdft_integrate_workspace_bytes", "gdft_fock", "gdft_coulomb",
+    "gdft_energy_densities", "gdft_vxc_from_potentials", "gdft_integrate", "gdft_integrate_workspace_bytes", "gdft_integrate_noalloc", "gdft_fock", "gdft_coulomb",
     "gdft_profile_enable", "gdft_profile_reset", "gdft_profile_read", "gdft_device_status", "gdft_selftest_umma",
     "gdft_umma_probe",
 )
@@ -83,6 +83,7 @@ _SIGS = {
     "gdft_vxc_from_potentials": ([PMOL, P, P, P, SZ, P], ctypes.c_int),
     "gdft_integrate": ([I64, I32, P, I32, P, P, D, P, P, SZ, P], ctypes.c_int),
     "gdft_integrate_workspace_bytes": ([I64, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_integrate_noalloc": ([I64, I32, P, I32, P, P, D, P, P], ctypes.c_int),
     "gdft_fock": ([I32, P, P, P, D, P, P], ctypes.c_int),
     "gdft_coulomb": ([I32, P, P, P, D, P, P, P], ctypes.c_int),
     "gdft_device_status": ([PMOL, P, SZ, ctypes.POINTER(I32), P], ctypes.c_int),

@@ -159,6 +159,19 @@ int gdft_integrate(int64_t n_grid, int32_t n_cols, const double *h_coeffs, int32
 /* Workspace bytes of gdft_integrate. */
 int gdft_integrate_workspace_bytes(int64_t n_grid, size_t *bytes);
 
+/* gdft_integrate without a workspace, for callers that cannot allocate device
+ * memory when they need the energy (e.g. a JAX/XLA custom-call handler, which
+ * must not allocate outside XLA's allocator, or a service whose device memory
+ * is fully reserved at start-up).  No counterpart in the reference.
+ * Its scratch is a fixed array in the library's device image (1 MiB, held by
+ * every GPU that loads the library until exit), so n_grid is limited to
+ * 33,554,432 points; larger grids are rejected with GDFT_ERR_INVALID.  The
+ * first call on a device looks up the array's device address (make it before
+ * any stream capture).  Calls share the array: calls that overlap on the GPU
+ * race.  Allocates nothing. */
+int gdft_integrate_noalloc(int64_t n_grid, int32_t n_cols, const double *h_coeffs, int32_t n_coeffs,
+                           const double *d_dens, const double *d_weights, double clip, double *d_exc, void *stream);
+
 /* Fock assembly of predict (train.py:147-163):
  * F = abs_clip(1/2 (G + G^T)) with G = abs_clip(h1e + J + V_xc), both spins.
  * d_h1e (ao, ao), d_vj (ao, ao) Coulomb potential, d_vxc (2, ao, ao) -> d_fock (2, ao, ao). */
