@@ -18,10 +18,10 @@
 // TMEM, with round-to-nearest FP32 adds on the CUDA cores, then reduces S
 // against the AO planes at the end of the job.
 //
-// Warp roles (192 threads): warp 0 = TMA producer (one thread issues bulk
+// Warp roles (320 threads): warp 0 = TMA producer (one thread issues bulk
 // copies of pre-tiled operand images: A 32 KB, the two D halves 4 x 8 KB),
-// warp 1 = TMEM owner and MMA issuer (one thread), warps 2-5 = epilogue
-// (TMEM lane quadrant = warp % 4).  Three 64 KB smem stages.  Every wait is
+// warp 1 = TMEM owner and MMA issuer (one thread), warps 2-9 = epilogue, one
+// per (TMEM lane quadrant = warp % 4, spin).  Three 64 KB smem stages.  Every wait is
 // bounded (umma::mbar_wait); on expiry the CTA records an error word, waits
 // for its own copies and MMAs to land and releases TMEM.
 #include "common.cuh"
@@ -35,7 +35,7 @@ namespace {
 constexpr int kStages = 3;
 constexpr uint32_t kHalf = umma::kBlockBytes / 2;                     // 64 rows x 32 fp32
 constexpr uint32_t kStageBytes = 2 * umma::kBlockBytes + 4 * kHalf;  // A hi|lo, B_a hi|lo, B_b hi|lo
-constexpr int kThreads = 192;
+constexpr int kThreads = 320;
 constexpr uint32_t kTmemCols = 512;  // W0 [0,128), W1 [128,256), S [256,384) (2 spins x 64 columns each)
 constexpr int kSubK = 32;             // K extent of one accumulation chain (one stage)
 constexpr int kBN = 64;               // output columns per job
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
     }
     for (int b = 0; b < 2; ++b) {
       umma::mbar_init(&wfull[b], 1);
-      umma::mbar_init(&wempty[b], 128);
+      umma::mbar_init(&wempty[b], 256);
     }
     umma::mbar_init(&drain, 1);
     umma::fence_barrier_init();
@@ -195,13 +195,12 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
   } else {
     // ------------------------------------------------------------ epilogue
     const int q = warp & 3;
+    const int sp = (warp - 2) >> 2;  // spin handled by this warp
     const int row = q * 32 + lane;
-    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
-    double F[2][6];
+    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16) + sp * kBN;  // this spin's 64 columns
+    double F[6];
 #pragma unroll
-    for (int sp = 0; sp < 2; ++sp)
-#pragma unroll
-      for (int k = 0; k < 6; ++k) F[sp][k] = 0.0;
+    for (int k = 0; k < 6; ++k) F[k] = 0.0;
     uint32_t sub = 0;
     bool ok = true;
     for (int j = 0; j < njobs && ok; ++j) {
@@ -214,10 +213,9 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
           break;
         }
         umma::tc_fence_after();
-        // S (+)= W, 32 columns at a time (round-to-nearest FP32 adds); the
-        // loads of W and S are issued together under one wait.
-#pragma unroll 1
-        for (int c = 0; c < 128; c += 32) {
+        // S (+)= W for this spin's 64 columns (round-to-nearest FP32 adds).
+#pragma unroll
+        for (int c = 0; c < kBN; c += 32) {
           uint32_t w[32], sv[32];
           umma::tmem_ld32_nowait(tl + buf * 128 + c, w);
           if (kq > 0) umma::tmem_ld32_nowait(tl + 256 + c, sv);
@@ -235,37 +233,36 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
       if (!ok) break;
       // Row reductions of S: FP32 FMA chains of 8 products, summed in FP64.
       for (int c0 = 0; c0 < kBN; c0 += 32) {
-        float x0[32], x1[32], pv[32];
-        umma::tmem_ld32(tl + 256 + c0, x0);
-        umma::tmem_ld32(tl + 256 + kBN + c0, x1);
+        float x[32], pv[32];
+        umma::tmem_ld32(tl + 256 + c0, x);
         const int kc = (cb * kBN + c0) / 32;
         const int k_lo = t == 0 ? 0 : t, k_hi = t == 0 ? kPlanes : t + 1;
 #pragma unroll 1
         for (int k = k_lo; k < k_hi; ++k) {
           load_row32(pm_blk(A, tile, k, kc), row, pv);
-          float a0[4] = {0.0f, 0.0f, 0.0f, 0.0f}, a1[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+          float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            a0[i & 3] = fmaf(x0[i], pv[i], a0[i & 3]);
-            a1[i & 3] = fmaf(x1[i], pv[i], a1[i & 3]);
+          for (int i = 0; i < 32; ++i) a[i & 3] = fmaf(x[i], pv[i], a[i & 3]);
+          const double d = ((double)a[0] + (double)a[1]) + ((double)a[2] + (double)a[3]);
+          switch (t == 0 ? k : 5) {
+            case 0: F[0] += d; break;
+            case 1: F[1] += d; break;
+            case 2: F[2] += d; break;
+            case 3: F[3] += d; break;
+            case 4: F[4] += d; break;
+            default: F[5] += d; break;
           }
-          const int slot = t == 0 ? k : 5;
-          F[0][slot] += ((double)a0[0] + (double)a0[1]) + ((double)a0[2] + (double)a0[3]);
-          F[1][slot] += ((double)a1[0] + (double)a1[1]) + ((double)a1[2] + (double)a1[3]);
         }
       }
     }
     const int64_t p = tile * 128 + row;
-#pragma unroll
-    for (int sp = 0; sp < 2; ++sp) {
-      double *fs = A.feat + (size_t)sp * kFeat * A.np;
-      fs[F_RHO * A.np + p] = F[sp][T_PHI];
-      fs[F_GX * A.np + p] = 2.0 * F[sp][T_DX];
-      fs[F_GY * A.np + p] = 2.0 * F[sp][T_DY];
-      fs[F_GZ * A.np + p] = 2.0 * F[sp][T_DZ];
-      fs[F_LAP * A.np + p] = 2.0 * F[sp][5] + 2.0 * F[sp][T_LAP];
-      fs[F_TAU * A.np + p] = 0.5 * F[sp][5];
-    }
+    double *fs = A.feat + (size_t)sp * kFeat * A.np;
+    fs[F_RHO * A.np + p] = F[T_PHI];
+    fs[F_GX * A.np + p] = 2.0 * F[T_DX];
+    fs[F_GY * A.np + p] = 2.0 * F[T_DY];
+    fs[F_GZ * A.np + p] = 2.0 * F[T_DZ];
+    fs[F_LAP * A.np + p] = 2.0 * F[5] + 2.0 * F[T_LAP];
+    fs[F_TAU * A.np + p] = 0.5 * F[5];
   }
   umma::tc_fence_before();
   __syncthreads();

@@ -200,34 +200,50 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_tc_kernel(const VxcArgs A) {
       }
       unsigned char *qa = smem + s * kStageBytes + 2 * umma::kBlockBytes;
       unsigned char *qb = qa + 2 * kHalfBlock;
-#pragma unroll 1
-      for (int gg = 0; gg < 4; ++gg) {
-        const int g = gq * 4 + gg;
-        const uint32_t src = (uint32_t)((((rsub + row) >> 3) * 8 + g) * 128 + (row & 7) * 16);
-        const uint32_t dst = (uint32_t)(((row >> 3) * 8 + g) * 128 + (row & 7) * 16);
-        const float *cf = scoef + (4 * g) * 12;
-        float4 q0, q1;
-        if (t == 0) {
-          const float4 ph = __ldg((const float4 *)(af_blk(A, btile, T_PHI, pc) + src / 4));
-          const float4 dx = __ldg((const float4 *)(af_blk(A, btile, T_DX, pc) + src / 4));
-          const float4 dy = __ldg((const float4 *)(af_blk(A, btile, T_DY, pc) + src / 4));
-          const float4 dz = __ldg((const float4 *)(af_blk(A, btile, T_DZ, pc) + src / 4));
-          const float4 lp = __ldg((const float4 *)(af_blk(A, btile, T_LAP, pc) + src / 4));
+      // All plane loads of the stage are issued before any use (memory-level parallelism).
+      if (t == 0) {
+        float4 ph[4], dx[4], dy[4], dz[4], lp[4];
+#pragma unroll
+        for (int gg = 0; gg < 4; ++gg) {
+          const int g = gq * 4 + gg;
+          const uint32_t src = (uint32_t)((((rsub + row) >> 3) * 8 + g) * 128 + (row & 7) * 16) / 4;
+          ph[gg] = __ldg((const float4 *)(af_blk(A, btile, T_PHI, pc) + src));
+          dx[gg] = __ldg((const float4 *)(af_blk(A, btile, T_DX, pc) + src));
+          dy[gg] = __ldg((const float4 *)(af_blk(A, btile, T_DY, pc) + src));
+          dz[gg] = __ldg((const float4 *)(af_blk(A, btile, T_DZ, pc) + src));
+          lp[gg] = __ldg((const float4 *)(af_blk(A, btile, T_LAP, pc) + src));
+        }
+#pragma unroll
+        for (int gg = 0; gg < 4; ++gg) {
+          const int g = gq * 4 + gg;
+          const uint32_t dst = (uint32_t)(((row >> 3) * 8 + g) * 128 + (row & 7) * 16);
+          const float *cf = scoef + (4 * g) * 12;
           const float *c0 = cf, *c1 = cf + 12, *c2 = cf + 24, *c3 = cf + 36;
 #define GDFT_Q0(SP, C, F)                                                                                   \
-  (C[SP * 6 + C_RHO] * ph.F + C[SP * 6 + C_GX] * dx.F + C[SP * 6 + C_GY] * dy.F + C[SP * 6 + C_GZ] * dz.F + \
-   C[SP * 6 + C_LAP] * lp.F)
-          q0 = make_float4(GDFT_Q0(0, c0, x), GDFT_Q0(0, c1, y), GDFT_Q0(0, c2, z), GDFT_Q0(0, c3, w));
-          q1 = make_float4(GDFT_Q0(1, c0, x), GDFT_Q0(1, c1, y), GDFT_Q0(1, c2, z), GDFT_Q0(1, c3, w));
+  (C[SP * 6 + C_RHO] * ph[gg].F + C[SP * 6 + C_GX] * dx[gg].F + C[SP * 6 + C_GY] * dy[gg].F +               \
+   C[SP * 6 + C_GZ] * dz[gg].F + C[SP * 6 + C_LAP] * lp[gg].F)
+          st_split(qa, dst, make_float4(GDFT_Q0(0, c0, x), GDFT_Q0(0, c1, y), GDFT_Q0(0, c2, z), GDFT_Q0(0, c3, w)));
+          st_split(qb, dst, make_float4(GDFT_Q0(1, c0, x), GDFT_Q0(1, c1, y), GDFT_Q0(1, c2, z), GDFT_Q0(1, c3, w)));
 #undef GDFT_Q0
-        } else {
-          const float4 dj = __ldg((const float4 *)(af_blk(A, btile, T_PHI + t, pc) + src / 4));
-          q0 = make_float4(cf[C_KIN] * dj.x, cf[12 + C_KIN] * dj.y, cf[24 + C_KIN] * dj.z, cf[36 + C_KIN] * dj.w);
-          q1 = make_float4(cf[6 + C_KIN] * dj.x, cf[18 + C_KIN] * dj.y, cf[30 + C_KIN] * dj.z,
-                           cf[42 + C_KIN] * dj.w);
         }
-        st_split(qa, dst, q0);
-        st_split(qb, dst, q1);
+      } else {
+        float4 dj[4];
+#pragma unroll
+        for (int gg = 0; gg < 4; ++gg) {
+          const int g = gq * 4 + gg;
+          const uint32_t src = (uint32_t)((((rsub + row) >> 3) * 8 + g) * 128 + (row & 7) * 16) / 4;
+          dj[gg] = __ldg((const float4 *)(af_blk(A, btile, T_PHI + t, pc) + src));
+        }
+#pragma unroll
+        for (int gg = 0; gg < 4; ++gg) {
+          const int g = gq * 4 + gg;
+          const uint32_t dst = (uint32_t)(((row >> 3) * 8 + g) * 128 + (row & 7) * 16);
+          const float *cf = scoef + (4 * g) * 12;
+          st_split(qa, dst, make_float4(cf[C_KIN] * dj[gg].x, cf[12 + C_KIN] * dj[gg].y, cf[24 + C_KIN] * dj[gg].z,
+                                        cf[36 + C_KIN] * dj[gg].w));
+          st_split(qb, dst, make_float4(cf[6 + C_KIN] * dj[gg].x, cf[18 + C_KIN] * dj[gg].y,
+                                        cf[30 + C_KIN] * dj[gg].z, cf[42 + C_KIN] * dj[gg].w));
+        }
       }
       umma::fence_proxy_async();
       umma::mbar_arrive(&bfull[s]);
