@@ -33,7 +33,9 @@ EXPORTS = (
     "gdft_molecule_eval_basis", "gdft_workspace_bytes", "gdft_density", "gdft_xc_energy_and_grads",
     "gdft_energy_densities", "gdft_vxc_from_potentials", "gdft_integrate", "gdft_integrate_workspace_bytes", "gdft_integrate_noalloc", "gdft_fock", "gdft_coulomb",
     "gdft_profile_enable", "gdft_profile_reset", "gdft_profile_read", "gdft_device_status", "gdft_selftest_umma",
-    "gdft_umma_probe",
+    "gdft_umma_probe", "gdft_network_param_count", "gdft_neural_workspace_bytes",
+    "gdft_neural_xc_energy_and_grads", "gdft_neural_inputs", "gdft_network_apply_workspace_bytes",
+    "gdft_network_apply",
 )
 STAGE_AO, STAGE_DENSITY, STAGE_POINT, STAGE_VXC, STAGE_REDUCE, STAGE_MLP = range(6)
 
@@ -61,6 +63,21 @@ class GdftMolecule(ctypes.Structure):
     ]
 
 
+class GdftNetwork(ctypes.Structure):
+    _fields_ = [
+        ("n_in", ctypes.c_int32),
+        ("width", ctypes.c_int32),
+        ("n_layers", ctypes.c_int32),
+        ("n_out", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("squash_offset", ctypes.c_double),
+        ("sigmoid_scale", ctypes.c_double),
+        ("ln_eps", ctypes.c_double),
+        ("clip", ctypes.c_double),
+    ]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -68,6 +85,7 @@ P = ctypes.c_void_p
 I32, I64, SZ, D = ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t, ctypes.c_double
 PMOL = ctypes.POINTER(GdftMolecule)
 PFN = ctypes.POINTER(GdftFunctional)
+PNET = ctypes.POINTER(GdftNetwork)
 
 _SIGS = {
     "gdft_abi_version": ([], ctypes.c_int),
@@ -89,6 +107,12 @@ _SIGS = {
     "gdft_device_status": ([PMOL, P, SZ, ctypes.POINTER(I32), P], ctypes.c_int),
     "gdft_selftest_umma": ([ctypes.POINTER(D)], ctypes.c_int),
     "gdft_umma_probe": ([P, P, P], ctypes.c_int),
+    "gdft_network_param_count": ([PNET, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_neural_workspace_bytes": ([PMOL, PNET, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_neural_xc_energy_and_grads": ([PMOL, P, PNET, P, P, P, P, P, P, SZ, P], ctypes.c_int),
+    "gdft_neural_inputs": ([PMOL, P, PNET, P, P, P, P, SZ, P], ctypes.c_int),
+    "gdft_network_apply_workspace_bytes": ([PNET, I64, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_network_apply": ([PNET, P, I64, P, P, P, SZ, P], ctypes.c_int),
     "gdft_profile_enable": ([I32], ctypes.c_int),
     "gdft_profile_reset": ([], ctypes.c_int),
     "gdft_profile_read": ([I32, ctypes.POINTER(D), ctypes.POINTER(I64)], ctypes.c_int),

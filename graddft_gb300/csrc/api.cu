@@ -5,6 +5,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "mlp.cuh"
 
 namespace gdft {
 
@@ -189,6 +190,49 @@ static const float *mol_am(const gdft_molecule *m) {
 }
 static const float *mol_af(const gdft_molecule *m) {
   return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_af);
+}
+
+static int check_network(const gdft_network *net) {
+  if (net == nullptr) {
+    set_error("network descriptor is required");
+    return GDFT_ERR_INVALID;
+  }
+  if (net->n_in != kDm21In || net->n_out != kDm21Out) {
+    set_error("network must map the %d DM21 inputs to %d coefficients (got %d -> %d)", kDm21In, kDm21Out, net->n_in,
+              net->n_out);
+    return GDFT_ERR_INVALID;
+  }
+  if (!mlp_width_supported(net->width) || net->n_layers < 0 || net->n_layers > 64) {
+    set_error("network width %d / layers %d not supported (width 32, 64, 128 or 256; 0..64 layers)", net->width,
+              net->n_layers);
+    return GDFT_ERR_INVALID;
+  }
+  if (net->precision != GDFT_FP64) {
+    set_error("network precision %d is not built", net->precision);
+    return GDFT_ERR_UNSUPPORTED;
+  }
+  if (!(net->sigmoid_scale != 0.0) || !(net->ln_eps >= 0.0) || !(net->squash_offset >= 0.0)) {
+    set_error("network constants out of range");
+    return GDFT_ERR_INVALID;
+  }
+  return GDFT_OK;
+}
+
+static MlpShape net_shape(const gdft_network *net) {
+  MlpShape S;
+  S.n_in = net->n_in;
+  S.width = net->width;
+  S.n_layers = net->n_layers;
+  S.n_out = net->n_out;
+  S.squash_offset = net->squash_offset;
+  S.sigmoid_scale = net->sigmoid_scale;
+  S.ln_eps = net->ln_eps;
+  return S;
+}
+
+// The network scratch follows the contraction workspace.
+static size_t neural_ws_bytes(const gdft_molecule *mol, const gdft_network *net) {
+  return ws_layout(mol).bytes + align256(mlp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
 }
 
 // Density stage into ws.feat.
@@ -428,6 +472,123 @@ int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, con
   return run_vxc(mol, coef, d_vxc, ws, st);
 }
 
+
+int gdft_network_param_count(const gdft_network *net, size_t *count) {
+  int rc = check_network(net);
+  if (rc) return rc;
+  if (count == nullptr) {
+    set_error("gdft_network_param_count: null output");
+    return GDFT_ERR_INVALID;
+  }
+  *count = mlp_param_count(net_shape(net));
+  return GDFT_OK;
+}
+
+int gdft_neural_workspace_bytes(const gdft_molecule *mol, const gdft_network *net, size_t *bytes) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_network(net))) return rc;
+  if (bytes == nullptr) {
+    set_error("gdft_neural_workspace_bytes: null output");
+    return GDFT_ERR_INVALID;
+  }
+  *bytes = neural_ws_bytes(mol, net);
+  return GDFT_OK;
+}
+
+int gdft_neural_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net,
+                                    const double *d_params, const double *d_ehf, double *d_exc, double *d_vxc,
+                                    double *d_dparams, void *d_ws, size_t ws_bytes, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_network(net))) return rc;
+  const size_t need = neural_ws_bytes(mol, net);
+  if (d_ws == nullptr || ws_bytes < need) {
+    set_error("workspace of %zu bytes is smaller than the %zu bytes required", ws_bytes, need);
+    return GDFT_ERR_WORKSPACE;
+  }
+  if (((uintptr_t)d_ws & 255u) != 0) {
+    set_error("workspace must be 256-byte aligned");
+    return GDFT_ERR_ALIGNMENT;
+  }
+  if (d_rdm1 == nullptr || d_params == nullptr || d_ehf == nullptr || d_exc == nullptr) {
+    set_error("gdft_neural_xc_energy_and_grads: rdm1, params, ehf and exc are required");
+    return GDFT_ERR_INVALID;
+  }
+  if ((rc = check_aligned8(d_params, "params")) || (rc = check_aligned8(d_ehf, "ehf")) ||
+      (d_dparams && (rc = check_aligned8(d_dparams, "dparams"))))
+    return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  const WsLayout W = ws_layout(mol);
+  if ((rc = run_density(mol, d_rdm1, ws, st))) return rc;
+  double *feat = (double *)(ws + W.off_feat);
+  double *coef = d_vxc ? (double *)(ws + W.off_coef) : nullptr;
+  {
+    StageTimer tm(GDFT_STAGE_MLP, st);
+    rc = mlp_run_f64(net_shape(net), d_params, d_dparams, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
+                     net->clip, (double *)(ws + W.bytes), d_exc, coef, st);
+    if (rc) return rc;
+  }
+  if (d_vxc == nullptr) return GDFT_OK;
+  return run_vxc(mol, coef, d_vxc, ws, st);
+}
+
+int gdft_neural_inputs(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net, const double *d_ehf,
+                       double *d_cinputs, double *d_dens, void *d_ws, size_t ws_bytes, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_network(net))) return rc;
+  const size_t need = neural_ws_bytes(mol, net);
+  if (d_ws == nullptr || ws_bytes < need) {
+    set_error("workspace of %zu bytes is smaller than the %zu bytes required", ws_bytes, need);
+    return GDFT_ERR_WORKSPACE;
+  }
+  if (((uintptr_t)d_ws & 255u) != 0) {
+    set_error("workspace must be 256-byte aligned");
+    return GDFT_ERR_ALIGNMENT;
+  }
+  if (d_rdm1 == nullptr || d_ehf == nullptr) {
+    set_error("gdft_neural_inputs: rdm1 and ehf are required");
+    return GDFT_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  const WsLayout W = ws_layout(mol);
+  if ((rc = run_density(mol, d_rdm1, ws, st))) return rc;
+  StageTimer tm(GDFT_STAGE_MLP, st);
+  return mlp_inputs_f64(net_shape(net), (const double *)(ws + W.off_feat), d_ehf, mol->n_grid, mol->n_grid_pad,
+                        net->clip, (double *)(ws + W.bytes), d_cinputs, d_dens, st);
+}
+
+int gdft_network_apply_workspace_bytes(const gdft_network *net, int64_t n_rows, size_t *bytes) {
+  int rc = check_network(net);
+  if (rc) return rc;
+  if (n_rows <= 0 || bytes == nullptr) {
+    set_error("gdft_network_apply_workspace_bytes: invalid arguments");
+    return GDFT_ERR_INVALID;
+  }
+  *bytes = align256(mlp_layout(net_shape(net), n_rows).doubles * sizeof(double));
+  return GDFT_OK;
+}
+
+int gdft_network_apply(const gdft_network *net, const double *d_params, int64_t n_rows, const double *d_x,
+                       double *d_c, void *d_ws, size_t ws_bytes, void *stream) {
+  int rc = check_network(net);
+  if (rc) return rc;
+  if (n_rows <= 0 || d_params == nullptr || d_x == nullptr || d_c == nullptr) {
+    set_error("gdft_network_apply: invalid arguments");
+    return GDFT_ERR_INVALID;
+  }
+  const size_t need = align256(mlp_layout(net_shape(net), n_rows).doubles * sizeof(double));
+  if (d_ws == nullptr || ws_bytes < need) {
+    set_error("workspace of %zu bytes is smaller than the %zu bytes required", ws_bytes, need);
+    return GDFT_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  StageTimer tm(GDFT_STAGE_MLP, st);
+  return mlp_apply_f64(net_shape(net), d_params, d_x, n_rows, (double *)d_ws, d_c, st);
+}
 
 int gdft_vxc_from_potentials(const gdft_molecule *mol, const double *d_pot, double *d_vxc, void *d_ws,
                              size_t ws_bytes, void *stream) {

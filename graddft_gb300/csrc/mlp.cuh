@@ -1,0 +1,50 @@
+// mlp.cuh - the DM21-style coefficient network on the grid (shape, scratch layout, launchers).
+#pragma once
+
+#include "common.cuh"
+
+namespace gdft {
+
+// Network inputs per point: 7 local features + 4 HF features (2 omegas x 2 spins).
+constexpr int kDm21In = 11;
+// Row stride of the squashed-input matrix u (and of dE/du): padded to 16 doubles.
+constexpr int kDm21InPad = 16;
+constexpr int kDm21Out = 3;
+// Blocks of the LayerNorm backward (per-block parameter-gradient partials).
+constexpr int kLnBlocks = 592;  // 4 x 148 SMs
+// Blocks of the column-sum (bias gradient) first pass.
+constexpr int kColBlocks = 296;
+
+struct MlpShape {
+  int n_in, width, n_layers, n_out;
+  double squash_offset, sigmoid_scale, ln_eps;
+};
+
+// Offsets (in doubles) of the network scratch inside its workspace region.
+struct MlpLayout {
+  size_t x, u, e, h, z, y, dy, de, d0, d1, du, kpart, lnpart, colpart, epart, doubles;
+  int nsplit;   // split-K factor of the weight-gradient GEMMs
+  int eblocks;  // energy partial sums
+};
+
+size_t mlp_param_count(const MlpShape &s);
+MlpLayout mlp_layout(const MlpShape &s, int64_t np);
+bool mlp_width_supported(int width);
+
+// Forward (E into *exc), and when coef/dparams are non-null the backward:
+// coef[2][6][np] = per-point adjoint coefficients for the V_xc contraction,
+// dparams = dE/dtheta in the flat parameter order.
+int mlp_run_f64(const MlpShape &S, const double *params, double *dparams, const double *feat, const double *ehf,
+                const double *w, int64_t n_grid, int64_t np, double clip, double *ws, double *exc, double *coef,
+                cudaStream_t st);
+
+// The 11 network inputs (grid x 11) and the 3 energy densities (grid x 3) of
+// the DM21 functional from the density features; scratch in ws.
+int mlp_inputs_f64(const MlpShape &S, const double *feat, const double *ehf, int64_t n_grid, int64_t np,
+                   double clip, double *ws, double *x_out, double *e_out, cudaStream_t st);
+
+// Coefficients c (rows x n_out) of the network on given inputs x (rows x n_in).
+int mlp_apply_f64(const MlpShape &S, const double *params, const double *x, int64_t rows, double *ws, double *c,
+                  cudaStream_t st);
+
+}  // namespace gdft

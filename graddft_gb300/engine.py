@@ -11,7 +11,7 @@ from typing import Optional, Sequence
 import torch
 
 from . import _lib
-from ._lib import GdftFunctional, GdftMolecule, check
+from ._lib import GdftFunctional, GdftMolecule, GdftNetwork, check
 
 F64 = torch.float64
 PRECISIONS = {"fp64": _lib.GDFT_FP64, "tf32x3": _lib.GDFT_TF32X3}
@@ -148,11 +148,50 @@ class Resident:
                                                    self.ws.numel(), _stream(self.device)))
         return vxc
 
+    def neural_xc_energy_and_grads(self, rdm1, net: "Network", flat_params, ehf, want_vxc=True,
+                                   want_dparams=False, exc_out=None, vxc_out=None, dparams_out=None):
+        """E_xc, V_xc = dE/dD and dE/dtheta of a DM21-style neural functional (flat FP64 parameters)."""
+        rdm1 = self._rdm1(rdm1)
+        ehf_t = as_device_f64(ehf, self.device)
+        if ehf_t is None or ehf_t.shape != (2, 2, self.n_grid):
+            raise ValueError(f"ehf must be (2, 2, {self.n_grid}) for the DM21 inputs, got "
+                             f"{None if ehf_t is None else tuple(ehf_t.shape)}")
+        flat = as_device_f64(flat_params, self.device)
+        if flat.ndim != 1 or flat.numel() != net.n_params:
+            raise ValueError(f"flat parameters must hold {net.n_params} values, got {tuple(flat.shape)}")
+        ws = self._neural_ws(net)
+        exc = exc_out if exc_out is not None else torch.empty((), dtype=F64, device=self.device)
+        vxc = None
+        if want_vxc:
+            vxc = vxc_out if vxc_out is not None else torch.empty((2, self.n_ao, self.n_ao), dtype=F64,
+                                                                   device=self.device)
+        dp = None
+        if want_dparams:
+            dp = dparams_out if dparams_out is not None else torch.empty(net.n_params, dtype=F64, device=self.device)
+        check(_lib.load().gdft_neural_xc_energy_and_grads(
+            ctypes.byref(self.desc), _ptr(rdm1), ctypes.byref(net.desc), _ptr(flat), _ptr(ehf_t), _ptr(exc),
+            _ptr(vxc), _ptr(dp), _ptr(ws), ws.numel(), _stream(self.device)))
+        return exc, vxc, dp
+
+    def _neural_ws(self, net: "Network") -> torch.Tensor:
+        key = net.key
+        cached = getattr(self, "_nws", None)
+        if cached is None or cached[0] != key:
+            nbytes = ctypes.c_size_t()
+            check(_lib.load().gdft_neural_workspace_bytes(ctypes.byref(self.desc), ctypes.byref(net.desc),
+                                                          ctypes.byref(nbytes)))
+            self._nws = (key, torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device))
+        return self._nws[1]
+
     def status(self) -> int:
         """Synchronise and raise if a kernel recorded an expired bounded wait since the last query."""
         st = ctypes.c_int32()
         check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(self.ws), self.ws.numel(),
                                              ctypes.byref(st), _stream(self.device)))
+        cached = getattr(self, "_nws", None)
+        if cached is not None:
+            check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(cached[1]), cached[1].numel(),
+                                                 ctypes.byref(st), _stream(self.device)))
         return st.value
 
     def _rdm1(self, rdm1) -> torch.Tensor:
@@ -160,6 +199,61 @@ class Resident:
         if rdm1.shape != (2, self.n_ao, self.n_ao):
             raise ValueError(f"rdm1 must be (2, {self.n_ao}, {self.n_ao}), got {tuple(rdm1.shape)}")
         return rdm1
+
+
+class Network:
+    """Shape and constants of a DM21-style coefficient network, and its flat parameter layout.
+
+    The flat order (the one include/gdft.h documents) follows the flax module
+    names of DM21.default_nn (functional.py:797-822, names at :876-891):
+    Dense_0 kernel/bias, then per layer Dense_i kernel/bias and LayerNorm_{i-1}
+    scale/bias, then the head Dense_{L+1} kernel/bias.
+    """
+
+    def __init__(self, n_layers: int = 6, width: int = 256, n_in: int = 11, n_out: int = 3,
+                 squash_offset: float = 1e-4, sigmoid_scale: float = 2.0, ln_eps: float = 1e-6,
+                 clip: float = 1e-30):
+        self.desc = GdftNetwork()
+        d = self.desc
+        d.n_in, d.width, d.n_layers, d.n_out = int(n_in), int(width), int(n_layers), int(n_out)
+        d.precision = _lib.GDFT_FP64
+        d.squash_offset, d.sigmoid_scale, d.ln_eps, d.clip = (float(squash_offset), float(sigmoid_scale),
+                                                              float(ln_eps), float(clip))
+        self.n_layers, self.width, self.n_in, self.n_out = d.n_layers, d.width, d.n_in, d.n_out
+        self.key = (d.n_in, d.width, d.n_layers, d.n_out, d.precision)
+        self.entries = self._entries()
+        self.n_params = sum(int(torch.Size(shape).numel()) for _, _, shape in self.entries)
+
+    def _entries(self):
+        W, L = self.width, self.n_layers
+        ent = [("Dense_0", "kernel", (self.n_in, W)), ("Dense_0", "bias", (W,))]
+        for i in range(1, L + 1):
+            ent += [(f"Dense_{i}", "kernel", (W, W)), (f"Dense_{i}", "bias", (W,)),
+                    (f"LayerNorm_{i - 1}", "scale", (W,)), (f"LayerNorm_{i - 1}", "bias", (W,))]
+        ent += [(f"Dense_{L + 1}", "kernel", (W, self.n_out)), (f"Dense_{L + 1}", "bias", (self.n_out,))]
+        return ent
+
+    def flatten(self, params, device) -> torch.Tensor:
+        """flax-style {'params': {module: {leaf: array}}} -> one contiguous FP64 device vector."""
+        p = params["params"] if "params" in params else params
+        parts = []
+        for mod, leaf, shape in self.entries:
+            if mod not in p or leaf not in p[mod]:
+                raise ValueError(f"params has no {mod}/{leaf}")
+            t = as_device_f64(p[mod][leaf], device)
+            if tuple(t.shape) != shape:
+                raise ValueError(f"params {mod}/{leaf} has shape {tuple(t.shape)}, expected {shape}")
+            parts.append(t.reshape(-1))
+        return torch.cat(parts)
+
+    def unflatten(self, flat: torch.Tensor):
+        """The inverse of flatten: a flax-style nested dict of views into flat."""
+        out, off = {}, 0
+        for mod, leaf, shape in self.entries:
+            n = int(torch.Size(shape).numel())
+            out.setdefault(mod, {})[leaf] = flat[off:off + n].view(shape)
+            off += n
+        return {"params": out}
 
 
 def selftest_umma() -> float:

@@ -20,15 +20,16 @@ def energy_predictor(functional, nlc_functional=None, clip_cte: float = CLIP, **
         raise NotImplementedError("dispersion (nlc) functionals are not part of the XC grid path")
 
     def predict(params, atoms, *args):
+        needs_chi = functional.densitygrads is not None or functional.coefficient_input_grads is not None
+        if needs_chi and getattr(atoms, "chi", None) is None:
+            raise ValueError("Precomputed chi tensor has not been loaded.")
         exc, vxc = functional.xc_energy_and_grads(params, atoms, clip_cte)
         rdm1 = atoms._rdm1()
         vj, enonxc = engine.coulomb(atoms.rep_tensor, rdm1, atoms.h1e, float(atoms.nuclear_repulsion),
                                     want_energy=True)
         energy = exc + enonxc
         fock = engine.fock(atoms.h1e, vj, vxc, clip_cte)
-        if functional.densitygrads is not None or functional.coefficient_input_grads is not None:
-            if getattr(atoms, "chi", None) is None:
-                raise ValueError("Precomputed chi tensor has not been loaded.")
+        if needs_chi:
             raise NotImplementedError("the chi-based HF Fock contributions are not built in this version")
         return energy, fock
 

@@ -133,6 +133,64 @@ int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, con
                              const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc,
                              void *d_ws, size_t ws_bytes, void *stream);
 
+/* The DM21-style coefficient network of a NeuralFunctional (DM21.default_nn,
+ * functional.py:797-822, with NeuralFunctional.head :407-419):
+ *   h0 = tanh(log(|x| + squash_offset) W0 + b0),
+ *   h_i = elu(LayerNorm_i(h_{i-1} W_i + b_i + h_{i-1})), i = 1..n_layers,
+ *   c = sigmoid_scale * sigmoid((h W_out + b_out) / sigmoid_scale).
+ * Inputs x are the 11 DM21 features (dm21_coefficient_inputs :504-531 plus the
+ * 4 HF columns of dm21_combine_cinputs :628-649); outputs multiply the 3
+ * energy densities [dm21_densities 'LDA', sum_s ehf(w0), sum_s ehf(w1)]
+ * (:534-626, :652-675). */
+typedef struct gdft_network {
+  int32_t n_in;          /* 11                                                  */
+  int32_t width;         /* hidden width: 32, 64, 128 or 256                    */
+  int32_t n_layers;      /* residual LayerNorm layers (6 in DM21.default_nn)    */
+  int32_t n_out;         /* 3                                                   */
+  int32_t precision;     /* GDFT_FP64                                           */
+  int32_t reserved;
+  double squash_offset;  /* 1e-4                                                */
+  double sigmoid_scale;  /* 2.0                                                 */
+  double ln_eps;         /* 1e-6 (flax LayerNorm default)                       */
+  double clip;           /* clip_cte, 1e-30                                     */
+} gdft_network;
+
+/* Number of FP64 parameters in the flat layout the calls below take:
+ * Dense_0 kernel (n_in x width, row-major as flax stores it) and bias; for
+ * i = 1..n_layers, Dense_i kernel and bias followed by LayerNorm_{i-1} scale
+ * and bias; Dense_{n_layers+1} kernel (width x n_out) and bias. */
+int gdft_network_param_count(const gdft_network *net, size_t *count);
+
+/* Workspace bytes of gdft_neural_xc_energy_and_grads on this molecule. */
+int gdft_neural_workspace_bytes(const gdft_molecule *mol, const gdft_network *net, size_t *bytes);
+
+/* xc_energy_and_grads (train.py:86-121) of a DM21-style NeuralFunctional with
+ * stop-gradient HF inputs, plus dE_xc/dtheta (the gradient of
+ * Functional.xc_energy with respect to params, as jax.grad gives it).
+ * d_params / d_dparams: flat FP64 as gdft_network_param_count describes.
+ * d_ehf: (2 omegas, 2 spins, grid).  d_vxc (2, ao, ao) and d_dparams may be
+ * NULL. */
+int gdft_neural_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net,
+                                    const double *d_params, const double *d_ehf, double *d_exc, double *d_vxc,
+                                    double *d_dparams, void *d_ws, size_t ws_bytes, void *stream);
+
+/* The DM21 network inputs and energy densities of a molecule: d_cinputs
+ * (grid, 11) = dm21_combine_cinputs(dm21_coefficient_inputs(...), ehf)
+ * (functional.py:504-531, 628-649) and d_dens (grid, 3) =
+ * dm21_combine_densities(dm21_densities('LDA'), ehf) before clipping
+ * (:534-626, :652-675).  Either output may be NULL.  Workspace as for
+ * gdft_neural_xc_energy_and_grads. */
+int gdft_neural_inputs(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net, const double *d_ehf,
+                       double *d_cinputs, double *d_dens, void *d_ws, size_t ws_bytes, void *stream);
+
+/* Workspace bytes of gdft_network_apply for n_rows inputs. */
+int gdft_network_apply_workspace_bytes(const gdft_network *net, int64_t n_rows, size_t *bytes);
+
+/* The network alone on given inputs (NeuralFunctional.apply, the coefficients
+ * of functional.py:797-822 + :407-419): d_x (n_rows, n_in) -> d_c (n_rows, n_out). */
+int gdft_network_apply(const gdft_network *net, const double *d_params, int64_t n_rows, const double *d_x,
+                       double *d_c, void *d_ws, size_t ws_bytes, void *stream);
+
 /* The transposed density contraction on given per-point potentials (the part
  * of jax.grad at train.py:86 downstream of the pointwise functional):
  *   V_s[a][b] = sum_r  c[s][0] phi_a phi_b + sum_j c[s][1+j] phi_a d_j phi_b

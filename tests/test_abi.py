@@ -62,3 +62,36 @@ def test_functional_dispatch_host_side():
     custom = g.Functional(coefficients=lambda self, *_: torch.tensor([[1.0]]), energy_densities=lambda m: None)
     with pytest.raises(NotImplementedError):
         custom._columns(None)
+
+
+def test_network_layout_host_side(built_lib):
+    """The flat DM21 parameter layout agrees between the library and the Python packing."""
+    import numpy as np
+    import pytest
+
+    from graddft_gb300 import _lib, engine, synthetic
+
+    lib = _lib.load(built_lib)
+    for layers, width in ((6, 256), (2, 64), (0, 32)):
+        net = engine.Network(n_layers=layers, width=width)
+        n = ctypes.c_size_t()
+        assert lib.gdft_network_param_count(ctypes.byref(net.desc), ctypes.byref(n)) == 0
+        assert n.value == net.n_params
+    net = engine.Network()
+    assert net.n_params == 11 * 256 + 256 + 6 * (256 * 256 + 3 * 256) + 256 * 3 + 3
+    params = synthetic.glorot_params(seed=7)
+    flat = net.flatten(params, "cpu")
+    assert flat.shape == (net.n_params,)
+    back = net.unflatten(flat)
+    for mod, d in params["params"].items():
+        for leaf, v in d.items():
+            np.testing.assert_array_equal(back["params"][mod][leaf].numpy(), v)
+    # Dense_0 kernel first, head bias last (the order include/gdft.h documents).
+    np.testing.assert_array_equal(flat[:5].numpy(), params["params"]["Dense_0"]["kernel"].reshape(-1)[:5])
+    np.testing.assert_array_equal(flat[-3:].numpy(), params["params"]["Dense_7"]["bias"])
+    bad = engine.Network(width=100)
+    assert lib.gdft_network_param_count(ctypes.byref(bad.desc), ctypes.byref(n)) == _lib.GDFT_ERR_INVALID
+    wrong = engine.Network(n_in=7)
+    assert lib.gdft_network_param_count(ctypes.byref(wrong.desc), ctypes.byref(n)) == _lib.GDFT_ERR_INVALID
+    with pytest.raises(ValueError):
+        net.flatten({"params": {"Dense_0": params["params"]["Dense_0"]}}, "cpu")
