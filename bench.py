@@ -34,6 +34,29 @@ N_AO, N_GRID, N_OCC, SEED = 512, 1 << 20, 64, 0
 WORKLOAD = "synthetic XC contraction: spin 2, n_ao 512 (s/p/d Gaussians), n_grid 2^20, B88+LYP, E_xc + V_xc"
 
 
+def _workload(n_grid: int, n_ao: int) -> str:
+    if (n_grid, n_ao) == (N_GRID, N_AO):
+        return WORKLOAD
+    return (f"synthetic XC contraction: spin 2, n_ao {n_ao} (s/p/d Gaussians), n_grid {n_grid}, B88+LYP, "
+            "E_xc + V_xc")
+
+
+def _profiled_traffic(kernel: str, n_grid: int, n_ao: int):
+    """DRAM bytes per launch of a kernel, from the committed ncu summary of a smaller case.
+
+    Traffic grows in proportion to the grid points a launch processes (each
+    tile streams its own table rows), so the per-point figure of the 65,536-
+    point capture is scaled to this launch.  Only the n_ao it was captured at.
+    """
+    path = os.path.join(ROOT, "profiles", f"{kernel}_n512_g65536.md")
+    if n_ao != 512 or not os.path.exists(path):
+        return None
+    for ln in open(path):
+        if ln.startswith("dram_bytes_per_grid_point_at_n_ao_512:"):
+            return float(ln.split(":")[1]) * n_grid
+    return None
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -298,8 +321,13 @@ def main():
         peak, bound, peak_src = 1.25, "fp64", "nominal GB300 FP64 rate (no measured FP64 peak)"
     else:
         peak, bound, peak_src = bf16, "tensor", f"{src} bf16 dense (the TF32 pipe nominally runs at half of it)"
+    traffic = None
+    if form == "tf32x3":
+        traffic = _profiled_traffic({"density": "dens_tc", "vxc": "vxc_tc"}[dom], args.n_grid, args.n_ao)
     roof = {"bound": bound, "kernel": f"{dom}_{form}", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+            "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 65,536-point capture "
+                              "(profiles/), scaled by grid points" if traffic else None,
             "flops_per_launch": flops_launch,
             "executed_flops_per_launch": flops_launch * (3 if form == "tf32x3" else 1),
             "stage_ms_per_step": {k: v[0] / args.steps for k, v in stage.items()}}
@@ -309,7 +337,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if form == "fp64" else "tf32x3",
         "data": "synthetic (seeded Gaussian basis evaluated on the device)",
-        "config": {"workload": WORKLOAD, "n_ao": args.n_ao, "n_grid": args.n_grid, "form": form,
+        "config": {"workload": _workload(args.n_grid, args.n_ao), "n_ao": args.n_ao, "n_grid": args.n_grid, "form": form,
                    "functional": "B88+LYP", "l2": "inputs larger than L2 (AO tables "
                                                  f"{5 * args.n_grid * args.n_ao * 8 / 2**30:.1f} GiB per layout)"},
         "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), **other,
