@@ -12,8 +12,10 @@
 //
 // Accumulation: the tensor cores truncate every MMA's products to the
 // accumulator's ulp grid, so long FP32 accumulation chains drift towards
-// zero.  Each job's K range is therefore split into sub-jobs of one 32-wide
-// stage (12 MMAs per accumulator) that accumulate in a TMEM buffer W
+// zero, by an amount proportional to the accumulator's size at each
+// instruction.  Each job's K range is therefore split into sub-jobs of one
+// 32-wide stage (12 MMAs per accumulator: the small hi*lo and lo*hi
+// corrections first, the hi*hi products last) that accumulate in a TMEM buffer W
 // (double-buffered); the epilogue folds W into a running sum S, also in
 // TMEM, with round-to-nearest FP32 adds on the CUDA cores, then reduces S
 // against the AO planes at the end of the job.
@@ -164,18 +166,26 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
             const uint32_t sb = umma::smem_u32(smem + s * kStageBytes);
             const bool first = kc == kq * kc_per_sub;
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-              const uint64_t ahi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-              const uint64_t alo = umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+            for (int sp = 0; sp < 2; ++sp) {
+              const uint32_t d = tbase + buf * 128 + sp * kBN;
+              // Corrections first (hi*lo, lo*hi, small), then the hi*hi products.
 #pragma unroll
-              for (int sp = 0; sp < 2; ++sp) {
-                const uint32_t bb = sb + 2 * umma::kBlockBytes + sp * 2 * kHalf + kk * 256;
-                const uint64_t bhi = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
-                const uint64_t blo = umma::sdesc(bb + kHalf, umma::kBlockLBO, umma::kBlockSBO);
-                const uint32_t d = tbase + buf * 128 + sp * kBN;
-                umma::mma_tf32(d, ahi, bhi, idesc, (first && kk == 0) ? 0u : 1u);
-                umma::mma_tf32(d, ahi, blo, idesc, 1u);
-                umma::mma_tf32(d, alo, bhi, idesc, 1u);
+              for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                  const uint64_t ahi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+                  const uint64_t alo =
+                      umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+                  const uint32_t bb = sb + 2 * umma::kBlockBytes + sp * 2 * kHalf + kk * 256;
+                  const uint64_t bhi = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
+                  const uint64_t blo = umma::sdesc(bb + kHalf, umma::kBlockLBO, umma::kBlockSBO);
+                  if (pass == 0) {
+                    umma::mma_tf32(d, ahi, blo, idesc, (first && kk == 0) ? 0u : 1u);
+                    umma::mma_tf32(d, alo, bhi, idesc, 1u);
+                  } else {
+                    umma::mma_tf32(d, ahi, bhi, idesc, 1u);
+                  }
+                }
               }
             }
             umma::mma_commit(&empty[s]);

@@ -10,12 +10,15 @@
 //       coefficients, split into TF32 hi/lo.
 // Three TF32 products per term (M = 128, N = 64).
 //
-// Accumulation: the tensor cores truncate each MMA's products to the
-// accumulator's ulp grid, so a window of 32 grid points (48 MMAs per
-// accumulator) is accumulated in TMEM region W (double-buffered) and four
-// drain warps fold it into a Kahan-compensated FP32 running sum (S, C) kept
-// in TMEM, with round-to-nearest arithmetic on the CUDA cores.  The slice's
-// sum S - C is written once, in FP64.
+// Accumulation: the tensor cores truncate each MMA's result to the
+// accumulator's ulp grid, an error proportional to the accumulator's size at
+// that instruction.  So each stage (32 grid points of one plane, 12 MMAs per
+// accumulator) is accumulated in TMEM region W (double-buffered), with the
+// small hi*lo and lo*hi correction products issued first (while the
+// accumulator is still small) and the hi*hi products last; four drain warps
+// fold every stage into a Kahan-compensated FP32 running sum (S, C) kept in
+// TMEM, with round-to-nearest arithmetic on the CUDA cores.  The slice's sum
+// S - C is written once, in FP64.
 //
 // Warp roles (320 threads): warp 0 = TMA producer of A, warp 1 = TMEM owner
 // and MMA issuer, warps 2-5 = B builders, warps 6-9 = drainers.  All waits
@@ -129,16 +132,12 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_tc_kernel(const VxcArgs A) {
     const uint32_t idesc = umma::idesc_tf32(128, kBN);
     for (int64_t it = 0; it < nst; ++it) {
       const int s = (int)(it % kStages);
-      const int64_t pcl = it / 4;
-      const int t = (int)(it % 4);
-      const int buf = (int)(pcl & 1);
-      if (t == 0) {
-        if (!umma::warp_wait(&wempty[buf], ((pcl >> 1) & 1) ^ 1)) {
-          if (lane == 0) flag(A.err, 23);
-          break;
-        }
-        umma::tc_fence_after();
+      const int buf = (int)(it & 1);
+      if (!umma::warp_wait(&wempty[buf], ((it >> 1) & 1) ^ 1)) {
+        if (lane == 0) flag(A.err, 23);
+        break;
       }
+      umma::tc_fence_after();
       const uint32_t ph = (it / kStages) & 1;
       if (!umma::warp_wait(&afull[s], ph) || !umma::warp_wait(&bfull[s], ph)) {
         if (lane == 0) flag(A.err, 24);
@@ -148,22 +147,29 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_tc_kernel(const VxcArgs A) {
       if (lane == 0) {
         const uint32_t sb = umma::smem_u32(smem + s * kStageBytes);
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const uint64_t ahi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-          const uint64_t alo = umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+        for (int sp = 0; sp < 2; ++sp) {
+          const uint32_t d = tbase + buf * 128 + sp * kBN;
+          // Corrections first (hi*lo, lo*hi), then the hi*hi products.
 #pragma unroll
-          for (int sp = 0; sp < 2; ++sp) {
-            const uint32_t bb = sb + 2 * umma::kBlockBytes + sp * 2 * kHalfBlock + kk * 256;
-            const uint64_t bhi = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
-            const uint64_t blo = umma::sdesc(bb + kHalfBlock, umma::kBlockLBO, umma::kBlockSBO);
-            const uint32_t d = tbase + buf * 128 + sp * kBN;
-            umma::mma_tf32(d, ahi, bhi, idesc, (t == 0 && kk == 0) ? 0u : 1u);
-            umma::mma_tf32(d, ahi, blo, idesc, 1u);
-            umma::mma_tf32(d, alo, bhi, idesc, 1u);
+          for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t ahi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+              const uint64_t alo = umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+              const uint32_t bb = sb + 2 * umma::kBlockBytes + sp * 2 * kHalfBlock + kk * 256;
+              const uint64_t bhi = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
+              const uint64_t blo = umma::sdesc(bb + kHalfBlock, umma::kBlockLBO, umma::kBlockSBO);
+              if (pass == 0) {
+                umma::mma_tf32(d, ahi, blo, idesc, kk == 0 ? 0u : 1u);
+                umma::mma_tf32(d, alo, bhi, idesc, 1u);
+              } else {
+                umma::mma_tf32(d, ahi, bhi, idesc, 1u);
+              }
+            }
           }
         }
         umma::mma_commit(&empty[s]);
-        if (t == 3) umma::mma_commit(&wfull[buf]);
+        umma::mma_commit(&wfull[buf]);
       }
       __syncwarp();
     }
@@ -252,10 +258,10 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_tc_kernel(const VxcArgs A) {
     // --------------------------------------------------------------- drains
     const int q = warp & 3;
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
-    int64_t pcl = 0;
-    for (; pcl < npcs; ++pcl) {
-      const int buf = (int)(pcl & 1);
-      if (!umma::warp_wait(&wfull[buf], (pcl >> 1) & 1)) {
+    int64_t it = 0;
+    for (; it < nst; ++it) {
+      const int buf = (int)(it & 1);
+      if (!umma::warp_wait(&wfull[buf], (it >> 1) & 1)) {
         if (lane == 0) flag(A.err, 27);
         break;
       }
@@ -264,7 +270,7 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_tc_kernel(const VxcArgs A) {
       for (int c = 0; c < 128; c += 32) {
         float w[32];
         umma::tmem_ld32(tl + buf * 128 + c, w);
-        if (pcl == 0) {
+        if (it == 0) {
           float z[32];
 #pragma unroll
           for (int i = 0; i < 32; ++i) z[i] = 0.0f;
@@ -292,7 +298,7 @@ __global__ void __launch_bounds__(kThreads, 1) vxc_tc_kernel(const VxcArgs A) {
     // The slice's sums, once, in FP64 (zeros for a slice without points).
     const int a = ta * 128 + q * 32 + lane;
     double *vp = A.vpart + (size_t)blockIdx.y * 2 * A.n * A.n;
-    const bool have = pcl == npcs && npcs > 0;
+    const bool have = it == nst && nst > 0;
 #pragma unroll 1
     for (int c = 0; c < 128; c += 32) {
       float sv[32], cv[32];
