@@ -31,6 +31,7 @@ from .popular_functionals import (
     vwn_density,
 )
 from .train import energy_predictor
+from .scf import diff_simple_scf_loop, safe_eigh, safe_fock_solver, safe_general_eigh
 from .neural import DM21, NeuralFunctional, dm21_coefficient_inputs, dm21_hfgrads_cinputs, dm21_hfgrads_densities
 
 __all__ = [
@@ -39,5 +40,5 @@ __all__ = [
     "stack_densities", "B3LYP", "B88", "BLYP", "LSDA", "LYP", "PW92", "VWN", "b3lyp_combine",
     "b3lyp_exhf_densities", "b88_density", "lsda_density", "lyp_density", "pw92_densities", "vwn_density",
     "energy_predictor", "DM21", "NeuralFunctional", "dm21_coefficient_inputs", "dm21_hfgrads_cinputs",
-    "dm21_hfgrads_densities",
+    "dm21_hfgrads_densities", "diff_simple_scf_loop", "safe_eigh", "safe_fock_solver", "safe_general_eigh",
 ]

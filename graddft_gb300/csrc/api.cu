@@ -234,6 +234,9 @@ static MlpShape net_shape(const gdft_network *net) {
 static size_t neural_ws_bytes(const gdft_molecule *mol, const gdft_network *net) {
   return ws_layout(mol).bytes + align256(mlp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
 }
+static size_t hvp_ws_bytes(const gdft_molecule *mol, const gdft_network *net) {
+  return ws_layout(mol).bytes + align256(mlp_hvp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
+}
 
 // Density stage into ws.feat.
 static int run_density(const gdft_molecule *m, const double *rdm1, char *ws, cudaStream_t st) {
@@ -588,6 +591,65 @@ int gdft_network_apply(const gdft_network *net, const double *d_params, int64_t 
   cudaStream_t st = (cudaStream_t)stream;
   StageTimer tm(GDFT_STAGE_MLP, st);
   return mlp_apply_f64(net_shape(net), d_params, d_x, n_rows, (double *)d_ws, d_c, st);
+}
+
+int gdft_neural_hvp_workspace_bytes(const gdft_molecule *mol, const gdft_network *net, size_t *bytes) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_network(net))) return rc;
+  if (bytes == nullptr) {
+    set_error("gdft_neural_hvp_workspace_bytes: null output");
+    return GDFT_ERR_INVALID;
+  }
+  *bytes = hvp_ws_bytes(mol, net);
+  return GDFT_OK;
+}
+
+int gdft_neural_xc_hvp(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net,
+                       const double *d_params, const double *d_ehf, const double *d_tangent, double *d_value,
+                       double *d_hrdm1, double *d_hparams, void *d_ws, size_t ws_bytes, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_network(net))) return rc;
+  const size_t need = hvp_ws_bytes(mol, net);
+  if (d_ws == nullptr || ws_bytes < need) {
+    set_error("workspace of %zu bytes is smaller than the %zu bytes required", ws_bytes, need);
+    return GDFT_ERR_WORKSPACE;
+  }
+  if (((uintptr_t)d_ws & 255u) != 0) {
+    set_error("workspace must be 256-byte aligned");
+    return GDFT_ERR_ALIGNMENT;
+  }
+  if (d_rdm1 == nullptr || d_params == nullptr || d_ehf == nullptr || d_tangent == nullptr) {
+    set_error("gdft_neural_xc_hvp: rdm1, params, ehf and tangent are required");
+    return GDFT_ERR_INVALID;
+  }
+  if ((rc = check_aligned8(d_params, "params")) || (rc = check_aligned8(d_ehf, "ehf")) ||
+      (rc = check_aligned8(d_tangent, "tangent")))
+    return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  const WsLayout W = ws_layout(mol);
+  const MlpShape S = net_shape(net);
+  const MlpHvpLayout H = mlp_hvp_layout(S, mol->n_grid_pad);
+  double *hws = (double *)(ws + W.bytes);
+  double *feat = (double *)(ws + W.off_feat);
+  // Features of D (kept in the second-order scratch), then of the tangent G.
+  if ((rc = run_density(mol, d_rdm1, ws, st))) return rc;
+  if ((rc = check_cuda(cudaMemcpyAsync(hws + H.featp, feat, (size_t)2 * kFeat * mol->n_grid_pad * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, st),
+                       "hvp feature copy")))
+    return rc;
+  if ((rc = run_density(mol, d_tangent, ws, st))) return rc;
+  double *coef = d_hrdm1 ? (double *)(ws + W.off_coef) : nullptr;
+  {
+    StageTimer tm(GDFT_STAGE_MLP, st);
+    rc = mlp_hvp_f64(S, d_params, d_hparams, hws + H.featp, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
+                     net->clip, hws, d_value, coef, st);
+    if (rc) return rc;
+  }
+  if (d_hrdm1 == nullptr) return GDFT_OK;
+  return run_vxc(mol, coef, d_hrdm1, ws, st);
 }
 
 int gdft_vxc_from_potentials(const gdft_molecule *mol, const double *d_pot, double *d_vxc, void *d_ws,

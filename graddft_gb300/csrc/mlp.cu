@@ -26,122 +26,12 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "mlp.cuh"
+#include "mlp_gemm.cuh"
 #include "xc_functionals.cuh"
 
 namespace gdft {
 
 namespace {
-
-// ----------------------------------------------------------------- GEMM ---
-// C[M x N] = op(A) op(B) (+ beta C); row-major operands with leading dimensions.
-//   kNN: A (M x K), B (K x N)       kNT: A (M x K), B stored (N x K)
-//   kTN: A stored (K x M), B (K x N); K is split over blockIdx.z, each split
-//        writing its own partial C at C + z * split_stride.
-enum { kNN = 0, kNT = 1, kTN = 2 };
-constexpr int GT = 64, GK = 16, GTH = 256;
-
-template <int MODE>
-__global__ void __launch_bounds__(GTH) gemm_f64_kernel(int M, int N, int K, const double *__restrict__ A, int lda,
-                                                      const double *__restrict__ B, int ldb, double *__restrict__ C,
-                                                      int ldc, double beta, int kchunk, size_t split_stride) {
-  __shared__ double As[GK][GT + 1];
-  __shared__ double Bs[GK][GT + 1];
-  const int tid = threadIdx.x, tr = tid >> 4, tc = tid & 15;
-  const int m0 = blockIdx.x * GT, n0 = blockIdx.y * GT;
-  const int kb = MODE == kTN ? blockIdx.z * kchunk : 0;
-  const int ke = MODE == kTN ? min(K, kb + kchunk) : K;
-  double acc[4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
-  for (int k0 = kb; k0 < ke; k0 += GK) {
-#pragma unroll
-    for (int i = 0; i < (GK * GT) / GTH; ++i) {
-      const int idx = tid + i * GTH;
-      // Index maps chosen so that consecutive threads read consecutive addresses.
-      {
-        int kk, mm;
-        if (MODE == kTN) {
-          kk = idx / GT, mm = idx % GT;  // A stored (K x M): m fastest
-        } else {
-          mm = idx / GK, kk = idx % GK;  // A (M x K): k fastest
-        }
-        const int m = m0 + mm, k = k0 + kk;
-        double a = 0.0;
-        if (m < M && k < ke) a = MODE == kTN ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
-        As[kk][mm] = a;
-      }
-      {
-        int kk, nn;
-        if (MODE == kNT) {
-          nn = idx / GK, kk = idx % GK;  // B stored (N x K): k fastest
-        } else {
-          kk = idx / GT, nn = idx % GT;  // B (K x N): n fastest
-        }
-        const int n = n0 + nn, k = k0 + kk;
-        double b = 0.0;
-        if (n < N && k < ke) b = MODE == kNT ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
-        Bs[kk][nn] = b;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < GK; ++kk) {
-      double a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][tr + 16 * i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tc + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-  double *Cz = C + (MODE == kTN ? (size_t)blockIdx.z * split_stride : 0);
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int m = m0 + tr + 16 * i, n = n0 + tc + 16 * j;
-      if (m < M && n < N) {
-        double *c = Cz + (size_t)m * ldc + n;
-        *c = beta != 0.0 ? beta * *c + acc[i][j] : acc[i][j];
-      }
-    }
-}
-
-// C[i] = sum over splits of part[split][i] (fixed order).
-__global__ void sum_splits_kernel(const double *__restrict__ part, int nsplit, size_t total, double *__restrict__ C) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= total) return;
-  double s = 0.0;
-  for (int k = 0; k < nsplit; ++k) s += part[(size_t)k * total + i];
-  C[i] = s;
-}
-
-// Column sums of X [rows][ncols] (stride ld), first pass: block b sums its row
-// range into part[b][ncols]; second pass sums the partials in block order.
-__global__ void colsum_part_kernel(const double *__restrict__ X, int64_t rows, int ncols, int ld,
-                                   double *__restrict__ part) {
-  const int64_t chunk = (rows + gridDim.x - 1) / gridDim.x;
-  const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
-  for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
-    double s = 0.0;
-    for (int64_t r = r0; r < r1; ++r) s += X[(size_t)r * ld + c];
-    part[(size_t)blockIdx.x * ncols + c] = s;
-  }
-}
-
-__global__ void colsum_final_kernel(const double *__restrict__ part, int nparts, int ncols, double *__restrict__ out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncols) return;
-  double s = 0.0;
-  for (int b = 0; b < nparts; ++b) s += part[(size_t)b * ncols + c];
-  out[c] = s;
-}
 
 // ------------------------------------------------------------- features ---
 // Per point: x (11), u = log(|x| + off) (row stride kDm21InPad), energy densities e (3).
@@ -199,11 +89,6 @@ __global__ void dm21_features_kernel(const double *__restrict__ feat, const doub
 }
 
 // ------------------------------------------------------------ row kernels -
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 
 // h0 = tanh(z + b0) in place.
 __global__ void tanh_bias_kernel(double *__restrict__ z, const double *__restrict__ b, size_t total, int width) {
@@ -427,13 +312,6 @@ __global__ void dm21_potentials_kernel(const double *__restrict__ feat, const do
     for (int k = 0; k < kFeat; ++k) coef[((size_t)s * kFeat + k) * np + p] = c[s][k];
 }
 
-template <int MODE>
-cudaError_t gemm(int M, int N, int K, const double *A, int lda, const double *B, int ldb, double *C, int ldc,
-                 double beta, cudaStream_t st) {
-  dim3 grid((M + GT - 1) / GT, (N + GT - 1) / GT, 1);
-  gemm_f64_kernel<MODE><<<grid, GTH, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, beta, K, 0);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_res_ln_elu_fwd(int width, double *z, const double *b, const double *hprev, const double *scale,
                                   const double *bias, double eps, int64_t rows, double *h, cudaStream_t st) {
@@ -619,21 +497,11 @@ int mlp_run_f64(const MlpShape &S, const double *params, double *dparams, const 
 
   // ---- backward ----
   const int ns = L.nsplit;
-  const int kchunk = (int)(((np + ns - 1) / ns + GK - 1) / GK * GK);
   auto weight_grad = [&](int M, int N, const double *A, int lda, const double *B, int ldb, double *C) {
-    dim3 grid((M + GT - 1) / GT, (N + GT - 1) / GT, ns);
-    gemm_f64_kernel<kTN><<<grid, GTH, 0, st>>>(M, N, (int)np, A, lda, B, ldb, kpart, N, 0.0, kchunk,
-                                               (size_t)M * N);
-    cudaError_t r = cudaGetLastError();
-    if (r != cudaSuccess) return r;
-    const size_t total = (size_t)M * N;
-    sum_splits_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(kpart, ns, total, C);
-    return cudaGetLastError();
+    return gemm_tn_split(M, N, np, A, lda, B, ldb, C, ns, kpart, st);
   };
   auto col_sum = [&](const double *X, int64_t rows, int ncols, int ld, double *out) {
-    colsum_part_kernel<<<kColBlocks, 256, 0, st>>>(X, rows, ncols, ld, colpart);
-    colsum_final_kernel<<<(ncols + 255) / 256, 256, 0, st>>>(colpart, kColBlocks, ncols, out);
-    return cudaGetLastError();
+    return col_sums(X, rows, ncols, ld, out, colpart, kColBlocks, st);
   };
   // Head: dW_out = h_L^T dy, db_out = sum_r dy, dh_L = dy W_out^T.
   if (dparams) {

@@ -38,6 +38,23 @@ int mlp_run_f64(const MlpShape &S, const double *params, double *dparams, const 
                 const double *w, int64_t n_grid, int64_t np, double clip, double *ws, double *exc, double *coef,
                 cudaStream_t st);
 
+// Scratch of the second-order pass (offsets in doubles).  Primal and tangent
+// activations are stacked as [2][np][width] so one GEMM serves both.
+struct MlpHvpLayout {
+  size_t featp, x, xt, u, e, et, h, z, y, gy, ge, d0, d1, gu, kpart, lnpart, colpart, lpart, doubles;
+  int nsplit;
+  int eblocks;
+};
+MlpHvpLayout mlp_hvp_layout(const MlpShape &s, int64_t np);
+
+// Second-order adjoint for L = <G, dE/dD>: from the density features of D
+// (featp) and of the tangent G (featt), writes coef[2][6][np] (the per-point
+// coefficients whose V contraction is dL/dD), dparams = dL/dtheta (may be
+// null) and *lval = L (may be null).
+int mlp_hvp_f64(const MlpShape &S, const double *params, double *dparams, const double *featp, const double *featt,
+                const double *ehf, const double *w, int64_t n_grid, int64_t np, double clip, double *ws,
+                double *lval, double *coef, cudaStream_t st);
+
 // The 11 network inputs (grid x 11) and the 3 energy densities (grid x 3) of
 // the DM21 functional from the density features; scratch in ws.
 int mlp_inputs_f64(const MlpShape &S, const double *feat, const double *ehf, int64_t n_grid, int64_t np,

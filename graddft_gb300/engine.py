@@ -173,6 +173,36 @@ class Resident:
             _ptr(vxc), _ptr(dp), _ptr(ws), ws.numel(), _stream(self.device)))
         return exc, vxc, dp
 
+    def neural_xc_hvp(self, rdm1, net: "Network", flat_params, ehf, tangent, want_value=False, want_drdm1=True,
+                      want_dparams=True):
+        """Gradients of L = <tangent, V_xc(D, theta)>: (L, dL/dD, dL/dtheta) (second-order adjoint)."""
+        rdm1 = self._rdm1(rdm1)
+        g = self._rdm1(tangent)
+        ehf_t = as_device_f64(ehf, self.device)
+        if ehf_t is None or ehf_t.shape != (2, 2, self.n_grid):
+            raise ValueError(f"ehf must be (2, 2, {self.n_grid})")
+        flat = as_device_f64(flat_params, self.device)
+        if flat.ndim != 1 or flat.numel() != net.n_params:
+            raise ValueError(f"flat parameters must hold {net.n_params} values, got {tuple(flat.shape)}")
+        ws = self._hvp_ws(net)
+        val = torch.empty((), dtype=F64, device=self.device) if want_value else None
+        hd = torch.empty((2, self.n_ao, self.n_ao), dtype=F64, device=self.device) if want_drdm1 else None
+        hp = torch.empty(net.n_params, dtype=F64, device=self.device) if want_dparams else None
+        check(_lib.load().gdft_neural_xc_hvp(ctypes.byref(self.desc), _ptr(rdm1), ctypes.byref(net.desc), _ptr(flat),
+                                             _ptr(ehf_t), _ptr(g), _ptr(val), _ptr(hd), _ptr(hp), _ptr(ws),
+                                             ws.numel(), _stream(self.device)))
+        return val, hd, hp
+
+    def _hvp_ws(self, net: "Network") -> torch.Tensor:
+        key = net.key
+        cached = getattr(self, "_hws", None)
+        if cached is None or cached[0] != key:
+            nbytes = ctypes.c_size_t()
+            check(_lib.load().gdft_neural_hvp_workspace_bytes(ctypes.byref(self.desc), ctypes.byref(net.desc),
+                                                              ctypes.byref(nbytes)))
+            self._hws = (key, torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device))
+        return self._hws[1]
+
     def _neural_ws(self, net: "Network") -> torch.Tensor:
         key = net.key
         cached = getattr(self, "_nws", None)
@@ -188,10 +218,11 @@ class Resident:
         st = ctypes.c_int32()
         check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(self.ws), self.ws.numel(),
                                              ctypes.byref(st), _stream(self.device)))
-        cached = getattr(self, "_nws", None)
-        if cached is not None:
-            check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(cached[1]), cached[1].numel(),
-                                                 ctypes.byref(st), _stream(self.device)))
+        for name in ("_nws", "_hws"):
+            cached = getattr(self, name, None)
+            if cached is not None:
+                check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(cached[1]), cached[1].numel(),
+                                                     ctypes.byref(st), _stream(self.device)))
         return st.value
 
     def _rdm1(self, rdm1) -> torch.Tensor:

@@ -70,6 +70,9 @@ class Molecule:
     # Extensions: stop-gradient HF energy densities (omega, spin, grid) supplied
     # directly when no chi tensor is available, and the arithmetic form.
     ehf: Optional[Any] = None
+    # Three-index density-fitting Coulomb tensor (naux, ao, ao), used for J
+    # when a four-index rep_tensor is too large to hold.
+    df_tensor: Optional[Any] = None
     precision: str = "fp64"
     _resident: Any = field(default=None, compare=False, repr=False)
 

@@ -91,6 +91,45 @@ class _NeuralXc(torch.autograd.Function):
         return gv, gp, None, None, None
 
 
+class _NeuralXcPair(torch.autograd.Function):
+    """(E_xc, V_xc)(D, theta), both differentiable.
+
+    Backward: for cotangents (gE, gV), dD = gE V + d<gV, V>/dD and
+    dtheta = gE dE/dtheta + d<gV, V>/dtheta, the second-order terms from the
+    library's Hessian-vector product.  Nothing of the network pass is kept
+    between forward and backward: the backward recomputes it (per-call
+    checkpointing), so long unrolled loops hold only D, theta and V.
+    """
+
+    @staticmethod
+    def forward(ctx, rdm1, flat, resident, net, ehf):
+        exc, vxc, dp = resident.neural_xc_energy_and_grads(rdm1.detach(), net, flat.detach(), ehf, want_vxc=True,
+                                                           want_dparams=ctx.needs_input_grad[1])
+        ctx.save_for_backward(rdm1.detach(), flat.detach(), vxc, *(t for t in (dp,) if t is not None))
+        ctx.resident, ctx.net, ctx.ehf = resident, net, ehf
+        return exc, vxc
+
+    @staticmethod
+    def backward(ctx, g_e, g_v):
+        saved = ctx.saved_tensors
+        rdm1, flat, vxc = saved[:3]
+        dp = saved[3] if len(saved) > 3 else None
+        d_rdm1 = d_flat = None
+        want_d, want_p = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if want_d:
+            d_rdm1 = g_e * vxc if g_e is not None else torch.zeros_like(vxc)
+        if want_p:
+            d_flat = g_e * dp if g_e is not None else torch.zeros_like(flat)
+        if g_v is not None and bool((g_v != 0).any()):
+            _, hd, hp = ctx.resident.neural_xc_hvp(rdm1, ctx.net, flat, ctx.ehf, g_v.contiguous(), want_value=False,
+                                                   want_drdm1=want_d, want_dparams=want_p)
+            if want_d:
+                d_rdm1 = d_rdm1 + hd
+            if want_p:
+                d_flat = d_flat + hp
+        return d_rdm1, d_flat, None, None, None
+
+
 @dataclass
 class NeuralFunctional(Functional):
     """functional.py:345-500: a Functional whose coefficients are a network.
@@ -209,6 +248,20 @@ class NeuralFunctional(Functional):
         exc, vxc, dp = r.neural_xc_energy_and_grads(atoms._rdm1(), net, flat, self._ehf(atoms), want_vxc=True,
                                                    want_dparams=want_dparams)
         return exc, vxc, (net.unflatten(dp) if dp is not None else None)
+
+    def xc_energy_and_potential(self, params, atoms, clip_cte: float = CLIP):
+        """(E_xc, V_xc), both differentiable in rdm1 and in the parameter tensors (to second order).
+
+        What value_and_grad(argnums=1) of train.py:86 gives inside a jax.grad-ed
+        program: the Fock matrices of an unrolled SCF loop are built from V_xc
+        and differentiated through.
+        """
+        self._check_slots()
+        r = atoms.resident()
+        net = self.network(clip_cte)
+        flat = net.flatten(params, r.device)
+        rdm1 = atoms.rdm1 if isinstance(atoms.rdm1, torch.Tensor) and atoms.rdm1.requires_grad else atoms._rdm1()
+        return _NeuralXcPair.apply(rdm1, flat, r, net, self._ehf(atoms))
 
     def energy_xc_only(self, params, atoms, *args, **kwargs):
         """E_xc as a differentiable torch scalar in rdm1 and in the parameter tensors."""

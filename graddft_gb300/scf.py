@@ -1,0 +1,164 @@
+"""Differentiable SCF loop on the GPU (evaluate.py:256-344) with the safe eigensolver.
+
+Mirrors ``diff_simple_scf_loop``: an initial energy/Fock evaluation, then
+``cycles`` iterations of generalized eigh of the Fock matrix, aufbau
+occupations, the density matrix, linear mixing and a new energy/Fock
+evaluation; the whole loop is differentiable.  The pieces follow the
+reference:
+
+* ``safe_eigh`` / ``safe_general_eigh`` / ``safe_fock_solver``:
+  utils/eigenproblem.py:26-149, including the Lorentzian-broadened reverse rule
+  for (near-)degenerate eigenvalues (DEGEN_TOL 1e-6, BROADENING 1e-10);
+* ``get_occ`` / ``make_rdm1``: molecule.py:816-889;
+* the energy and Fock matrix of ``energy_predictor.predict``
+  (train.py:124-163): E = E_xc + E_nuc + tr(D h) + 1/2 tr(D J) and
+  F = abs_clip(1/2 (G + G^T)), G = abs_clip(h + J + V_xc).
+
+The n x n linear algebra (Cholesky, inverse, eigh) runs in FP64 through
+torch's CUDA linear-algebra calls (cuSOLVER/cuBLAS); E_xc and V_xc come from
+the library's kernels, and the backward through V_xc uses its
+Hessian-vector product (one recomputation of the network pass per iteration:
+per-iteration checkpointing).  The Coulomb matrix comes from the molecule's
+four-index ``rep_tensor`` or, for larger bases, a three-index
+density-fitting tensor ``df_tensor`` (naux, n, n): J = sum_P B_P tr(B_P D).
+"""
+from __future__ import annotations
+
+from typing import Callable
+
+import torch
+
+from .functional import CLIP
+
+DEGEN_TOL = 1e-6
+BROADENING = 1e-10
+F64 = torch.float64
+
+
+class _SafeEigh(torch.autograd.Function):
+    """eigh with the reverse rule of utils/eigenproblem.py:41-107."""
+
+    @staticmethod
+    def forward(ctx, A):
+        evals, evecs = torch.linalg.eigh(A)
+        ctx.save_for_backward(evals, evecs)
+        return evals, evecs
+
+    @staticmethod
+    def backward(ctx, g_evals, g_evecs):
+        evals, evecs = ctx.saved_tensors
+        if g_evals is None:
+            g_evals = torch.zeros_like(evals)
+        if g_evecs is None:
+            g_evecs = torch.zeros_like(evecs)
+        vt = evecs.transpose(-1, -2)
+        diff = evals.unsqueeze(-2) - evals.unsqueeze(-1)  # [i][j] = e_j - e_i
+        degen = diff.abs() < DEGEN_TOL
+        regular = torch.nan_to_num(1.0 / diff, nan=0.0, posinf=torch.finfo(F64).max, neginf=-torch.finfo(F64).max)
+        broadened = diff / (diff * diff + BROADENING)
+        Fm = 0.5 * torch.where(degen, broadened, regular)
+        Fm = Fm - torch.diag_embed(torch.diagonal(Fm, dim1=-2, dim2=-1))
+        inner = 0.5 * torch.diag_embed(g_evals) + Fm * (vt @ g_evecs)
+        grad = torch.linalg.inv(vt) @ inner @ vt
+        return grad + grad.transpose(-1, -2)
+
+
+def safe_eigh(A):
+    """Eigenvalues and eigenvectors of a real symmetric matrix (eigenproblem.py:26-38)."""
+    return _SafeEigh.apply(A)
+
+
+def safe_general_eigh(A, B):
+    """A C = B C E via Cholesky of B (eigenproblem.py:110-131)."""
+    L = torch.linalg.cholesky(B)
+    L_inv = torch.linalg.inv(L)
+    C = L_inv @ A @ L_inv.transpose(-1, -2)
+    evals, evecs_t = safe_eigh(C)
+    return evals, L_inv.transpose(-1, -2) @ evecs_t
+
+
+def safe_fock_solver(fock, overlap):
+    """Both spins (eigenproblem.py:134-149): (mo_energy (2, n), mo_coeff (2, n, n))."""
+    e_up, c_up = safe_general_eigh(fock[0], overlap)
+    e_dn, c_dn = safe_general_eigh(fock[1], overlap)
+    return torch.stack((e_up, e_dn)), torch.stack((c_up, c_dn))
+
+
+def get_occ(mo_energies, nelecs):
+    """Aufbau occupations: the nelec lowest orbitals of each spin (molecule.py:848-889)."""
+    occ = torch.zeros_like(mo_energies)
+    for s in range(2):
+        idx = torch.argsort(mo_energies[s].detach())
+        occ[s, idx[: int(nelecs[s])]] = 1.0
+    return occ
+
+
+def make_rdm1(mo_coeff, mo_occ):
+    """D_s = C_s diag(occ_s) C_s^T (molecule.py:816-846)."""
+    return torch.einsum("sij,sj,skj->sik", mo_coeff, mo_occ, mo_coeff)
+
+
+def _abs_clip(x, clip):
+    return torch.where(x.abs() > clip, x, torch.zeros((), dtype=x.dtype, device=x.device))
+
+
+def coulomb_matrix(atoms, rdm1_total):
+    """J from rep_tensor (molecule.py:783-811) or from a density-fitting tensor."""
+    df = getattr(atoms, "df_tensor", None)
+    if df is not None:
+        return torch.einsum("P,Pmn->mn", torch.einsum("Pls,ls->P", df, rdm1_total), df)
+    if atoms.rep_tensor is None:
+        raise ValueError("the molecule has neither rep_tensor nor df_tensor for the Coulomb matrix")
+    return torch.einsum("mnls,ls->mn", atoms.rep_tensor, rdm1_total)
+
+
+def energy_and_fock(functional, params, atoms, clip_cte: float = CLIP):
+    """energy_predictor.predict (train.py:124-163), differentiable in rdm1 and params (also through V_xc)."""
+    exc, vxc = functional.xc_energy_and_potential(params, atoms, clip_cte)
+    rdm1 = atoms.rdm1
+    d_tot = rdm1.sum(0)
+    h1e = atoms.h1e
+    J = coulomb_matrix(atoms, d_tot)
+    energy = exc + atoms.nuclear_repulsion + torch.sum(d_tot * h1e) + 0.5 * torch.sum(d_tot * J)
+    fock = _abs_clip(h1e + J + vxc, clip_cte)
+    fock = 0.5 * (fock + fock.transpose(-1, -2))
+    return energy, _abs_clip(fock, clip_cte)
+
+
+def orbital_grad(mo_coeff, mo_occ, fock):
+    """molecule.py:344-383: 2 C_vir^T F C_occ per spin, concatenated."""
+    out = []
+    for s in range(2):
+        occ = mo_occ[s] > 0
+        out.append((2.0 * mo_coeff[s][:, ~occ].T @ fock[s] @ mo_coeff[s][:, occ]).reshape(-1))
+    return torch.cat(out)
+
+
+def diff_simple_scf_loop(functional, cycles: int = 25, mixing_factor: float = 0.4,
+                         clip_cte: float = CLIP) -> Callable:
+    """evaluate.py:256-344: returns ``iterator(params, atoms) -> atoms`` with the final
+    rdm1, fock, energy, mo_coeff, mo_energy and mo_occ."""
+
+    def iterator(params, atoms, *args):
+        dev = atoms.resident().device
+        t = lambda x: x if isinstance(x, torch.Tensor) and x.device == dev else torch.as_tensor(x, dtype=F64, device=dev)  # noqa: E731
+        atoms = atoms.replace(rdm1=t(atoms.rdm1), h1e=t(atoms.h1e), s1e=t(atoms.s1e),
+                              nuclear_repulsion=t(atoms.nuclear_repulsion), mo_occ=t(atoms.mo_occ))
+        if getattr(atoms, "df_tensor", None) is not None:
+            atoms = atoms.replace(df_tensor=t(atoms.df_tensor))
+        elif atoms.rep_tensor is not None:
+            atoms = atoms.replace(rep_tensor=t(atoms.rep_tensor))
+        nelecs = [int(round(float(atoms.mo_occ[s].sum()))) for s in range(2)]
+        energy, fock = energy_and_fock(functional, params, atoms, clip_cte)
+        atoms = atoms.replace(fock=fock, energy=energy)
+        for _ in range(cycles):
+            old_rdm1 = atoms.rdm1
+            mo_energy, mo_coeff = safe_fock_solver(atoms.fock, atoms.s1e)
+            mo_occ = get_occ(mo_energy, nelecs)
+            rdm1 = (1.0 - mixing_factor) * old_rdm1 + mixing_factor * make_rdm1(mo_coeff, mo_occ)
+            atoms = atoms.replace(mo_energy=mo_energy, mo_coeff=mo_coeff, mo_occ=mo_occ, rdm1=rdm1)
+            energy, fock = energy_and_fock(functional, params, atoms, clip_cte)
+            atoms = atoms.replace(fock=fock, energy=energy)
+        return atoms
+
+    return iterator

@@ -36,6 +36,7 @@ S, P, D = 0, 1, 2
 
 STREAM_GEOMETRY, STREAM_EXPONENTS, STREAM_D_ALPHA, STREAM_D_BETA = 0, 1, 2, 3
 STREAM_WEIGHTS, STREAM_THETA, STREAM_EHF = 4, 5, 6
+STREAM_SCF = 7
 
 
 def rng(seed: int, stream: int) -> np.random.Generator:
@@ -166,6 +167,43 @@ def glorot_params(layer_widths=(256,) * 6, n_in: int = 11, n_out: int = 3, seed:
     last = layer_widths[-1]
     params[f"Dense_{len(layer_widths) + 1}"] = {"kernel": glorot(last, n_out), "bias": g.uniform(-0.1, 0.1, n_out)}
     return {"params": params}
+
+
+@dataclass
+class ScfSystem:
+    """One-electron data of the synthetic differentiable-SCF problem."""
+
+    h1e: np.ndarray        # (n, n) core Hamiltonian, eigenvalues uniform in [-20, 5] Ha
+    s1e: np.ndarray        # (n, n) overlap I + 0.05 M / |M|_2, M random SPD
+    df_tensor: np.ndarray  # (naux, n, n) positive, symmetric in (m, n)
+    rdm1: np.ndarray       # (2, n, n) core-guess density matrix
+    mo_occ: np.ndarray     # (2, n) aufbau occupations of the core guess
+    nuclear_repulsion: float
+
+
+def make_scf_system(n_ao: int, n_occ: int, naux: int = 768, seed: int = 0) -> ScfSystem:
+    """H, S, a density-fitting Coulomb tensor and the core-guess D for the SCF loop."""
+    g = rng(seed, STREAM_SCF)
+    q, _ = np.linalg.qr(g.standard_normal((n_ao, n_ao)))
+    h = (q * g.uniform(-20.0, 5.0, n_ao)) @ q.T
+    h = 0.5 * (h + h.T)
+    a = g.standard_normal((n_ao, n_ao))
+    m = a @ a.T + n_ao * np.eye(n_ao)
+    s = np.eye(n_ao) + 0.05 * m / np.linalg.norm(m, 2)
+    b = np.abs(g.standard_normal((naux, n_ao, n_ao)))
+    b = 0.5 * (b + b.transpose(0, 2, 1)) / np.sqrt(naux * n_ao * n_ao)
+    lc = np.linalg.cholesky(s)
+    li = np.linalg.inv(lc)
+    e, v = np.linalg.eigh(li @ h @ li.T)
+    c = li.T @ v[:, np.argsort(e)]
+    occ = np.zeros((2, n_ao))
+    occ[:, :n_occ] = 1.0
+    d = np.stack([(c[:, :n_occ]) @ c[:, :n_occ].T] * 2)
+    # Scale B so the core-guess Coulomb matrix has entries of order 1 Ha.
+    dt = d.sum(0)
+    j = np.einsum("P,Pmn->mn", np.einsum("Pls,ls->P", b, dt), b)
+    b *= 1.0 / np.sqrt(np.abs(j).max())
+    return ScfSystem(h, s, b, d, occ, float(g.uniform(5.0, 10.0)))
 
 
 @dataclass

@@ -174,6 +174,20 @@ int gdft_neural_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rd
                                     const double *d_params, const double *d_ehf, double *d_exc, double *d_vxc,
                                     double *d_dparams, void *d_ws, size_t ws_bytes, void *stream);
 
+/* Workspace bytes of gdft_neural_xc_hvp on this molecule. */
+int gdft_neural_hvp_workspace_bytes(const gdft_molecule *mol, const gdft_network *net, size_t *bytes);
+
+/* Second-order adjoint of gdft_neural_xc_energy_and_grads: for a cotangent G
+ * on V_xc (d_tangent, (2, ao, ao)), the gradients of L = <G, V_xc(D, theta)>
+ * = sum_sab G_sab dE_xc/dD_sab: d_hrdm1 = dL/dD (2, ao, ao), d_hparams =
+ * dL/dtheta (flat), d_value = L (each may be NULL).  This is the vector-
+ * Jacobian product jax.grad forms when it differentiates through a Fock
+ * matrix built from V_xc in the differentiable SCF loop (evaluate.py:314-344,
+ * train.py:86-163).  No separate function in the reference (JAX derives it). */
+int gdft_neural_xc_hvp(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net,
+                       const double *d_params, const double *d_ehf, const double *d_tangent, double *d_value,
+                       double *d_hrdm1, double *d_hparams, void *d_ws, size_t ws_bytes, void *stream);
+
 /* The DM21 network inputs and energy densities of a molecule: d_cinputs
  * (grid, 11) = dm21_combine_cinputs(dm21_coefficient_inputs(...), ehf)
  * (functional.py:504-531, 628-649) and d_dens (grid, 3) =

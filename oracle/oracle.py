@@ -28,7 +28,7 @@ __all__ = [
     "exchange_polarization_correction", "correlation_polarization_correction",
     "dm21_coefficient_inputs", "dm21_densities", "dm21_combine_cinputs", "dm21_combine_densities",
     "densities_generic", "dm21_network", "FUNCTIONALS", "energy_densities", "xc_energy",
-    "xc_energy_and_grads", "predict_fock", "t64", "features_numpy", "FZETA_PP0",
+    "xc_energy_and_grads", "xc_hvp", "predict_fock", "t64", "features_numpy", "FZETA_PP0",
 ]
 
 
@@ -464,6 +464,34 @@ def xc_energy_and_grads(name, rdm1, ao, grad_ao, grad2_ao, weights, params=None,
     for ((k, kk), _), g in zip(leaves, grads[1:]):
         dparams.setdefault(k, {})[kk] = (torch.zeros_like(_) if g is None else g).numpy()
     return float(E.detach()), V.numpy(), {"params": dparams}
+
+
+def xc_hvp(name, rdm1, ao, grad_ao, grad2_ao, weights, tangent, params=None, ehf=None, clip_cte=CLIP):
+    """Second-order adjoint of ``xc_energy_and_grads``: with L = <G, dE_xc/dD> (G = ``tangent``),
+    return (L, dL/dD, dL/dtheta).  This is what jax.grad computes when it differentiates through a
+    Fock matrix built from V_xc, as in the differentiable SCF loop (evaluate.py:314-344)."""
+    D = t64(rdm1).clone().requires_grad_(True)
+    G = t64(tangent)
+    ao, grad_ao = t64(ao), t64(grad_ao)
+    grad2_ao = None if grad2_ao is None else t64(grad2_ao)
+    weights = t64(weights)
+    ehf = None if ehf is None else t64(ehf)
+    tparams, leaves = None, []
+    if params is not None:
+        p, names = _tree_leaves(params)
+        tparams = {"params": {k: {} for k in p}}
+        for k, kk in names:
+            t = t64(p[k][kk]).clone().requires_grad_(True)
+            tparams["params"][k][kk] = t
+            leaves.append(((k, kk), t))
+    E = _energy(name, D, ao, grad_ao, grad2_ao, weights, tparams, ehf, clip_cte)
+    (V,) = torch.autograd.grad(E, D, create_graph=True)
+    L = (V * G).sum()
+    grads = torch.autograd.grad(L, [D] + [t for _, t in leaves], allow_unused=True)
+    dparams = {}
+    for ((k, kk), t), g in zip(leaves, grads[1:]):
+        dparams.setdefault(k, {})[kk] = (torch.zeros_like(t) if g is None else g).detach().numpy()
+    return float(L.detach()), grads[0].detach().numpy(), ({"params": dparams} if leaves else None)
 
 
 def predict_fock(E_xc, V_xc, h1e, vj, nonxc_energy, clip_cte=CLIP):

@@ -1,0 +1,149 @@
+"""GPU parity of the second-order adjoint (Hessian-vector product of E_xc) and
+of the differentiable SCF loop, against the oracle's torch double-backward."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from graddft_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def G(built_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import graddft_gb300 as G
+
+    return G
+
+
+def _t(x):
+    return torch.as_tensor(np.asarray(x), dtype=torch.float64, device="cuda")
+
+
+def _params(seed):
+    p = synthetic.glorot_params(seed=seed)
+    return {"params": {k: {kk: torch.as_tensor(v) for kk, v in d.items()} for k, d in p["params"].items()}}
+
+
+def _dm21(G):
+    hf = lambda atoms, *_, **__: atoms.ehf  # noqa: E731
+    return G.DM21(densitygrads=None, coefficient_input_grads=None, nograd_densities=hf, nograd_coefficient_inputs=hf)
+
+
+def _case(n_grid=2048, n_ao=24, n_occ=4, seed=31):
+    wl = synthetic.make_workload(n_grid, n_ao, n_occ, seed=seed, box_angstrom=7.0, centre_box_angstrom=5.0)
+    ao, g1, g2 = O.eval_ao_planes(wl.basis, wl.coords)
+    rho = np.einsum("sab,ra,rb->rs", wl.rdm1, ao, ao)
+    ehf = synthetic.make_ehf(n_grid, seed + 1, rho, n_omega=2)
+    return wl, ao, g1, g2, ehf
+
+
+def _molecule(G, ao, g1, g2, w, rdm1, ehf, precision="fp64", **extra):
+    return G.Molecule(grid=G.Grid(coords=None, weights=_t(w)), atom_index=None, nuclear_pos=None, ao=_t(ao),
+                      grad_ao=_t(g1), grad_n_ao={2: _t(g2)}, rdm1=_t(rdm1), nuclear_repulsion=0.0, h1e=None,
+                      vj=None, mo_coeff=None, mo_occ=None, mo_energy=None, ehf=_t(ehf), precision=precision,
+                      **extra)
+
+
+def test_hvp_vs_oracle(G):
+    wl, ao, g1, g2, ehf = _case()
+    params = synthetic.glorot_params(seed=6)
+    tangent = np.random.default_rng(5).standard_normal(wl.rdm1.shape)
+    L_ref, hD_ref, hp_ref = O.xc_hvp("DM21", wl.rdm1, ao, g1, g2, wl.weights, tangent, params=params, ehf=ehf)
+    mol = _molecule(G, ao, g1, g2, wl.weights, wl.rdm1, ehf)
+    f = _dm21(G)
+    net = f.network()
+    r = mol.resident()
+    flat = net.flatten(_params(6), r.device)
+    L, hD, hp = r.neural_xc_hvp(mol._rdm1(), net, flat, mol.ehf, _t(tangent), want_value=True)
+    assert r.status() == 0
+    # <G, V> from the first-order path
+    _, v, _ = r.neural_xc_energy_and_grads(mol._rdm1(), net, flat, mol.ehf)
+    assert abs(float(L) - L_ref) <= 1e-10 * abs(L_ref), (float(L), L_ref)
+    assert abs(float((v * _t(tangent)).sum()) - L_ref) <= 1e-10 * abs(L_ref)
+    assert _rel(hD, hD_ref) <= 1e-9, _rel(hD, hD_ref)
+    hp_tree = net.unflatten(hp)
+    for mod, d in hp_ref["params"].items():
+        for leaf, g in d.items():
+            err = _rel(hp_tree["params"][mod][leaf], g)
+            assert err <= 1e-8, (mod, leaf, err)
+
+
+def test_hvp_vs_finite_differences_of_vxc(G):
+    """<dL/dD, H> against central differences of <G, V_xc(D + h H)> on the device."""
+    wl, ao, g1, g2, ehf = _case(seed=41)
+    mol = _molecule(G, ao, g1, g2, wl.weights, wl.rdm1, ehf)
+    f = _dm21(G)
+    net = f.network()
+    r = mol.resident()
+    flat = net.flatten(_params(8), r.device)
+    rng = np.random.default_rng(9)
+    tangent, H = _t(rng.standard_normal(wl.rdm1.shape)), rng.standard_normal(wl.rdm1.shape)
+    _, hD, _ = r.neural_xc_hvp(mol._rdm1(), net, flat, mol.ehf, tangent, want_dparams=False)
+    h = 1e-5
+    vals = []
+    for sgn in (1.0, -1.0):
+        _, v, _ = r.neural_xc_energy_and_grads(_t(wl.rdm1 + sgn * h * H), net, flat, mol.ehf)
+        vals.append(float((v * tangent).sum()))
+    fd = (vals[0] - vals[1]) / (2 * h)
+    an = float((hD * _t(H)).sum())
+    # Central differences of a function with abs_clip / clip kinks agree to ~1e-5
+    # (the oracle's double-backward above is the exact check).
+    assert abs(fd - an) <= 1e-4 * abs(an), (fd, an)
+
+
+def test_pair_autograd_second_order(G):
+    """(E, V) from xc_energy_and_potential carry second-order gradients through V."""
+    wl, ao, g1, g2, ehf = _case(seed=51)
+    params = synthetic.glorot_params(seed=4)
+    tangent = np.random.default_rng(3).standard_normal(wl.rdm1.shape)
+    L_ref, hD_ref, hp_ref = O.xc_hvp("DM21", wl.rdm1, ao, g1, g2, wl.weights, tangent, params=params, ehf=ehf)
+    e_ref, v_ref, dp_ref = O.xc_energy_and_grads("DM21", wl.rdm1, ao, g1, g2, wl.weights, params=params, ehf=ehf,
+                                                 want_param_grads=True)
+    rdm1 = _t(wl.rdm1).requires_grad_(True)
+    mol = _molecule(G, ao, g1, g2, wl.weights, wl.rdm1, ehf).replace(rdm1=rdm1)
+    tp = _params(4)
+    leaves = {k: {kk: t.cuda().requires_grad_(True) for kk, t in d.items()} for k, d in tp["params"].items()}
+    e, v = _dm21(G).xc_energy_and_potential({"params": leaves}, mol)
+    loss = 0.5 * e + (v * _t(tangent)).sum()
+    loss.backward()
+    assert _rel(rdm1.grad, 0.5 * v_ref + hD_ref) <= 1e-9
+    for mod, d in hp_ref["params"].items():
+        for leaf, g in d.items():
+            want = 0.5 * dp_ref["params"][mod][leaf] + g
+            assert _rel(leaves[mod][leaf].grad, want) <= 1e-8, (mod, leaf)
+
+
+def test_scf_loop_vs_oracle(G):
+    n_ao, n_occ, cycles, mix = 24, 4, 3, 0.3
+    wl, ao, g1, g2, _ = _case(n_grid=1024, n_ao=n_ao, n_occ=n_occ, seed=3)
+    sysm = synthetic.make_scf_system(n_ao, n_occ, naux=64, seed=1)
+    rho = np.einsum("sab,ra,rb->rs", sysm.rdm1, ao, ao)
+    ehf = synthetic.make_ehf(wl.n_grid, 5, rho, 2)
+    params = synthetic.glorot_params(seed=2)
+    from oracle import scf as OS
+
+    e_ref, g_ref, d_ref = OS.scf_energy_and_grads(params, ao, g1, g2, wl.weights, ehf, sysm.h1e, sysm.s1e,
+                                                  sysm.df_tensor, sysm.nuclear_repulsion, sysm.rdm1, sysm.mo_occ,
+                                                  cycles, mix)
+    mol = _molecule(G, ao, g1, g2, wl.weights, sysm.rdm1, ehf, df_tensor=_t(sysm.df_tensor)).replace(
+        h1e=_t(sysm.h1e), s1e=_t(sysm.s1e), nuclear_repulsion=_t(sysm.nuclear_repulsion), mo_occ=_t(sysm.mo_occ))
+    tp = _params(2)
+    leaves = {k: {kk: t.cuda().requires_grad_(True) for kk, t in d.items()} for k, d in tp["params"].items()}
+    out = G.diff_simple_scf_loop(_dm21(G), cycles=cycles, mixing_factor=mix)({"params": leaves}, mol)
+    out.energy.backward()
+    assert abs(float(out.energy.detach()) - e_ref) <= 1e-10 * abs(e_ref), (float(out.energy), e_ref)
+    assert _rel(out.rdm1.detach(), d_ref) <= 1e-9
+    for mod, d in g_ref["params"].items():
+        for leaf, g in d.items():
+            err = _rel(leaves[mod][leaf].grad, g)
+            assert err <= 1e-7, (mod, leaf, err)
