@@ -213,10 +213,9 @@ def main():
     def step(res=r):
         res.xc_energy_and_grads(rdm1, fn, None, True, exc, vxc)
         if world > 1:
-            import torch.distributed as dist
+            from graddft_gb300 import sharding
 
-            dist.all_reduce(vxc)
-            dist.all_reduce(exc)
+            sharding.allreduce_sum([exc, vxc])
 
     def barrier():
         if world > 1:

@@ -329,9 +329,14 @@ def _layer_norm(x, scale, bias, eps=1e-6):
     return (x - mean) * torch.rsqrt(var + eps) * scale + bias
 
 
-def dm21_network(params: dict, x, n_layers: int = 6, squash_offset=1e-4, sigmoid_scale_factor=2.0):
-    """functional.py:797-822 (DM21.default_nn) + NeuralFunctional.head (:407-419)."""
+def dm21_network(params: dict, x, n_layers: int | None = None, squash_offset=1e-4, sigmoid_scale_factor=2.0):
+    """functional.py:797-822 (DM21.default_nn) + NeuralFunctional.head (:407-419).
+
+    n_layers defaults to the number of LayerNorm modules in params (6 for
+    DM21's layer_widths)."""
     p = params["params"] if "params" in params else params
+    if n_layers is None:
+        n_layers = sum(1 for k in p if k.startswith("LayerNorm_"))
     if x.ndim == 1:  # canonicalize_inputs, functional.py:934-945
         x = x[:, None]
     x = torch.log(torch.abs(x) + squash_offset)
