@@ -43,14 +43,14 @@ def shard_molecule(mol, rank: int, world: int):
 
 
 def allreduce_sum(tensors: Sequence[torch.Tensor], group=None) -> list:
-    """Sum every tensor over the ranks with one collective (packed into one buffer)."""
+    """Sum every tensor over the ranks in place, with one collective (packed into one buffer)."""
     import torch.distributed as dist
 
     flat = torch.cat([t.reshape(-1) for t in tensors])
     dist.all_reduce(flat, op=dist.ReduceOp.SUM, group=group)
-    out, off = [], 0
+    off = 0
     for t in tensors:
         n = t.numel()
-        out.append(flat[off:off + n].view_as(t))
+        t.copy_(flat[off:off + n].view_as(t))
         off += n
-    return out
+    return list(tensors)
