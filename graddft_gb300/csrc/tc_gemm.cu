@@ -1,0 +1,388 @@
+// tc_gemm.cu - TF32x3 tensor-core GEMM on pre-packed operand blocks (tcgen05).
+//
+//   D[M x N] = sum_K A[M x K] B[N x K]^T      (both operands K-major)
+//
+// Operands arrive as 16 KB blocks of 128 rows x 32 K (TF32 hi and lo images,
+// the K-major no-swizzle shared-memory layout of umma::kblock_off), stored
+// [row tile][K chunk][hi|lo]; one stage is one bulk copy of A (32 KB) and one
+// of B (32 KB).  Three products per term (hi*hi + hi*lo + lo*hi), M = 128,
+// N = 128 per CTA.  Accumulation as in the V_xc contraction: each 32-wide K
+// chunk is accumulated in a TMEM buffer W (double-buffered), correction
+// products first, and four drain warps fold it into a Kahan-compensated FP32
+// running sum (S, C) in TMEM.  The K range may be split across blockIdx.y
+// (split-K); each split writes its S - C either as FP32 into a row-major
+// output (single split) or as FP64 partials [split][M][N].
+//
+// Warp roles (192 threads): warp 0 = TMA producer, warp 1 = TMEM owner and
+// MMA issuer, warps 2-5 = drains.  All waits are bounded; on expiry the CTA
+// records an error word and winds down.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "tc_gemm.cuh"
+#include "umma.cuh"
+
+namespace gdft {
+
+namespace {
+
+constexpr int kStages = 3;
+constexpr uint32_t kOpBytes = 2 * umma::kBlockBytes;   // hi | lo of one 128 x 32 block
+constexpr uint32_t kStageBytes = 2 * kOpBytes;         // A and B
+constexpr int kThreads = 192;
+constexpr uint32_t kTmemCols = 512;  // W0 [0,128), W1 [128,256), S [256,384), C [384,512)
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;
+
+__device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, code); }
+
+__global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], wfull[2], wempty[2], drain;
+  __shared__ uint32_t tmem_base;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x % A.m_tiles, nt = blockIdx.x / A.m_tiles;
+  const int64_t c0 = (int64_t)blockIdx.y * A.chunks_per_split;
+  const int64_t c1 = c0 + A.chunks_per_split < A.k_chunks ? c0 + A.chunks_per_split : A.k_chunks;
+  const int64_t nst = c1 > c0 ? c1 - c0 : 0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      umma::mbar_init(&full[s], 1);
+      umma::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      umma::mbar_init(&wfull[b], 1);
+      umma::mbar_init(&wempty[b], 128);
+    }
+    umma::mbar_init(&drain, 1);
+    umma::fence_barrier_init();
+  }
+  if (warp == 1) umma::tmem_alloc(&tmem_base, kTmemCols);
+  umma::tc_fence_before();
+  __syncthreads();
+  umma::tc_fence_after();
+  const uint32_t tbase = tmem_base;
+  const float *a_tile = A.a + (size_t)mt * A.a_chunks * (kOpBytes / 4);
+  const float *b_tile = A.b + (size_t)nt * A.b_chunks * (kOpBytes / 4);
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    int64_t it = 0;
+    for (; it < nst; ++it) {
+      const int s = (int)(it % kStages);
+      if (!umma::warp_wait(&empty[s], ((it / kStages) & 1) ^ 1)) {
+        if (lane == 0) flag(A.err, 41);
+        break;
+      }
+      if (lane == 0) {
+        const int64_t kc = c0 + it;
+        umma::mbar_arrive_expect_tx(&full[s], kStageBytes);
+        umma::bulk_g2s(smem + s * kStageBytes, a_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
+        umma::bulk_g2s(smem + s * kStageBytes + kOpBytes, b_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
+      }
+      __syncwarp();
+    }
+    // Our own copies land before the CTA can release shared memory.
+    for (int64_t i = it > kStages ? it - kStages : 0; i < it; ++i)
+      if (!umma::warp_wait(&full[i % kStages], (i / kStages) & 1) && lane == 0) flag(A.err, 42);
+  } else if (warp == 1) {
+    // ---------------------------------------------------------- MMA issuer
+    const uint32_t idesc = umma::idesc_tf32(128, 128);
+    for (int64_t it = 0; it < nst; ++it) {
+      const int s = (int)(it % kStages);
+      const int buf = (int)(it & 1);
+      if (!umma::warp_wait(&wempty[buf], ((it >> 1) & 1) ^ 1)) {
+        if (lane == 0) flag(A.err, 43);
+        break;
+      }
+      umma::tc_fence_after();
+      if (!umma::warp_wait(&full[s], (it / kStages) & 1)) {
+        if (lane == 0) flag(A.err, 44);
+        break;
+      }
+      umma::tc_fence_after();
+      if (lane == 0) {
+        const uint32_t sa = umma::smem_u32(smem + s * kStageBytes), sb = sa + kOpBytes;
+        const uint32_t d = tbase + buf * 128;
+#pragma unroll
+        for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t ahi = umma::sdesc(sa + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+            const uint64_t alo = umma::sdesc(sa + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+            const uint64_t bhi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+            const uint64_t blo = umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
+            if (pass == 0) {  // small correction products first
+              umma::mma_tf32(d, ahi, blo, idesc, kk == 0 ? 0u : 1u);
+              umma::mma_tf32(d, alo, bhi, idesc, 1u);
+            } else {
+              umma::mma_tf32(d, ahi, bhi, idesc, 1u);
+            }
+          }
+        }
+        umma::mma_commit(&empty[s]);
+        umma::mma_commit(&wfull[buf]);
+      }
+      __syncwarp();
+    }
+    if (lane == 0) umma::mma_commit(&drain);
+    __syncwarp();
+    if (!umma::warp_wait(&drain, 0) && lane == 0) flag(A.err, 45);
+  } else {
+    // -------------------------------------------------------------- drains
+    const int q = warp & 3;
+    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
+    int64_t it = 0;
+    for (; it < nst; ++it) {
+      const int buf = (int)(it & 1);
+      if (!umma::warp_wait(&wfull[buf], (it >> 1) & 1)) {
+        if (lane == 0) flag(A.err, 46);
+        break;
+      }
+      umma::tc_fence_after();
+#pragma unroll 1
+      for (int c = 0; c < 128; c += 32) {
+        float w[32];
+        umma::tmem_ld32(tl + buf * 128 + c, w);
+        if (it == 0) {
+          float z[32];
+#pragma unroll
+          for (int i = 0; i < 32; ++i) z[i] = 0.0f;
+          umma::tmem_st32(tl + 256 + c, w);
+          umma::tmem_st32(tl + 384 + c, z);
+        } else {
+          float sv[32], cv[32];
+          umma::tmem_ld32(tl + 256 + c, sv);
+          umma::tmem_ld32(tl + 384 + c, cv);
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {  // Kahan: s + (w - c)
+            const float y = w[i] - cv[i];
+            const float t = sv[i] + y;
+            cv[i] = (t - sv[i]) - y;
+            sv[i] = t;
+          }
+          umma::tmem_st32(tl + 256 + c, sv);
+          umma::tmem_st32(tl + 384 + c, cv);
+        }
+      }
+      umma::tmem_st_wait();
+      umma::tc_fence_before();
+      umma::mbar_arrive(&wempty[buf]);
+    }
+    const bool have = it == nst && nst > 0;
+    const int m = mt * 128 + q * 32 + lane;
+#pragma unroll 1
+    for (int c = 0; c < 128; c += 32) {
+      float sv[32], cv[32];
+      if (have) {
+        umma::tmem_ld32(tl + 256 + c, sv);
+        umma::tmem_ld32(tl + 384 + c, cv);
+      }
+      if (m < A.m_valid) {
+        if (A.out32) {
+          float *row = A.out32 + (size_t)m * A.ldo + nt * 128 + c;
+#pragma unroll
+          for (int i = 0; i < 32; ++i)
+            if (nt * 128 + c + i < A.n_valid) row[i] = have ? (float)((double)sv[i] - (double)cv[i]) : 0.0f;
+        } else {
+          double *row = A.out64 + ((size_t)blockIdx.y * A.m_valid + m) * A.n_valid + nt * 128 + c;
+#pragma unroll
+          for (int i = 0; i < 32; ++i)
+            if (nt * 128 + c + i < A.n_valid) row[i] = have ? (double)sv[i] - (double)cv[i] : 0.0;
+        }
+      }
+    }
+  }
+  umma::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) umma::tmem_dealloc(tbase, kTmemCols);
+}
+
+}  // namespace
+
+cudaError_t launch_tcg(const TcgArgs &a, int nsplit, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  if (a.m_tiles <= 0 || a.n_tiles <= 0 || nsplit <= 0 || (a.out32 == nullptr) == (a.out64 == nullptr) ||
+      (a.out32 && nsplit != 1) || a.k_chunks > a.a_chunks || a.k_chunks > a.b_chunks)
+    return cudaErrorInvalidValue;
+  dim3 grid(a.m_tiles * a.n_tiles, nsplit);
+  tcg_kernel<<<grid, kThreads, kSmemBytes, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace gdft
+
+namespace gdft {
+
+namespace {
+
+template <class T>
+__device__ __forceinline__ void split4(const T (&v)[4], float4 &h, float4 &l) {
+  umma::split_tf32((double)v[0], h.x, l.x);
+  umma::split_tf32((double)v[1], h.y, l.y);
+  umma::split_tf32((double)v[2], h.z, l.z);
+  umma::split_tf32((double)v[3], h.w, l.w);
+}
+
+// One CTA per block pair; 256 threads, each 4 (row, 4-wide k group) items.
+template <class T>
+__global__ void pack_rt_kernel(const T *__restrict__ X, int64_t rows, int cols, int ld, int kchunks,
+                               float *__restrict__ out) {
+  const int64_t t = blockIdx.x / kchunks;
+  const int kc = blockIdx.x % kchunks;
+  float *blk = out + (size_t)blockIdx.x * 2 * (umma::kBlockBytes / 4);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int item = threadIdx.x + i * 256;  // 0..1023
+    const int row = item >> 3, k4 = item & 7;
+    const int64_t r = t * 128 + row;
+    T v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = kc * 32 + k4 * 4 + j;
+      v[j] = (r < rows && c < cols) ? X[(size_t)r * ld + c] : (T)0;
+    }
+    float4 h, l;
+    split4(v, h, l);
+    const uint32_t off = umma::kblock_off(row, k4 * 4) / 4;
+    *(float4 *)(blk + off) = h;
+    *(float4 *)(blk + umma::kBlockBytes / 4 + off) = l;
+  }
+}
+
+template <class T>
+__global__ void pack_ct_kernel(const T *__restrict__ X, int64_t rows, int cols, int ld, int64_t rchunks,
+                               float *__restrict__ out) {
+  const int ft = (int)(blockIdx.x / rchunks);
+  const int64_t rc = blockIdx.x % rchunks;
+  float *blk = out + (size_t)blockIdx.x * 2 * (umma::kBlockBytes / 4);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int item = threadIdx.x + i * 256;
+    const int m = item & 127, k4 = item >> 7;  // consecutive threads: consecutive columns of X
+    const int c = ft * 128 + m;
+    T v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t r = rc * 32 + k4 * 4 + j;
+      v[j] = (r < rows && c < cols) ? X[(size_t)r * ld + c] : (T)0;
+    }
+    float4 h, l;
+    split4(v, h, l);
+    const uint32_t off = umma::kblock_off(m, k4 * 4) / 4;
+    *(float4 *)(blk + off) = h;
+    *(float4 *)(blk + umma::kBlockBytes / 4 + off) = l;
+  }
+}
+
+}  // namespace
+
+template <class T>
+cudaError_t launch_pack_rt(const T *X, int64_t rows, int cols, int ld, int64_t tiles, int kchunks, float *out,
+                           cudaStream_t st) {
+  if (tiles <= 0 || kchunks <= 0) return cudaErrorInvalidValue;
+  pack_rt_kernel<T><<<(unsigned)(tiles * kchunks), 256, 0, st>>>(X, rows, cols, ld, kchunks, out);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_pack_ct(const T *X, int64_t rows, int cols, int ld, int ftiles, int64_t rchunks, float *out,
+                           cudaStream_t st) {
+  if (ftiles <= 0 || rchunks <= 0) return cudaErrorInvalidValue;
+  pack_ct_kernel<T><<<(unsigned)(ftiles * rchunks), 256, 0, st>>>(X, rows, cols, ld, rchunks, out);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_pack_rt<float>(const float *, int64_t, int, int, int64_t, int, float *, cudaStream_t);
+template cudaError_t launch_pack_rt<double>(const double *, int64_t, int, int, int64_t, int, float *, cudaStream_t);
+template cudaError_t launch_pack_ct<float>(const float *, int64_t, int, int, int, int64_t, float *, cudaStream_t);
+template cudaError_t launch_pack_ct<double>(const double *, int64_t, int, int, int, int64_t, float *, cudaStream_t);
+
+}  // namespace gdft
+
+// Host-array probe of the packed TF32x3 GEMM (synchronous; allocates its own
+// buffers): D (M x N, FP64) = A (M x K) B (N x K)^T, through the row-tile packer
+// and tcg_kernel, FP32 output for nsplit == 1, FP64 split-K partials summed on
+// the host otherwise.
+extern "C" int gdft_tc_gemm_probe(int32_t M, int32_t N, int32_t K, int32_t nsplit, const double *h_a,
+                                  const double *h_b, double *h_d) {
+  using namespace gdft;
+  if (M <= 0 || N <= 0 || K <= 0 || nsplit <= 0 || !h_a || !h_b || !h_d || M > 4096 || N > 4096 ||
+      K > (1 << 20)) {
+    set_error("gdft_tc_gemm_probe: invalid arguments");
+    return GDFT_ERR_INVALID;
+  }
+  const int mt = (M + 127) / 128, ntl = (N + 127) / 128;
+  const int64_t kch = (K + 31) / 32;
+  const size_t blk = 2 * (umma::kBlockBytes / 4);
+  double *dA = nullptr, *dB = nullptr, *d64 = nullptr;
+  float *pA = nullptr, *pB = nullptr, *d32 = nullptr;
+  int *err = nullptr;
+  int rc = GDFT_OK;
+  auto ck = [&](cudaError_t e, const char *w) {
+    if (rc == GDFT_OK) rc = check_cuda(e, w);
+    return rc == GDFT_OK;
+  };
+  const int64_t cps = (kch + nsplit - 1) / nsplit;
+  if (ck(cudaMalloc(&dA, (size_t)M * K * 8), "probe alloc") && ck(cudaMalloc(&dB, (size_t)N * K * 8), "probe alloc") &&
+      ck(cudaMalloc(&pA, (size_t)mt * kch * blk * 4), "probe alloc") &&
+      ck(cudaMalloc(&pB, (size_t)ntl * kch * blk * 4), "probe alloc") &&
+      ck(cudaMalloc(&d32, (size_t)M * N * 4), "probe alloc") &&
+      ck(cudaMalloc(&d64, (size_t)nsplit * M * N * 8), "probe alloc") && ck(cudaMalloc(&err, 4), "probe alloc") &&
+      ck(cudaMemset(err, 0, 4), "probe memset") &&
+      ck(cudaMemcpy(dA, h_a, (size_t)M * K * 8, cudaMemcpyHostToDevice), "probe copy") &&
+      ck(cudaMemcpy(dB, h_b, (size_t)N * K * 8, cudaMemcpyHostToDevice), "probe copy") &&
+      ck(launch_pack_rt<double>(dA, M, K, K, mt, (int)kch, pA, 0), "probe pack A") &&
+      ck(launch_pack_rt<double>(dB, N, K, K, ntl, (int)kch, pB, 0), "probe pack B")) {
+    TcgArgs a{};
+    a.a = pA;
+    a.b = pB;
+    a.m_tiles = mt;
+    a.n_tiles = ntl;
+    a.a_chunks = a.b_chunks = a.k_chunks = kch;
+    a.chunks_per_split = nsplit == 1 ? kch : cps;
+    a.out32 = nsplit == 1 ? d32 : nullptr;
+    a.ldo = N;
+    a.out64 = nsplit == 1 ? nullptr : d64;
+    a.m_valid = M;
+    a.n_valid = N;
+    a.err = err;
+    if (ck(launch_tcg(a, nsplit, 0), "probe tcg") && ck(cudaDeviceSynchronize(), "probe sync")) {
+      int herr = 0;
+      if (ck(cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost), "probe err")) {
+        if (herr) {
+          set_error("gdft_tc_gemm_probe: bounded wait expired (code %d)", herr);
+          rc = GDFT_ERR_DEVICE;
+        } else if (nsplit == 1) {
+          float *tmp = new float[(size_t)M * N];
+          if (ck(cudaMemcpy(tmp, d32, (size_t)M * N * 4, cudaMemcpyDeviceToHost), "probe out"))
+            for (size_t i = 0; i < (size_t)M * N; ++i) h_d[i] = tmp[i];
+          delete[] tmp;
+        } else {
+          double *tmp = new double[(size_t)nsplit * M * N];
+          if (ck(cudaMemcpy(tmp, d64, (size_t)nsplit * M * N * 8, cudaMemcpyDeviceToHost), "probe out"))
+            for (size_t i = 0; i < (size_t)M * N; ++i) {
+              double s = 0.0;
+              for (int z = 0; z < nsplit; ++z) s += tmp[(size_t)z * M * N + i];
+              h_d[i] = s;
+            }
+          delete[] tmp;
+        }
+      }
+    }
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(pA);
+  cudaFree(pB);
+  cudaFree(d32);
+  cudaFree(d64);
+  cudaFree(err);
+  return rc;
+}

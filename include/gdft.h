@@ -276,6 +276,14 @@ int gdft_selftest_umma(double *max_abs_err);
  * the reference. */
 int gdft_umma_probe(const float *h_a, const float *h_b, float *h_d);
 
+/* D (M x N) = A (M x K) B (N x K)^T (host FP64 arrays, row-major) through the
+ * packed TF32x3 tensor-core GEMM used by the network's mixed form (packing,
+ * tcgen05, Kahan-folded FP32 sums; FP32 output for nsplit 1, FP64 split-K
+ * partials otherwise).  Synchronous, allocates its own buffers.  No
+ * counterpart in the reference. */
+int gdft_tc_gemm_probe(int32_t M, int32_t N, int32_t K, int32_t nsplit, const double *h_a, const double *h_b,
+                       double *h_d);
+
 /* Stage timing (observability; no counterpart in the reference, whose only
  * tracing is jax.profiler.annotate_function at train.py:123).  When enabled,
  * the library records a CUDA event pair on the launching stream around every
