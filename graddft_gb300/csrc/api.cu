@@ -207,8 +207,13 @@ static int check_network(const gdft_network *net) {
               net->n_layers);
     return GDFT_ERR_INVALID;
   }
-  if (net->precision != GDFT_FP64) {
+  if (net->precision != GDFT_FP64 && net->precision != GDFT_TF32X3) {
     set_error("network precision %d is not built", net->precision);
+    return GDFT_ERR_UNSUPPORTED;
+  }
+  if (net->precision == GDFT_TF32X3 && (!mlp_tc_width_supported(net->width) || net->n_layers < 1)) {
+    set_error("the TF32x3 network form needs width 128 or 256 and at least one residual layer (got %d, %d)",
+              net->width, net->n_layers);
     return GDFT_ERR_UNSUPPORTED;
   }
   if (!(net->sigmoid_scale != 0.0) || !(net->ln_eps >= 0.0) || !(net->squash_offset >= 0.0)) {
@@ -232,7 +237,12 @@ static MlpShape net_shape(const gdft_network *net) {
 
 // The network scratch follows the contraction workspace.
 static size_t neural_ws_bytes(const gdft_molecule *mol, const gdft_network *net) {
-  return ws_layout(mol).bytes + align256(mlp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
+  const size_t f64 = align256(mlp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
+  if (net->precision == GDFT_TF32X3) {
+    const size_t tc = mlp_tc_layout(net_shape(net), mol->n_grid_pad).bytes;
+    return ws_layout(mol).bytes + (tc > f64 ? tc : f64);
+  }
+  return ws_layout(mol).bytes + f64;
 }
 static size_t hvp_ws_bytes(const gdft_molecule *mol, const gdft_network *net) {
   return ws_layout(mol).bytes + align256(mlp_hvp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
@@ -529,8 +539,12 @@ int gdft_neural_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rd
   double *coef = d_vxc ? (double *)(ws + W.off_coef) : nullptr;
   {
     StageTimer tm(GDFT_STAGE_MLP, st);
-    rc = mlp_run_f64(net_shape(net), d_params, d_dparams, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
-                     net->clip, (double *)(ws + W.bytes), d_exc, coef, st);
+    if (net->precision == GDFT_TF32X3)
+      rc = mlp_run_tc(net_shape(net), d_params, d_dparams, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
+                      net->clip, ws + W.bytes, d_exc, coef, (int *)(ws + W.off_err), st);
+    else
+      rc = mlp_run_f64(net_shape(net), d_params, d_dparams, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
+                       net->clip, (double *)(ws + W.bytes), d_exc, coef, st);
     if (rc) return rc;
   }
   if (d_vxc == nullptr) return GDFT_OK;

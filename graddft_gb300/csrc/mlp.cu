@@ -340,6 +340,20 @@ cudaError_t launch_res_ln_elu_bwd(int width, double *dh, const double *z, const 
 
 }  // namespace
 
+cudaError_t launch_dm21_features(const double *feat, const double *ehf, int64_t n_grid, int64_t np, double clip,
+                                 double off, double *x, double *u, double *e, cudaStream_t st) {
+  dm21_features_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(feat, ehf, n_grid, np, clip, off, x, u, e);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dm21_potentials(const double *feat, const double *x, const double *du, const double *de,
+                                   int64_t n_grid, int64_t np, double clip, double off, double *coef,
+                                   cudaStream_t st) {
+  dm21_potentials_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(feat, x, du, de, n_grid, np, clip, off,
+                                                                      coef);
+  return cudaGetLastError();
+}
+
 bool mlp_width_supported(int width) { return width == 32 || width == 64 || width == 128 || width == 256; }
 
 size_t mlp_param_count(const MlpShape &s) {

@@ -28,6 +28,14 @@ struct MlpLayout {
 };
 
 size_t mlp_param_count(const MlpShape &s);
+
+// Per-point DM21 inputs x (np x 11), squashed u (np x 16), energy densities e
+// (np x 3); and the V-contraction coefficients from dE/du and dE/de.
+cudaError_t launch_dm21_features(const double *feat, const double *ehf, int64_t n_grid, int64_t np, double clip,
+                                 double off, double *x, double *u, double *e, cudaStream_t st);
+cudaError_t launch_dm21_potentials(const double *feat, const double *x, const double *du, const double *de,
+                                   int64_t n_grid, int64_t np, double clip, double off, double *coef,
+                                   cudaStream_t st);
 MlpLayout mlp_layout(const MlpShape &s, int64_t np);
 bool mlp_width_supported(int width);
 
@@ -54,6 +62,20 @@ MlpHvpLayout mlp_hvp_layout(const MlpShape &s, int64_t np);
 int mlp_hvp_f64(const MlpShape &S, const double *params, double *dparams, const double *featp, const double *featt,
                 const double *ehf, const double *w, int64_t n_grid, int64_t np, double clip, double *ws,
                 double *lval, double *coef, cudaStream_t st);
+
+// Mixed (TF32x3 tensor-core) form of mlp_run_f64: FP32 activations, FP64 row
+// statistics, head, features and potentials; widths 128 and 256.
+struct MlpTcLayout {
+  size_t bytes;
+  size_t x, u, e, dy, de, du, epart, kpart, lnpart, colpart, colpart2;            // FP64 regions (byte offsets)
+  size_t pu, cu, wt, wr, zf, hf, ph, ch, gz, dhp, pg, cg;                        // FP32 regions (byte offsets)
+  int nsplit;
+};
+MlpTcLayout mlp_tc_layout(const MlpShape &s, int64_t np);
+bool mlp_tc_width_supported(int width);
+int mlp_run_tc(const MlpShape &S, const double *params, double *dparams, const double *feat, const double *ehf,
+               const double *w, int64_t n_grid, int64_t np, double clip, char *ws, double *exc, double *coef, int *err,
+               cudaStream_t st);
 
 // The 11 network inputs (grid x 11) and the 3 energy densities (grid x 3) of
 // the DM21 functional from the density features; scratch in ws.

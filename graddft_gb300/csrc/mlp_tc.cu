@@ -1,0 +1,489 @@
+// mlp_tc.cu - mixed form of the DM21-style network: hidden-layer GEMMs on the
+// tensor cores (TF32x3, tc_gemm.cu), FP32 activations, FP64 row statistics.
+//
+// Same computation and adjoint as mlp.cu (DM21.default_nn + head,
+// functional.py:797-822, 407-419; jax.value_and_grad at train.py:86):
+//   forward  z_i = h_{i-1} W_i            tcgen05, A = row-tile pack of h, B = column-tile pack of W_i
+//   backward dh_{i-1} = dz_i W_i^T       tcgen05, A = row-tile pack of dz, B = row-tile pack of W_i
+//            dW_i = h_{i-1}^T dz_i       tcgen05 split-K over grid points, FP64 partials,
+//                                        A / B = column-tile packs of h_{i-1} / dz_i
+// The 11-wide input layer's gradient, the 3-wide head and the bias / LayerNorm
+// parameter sums run on the CUDA cores in FP64 from FP32 activations.  Row
+// kernels: one warp per row of the hidden width, FP64 statistics.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "mlp.cuh"
+#include "mlp_gemm.cuh"
+#include "tc_gemm.cuh"
+#include "umma.cuh"
+
+namespace gdft {
+
+namespace {
+
+constexpr size_t kBlk = 2 * (umma::kBlockBytes / 4);  // floats in one packed hi|lo block pair
+
+__device__ __forceinline__ double elu(double a) { return a > 0.0 ? a : expm1(a); }
+
+// z = zW + b (stored back); h = tanh(z).
+__global__ void l0_fwd_kernel(float *__restrict__ Z, const double *__restrict__ b, size_t total, int width,
+                              float *__restrict__ H) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const double z = (double)Z[i] + b[i % width];
+  Z[i] = (float)z;
+  H[i] = (float)tanh(z);
+}
+
+// z = zW + b + h_prev (stored back into Z); h = elu(LayerNorm(z)) (in place of h_prev).
+template <int PL>
+__global__ void layer_fwd_kernel(float *__restrict__ Z, const double *__restrict__ b, float *__restrict__ H,
+                                 const double *__restrict__ gam, const double *__restrict__ bet, double eps,
+                                 int64_t rows) {
+  constexpr int W = 32 * PL;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= rows) return;
+  float *z = Z + (size_t)r * W, *h = H + (size_t)r * W;
+  double v[PL], s1 = 0.0, s2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < PL; ++k) {
+    const int c = lane + 32 * k;
+    v[k] = ((double)z[c] + b[c]) + (double)h[c];
+    s1 += v[k];
+    s2 += v[k] * v[k];
+  }
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  const double mean = s1 / W;
+  const double var = fmax(0.0, s2 / W - mean * mean);
+  const double rs = 1.0 / sqrt(var + eps);
+#pragma unroll
+  for (int k = 0; k < PL; ++k) {
+    const int c = lane + 32 * k;
+    z[c] = (float)v[k];
+    h[c] = (float)elu((v[k] - mean) * (rs * gam[c]) + bet[c]);
+  }
+}
+
+// Head and energy, one warp per row: y = h W_out + b_out, c = s sigmoid(y / s),
+// E partials per block of 8 rows, dE/dy and dE/de (as head_energy_kernel).
+template <int PL>
+__global__ void __launch_bounds__(256) head_kernel(const float *__restrict__ H, const double *__restrict__ Wo,
+                                                   const double *__restrict__ bo, const double *__restrict__ e,
+                                                   const double *__restrict__ w, int64_t n_grid, int64_t rows,
+                                                   double clip, double sscale, double *__restrict__ dy,
+                                                   double *__restrict__ de, double *__restrict__ epart) {
+  constexpr int W = 32 * PL;
+  __shared__ double red[8];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t r = (int64_t)blockIdx.x * 8 + wid;
+  double e_r = 0.0;
+  if (r < rows) {
+    double y[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < PL; ++k) {
+      const int c = lane + 32 * k;
+      const double hv = (double)H[(size_t)r * W + c];
+#pragma unroll
+      for (int f = 0; f < 3; ++f) y[f] += hv * Wo[c * 3 + f];
+    }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) y[f] = warp_sum(y[f]);
+    if (lane == 0) {
+      double dyv[3] = {0.0, 0.0, 0.0}, dev[3] = {0.0, 0.0, 0.0};
+      if (r < n_grid) {
+        double c[3], ec[3], sg[3], exc = 0.0;
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          sg[f] = 1.0 / (1.0 + exp(-((y[f] + bo[f]) / sscale)));
+          c[f] = sscale * sg[f];
+          const double ev = e[(size_t)r * 3 + f];
+          ec[f] = fabs(ev) > clip ? ev : 0.0;
+          exc = f == 0 ? c[f] * ec[f] : exc + c[f] * ec[f];
+        }
+        const bool m = fabs(exc) > clip;
+        const double Wt = fabs(w[r]) > clip ? w[r] : 0.0;
+        e_r = m ? Wt * exc : 0.0;
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          dyv[f] = (m ? Wt * ec[f] : 0.0) * (sg[f] * (1.0 - sg[f]));
+          dev[f] = (m && fabs(e[(size_t)r * 3 + f]) > clip) ? Wt * c[f] : 0.0;
+        }
+      }
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        dy[(size_t)r * 3 + f] = dyv[f];
+        de[(size_t)r * 3 + f] = dev[f];
+      }
+    }
+  }
+  if (lane == 0) red[wid] = e_r;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < 8; ++i) s += red[i];
+    epart[blockIdx.x] = s;
+  }
+}
+
+// Head weight gradients: part[block][c][0..2] = sum_r h[r][c] dy[r][f] over the
+// block's row range, part[block][W*3 + f] = sum_r dy[r][f]; one thread per column.
+__global__ void head_wgrad_part_kernel(const float *__restrict__ H, const double *__restrict__ dy, int64_t rows,
+                                       int width, double *__restrict__ part) {
+  const int64_t chunk = (rows + gridDim.x - 1) / gridDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
+  double *pb = part + (size_t)blockIdx.x * (3 * width + 3);
+  for (int c = threadIdx.x; c < width; c += blockDim.x) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int64_t r = r0; r < r1; ++r) {
+      const double hv = (double)H[(size_t)r * width + c];
+      a0 += hv * dy[r * 3 + 0];
+      a1 += hv * dy[r * 3 + 1];
+      a2 += hv * dy[r * 3 + 2];
+    }
+    pb[c * 3 + 0] = a0;
+    pb[c * 3 + 1] = a1;
+    pb[c * 3 + 2] = a2;
+  }
+  if (threadIdx.x < 3) {
+    double s = 0.0;
+    for (int64_t r = r0; r < r1; ++r) s += dy[r * 3 + threadIdx.x];
+    pb[3 * width + threadIdx.x] = s;
+  }
+}
+
+// Reverse of a residual layer, one warp per row.  The incoming dE/dh is
+// dy W_out^T (last layer: dy != null) or dhp + gres (the GEMM output plus the
+// residual branch of the layer above).  Writes dE/dz (FP32) and per-block
+// partial sums [block][3][W] of dE/dgamma, dE/dbeta and dE/db (= sum dz).
+template <int PL>
+__global__ void __launch_bounds__(256) layer_bwd_kernel(const float *__restrict__ dhp, const float *__restrict__ gres,
+                                                        const double *__restrict__ dy, const double *__restrict__ Wo,
+                                                        const float *__restrict__ Z, const double *__restrict__ gam,
+                                                        const double *__restrict__ bet, double eps, int64_t rows,
+                                                        float *__restrict__ gz, double *__restrict__ part) {
+  constexpr int W = 32 * PL;
+  __shared__ double sacc[8][3][W];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double pg[PL], pb[PL], pd[PL];
+#pragma unroll
+  for (int k = 0; k < PL; ++k) pg[k] = pb[k] = pd[k] = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * 8 + wid; r < rows; r += (int64_t)gridDim.x * 8) {
+    const float *z = Z + (size_t)r * W;
+    double zv[PL], gh[PL], s1 = 0.0, s2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < PL; ++k) {
+      const int c = lane + 32 * k;
+      zv[k] = (double)z[c];
+      s1 += zv[k];
+      s2 += zv[k] * zv[k];
+      if (dy) {
+        gh[k] = dy[r * 3 + 0] * Wo[c * 3 + 0] + dy[r * 3 + 1] * Wo[c * 3 + 1] + dy[r * 3 + 2] * Wo[c * 3 + 2];
+      } else {
+        gh[k] = (double)dhp[(size_t)r * W + c] + (double)gres[(size_t)r * W + c];
+      }
+    }
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    const double mean = s1 / W;
+    const double var = fmax(0.0, s2 / W - mean * mean);
+    const double rs = 1.0 / sqrt(var + eps);
+    double g[PL], xh[PL], m1 = 0.0, m2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < PL; ++k) {
+      const int c = lane + 32 * k;
+      xh[k] = (zv[k] - mean) * rs;
+      const double a = (zv[k] - mean) * (rs * gam[c]) + bet[c];
+      const double da = gh[k] * (a > 0.0 ? 1.0 : exp(a));
+      pg[k] += da * xh[k];
+      pb[k] += da;
+      g[k] = da * gam[c];
+      m1 += g[k];
+      m2 += g[k] * xh[k];
+    }
+    m1 = warp_sum(m1) / W;
+    m2 = warp_sum(m2) / W;
+#pragma unroll
+    for (int k = 0; k < PL; ++k) {
+      const double d = rs * (g[k] - m1 - xh[k] * m2);
+      pd[k] += d;
+      gz[(size_t)r * W + lane + 32 * k] = (float)d;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < PL; ++k) {
+    sacc[wid][0][lane + 32 * k] = pg[k];
+    sacc[wid][1][lane + 32 * k] = pb[k];
+    sacc[wid][2][lane + 32 * k] = pd[k];
+  }
+  __syncthreads();
+  double *out = part + (size_t)blockIdx.x * 3 * W;
+  for (int c = threadIdx.x; c < 3 * W; c += blockDim.x) {
+    const int q = c / W, cc = c % W;
+    double s = 0.0;
+    for (int w8 = 0; w8 < 8; ++w8) s += sacc[w8][q][cc];
+    out[c] = s;
+  }
+}
+
+// Layer 0 reverse: dz0 = (dhp + gres) (1 - tanh(z0)^2), FP32.
+__global__ void l0_bwd_kernel(const float *__restrict__ dhp, const float *__restrict__ gres,
+                              const float *__restrict__ Z0, size_t total, float *__restrict__ gz) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const double h = tanh((double)Z0[i]);
+  gz[i] = (float)(((double)dhp[i] + (double)gres[i]) * (1.0 - h * h));
+}
+
+// Column sums of an FP32 matrix (FP64 accumulation), first pass per block.
+__global__ void colsum_f32_part_kernel(const float *__restrict__ X, int64_t rows, int ncols,
+                                       double *__restrict__ part) {
+  const int64_t chunk = (rows + gridDim.x - 1) / gridDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
+  for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+    double s = 0.0;
+    for (int64_t r = r0; r < r1; ++r) s += (double)X[(size_t)r * ncols + c];
+    part[(size_t)blockIdx.x * ncols + c] = s;
+  }
+}
+
+// du[r][k] = sum_c dz0[r][c] W0[k][c] for the n_in inputs, one warp per row (FP64).
+template <int PL>
+__global__ void du_kernel(const float *__restrict__ gz, const double *__restrict__ W0, int n_in, int64_t rows,
+                          double *__restrict__ du) {
+  constexpr int W = 32 * PL;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= rows) return;
+  double g[PL];
+#pragma unroll
+  for (int k = 0; k < PL; ++k) g[k] = (double)gz[(size_t)r * W + lane + 32 * k];
+  for (int j = 0; j < kDm21InPad; ++j) {
+    double s = 0.0;
+    if (j < n_in) {
+#pragma unroll
+      for (int k = 0; k < PL; ++k) s += g[k] * W0[(size_t)j * W + lane + 32 * k];
+      s = warp_sum(s);
+    }
+    if (lane == 0) du[(size_t)r * kDm21InPad + j] = s;
+  }
+}
+
+size_t tc_layer_offset(const MlpShape &S, int i) {
+  return (size_t)S.n_in * S.width + S.width + (size_t)i * ((size_t)S.width * S.width + 3 * (size_t)S.width);
+}
+
+template <int PL>
+int run_tc(const MlpShape &S, const double *params, double *dparams, const double *feat, const double *ehf,
+           const double *w, int64_t n_grid, int64_t np, double clip, char *ws, double *exc, double *coef, int *err,
+           cudaStream_t st) {
+  constexpr int Wd = 32 * PL;
+  const MlpTcLayout L = mlp_tc_layout(S, np);
+  auto d64 = [&](size_t off) { return (double *)(ws + off); };
+  auto f32 = [&](size_t off) { return (float *)(ws + off); };
+  double *x = d64(L.x), *u = d64(L.u), *e = d64(L.e), *dy = d64(L.dy), *de = d64(L.de), *du = d64(L.du);
+  double *epart = d64(L.epart), *kpart = d64(L.kpart), *lnpart = d64(L.lnpart), *colpart = d64(L.colpart);
+  double *colpart2 = d64(L.colpart2);
+  float *PU = f32(L.pu), *CU = f32(L.cu), *WT = f32(L.wt), *WR = f32(L.wr), *ZF = f32(L.zf), *HF = f32(L.hf);
+  float *PH = f32(L.ph), *CH = f32(L.ch), *GZ = f32(L.gz), *DHP = f32(L.dhp), *PG = f32(L.pg), *CG = f32(L.cg);
+  const size_t act = (size_t)np * Wd;
+  const int64_t rt = np / kPointTile, rc = np / 32;  // row tiles, row chunks
+  constexpr int ft = Wd / 128, kcw = Wd / 32;         // feature tiles, K chunks of the width
+  const size_t wt0 = (size_t)ft * kBlk, wti = (size_t)ft * kcw * kBlk;  // packed W0^T, W_i^T sizes
+  auto WTi = [&](int i) { return WT + (i == 0 ? 0 : wt0 + (size_t)(i - 1) * wti); };
+  auto WRi = [&](int i) { return WR + (size_t)(i - 1) * wti; };
+  auto CHi = [&](int i) { return CH + (size_t)i * ft * rc * kBlk; };
+  const size_t head_off = tc_layer_offset(S, S.n_layers);
+  const double *W0 = params, *b0 = W0 + (size_t)S.n_in * Wd;
+  const double *Wo = params + head_off, *bo = Wo + (size_t)Wd * S.n_out;
+  int rc_;
+#define GDFT_CK(expr, what)                                      \
+  do {                                                           \
+    if ((rc_ = check_cuda((expr), what)) != GDFT_OK) return rc_; \
+  } while (0)
+  auto gemm_act = [&](const float *A, int64_t a_chunks, const float *B, int64_t b_chunks, int64_t kch, float *out) {
+    TcgArgs a{};
+    a.a = A;
+    a.b = B;
+    a.m_tiles = (int)rt;
+    a.n_tiles = ft;
+    a.a_chunks = a_chunks;
+    a.b_chunks = b_chunks;
+    a.k_chunks = kch;
+    a.chunks_per_split = kch;
+    a.out32 = out;
+    a.ldo = Wd;
+    a.m_valid = (int)np;
+    a.n_valid = Wd;
+    a.err = err;
+    return launch_tcg(a, 1, st);
+  };
+  auto gemm_wgrad = [&](const float *A, int m_tiles, int m_valid, const float *B, double *out) -> cudaError_t {
+    TcgArgs a{};
+    a.a = A;
+    a.b = B;
+    a.m_tiles = m_tiles;
+    a.n_tiles = ft;
+    a.a_chunks = a.b_chunks = a.k_chunks = rc;
+    a.chunks_per_split = (rc + L.nsplit - 1) / L.nsplit;
+    a.out64 = kpart;
+    a.m_valid = m_valid;
+    a.n_valid = Wd;
+    a.err = err;
+    cudaError_t r = launch_tcg(a, L.nsplit, st);
+    if (r != cudaSuccess) return r;
+    const size_t total = (size_t)m_valid * Wd;
+    sum_splits_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(kpart, L.nsplit, total, out);
+    return cudaGetLastError();
+  };
+  const unsigned wblocks = (unsigned)((np * 32 + 255) / 256);  // one warp per row
+  const unsigned eblocks = (unsigned)((act + 255) / 256);
+
+  // ---- weights: packed once per call ----
+  GDFT_CK(launch_pack_ct<double>(W0, S.n_in, Wd, Wd, ft, 1, WTi(0), st), "mlp_tc pack W0");
+  for (int i = 1; i <= S.n_layers; ++i) {
+    const double *Wi = params + tc_layer_offset(S, i - 1);
+    GDFT_CK(launch_pack_ct<double>(Wi, Wd, Wd, Wd, ft, kcw, WTi(i), st), "mlp_tc pack W^T");
+    GDFT_CK(launch_pack_rt<double>(Wi, Wd, Wd, Wd, ft, kcw, WRi(i), st), "mlp_tc pack W");
+  }
+
+  // ---- forward ----
+  GDFT_CK(launch_dm21_features(feat, ehf, n_grid, np, clip, S.squash_offset, x, u, e, st), "mlp_tc features");
+  GDFT_CK(launch_pack_rt<double>(u, np, S.n_in, kDm21InPad, rt, 1, PU, st), "mlp_tc pack u");
+  GDFT_CK(gemm_act(PU, 1, WTi(0), 1, 1, ZF), "mlp_tc dense_0");
+  l0_fwd_kernel<<<eblocks, 256, 0, st>>>(ZF, b0, act, Wd, HF);
+  GDFT_CK(cudaGetLastError(), "mlp_tc tanh");
+  for (int i = 1; i <= S.n_layers; ++i) {
+    const double *Wi = params + tc_layer_offset(S, i - 1), *bi = Wi + (size_t)Wd * Wd, *gi = bi + Wd, *bei = gi + Wd;
+    GDFT_CK(launch_pack_rt<float>(HF, np, Wd, Wd, rt, kcw, PH, st), "mlp_tc pack h");
+    if (dparams) GDFT_CK(launch_pack_ct<float>(HF, np, Wd, Wd, ft, rc, CHi(i - 1), st), "mlp_tc pack h^T");
+    float *Zi = ZF + (size_t)i * act;
+    GDFT_CK(gemm_act(PH, kcw, WTi(i), kcw, kcw, Zi), "mlp_tc dense_i");
+    layer_fwd_kernel<PL><<<wblocks, 256, 0, st>>>(Zi, bi, HF, gi, bei, S.ln_eps, np);
+    GDFT_CK(cudaGetLastError(), "mlp_tc layernorm");
+  }
+  const unsigned hblocks = (unsigned)((np + 7) / 8);
+  head_kernel<PL><<<hblocks, 256, 0, st>>>(HF, Wo, bo, e, w, n_grid, np, clip, S.sigmoid_scale, dy, de, epart);
+  GDFT_CK(cudaGetLastError(), "mlp_tc head");
+  GDFT_CK(launch_energy_reduce(epart, (int)hblocks, exc, st), "mlp_tc energy_reduce");
+  if (coef == nullptr && dparams == nullptr) return GDFT_OK;
+
+  // ---- backward ----
+  if (dparams) {
+    head_wgrad_part_kernel<<<kColBlocks, 256, 0, st>>>(HF, dy, np, Wd, colpart);
+    colsum_final_kernel<<<(3 * Wd + 3 + 255) / 256, 256, 0, st>>>(colpart, kColBlocks, 3 * Wd + 3,
+                                                                  dparams + head_off);
+    GDFT_CK(cudaGetLastError(), "mlp_tc head wgrad");
+  }
+  float *gz_cur = GZ, *gz_prev = GZ + act;
+  for (int i = S.n_layers; i >= 1; --i) {
+    const double *Wi = params + tc_layer_offset(S, i - 1), *gi = Wi + (size_t)Wd * Wd + Wd, *bei = gi + Wd;
+    const float *Zi = ZF + (size_t)i * act;
+    const bool last = i == S.n_layers;
+    layer_bwd_kernel<PL><<<kLnBlocks, 256, 0, st>>>(last ? nullptr : DHP, last ? nullptr : gz_prev,
+                                                    last ? dy : nullptr, Wo, Zi, gi, bei, S.ln_eps, np, gz_cur,
+                                                    lnpart);
+    GDFT_CK(cudaGetLastError(), "mlp_tc layernorm bwd");
+    GDFT_CK(launch_pack_rt<float>(gz_cur, np, Wd, Wd, rt, kcw, PG, st), "mlp_tc pack dz");
+    if (dparams) {
+      double *dWi = dparams + tc_layer_offset(S, i - 1);
+      GDFT_CK(launch_pack_ct<float>(gz_cur, np, Wd, Wd, ft, rc, CG, st), "mlp_tc pack dz^T");
+      GDFT_CK(gemm_wgrad(CHi(i - 1), ft, Wd, CG, dWi), "mlp_tc dW_i");
+      // [dgamma | dbeta | db] partials -> db, then (dgamma, dbeta) in the flat order (db, gamma, beta).
+      colsum_final_kernel<<<(3 * Wd + 255) / 256, 256, 0, st>>>(lnpart, kLnBlocks, 3 * Wd, colpart2);
+      GDFT_CK(cudaGetLastError(), "mlp_tc ln sums");
+      GDFT_CK(cudaMemcpyAsync(dWi + (size_t)Wd * Wd, colpart2 + 2 * Wd, Wd * sizeof(double),
+                              cudaMemcpyDeviceToDevice, st),
+              "mlp_tc db");
+      GDFT_CK(cudaMemcpyAsync(dWi + (size_t)Wd * Wd + Wd, colpart2, 2 * Wd * sizeof(double),
+                              cudaMemcpyDeviceToDevice, st),
+              "mlp_tc dln");
+    }
+    GDFT_CK(gemm_act(PG, kcw, WRi(i), kcw, kcw, DHP), "mlp_tc dh");
+    float *t = gz_cur;
+    gz_cur = gz_prev;
+    gz_prev = t;
+  }
+  // Layer 0: gz_prev holds dE/dz_1, DHP its product with W_1^T.
+  l0_bwd_kernel<<<eblocks, 256, 0, st>>>(DHP, gz_prev, ZF, act, gz_cur);
+  GDFT_CK(cudaGetLastError(), "mlp_tc tanh bwd");
+  if (dparams) {
+    GDFT_CK(launch_pack_ct<double>(u, np, S.n_in, kDm21InPad, 1, rc, CU, st), "mlp_tc pack u^T");
+    GDFT_CK(launch_pack_ct<float>(gz_cur, np, Wd, Wd, ft, rc, CG, st), "mlp_tc pack dz0^T");
+    GDFT_CK(gemm_wgrad(CU, 1, S.n_in, CG, dparams), "mlp_tc dW_0");
+    colsum_f32_part_kernel<<<kColBlocks, 256, 0, st>>>(gz_cur, np, Wd, colpart);
+    colsum_final_kernel<<<(Wd + 255) / 256, 256, 0, st>>>(colpart, kColBlocks, Wd, dparams + (size_t)S.n_in * Wd);
+    GDFT_CK(cudaGetLastError(), "mlp_tc db0");
+  }
+  if (coef) {
+    du_kernel<PL><<<wblocks, 256, 0, st>>>(gz_cur, W0, S.n_in, np, du);
+    GDFT_CK(cudaGetLastError(), "mlp_tc du");
+    GDFT_CK(launch_dm21_potentials(feat, x, du, de, n_grid, np, clip, S.squash_offset, coef, st),
+            "mlp_tc potentials");
+  }
+#undef GDFT_CK
+  return GDFT_OK;
+}
+
+}  // namespace
+
+bool mlp_tc_width_supported(int width) { return width == 128 || width == 256; }
+
+MlpTcLayout mlp_tc_layout(const MlpShape &s, int64_t np) {
+  MlpTcLayout L;
+  const int W = s.width;
+  const size_t act = (size_t)np * W;
+  const int64_t rt = np / kPointTile, rc = np / 32;
+  const int ft = W / 128, kcw = W / 32;
+  L.nsplit = 148;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += (bytes + 255) / 256 * 256;
+    return o;
+  };
+  L.x = take((size_t)np * kDm21In * 8);
+  L.u = take((size_t)np * kDm21InPad * 8);
+  L.e = take((size_t)np * 3 * 8);
+  L.dy = take((size_t)np * 3 * 8);
+  L.de = take((size_t)np * 3 * 8);
+  L.du = take((size_t)np * kDm21InPad * 8);
+  L.epart = take((size_t)((np + 7) / 8) * 8);
+  L.kpart = take((size_t)L.nsplit * W * W * 8);
+  L.lnpart = take((size_t)kLnBlocks * 3 * W * 8);
+  L.colpart = take((size_t)kColBlocks * (3 * W + 3) * 8);
+  L.colpart2 = take((size_t)3 * W * 8);
+  L.pu = take((size_t)rt * kBlk * 4);
+  L.cu = take((size_t)rc * kBlk * 4);
+  L.wt = take(((size_t)ft * kBlk + (size_t)s.n_layers * ft * kcw * kBlk) * 4);
+  L.wr = take((size_t)(s.n_layers > 0 ? s.n_layers : 1) * ft * kcw * kBlk * 4);
+  L.zf = take(act * (s.n_layers + 1) * 4);
+  L.hf = take(act * 4);
+  L.ph = take((size_t)rt * kcw * kBlk * 4);
+  L.ch = take((size_t)(s.n_layers > 0 ? s.n_layers : 1) * ft * rc * kBlk * 4);
+  L.gz = take(2 * act * 4);
+  L.dhp = take(act * 4);
+  L.pg = take((size_t)rt * kcw * kBlk * 4);
+  L.cg = take((size_t)ft * rc * kBlk * 4);
+  L.bytes = off;
+  return L;
+}
+
+int mlp_run_tc(const MlpShape &S, const double *params, double *dparams, const double *feat, const double *ehf,
+               const double *w, int64_t n_grid, int64_t np, double clip, char *ws, double *exc, double *coef, int *err,
+               cudaStream_t st) {
+  if (np % kPointTile != 0 || S.n_in > 128) {
+    set_error("mlp_tc: grid padding or input width not supported");
+    return GDFT_ERR_INVALID;
+  }
+  switch (S.width) {
+    case 128: return run_tc<4>(S, params, dparams, feat, ehf, w, n_grid, np, clip, ws, exc, coef, err, st);
+    case 256: return run_tc<8>(S, params, dparams, feat, ehf, w, n_grid, np, clip, ws, exc, coef, err, st);
+    default:
+      set_error("mlp_tc: width %d not built for the mixed form (128 or 256)", S.width);
+      return GDFT_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace gdft

@@ -243,11 +243,14 @@ class Network:
 
     def __init__(self, n_layers: int = 6, width: int = 256, n_in: int = 11, n_out: int = 3,
                  squash_offset: float = 1e-4, sigmoid_scale: float = 2.0, ln_eps: float = 1e-6,
-                 clip: float = 1e-30):
+                 clip: float = 1e-30, precision: str = "fp64"):
         self.desc = GdftNetwork()
         d = self.desc
         d.n_in, d.width, d.n_layers, d.n_out = int(n_in), int(width), int(n_layers), int(n_out)
-        d.precision = _lib.GDFT_FP64
+        if precision not in PRECISIONS:
+            raise ValueError(f"network precision must be one of {sorted(PRECISIONS)}, got {precision!r}")
+        d.precision = PRECISIONS[precision]
+        self.precision = precision
         d.squash_offset, d.sigmoid_scale, d.ln_eps, d.clip = (float(squash_offset), float(sigmoid_scale),
                                                               float(ln_eps), float(clip))
         self.n_layers, self.width, self.n_in, self.n_out = d.n_layers, d.width, d.n_in, d.n_out

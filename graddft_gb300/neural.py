@@ -148,6 +148,9 @@ class NeuralFunctional(Functional):
     local_features: int = 3
     sigmoid_scale_factor: float = 2.0
     n_input_features: int = 11
+    # Arithmetic form of the network on the device: "fp64" (reference form) or
+    # "tf32x3" (hidden-layer GEMMs on the tensor cores, FP32 activations).
+    precision: str = "fp64"
 
     def network(self, clip_cte: float = CLIP) -> engine.Network:
         widths = set(self.layer_widths)
@@ -157,7 +160,7 @@ class NeuralFunctional(Functional):
             raise NotImplementedError("the device network implements the elu activation of DM21")
         return engine.Network(n_layers=len(self.layer_widths), width=widths.pop(), n_in=self.n_input_features,
                               n_out=self.local_features, squash_offset=self.squash_offset,
-                              sigmoid_scale=self.sigmoid_scale_factor, clip=clip_cte)
+                              sigmoid_scale=self.sigmoid_scale_factor, clip=clip_cte, precision=self.precision)
 
     # ---------------------------------------------------------- flax-like
     def init(self, rng=0, example_inputs=None):

@@ -193,3 +193,32 @@ def test_errors(G, ref):
         f.xc_energy_and_grads_params(bad, mol)
     with pytest.raises(ValueError):  # reference default: HF-Fock terms need chi
         G.energy_predictor(G.DM21())(_params(), mol)
+
+
+@pytest.mark.parametrize("mol_prec", ["fp64", "tf32x3"])
+def test_tensor_core_network_vs_fp64_network(G, mol_prec):
+    """The TF32x3 network form against the FP64 one on the same molecule: E, V_xc, dE/dtheta."""
+    wl = synthetic.make_workload(n_grid=16384, n_ao=64, n_occ=8, seed=61, box_angstrom=9.0, centre_box_angstrom=6.0)
+    ao, g1, g2 = O.eval_ao_planes(wl.basis, wl.coords)
+    rho = np.einsum("sab,ra,rb->rs", wl.rdm1, ao, ao)
+    ehf = synthetic.make_ehf(wl.n_grid, 62, rho, n_omega=2)
+    mol = _molecule(G, ao, g1, g2, wl.weights, wl.rdm1, ehf, precision=mol_prec)
+    out = {}
+    for prec in ("fp64", "tf32x3"):
+        f = _dm21(G)
+        f.precision = prec
+        out[prec] = f.xc_energy_and_grads_params(_params(9), mol)
+    assert mol.resident().status() == 0
+    (e64, v64, d64), (etc, vtc, dtc) = out["fp64"], out["tf32x3"]
+    de = abs(float(etc) - float(e64))
+    dv = float((vtc - v64).abs().max()) / float(v64.abs().max())
+    print("E", float(e64), "|dE|", de, "rel dV", dv)
+    assert de <= 1e-6 * max(1.0, abs(float(e64)))
+    assert dv <= 1e-5
+    worst = 0.0
+    for mod, d in d64["params"].items():
+        for leaf, g in d.items():
+            err = float((dtc["params"][mod][leaf] - g).abs().max()) / max(float(g.abs().max()), 1e-300)
+            worst = max(worst, err)
+            assert err <= 1e-4, (mod, leaf, err)
+    print("worst rel d theta", worst)
