@@ -162,6 +162,163 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+NEURAL_WORKLOAD = ("synthetic neural functional (DM21-style network, 6 x 256, 11 inputs, 3 outputs, Glorot theta): "
+                   "spin 2, n_ao 256, n_grid 2^19, E_xc + V_xc + dE/dtheta")
+
+
+def _neural_launches(n_layers: int) -> int:
+    """Kernels one mixed neural step launches (the sequence in mlp_tc.cu plus the two contractions)."""
+    return (1 + 2 * n_layers) + (4 + 4 * n_layers + 2) + (2 + 7 * n_layers + 9) + 4
+
+
+def run_neural(args):
+    """Neural-functional forward+backward: E_xc, V_xc and dE/dtheta per step (the gradient of a
+    loss (E - E_ref)^2 is 2 (E - E_ref) times these, the same kernels)."""
+    import ctypes
+
+    import torch
+
+    from graddft_gb300 import _lib, build, engine, synthetic
+
+    build.build()
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    n_grid = args.n_grid if args.n_grid != N_GRID else 1 << 19
+    n_ao = args.n_ao if args.n_ao != N_AO else 256
+    n_occ = max(1, n_ao // 8)
+    wl = synthetic.make_workload(n_grid, n_ao, n_occ, SEED)
+    rdm1 = torch.as_tensor(wl.rdm1, device=dev)
+    params = synthetic.glorot_params(seed=SEED)
+    net64, nettc = engine.Network(precision="fp64"), engine.Network(precision="tf32x3")
+    flat = nettc.flatten(params, dev)
+
+    def resident(prec):
+        return engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, prec, dev)
+
+    r = resident("tf32x3")
+    rho = r.density(rdm1, want=("rho",))["rho"].cpu().numpy()
+    ehf = torch.as_tensor(synthetic.make_ehf(n_grid, SEED, rho, 2), device=dev)
+    exc = torch.empty((), dtype=torch.float64, device=dev)
+    vxc = torch.empty((2, n_ao, n_ao), dtype=torch.float64, device=dev)
+    dp = torch.empty(nettc.n_params, dtype=torch.float64, device=dev)
+
+    def step(res=r, net=nettc):
+        res.neural_xc_energy_and_grads(rdm1, net, flat, ehf, True, True, exc, vxc, dp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    r.status()
+    lib.gdft_profile_reset()
+    lib.gdft_profile_enable(1)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    lib.gdft_profile_enable(0)
+    r.status()
+    ms_step = e0.elapsed_time(e1) / args.steps
+    stage = {}
+    for name, sid in (("density", _lib.STAGE_DENSITY), ("network", _lib.STAGE_MLP), ("vxc", _lib.STAGE_VXC),
+                      ("reduce", _lib.STAGE_REDUCE)):
+        t, n = ctypes.c_double(), ctypes.c_int64()
+        _lib.check(lib.gdft_profile_read(sid, ctypes.byref(t), ctypes.byref(n)))
+        stage[name] = t.value / args.steps
+    e_tc, v_tc, d_tc = exc.clone(), vxc.clone(), dp.clone()
+
+    h_rdm1 = rdm1.cpu().pin_memory()
+    h_v = torch.empty(vxc.shape, dtype=torch.float64).pin_memory()
+    h_d = torch.empty(dp.shape, dtype=torch.float64).pin_memory()
+    h_e = torch.empty((), dtype=torch.float64).pin_memory()
+    d_rdm1 = torch.empty_like(rdm1)
+
+    def e2e_step():
+        d_rdm1.copy_(h_rdm1, non_blocking=True)
+        r.neural_xc_energy_and_grads(d_rdm1, nettc, flat, ehf, True, True, exc, vxc, dp)
+        h_v.copy_(vxc, non_blocking=True)
+        h_d.copy_(dp, non_blocking=True)
+        h_e.copy_(exc, non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+
+    other = {}
+    if not args.no_fp64:
+        del r
+        torch.cuda.empty_cache()
+        r64 = resident("fp64")
+        step(r64, net64)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        step(r64, net64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        r64.status()
+        ms64 = e0.elapsed_time(e1)
+        worst = 0.0
+        tree64, treetc = net64.unflatten(dp), nettc.unflatten(d_tc)
+        for mod, d in tree64["params"].items():
+            for leaf, g in d.items():
+                worst = max(worst, float((treetc["params"][mod][leaf] - g).abs().max()) /
+                            max(float(g.abs().max()), 1e-300))
+        other = {"fp64_form_value": n_grid / (ms64 * 1e-3), "fp64_form_ms_per_step": ms64,
+                 "mixed_over_fp64": ms64 / ms_step,
+                 "accuracy_vs_fp64": {"E_xc": float(exc), "abs_dE": abs(float(e_tc) - float(exc)),
+                                      "max_abs_V": float(vxc.abs().max()),
+                                      "max_abs_dV": float((v_tc - vxc).abs().max()),
+                                      "max_rel_dtheta_per_leaf": worst}}
+    hbm, bf16, src = _peaks()
+    W, L = nettc.width, nettc.n_layers
+    net_flops = 2.0 * n_grid * W * (16 + L * W) + 2.0 * n_grid * L * W * W + 2.0 * n_grid * W * (16 + L * W)
+    con_flops = 32.0 * n_grid * n_ao ** 2
+    dom = max(("density", "network", "vxc"), key=lambda k: stage[k])
+    dom_flops = {"density": con_flops / 2, "vxc": con_flops / 2, "network": net_flops}[dom]
+    achieved = dom_flops / (stage[dom] * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": n_grid / (ms_step * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "tf32x3", "data": "synthetic (seeded Gaussian basis evaluated on the device)",
+        "config": {"workload": NEURAL_WORKLOAD if (n_grid, n_ao) == (1 << 19, 256) else
+                   f"synthetic neural functional, n_ao {n_ao}, n_grid {n_grid}", "n_ao": n_ao, "n_grid": n_grid,
+                   "network": "tf32x3 (tensor cores), FP32 activations", "contractions": "tf32x3",
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                     "frac": achieved / bf16, "peak_source": f"{src} bf16 dense (TF32 nominally half)",
+                     "traffic": None, "flops_per_step": {"network": net_flops, "contractions": con_flops},
+                     "stage_ms_per_step": stage},
+        "e2e": {"value": n_grid / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": rdm1.numel() * 8,
+                "d2h_bytes_per_step": vxc.numel() * 8 + dp.numel() * 8 + 8},
+        "gpu_launches": _neural_launches(L) * args.steps, "clocks": clk.summary(), **other,
+    }
+    if not args.no_cpu:
+        import oracle as O
+
+        torch.set_num_threads(os.cpu_count() or 1)
+        n_s = min(args.cpu_sample, 2048)
+        ao, g1, g2 = O.eval_ao_planes(wl.basis, wl.coords[:n_s])
+        t0 = time.perf_counter()
+        O.xc_energy_and_grads("DM21", wl.rdm1, ao, g1, g2, wl.weights[:n_s], params=params,
+                              ehf=ehf[..., :n_s].cpu().numpy(), want_param_grads=True)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_s / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{n_s} grid points of the same workload ({dt:.1f} s), FP64 torch-CPU "
+                                          "restatement, autograd for V_xc and dE/dtheta"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -176,9 +333,13 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
+    ap.add_argument("--workload", default="xc", choices=["xc", "neural"],
+                    help="xc: B88+LYP contraction benchmark (headline); neural: DM21-style network fwd+bwd")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "neural":
+        return run_neural(args)
 
     import torch
 

@@ -23,124 +23,161 @@ namespace {
 
 constexpr size_t kBlk = 2 * (umma::kBlockBytes / 4);  // floats in one packed hi|lo block pair
 
-__device__ __forceinline__ double elu(double a) { return a > 0.0 ? a : expm1(a); }
+__device__ __forceinline__ float eluf(float a) { return a > 0.0f ? a : expm1f(a); }
+
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Per-element arithmetic and per-row statistics of these row kernels are FP32
+// (GB300's FP64 rate is a small fraction of its FP32 rate, and the activations
+// are FP32); long accumulations over grid points and the energy stay FP64.
 
 // z = zW + b (stored back); h = tanh(z).
-__global__ void l0_fwd_kernel(float *__restrict__ Z, const double *__restrict__ b, size_t total, int width,
+__global__ void l0_fwd_kernel(float *__restrict__ Z, const float *__restrict__ b, size_t total, int width,
                               float *__restrict__ H) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
-  const double z = (double)Z[i] + b[i % width];
-  Z[i] = (float)z;
-  H[i] = (float)tanh(z);
+  const float z = Z[i] + b[i % width];
+  Z[i] = z;
+  H[i] = tanhf(z);
 }
 
 // z = zW + b + h_prev (stored back into Z); h = elu(LayerNorm(z)) (in place of h_prev).
+// Mean and variance are taken in two passes over the row held in registers.
 template <int PL>
-__global__ void layer_fwd_kernel(float *__restrict__ Z, const double *__restrict__ b, float *__restrict__ H,
-                                 const double *__restrict__ gam, const double *__restrict__ bet, double eps,
+__global__ void layer_fwd_kernel(float *__restrict__ Z, const float *__restrict__ b, float *__restrict__ H,
+                                 const float *__restrict__ gam, const float *__restrict__ bet, double eps,
                                  int64_t rows) {
   constexpr int W = 32 * PL;
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= rows) return;
   float *z = Z + (size_t)r * W, *h = H + (size_t)r * W;
-  double v[PL], s1 = 0.0, s2 = 0.0;
+  float v[PL], s1 = 0.0f;
 #pragma unroll
   for (int k = 0; k < PL; ++k) {
     const int c = lane + 32 * k;
-    v[k] = ((double)z[c] + b[c]) + (double)h[c];
+    v[k] = (z[c] + b[c]) + h[c];
     s1 += v[k];
-    s2 += v[k] * v[k];
   }
-  s1 = warp_sum(s1);
-  s2 = warp_sum(s2);
-  const double mean = s1 / W;
-  const double var = fmax(0.0, s2 / W - mean * mean);
-  const double rs = 1.0 / sqrt(var + eps);
+  const float mean = warp_sumf(s1) * (1.0f / W);
+  float s2 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < PL; ++k) {
+    const float d = v[k] - mean;
+    s2 += d * d;
+  }
+  const float rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
 #pragma unroll
   for (int k = 0; k < PL; ++k) {
     const int c = lane + 32 * k;
-    z[c] = (float)v[k];
-    h[c] = (float)elu((v[k] - mean) * (rs * gam[c]) + bet[c]);
+    z[c] = v[k];
+    h[c] = eluf((v[k] - mean) * (rs * gam[c]) + bet[c]);
   }
 }
 
-// Head and energy, one warp per row: y = h W_out + b_out, c = s sigmoid(y / s),
-// E partials per block of 8 rows, dE/dy and dE/de (as head_energy_kernel).
+// Head and energy: each warp takes 32 rows; y = h W_out (FP32 row sums) for
+// row i lands in lane i, which then evaluates c = s sigmoid((y + b_out) / s),
+// its energy term, dE/dy and dE/de in FP64 (as head_energy_kernel).  E
+// partials per block of 256 rows.
 template <int PL>
-__global__ void __launch_bounds__(256) head_kernel(const float *__restrict__ H, const double *__restrict__ Wo,
+__global__ void __launch_bounds__(256) head_kernel(const float *__restrict__ H, const float *__restrict__ Wo,
                                                    const double *__restrict__ bo, const double *__restrict__ e,
                                                    const double *__restrict__ w, int64_t n_grid, int64_t rows,
                                                    double clip, double sscale, double *__restrict__ dy,
-                                                   double *__restrict__ de, double *__restrict__ epart) {
+                                                   float *__restrict__ dyf, double *__restrict__ de,
+                                                   double *__restrict__ epart) {
   constexpr int W = 32 * PL;
   __shared__ double red[8];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t r = (int64_t)blockIdx.x * 8 + wid;
-  double e_r = 0.0;
-  if (r < rows) {
-    double y[3] = {0.0, 0.0, 0.0};
+  const int64_t base = ((int64_t)blockIdx.x * 8 + wid) * 32;
+  float wo[PL][3];
+#pragma unroll
+  for (int k = 0; k < PL; ++k)
+#pragma unroll
+    for (int f = 0; f < 3; ++f) wo[k][f] = Wo[(lane + 32 * k) * 3 + f];
+  float my[3] = {0.0f, 0.0f, 0.0f};
+  for (int i = 0; i < 32; ++i) {
+    const int64_t r = base + i;
+    if (r >= rows) break;
+    float yf[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
     for (int k = 0; k < PL; ++k) {
-      const int c = lane + 32 * k;
-      const double hv = (double)H[(size_t)r * W + c];
+      const float hv = H[(size_t)r * W + lane + 32 * k];
 #pragma unroll
-      for (int f = 0; f < 3; ++f) y[f] += hv * Wo[c * 3 + f];
+      for (int f = 0; f < 3; ++f) yf[f] = fmaf(hv, wo[k][f], yf[f]);
     }
 #pragma unroll
-    for (int f = 0; f < 3; ++f) y[f] = warp_sum(y[f]);
-    if (lane == 0) {
-      double dyv[3] = {0.0, 0.0, 0.0}, dev[3] = {0.0, 0.0, 0.0};
-      if (r < n_grid) {
-        double c[3], ec[3], sg[3], exc = 0.0;
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          sg[f] = 1.0 / (1.0 + exp(-((y[f] + bo[f]) / sscale)));
-          c[f] = sscale * sg[f];
-          const double ev = e[(size_t)r * 3 + f];
-          ec[f] = fabs(ev) > clip ? ev : 0.0;
-          exc = f == 0 ? c[f] * ec[f] : exc + c[f] * ec[f];
-        }
-        const bool m = fabs(exc) > clip;
-        const double Wt = fabs(w[r]) > clip ? w[r] : 0.0;
-        e_r = m ? Wt * exc : 0.0;
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          dyv[f] = (m ? Wt * ec[f] : 0.0) * (sg[f] * (1.0 - sg[f]));
-          dev[f] = (m && fabs(e[(size_t)r * 3 + f]) > clip) ? Wt * c[f] : 0.0;
-        }
-      }
-#pragma unroll
-      for (int f = 0; f < 3; ++f) {
-        dy[(size_t)r * 3 + f] = dyv[f];
-        de[(size_t)r * 3 + f] = dev[f];
-      }
+    for (int f = 0; f < 3; ++f) {
+      const float t = warp_sumf(yf[f]);
+      if (lane == i) my[f] = t;
     }
   }
-  if (lane == 0) red[wid] = e_r;
+  const int64_t r = base + lane;
+  double e_r = 0.0;
+  if (r < rows) {
+    double dyv[3] = {0.0, 0.0, 0.0}, dev[3] = {0.0, 0.0, 0.0};
+    if (r < n_grid) {
+      double c[3], ec[3], sg[3], exc = 0.0;
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        sg[f] = 1.0 / (1.0 + exp(-(((double)my[f] + bo[f]) / sscale)));
+        c[f] = sscale * sg[f];
+        const double ev = e[(size_t)r * 3 + f];
+        ec[f] = fabs(ev) > clip ? ev : 0.0;
+        exc = f == 0 ? c[f] * ec[f] : exc + c[f] * ec[f];
+      }
+      const bool m = fabs(exc) > clip;
+      const double Wt = fabs(w[r]) > clip ? w[r] : 0.0;
+      e_r = m ? Wt * exc : 0.0;
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        dyv[f] = (m ? Wt * ec[f] : 0.0) * (sg[f] * (1.0 - sg[f]));
+        dev[f] = (m && fabs(e[(size_t)r * 3 + f]) > clip) ? Wt * c[f] : 0.0;
+      }
+    }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      dy[(size_t)r * 3 + f] = dyv[f];
+      dyf[(size_t)r * 3 + f] = (float)dyv[f];
+      de[(size_t)r * 3 + f] = dev[f];
+    }
+  }
+  const double ws = warp_sum(e_r);
+  if (lane == 0) red[wid] = ws;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < 8; ++i) s += red[i];
-    epart[blockIdx.x] = s;
+    double t = 0.0;
+    for (int i = 0; i < 8; ++i) t += red[i];
+    epart[blockIdx.x] = t;
   }
 }
 
 // Head weight gradients: part[block][c][0..2] = sum_r h[r][c] dy[r][f] over the
 // block's row range, part[block][W*3 + f] = sum_r dy[r][f]; one thread per column.
-__global__ void head_wgrad_part_kernel(const float *__restrict__ H, const double *__restrict__ dy, int64_t rows,
-                                       int width, double *__restrict__ part) {
+__global__ void head_wgrad_part_kernel(const float *__restrict__ H, const float *__restrict__ dyf,
+                                       const double *__restrict__ dy, int64_t rows, int width,
+                                       double *__restrict__ part) {
   const int64_t chunk = (rows + gridDim.x - 1) / gridDim.x;
   const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
   double *pb = part + (size_t)blockIdx.x * (3 * width + 3);
   for (int c = threadIdx.x; c < width; c += blockDim.x) {
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    for (int64_t r = r0; r < r1; ++r) {
-      const double hv = (double)H[(size_t)r * width + c];
-      a0 += hv * dy[r * 3 + 0];
-      a1 += hv * dy[r * 3 + 1];
-      a2 += hv * dy[r * 3 + 2];
+    for (int64_t rb = r0; rb < r1; rb += 16) {  // FP32 over 16 rows, FP64 across
+      float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
+      const int64_t re = rb + 16 < r1 ? rb + 16 : r1;
+      for (int64_t r = rb; r < re; ++r) {
+        const float hv = H[(size_t)r * width + c];
+        f0 = fmaf(hv, dyf[r * 3 + 0], f0);
+        f1 = fmaf(hv, dyf[r * 3 + 1], f1);
+        f2 = fmaf(hv, dyf[r * 3 + 2], f2);
+      }
+      a0 += f0;
+      a1 += f1;
+      a2 += f2;
     }
     pb[c * 3 + 0] = a0;
     pb[c * 3 + 1] = a1;
@@ -156,63 +193,95 @@ __global__ void head_wgrad_part_kernel(const float *__restrict__ H, const double
 // Reverse of a residual layer, one warp per row.  The incoming dE/dh is
 // dy W_out^T (last layer: dy != null) or dhp + gres (the GEMM output plus the
 // residual branch of the layer above).  Writes dE/dz (FP32) and per-block
-// partial sums [block][3][W] of dE/dgamma, dE/dbeta and dE/db (= sum dz).
+// partial sums [block][3][W] of dE/dgamma, dE/dbeta and dE/db (= sum dz),
+// accumulated in FP64 over the rows.
 template <int PL>
 __global__ void __launch_bounds__(256) layer_bwd_kernel(const float *__restrict__ dhp, const float *__restrict__ gres,
-                                                        const double *__restrict__ dy, const double *__restrict__ Wo,
-                                                        const float *__restrict__ Z, const double *__restrict__ gam,
-                                                        const double *__restrict__ bet, double eps, int64_t rows,
+                                                        const double *__restrict__ dy, const float *__restrict__ Wo,
+                                                        const float *__restrict__ Z, const float *__restrict__ gam,
+                                                        const float *__restrict__ bet, double eps, int64_t rows,
                                                         float *__restrict__ gz, double *__restrict__ part) {
   constexpr int W = 32 * PL;
   __shared__ double sacc[8][3][W];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double pg[PL], pb[PL], pd[PL];
+  float gmf[PL], btf[PL], wo[PL][3];
 #pragma unroll
-  for (int k = 0; k < PL; ++k) pg[k] = pb[k] = pd[k] = 0.0;
+  for (int k = 0; k < PL; ++k) {
+    const int c = lane + 32 * k;
+    gmf[k] = gam[c];
+    btf[k] = bet[c];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) wo[k][f] = dy ? Wo[c * 3 + f] : 0.0f;
+  }
+  // Parameter-gradient sums: FP32 over 16 rows at a time, then FP64.
+  double pg[PL], pb[PL], pd[PL];
+  float fg[PL], fb[PL], fd[PL];
+#pragma unroll
+  for (int k = 0; k < PL; ++k) {
+    pg[k] = pb[k] = pd[k] = 0.0;
+    fg[k] = fb[k] = fd[k] = 0.0f;
+  }
+  int nrow = 0;
   for (int64_t r = (int64_t)blockIdx.x * 8 + wid; r < rows; r += (int64_t)gridDim.x * 8) {
     const float *z = Z + (size_t)r * W;
-    double zv[PL], gh[PL], s1 = 0.0, s2 = 0.0;
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      const int c = lane + 32 * k;
-      zv[k] = (double)z[c];
-      s1 += zv[k];
-      s2 += zv[k] * zv[k];
-      if (dy) {
-        gh[k] = dy[r * 3 + 0] * Wo[c * 3 + 0] + dy[r * 3 + 1] * Wo[c * 3 + 1] + dy[r * 3 + 2] * Wo[c * 3 + 2];
-      } else {
-        gh[k] = (double)dhp[(size_t)r * W + c] + (double)gres[(size_t)r * W + c];
-      }
+    float zv[PL], gh[PL], s1 = 0.0f;
+    float dy0 = 0.0f, dy1 = 0.0f, dy2 = 0.0f;
+    if (dy) {
+      dy0 = (float)dy[r * 3 + 0];
+      dy1 = (float)dy[r * 3 + 1];
+      dy2 = (float)dy[r * 3 + 2];
     }
-    s1 = warp_sum(s1);
-    s2 = warp_sum(s2);
-    const double mean = s1 / W;
-    const double var = fmax(0.0, s2 / W - mean * mean);
-    const double rs = 1.0 / sqrt(var + eps);
-    double g[PL], xh[PL], m1 = 0.0, m2 = 0.0;
 #pragma unroll
     for (int k = 0; k < PL; ++k) {
       const int c = lane + 32 * k;
+      zv[k] = z[c];
+      s1 += zv[k];
+      gh[k] = dy ? fmaf(dy0, wo[k][0], fmaf(dy1, wo[k][1], dy2 * wo[k][2]))
+                 : dhp[(size_t)r * W + c] + gres[(size_t)r * W + c];
+    }
+    const float mean = warp_sumf(s1) * (1.0f / W);
+    float s2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < PL; ++k) {
+      const float d = zv[k] - mean;
+      s2 += d * d;
+    }
+    const float rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
+    float g[PL], xh[PL], m1 = 0.0f, m2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < PL; ++k) {
       xh[k] = (zv[k] - mean) * rs;
-      const double a = (zv[k] - mean) * (rs * gam[c]) + bet[c];
-      const double da = gh[k] * (a > 0.0 ? 1.0 : exp(a));
-      pg[k] += da * xh[k];
-      pb[k] += da;
-      g[k] = da * gam[c];
+      const float a = xh[k] * gmf[k] + btf[k];
+      const float da = gh[k] * (a > 0.0f ? 1.0f : expf(a));
+      fg[k] = fmaf(da, xh[k], fg[k]);
+      fb[k] += da;
+      g[k] = da * gmf[k];
       m1 += g[k];
       m2 += g[k] * xh[k];
     }
-    m1 = warp_sum(m1) / W;
-    m2 = warp_sum(m2) / W;
+    const float mm1 = warp_sumf(m1) * (1.0f / W), mm2 = warp_sumf(m2) * (1.0f / W);
 #pragma unroll
     for (int k = 0; k < PL; ++k) {
-      const double d = rs * (g[k] - m1 - xh[k] * m2);
-      pd[k] += d;
-      gz[(size_t)r * W + lane + 32 * k] = (float)d;
+      const float d = rs * (g[k] - mm1 - xh[k] * mm2);
+      fd[k] += d;
+      gz[(size_t)r * W + lane + 32 * k] = d;
+    }
+    if (++nrow == 16) {
+      nrow = 0;
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        pg[k] += fg[k];
+        pb[k] += fb[k];
+        pd[k] += fd[k];
+        fg[k] = fb[k] = fd[k] = 0.0f;
+      }
     }
   }
 #pragma unroll
   for (int k = 0; k < PL; ++k) {
+    pg[k] += fg[k];
+    pb[k] += fb[k];
+    pd[k] += fd[k];
     sacc[wid][0][lane + 32 * k] = pg[k];
     sacc[wid][1][lane + 32 * k] = pb[k];
     sacc[wid][2][lane + 32 * k] = pd[k];
@@ -232,8 +301,8 @@ __global__ void l0_bwd_kernel(const float *__restrict__ dhp, const float *__rest
                               const float *__restrict__ Z0, size_t total, float *__restrict__ gz) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
-  const double h = tanh((double)Z0[i]);
-  gz[i] = (float)(((double)dhp[i] + (double)gres[i]) * (1.0 - h * h));
+  const float h = tanhf(Z0[i]);
+  gz[i] = (dhp[i] + gres[i]) * (1.0f - h * h);
 }
 
 // Column sums of an FP32 matrix (FP64 accumulation), first pass per block.
@@ -248,26 +317,33 @@ __global__ void colsum_f32_part_kernel(const float *__restrict__ X, int64_t rows
   }
 }
 
-// du[r][k] = sum_c dz0[r][c] W0[k][c] for the n_in inputs, one warp per row (FP64).
+// du[r][k] = sum_c dz0[r][c] W0[k][c] for the n_in inputs, one warp per row
+// (FP32 products per lane, FP64 warp sums).
 template <int PL>
-__global__ void du_kernel(const float *__restrict__ gz, const double *__restrict__ W0, int n_in, int64_t rows,
+__global__ void du_kernel(const float *__restrict__ gz, const float *__restrict__ W0, int n_in, int64_t rows,
                           double *__restrict__ du) {
   constexpr int W = 32 * PL;
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (r >= rows) return;
-  double g[PL];
+  float g[PL];
 #pragma unroll
-  for (int k = 0; k < PL; ++k) g[k] = (double)gz[(size_t)r * W + lane + 32 * k];
+  for (int k = 0; k < PL; ++k) g[k] = gz[(size_t)r * W + lane + 32 * k];
   for (int j = 0; j < kDm21InPad; ++j) {
     double s = 0.0;
     if (j < n_in) {
+      float sf = 0.0f;
 #pragma unroll
-      for (int k = 0; k < PL; ++k) s += g[k] * W0[(size_t)j * W + lane + 32 * k];
-      s = warp_sum(s);
+      for (int k = 0; k < PL; ++k) sf = fmaf(g[k], W0[(size_t)j * W + lane + 32 * k], sf);
+      s = (double)warp_sumf(sf);
     }
     if (lane == 0) du[(size_t)r * kDm21InPad + j] = s;
   }
+}
+
+__global__ void to_f32_kernel(const double *__restrict__ x, size_t n, float *__restrict__ y) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (float)x[i];
 }
 
 size_t tc_layer_offset(const MlpShape &S, int i) {
@@ -295,8 +371,12 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
   auto WRi = [&](int i) { return WR + (size_t)(i - 1) * wti; };
   auto CHi = [&](int i) { return CH + (size_t)i * ft * rc * kBlk; };
   const size_t head_off = tc_layer_offset(S, S.n_layers);
-  const double *W0 = params, *b0 = W0 + (size_t)S.n_in * Wd;
+  const double *W0 = params;
   const double *Wo = params + head_off, *bo = Wo + (size_t)Wd * S.n_out;
+  // FP32 copy of the parameters for the row kernels (FP64 -> FP32 conversions
+  // run at the FP64 rate, so they are done once per call, not per element).
+  float *pf = f32(L.pf);
+  const float *W0f = pf, *b0f = pf + (size_t)S.n_in * Wd, *Wof = pf + head_off;
   int rc_;
 #define GDFT_CK(expr, what)                                      \
   do {                                                           \
@@ -341,6 +421,11 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
   const unsigned eblocks = (unsigned)((act + 255) / 256);
 
   // ---- weights: packed once per call ----
+  {
+    const size_t n = mlp_param_count(S);
+    to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(params, n, pf);
+    GDFT_CK(cudaGetLastError(), "mlp_tc params f32");
+  }
   GDFT_CK(launch_pack_ct<double>(W0, S.n_in, Wd, Wd, ft, 1, WTi(0), st), "mlp_tc pack W0");
   for (int i = 1; i <= S.n_layers; ++i) {
     const double *Wi = params + tc_layer_offset(S, i - 1);
@@ -352,10 +437,10 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
   GDFT_CK(launch_dm21_features(feat, ehf, n_grid, np, clip, S.squash_offset, x, u, e, st), "mlp_tc features");
   GDFT_CK(launch_pack_rt<double>(u, np, S.n_in, kDm21InPad, rt, 1, PU, st), "mlp_tc pack u");
   GDFT_CK(gemm_act(PU, 1, WTi(0), 1, 1, ZF), "mlp_tc dense_0");
-  l0_fwd_kernel<<<eblocks, 256, 0, st>>>(ZF, b0, act, Wd, HF);
+  l0_fwd_kernel<<<eblocks, 256, 0, st>>>(ZF, b0f, act, Wd, HF);
   GDFT_CK(cudaGetLastError(), "mlp_tc tanh");
   for (int i = 1; i <= S.n_layers; ++i) {
-    const double *Wi = params + tc_layer_offset(S, i - 1), *bi = Wi + (size_t)Wd * Wd, *gi = bi + Wd, *bei = gi + Wd;
+    const float *Wif = pf + tc_layer_offset(S, i - 1), *bi = Wif + (size_t)Wd * Wd, *gi = bi + Wd, *bei = gi + Wd;
     GDFT_CK(launch_pack_rt<float>(HF, np, Wd, Wd, rt, kcw, PH, st), "mlp_tc pack h");
     if (dparams) GDFT_CK(launch_pack_ct<float>(HF, np, Wd, Wd, ft, rc, CHi(i - 1), st), "mlp_tc pack h^T");
     float *Zi = ZF + (size_t)i * act;
@@ -363,26 +448,28 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
     layer_fwd_kernel<PL><<<wblocks, 256, 0, st>>>(Zi, bi, HF, gi, bei, S.ln_eps, np);
     GDFT_CK(cudaGetLastError(), "mlp_tc layernorm");
   }
-  const unsigned hblocks = (unsigned)((np + 7) / 8);
-  head_kernel<PL><<<hblocks, 256, 0, st>>>(HF, Wo, bo, e, w, n_grid, np, clip, S.sigmoid_scale, dy, de, epart);
+  const unsigned hblocks = (unsigned)((np + 255) / 256);
+  float *dyf = f32(L.dyf);
+  head_kernel<PL><<<hblocks, 256, 0, st>>>(HF, Wof, bo, e, w, n_grid, np, clip, S.sigmoid_scale, dy, dyf, de,
+                                           epart);
   GDFT_CK(cudaGetLastError(), "mlp_tc head");
   GDFT_CK(launch_energy_reduce(epart, (int)hblocks, exc, st), "mlp_tc energy_reduce");
   if (coef == nullptr && dparams == nullptr) return GDFT_OK;
 
   // ---- backward ----
   if (dparams) {
-    head_wgrad_part_kernel<<<kColBlocks, 256, 0, st>>>(HF, dy, np, Wd, colpart);
+    head_wgrad_part_kernel<<<kColBlocks, 256, 0, st>>>(HF, dyf, dy, np, Wd, colpart);
     colsum_final_kernel<<<(3 * Wd + 3 + 255) / 256, 256, 0, st>>>(colpart, kColBlocks, 3 * Wd + 3,
                                                                   dparams + head_off);
     GDFT_CK(cudaGetLastError(), "mlp_tc head wgrad");
   }
   float *gz_cur = GZ, *gz_prev = GZ + act;
   for (int i = S.n_layers; i >= 1; --i) {
-    const double *Wi = params + tc_layer_offset(S, i - 1), *gi = Wi + (size_t)Wd * Wd + Wd, *bei = gi + Wd;
+    const float *Wif = pf + tc_layer_offset(S, i - 1), *gi = Wif + (size_t)Wd * Wd + Wd, *bei = gi + Wd;
     const float *Zi = ZF + (size_t)i * act;
     const bool last = i == S.n_layers;
     layer_bwd_kernel<PL><<<kLnBlocks, 256, 0, st>>>(last ? nullptr : DHP, last ? nullptr : gz_prev,
-                                                    last ? dy : nullptr, Wo, Zi, gi, bei, S.ln_eps, np, gz_cur,
+                                                    last ? dy : nullptr, Wof, Zi, gi, bei, S.ln_eps, np, gz_cur,
                                                     lnpart);
     GDFT_CK(cudaGetLastError(), "mlp_tc layernorm bwd");
     GDFT_CK(launch_pack_rt<float>(gz_cur, np, Wd, Wd, rt, kcw, PG, st), "mlp_tc pack dz");
@@ -417,7 +504,7 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
     GDFT_CK(cudaGetLastError(), "mlp_tc db0");
   }
   if (coef) {
-    du_kernel<PL><<<wblocks, 256, 0, st>>>(gz_cur, W0, S.n_in, np, du);
+    du_kernel<PL><<<wblocks, 256, 0, st>>>(gz_cur, W0f, S.n_in, np, du);
     GDFT_CK(cudaGetLastError(), "mlp_tc du");
     GDFT_CK(launch_dm21_potentials(feat, x, du, de, n_grid, np, clip, S.squash_offset, coef, st),
             "mlp_tc potentials");
@@ -449,11 +536,13 @@ MlpTcLayout mlp_tc_layout(const MlpShape &s, int64_t np) {
   L.dy = take((size_t)np * 3 * 8);
   L.de = take((size_t)np * 3 * 8);
   L.du = take((size_t)np * kDm21InPad * 8);
-  L.epart = take((size_t)((np + 7) / 8) * 8);
+  L.epart = take((size_t)((np + 255) / 256) * 8);
   L.kpart = take((size_t)L.nsplit * W * W * 8);
   L.lnpart = take((size_t)kLnBlocks * 3 * W * 8);
   L.colpart = take((size_t)kColBlocks * (3 * W + 3) * 8);
   L.colpart2 = take((size_t)3 * W * 8);
+  L.pf = take(mlp_param_count(s) * 4);
+  L.dyf = take((size_t)np * 3 * 4);
   L.pu = take((size_t)rt * kBlk * 4);
   L.cu = take((size_t)rc * kBlk * 4);
   L.wt = take(((size_t)ft * kBlk + (size_t)s.n_layers * ft * kcw * kBlk) * 4);

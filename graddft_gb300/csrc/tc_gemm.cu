@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
           float *row = A.out32 + (size_t)m * A.ldo + nt * 128 + c;
 #pragma unroll
           for (int i = 0; i < 32; ++i)
-            if (nt * 128 + c + i < A.n_valid) row[i] = have ? (float)((double)sv[i] - (double)cv[i]) : 0.0f;
+            if (nt * 128 + c + i < A.n_valid) row[i] = have ? sv[i] - cv[i] : 0.0f;
         } else {
           double *row = A.out64 + ((size_t)blockIdx.y * A.m_valid + m) * A.n_valid + nt * 128 + c;
 #pragma unroll
@@ -222,12 +222,19 @@ namespace gdft {
 
 namespace {
 
-template <class T>
-__device__ __forceinline__ void split4(const T (&v)[4], float4 &h, float4 &l) {
-  umma::split_tf32((double)v[0], h.x, l.x);
-  umma::split_tf32((double)v[1], h.y, l.y);
-  umma::split_tf32((double)v[2], h.z, l.z);
-  umma::split_tf32((double)v[3], h.w, l.w);
+// TF32 hi/lo split: FP64 sources through FP64 (22 of their 53 bits kept),
+// FP32 sources in FP32 arithmetic (exact: x - hi is representable).
+__device__ __forceinline__ void split4(const double (&v)[4], float4 &h, float4 &l) {
+  umma::split_tf32(v[0], h.x, l.x);
+  umma::split_tf32(v[1], h.y, l.y);
+  umma::split_tf32(v[2], h.z, l.z);
+  umma::split_tf32(v[3], h.w, l.w);
+}
+__device__ __forceinline__ void split4(const float (&v)[4], float4 &h, float4 &l) {
+  umma::split_tf32f(v[0], h.x, l.x);
+  umma::split_tf32f(v[1], h.y, l.y);
+  umma::split_tf32f(v[2], h.z, l.z);
+  umma::split_tf32f(v[3], h.w, l.w);
 }
 
 // One CTA per block pair; 256 threads, each 4 (row, 4-wide k group) items.
