@@ -245,6 +245,7 @@ static size_t neural_ws_bytes(const gdft_molecule *mol, const gdft_network *net)
   return ws_layout(mol).bytes + f64;
 }
 static size_t hvp_ws_bytes(const gdft_molecule *mol, const gdft_network *net) {
+  if (net->precision == GDFT_TF32X3) return ws_layout(mol).bytes + mlp_hvp_tc_layout(net_shape(net), mol->n_grid_pad).bytes;
   return ws_layout(mol).bytes + align256(mlp_hvp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
 }
 
@@ -645,12 +646,14 @@ int gdft_neural_xc_hvp(const gdft_molecule *mol, const double *d_rdm1, const gdf
   char *ws = (char *)d_ws;
   const WsLayout W = ws_layout(mol);
   const MlpShape S = net_shape(net);
-  const MlpHvpLayout H = mlp_hvp_layout(S, mol->n_grid_pad);
-  double *hws = (double *)(ws + W.bytes);
+  const bool tc = net->precision == GDFT_TF32X3;
+  char *hws = ws + W.bytes;
+  double *featp = (double *)(hws + (tc ? mlp_hvp_tc_layout(S, mol->n_grid_pad).featp
+                                       : mlp_hvp_layout(S, mol->n_grid_pad).featp * sizeof(double)));
   double *feat = (double *)(ws + W.off_feat);
   // Features of D (kept in the second-order scratch), then of the tangent G.
   if ((rc = run_density(mol, d_rdm1, ws, st))) return rc;
-  if ((rc = check_cuda(cudaMemcpyAsync(hws + H.featp, feat, (size_t)2 * kFeat * mol->n_grid_pad * sizeof(double),
+  if ((rc = check_cuda(cudaMemcpyAsync(featp, feat, (size_t)2 * kFeat * mol->n_grid_pad * sizeof(double),
                                        cudaMemcpyDeviceToDevice, st),
                        "hvp feature copy")))
     return rc;
@@ -658,8 +661,12 @@ int gdft_neural_xc_hvp(const gdft_molecule *mol, const double *d_rdm1, const gdf
   double *coef = d_hrdm1 ? (double *)(ws + W.off_coef) : nullptr;
   {
     StageTimer tm(GDFT_STAGE_MLP, st);
-    rc = mlp_hvp_f64(S, d_params, d_hparams, hws + H.featp, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
-                     net->clip, hws, d_value, coef, st);
+    if (tc)
+      rc = mlp_hvp_tc(S, d_params, d_hparams, featp, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
+                      net->clip, hws, d_value, coef, (int *)(ws + W.off_err), st);
+    else
+      rc = mlp_hvp_f64(S, d_params, d_hparams, featp, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
+                       net->clip, (double *)hws, d_value, coef, st);
     if (rc) return rc;
   }
   if (d_hrdm1 == nullptr) return GDFT_OK;

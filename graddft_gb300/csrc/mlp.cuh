@@ -77,6 +77,29 @@ int mlp_run_tc(const MlpShape &S, const double *params, double *dparams, const d
                const double *w, int64_t n_grid, int64_t np, double clip, char *ws, double *exc, double *coef, int *err,
                cudaStream_t st);
 
+// Per-point pieces of the second-order pass shared by its FP64 and mixed forms:
+// primal/tangent inputs (u stacked [2][np][16]) and energy densities, and the
+// V-contraction coefficients from [dL/du; dL/du~] (GU) and dL/de (ge [np][2]).
+cudaError_t launch_features_tan(const double *featp, const double *featt, const double *ehf, int64_t n_grid,
+                                int64_t np, double clip, double off, double *x, double *xt, double *u, double *e,
+                                double *et, cudaStream_t st);
+cudaError_t launch_hvp_potentials(const double *featp, const double *featt, const double *x, const double *xt,
+                                  const double *GU, const double *ge, int64_t n_grid, int64_t np, double clip,
+                                  double off, double *coef, cudaStream_t st);
+
+// Mixed form of mlp_hvp_f64 (tensor-core GEMMs over the stacked 2 np rows,
+// FP32 activations and row statistics, FP64 sums over grid points).
+struct MlpHvpTcLayout {
+  size_t bytes;
+  size_t featp, x, xt, u, e, et, gy, ge, gu, lpart, kpart, lnpart, colpart, colpart2;  // FP64 (byte offsets)
+  size_t pf, gyf, pu, cu, wt, wr, z, h, ph, ch, gz, dhp, pg, cg;                    // FP32 (byte offsets)
+  int nsplit;
+};
+MlpHvpTcLayout mlp_hvp_tc_layout(const MlpShape &s, int64_t np);
+int mlp_hvp_tc(const MlpShape &S, const double *params, double *dparams, const double *featp, const double *featt,
+               const double *ehf, const double *w, int64_t n_grid, int64_t np, double clip, char *ws, double *lval,
+               double *coef, int *err, cudaStream_t st);
+
 // The 11 network inputs (grid x 11) and the 3 energy densities (grid x 3) of
 // the DM21 functional from the density features; scratch in ws.
 int mlp_inputs_f64(const MlpShape &S, const double *feat, const double *ehf, int64_t n_grid, int64_t np,

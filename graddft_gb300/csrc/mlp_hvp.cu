@@ -439,6 +439,22 @@ size_t hvp_layer_offset(const MlpShape &S, int i) {
 
 }  // namespace
 
+cudaError_t launch_features_tan(const double *featp, const double *featt, const double *ehf, int64_t n_grid,
+                                int64_t np, double clip, double off, double *x, double *xt, double *u, double *e,
+                                double *et, cudaStream_t st) {
+  features_tan_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(featp, featt, ehf, n_grid, np, clip, off, x, xt,
+                                                                   u, e, et);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hvp_potentials(const double *featp, const double *featt, const double *x, const double *xt,
+                                  const double *GU, const double *ge, int64_t n_grid, int64_t np, double clip,
+                                  double off, double *coef, cudaStream_t st) {
+  hvp_potentials_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(featp, featt, x, xt, GU, ge, n_grid, np, clip,
+                                                                     off, coef);
+  return cudaGetLastError();
+}
+
 MlpHvpLayout mlp_hvp_layout(const MlpShape &s, int64_t np) {
   MlpHvpLayout L;
   const size_t act2 = 2 * (size_t)np * s.width;

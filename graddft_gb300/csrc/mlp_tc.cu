@@ -23,14 +23,6 @@ namespace {
 
 constexpr size_t kBlk = 2 * (umma::kBlockBytes / 4);  // floats in one packed hi|lo block pair
 
-__device__ __forceinline__ float eluf(float a) { return a > 0.0f ? a : expm1f(a); }
-
-__device__ __forceinline__ float warp_sumf(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 // Per-element arithmetic and per-row statistics of these row kernels are FP32
 // (GB300's FP64 rate is a small fraction of its FP32 rate, and the activations
 // are FP32); long accumulations over grid points and the energy stay FP64.
@@ -156,40 +148,6 @@ __global__ void __launch_bounds__(256) head_kernel(const float *__restrict__ H, 
   }
 }
 
-// Head weight gradients: part[block][c][0..2] = sum_r h[r][c] dy[r][f] over the
-// block's row range, part[block][W*3 + f] = sum_r dy[r][f]; one thread per column.
-__global__ void head_wgrad_part_kernel(const float *__restrict__ H, const float *__restrict__ dyf,
-                                       const double *__restrict__ dy, int64_t rows, int width,
-                                       double *__restrict__ part) {
-  const int64_t chunk = (rows + gridDim.x - 1) / gridDim.x;
-  const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
-  double *pb = part + (size_t)blockIdx.x * (3 * width + 3);
-  for (int c = threadIdx.x; c < width; c += blockDim.x) {
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    for (int64_t rb = r0; rb < r1; rb += 16) {  // FP32 over 16 rows, FP64 across
-      float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
-      const int64_t re = rb + 16 < r1 ? rb + 16 : r1;
-      for (int64_t r = rb; r < re; ++r) {
-        const float hv = H[(size_t)r * width + c];
-        f0 = fmaf(hv, dyf[r * 3 + 0], f0);
-        f1 = fmaf(hv, dyf[r * 3 + 1], f1);
-        f2 = fmaf(hv, dyf[r * 3 + 2], f2);
-      }
-      a0 += f0;
-      a1 += f1;
-      a2 += f2;
-    }
-    pb[c * 3 + 0] = a0;
-    pb[c * 3 + 1] = a1;
-    pb[c * 3 + 2] = a2;
-  }
-  if (threadIdx.x < 3) {
-    double s = 0.0;
-    for (int64_t r = r0; r < r1; ++r) s += dy[r * 3 + threadIdx.x];
-    pb[3 * width + threadIdx.x] = s;
-  }
-}
-
 // Reverse of a residual layer, one warp per row.  The incoming dE/dh is
 // dy W_out^T (last layer: dy != null) or dhp + gres (the GEMM output plus the
 // residual branch of the layer above).  Writes dE/dz (FP32) and per-block
@@ -305,47 +263,6 @@ __global__ void l0_bwd_kernel(const float *__restrict__ dhp, const float *__rest
   gz[i] = (dhp[i] + gres[i]) * (1.0f - h * h);
 }
 
-// Column sums of an FP32 matrix (FP64 accumulation), first pass per block.
-__global__ void colsum_f32_part_kernel(const float *__restrict__ X, int64_t rows, int ncols,
-                                       double *__restrict__ part) {
-  const int64_t chunk = (rows + gridDim.x - 1) / gridDim.x;
-  const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
-  for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
-    double s = 0.0;
-    for (int64_t r = r0; r < r1; ++r) s += (double)X[(size_t)r * ncols + c];
-    part[(size_t)blockIdx.x * ncols + c] = s;
-  }
-}
-
-// du[r][k] = sum_c dz0[r][c] W0[k][c] for the n_in inputs, one warp per row
-// (FP32 products per lane, FP64 warp sums).
-template <int PL>
-__global__ void du_kernel(const float *__restrict__ gz, const float *__restrict__ W0, int n_in, int64_t rows,
-                          double *__restrict__ du) {
-  constexpr int W = 32 * PL;
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (r >= rows) return;
-  float g[PL];
-#pragma unroll
-  for (int k = 0; k < PL; ++k) g[k] = gz[(size_t)r * W + lane + 32 * k];
-  for (int j = 0; j < kDm21InPad; ++j) {
-    double s = 0.0;
-    if (j < n_in) {
-      float sf = 0.0f;
-#pragma unroll
-      for (int k = 0; k < PL; ++k) sf = fmaf(g[k], W0[(size_t)j * W + lane + 32 * k], sf);
-      s = (double)warp_sumf(sf);
-    }
-    if (lane == 0) du[(size_t)r * kDm21InPad + j] = s;
-  }
-}
-
-__global__ void to_f32_kernel(const double *__restrict__ x, size_t n, float *__restrict__ y) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = (float)x[i];
-}
-
 size_t tc_layer_offset(const MlpShape &S, int i) {
   return (size_t)S.n_in * S.width + S.width + (size_t)i * ((size_t)S.width * S.width + 3 * (size_t)S.width);
 }
@@ -458,7 +375,7 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
 
   // ---- backward ----
   if (dparams) {
-    head_wgrad_part_kernel<<<kColBlocks, 256, 0, st>>>(HF, dyf, dy, np, Wd, colpart);
+    head_wgrad_part_kernel<<<kColBlocks, 256, 0, st>>>(HF, dyf, dy, np, np, Wd, colpart);
     colsum_final_kernel<<<(3 * Wd + 3 + 255) / 256, 256, 0, st>>>(colpart, kColBlocks, 3 * Wd + 3,
                                                                   dparams + head_off);
     GDFT_CK(cudaGetLastError(), "mlp_tc head wgrad");

@@ -147,3 +147,60 @@ def test_scf_loop_vs_oracle(G):
         for leaf, g in d.items():
             err = _rel(leaves[mod][leaf].grad, g)
             assert err <= 1e-7, (mod, leaf, err)
+
+
+@pytest.mark.parametrize("mol_prec", ["fp64", "tf32x3"])
+def test_hvp_tensor_core_vs_fp64(G, mol_prec):
+    """The mixed (tensor-core) second-order pass against the FP64 one."""
+    wl, ao, g1, g2, ehf = _case(n_grid=8192, n_ao=48, n_occ=6, seed=71)
+    mol = _molecule(G, ao, g1, g2, wl.weights, wl.rdm1, ehf, precision=mol_prec)
+    r = mol.resident()
+    tangent = _t(np.random.default_rng(7).standard_normal(wl.rdm1.shape))
+    out = {}
+    for prec in ("fp64", "tf32x3"):
+        f = _dm21(G)
+        f.precision = prec
+        net = f.network()
+        flat = net.flatten(_params(12), r.device)
+        L, hD, hp = r.neural_xc_hvp(mol._rdm1(), net, flat, mol.ehf, tangent, want_value=True)
+        out[prec] = (float(L), hD, net.unflatten(hp))
+    assert r.status() == 0
+    (L64, hD64, hp64), (Ltc, hDtc, hptc) = out["fp64"], out["tf32x3"]
+    print("L", L64, "rel dL", abs(Ltc - L64) / abs(L64), "rel dD", _rel(hDtc, hD64.cpu().numpy()))
+    assert abs(Ltc - L64) <= 1e-5 * abs(L64)
+    assert _rel(hDtc, hD64.cpu().numpy()) <= 1e-4
+    worst = 0.0
+    for mod, d in hp64["params"].items():
+        for leaf, g in d.items():
+            worst = max(worst, _rel(hptc["params"][mod][leaf], g.cpu().numpy()))
+    print("worst rel dtheta", worst)
+    assert worst <= 1e-3
+
+
+def test_scf_loop_mixed_vs_oracle(G):
+    """The SCF loop with TF32x3 contractions and the tensor-core network (forward and second order)."""
+    n_ao, n_occ, cycles, mix = 24, 4, 3, 0.3
+    wl, ao, g1, g2, _ = _case(n_grid=1024, n_ao=n_ao, n_occ=n_occ, seed=3)
+    sysm = synthetic.make_scf_system(n_ao, n_occ, naux=64, seed=1)
+    rho = np.einsum("sab,ra,rb->rs", sysm.rdm1, ao, ao)
+    ehf = synthetic.make_ehf(wl.n_grid, 5, rho, 2)
+    params = synthetic.glorot_params(seed=2)
+    from oracle import scf as OS
+
+    e_ref, g_ref, _ = OS.scf_energy_and_grads(params, ao, g1, g2, wl.weights, ehf, sysm.h1e, sysm.s1e,
+                                              sysm.df_tensor, sysm.nuclear_repulsion, sysm.rdm1, sysm.mo_occ,
+                                              cycles, mix)
+    mol = _molecule(G, ao, g1, g2, wl.weights, sysm.rdm1, ehf, precision="tf32x3",
+                    df_tensor=_t(sysm.df_tensor)).replace(
+        h1e=_t(sysm.h1e), s1e=_t(sysm.s1e), nuclear_repulsion=_t(sysm.nuclear_repulsion), mo_occ=_t(sysm.mo_occ))
+    tp = _params(2)
+    leaves = {k: {kk: t.cuda().requires_grad_(True) for kk, t in d.items()} for k, d in tp["params"].items()}
+    f = _dm21(G)
+    f.precision = "tf32x3"
+    out = G.diff_simple_scf_loop(f, cycles=cycles, mixing_factor=mix)({"params": leaves}, mol)
+    out.energy.backward()
+    de = abs(float(out.energy.detach()) - e_ref)
+    worst = max(_rel(leaves[m][l].grad, g) for m, d in g_ref["params"].items() for l, g in d.items())
+    print("|dE|", de, "worst rel dtheta", worst)
+    assert de <= 1e-6 * abs(e_ref)
+    assert worst <= 1e-3
