@@ -319,6 +319,90 @@ def run_neural(args):
     print(json.dumps(line), flush=True)
 
 
+SCF_WORKLOAD = ("differentiable SCF loop: n_ao 256, n_grid 2^19, 20 iterations, linear mixing 0.3, "
+                "H eigenvalues U[-20, 5] Ha, S = I + 0.05 SPD, density-fitting J (naux 768), DM21-style network; "
+                "forward loop + backward dE/dtheta through all iterations")
+
+
+def run_scf(args):
+    """Differentiable SCF loop (config 5 shape): loops/s, and dE/dtheta vs the FP64 form."""
+    import torch
+
+    import graddft_gb300 as G
+    from graddft_gb300 import _lib, build, synthetic
+
+    build.build()
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    n_grid = args.n_grid if args.n_grid != N_GRID else 1 << 19
+    n_ao = args.n_ao if args.n_ao != N_AO else 256
+    n_occ, cycles, mix = max(1, n_ao // 8), args.cycles, 0.3
+    wl = synthetic.make_workload(n_grid, n_ao, n_occ, SEED)
+    sysm = synthetic.make_scf_system(n_ao, n_occ, naux=768, seed=SEED)
+    params = synthetic.glorot_params(seed=SEED)
+    t = lambda x: torch.as_tensor(x, dtype=torch.float64, device=dev)  # noqa: E731
+
+    def molecule(prec):
+        r = G.engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, prec, dev)
+        mol = G.Molecule(grid=G.Grid(coords=None, weights=t(wl.weights)), atom_index=None, nuclear_pos=None,
+                         ao=None, grad_ao=None, grad_n_ao=None, rdm1=t(sysm.rdm1), nuclear_repulsion=t(
+                             sysm.nuclear_repulsion), h1e=t(sysm.h1e), vj=None, mo_coeff=None, mo_occ=t(sysm.mo_occ),
+                         mo_energy=None, s1e=t(sysm.s1e), df_tensor=t(sysm.df_tensor), precision=prec, _resident=r)
+        rho = r.density(t(sysm.rdm1), want=("rho",))["rho"].cpu().numpy()
+        return mol.replace(ehf=t(synthetic.make_ehf(n_grid, SEED, rho, 2)))
+
+    def run(mol, prec):
+        hf = lambda atoms, *_, **__: atoms.ehf  # noqa: E731
+        f = G.DM21(densitygrads=None, coefficient_input_grads=None, nograd_densities=hf,
+                   nograd_coefficient_inputs=hf, precision=prec)
+        leaves = {k: {kk: t(v).requires_grad_(True) for kk, v in d.items()} for k, d in params["params"].items()}
+        out = G.diff_simple_scf_loop(f, cycles=cycles, mixing_factor=mix)({"params": leaves}, mol)
+        out.energy.backward()
+        return float(out.energy.detach()), leaves
+
+    mol = molecule("tf32x3")
+    for _ in range(max(1, args.warmup // 3)):
+        run(mol, "tf32x3")
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 3))
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            e_tc, g_tc = run(mol, "tf32x3")
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    line = {
+        "metric": "differentiable SCF loops/s (forward + dE/dtheta through all iterations)", "value": 1e3 / ms,
+        "unit": "loops/s", "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup // 3), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3",
+        "data": "synthetic (seeded basis, H, S, density-fitting tensor)",
+        "config": {"workload": SCF_WORKLOAD if (n_grid, n_ao, cycles) == (1 << 19, 256, 20) else
+                   f"differentiable SCF loop, n_ao {n_ao}, n_grid {n_grid}, {cycles} iterations",
+                   "n_ao": n_ao, "n_grid": n_grid, "cycles": cycles, "mixing": mix, "naux": 768,
+                   "eigensolver": "FP64 generalized eigh (cuSOLVER through torch), Lorentzian-broadened reverse"},
+        "grid_pts_per_s": n_grid * (cycles + 1) / (ms * 1e-3), "energy": e_tc, "clocks": clk.summary(),
+    }
+    if not args.no_fp64:
+        del mol
+        torch.cuda.empty_cache()
+        mol64 = molecule("fp64")
+        torch.cuda.synchronize()
+        e0.record(stream)
+        e_64, g_64 = run(mol64, "fp64")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        worst = max(float((g_tc[m][l].grad - g.grad).abs().max()) / max(float(g.grad.abs().max()), 1e-300)
+                    for m, d in g_64.items() for l, g in d.items())
+        line.update({"fp64_form_ms_per_step": e0.elapsed_time(e1), "mixed_over_fp64": e0.elapsed_time(e1) / ms,
+                     "accuracy_vs_fp64": {"energy": e_64, "abs_dE": abs(e_tc - e_64),
+                                          "max_rel_dtheta_per_leaf": worst}})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -333,13 +417,17 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
-    ap.add_argument("--workload", default="xc", choices=["xc", "neural"],
-                    help="xc: B88+LYP contraction benchmark (headline); neural: DM21-style network fwd+bwd")
+    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf"],
+                    help="xc: B88+LYP contraction benchmark (headline); neural: DM21-style network fwd+bwd; "
+                         "scf: differentiable SCF loop")
+    ap.add_argument("--cycles", type=int, default=20, help="SCF iterations (--workload scf)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "neural":
         return run_neural(args)
+    if args.workload == "scf":
+        return run_scf(args)
 
     import torch
 
