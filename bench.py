@@ -403,6 +403,120 @@ def run_scf(args):
     print(json.dumps(line), flush=True)
 
 
+BATCH_WORKLOAD = ("batched ragged training step: 64 synthetic molecules, n_ao ~ U[24, 400], n_grid = 150 n_ao "
+                  "(rounded to 128), DM21-style network, loss sum_m (E_m - E_ref_m)^2, fwd+bwd (dloss/dtheta, "
+                  "dloss/dD_m); one captured CUDA graph vs one molecule at a time")
+
+
+def run_batch(args):
+    """Config-4 shape at a tenth of its grid: batched graph replay vs one molecule at a time."""
+    import ctypes
+
+    import torch
+
+    import graddft_gb300 as G
+    from graddft_gb300 import _lib, build, engine, synthetic
+    from graddft_gb300.batch import NeuralBatch
+
+    build.build()
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(SEED)
+    n_mol = args.n_mol
+    naos = rng.integers(24, 401, size=n_mol)
+    pts_per_ao = args.points_per_ao
+    t = lambda x: torch.as_tensor(x, dtype=torch.float64, device=dev)  # noqa: E731
+    mols = []
+    for i, n_ao in enumerate(naos):
+        n_grid = int(round(pts_per_ao * n_ao / 128.0)) * 128
+        wl = synthetic.make_workload(n_grid, int(n_ao), max(1, int(n_ao) // 8), seed=SEED + 1 + i)
+        r = engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "tf32x3", dev)
+        rho = r.density(t(wl.rdm1), want=("rho",))["rho"].cpu().numpy()
+        mols.append(G.Molecule(grid=G.Grid(coords=None, weights=t(wl.weights)), atom_index=None, nuclear_pos=None,
+                               ao=None, grad_ao=None, grad_n_ao=None, rdm1=t(wl.rdm1), nuclear_repulsion=0.0,
+                               h1e=None, vj=None, mo_coeff=None, mo_occ=None, mo_energy=None,
+                               ehf=t(synthetic.make_ehf(n_grid, SEED + 100 + i, rho, 2)), precision="tf32x3",
+                               _resident=r))
+    hf = lambda atoms, *_, **__: atoms.ehf  # noqa: E731
+    f = G.DM21(densitygrads=None, coefficient_input_grads=None, nograd_densities=hf, nograd_coefficient_inputs=hf,
+               precision="tf32x3")
+    params = f.init(SEED)
+    b = NeuralBatch(mols, f)
+    e_ref = torch.zeros(n_mol, dtype=torch.float64)
+    b.step(params, eref=e_ref)
+    e_ref = (b.energies.cpu() + 0.01 * torch.randn(n_mol, dtype=torch.float64,
+                                                   generator=torch.Generator().manual_seed(SEED)))
+    b.set_inputs(eref=e_ref)
+    b.capture()
+    for _ in range(args.warmup):
+        b.replay()
+    torch.cuda.synchronize()
+    b.status()
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            b.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms_batch = e0.elapsed_time(e1) / args.steps
+    n_pts = b.n_points
+
+    # One molecule at a time through the same library entry, one shared workspace.
+    net = f.network()
+    flat = net.flatten(params, dev)
+    wsb = max(ctypes.c_size_t(0).value, 0)
+    for m in mols:
+        nb = ctypes.c_size_t()
+        _lib.check(lib.gdft_neural_workspace_bytes(ctypes.byref(m.resident().desc), ctypes.byref(net.desc),
+                                                   ctypes.byref(nb)))
+        wsb = max(wsb, nb.value)
+    del b
+    torch.cuda.empty_cache()
+    ws = torch.zeros(wsb, dtype=torch.uint8, device=dev)
+    exc = torch.empty(n_mol, dtype=torch.float64, device=dev)
+    vx = [torch.empty((2, m.resident().n_ao, m.resident().n_ao), dtype=torch.float64, device=dev) for m in mols]
+    dps = torch.empty((n_mol, net.n_params), dtype=torch.float64, device=dev)
+    rd = [m._rdm1() for m in mols]
+
+    def seq_step():
+        for i, m in enumerate(mols):
+            r = m.resident()
+            _lib.check(lib.gdft_neural_xc_energy_and_grads(
+                ctypes.byref(r.desc), engine._ptr(rd[i]), ctypes.byref(net.desc), engine._ptr(flat),
+                engine._ptr(m.ehf), ctypes.c_void_p(exc.data_ptr() + 8 * i), engine._ptr(vx[i]),
+                ctypes.c_void_p(dps[i].data_ptr()), engine._ptr(ws), ws.numel(), engine._stream(dev)))
+        g = 2.0 * (exc - e_ref.to(dev))
+        return (g[:, None] * dps).sum(0)
+
+    for _ in range(max(1, args.warmup // 3)):
+        seq_step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(max(1, args.steps // 2)):
+        seq_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1) / max(1, args.steps // 2)
+    line = {
+        "metric": "batched training step molecules/s (one CUDA graph) vs one molecule at a time",
+        "value": n_mol / (ms_batch * 1e-3), "unit": "molecules/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "tf32x3", "data": "synthetic (seeded basis per molecule)",
+        "config": {"workload": BATCH_WORKLOAD if (n_mol, pts_per_ao) == (64, 150) else
+                   f"batched step, {n_mol} molecules, n_grid = {pts_per_ao} n_ao", "n_mol": n_mol,
+                   "n_ao_range": [int(naos.min()), int(naos.max())], "grid_points_total": n_pts,
+                   "grid_scale": "150 points per AO (the full 1500 per AO needs ~620 GB of resident AO tables)"},
+        "grid_pts_per_s": n_pts / (ms_batch * 1e-3),
+        "one_at_a_time": {"ms_per_step": ms_seq, "molecules_per_s": n_mol / (ms_seq * 1e-3),
+                          "grid_pts_per_s": n_pts / (ms_seq * 1e-3)},
+        "batched_over_one_at_a_time": ms_seq / ms_batch, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -417,9 +531,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
-    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf"],
+    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch"],
                     help="xc: B88+LYP contraction benchmark (headline); neural: DM21-style network fwd+bwd; "
-                         "scf: differentiable SCF loop")
+                         "scf: differentiable SCF loop; batch: many molecules per step")
+    ap.add_argument("--n-mol", type=int, default=64, help="molecules (--workload batch)")
+    ap.add_argument("--points-per-ao", type=int, default=150, help="grid points per AO (--workload batch)")
     ap.add_argument("--cycles", type=int, default=20, help="SCF iterations (--workload scf)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -428,6 +544,8 @@ def main():
         return run_neural(args)
     if args.workload == "scf":
         return run_scf(args)
+    if args.workload == "batch":
+        return run_batch(args)
 
     import torch
 

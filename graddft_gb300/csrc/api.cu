@@ -237,16 +237,68 @@ static MlpShape net_shape(const gdft_network *net) {
 
 // The network scratch follows the contraction workspace.
 static size_t neural_ws_bytes(const gdft_molecule *mol, const gdft_network *net) {
-  const size_t f64 = align256(mlp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
-  if (net->precision == GDFT_TF32X3) {
-    const size_t tc = mlp_tc_layout(net_shape(net), mol->n_grid_pad).bytes;
-    return ws_layout(mol).bytes + (tc > f64 ? tc : f64);
-  }
-  return ws_layout(mol).bytes + f64;
+  // The TF32x3 scratch also holds what gdft_neural_inputs writes there (the
+  // FP64 layout's leading x, u, e arrays, 30 doubles per point).
+  if (net->precision == GDFT_TF32X3) return ws_layout(mol).bytes + mlp_tc_layout(net_shape(net), mol->n_grid_pad).bytes;
+  return ws_layout(mol).bytes + align256(mlp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
 }
 static size_t hvp_ws_bytes(const gdft_molecule *mol, const gdft_network *net) {
   if (net->precision == GDFT_TF32X3) return ws_layout(mol).bytes + mlp_hvp_tc_layout(net_shape(net), mol->n_grid_pad).bytes;
   return ws_layout(mol).bytes + align256(mlp_hvp_layout(net_shape(net), mol->n_grid_pad).doubles * sizeof(double));
+}
+
+// Segment offsets travel to the device as a kernel argument (captured by value
+// in a CUDA graph, no host buffer involved).
+constexpr int kBatchMax = 256;
+struct SegTable {
+  int64_t off[kBatchMax + 1];
+};
+__global__ void write_seg_kernel(const SegTable t, int n, int64_t *__restrict__ out) {
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) out[i] = t.off[i];
+}
+
+// Batch workspace: each molecule's own workspace, then the concatenated point
+// arrays (segments padded to 256 rows) and the network scratch.
+struct BatchLayout {
+  size_t mol_off[kBatchMax];
+  int64_t seg[kBatchMax + 1];
+  int64_t npt;
+  size_t off_feat, off_w, off_ehf, off_coef, off_seg, off_cot, off_net, bytes;
+};
+
+static int batch_layout(int n_mol, const gdft_molecule *mols, const gdft_network *net, BatchLayout *B) {
+  if (n_mol < 1 || n_mol > kBatchMax || mols == nullptr) {
+    set_error("batch of %d molecules (1..%d supported)", n_mol, kBatchMax);
+    return GDFT_ERR_INVALID;
+  }
+  size_t off = 0;
+  int64_t npt = 0;
+  for (int m = 0; m < n_mol; ++m) {
+    int rc = check_mol(&mols[m]);
+    if (rc) return rc;
+    B->mol_off[m] = off;
+    off += align256(ws_layout(&mols[m]).bytes);
+    B->seg[m] = npt;
+    npt += round_up(mols[m].n_grid_pad, 256);
+  }
+  B->seg[n_mol] = npt;
+  B->npt = npt;
+  B->off_feat = off;
+  off += align256((size_t)2 * kFeat * npt * 8);
+  B->off_w = off;
+  off += align256((size_t)npt * 8);
+  B->off_ehf = off;
+  off += align256((size_t)4 * npt * 8);
+  B->off_coef = off;
+  off += align256((size_t)2 * kFeat * npt * 8);
+  B->off_seg = off;
+  off += align256((size_t)(n_mol + 1) * 8);
+  B->off_cot = off;
+  off += align256((size_t)n_mol * 8);
+  B->off_net = off;
+  off += mlp_tc_layout(net_shape(net), npt).bytes;
+  B->bytes = off;
+  return GDFT_OK;
 }
 
 // Density stage into ws.feat.
@@ -671,6 +723,100 @@ int gdft_neural_xc_hvp(const gdft_molecule *mol, const double *d_rdm1, const gdf
   }
   if (d_hrdm1 == nullptr) return GDFT_OK;
   return run_vxc(mol, coef, d_hrdm1, ws, st);
+}
+
+int gdft_neural_batch_workspace_bytes(int32_t n_mol, const gdft_molecule *mols, const gdft_network *net,
+                                      size_t *bytes) {
+  int rc = check_network(net);
+  if (rc) return rc;
+  if (bytes == nullptr) {
+    set_error("gdft_neural_batch_workspace_bytes: null output");
+    return GDFT_ERR_INVALID;
+  }
+  static thread_local BatchLayout B;
+  if ((rc = batch_layout(n_mol, mols, net, &B))) return rc;
+  *bytes = B.bytes;
+  return GDFT_OK;
+}
+
+int gdft_neural_batch_xc(int32_t n_mol, const gdft_molecule *mols, const double *const *h_rdm1,
+                         const double *const *h_ehf, const gdft_network *net, const double *d_params,
+                         const double *d_eref, double *d_energies, double *d_loss, double *const *h_vxc,
+                         double *d_dparams, void *d_ws, size_t ws_bytes, void *stream) {
+  int rc = check_network(net);
+  if (rc) return rc;
+  if (net->precision != GDFT_TF32X3) {
+    set_error("gdft_neural_batch_xc needs the TF32x3 network form");
+    return GDFT_ERR_UNSUPPORTED;
+  }
+  static thread_local BatchLayout B;
+  if ((rc = batch_layout(n_mol, mols, net, &B))) return rc;
+  if (d_ws == nullptr || ws_bytes < B.bytes || ((uintptr_t)d_ws & 255u) != 0) {
+    set_error("batch workspace of %zu bytes (256-byte aligned) is smaller than the %zu bytes required", ws_bytes,
+              B.bytes);
+    return GDFT_ERR_WORKSPACE;
+  }
+  if (h_rdm1 == nullptr || h_ehf == nullptr || d_params == nullptr || d_energies == nullptr) {
+    set_error("gdft_neural_batch_xc: rdm1, ehf, params and energies are required");
+    return GDFT_ERR_INVALID;
+  }
+  for (int m = 0; m < n_mol; ++m)
+    if (h_rdm1[m] == nullptr || h_ehf[m] == nullptr) {
+      set_error("gdft_neural_batch_xc: molecule %d has no rdm1 or ehf", m);
+      return GDFT_ERR_INVALID;
+    }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  const int64_t npt = B.npt;
+  double *feat = (double *)(ws + B.off_feat), *w = (double *)(ws + B.off_w), *ehf = (double *)(ws + B.off_ehf);
+  double *coef = (double *)(ws + B.off_coef), *cot = (double *)(ws + B.off_cot);
+  int64_t *seg = (int64_t *)(ws + B.off_seg);
+  {
+    SegTable t;
+    for (int m = 0; m <= n_mol; ++m) t.off[m] = B.seg[m];
+    write_seg_kernel<<<1, 256, 0, st>>>(t, n_mol, seg);
+    if ((rc = check_cuda(cudaGetLastError(), "batch segments"))) return rc;
+  }
+  if ((rc = check_cuda(cudaMemsetAsync(feat, 0, (size_t)2 * kFeat * npt * 8, st), "batch clear")) ||
+      (rc = check_cuda(cudaMemsetAsync(w, 0, (size_t)npt * 8, st), "batch clear")) ||
+      (rc = check_cuda(cudaMemsetAsync(ehf, 0, (size_t)4 * npt * 8, st), "batch clear")))
+    return rc;
+  for (int m = 0; m < n_mol; ++m) {
+    const gdft_molecule *mol = &mols[m];
+    char *wsm = ws + B.mol_off[m];
+    const WsLayout W = ws_layout(mol);
+    const int64_t np = mol->n_grid_pad, off = B.seg[m];
+    if ((rc = run_density(mol, h_rdm1[m], wsm, st))) return rc;
+    if ((rc = check_cuda(cudaMemcpy2DAsync(feat + off, (size_t)npt * 8, wsm + W.off_feat, (size_t)np * 8,
+                                           (size_t)np * 8, 2 * kFeat, cudaMemcpyDeviceToDevice, st),
+                         "batch features")) ||
+        (rc = check_cuda(cudaMemcpyAsync(w + off, mol_w(mol), (size_t)np * 8, cudaMemcpyDeviceToDevice, st),
+                         "batch weights")) ||
+        (rc = check_cuda(cudaMemcpy2DAsync(ehf + off, (size_t)npt * 8, h_ehf[m], (size_t)mol->n_grid * 8,
+                                           (size_t)mol->n_grid * 8, 4, cudaMemcpyDeviceToDevice, st),
+                         "batch ehf")))
+      return rc;
+  }
+  MlpSegments sg{n_mol, seg, d_eref, d_energies, d_loss, cot};
+  {
+    StageTimer tm(GDFT_STAGE_MLP, st);
+    rc = mlp_run_tc(net_shape(net), d_params, d_dparams, feat, ehf, w, npt, npt, net->clip, ws + B.off_net, nullptr,
+                    coef, (int *)(ws + B.mol_off[0] + ws_layout(&mols[0]).off_err), st, &sg);
+    if (rc) return rc;
+  }
+  for (int m = 0; m < n_mol; ++m) {
+    if (h_vxc == nullptr || h_vxc[m] == nullptr) continue;
+    const gdft_molecule *mol = &mols[m];
+    char *wsm = ws + B.mol_off[m];
+    const WsLayout W = ws_layout(mol);
+    const int64_t np = mol->n_grid_pad, off = B.seg[m];
+    if ((rc = check_cuda(cudaMemcpy2DAsync(wsm + W.off_coef, (size_t)np * 8, coef + off, (size_t)npt * 8,
+                                           (size_t)np * 8, 2 * kFeat, cudaMemcpyDeviceToDevice, st),
+                         "batch coefficients")))
+      return rc;
+    if ((rc = run_vxc(mol, (const double *)(wsm + W.off_coef), h_vxc[m], wsm, st))) return rc;
+  }
+  return GDFT_OK;
 }
 
 int gdft_vxc_from_potentials(const gdft_molecule *mol, const double *d_pot, double *d_vxc, void *d_ws,

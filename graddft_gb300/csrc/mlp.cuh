@@ -73,9 +73,25 @@ struct MlpTcLayout {
 };
 MlpTcLayout mlp_tc_layout(const MlpShape &s, int64_t np);
 bool mlp_tc_width_supported(int width);
+
+// Several molecules' grid points in one network pass: segment m is rows
+// [seg_off[m], seg_off[m + 1]) (multiples of 256).  After the forward, the
+// per-segment energies E_m and the loss (sum_m (E_m - e_ref_m)^2, or sum_m E_m
+// without references) are formed on the device, and the backward is seeded
+// with dloss/dE_m per segment, so dparams = dloss/dtheta and coef carries
+// dloss/dE_m for each molecule's points.
+struct MlpSegments {
+  int n_seg;
+  const int64_t *d_seg_off;  // n_seg + 1 row offsets (device)
+  const double *d_eref;      // n_seg reference energies or null
+  double *d_energies;        // n_seg out
+  double *d_loss;            // 1 out (may be null)
+  double *d_cot;             // n_seg scratch: dloss/dE_m
+};
+
 int mlp_run_tc(const MlpShape &S, const double *params, double *dparams, const double *feat, const double *ehf,
                const double *w, int64_t n_grid, int64_t np, double clip, char *ws, double *exc, double *coef, int *err,
-               cudaStream_t st);
+               cudaStream_t st, const MlpSegments *seg = nullptr);
 
 // Per-point pieces of the second-order pass shared by its FP64 and mixed forms:
 // primal/tangent inputs (u stacked [2][np][16]) and energy densities, and the

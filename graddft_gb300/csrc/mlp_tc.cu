@@ -263,6 +263,45 @@ __global__ void l0_bwd_kernel(const float *__restrict__ dhp, const float *__rest
   gz[i] = (dhp[i] + gres[i]) * (1.0f - h * h);
 }
 
+// Per-segment energies from the 256-row energy partials (Kahan), the loss and
+// its cotangents dloss/dE_m.  One thread per segment; thread 0 sums the loss.
+__global__ void segment_loss_kernel(const double *__restrict__ epart, const int64_t *__restrict__ seg_off, int n_seg,
+                                    const double *__restrict__ eref, double *__restrict__ energies,
+                                    double *__restrict__ cot, double *__restrict__ loss) {
+  for (int m = threadIdx.x; m < n_seg; m += blockDim.x) {
+    Kahan k{0.0, 0.0};
+    for (int64_t b = seg_off[m] / 256; b < seg_off[m + 1] / 256; ++b) k.add(epart[b]);
+    energies[m] = k.s;
+    cot[m] = eref ? 2.0 * (k.s - eref[m]) : 1.0;
+  }
+  __syncthreads();
+  if (loss && threadIdx.x == 0) {
+    double t = 0.0;
+    for (int m = 0; m < n_seg; ++m) t += eref ? (energies[m] - eref[m]) * (energies[m] - eref[m]) : energies[m];
+    *loss = t;
+  }
+}
+
+// Seeds the backward with each row's segment cotangent: dy, dyf, de *= dloss/dE_m.
+__global__ void scale_rows_kernel(const int64_t *__restrict__ seg_off, int n_seg, const double *__restrict__ cot,
+                                  int64_t rows, double *__restrict__ dy, float *__restrict__ dyf,
+                                  double *__restrict__ de) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  int lo = 0, hi = n_seg;  // seg_off[lo] <= r < seg_off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) / 2;
+    if (seg_off[mid] <= r) lo = mid; else hi = mid;
+  }
+  const double g = cot[lo];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    dy[r * 3 + f] *= g;
+    dyf[r * 3 + f] = (float)dy[r * 3 + f];
+    de[r * 3 + f] *= g;
+  }
+}
+
 size_t tc_layer_offset(const MlpShape &S, int i) {
   return (size_t)S.n_in * S.width + S.width + (size_t)i * ((size_t)S.width * S.width + 3 * (size_t)S.width);
 }
@@ -270,7 +309,7 @@ size_t tc_layer_offset(const MlpShape &S, int i) {
 template <int PL>
 int run_tc(const MlpShape &S, const double *params, double *dparams, const double *feat, const double *ehf,
            const double *w, int64_t n_grid, int64_t np, double clip, char *ws, double *exc, double *coef, int *err,
-           cudaStream_t st) {
+           cudaStream_t st, const MlpSegments *seg) {
   constexpr int Wd = 32 * PL;
   const MlpTcLayout L = mlp_tc_layout(S, np);
   auto d64 = [&](size_t off) { return (double *)(ws + off); };
@@ -370,7 +409,15 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
   head_kernel<PL><<<hblocks, 256, 0, st>>>(HF, Wof, bo, e, w, n_grid, np, clip, S.sigmoid_scale, dy, dyf, de,
                                            epart);
   GDFT_CK(cudaGetLastError(), "mlp_tc head");
-  GDFT_CK(launch_energy_reduce(epart, (int)hblocks, exc, st), "mlp_tc energy_reduce");
+  if (exc) GDFT_CK(launch_energy_reduce(epart, (int)hblocks, exc, st), "mlp_tc energy_reduce");
+  if (seg) {
+    segment_loss_kernel<<<1, 256, 0, st>>>(epart, seg->d_seg_off, seg->n_seg, seg->d_eref, seg->d_energies,
+                                           seg->d_cot, seg->d_loss);
+    GDFT_CK(cudaGetLastError(), "mlp_tc segment loss");
+    scale_rows_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(seg->d_seg_off, seg->n_seg, seg->d_cot, np, dy,
+                                                                     dyf, de);
+    GDFT_CK(cudaGetLastError(), "mlp_tc segment seed");
+  }
   if (coef == nullptr && dparams == nullptr) return GDFT_OK;
 
   // ---- backward ----
@@ -478,14 +525,14 @@ MlpTcLayout mlp_tc_layout(const MlpShape &s, int64_t np) {
 
 int mlp_run_tc(const MlpShape &S, const double *params, double *dparams, const double *feat, const double *ehf,
                const double *w, int64_t n_grid, int64_t np, double clip, char *ws, double *exc, double *coef, int *err,
-               cudaStream_t st) {
-  if (np % kPointTile != 0 || S.n_in > 128) {
+               cudaStream_t st, const MlpSegments *seg) {
+  if (np % kPointTile != 0 || S.n_in > 128 || (seg && (seg->n_seg < 1 || np % 256 != 0))) {
     set_error("mlp_tc: grid padding or input width not supported");
     return GDFT_ERR_INVALID;
   }
   switch (S.width) {
-    case 128: return run_tc<4>(S, params, dparams, feat, ehf, w, n_grid, np, clip, ws, exc, coef, err, st);
-    case 256: return run_tc<8>(S, params, dparams, feat, ehf, w, n_grid, np, clip, ws, exc, coef, err, st);
+    case 128: return run_tc<4>(S, params, dparams, feat, ehf, w, n_grid, np, clip, ws, exc, coef, err, st, seg);
+    case 256: return run_tc<8>(S, params, dparams, feat, ehf, w, n_grid, np, clip, ws, exc, coef, err, st, seg);
     default:
       set_error("mlp_tc: width %d not built for the mixed form (128 or 256)", S.width);
       return GDFT_ERR_UNSUPPORTED;

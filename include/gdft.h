@@ -188,6 +188,27 @@ int gdft_neural_xc_hvp(const gdft_molecule *mol, const double *d_rdm1, const gdf
                        const double *d_params, const double *d_ehf, const double *d_tangent, double *d_value,
                        double *d_hrdm1, double *d_hparams, void *d_ws, size_t ws_bytes, void *stream);
 
+/* Workspace bytes of gdft_neural_batch_xc for these molecules. */
+int gdft_neural_batch_workspace_bytes(int32_t n_mol, const gdft_molecule *mols, const gdft_network *net,
+                                      size_t *bytes);
+
+/* A batch of molecules of different sizes in one call (a training step over a
+ * dataset, train.py:34-218 applied per molecule): every molecule's density
+ * contraction, then ONE pass of the network over all molecules' grid points,
+ * per-molecule energies E_m and the loss L = sum_m (E_m - e_ref_m)^2 (or
+ * sum_m E_m when d_eref is NULL) formed on the device, the backward seeded with
+ * dL/dE_m, and every molecule's V contraction.  Outputs: d_energies (n_mol),
+ * d_loss (may be NULL), d_vxc[m] = dL/dD_m (2, ao_m, ao_m) (array of device
+ * pointers; entries may be NULL), d_dparams = dL/dtheta.  h_rdm1 / h_ehf /
+ * h_vxc are HOST arrays of n_mol device pointers.  The network must be the
+ * TF32x3 form.  Nothing synchronises the host, so the call can be captured in
+ * a CUDA graph.  No counterpart in the reference (JAX vmaps/loops over
+ * molecules). */
+int gdft_neural_batch_xc(int32_t n_mol, const gdft_molecule *mols, const double *const *h_rdm1,
+                         const double *const *h_ehf, const gdft_network *net, const double *d_params,
+                         const double *d_eref, double *d_energies, double *d_loss, double *const *h_vxc,
+                         double *d_dparams, void *d_ws, size_t ws_bytes, void *stream);
+
 /* The DM21 network inputs and energy densities of a molecule: d_cinputs
  * (grid, 11) = dm21_combine_cinputs(dm21_coefficient_inputs(...), ehf)
  * (functional.py:504-531, 628-649) and d_dens (grid, 3) =
