@@ -90,8 +90,7 @@ WsLayout ws_layout(const gdft_molecule *m) {
   WsLayout W;
   const int64_t np = m->n_grid_pad;
   W.n_eblocks = xc_point_blocks(np);
-  W.vrange = 0;
-  W.n_vsplit = m->precision == GDFT_FP64 ? vxc_f64_splits(np, m->n_ao) : vxc_tc_splits(np, m->n_ao, &W.vrange);
+  W.n_vsplit = m->precision == GDFT_FP64 ? vxc_f64_splits(np, m->n_ao) : vxc_q_splits(np, m->n_ao);
   size_t off = 0;
   W.off_feat = off;
   off = align256(off + (size_t)2 * kFeat * np * sizeof(double));
@@ -100,11 +99,18 @@ WsLayout ws_layout(const gdft_molecule *m) {
   W.off_epart = off;
   off = align256(off + (size_t)W.n_eblocks * sizeof(double));
   W.off_vpart = off;
-  off = align256(off + (size_t)W.n_vsplit * 2 * m->n_ao * m->n_ao * sizeof(double));
+  if (m->precision == GDFT_FP64) {
+    off = align256(off + (size_t)W.n_vsplit * 2 * m->n_ao * m->n_ao * sizeof(double));
+  } else {  // split-K partials of the packed GEMM: [split][n_ao][2 ldk]
+    off = align256(off + (size_t)W.n_vsplit * m->n_ao * 2 * round_up(m->n_ao, 128) * sizeof(double));
+  }
   W.off_dpk = off;
+  W.off_q = off;
   if (m->precision == GDFT_TF32X3) {
     const size_t ldk = (size_t)round_up(m->n_ao, 128);
     off = align256(off + 2 * ldk * ldk * 2 * sizeof(float));
+    W.off_q = off;
+    off = align256(off + vxc_q_bytes(np, m->n_ao));
   }
   W.off_err = off;
   off = align256(off + 64);
@@ -340,15 +346,11 @@ static int run_vxc(const gdft_molecule *mol, const double *coef, double *d_vxc, 
     StageTimer tm(GDFT_STAGE_REDUCE, st);
     return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
   }
-  {
-    StageTimer tm(GDFT_STAGE_VXC, st);
-    rc = check_cuda(launch_vxc_tc(mol_am(mol), mol_af(mol), coef, mol->n_grid_pad, (int)round_up(mol->n_ao, 128), mol->n_ao,
-                                  W.n_vsplit, W.vrange, vpart, (int *)(ws + W.off_err), st),
-                    "vxc_tc");
-    if (rc) return rc;
-  }
-  StageTimer tm(GDFT_STAGE_REDUCE, st);
-  return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
+  StageTimer tm(GDFT_STAGE_VXC, st);
+  return check_cuda(launch_vxc_q_tc(mol_am(mol), mol_af(mol), coef, mol->n_grid_pad, (int)round_up(mol->n_ao, 128),
+                                    mol->n_ao, (float *)(ws + W.off_q), W.n_vsplit, vpart, d_vxc,
+                                    (int *)(ws + W.off_err), st),
+                    "vxc_q_tc");
 }
 
 extern "C" {

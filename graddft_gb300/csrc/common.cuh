@@ -43,10 +43,9 @@ MolLayout mol_layout(int64_t n_grid, int n_ao, int precision);
 
 // Layout of the per-call workspace.
 struct WsLayout {
-  size_t off_feat, off_coef, off_epart, off_vpart, off_dpk, off_err, bytes;
+  size_t off_feat, off_coef, off_epart, off_vpart, off_dpk, off_q, off_err, bytes;
   int n_eblocks;   // blocks of the point kernel (energy partial sums)
   int n_vsplit;    // split-K factor of the V contraction
-  int64_t vrange;  // grid points per split (TF32x3 form)
 };
 
 WsLayout ws_layout(const gdft_molecule *m);

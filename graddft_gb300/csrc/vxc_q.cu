@@ -1,0 +1,132 @@
+// vxc_q.cu - mixed (TF32x3) form of the V_xc contraction as a packed tensor-core GEMM.
+//
+//   V_sigma[a][b] = sum_r sum_t P_t[r][a] Q_sigma,t[r][b]
+//   Q_sigma,0 = c_rho phi + c_gx d_x phi + c_gy d_y phi + c_gz d_z phi + c_lap lap phi
+//   Q_sigma,j = c_kin d_j phi                                    (j = x, y, z)
+// with P_0 = phi, P_j = d_j phi and c the per-point adjoint coefficients (the
+// transposed density contraction of jax.grad at train.py:86; the same sum as
+// vxc_f64.cu).  A memory-bound pre-pass forms Q for both spins once per call,
+// directly as TF32 hi/lo blocks in the AO-major layout of the AO tables; the
+// contraction is then tcg_kernel with A = the AO-major phi planes (K = 4
+// planes x grid points), B = Q of both spins (N = 2 x n_ao), split-K over the
+// grid, FP64 partials, and a reduction that also splits the spins.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "tc_gemm.cuh"
+#include "umma.cuh"
+
+namespace gdft {
+
+namespace {
+
+constexpr int kBlkF = umma::kBlockBytes / 4;  // floats in one 128 x 32 block
+
+// One CTA per (b tile, 32-point chunk): reads the five AO-major FP32 planes of
+// that block and the chunk's coefficients, writes Q for 2 spins x 4 planes as
+// hi/lo blocks.  Threads walk the blocks in memory order (16-byte chunks), so
+// loads and stores are coalesced.
+__global__ void __launch_bounds__(256) build_q_kernel(const float *__restrict__ af, const double *__restrict__ coef,
+                                                      int64_t np, int nbt, float *__restrict__ q) {
+  __shared__ float sc[32][2][kFeat];
+  const int64_t npc = np / 32;
+  const int bt = (int)(blockIdx.x / npc);
+  const int64_t pc = blockIdx.x % npc;
+  for (int i = threadIdx.x; i < 32 * 2 * kFeat; i += blockDim.x) {
+    const int pt = i / (2 * kFeat), s = (i / kFeat) % 2, c = i % kFeat;
+    sc[pt][s][c] = (float)coef[((size_t)s * kFeat + c) * np + pc * 32 + pt];
+  }
+  __syncthreads();
+  const float *src[kPlanes];
+#pragma unroll
+  for (int p = 0; p < kPlanes; ++p) src[p] = af + ((size_t)(bt * kPlanes + p) * npc + pc) * kBlkF;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int chunk = threadIdx.x + i * 256;  // 16-byte chunk in memory order
+    const int k4 = (chunk >> 3) & 7;          // 4-point group: points 4 k4 .. 4 k4 + 3
+    const uint32_t off = (uint32_t)chunk * 4;
+    float4 v[kPlanes];
+#pragma unroll
+    for (int p = 0; p < kPlanes; ++p) v[p] = __ldg((const float4 *)(src[p] + off));
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      float qv[4][4];  // [plane t][point j]
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float *c = sc[4 * k4 + j][s];
+        const float ph = (&v[T_PHI].x)[j], dx = (&v[T_DX].x)[j], dy = (&v[T_DY].x)[j], dz = (&v[T_DZ].x)[j],
+                    lp = (&v[T_LAP].x)[j];
+        qv[0][j] = c[C_RHO] * ph + c[C_GX] * dx + c[C_GY] * dy + c[C_GZ] * dz + c[C_LAP] * lp;
+        qv[1][j] = c[C_KIN] * dx;
+        qv[2][j] = c[C_KIN] * dy;
+        qv[3][j] = c[C_KIN] * dz;
+      }
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        float4 h, l;
+        umma::split_tf32f(qv[t][0], h.x, l.x);
+        umma::split_tf32f(qv[t][1], h.y, l.y);
+        umma::split_tf32f(qv[t][2], h.z, l.z);
+        umma::split_tf32f(qv[t][3], h.w, l.w);
+        float *blk = q + ((((size_t)s * nbt + bt) * 4 + t) * npc + pc) * 2 * kBlkF;
+        *(float4 *)(blk + off) = h;
+        *(float4 *)(blk + kBlkF + off) = l;
+      }
+    }
+  }
+}
+
+// V[s][a][b] = sum over splits of part[split][a][s * ldk + b], a, b < n.
+__global__ void vxc_q_reduce_kernel(const double *__restrict__ part, int nsplit, int n, int ldk,
+                                    double *__restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t total = (size_t)2 * n * n;
+  if (i >= total) return;
+  const int s = (int)(i / ((size_t)n * n)), a = (int)((i / n) % n), b = (int)(i % n);
+  const size_t stride = (size_t)n * 2 * ldk;
+  double acc = 0.0;
+  for (int k = 0; k < nsplit; ++k) acc += part[(size_t)k * stride + (size_t)a * 2 * ldk + (size_t)s * ldk + b];
+  out[i] = acc;
+}
+
+}  // namespace
+
+// Split-K factor: about four waves of CTAs over the (a tile, b tile of both spins) grid.
+int vxc_q_splits(int64_t np, int n_ao) {
+  const int nbt = (int)(round_up(n_ao, 128) / 128);
+  const int tiles = nbt * 2 * nbt;
+  const int64_t kch = 4 * (np / 32);
+  int s = (4 * 148 + tiles - 1) / tiles;
+  if (s > kch) s = (int)kch;
+  return s < 1 ? 1 : s;
+}
+
+size_t vxc_q_bytes(int64_t np, int n_ao) {
+  const int ldk = (int)round_up(n_ao, 128);
+  return (size_t)2 * 4 * np * ldk * 2 * sizeof(float);
+}
+
+cudaError_t launch_vxc_q_tc(const float *am, const float *af, const double *coef, int64_t np, int ldk, int n_ao,
+                            float *q, int nsplit, double *vpart, double *vxc, int *err, cudaStream_t st) {
+  const int nbt = ldk / 128;
+  const int64_t npc = np / 32;
+  build_q_kernel<<<(unsigned)(nbt * npc), 256, 0, st>>>(af, coef, np, nbt, q);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  TcgArgs a{};
+  a.a = am;
+  a.b = q;
+  a.m_tiles = nbt;
+  a.n_tiles = 2 * nbt;
+  a.a_chunks = a.b_chunks = a.k_chunks = 4 * npc;
+  a.chunks_per_split = (a.k_chunks + nsplit - 1) / nsplit;
+  a.out64 = vpart;
+  a.m_valid = n_ao;
+  a.n_valid = 2 * ldk;
+  a.err = err;
+  if ((e = launch_tcg(a, nsplit, st)) != cudaSuccess) return e;
+  const size_t total = (size_t)2 * n_ao * n_ao;
+  vxc_q_reduce_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(vpart, nsplit, n_ao, ldk, vxc);
+  return cudaGetLastError();
+}
+
+}  // namespace gdft
