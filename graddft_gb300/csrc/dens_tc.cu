@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
           uint32_t w[32], sv[32];
           umma::tmem_ld32_nowait(tl + buf * 128 + c, w);
           if (kq > 0) umma::tmem_ld32_nowait(tl + 256 + c, sv);
-          umma::tmem_ld_wait();
+          umma::tmem_ld_wait(w, sv);
           float o[32];
 #pragma unroll
           for (int i = 0; i < 32; ++i)

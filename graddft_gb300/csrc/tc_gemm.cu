@@ -6,16 +6,19 @@
 // the K-major no-swizzle shared-memory layout of umma::kblock_off), stored
 // [row tile][K chunk][hi|lo]; one stage is one bulk copy of A (32 KB) and one
 // of B (32 KB).  Three products per term (hi*hi + hi*lo + lo*hi), M = 128,
-// N = 128 per CTA.  Accumulation as in the V_xc contraction: each 32-wide K
-// chunk is accumulated in a TMEM buffer W (double-buffered), correction
-// products first, and four drain warps fold it into a Kahan-compensated FP32
-// running sum (S, C) in TMEM.  The K range may be split across blockIdx.y
-// (split-K); each split writes its S - C either as FP32 into a row-major
-// output (single split) or as FP64 partials [split][M][N].
+// N = 128 per CTA.  Accumulation: each 32-wide K chunk is accumulated in one
+// of three TMEM buffers W (128 columns each; the MMA runs up to two chunks
+// ahead of the drains), correction products first, and eight drain warps fold
+// it into a Kahan-compensated FP32 running sum: S in TMEM (128 columns), the
+// compensation C in registers (each drain thread owns one output row and 64
+// columns).  The K range may be split
+// across blockIdx.y (split-K); each split writes its S - C either as FP32 into
+// a row-major output (single split) or as FP64 partials [split][M][N].
 //
-// Warp roles (192 threads): warp 0 = TMA producer, warp 1 = TMEM owner and
-// MMA issuer, warps 2-5 = drains.  All waits are bounded; on expiry the CTA
-// records an error word and winds down.
+// Warp roles (320 threads): warp 0 = TMA producer, warp 1 = TMEM owner and
+// MMA issuer, warps 2-9 = drains (TMEM lane quadrant warp % 4, column half
+// (warp - 2) / 4).  All waits are bounded; on expiry the CTA records an error
+// word and winds down.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "tc_gemm.cuh"
@@ -28,8 +31,10 @@ namespace {
 constexpr int kStages = 3;
 constexpr uint32_t kOpBytes = 2 * umma::kBlockBytes;   // hi | lo of one 128 x 32 block
 constexpr uint32_t kStageBytes = 2 * kOpBytes;         // A and B
-constexpr int kThreads = 192;
-constexpr uint32_t kTmemCols = 512;  // W0 [0,128), W1 [128,256), S [256,384), C [384,512)
+constexpr int kThreads = 320;
+constexpr int kWBufs = 3;
+constexpr uint32_t kTmemCols = 512;  // W0..W2 [0, 384), S [384, 512)
+constexpr uint32_t kScol = 384;
 constexpr int kSmemBytes = kStages * kStageBytes + 1024;
 
 __device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, code); }
@@ -37,7 +42,7 @@ __device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, cod
 __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], wfull[2], wempty[2], drain;
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], wfull[kWBufs], wempty[kWBufs], drain;
   __shared__ uint32_t tmem_base;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -51,9 +56,9 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
       umma::mbar_init(&full[s], 1);
       umma::mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kWBufs; ++b) {
       umma::mbar_init(&wfull[b], 1);
-      umma::mbar_init(&wempty[b], 128);
+      umma::mbar_init(&wempty[b], 256);
     }
     umma::mbar_init(&drain, 1);
     umma::fence_barrier_init();
@@ -68,103 +73,99 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    int64_t it = 0;
-    for (; it < nst; ++it) {
-      const int s = (int)(it % kStages);
-      if (!umma::warp_wait(&empty[s], ((it / kStages) & 1) ^ 1)) {
-        if (lane == 0) flag(A.err, 41);
-        break;
-      }
-      if (lane == 0) {
+    // One thread issues the copies; its waits are bounded and single-threaded.
+    if (lane == 0) {
+      int64_t it = 0;
+      for (; it < nst; ++it) {
+        const int s = (int)(it % kStages);
+        if (!umma::mbar_wait(&empty[s], ((it / kStages) & 1) ^ 1)) {
+          flag(A.err, 41);
+          break;
+        }
         const int64_t kc = c0 + it;
         umma::mbar_arrive_expect_tx(&full[s], kStageBytes);
         umma::bulk_g2s(smem + s * kStageBytes, a_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
         umma::bulk_g2s(smem + s * kStageBytes + kOpBytes, b_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
       }
-      __syncwarp();
+      // Our own copies land before the CTA can release shared memory.
+      for (int64_t i = it > kStages ? it - kStages : 0; i < it; ++i)
+        if (!umma::mbar_wait(&full[i % kStages], (i / kStages) & 1)) flag(A.err, 42);
     }
-    // Our own copies land before the CTA can release shared memory.
-    for (int64_t i = it > kStages ? it - kStages : 0; i < it; ++i)
-      if (!umma::warp_wait(&full[i % kStages], (i / kStages) & 1) && lane == 0) flag(A.err, 42);
+    __syncwarp();
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
-    const uint32_t idesc = umma::idesc_tf32(128, 128);
-    for (int64_t it = 0; it < nst; ++it) {
-      const int s = (int)(it % kStages);
-      const int buf = (int)(it & 1);
-      if (!umma::warp_wait(&wempty[buf], ((it >> 1) & 1) ^ 1)) {
-        if (lane == 0) flag(A.err, 43);
-        break;
-      }
-      umma::tc_fence_after();
-      if (!umma::warp_wait(&full[s], (it / kStages) & 1)) {
-        if (lane == 0) flag(A.err, 44);
-        break;
-      }
-      umma::tc_fence_after();
-      if (lane == 0) {
-        const uint32_t sa = umma::smem_u32(smem + s * kStageBytes), sb = sa + kOpBytes;
-        const uint32_t d = tbase + buf * 128;
-#pragma unroll
-        for (int pass = 0; pass < 2; ++pass) {
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const uint64_t ahi = umma::sdesc(sa + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-            const uint64_t alo = umma::sdesc(sa + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-            const uint64_t bhi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-            const uint64_t blo = umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-            if (pass == 0) {  // small correction products first
-              umma::mma_tf32(d, ahi, blo, idesc, kk == 0 ? 0u : 1u);
-              umma::mma_tf32(d, alo, bhi, idesc, 1u);
-            } else {
-              umma::mma_tf32(d, ahi, bhi, idesc, 1u);
-            }
-          }
+    // One thread issues every MMA.  The four operand descriptors are built once
+    // for slot 0; a slot (64 KB) adds 4096 and a K step of 8 (256 bytes) adds
+    // 16 to the start-address field (address >> 4, bits 0-13; shared memory
+    // addresses stay below 2^18).
+    if (lane == 0) {
+      const uint32_t idesc = umma::idesc_tf32(128, 128);
+      const uint32_t sa0 = umma::smem_u32(smem);
+      const uint64_t dahi0 = umma::sdesc(sa0, umma::kBlockLBO, umma::kBlockSBO);
+      const uint64_t dalo0 = umma::sdesc(sa0 + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
+      const uint64_t dbhi0 = umma::sdesc(sa0 + kOpBytes, umma::kBlockLBO, umma::kBlockSBO);
+      const uint64_t dblo0 = umma::sdesc(sa0 + kOpBytes + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
+      for (int64_t it = 0; it < nst; ++it) {
+        const int s = (int)(it % kStages);
+        const int buf = (int)(it % kWBufs);
+        if (!umma::mbar_wait(&wempty[buf], ((it / kWBufs) & 1) ^ 1) ||
+            !umma::mbar_wait(&full[s], (it / kStages) & 1)) {
+          flag(A.err, 43);
+          break;
         }
+        umma::tc_fence_after();
+        const uint32_t d = tbase + buf * 128;
+        const uint64_t so = (uint64_t)s * (kStageBytes >> 4);  // slot offset in the address field
+        const uint64_t ahi = dahi0 + so, alo = dalo0 + so, bhi = dbhi0 + so, blo = dblo0 + so;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)  // small correction products first
+          umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, kk == 0 ? 0u : 1u),
+              umma::mma_tf32(d, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(d, ahi + 16 * kk, bhi + 16 * kk, idesc, 1u);
         umma::mma_commit(&empty[s]);
         umma::mma_commit(&wfull[buf]);
       }
-      __syncwarp();
+      umma::mma_commit(&drain);
+      if (!umma::mbar_wait(&drain, 0)) flag(A.err, 45);
     }
-    if (lane == 0) umma::mma_commit(&drain);
     __syncwarp();
-    if (!umma::warp_wait(&drain, 0) && lane == 0) flag(A.err, 45);
   } else {
     // -------------------------------------------------------------- drains
-    const int q = warp & 3;
-    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
+    const int q = warp & 3, half = (warp - 2) >> 2;
+    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16) + half * 64;
+    float C[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) C[i] = 0.0f;
     int64_t it = 0;
     for (; it < nst; ++it) {
-      const int buf = (int)(it & 1);
-      if (!umma::warp_wait(&wfull[buf], (it >> 1) & 1)) {
+      const int buf = (int)(it % kWBufs);
+      if (!umma::warp_wait(&wfull[buf], (it / kWBufs) & 1)) {
         if (lane == 0) flag(A.err, 46);
         break;
       }
       umma::tc_fence_after();
-#pragma unroll 1
-      for (int c = 0; c < 128; c += 32) {
-        float w[32];
-        umma::tmem_ld32(tl + buf * 128 + c, w);
-        if (it == 0) {
-          float z[32];
 #pragma unroll
-          for (int i = 0; i < 32; ++i) z[i] = 0.0f;
-          umma::tmem_st32(tl + 256 + c, w);
-          umma::tmem_st32(tl + 384 + c, z);
-        } else {
-          float sv[32], cv[32];
-          umma::tmem_ld32(tl + 256 + c, sv);
-          umma::tmem_ld32(tl + 384 + c, cv);
+      for (int c = 0; c < 64; c += 32) {
+        uint32_t wr[32], sr[32];
+        umma::tmem_ld32_nowait(tl + buf * 128 + c, wr);
+        if (it > 0) umma::tmem_ld32_nowait(tl + kScol + c, sr);
+        umma::tmem_ld_wait(wr, sr);
+        float sv[32];
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {  // Kahan: s + (w - c)
-            const float y = w[i] - cv[i];
-            const float t = sv[i] + y;
-            cv[i] = (t - sv[i]) - y;
+        for (int i = 0; i < 32; ++i) {
+          const float w = __uint_as_float(wr[i]);
+          if (it == 0) {
+            sv[i] = w;
+          } else {  // Kahan: S + (w - C)
+            const float sp = __uint_as_float(sr[i]);
+            const float y = w - C[c + i];
+            const float t = sp + y;
+            C[c + i] = (t - sp) - y;
             sv[i] = t;
           }
-          umma::tmem_st32(tl + 256 + c, sv);
-          umma::tmem_st32(tl + 384 + c, cv);
         }
+        umma::tmem_st32(tl + kScol + c, sv);
       }
       umma::tmem_st_wait();
       umma::tc_fence_before();
@@ -172,24 +173,22 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
     }
     const bool have = it == nst && nst > 0;
     const int m = mt * 128 + q * 32 + lane;
-#pragma unroll 1
-    for (int c = 0; c < 128; c += 32) {
-      float sv[32], cv[32];
-      if (have) {
-        umma::tmem_ld32(tl + 256 + c, sv);
-        umma::tmem_ld32(tl + 384 + c, cv);
-      }
+    const int n0 = nt * 128 + half * 64;
+#pragma unroll
+    for (int c = 0; c < 64; c += 32) {
+      float sv[32];
+      if (have) umma::tmem_ld32(tl + kScol + c, sv);
       if (m < A.m_valid) {
         if (A.out32) {
-          float *row = A.out32 + (size_t)m * A.ldo + nt * 128 + c;
+          float *row = A.out32 + (size_t)m * A.ldo + n0 + c;
 #pragma unroll
           for (int i = 0; i < 32; ++i)
-            if (nt * 128 + c + i < A.n_valid) row[i] = have ? sv[i] - cv[i] : 0.0f;
+            if (n0 + c + i < A.n_valid) row[i] = have ? sv[i] - C[c + i] : 0.0f;
         } else {
-          double *row = A.out64 + ((size_t)blockIdx.y * A.m_valid + m) * A.n_valid + nt * 128 + c;
+          double *row = A.out64 + ((size_t)blockIdx.y * A.m_valid + m) * A.n_valid + n0 + c;
 #pragma unroll
           for (int i = 0; i < 32; ++i)
-            if (nt * 128 + c + i < A.n_valid) row[i] = have ? (double)sv[i] - (double)cv[i] : 0.0;
+            if (n0 + c + i < A.n_valid) row[i] = have ? (double)sv[i] - (double)C[c + i] : 0.0;
         }
       }
     }
