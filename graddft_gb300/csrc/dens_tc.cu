@@ -106,24 +106,24 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
-    // The whole warp runs the loop (uniform control flow); lane 0 issues.
-    uint32_t it = 0;
-    bool ok = true;
-    for (int j = 0; j < njobs && ok; ++j) {
-      const int t = j / ncb, cb = j % ncb;
-      for (int kc = 0; kc < nkc; ++kc) {
-        const int s = it % kStages;
-        if (!umma::warp_wait(&empty[s], ((it / kStages) & 1) ^ 1)) {
-          if (lane == 0) flag(A.err, 11);
-          ok = false;
-          break;
-        }
-        if (lane == 0) {
+    // One thread issues the copies; its waits are bounded and single-threaded.
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      const int ncb128 = A.ldk / 128;
+      for (int j = 0; j < njobs && ok; ++j) {
+        const int t = j / ncb, cb = j % ncb;
+        for (int kc = 0; kc < nkc; ++kc) {
+          const int s = it % kStages;
+          if (!umma::mbar_wait(&empty[s], ((it / kStages) & 1) ^ 1)) {
+            flag(A.err, 11);
+            ok = false;
+            break;
+          }
           unsigned char *st = smem + s * kStageBytes;
           umma::mbar_arrive_expect_tx(&full[s], kStageBytes);
           umma::bulk_g2s(st, pm_blk(A, tile, t, kc), 2 * umma::kBlockBytes, &full[s]);
           // D blocks hold 128 columns; this job's 64 are a contiguous half of each.
-          const int ncb128 = A.ldk / 128;
           for (int sp = 0; sp < 2; ++sp) {
             const float *b = A.dpk + (((size_t)sp * ncb128 + cb / 2) * nkc + kc) * 2 * (umma::kBlockBytes / 4) +
                              (cb & 1) * (kHalf / 4);
@@ -131,77 +131,77 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
             umma::bulk_g2s(dst, b, kHalf, &full[s]);
             umma::bulk_g2s(dst + kHalf, b + umma::kBlockBytes / 4, kHalf, &full[s]);
           }
+          ++it;
         }
-        __syncwarp();
-        ++it;
       }
+      // Wait for the copies still in flight before the CTA can retire.
+      for (uint32_t i = it > kStages ? it - kStages : 0; i < it; ++i)
+        if (!umma::mbar_wait(&full[i % kStages], (i / kStages) & 1)) flag(A.err, 12);
     }
-    // Wait for the copies still in flight before the CTA can retire.
-    for (uint32_t i = it > kStages ? it - kStages : 0; i < it; ++i) {
-      if (!umma::warp_wait(&full[i % kStages], (i / kStages) & 1) && lane == 0) flag(A.err, 12);
-    }
+    __syncwarp();
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
-    const uint32_t idesc = umma::idesc_tf32(128, kBN);
-    uint32_t it = 0, sub = 0;
-    bool ok = true;
-    for (int j = 0; j < njobs && ok; ++j) {
-      for (int kq = 0; kq < nkq && ok; ++kq, ++sub) {
-        const int buf = sub & 1;
-        if (!umma::warp_wait(&wempty[buf], ((sub >> 1) & 1) ^ 1)) {
-          if (lane == 0) flag(A.err, 13);
-          ok = false;
-          break;
-        }
-        umma::tc_fence_after();
-        for (int kc = kq * kc_per_sub; kc < (kq + 1) * kc_per_sub; ++kc) {
-          const int s = it % kStages;
-          if (!umma::warp_wait(&full[s], (it / kStages) & 1)) {
-            if (lane == 0) flag(A.err, 14);
+    // One thread issues every MMA.  Operand descriptors are built once for
+    // slot 0; a slot adds kStageBytes >> 4 and a K step of 8 (256 bytes) adds
+    // 16 to the start-address field (address >> 4, bits 0-13).
+    if (lane == 0) {
+      const uint32_t idesc = umma::idesc_tf32(128, kBN);
+      const uint32_t s0 = umma::smem_u32(smem);
+      const uint64_t dahi0 = umma::sdesc(s0, umma::kBlockLBO, umma::kBlockSBO);
+      const uint64_t dalo0 = umma::sdesc(s0 + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
+      uint64_t dbhi0[2], dblo0[2];
+#pragma unroll
+      for (int sp = 0; sp < 2; ++sp) {
+        const uint32_t bb = s0 + 2 * umma::kBlockBytes + sp * 2 * kHalf;
+        dbhi0[sp] = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
+        dblo0[sp] = umma::sdesc(bb + kHalf, umma::kBlockLBO, umma::kBlockSBO);
+      }
+      uint32_t it = 0, sub = 0;
+      bool ok = true;
+      for (int j = 0; j < njobs && ok; ++j) {
+        for (int kq = 0; kq < nkq && ok; ++kq, ++sub) {
+          const int buf = sub & 1;
+          if (!umma::mbar_wait(&wempty[buf], ((sub >> 1) & 1) ^ 1)) {
+            flag(A.err, 13);
             ok = false;
             break;
           }
           umma::tc_fence_after();
-          if (lane == 0) {
-            const uint32_t sb = umma::smem_u32(smem + s * kStageBytes);
+          for (int kc = kq * kc_per_sub; kc < (kq + 1) * kc_per_sub; ++kc) {
+            const int s = it % kStages;
+            if (!umma::mbar_wait(&full[s], (it / kStages) & 1)) {
+              flag(A.err, 14);
+              ok = false;
+              break;
+            }
+            umma::tc_fence_after();
+            const uint64_t so = (uint64_t)s * (kStageBytes >> 4);
             const bool first = kc == kq * kc_per_sub;
 #pragma unroll
             for (int sp = 0; sp < 2; ++sp) {
               const uint32_t d = tbase + buf * 128 + sp * kBN;
+              const uint64_t ahi = dahi0 + so, alo = dalo0 + so, bhi = dbhi0[sp] + so, blo = dblo0[sp] + so;
               // Corrections first (hi*lo, lo*hi, small), then the hi*hi products.
 #pragma unroll
-              for (int pass = 0; pass < 2; ++pass) {
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                  const uint64_t ahi = umma::sdesc(sb + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-                  const uint64_t alo =
-                      umma::sdesc(sb + umma::kBlockBytes + kk * 256, umma::kBlockLBO, umma::kBlockSBO);
-                  const uint32_t bb = sb + 2 * umma::kBlockBytes + sp * 2 * kHalf + kk * 256;
-                  const uint64_t bhi = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
-                  const uint64_t blo = umma::sdesc(bb + kHalf, umma::kBlockLBO, umma::kBlockSBO);
-                  if (pass == 0) {
-                    umma::mma_tf32(d, ahi, blo, idesc, (first && kk == 0) ? 0u : 1u);
-                    umma::mma_tf32(d, alo, bhi, idesc, 1u);
-                  } else {
-                    umma::mma_tf32(d, ahi, bhi, idesc, 1u);
-                  }
-                }
+              for (int kk = 0; kk < 4; ++kk) {
+                umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, (first && kk == 0) ? 0u : 1u);
+                umma::mma_tf32(d, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
               }
+#pragma unroll
+              for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(d, ahi + 16 * kk, bhi + 16 * kk, idesc, 1u);
             }
             umma::mma_commit(&empty[s]);
+            ++it;
           }
-          __syncwarp();
-          ++it;
+          if (!ok) break;
+          umma::mma_commit(&wfull[buf]);
         }
-        if (!ok) break;
-        if (lane == 0) umma::mma_commit(&wfull[buf]);
-        __syncwarp();
       }
+      // All issued MMAs complete before TMEM is released.
+      umma::mma_commit(&drain);
+      if (!umma::mbar_wait(&drain, 0)) flag(A.err, 15);
     }
-    // All issued MMAs complete before TMEM is released.
-    if (lane == 0) umma::mma_commit(&drain);
     __syncwarp();
-    if (!umma::warp_wait(&drain, 0) && lane == 0) flag(A.err, 15);
   } else {
     // ------------------------------------------------------------ epilogue
     const int q = warp & 3;
