@@ -689,7 +689,7 @@ def main():
         peak, bound, peak_src = bf16, "tensor", f"{src} bf16 dense (the TF32 pipe nominally runs at half of it)"
     traffic = None
     if form == "tf32x3":
-        traffic = _profiled_traffic({"density": "dens_tc", "vxc": "vxc_tc"}[dom], args.n_grid, args.n_ao)
+        traffic = _profiled_traffic({"density": "dens_tc", "vxc": "tcg_vxc"}[dom], args.n_grid, args.n_ao)
     roof = {"bound": bound, "kernel": f"{dom}_{form}", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 65,536-point capture "
