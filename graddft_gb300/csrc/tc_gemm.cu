@@ -28,18 +28,25 @@ namespace gdft {
 
 namespace {
 
-constexpr int kStages = 3;
 constexpr uint32_t kOpBytes = 2 * umma::kBlockBytes;   // hi | lo of one 128 x 32 block
-constexpr uint32_t kStageBytes = 2 * kOpBytes;         // A and B
+// Stage = A hi|lo, B hi|lo (and, with a third A slice, that block too).
+template <bool kThree>
+struct Cfg {
+  static constexpr uint32_t kStageBytes = 2 * kOpBytes + (kThree ? umma::kBlockBytes : 0);
+  static constexpr int kStages = kThree ? 2 : 3;
+  static constexpr int kSmemBytes = kStages * kStageBytes + 1024;
+};
 constexpr int kThreads = 320;
 constexpr int kWBufs = 3;
 constexpr uint32_t kTmemCols = 512;  // W0..W2 [0, 384), S [384, 512)
 constexpr uint32_t kScol = 384;
-constexpr int kSmemBytes = kStages * kStageBytes + 1024;
 
 __device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, code); }
 
+template <bool kThree>
 __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
+  constexpr int kStages = Cfg<kThree>::kStages;
+  constexpr uint32_t kStageBytes = Cfg<kThree>::kStageBytes;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full[kStages], empty[kStages], wfull[kWBufs], wempty[kWBufs], drain;
@@ -69,6 +76,7 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
   umma::tc_fence_after();
   const uint32_t tbase = tmem_base;
   const float *a_tile = A.a + (size_t)mt * A.a_chunks * (kOpBytes / 4);
+  const float *a3_tile = kThree ? A.a3 + (size_t)mt * A.a_chunks * (umma::kBlockBytes / 4) : nullptr;
   const float *b_tile = A.b + (size_t)nt * A.b_chunks * (kOpBytes / 4);
 
   if (warp == 0) {
@@ -86,6 +94,9 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
         umma::mbar_arrive_expect_tx(&full[s], kStageBytes);
         umma::bulk_g2s(smem + s * kStageBytes, a_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
         umma::bulk_g2s(smem + s * kStageBytes + kOpBytes, b_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
+        if (kThree)
+          umma::bulk_g2s(smem + s * kStageBytes + 2 * kOpBytes, a3_tile + (size_t)kc * (umma::kBlockBytes / 4),
+                         umma::kBlockBytes, &full[s]);
       }
       // Our own copies land before the CTA can release shared memory.
       for (int64_t i = it > kStages ? it - kStages : 0; i < it; ++i)
@@ -105,6 +116,7 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
       const uint64_t dalo0 = umma::sdesc(sa0 + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
       const uint64_t dbhi0 = umma::sdesc(sa0 + kOpBytes, umma::kBlockLBO, umma::kBlockSBO);
       const uint64_t dblo0 = umma::sdesc(sa0 + kOpBytes + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
+      const uint64_t da30 = umma::sdesc(sa0 + 2 * kOpBytes, umma::kBlockLBO, umma::kBlockSBO);
       for (int64_t it = 0; it < nst; ++it) {
         const int s = (int)(it % kStages);
         const int buf = (int)(it % kWBufs);
@@ -117,9 +129,18 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
         const uint32_t d = tbase + buf * 128;
         const uint64_t so = (uint64_t)s * (kStageBytes >> 4);  // slot offset in the address field
         const uint64_t ahi = dahi0 + so, alo = dalo0 + so, bhi = dbhi0 + so, blo = dblo0 + so;
+        // Products from the smallest up, the hi*hi ones last (the accumulator's
+        // truncation is relative to its size at each instruction).
+        if (kThree) {
+          const uint64_t a3 = da30 + so;
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk)  // small correction products first
-          umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, kk == 0 ? 0u : 1u),
+          for (int kk = 0; kk < 4; ++kk)
+            umma::mma_tf32(d, alo + 16 * kk, blo + 16 * kk, idesc, kk == 0 ? 0u : 1u),
+                umma::mma_tf32(d, a3 + 16 * kk, bhi + 16 * kk, idesc, 1u);
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+          umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, (!kThree && kk == 0) ? 0u : 1u),
               umma::mma_tf32(d, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(d, ahi + 16 * kk, bhi + 16 * kk, idesc, 1u);
@@ -201,17 +222,27 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
 }  // namespace
 
 cudaError_t launch_tcg(const TcgArgs &a, int nsplit, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  static bool attr2 = false, attr3 = false;
+  if (!attr2) {
+    cudaError_t e = cudaFuncSetAttribute(tcg_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         Cfg<false>::kSmemBytes);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr2 = true;
+  }
+  if (!attr3) {
+    cudaError_t e = cudaFuncSetAttribute(tcg_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         Cfg<true>::kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr3 = true;
   }
   if (a.m_tiles <= 0 || a.n_tiles <= 0 || nsplit <= 0 || (a.out32 == nullptr) == (a.out64 == nullptr) ||
       (a.out32 && nsplit != 1) || a.k_chunks > a.a_chunks || a.k_chunks > a.b_chunks)
     return cudaErrorInvalidValue;
   dim3 grid(a.m_tiles * a.n_tiles, nsplit);
-  tcg_kernel<<<grid, kThreads, kSmemBytes, st>>>(a);
+  if (a.a3)
+    tcg_kernel<true><<<grid, kThreads, Cfg<true>::kSmemBytes, st>>>(a);
+  else
+    tcg_kernel<false><<<grid, kThreads, Cfg<false>::kSmemBytes, st>>>(a);
   return cudaGetLastError();
 }
 

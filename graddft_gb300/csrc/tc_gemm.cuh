@@ -8,6 +8,7 @@ namespace gdft {
 // D = A B^T over K, operands as [tile of 128 rows][K chunk of 32][hi|lo] blocks.
 struct TcgArgs {
   const float *a, *b;
+  const float *a3;             // optional third TF32 slice of A: [tile][K chunk] single blocks
   int m_tiles, n_tiles;       // 128-row tiles of A and of B
   int64_t a_chunks, b_chunks;  // K chunks stored per tile (tile stride)
   int64_t k_chunks;            // K chunks contracted (<= both)

@@ -8,7 +8,9 @@
 //   point-major  [point tile (128)][plane][AO chunk (32)][hi|lo] : 128 points x 32 AO
 //     (A operand of the density contraction and its epilogue partners)
 //   AO-major     [AO tile (128)][plane 0-3][point chunk (32)][hi|lo] : 128 AO x 32 points
-//     (A operand of the V_xc contraction, contracted over points)
+//     (A operand of the V_xc contraction, contracted over points), plus a third
+//     TF32 slice lo2 = tf32(x - hi - lo) of the same blocks in a separate array
+//     [AO tile][plane 0-3][point chunk]: hi + lo + lo2 ~= x to about 33 bits
 //   AO-major FP32 [AO tile (128)][plane][point chunk (32)] : the same blocks as single
 //     FP32 values (inputs of the B operand that is built per stage)
 // The density matrix is packed per call as the B operand of the density
@@ -47,7 +49,7 @@ __global__ void pack_tables_kernel(const double *__restrict__ ao, const double *
                                    const double *__restrict__ grad2_ao, const double *__restrict__ basis,
                                    const double *__restrict__ coords, const double *__restrict__ w, int64_t n_grid,
                                    int n_ao, int64_t np, int ldk, float *__restrict__ pm, float *__restrict__ am,
-                                   float *__restrict__ af, double *__restrict__ wout) {
+                                   float *__restrict__ am3, float *__restrict__ af, double *__restrict__ wout) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)np * ldk) return;
   const int64_t p = (int64_t)(idx / ldk);
@@ -112,7 +114,14 @@ __global__ void pack_tables_kernel(const double *__restrict__ ao, const double *
 #pragma unroll
   for (int t = 0; t < kPlanes; ++t) {
     store_split(pm, pm_block(tile, t, a / 32, nkc), umma::kblock_off((int)(p % 128), a % 32), v[t]);
-    if (t < 4) store_split(am, am_block(a / 128, t, p / 32, npc), umma::kblock_off(a % 128, (int)(p % 32)), v[t]);
+    if (t < 4) {
+      const uint32_t off = umma::kblock_off(a % 128, (int)(p % 32));
+      store_split(am, am_block(a / 128, t, p / 32, npc), off, v[t]);
+      float hi, lo;
+      umma::split_tf32(v[t], hi, lo);
+      am3[(am_block(a / 128, t, p / 32, npc) / 2) * (umma::kBlockBytes / 4) + off / 4] =
+          umma::tf32_rn((float)((v[t] - (double)hi) - (double)lo));
+    }
     af[af_block(a / 128, t, p / 32, npc) * (umma::kBlockBytes / 4) + umma::kblock_off(a % 128, (int)(p % 32)) / 4] =
         (float)v[t];
   }
@@ -137,15 +146,15 @@ __global__ void pack_rdm1_kernel(const double *__restrict__ D, int n, int ldk, f
 
 cudaError_t launch_pack_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *basis,
                                const double *coords, const double *w, int64_t n_grid, int n_ao, int64_t np, int ldk,
-                               float *pm, float *am, float *af, double *wout, cudaStream_t st) {
+                               float *pm, float *am, float *am3, float *af, double *wout, cudaStream_t st) {
   const size_t total = (size_t)np * ldk;
   const unsigned blocks = (unsigned)((total + 255) / 256);
   if (basis != nullptr)
     pack_tables_kernel<true><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
-                                                     pm, am, af, wout);
+                                                     pm, am, am3, af, wout);
   else
     pack_tables_kernel<false><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
-                                                      pm, am, af, wout);
+                                                      pm, am, am3, af, wout);
   return cudaGetLastError();
 }
 

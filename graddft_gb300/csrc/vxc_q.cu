@@ -8,8 +8,10 @@
 // vxc_f64.cu).  A memory-bound pre-pass forms Q for both spins once per call,
 // directly as TF32 hi/lo blocks in the AO-major layout of the AO tables; the
 // contraction is then tcg_kernel with A = the AO-major phi planes (K = 4
-// planes x grid points), B = Q of both spins (N = 2 x n_ao), split-K over the
-// grid, FP64 partials, and a reduction that also splits the spins.
+// planes x grid points) in three TF32 slices, B = Q of both spins (N = 2 x
+// n_ao) in two, split-K over the grid, FP64 partials, and a reduction that
+// also splits the spins.  Five products per term (hi*hi, hi*lo, lo*hi, lo*lo,
+// lo2*hi): the phi planes' representation, not Q's, limits the 3-product form.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "tc_gemm.cuh"
@@ -105,8 +107,9 @@ size_t vxc_q_bytes(int64_t np, int n_ao) {
   return (size_t)2 * 4 * np * ldk * 2 * sizeof(float);
 }
 
-cudaError_t launch_vxc_q_tc(const float *am, const float *af, const double *coef, int64_t np, int ldk, int n_ao,
-                            float *q, int nsplit, double *vpart, double *vxc, int *err, cudaStream_t st) {
+cudaError_t launch_vxc_q_tc(const float *am, const float *am3, const float *af, const double *coef, int64_t np,
+                            int ldk, int n_ao, float *q, int nsplit, double *vpart, double *vxc, int *err,
+                            cudaStream_t st) {
   const int nbt = ldk / 128;
   const int64_t npc = np / 32;
   build_q_kernel<<<(unsigned)(nbt * npc), 256, 0, st>>>(af, coef, np, nbt, q);
@@ -114,6 +117,7 @@ cudaError_t launch_vxc_q_tc(const float *am, const float *af, const double *coef
   if (e != cudaSuccess) return e;
   TcgArgs a{};
   a.a = am;
+  a.a3 = am3;  // third slice of phi: (1,1) and (2,0) products as well
   a.b = q;
   a.m_tiles = nbt;
   a.n_tiles = 2 * nbt;
