@@ -36,7 +36,7 @@ EXPORTS = (
     "gdft_umma_probe", "gdft_network_param_count", "gdft_neural_workspace_bytes",
     "gdft_neural_xc_energy_and_grads", "gdft_neural_inputs", "gdft_network_apply_workspace_bytes",
     "gdft_network_apply", "gdft_neural_hvp_workspace_bytes", "gdft_neural_xc_hvp", "gdft_tc_gemm_probe",
-    "gdft_neural_batch_workspace_bytes", "gdft_neural_batch_xc",
+    "gdft_tc_gemm3_probe", "gdft_neural_batch_workspace_bytes", "gdft_neural_batch_xc",
 )
 STAGE_AO, STAGE_DENSITY, STAGE_POINT, STAGE_VXC, STAGE_REDUCE, STAGE_MLP = range(6)
 
@@ -117,6 +117,7 @@ _SIGS = {
     "gdft_neural_hvp_workspace_bytes": ([PMOL, PNET, ctypes.POINTER(SZ)], ctypes.c_int),
     "gdft_neural_xc_hvp": ([PMOL, P, PNET, P, P, P, P, P, P, P, SZ, P], ctypes.c_int),
     "gdft_tc_gemm_probe": ([I32, I32, I32, I32, P, P, P], ctypes.c_int),
+    "gdft_tc_gemm3_probe": ([I32, I32, I32, I32, P, P, P], ctypes.c_int),
     "gdft_neural_batch_workspace_bytes": ([I32, P, PNET, ctypes.POINTER(SZ)], ctypes.c_int),
     "gdft_neural_batch_xc": ([I32, P, P, P, PNET, P, P, P, P, P, P, P, SZ, P], ctypes.c_int),
     "gdft_profile_enable": ([I32], ctypes.c_int),

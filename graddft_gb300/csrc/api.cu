@@ -68,19 +68,17 @@ MolLayout mol_layout(int64_t n_grid, int n_ao, int precision) {
   size_t off = 0;
   L.off_w = off;
   off = align256(off + (size_t)L.np * sizeof(double));
-  L.off_tab = L.off_pm = L.off_am = L.off_am3 = L.off_af = off;
+  L.off_tab = L.off_pm = L.off_av = L.off_af = off;
   if (precision == GDFT_FP64) {
     off = align256(off + (size_t)kPlanes * L.plane_elems() * sizeof(double));
   } else {
-    // Point-major hi/lo of the five planes, AO-major hi/lo of four planes and
-    // their third TF32 slice, and AO-major FP32 of the five planes.
+    // Point-major hi/lo of the five planes, AO-major block-scaled hi/lo/lo2 of
+    // four planes, and AO-major FP32 of the five planes.
     const size_t plane = (size_t)L.np * L.ldk * sizeof(float);
     L.off_pm = off;
     off = align256(off + kPlanes * 2 * plane);
-    L.off_am = off;
-    off = align256(off + 4 * 2 * plane);
-    L.off_am3 = off;
-    off = align256(off + 4 * plane);
+    L.off_av = off;
+    off = align256(off + 4 * 3 * plane);
     L.off_af = off;
     off = align256(off + kPlanes * plane);
   }
@@ -193,11 +191,8 @@ static const double *mol_w(const gdft_molecule *m) {
 static const float *mol_pm(const gdft_molecule *m) {
   return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_pm);
 }
-static const float *mol_am(const gdft_molecule *m) {
-  return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_am);
-}
-static const float *mol_am3(const gdft_molecule *m) {
-  return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_am3);
+static const float *mol_av(const gdft_molecule *m) {
+  return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_av);
 }
 static const float *mol_af(const gdft_molecule *m) {
   return (const float *)((const char *)m->buffer + mol_layout(m->n_grid, m->n_ao, m->precision).off_af);
@@ -352,7 +347,7 @@ static int run_vxc(const gdft_molecule *mol, const double *coef, double *d_vxc, 
     return check_cuda(launch_vxc_reduce(vpart, W.n_vsplit, mol->n_ao, d_vxc, st), "vxc_reduce");
   }
   StageTimer tm(GDFT_STAGE_VXC, st);
-  return check_cuda(launch_vxc_q_tc(mol_am(mol), mol_am3(mol), mol_af(mol), coef, mol->n_grid_pad, (int)round_up(mol->n_ao, 128),
+  return check_cuda(launch_vxc_q_tc(mol_av(mol), mol_af(mol), coef, mol->n_grid_pad, (int)round_up(mol->n_ao, 128),
                                     mol->n_ao, (float *)(ws + W.off_q), W.n_vsplit, vpart, d_vxc,
                                     (int *)(ws + W.off_err), st),
                     "vxc_q_tc");
@@ -452,8 +447,7 @@ int gdft_molecule_load(const gdft_molecule *mol, const double *d_ao, const doubl
   if (mol->precision == GDFT_TF32X3)
     return check_cuda(launch_pack_tables(d_ao, d_grad_ao, d_grad2_ao, nullptr, nullptr, d_weights, mol->n_grid,
                                          mol->n_ao, L.np, L.ldk, (float *)((char *)mol->buffer + L.off_pm),
-                                         (float *)((char *)mol->buffer + L.off_am),
-                                         (float *)((char *)mol->buffer + L.off_am3),
+                                         (float *)((char *)mol->buffer + L.off_av),
                                          (float *)((char *)mol->buffer + L.off_af), w, (cudaStream_t)stream),
                       "pack_tables");
   return check_cuda(launch_load_tables(d_ao, d_grad_ao, d_grad2_ao, d_weights, mol->n_grid, mol->n_ao, L.np, L.ld,
@@ -476,8 +470,7 @@ int gdft_molecule_eval_basis(const gdft_molecule *mol, const double *d_basis, co
   if (mol->precision == GDFT_TF32X3)
     return check_cuda(launch_pack_tables(nullptr, nullptr, nullptr, d_basis, d_coords, d_weights, mol->n_grid,
                                          mol->n_ao, L.np, L.ldk, (float *)((char *)mol->buffer + L.off_pm),
-                                         (float *)((char *)mol->buffer + L.off_am),
-                                         (float *)((char *)mol->buffer + L.off_am3),
+                                         (float *)((char *)mol->buffer + L.off_av),
                                          (float *)((char *)mol->buffer + L.off_af), w, (cudaStream_t)stream),
                       "pack_tables");
   return check_cuda(launch_eval_basis(d_basis, d_coords, d_weights, mol->n_grid, mol->n_ao, L.np, L.ld, tab, w,

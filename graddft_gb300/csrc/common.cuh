@@ -35,7 +35,7 @@ struct MolLayout {
   int64_t np;   // padded grid points
   int ld;       // AO leading dimension of the FP64 planes
   int ldk;      // AO extent of the TF32x3 tables (multiple of 128)
-  size_t off_tab, off_w, off_pm, off_am, off_am3, off_af, bytes;
+  size_t off_tab, off_w, off_pm, off_av, off_af, bytes;
   size_t plane_elems() const { return (size_t)np * ld; }
 };
 

@@ -24,15 +24,15 @@ cudaError_t launch_vxc_f64(const double *tab, int64_t np, int ld, int n_ao, cons
 // tc_pack.cu / dens_tc.cu: TF32x3 form.
 cudaError_t launch_pack_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *basis,
                                const double *coords, const double *w, int64_t n_grid, int n_ao, int64_t np, int ldk,
-                               float *pm, float *am, float *am3, float *af, double *wout, cudaStream_t st);
+                               float *pm, float *av, float *af, double *wout, cudaStream_t st);
 cudaError_t launch_pack_rdm1(const double *D, int n, int ldk, float *out, cudaStream_t st);
 cudaError_t launch_dens_tc(const float *pm, const float *dpk, int64_t np, int ldk, double *feat, int *err,
                            cudaStream_t st);
 
-// vxc_q.cu: TF32x3 V_xc as Q pre-pass + packed tensor-core GEMM.
+// vxc_q.cu: mixed V_xc as Q pre-pass + block-scaled three-slice tensor-core GEMM.
 int vxc_q_splits(int64_t np, int n_ao);
 size_t vxc_q_bytes(int64_t np, int n_ao);
-cudaError_t launch_vxc_q_tc(const float *am, const float *am3, const float *af, const double *coef, int64_t np,
+cudaError_t launch_vxc_q_tc(const float *av, const float *af, const double *coef, int64_t np,
                             int ldk, int n_ao, float *q, int nsplit, double *vpart, double *vxc, int *err,
                             cudaStream_t st);
 

@@ -1,24 +1,38 @@
-// tc_gemm.cu - TF32x3 tensor-core GEMM on pre-packed operand blocks (tcgen05).
+// tc_gemm.cu - tensor-core GEMMs on pre-packed operand blocks (tcgen05, kind::tf32).
 //
 //   D[M x N] = sum_K A[M x K] B[N x K]^T      (both operands K-major)
 //
-// Operands arrive as 16 KB blocks of 128 rows x 32 K (TF32 hi and lo images,
-// the K-major no-swizzle shared-memory layout of umma::kblock_off), stored
-// [row tile][K chunk][hi|lo]; one stage is one bulk copy of A (32 KB) and one
-// of B (32 KB).  Three products per term (hi*hi + hi*lo + lo*hi), M = 128,
-// N = 128 per CTA.  Accumulation: each 32-wide K chunk is accumulated in one
-// of three TMEM buffers W (128 columns each; the MMA runs up to two chunks
-// ahead of the drains), correction products first, and eight drain warps fold
-// it into a Kahan-compensated FP32 running sum: S in TMEM (128 columns), the
-// compensation C in registers (each drain thread owns one output row and 64
-// columns).  The K range may be split
-// across blockIdx.y (split-K); each split writes its S - C either as FP32 into
-// a row-major output (single split) or as FP64 partials [split][M][N].
+// Operands arrive as 16 KB blocks of 128 rows x 32 K in the K-major
+// no-swizzle shared-memory layout of umma::kblock_off, so that one stage is
+// one bulk copy per operand.  M = 128 and N = 128 per CTA; the K range may be
+// split across blockIdx.y, each split writing FP64 partials [split][M][N].
+//
+// tcg_kernel (TF32x3): blocks [tile][K chunk][hi|lo] of TF32 roundings, three
+// products per term (hi*hi + hi*lo + lo*hi).  Each 32-wide K chunk is
+// accumulated in one of three TMEM buffers W (the MMA runs up to two chunks
+// ahead of the drains), correction products first, and the drains fold it into
+// a Kahan-compensated FP32 running sum: S in TMEM (columns 384-511), the
+// compensation C in registers.  A single split may write FP32 output instead.
+//
+// tcg3_kernel (block-scaled, six products): blocks [tile][K chunk][hi|lo|lo2]
+// written by umma::store_row3, whose hi slices are quantised per row and K
+// chunk so that a chunk's hi*hi sum is exact in FP32.  The tensor core
+// truncates its FP32 accumulator toward zero; with plain TF32 slices that bias
+// adds up over the chunks of a long contraction (about 2^-23 of the result
+// where the chunk sums share a sign).  Here the hi*hi products go to an
+// accumulator Y of their own, which stays exact, and the five correction
+// products (hi*lo, lo*hi, lo*lo, hi*lo2, lo2*hi, all below 2^-10 of the terms)
+// to a second accumulator X.  Two TMEM buffers of (Y, X) take all 512 columns.
+// The drains fold Y and X into a running FP32 sum S held in registers (TwoSum
+// for Y, Fast2Sum for the small X) and store the rounding errors back into the
+// X they just read: the MMA accumulates that buffer's next corrections on top
+// of them (X is never reset), so the compensation travels in TMEM and the two
+// pending ones are added at the end.
 //
 // Warp roles (320 threads): warp 0 = TMA producer, warp 1 = TMEM owner and
 // MMA issuer, warps 2-9 = drains (TMEM lane quadrant warp % 4, column half
-// (warp - 2) / 4).  All waits are bounded; on expiry the CTA records an error
-// word and winds down.
+// (warp - 2) / 4; each drain thread owns one output row and 64 columns).  All
+// waits are bounded; on expiry the CTA records an error word and winds down.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "tc_gemm.cuh"
@@ -28,25 +42,22 @@ namespace gdft {
 
 namespace {
 
-constexpr uint32_t kOpBytes = 2 * umma::kBlockBytes;   // hi | lo of one 128 x 32 block
-// Stage = A hi|lo, B hi|lo (and, with a third A slice, that block too).
-template <bool kThree>
-struct Cfg {
-  static constexpr uint32_t kStageBytes = 2 * kOpBytes + (kThree ? umma::kBlockBytes : 0);
-  static constexpr int kStages = kThree ? 2 : 3;
-  static constexpr int kSmemBytes = kStages * kStageBytes + 1024;
-};
+constexpr uint32_t kOpBytes = 2 * umma::kBlockBytes;    // hi | lo of one 128 x 32 block
+constexpr uint32_t kStageBytes = 2 * kOpBytes;          // A hi|lo, B hi|lo
+constexpr int kStages = 3;
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;
+constexpr uint32_t kOp3Bytes = 3 * umma::kBlockBytes;   // hi | lo | lo2
+constexpr uint32_t kStage3Bytes = 2 * kOp3Bytes;        // A, B
+constexpr int kStages3 = 2;
+constexpr int kSmem3Bytes = kStages3 * kStage3Bytes + 1024;
 constexpr int kThreads = 320;
 constexpr int kWBufs = 3;
-constexpr uint32_t kTmemCols = 512;  // W0..W2 [0, 384), S [384, 512)
+constexpr uint32_t kTmemCols = 512;  // tcg: W0..W2 [0, 384), S [384, 512); tcg3: (Y, X) x 2
 constexpr uint32_t kScol = 384;
 
 __device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, code); }
 
-template <bool kThree>
 __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
-  constexpr int kStages = Cfg<kThree>::kStages;
-  constexpr uint32_t kStageBytes = Cfg<kThree>::kStageBytes;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full[kStages], empty[kStages], wfull[kWBufs], wempty[kWBufs], drain;
@@ -76,7 +87,6 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
   umma::tc_fence_after();
   const uint32_t tbase = tmem_base;
   const float *a_tile = A.a + (size_t)mt * A.a_chunks * (kOpBytes / 4);
-  const float *a3_tile = kThree ? A.a3 + (size_t)mt * A.a_chunks * (umma::kBlockBytes / 4) : nullptr;
   const float *b_tile = A.b + (size_t)nt * A.b_chunks * (kOpBytes / 4);
 
   if (warp == 0) {
@@ -94,9 +104,6 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
         umma::mbar_arrive_expect_tx(&full[s], kStageBytes);
         umma::bulk_g2s(smem + s * kStageBytes, a_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
         umma::bulk_g2s(smem + s * kStageBytes + kOpBytes, b_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
-        if (kThree)
-          umma::bulk_g2s(smem + s * kStageBytes + 2 * kOpBytes, a3_tile + (size_t)kc * (umma::kBlockBytes / 4),
-                         umma::kBlockBytes, &full[s]);
       }
       // Our own copies land before the CTA can release shared memory.
       for (int64_t i = it > kStages ? it - kStages : 0; i < it; ++i)
@@ -116,7 +123,6 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
       const uint64_t dalo0 = umma::sdesc(sa0 + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
       const uint64_t dbhi0 = umma::sdesc(sa0 + kOpBytes, umma::kBlockLBO, umma::kBlockSBO);
       const uint64_t dblo0 = umma::sdesc(sa0 + kOpBytes + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
-      const uint64_t da30 = umma::sdesc(sa0 + 2 * kOpBytes, umma::kBlockLBO, umma::kBlockSBO);
       for (int64_t it = 0; it < nst; ++it) {
         const int s = (int)(it % kStages);
         const int buf = (int)(it % kWBufs);
@@ -131,16 +137,9 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
         const uint64_t ahi = dahi0 + so, alo = dalo0 + so, bhi = dbhi0 + so, blo = dblo0 + so;
         // Products from the smallest up, the hi*hi ones last (the accumulator's
         // truncation is relative to its size at each instruction).
-        if (kThree) {
-          const uint64_t a3 = da30 + so;
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            umma::mma_tf32(d, alo + 16 * kk, blo + 16 * kk, idesc, kk == 0 ? 0u : 1u),
-                umma::mma_tf32(d, a3 + 16 * kk, bhi + 16 * kk, idesc, 1u);
-        }
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk)
-          umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, (!kThree && kk == 0) ? 0u : 1u),
+          umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, kk == 0 ? 0u : 1u),
               umma::mma_tf32(d, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(d, ahi + 16 * kk, bhi + 16 * kk, idesc, 1u);
@@ -219,30 +218,207 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
   if (warp == 1) umma::tmem_dealloc(tbase, kTmemCols);
 }
 
+__global__ void __launch_bounds__(kThreads, 1) tcg3_kernel(const TcgArgs A) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full[kStages3], empty[kStages3], wfull[2], wempty[2], drain;
+  __shared__ uint32_t tmem_base;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x % A.m_tiles, nt = blockIdx.x / A.m_tiles;
+  const int64_t c0 = (int64_t)blockIdx.y * A.chunks_per_split;
+  const int64_t c1 = c0 + A.chunks_per_split < A.k_chunks ? c0 + A.chunks_per_split : A.k_chunks;
+  const int64_t nst = c1 > c0 ? c1 - c0 : 0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages3; ++s) {
+      umma::mbar_init(&full[s], 1);
+      umma::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      umma::mbar_init(&wfull[b], 1);
+      umma::mbar_init(&wempty[b], 256);
+    }
+    umma::mbar_init(&drain, 1);
+    umma::fence_barrier_init();
+  }
+  if (warp == 1) umma::tmem_alloc(&tmem_base, kTmemCols);
+  umma::tc_fence_before();
+  __syncthreads();
+  umma::tc_fence_after();
+  const uint32_t tbase = tmem_base;
+  if (warp >= 2) {  // both X accumulators start at zero (the MMA only ever accumulates into them)
+    const uint32_t tl = tbase + ((uint32_t)((warp & 3) * 32) << 16) + ((warp - 2) >> 2) * 64;
+    uint32_t z[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) z[i] = 0u;
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int c = 0; c < 64; c += 16) umma::tmem_st16(tl + b * 256 + 128 + c, z);
+    umma::tmem_st_wait();
+  }
+  umma::tc_fence_before();
+  __syncthreads();
+  umma::tc_fence_after();
+  const float *a_tile = A.a + (size_t)mt * A.a_chunks * (kOp3Bytes / 4);
+  const float *b_tile = A.b + (size_t)nt * A.b_chunks * (kOp3Bytes / 4);
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      int64_t it = 0;
+      for (; it < nst; ++it) {
+        const int s = (int)(it % kStages3);
+        if (!umma::mbar_wait(&empty[s], ((it / kStages3) & 1) ^ 1)) {
+          flag(A.err, 51);
+          break;
+        }
+        const int64_t kc = c0 + it;
+        umma::mbar_arrive_expect_tx(&full[s], kStage3Bytes);
+        umma::bulk_g2s(smem + s * kStage3Bytes, a_tile + (size_t)kc * (kOp3Bytes / 4), kOp3Bytes, &full[s]);
+        umma::bulk_g2s(smem + s * kStage3Bytes + kOp3Bytes, b_tile + (size_t)kc * (kOp3Bytes / 4), kOp3Bytes,
+                       &full[s]);
+      }
+      for (int64_t i = it > kStages3 ? it - kStages3 : 0; i < it; ++i)
+        if (!umma::mbar_wait(&full[i % kStages3], (i / kStages3) & 1)) flag(A.err, 52);
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------------------------------------------------- MMA issuer
+    // Descriptors of slot 0's hi blocks; lo and lo2 add one and two blocks
+    // (1024 and 2048 in the address field), a slot (96 KB) adds 6144, a K step
+    // of 8 adds 16.
+    if (lane == 0) {
+      const uint32_t idesc = umma::idesc_tf32(128, 128);
+      const uint32_t sa0 = umma::smem_u32(smem);
+      constexpr uint64_t kBlk = umma::kBlockBytes >> 4;
+      const uint64_t da0 = umma::sdesc(sa0, umma::kBlockLBO, umma::kBlockSBO);
+      const uint64_t db0 = umma::sdesc(sa0 + kOp3Bytes, umma::kBlockLBO, umma::kBlockSBO);
+      for (int64_t it = 0; it < nst; ++it) {
+        const int s = (int)(it % kStages3);
+        const int buf = (int)(it & 1);
+        if (!umma::mbar_wait(&wempty[buf], ((it >> 1) & 1) ^ 1) ||
+            !umma::mbar_wait(&full[s], (it / kStages3) & 1)) {
+          flag(A.err, 53);
+          break;
+        }
+        umma::tc_fence_after();
+        const uint32_t y = tbase + buf * 256, x = y + 128;
+        const uint64_t so = (uint64_t)s * (kStage3Bytes >> 4);
+        const uint64_t ahi = da0 + so, alo = ahi + kBlk, alo2 = ahi + 2 * kBlk;
+        const uint64_t bhi = db0 + so, blo = bhi + kBlk, blo2 = bhi + 2 * kBlk;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+          umma::mma_tf32(x, alo + 16 * kk, blo + 16 * kk, idesc, 1u),
+              umma::mma_tf32(x, ahi + 16 * kk, blo2 + 16 * kk, idesc, 1u),
+              umma::mma_tf32(x, alo2 + 16 * kk, bhi + 16 * kk, idesc, 1u);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+          umma::mma_tf32(x, ahi + 16 * kk, blo + 16 * kk, idesc, 1u),
+              umma::mma_tf32(x, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(y, ahi + 16 * kk, bhi + 16 * kk, idesc, kk == 0 ? 0u : 1u);
+        umma::mma_commit(&empty[s]);
+        umma::mma_commit(&wfull[buf]);
+      }
+      umma::mma_commit(&drain);
+      if (!umma::mbar_wait(&drain, 0)) flag(A.err, 55);
+    }
+    __syncwarp();
+  } else {
+    // -------------------------------------------------------------- drains
+    const int q = warp & 3, half = (warp - 2) >> 2;
+    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16) + half * 64;
+    float S[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) S[i] = 0.0f;
+    int64_t it = 0;
+    for (; it < nst; ++it) {
+      const int buf = (int)(it & 1);
+      if (!umma::warp_wait(&wfull[buf], (it >> 1) & 1)) {
+        if (lane == 0) flag(A.err, 56);
+        break;
+      }
+      umma::tc_fence_after();
+#pragma unroll
+      for (int c = 0; c < 64; c += 16) {
+        uint32_t yr[16], xr[16];
+        umma::tmem_ld16_nowait(tl + buf * 256 + c, yr);
+        umma::tmem_ld16_nowait(tl + buf * 256 + 128 + c, xr);
+        umma::tmem_ld_wait(yr, xr);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          // S + Y = t + e1 exactly (TwoSum); t + X = u + e2 (Fast2Sum: X is
+          // below 2^-10 of the chunk's terms, t holds the sum so far).
+          const float yv = __uint_as_float(yr[i]), xv = __uint_as_float(xr[i]);
+          const float t = S[c + i] + yv;
+          const float bp = t - S[c + i];
+          const float e1 = (S[c + i] - (t - bp)) + (yv - bp);
+          const float u = t + xv;
+          const float e2 = xv - (u - t);
+          S[c + i] = u;
+          xr[i] = __float_as_uint(e1 + e2);
+        }
+        umma::tmem_st16(tl + buf * 256 + 128 + c, xr);
+      }
+      umma::tmem_st_wait();
+      umma::tc_fence_before();
+      umma::mbar_arrive(&wempty[buf]);
+    }
+    const bool have = it == nst;
+    const int m = mt * 128 + q * 32 + lane;
+    const int n0 = nt * 128 + half * 64;
+    double *row = A.out64 + ((size_t)blockIdx.y * A.m_valid + (m < A.m_valid ? m : 0)) * A.n_valid + n0;
+#pragma unroll
+    for (int c = 0; c < 64; c += 16) {  // S plus the two compensations still pending in X
+      uint32_t e0[16], e1[16];
+      umma::tmem_ld16_nowait(tl + 128 + c, e0);
+      umma::tmem_ld16_nowait(tl + 256 + 128 + c, e1);
+      umma::tmem_ld_wait(e0, e1);
+      if (m < A.m_valid) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          if (n0 + c + i < A.n_valid)
+            row[c + i] = have ? ((double)S[c + i] + (double)__uint_as_float(e0[i])) + (double)__uint_as_float(e1[i])
+                              : 0.0;
+      }
+    }
+  }
+  umma::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) umma::tmem_dealloc(tbase, kTmemCols);
+}
+
 }  // namespace
 
 cudaError_t launch_tcg(const TcgArgs &a, int nsplit, cudaStream_t st) {
-  static bool attr2 = false, attr3 = false;
-  if (!attr2) {
-    cudaError_t e = cudaFuncSetAttribute(tcg_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         Cfg<false>::kSmemBytes);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     if (e != cudaSuccess) return e;
-    attr2 = true;
-  }
-  if (!attr3) {
-    cudaError_t e = cudaFuncSetAttribute(tcg_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         Cfg<true>::kSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr3 = true;
+    attr = true;
   }
   if (a.m_tiles <= 0 || a.n_tiles <= 0 || nsplit <= 0 || (a.out32 == nullptr) == (a.out64 == nullptr) ||
       (a.out32 && nsplit != 1) || a.k_chunks > a.a_chunks || a.k_chunks > a.b_chunks)
     return cudaErrorInvalidValue;
   dim3 grid(a.m_tiles * a.n_tiles, nsplit);
-  if (a.a3)
-    tcg_kernel<true><<<grid, kThreads, Cfg<true>::kSmemBytes, st>>>(a);
-  else
-    tcg_kernel<false><<<grid, kThreads, Cfg<false>::kSmemBytes, st>>>(a);
+  tcg_kernel<<<grid, kThreads, kSmemBytes, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tcg3(const TcgArgs &a, int nsplit, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tcg3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem3Bytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  if (a.m_tiles <= 0 || a.n_tiles <= 0 || nsplit <= 0 || a.out64 == nullptr || a.out32 != nullptr ||
+      a.k_chunks > a.a_chunks || a.k_chunks > a.b_chunks)
+    return cudaErrorInvalidValue;
+  dim3 grid(a.m_tiles * a.n_tiles, nsplit);
+  tcg3_kernel<<<grid, kThreads, kSmem3Bytes, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -318,7 +494,30 @@ __global__ void pack_ct_kernel(const T *__restrict__ X, int64_t rows, int cols, 
   }
 }
 
+// One CTA of 128 threads per block set, one row per thread.
+__global__ void __launch_bounds__(128) pack_rt3_kernel(const double *__restrict__ X, int64_t rows, int cols, int ld,
+                                                       int kchunks, float *__restrict__ out) {
+  const int64_t t = blockIdx.x / kchunks;
+  const int kc = blockIdx.x % kchunks;
+  const int row = threadIdx.x;
+  const int64_t r = t * 128 + row;
+  double v[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    const int c = kc * 32 + k;
+    v[k] = (r < rows && c < cols) ? X[(size_t)r * ld + c] : 0.0;
+  }
+  umma::store_row3(out + (size_t)blockIdx.x * 3 * (umma::kBlockBytes / 4), row, v);
+}
+
 }  // namespace
+
+cudaError_t launch_pack_rt3(const double *X, int64_t rows, int cols, int ld, int64_t tiles, int kchunks, float *out,
+                            cudaStream_t st) {
+  if (tiles <= 0 || kchunks <= 0) return cudaErrorInvalidValue;
+  pack_rt3_kernel<<<(unsigned)(tiles * kchunks), 128, 0, st>>>(X, rows, cols, ld, kchunks, out);
+  return cudaGetLastError();
+}
 
 template <class T>
 cudaError_t launch_pack_rt(const T *X, int64_t rows, int cols, int ld, int64_t tiles, int kchunks, float *out,
@@ -343,21 +542,23 @@ template cudaError_t launch_pack_ct<double>(const double *, int64_t, int, int, i
 
 }  // namespace gdft
 
-// Host-array probe of the packed TF32x3 GEMM (synchronous; allocates its own
-// buffers): D (M x N, FP64) = A (M x K) B (N x K)^T, through the row-tile packer
-// and tcg_kernel, FP32 output for nsplit == 1, FP64 split-K partials summed on
-// the host otherwise.
-extern "C" int gdft_tc_gemm_probe(int32_t M, int32_t N, int32_t K, int32_t nsplit, const double *h_a,
-                                  const double *h_b, double *h_d) {
+// Host-array probes of the packed GEMMs (synchronous; they allocate their own
+// buffers): D (M x N, FP64) = A (M x K) B (N x K)^T through a row-tile packer
+// and the kernel; FP32 output for a single split of the TF32x3 form, FP64
+// split-K partials summed on the host otherwise.
+static int tc_gemm_probe(bool three, int32_t M, int32_t N, int32_t K, int32_t nsplit, const double *h_a,
+                         const double *h_b, double *h_d) {
   using namespace gdft;
+  const char *name = three ? "gdft_tc_gemm3_probe" : "gdft_tc_gemm_probe";
   if (M <= 0 || N <= 0 || K <= 0 || nsplit <= 0 || !h_a || !h_b || !h_d || M > 4096 || N > 4096 ||
       K > (1 << 20)) {
-    set_error("gdft_tc_gemm_probe: invalid arguments");
+    set_error("%s: invalid arguments", name);
     return GDFT_ERR_INVALID;
   }
   const int mt = (M + 127) / 128, ntl = (N + 127) / 128;
   const int64_t kch = (K + 31) / 32;
-  const size_t blk = 2 * (umma::kBlockBytes / 4);
+  const size_t blk = (three ? 3 : 2) * (umma::kBlockBytes / 4);
+  const bool f32out = !three && nsplit == 1;
   double *dA = nullptr, *dB = nullptr, *d64 = nullptr;
   float *pA = nullptr, *pB = nullptr, *d32 = nullptr;
   int *err = nullptr;
@@ -375,8 +576,10 @@ extern "C" int gdft_tc_gemm_probe(int32_t M, int32_t N, int32_t K, int32_t nspli
       ck(cudaMemset(err, 0, 4), "probe memset") &&
       ck(cudaMemcpy(dA, h_a, (size_t)M * K * 8, cudaMemcpyHostToDevice), "probe copy") &&
       ck(cudaMemcpy(dB, h_b, (size_t)N * K * 8, cudaMemcpyHostToDevice), "probe copy") &&
-      ck(launch_pack_rt<double>(dA, M, K, K, mt, (int)kch, pA, 0), "probe pack A") &&
-      ck(launch_pack_rt<double>(dB, N, K, K, ntl, (int)kch, pB, 0), "probe pack B")) {
+      ck(three ? launch_pack_rt3(dA, M, K, K, mt, (int)kch, pA, 0) : launch_pack_rt<double>(dA, M, K, K, mt, (int)kch, pA, 0),
+         "probe pack A") &&
+      ck(three ? launch_pack_rt3(dB, N, K, K, ntl, (int)kch, pB, 0) : launch_pack_rt<double>(dB, N, K, K, ntl, (int)kch, pB, 0),
+         "probe pack B")) {
     TcgArgs a{};
     a.a = pA;
     a.b = pB;
@@ -384,19 +587,20 @@ extern "C" int gdft_tc_gemm_probe(int32_t M, int32_t N, int32_t K, int32_t nspli
     a.n_tiles = ntl;
     a.a_chunks = a.b_chunks = a.k_chunks = kch;
     a.chunks_per_split = nsplit == 1 ? kch : cps;
-    a.out32 = nsplit == 1 ? d32 : nullptr;
+    a.out32 = f32out ? d32 : nullptr;
     a.ldo = N;
-    a.out64 = nsplit == 1 ? nullptr : d64;
+    a.out64 = f32out ? nullptr : d64;
     a.m_valid = M;
     a.n_valid = N;
     a.err = err;
-    if (ck(launch_tcg(a, nsplit, 0), "probe tcg") && ck(cudaDeviceSynchronize(), "probe sync")) {
+    if (ck(three ? launch_tcg3(a, nsplit, 0) : launch_tcg(a, nsplit, 0), "probe tcg") &&
+        ck(cudaDeviceSynchronize(), "probe sync")) {
       int herr = 0;
       if (ck(cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost), "probe err")) {
         if (herr) {
-          set_error("gdft_tc_gemm_probe: bounded wait expired (code %d)", herr);
+          set_error("%s: bounded wait expired (code %d)", name, herr);
           rc = GDFT_ERR_DEVICE;
-        } else if (nsplit == 1) {
+        } else if (f32out) {
           float *tmp = new float[(size_t)M * N];
           if (ck(cudaMemcpy(tmp, d32, (size_t)M * N * 4, cudaMemcpyDeviceToHost), "probe out"))
             for (size_t i = 0; i < (size_t)M * N; ++i) h_d[i] = tmp[i];
@@ -422,4 +626,14 @@ extern "C" int gdft_tc_gemm_probe(int32_t M, int32_t N, int32_t K, int32_t nspli
   cudaFree(d64);
   cudaFree(err);
   return rc;
+}
+
+extern "C" int gdft_tc_gemm_probe(int32_t M, int32_t N, int32_t K, int32_t nsplit, const double *h_a,
+                                  const double *h_b, double *h_d) {
+  return tc_gemm_probe(false, M, N, K, nsplit, h_a, h_b, h_d);
+}
+
+extern "C" int gdft_tc_gemm3_probe(int32_t M, int32_t N, int32_t K, int32_t nsplit, const double *h_a,
+                                   const double *h_b, double *h_d) {
+  return tc_gemm_probe(true, M, N, K, nsplit, h_a, h_b, h_d);
 }

@@ -1,18 +1,18 @@
 // tc_pack.cu - operand layouts of the TF32x3 (mixed) form.
 //
-// The AO planes (phi, d_x phi, d_y phi, d_z phi, lap phi) are kept resident as
-// pairs of TF32 values (hi + lo ~= the FP64 value to about 22 bits) in two
-// pre-tiled layouts whose 16 KB blocks are exactly the shared-memory images
-// the tensor cores read (K-major, no swizzle, see umma::kblock_off), so every
+// The AO planes (phi, d_x phi, d_y phi, d_z phi, lap phi) are kept resident in
+// pre-tiled layouts whose 16 KB blocks are exactly the shared-memory images the
+// tensor cores read (K-major, no swizzle, see umma::kblock_off), so every
 // operand stage is one contiguous bulk copy:
-//   point-major  [point tile (128)][plane][AO chunk (32)][hi|lo] : 128 points x 32 AO
+//   point-major  [point tile (128)][plane][AO chunk (32)][hi|lo] : 128 points x 32 AO,
+//     TF32 pairs hi + lo ~= the FP64 value to about 22 bits
 //     (A operand of the density contraction and its epilogue partners)
-//   AO-major     [AO tile (128)][plane 0-3][point chunk (32)][hi|lo] : 128 AO x 32 points
-//     (A operand of the V_xc contraction, contracted over points), plus a third
-//     TF32 slice lo2 = tf32(x - hi - lo) of the same blocks in a separate array
-//     [AO tile][plane 0-3][point chunk]: hi + lo + lo2 ~= x to about 33 bits
+//   AO-major     [AO tile (128)][plane 0-3][point chunk (32)][hi|lo|lo2] : 128 AO x 32 points,
+//     block-scaled three-slice sets (umma::store_row3: hi quantised per AO and
+//     point chunk, hi + lo + lo2 ~= x to about 2^-33 of the chunk's largest value)
+//     (A operand of the V_xc contraction, contracted over points)
 //   AO-major FP32 [AO tile (128)][plane][point chunk (32)] : the same blocks as single
-//     FP32 values (inputs of the B operand that is built per stage)
+//     FP32 values (inputs of the B operand that is built per call)
 // The density matrix is packed per call as the B operand of the density
 // contraction: [spin][column tile (128)][k chunk (32)][hi|lo], element (c, k) = D[k][c].
 #include "common.cuh"
@@ -26,8 +26,8 @@ namespace {
 __device__ __forceinline__ size_t pm_block(int64_t tile, int plane, int kc, int nkc) {
   return ((size_t)(tile * kPlanes + plane) * nkc + kc) * 2;  // in units of 16 KB blocks (hi; lo = +1)
 }
-__device__ __forceinline__ size_t am_block(int atile, int plane, int64_t pc, int64_t npc) {
-  return ((size_t)(atile * 4 + plane) * npc + pc) * 2;
+__device__ __forceinline__ size_t av_set(int atile, int plane, int64_t pc, int64_t npc) {
+  return (size_t)(atile * 4 + plane) * npc + pc;  // in units of three-block sets (48 KB)
 }
 __device__ __forceinline__ size_t af_block(int atile, int plane, int64_t pc, int64_t npc) {
   return (size_t)(atile * kPlanes + plane) * npc + pc;
@@ -43,13 +43,16 @@ __device__ __forceinline__ void store_split(float *base, size_t blk, uint32_t of
 
 // One thread per (point, AO) of the padded tables: computes the five plane
 // values (from reference layouts or from the synthetic basis) and scatters
-// them, split, into both layouts.
+// them into the point-major and FP32 layouts.  The AO-major three-slice sets
+// need each AO's maximum over a point chunk first: this pass parks the FP64
+// values of a set, [point (32)][AO (128)], in the set's own first 32 KB and
+// pack_av_kernel splits them in place.
 template <bool kBasis>
 __global__ void pack_tables_kernel(const double *__restrict__ ao, const double *__restrict__ grad_ao,
                                    const double *__restrict__ grad2_ao, const double *__restrict__ basis,
                                    const double *__restrict__ coords, const double *__restrict__ w, int64_t n_grid,
-                                   int n_ao, int64_t np, int ldk, float *__restrict__ pm, float *__restrict__ am,
-                                   float *__restrict__ am3, float *__restrict__ af, double *__restrict__ wout) {
+                                   int n_ao, int64_t np, int ldk, float *__restrict__ pm, float *__restrict__ av,
+                                   float *__restrict__ af, double *__restrict__ wout) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)np * ldk) return;
   const int64_t p = (int64_t)(idx / ldk);
@@ -114,18 +117,26 @@ __global__ void pack_tables_kernel(const double *__restrict__ ao, const double *
 #pragma unroll
   for (int t = 0; t < kPlanes; ++t) {
     store_split(pm, pm_block(tile, t, a / 32, nkc), umma::kblock_off((int)(p % 128), a % 32), v[t]);
-    if (t < 4) {
-      const uint32_t off = umma::kblock_off(a % 128, (int)(p % 32));
-      store_split(am, am_block(a / 128, t, p / 32, npc), off, v[t]);
-      float hi, lo;
-      umma::split_tf32(v[t], hi, lo);
-      am3[(am_block(a / 128, t, p / 32, npc) / 2) * (umma::kBlockBytes / 4) + off / 4] =
-          umma::tf32_rn((float)((v[t] - (double)hi) - (double)lo));
-    }
+    if (t < 4)
+      ((double *)(av + av_set(a / 128, t, p / 32, npc) * 3 * (umma::kBlockBytes / 4)))[(p % 32) * 128 + a % 128] =
+          v[t];
     af[af_block(a / 128, t, p / 32, npc) * (umma::kBlockBytes / 4) + umma::kblock_off(a % 128, (int)(p % 32)) / 4] =
         (float)v[t];
   }
   if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
+}
+
+// One CTA of 128 threads per AO-major set, one AO row per thread: reads the
+// parked FP64 values, then (after the whole CTA has read) writes hi|lo|lo2 over them.
+__global__ void __launch_bounds__(128) pack_av_kernel(float *__restrict__ av) {
+  float *set = av + (size_t)blockIdx.x * 3 * (umma::kBlockBytes / 4);
+  const double *parked = (const double *)set;
+  const int row = threadIdx.x;
+  double v[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = parked[k * 128 + row];
+  __syncthreads();
+  umma::store_row3(set, row, v);
 }
 
 // D (2, n, n) -> [spin][column tile][k chunk][hi|lo] blocks with (c, k) = D[k][c].
@@ -146,15 +157,18 @@ __global__ void pack_rdm1_kernel(const double *__restrict__ D, int n, int ldk, f
 
 cudaError_t launch_pack_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *basis,
                                const double *coords, const double *w, int64_t n_grid, int n_ao, int64_t np, int ldk,
-                               float *pm, float *am, float *am3, float *af, double *wout, cudaStream_t st) {
+                               float *pm, float *av, float *af, double *wout, cudaStream_t st) {
   const size_t total = (size_t)np * ldk;
   const unsigned blocks = (unsigned)((total + 255) / 256);
   if (basis != nullptr)
     pack_tables_kernel<true><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
-                                                     pm, am, am3, af, wout);
+                                                     pm, av, af, wout);
   else
     pack_tables_kernel<false><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
-                                                      pm, am, am3, af, wout);
+                                                      pm, av, af, wout);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  pack_av_kernel<<<(unsigned)((size_t)(ldk / 128) * 4 * (np / 32)), 128, 0, st>>>(av);
   return cudaGetLastError();
 }
 

@@ -150,6 +150,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Issue a 16-column TMEM load without waiting.
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&a)[16], uint32_t (&b)[16]) {
+  tmem_ld_wait();
+#pragma unroll
+  for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(a[i]), "+r"(b[i]));
+}
+
 // Store 32 consecutive 32-bit TMEM columns of this thread's lane (warp-collective).
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) {
   asm volatile(
@@ -166,6 +181,15 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) 
       "r"(__float_as_uint(v[23])), "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])),
       "r"(__float_as_uint(v[26])), "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])),
       "r"(__float_as_uint(v[29])), "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+      : "memory");
+}
+// Store 16 consecutive 32-bit TMEM columns of this thread's lane (warp-collective).
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
       : "memory");
 }
 __device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
@@ -230,6 +254,45 @@ __device__ __forceinline__ void split_tf32f(float x, float &hi, float &lo) {
   lo = tf32_rn(x - hi);
 }
 
+// ------------------------------------------- block-scaled three-slice split
+// x = hi + lo + lo2 (+ about 2^-33 of the block row's largest magnitude m),
+// where hi is x rounded to the row's quantum q = 2^(E - 9), 2^(E-1) <= m < 2^E
+// (|hi| <= 512 q: at most ten significant bits), and lo, lo2 are TF32
+// roundings of the remainders.  All hi values of a row share q, so a sum of
+// 32 products hi_a * hi_b of two such rows is a multiple of q_a q_b below
+// 2^23 q_a q_b: exact in an FP32 accumulator, whatever the tensor core's
+// alignment and truncation.  Rows whose quantum would leave the FP32 normal
+// range keep hi = 0.
+struct Quant {
+  float q, inv;
+};
+__device__ __forceinline__ Quant quant(float m) {
+  const uint32_t eb = (__float_as_uint(m) >> 23) & 0xFFu;  // m in [2^(eb-127), 2^(eb-126))
+  Quant u;
+  if (eb >= 9u && eb < 255u) {
+    u.q = __uint_as_float((eb - 8u) << 23);     // 2^(eb - 135)
+    u.inv = __uint_as_float((262u - eb) << 23);  // 2^(135 - eb)
+  } else {
+    u.q = 0.0f;
+    u.inv = 0.0f;
+  }
+  return u;
+}
+// FP32 source: every step is exact except the two TF32 roundings.
+__device__ __forceinline__ void split3(float x, Quant u, float &hi, float &lo, float &lo2) {
+  hi = rintf(x * u.inv) * u.q;
+  const float r = x - hi;
+  lo = tf32_rn(r);
+  lo2 = tf32_rn(r - lo);
+}
+// FP64 source (the remainders are taken in FP64).
+__device__ __forceinline__ void split3(double x, Quant u, float &hi, float &lo, float &lo2) {
+  hi = (float)(rint(x * (double)u.inv) * (double)u.q);
+  const double r = x - (double)hi;
+  lo = tf32_rn((float)r);
+  lo2 = tf32_rn((float)(r - (double)lo));
+}
+
 // Byte offset of element (row, k) inside a K-major no-swizzle block of
 // `rows` x 32 fp32 (core matrices 8 rows x 4 elements; row-groups of 8 at
 // 1024 bytes, k-groups of 4 at 128 bytes): LBO = 128, SBO = 1024.
@@ -239,6 +302,28 @@ __host__ __device__ constexpr uint32_t kblock_off(int row, int k) {
 constexpr uint32_t kBlockLBO = 128, kBlockSBO = 1024;
 // A block of 128 rows x 32 fp32 = 16 KB.
 constexpr uint32_t kBlockBytes = 128 * 32 * 4;
+
+// Writes one row (32 K values) of a three-slice block set [hi | lo | lo2]
+// (three consecutive 16 KB blocks), quantised on the row's own maximum.
+template <class T>
+__device__ __forceinline__ void store_row3(float *blk3, int row, const T (&v)[32]) {
+  T m = 0;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) m = fmax(m, fabs(v[k]));
+  const Quant u = quant((float)m);
+#pragma unroll
+  for (int k4 = 0; k4 < 8; ++k4) {
+    float4 h, l, l2;
+    split3(v[4 * k4 + 0], u, h.x, l.x, l2.x);
+    split3(v[4 * k4 + 1], u, h.y, l.y, l2.y);
+    split3(v[4 * k4 + 2], u, h.z, l.z, l2.z);
+    split3(v[4 * k4 + 3], u, h.w, l.w, l2.w);
+    const uint32_t off = kblock_off(row, 4 * k4) / 4;
+    *(float4 *)(blk3 + off) = h;
+    *(float4 *)(blk3 + kBlockBytes / 4 + off) = l;
+    *(float4 *)(blk3 + kBlockBytes / 2 + off) = l2;
+  }
+}
 
 }  // namespace umma
 }  // namespace gdft

@@ -1,4 +1,4 @@
-// vxc_q.cu - mixed (TF32x3) form of the V_xc contraction as a packed tensor-core GEMM.
+// vxc_q.cu - mixed form of the V_xc contraction as a packed tensor-core GEMM.
 //
 //   V_sigma[a][b] = sum_r sum_t P_t[r][a] Q_sigma,t[r][b]
 //   Q_sigma,0 = c_rho phi + c_gx d_x phi + c_gy d_y phi + c_gz d_z phi + c_lap lap phi
@@ -6,12 +6,14 @@
 // with P_0 = phi, P_j = d_j phi and c the per-point adjoint coefficients (the
 // transposed density contraction of jax.grad at train.py:86; the same sum as
 // vxc_f64.cu).  A memory-bound pre-pass forms Q for both spins once per call,
-// directly as TF32 hi/lo blocks in the AO-major layout of the AO tables; the
-// contraction is then tcg_kernel with A = the AO-major phi planes (K = 4
-// planes x grid points) in three TF32 slices, B = Q of both spins (N = 2 x
-// n_ao) in two, split-K over the grid, FP64 partials, and a reduction that
-// also splits the spins.  Five products per term (hi*hi, hi*lo, lo*hi, lo*lo,
-// lo2*hi): the phi planes' representation, not Q's, limits the 3-product form.
+// directly as block-scaled three-slice sets (umma::split3) in the AO-major
+// layout of the AO tables; the contraction is then tcg3_kernel with A = the
+// AO-major phi planes (K = 4 planes x grid points), B = Q of both spins
+// (N = 2 x n_ao), split-K over the grid, FP64 partials, and a reduction that
+// also splits the spins.  Both operands' hi slices are quantised per row and
+// 32-point chunk, so each chunk's hi*hi sum is exact in the tensor core's FP32
+// accumulator and only the corrections (below 2^-10 of the terms) meet its
+// truncation.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "tc_gemm.cuh"
@@ -25,8 +27,10 @@ constexpr int kBlkF = umma::kBlockBytes / 4;  // floats in one 128 x 32 block
 
 // One CTA per (b tile, 32-point chunk): reads the five AO-major FP32 planes of
 // that block and the chunk's coefficients, writes Q for 2 spins x 4 planes as
-// hi/lo blocks.  Threads walk the blocks in memory order (16-byte chunks), so
-// loads and stores are coalesced.
+// hi|lo|lo2 sets.  Item u of the block (1024 16-byte items) is AO row u / 8 and
+// points 4 (u % 8) .. 4 (u % 8) + 3, so the eight items of a row sit in eight
+// adjacent lanes (the row maximum is three shuffles) and a warp's accesses
+// cover 64-byte runs.
 __global__ void __launch_bounds__(256) build_q_kernel(const float *__restrict__ af, const double *__restrict__ coef,
                                                       int64_t np, int nbt, float *__restrict__ q) {
   __shared__ float sc[32][2][kFeat];
@@ -41,11 +45,11 @@ __global__ void __launch_bounds__(256) build_q_kernel(const float *__restrict__ 
   const float *src[kPlanes];
 #pragma unroll
   for (int p = 0; p < kPlanes; ++p) src[p] = af + ((size_t)(bt * kPlanes + p) * npc + pc) * kBlkF;
-#pragma unroll
+#pragma unroll 1
   for (int i = 0; i < 4; ++i) {
-    const int chunk = threadIdx.x + i * 256;  // 16-byte chunk in memory order
-    const int k4 = (chunk >> 3) & 7;          // 4-point group: points 4 k4 .. 4 k4 + 3
-    const uint32_t off = (uint32_t)chunk * 4;
+    const int u = threadIdx.x + i * 256;
+    const int k4 = u & 7, row = u >> 3;
+    const uint32_t off = umma::kblock_off(row, 4 * k4) / 4;
     float4 v[kPlanes];
 #pragma unroll
     for (int p = 0; p < kPlanes; ++p) v[p] = __ldg((const float4 *)(src[p] + off));
@@ -64,14 +68,20 @@ __global__ void __launch_bounds__(256) build_q_kernel(const float *__restrict__ 
       }
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
-        float4 h, l;
-        umma::split_tf32f(qv[t][0], h.x, l.x);
-        umma::split_tf32f(qv[t][1], h.y, l.y);
-        umma::split_tf32f(qv[t][2], h.z, l.z);
-        umma::split_tf32f(qv[t][3], h.w, l.w);
-        float *blk = q + ((((size_t)s * nbt + bt) * 4 + t) * npc + pc) * 2 * kBlkF;
-        *(float4 *)(blk + off) = h;
-        *(float4 *)(blk + kBlkF + off) = l;
+        float m = fmaxf(fmaxf(fabsf(qv[t][0]), fabsf(qv[t][1])), fmaxf(fabsf(qv[t][2]), fabsf(qv[t][3])));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 4));
+        const umma::Quant uq = umma::quant(m);
+        float4 h, l, l2;
+        umma::split3(qv[t][0], uq, h.x, l.x, l2.x);
+        umma::split3(qv[t][1], uq, h.y, l.y, l2.y);
+        umma::split3(qv[t][2], uq, h.z, l.z, l2.z);
+        umma::split3(qv[t][3], uq, h.w, l.w, l2.w);
+        float *set = q + ((((size_t)s * nbt + bt) * 4 + t) * npc + pc) * 3 * kBlkF;
+        *(float4 *)(set + off) = h;
+        *(float4 *)(set + kBlkF + off) = l;
+        *(float4 *)(set + 2 * kBlkF + off) = l2;
       }
     }
   }
@@ -104,10 +114,10 @@ int vxc_q_splits(int64_t np, int n_ao) {
 
 size_t vxc_q_bytes(int64_t np, int n_ao) {
   const int ldk = (int)round_up(n_ao, 128);
-  return (size_t)2 * 4 * np * ldk * 2 * sizeof(float);
+  return (size_t)2 * 4 * np * ldk * 3 * sizeof(float);
 }
 
-cudaError_t launch_vxc_q_tc(const float *am, const float *am3, const float *af, const double *coef, int64_t np,
+cudaError_t launch_vxc_q_tc(const float *av, const float *af, const double *coef, int64_t np,
                             int ldk, int n_ao, float *q, int nsplit, double *vpart, double *vxc, int *err,
                             cudaStream_t st) {
   const int nbt = ldk / 128;
@@ -116,8 +126,7 @@ cudaError_t launch_vxc_q_tc(const float *am, const float *am3, const float *af, 
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   TcgArgs a{};
-  a.a = am;
-  a.a3 = am3;  // third slice of phi: (1,1) and (2,0) products as well
+  a.a = av;
   a.b = q;
   a.m_tiles = nbt;
   a.n_tiles = 2 * nbt;
@@ -127,7 +136,7 @@ cudaError_t launch_vxc_q_tc(const float *am, const float *am3, const float *af, 
   a.m_valid = n_ao;
   a.n_valid = 2 * ldk;
   a.err = err;
-  if ((e = launch_tcg(a, nsplit, st)) != cudaSuccess) return e;
+  if ((e = launch_tcg3(a, nsplit, st)) != cudaSuccess) return e;
   const size_t total = (size_t)2 * n_ao * n_ao;
   vxc_q_reduce_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(vpart, nsplit, n_ao, ldk, vxc);
   return cudaGetLastError();

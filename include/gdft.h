@@ -305,6 +305,14 @@ int gdft_umma_probe(const float *h_a, const float *h_b, float *h_d);
 int gdft_tc_gemm_probe(int32_t M, int32_t N, int32_t K, int32_t nsplit, const double *h_a, const double *h_b,
                        double *h_d);
 
+/* The same product through the block-scaled three-slice GEMM of the mixed
+ * V_xc contraction (hi slices quantised per row and 32-wide K chunk so that
+ * each chunk's hi*hi sum is exact in the FP32 accumulator; six products per
+ * term; FP64 split-K partials summed on the host).  Synchronous, allocates its
+ * own buffers.  No counterpart in the reference. */
+int gdft_tc_gemm3_probe(int32_t M, int32_t N, int32_t K, int32_t nsplit, const double *h_a, const double *h_b,
+                        double *h_d);
+
 /* Stage timing (observability; no counterpart in the reference, whose only
  * tracing is jax.profiler.annotate_function at train.py:123).  When enabled,
  * the library records a CUDA event pair on the launching stream around every
