@@ -24,10 +24,11 @@
 // products (hi*lo, lo*hi, lo*lo, hi*lo2, lo2*hi, all below 2^-10 of the terms)
 // to a second accumulator X.  Two TMEM buffers of (Y, X) take all 512 columns.
 // The drains fold Y and X into a running FP32 sum S held in registers (TwoSum
-// for Y, Fast2Sum for the small X) and store the rounding errors back into the
-// X they just read: the MMA accumulates that buffer's next corrections on top
-// of them (X is never reset), so the compensation travels in TMEM and the two
-// pending ones are added at the end.
+// for Y, Fast2Sum for the small X; packed f32x2 arithmetic, two columns per
+// instruction) and store the rounding errors back into the X they just read:
+// the MMA accumulates that buffer's next corrections on top of them (X is never
+// reset), so the compensation travels in TMEM and the two pending ones are
+// added at the end.
 //
 // Warp roles (320 threads): warp 0 = TMA producer, warp 1 = TMEM owner and
 // MMA issuer, warps 2-9 = drains (TMEM lane quadrant warp % 4, column half
@@ -330,9 +331,9 @@ __global__ void __launch_bounds__(kThreads, 1) tcg3_kernel(const TcgArgs A) {
     // -------------------------------------------------------------- drains
     const int q = warp & 3, half = (warp - 2) >> 2;
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16) + half * 64;
-    float S[64];
+    uint64_t S[32];  // column pairs (2i, 2i + 1), packed FP32
 #pragma unroll
-    for (int i = 0; i < 64; ++i) S[i] = 0.0f;
+    for (int i = 0; i < 32; ++i) S[i] = 0ull;
     int64_t it = 0;
     for (; it < nst; ++it) {
       const int buf = (int)(it & 1);
@@ -348,17 +349,20 @@ __global__ void __launch_bounds__(kThreads, 1) tcg3_kernel(const TcgArgs A) {
         umma::tmem_ld16_nowait(tl + buf * 256 + 128 + c, xr);
         umma::tmem_ld_wait(yr, xr);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
+        for (int i = 0; i < 8; ++i) {
           // S + Y = t + e1 exactly (TwoSum); t + X = u + e2 (Fast2Sum: X is
-          // below 2^-10 of the chunk's terms, t holds the sum so far).
-          const float yv = __uint_as_float(yr[i]), xv = __uint_as_float(xr[i]);
-          const float t = S[c + i] + yv;
-          const float bp = t - S[c + i];
-          const float e1 = (S[c + i] - (t - bp)) + (yv - bp);
-          const float u = t + xv;
-          const float e2 = xv - (u - t);
-          S[c + i] = u;
-          xr[i] = __float_as_uint(e1 + e2);
+          // below 2^-10 of the chunk's terms, t holds the sum so far).  Two
+          // columns per instruction.
+          using namespace umma;
+          const uint64_t yv = pk2(yr[2 * i], yr[2 * i + 1]), xv = pk2(xr[2 * i], xr[2 * i + 1]);
+          const uint64_t sv = S[c / 2 + i];
+          const uint64_t t = add2(sv, yv);
+          const uint64_t bp = sub2(t, sv);
+          const uint64_t e1 = add2(sub2(sv, sub2(t, bp)), sub2(yv, bp));
+          const uint64_t u = add2(t, xv);
+          const uint64_t e2 = sub2(xv, sub2(u, t));
+          S[c / 2 + i] = u;
+          unpk2(add2(e1, e2), xr[2 * i], xr[2 * i + 1]);
         }
         umma::tmem_st16(tl + buf * 256 + 128 + c, xr);
       }
@@ -378,10 +382,14 @@ __global__ void __launch_bounds__(kThreads, 1) tcg3_kernel(const TcgArgs A) {
       umma::tmem_ld_wait(e0, e1);
       if (m < A.m_valid) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i)
+        for (int i = 0; i < 16; ++i) {
+          uint32_t sp[2];
+          umma::unpk2(S[(c + i) / 2], sp[0], sp[1]);
           if (n0 + c + i < A.n_valid)
-            row[c + i] = have ? ((double)S[c + i] + (double)__uint_as_float(e0[i])) + (double)__uint_as_float(e1[i])
+            row[c + i] = have ? ((double)__uint_as_float(sp[i & 1]) + (double)__uint_as_float(e0[i])) +
+                                    (double)__uint_as_float(e1[i])
                               : 0.0;
+        }
       }
     }
   }

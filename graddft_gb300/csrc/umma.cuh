@@ -254,6 +254,28 @@ __device__ __forceinline__ void split_tf32f(float x, float &hi, float &lo) {
   lo = tf32_rn(x - hi);
 }
 
+// ------------------------------------------------------ packed FP32 pairs
+// Two FP32 values in one 64-bit register, added or subtracted by one
+// instruction (add/sub.rn.f32x2), each lane rounded to nearest like the scalar op.
+__device__ __forceinline__ uint64_t pk2(uint32_t lo, uint32_t hi) {
+  uint64_t d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "r"(lo), "r"(hi));
+  return d;
+}
+__device__ __forceinline__ void unpk2(uint64_t v, uint32_t &lo, uint32_t &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
 // ------------------------------------------- block-scaled three-slice split
 // x = hi + lo + lo2 (+ about 2^-33 of the block row's largest magnitude m),
 // where hi is x rounded to the row's quantum q = 2^(E - 9), 2^(E-1) <= m < 2^E
@@ -272,6 +294,18 @@ __device__ __forceinline__ Quant quant(float m) {
   if (eb >= 9u && eb < 255u) {
     u.q = __uint_as_float((eb - 8u) << 23);     // 2^(eb - 135)
     u.inv = __uint_as_float((262u - eb) << 23);  // 2^(135 - eb)
+  } else {
+    u.q = 0.0f;
+    u.inv = 0.0f;
+  }
+  return u;
+}
+// The same from the biased FP32 exponent field of the row maximum alone.
+__device__ __forceinline__ Quant quant_eb(uint32_t eb) {
+  Quant u;
+  if (eb >= 9u && eb < 255u) {
+    u.q = __uint_as_float((eb - 8u) << 23);
+    u.inv = __uint_as_float((262u - eb) << 23);
   } else {
     u.q = 0.0f;
     u.inv = 0.0f;

@@ -27,61 +27,84 @@ constexpr int kBlkF = umma::kBlockBytes / 4;  // floats in one 128 x 32 block
 
 // One CTA per (b tile, 32-point chunk): reads the five AO-major FP32 planes of
 // that block and the chunk's coefficients, writes Q for 2 spins x 4 planes as
-// hi|lo|lo2 sets.  Item u of the block (1024 16-byte items) is AO row u / 8 and
-// points 4 (u % 8) .. 4 (u % 8) + 3, so the eight items of a row sit in eight
-// adjacent lanes (the row maximum is three shuffles) and a warp's accesses
-// cover 64-byte runs.
+// hi|lo|lo2 sets.  A block is 1024 16-byte items in memory order c = 64 g +
+// 8 k4 + r (AO row 8 g + r, points 4 k4 .. 4 k4 + 3); warp w takes row groups
+// 2w and 2w + 1, lane l the items c = 64 g + l and 64 g + 32 + l of each, so
+// every warp access is 512 contiguous bytes and a thread holds half of its
+// row's points.  A row's quantum needs only the exponent of its largest value:
+// a spin's four plane exponents travel as the bytes of one word (byte max over
+// the thread's two items, then over the four lanes l ^ 8, l ^ 16 that share
+// the row).
 __global__ void __launch_bounds__(256) build_q_kernel(const float *__restrict__ af, const double *__restrict__ coef,
                                                       int64_t np, int nbt, float *__restrict__ q) {
-  __shared__ float sc[32][2][kFeat];
+  __shared__ __align__(16) float sc[2][kFeat][32];  // [spin][coefficient][point]
   const int64_t npc = np / 32;
   const int bt = (int)(blockIdx.x / npc);
   const int64_t pc = blockIdx.x % npc;
-  for (int i = threadIdx.x; i < 32 * 2 * kFeat; i += blockDim.x) {
-    const int pt = i / (2 * kFeat), s = (i / kFeat) % 2, c = i % kFeat;
-    sc[pt][s][c] = (float)coef[((size_t)s * kFeat + c) * np + pc * 32 + pt];
-  }
+  for (int i = threadIdx.x; i < 2 * kFeat * 32; i += blockDim.x)
+    (&sc[0][0][0])[i] = (float)coef[(size_t)(i / 32) * np + pc * 32 + i % 32];
   __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float *src[kPlanes];
 #pragma unroll
   for (int p = 0; p < kPlanes; ++p) src[p] = af + ((size_t)(bt * kPlanes + p) * npc + pc) * kBlkF;
 #pragma unroll 1
-  for (int i = 0; i < 4; ++i) {
-    const int u = threadIdx.x + i * 256;
-    const int k4 = u & 7, row = u >> 3;
-    const uint32_t off = umma::kblock_off(row, 4 * k4) / 4;
-    float4 v[kPlanes];
+  for (int gi = 0; gi < 2; ++gi) {
+    const int g = 2 * warp + gi;
+    uint32_t off[2];
+    float4 v[2][kPlanes];
 #pragma unroll
-    for (int p = 0; p < kPlanes; ++p) v[p] = __ldg((const float4 *)(src[p] + off));
+    for (int h = 0; h < 2; ++h) {
+      off[h] = (uint32_t)(64 * g + 32 * h + lane) * 4;  // floats
+#pragma unroll
+      for (int p = 0; p < kPlanes; ++p) v[h][p] = __ldg((const float4 *)(src[p] + off[h]));
+    }
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      float qv[4][4];  // [plane t][point j]
+      float qv[2][4][4];  // [item][plane t][point j]
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float *c = sc[4 * k4 + j][s];
-        const float ph = (&v[T_PHI].x)[j], dx = (&v[T_DX].x)[j], dy = (&v[T_DY].x)[j], dz = (&v[T_DZ].x)[j],
-                    lp = (&v[T_LAP].x)[j];
-        qv[0][j] = c[C_RHO] * ph + c[C_GX] * dx + c[C_GY] * dy + c[C_GZ] * dz + c[C_LAP] * lp;
-        qv[1][j] = c[C_KIN] * dx;
-        qv[2][j] = c[C_KIN] * dy;
-        qv[3][j] = c[C_KIN] * dz;
+      for (int h = 0; h < 2; ++h) {
+        const int p0 = 4 * (4 * h + (lane >> 3));  // first point of the item
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float ph = (&v[h][T_PHI].x)[j], dx = (&v[h][T_DX].x)[j], dy = (&v[h][T_DY].x)[j],
+                      dz = (&v[h][T_DZ].x)[j], lp = (&v[h][T_LAP].x)[j];
+          const float *c = &sc[s][0][p0 + j];
+          const float ck = c[32 * C_KIN];
+          qv[h][0][j] = c[32 * C_RHO] * ph + c[32 * C_GX] * dx + c[32 * C_GY] * dy + c[32 * C_GZ] * dz +
+                        c[32 * C_LAP] * lp;
+          qv[h][1][j] = ck * dx;
+          qv[h][2][j] = ck * dy;
+          qv[h][3][j] = ck * dz;
+        }
       }
+      uint32_t ebw = 0u;  // byte t: exponent field of the largest |Q_t| of the row
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
-        float m = fmaxf(fmaxf(fabsf(qv[t][0]), fabsf(qv[t][1])), fmaxf(fabsf(qv[t][2]), fabsf(qv[t][3])));
-        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
-        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
-        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 4));
-        const umma::Quant uq = umma::quant(m);
-        float4 h, l, l2;
-        umma::split3(qv[t][0], uq, h.x, l.x, l2.x);
-        umma::split3(qv[t][1], uq, h.y, l.y, l2.y);
-        umma::split3(qv[t][2], uq, h.z, l.z, l2.z);
-        umma::split3(qv[t][3], uq, h.w, l.w, l2.w);
+        float m = 0.0f;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) m = fmaxf(m, fabsf(qv[h][t][j]));
+        ebw |= ((__float_as_uint(m) >> 23) & 0xFFu) << (8 * t);
+      }
+      ebw = __vmaxu4(ebw, __shfl_xor_sync(0xffffffffu, ebw, 8));
+      ebw = __vmaxu4(ebw, __shfl_xor_sync(0xffffffffu, ebw, 16));
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const umma::Quant uq = umma::quant_eb((ebw >> (8 * t)) & 0xFFu);
         float *set = q + ((((size_t)s * nbt + bt) * 4 + t) * npc + pc) * 3 * kBlkF;
-        *(float4 *)(set + off) = h;
-        *(float4 *)(set + kBlkF + off) = l;
-        *(float4 *)(set + 2 * kBlkF + off) = l2;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          float4 hi, lo, lo2;
+          umma::split3(qv[h][t][0], uq, hi.x, lo.x, lo2.x);
+          umma::split3(qv[h][t][1], uq, hi.y, lo.y, lo2.y);
+          umma::split3(qv[h][t][2], uq, hi.z, lo.z, lo2.z);
+          umma::split3(qv[h][t][3], uq, hi.w, lo.w, lo2.w);
+          *(float4 *)(set + off[h]) = hi;
+          *(float4 *)(set + kBlkF + off[h]) = lo;
+          *(float4 *)(set + 2 * kBlkF + off[h]) = lo2;
+        }
       }
     }
   }
