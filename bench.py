@@ -695,7 +695,8 @@ def main():
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 65,536-point capture "
                               "(profiles/), scaled by grid points" if traffic else None,
             "flops_per_launch": flops_launch,
-            "executed_flops_per_launch": flops_launch * (3 if form == "tf32x3" else 1),
+            # TF32 products per term: three in the density, six in the V_xc GEMM.
+            "executed_flops_per_launch": flops_launch * ((3 if dom == "density" else 6) if form == "tf32x3" else 1),
             "stage_ms_per_step": {k: v[0] / args.steps for k, v in stage.items()}}
 
     line = {
