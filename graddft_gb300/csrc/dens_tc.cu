@@ -4,7 +4,9 @@
 // and every 64-column block cb of the output it forms, for both spins,
 //   X_t,sigma[:, cb] = T_t D_sigma[:, cb]          (M = 128, N = 64, K = n_ao)
 // in TMEM with three TF32 products per term (hi*hi + hi*lo + lo*hi of the
-// split operands, FP32 accumulation), then the epilogue warps reduce each row
+// split operands, FP32 accumulation; both spins' 64 columns form one N = 128
+// operand, so each MMA reads the A tile once for both), then the epilogue
+// warps reduce each row
 // against the AO planes exactly as the FP64 form (dens_f64.cu) does:
 //   t = phi : rho, grad rho (x2), and the phi*lap part of the Laplacian
 //   t = d_j : the d_j phi . d_j phi part of the Laplacian and tau.
@@ -14,14 +16,15 @@
 // accumulator's ulp grid, so long FP32 accumulation chains drift towards
 // zero, by an amount proportional to the accumulator's size at each
 // instruction.  Each job's K range is therefore split into sub-jobs of one
-// 32-wide stage (12 MMAs per accumulator: the small hi*lo and lo*hi
-// corrections first, the hi*hi products last) that accumulate in a TMEM buffer W
-// (double-buffered); the epilogue folds W into a running sum S, also in
-// TMEM, with round-to-nearest FP32 adds on the CUDA cores, then reduces S
-// against the AO planes at the end of the job.
+// 32-wide stage (12 MMAs: the small hi*lo and lo*hi corrections first, the
+// hi*hi products last) that accumulate in a TMEM buffer W (double-buffered);
+// the epilogue folds W into a running sum S, also in TMEM, with
+// round-to-nearest FP32 adds on the CUDA cores.  S is double-buffered too: a
+// job's row reductions against the AO planes run, unit by unit, between the
+// folds of the next job's stages, so they never hold up the MMA pipeline.
 //
 // Warp roles (320 threads): warp 0 = TMA producer (one thread issues bulk
-// copies of pre-tiled operand images: A 32 KB, the two D halves 4 x 8 KB),
+// copies of pre-tiled operand images: A 32 KB, the two spins' D halves 4 x 8 KB),
 // warp 1 = TMEM owner and MMA issuer (one thread), warps 2-9 = epilogue, one
 // per (TMEM lane quadrant = warp % 4, spin).  Three 64 KB smem stages.  Every wait is
 // bounded (umma::mbar_wait); on expiry the CTA records an error word, waits
@@ -36,9 +39,10 @@ namespace {
 
 constexpr int kStages = 3;
 constexpr uint32_t kHalf = umma::kBlockBytes / 2;                     // 64 rows x 32 fp32
-constexpr uint32_t kStageBytes = 2 * umma::kBlockBytes + 4 * kHalf;  // A hi|lo, B_a hi|lo, B_b hi|lo
+constexpr uint32_t kStageBytes = 2 * umma::kBlockBytes + 4 * kHalf;  // A hi|lo, B hi (both spins), B lo
 constexpr int kThreads = 320;
-constexpr uint32_t kTmemCols = 512;  // W0 [0,128), W1 [128,256), S [256,384) (2 spins x 64 columns each)
+constexpr uint32_t kTmemCols = 512;  // W0 [0,128), W1 [128,256), S0 [256,384), S1 [384,512) (2 spins x 64 columns)
+constexpr uint32_t kScol = 256;
 constexpr int kSubK = 32;             // K extent of one accumulation chain (one stage)
 constexpr int kBN = 64;               // output columns per job
 constexpr int kSmemBytes = kStages * kStageBytes + 1024;
@@ -58,21 +62,6 @@ __device__ __forceinline__ const float *pm_blk(const DensArgs &A, int64_t tile, 
 }
 
 __device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, code); }
-
-// The row's 32 values (hi + lo) of a point-major block.
-__device__ __forceinline__ void load_row32(const float *blk, int row, float (&v)[32]) {
-  const float4 *hi = (const float4 *)blk;
-  const float4 *lo = (const float4 *)(blk + umma::kBlockBytes / 4);
-#pragma unroll
-  for (int g = 0; g < 8; ++g) {
-    const int o = (((row >> 3) * 8 + g) * 128 + (row & 7) * 16) / 16;
-    const float4 h = __ldg(hi + o), l = __ldg(lo + o);
-    v[4 * g + 0] = h.x + l.x;
-    v[4 * g + 1] = h.y + l.y;
-    v[4 * g + 2] = h.z + l.z;
-    v[4 * g + 3] = h.w + l.w;
-  }
-}
 
 __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) {
   extern __shared__ unsigned char smem_raw[];
@@ -127,9 +116,10 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
           for (int sp = 0; sp < 2; ++sp) {
             const float *b = A.dpk + (((size_t)sp * ncb128 + cb / 2) * nkc + kc) * 2 * (umma::kBlockBytes / 4) +
                              (cb & 1) * (kHalf / 4);
-            unsigned char *dst = st + 2 * umma::kBlockBytes + sp * 2 * kHalf;
+            // B rows 0-63 = spin 0's columns, 64-127 = spin 1's: one N = 128 operand.
+            unsigned char *dst = st + 2 * umma::kBlockBytes + sp * kHalf;
             umma::bulk_g2s(dst, b, kHalf, &full[s]);
-            umma::bulk_g2s(dst + kHalf, b + umma::kBlockBytes / 4, kHalf, &full[s]);
+            umma::bulk_g2s(dst + 2 * kHalf, b + umma::kBlockBytes / 4, kHalf, &full[s]);
           }
           ++it;
         }
@@ -145,17 +135,12 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
     // slot 0; a slot adds kStageBytes >> 4 and a K step of 8 (256 bytes) adds
     // 16 to the start-address field (address >> 4, bits 0-13).
     if (lane == 0) {
-      const uint32_t idesc = umma::idesc_tf32(128, kBN);
+      const uint32_t idesc = umma::idesc_tf32(128, 2 * kBN);  // both spins in one MMA
       const uint32_t s0 = umma::smem_u32(smem);
       const uint64_t dahi0 = umma::sdesc(s0, umma::kBlockLBO, umma::kBlockSBO);
       const uint64_t dalo0 = umma::sdesc(s0 + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
-      uint64_t dbhi0[2], dblo0[2];
-#pragma unroll
-      for (int sp = 0; sp < 2; ++sp) {
-        const uint32_t bb = s0 + 2 * umma::kBlockBytes + sp * 2 * kHalf;
-        dbhi0[sp] = umma::sdesc(bb, umma::kBlockLBO, umma::kBlockSBO);
-        dblo0[sp] = umma::sdesc(bb + kHalf, umma::kBlockLBO, umma::kBlockSBO);
-      }
+      const uint64_t dbhi0 = umma::sdesc(s0 + 2 * umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
+      const uint64_t dblo0 = umma::sdesc(s0 + 2 * umma::kBlockBytes + 2 * kHalf, umma::kBlockLBO, umma::kBlockSBO);
       uint32_t it = 0, sub = 0;
       bool ok = true;
       for (int j = 0; j < njobs && ok; ++j) {
@@ -177,19 +162,16 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
             umma::tc_fence_after();
             const uint64_t so = (uint64_t)s * (kStageBytes >> 4);
             const bool first = kc == kq * kc_per_sub;
+            const uint32_t d = tbase + buf * 128;
+            const uint64_t ahi = dahi0 + so, alo = dalo0 + so, bhi = dbhi0 + so, blo = dblo0 + so;
+            // Corrections first (hi*lo, lo*hi, small), then the hi*hi products.
 #pragma unroll
-            for (int sp = 0; sp < 2; ++sp) {
-              const uint32_t d = tbase + buf * 128 + sp * kBN;
-              const uint64_t ahi = dahi0 + so, alo = dalo0 + so, bhi = dbhi0[sp] + so, blo = dblo0[sp] + so;
-              // Corrections first (hi*lo, lo*hi, small), then the hi*hi products.
-#pragma unroll
-              for (int kk = 0; kk < 4; ++kk) {
-                umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, (first && kk == 0) ? 0u : 1u);
-                umma::mma_tf32(d, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
-              }
-#pragma unroll
-              for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(d, ahi + 16 * kk, bhi + 16 * kk, idesc, 1u);
+            for (int kk = 0; kk < 4; ++kk) {
+              umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, (first && kk == 0) ? 0u : 1u);
+              umma::mma_tf32(d, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
             }
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(d, ahi + 16 * kk, bhi + 16 * kk, idesc, 1u);
             umma::mma_commit(&empty[s]);
             ++it;
           }
@@ -204,6 +186,11 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
     __syncwarp();
   } else {
     // ------------------------------------------------------------ epilogue
+    // Job j's stages fold into S[j & 1]; job j - 1's row reductions, split
+    // into (plane, 32-column) units, run between those folds and are
+    // software-pipelined: a unit's row values are loaded during one stage and
+    // consumed in the next, so neither the loads' latency nor the reductions
+    // hold up the MMA pipeline.
     const int q = warp & 3;
     const int sp = (warp - 2) >> 2;  // spin handled by this warp
     const int row = q * 32 + lane;
@@ -211,10 +198,51 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
     double F[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) F[k] = 0.0;
+    // Row-reduction unit u of job jr: plane k, columns 32 (u % 2) .. + 31 of the job's block.
+    auto unit_plane = [&](int jr, int u) { return (jr / ncb == 0 ? 0 : jr / ncb) + (u >> 1); };
+    auto unit_blk = [&](int jr, int u) {
+      return pm_blk(A, tile, unit_plane(jr, u), ((jr % ncb) * kBN + (u & 1) * 32) / 32);
+    };
+    auto n_units = [&](int jr) { return jr / ncb == 0 ? 2 * kPlanes : 2; };
+    float4 ph[8], pl[8];  // row values of the pending unit (hi, lo), in flight
+    auto issue = [&](int jr, int u) {
+      const float4 *hi = (const float4 *)unit_blk(jr, u);
+      const float4 *lo = hi + umma::kBlockBytes / 16;
+#pragma unroll
+      for (int g = 0; g < 8; ++g) {
+        const int o = (((row >> 3) * 8 + g) * 128 + (row & 7) * 16) / 16;
+        ph[g] = __ldg(hi + o);
+        pl[g] = __ldg(lo + o);
+      }
+    };
+    auto consume = [&](int jr, int u) {
+      float x[32];
+      umma::tmem_ld32(tl + kScol + (jr & 1) * 128 + (u & 1) * 32, x);
+      float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int g = 0; g < 8; ++g) {
+        a[0] = fmaf(x[4 * g + 0], ph[g].x + pl[g].x, a[0]);
+        a[1] = fmaf(x[4 * g + 1], ph[g].y + pl[g].y, a[1]);
+        a[2] = fmaf(x[4 * g + 2], ph[g].z + pl[g].z, a[2]);
+        a[3] = fmaf(x[4 * g + 3], ph[g].w + pl[g].w, a[3]);
+      }
+      const double d = ((double)a[0] + (double)a[1]) + ((double)a[2] + (double)a[3]);
+      const int k = unit_plane(jr, u);
+      switch (jr / ncb == 0 ? k : 5) {
+        case 0: F[0] += d; break;
+        case 1: F[1] += d; break;
+        case 2: F[2] += d; break;
+        case 3: F[3] += d; break;
+        case 4: F[4] += d; break;
+        default: F[5] += d; break;
+      }
+    };
+    int pj = -1, pu = 0;  // pending unit (job, index), issued but not consumed
     uint32_t sub = 0;
     bool ok = true;
     for (int j = 0; j < njobs && ok; ++j) {
-      const int t = j / ncb, cb = j % ncb;
+      const uint32_t sdst = tl + kScol + (j & 1) * 128;
+      const int up = j > 0 ? n_units(j - 1) : 0;
       for (int kq = 0; kq < nkq; ++kq, ++sub) {
         const int buf = sub & 1;
         if (!umma::warp_wait(&wfull[buf], (sub >> 1) & 1)) {
@@ -223,46 +251,48 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
           break;
         }
         umma::tc_fence_after();
-        // S (+)= W for this spin's 64 columns (round-to-nearest FP32 adds).
+        // The unit loaded during the previous stage (its S buffer is about to
+        // be reused when it belongs to job j - 2).
+        if (pj >= 0) {
+          consume(pj, pu);
+          pj = -1;
+        }
+        // S[j & 1] (+)= W for this spin's 64 columns (round-to-nearest FP32 adds).
 #pragma unroll
-        for (int c = 0; c < kBN; c += 32) {
-          uint32_t w[32], sv[32];
-          umma::tmem_ld32_nowait(tl + buf * 128 + c, w);
-          if (kq > 0) umma::tmem_ld32_nowait(tl + 256 + c, sv);
+        for (int c = 0; c < kBN; c += 16) {
+          uint32_t w[16], sv[16];
+          umma::tmem_ld16_nowait(tl + buf * 128 + c, w);
+          if (kq > 0) umma::tmem_ld16_nowait(sdst + c, sv);
           umma::tmem_ld_wait(w, sv);
-          float o[32];
 #pragma unroll
-          for (int i = 0; i < 32; ++i)
-            o[i] = kq > 0 ? __uint_as_float(w[i]) + __uint_as_float(sv[i]) : __uint_as_float(w[i]);
-          umma::tmem_st32(tl + 256 + c, o);
+          for (int i = 0; i < 16; ++i)
+            if (kq > 0) w[i] = __float_as_uint(__uint_as_float(w[i]) + __uint_as_float(sv[i]));
+          umma::tmem_st16(sdst + c, w);
         }
         umma::tmem_st_wait();
         umma::tc_fence_before();
         umma::mbar_arrive(&wempty[buf]);
-      }
-      if (!ok) break;
-      // Row reductions of S: FP32 FMA chains of 8 products, summed in FP64.
-      for (int c0 = 0; c0 < kBN; c0 += 32) {
-        float x[32], pv[32];
-        umma::tmem_ld32(tl + 256 + c0, x);
-        const int kc = (cb * kBN + c0) / 32;
-        const int k_lo = t == 0 ? 0 : t, k_hi = t == 0 ? kPlanes : t + 1;
+        // This stage's share of job j - 1's units: the last one due is left
+        // in flight for the next stage, any earlier ones run now.
+        const int u0 = kq * up / nkq, u1 = (kq + 1) * up / nkq;
 #pragma unroll 1
-        for (int k = k_lo; k < k_hi; ++k) {
-          load_row32(pm_blk(A, tile, k, kc), row, pv);
-          float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-          for (int i = 0; i < 32; ++i) a[i & 3] = fmaf(x[i], pv[i], a[i & 3]);
-          const double d = ((double)a[0] + (double)a[1]) + ((double)a[2] + (double)a[3]);
-          switch (t == 0 ? k : 5) {
-            case 0: F[0] += d; break;
-            case 1: F[1] += d; break;
-            case 2: F[2] += d; break;
-            case 3: F[3] += d; break;
-            case 4: F[4] += d; break;
-            default: F[5] += d; break;
+        for (int u = u0; u < u1; ++u) {
+          issue(j - 1, u);
+          if (u + 1 < u1) {
+            consume(j - 1, u);
+          } else {
+            pj = j - 1;
+            pu = u;
           }
         }
+      }
+    }
+    if (ok) {
+      if (pj >= 0) consume(pj, pu);
+#pragma unroll 1
+      for (int u = 0; u < n_units(njobs - 1); ++u) {
+        issue(njobs - 1, u);
+        consume(njobs - 1, u);
       }
     }
     const int64_t p = tile * 128 + row;
