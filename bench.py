@@ -697,6 +697,12 @@ def main():
             "flops_per_launch": flops_launch,
             # TF32 products per term: three in the density, six in the V_xc GEMM.
             "executed_flops_per_launch": flops_launch * ((3 if dom == "density" else 6) if form == "tf32x3" else 1),
+            # The same stage measured as the tensor work it executes, against the
+            # TF32 rate (nominally half the dense BF16 one).
+            "executed_tflops": (flops_launch * ((3 if dom == "density" else 6) if form == "tf32x3" else 1)
+                                / (t_dom / n_dom * 1e-3) / 1e12),
+            "executed_frac_of_tf32": ((flops_launch * (3 if dom == "density" else 6) / (t_dom / n_dom * 1e-3) / 1e12)
+                                      / (peak / 2) if form == "tf32x3" else None),
             "stage_ms_per_step": {k: v[0] / args.steps for k, v in stage.items()}}
 
     line = {
