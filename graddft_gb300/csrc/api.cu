@@ -507,15 +507,19 @@ int gdft_density(const gdft_molecule *mol, const double *d_rdm1, double *d_rho, 
                     "feat_to_reference");
 }
 
-int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,
-                             const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc, void *d_ws,
-                             size_t ws_bytes, void *stream) {
+static int xc_energy_and_grads(const char *who, const gdft_molecule *mol, const double *d_rdm1,
+                               const gdft_functional *fn, const double *d_ehf, int32_t n_omega, double *d_exc,
+                               double *d_vxc, double *d_ghf, void *d_ws, size_t ws_bytes, void *stream) {
   int rc = check_mol(mol);
   if (rc) return rc;
   if ((rc = check_ws(mol, d_ws, ws_bytes))) return rc;
   if ((rc = check_functional(fn, d_ehf, n_omega))) return rc;
   if (d_rdm1 == nullptr || d_exc == nullptr) {
-    set_error("gdft_xc_energy_and_grads: rdm1 and exc are required");
+    set_error("%s: rdm1 and exc are required", who);
+    return GDFT_ERR_INVALID;
+  }
+  if (d_ghf != nullptr && ((uintptr_t)d_ghf & 7)) {
+    set_error("%s: ghf must be 8-byte aligned", who);
     return GDFT_ERR_INVALID;
   }
   cudaStream_t st = (cudaStream_t)stream;
@@ -528,7 +532,7 @@ int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, con
   {
     StageTimer tm(GDFT_STAGE_POINT, st);
     rc = check_cuda(launch_xc_point(feat, mol_w(mol), mol->n_grid, mol->n_grid_pad, *fn, d_ehf, n_omega, coef, epart,
-                                    nullptr, st),
+                                    nullptr, st, d_ghf),
                     "xc_point");
     if (rc) return rc;
   }
@@ -538,6 +542,20 @@ int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, con
   }
   if (d_vxc == nullptr) return GDFT_OK;
   return run_vxc(mol, coef, d_vxc, ws, st);
+}
+
+int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,
+                             const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc, void *d_ws,
+                             size_t ws_bytes, void *stream) {
+  return xc_energy_and_grads("gdft_xc_energy_and_grads", mol, d_rdm1, fn, d_ehf, n_omega, d_exc, d_vxc, nullptr,
+                             d_ws, ws_bytes, stream);
+}
+
+int gdft_xc_energy_grads_hf(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,
+                            const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc, double *d_ghf,
+                            void *d_ws, size_t ws_bytes, void *stream) {
+  return xc_energy_and_grads("gdft_xc_energy_grads_hf", mol, d_rdm1, fn, d_ehf, n_omega, d_exc, d_vxc, d_ghf, d_ws,
+                             ws_bytes, stream);
 }
 
 

@@ -40,7 +40,7 @@ cudaError_t launch_vxc_q_tc(const float *av, const float *af, const double *coef
 int xc_point_blocks(int64_t np);
 cudaError_t launch_xc_point(const double *feat, const double *w, int64_t n_grid, int64_t np,
                             const gdft_functional &fn, const double *ehf, int n_omega, double *coef,
-                            double *epart, double *dens, cudaStream_t st);
+                            double *epart, double *dens, cudaStream_t st, double *ghf = nullptr);
 
 // reduce.cu
 int integrate_blocks(int64_t n_grid);

@@ -11,7 +11,12 @@
 //       C_RHO = dE/drho, C_GJ = 2 dE/d(d_j rho), C_LAP = 2 dE/d(lap rho),
 //       C_KIN = 2 dE/d(lap rho) + 1/2 dE/dtau,
 //     so that V_ab = sum_r phi_a (C_RHO phi_b + sum_j C_GJ d_j phi_b + C_LAP lap phi_b)
-//                  + sum_r C_KIN sum_j d_j phi_a d_j phi_b.
+//                  + sum_r C_KIN sum_j d_j phi_a d_j phi_b;
+//   * optionally, g_r = dE/d ehf[w][s][r] for a functional whose HF column is
+//     the sum of ehf over omega and spin (b3lyp_combine): the gradient that
+//     HF_density_grad_2_Fock takes (molecule.py:598-603), i.e. with the
+//     other columns unclipped (energy_densities as predict passes them,
+//     train.py:167-178): abs_clip(w_r) * [|sum_f c_f e_f| > clip] * c_HF.
 #include "common.cuh"
 #include "xc_functionals.cuh"
 #include "kernels.cuh"
@@ -55,7 +60,7 @@ __global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restri
                                                           int64_t n_grid, int64_t np, gdft_functional fn,
                                                           const double *__restrict__ ehf, int n_omega,
                                                           double *__restrict__ coef, double *__restrict__ epart,
-                                                          double *__restrict__ dens) {
+                                                          double *__restrict__ dens, double *__restrict__ ghf) {
   const int64_t p = (int64_t)blockIdx.x * kBlock + threadIdx.x;
   double e_r = 0.0;
   if (p < np) {
@@ -93,18 +98,22 @@ __global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restri
       }
       // Energy density: sum_f c_f * abs_clip(e_f), then abs_clip; weight abs_clip(w).
       Dual<KV> exc = dconst<KV>(0.0);
+      double e_raw = 0.0, c_hf = 0.0;  // unclipped columns' sum; coefficient of the HF column
       unsigned poison = 0;  // spins whose rho gradient is NaN in the reference (see corr_pol)
       for (int i = 0; i < fn.n_cols; ++i) {
         Dual<KV> e = column<Dual<KV>>(fn.cols[i], rho, sg, lap, hf, hf0, hf1, clip, &poison);
         if (dens != nullptr) dens[(size_t)p * fn.n_cols + i] = e.v;
-        if (!(fabs(e.v) > clip)) e = dconst<KV>(0.0);  // abs_clip(densities), functional.py:184
         const double ci = fn.n_coeffs == 1 ? fn.coeffs[0] : fn.coeffs[i];
+        e_raw += ci * e.v;
+        if (fn.cols[i] == GDFT_COL_HF) c_hf += ci;
+        if (!(fabs(e.v) > clip)) e = dconst<KV>(0.0);  // abs_clip(densities), functional.py:184
         exc = i == 0 ? ci * e : exc + ci * e;
       }
       if (!(fabs(exc.v) > clip)) exc = dconst<KV>(0.0);  // functional.py:252 and :342
       const double wr = w[p];
       const double W = fabs(wr) > clip ? wr : 0.0;      // abs_clip(gridweights), functional.py:342
       e_r = W * exc.v;
+      if (ghf != nullptr) ghf[p] = fabs(e_raw) > clip ? W * c_hf : 0.0;
       // dE_r/dvar = W * d exc/dvar.
       double dv[KV];
 #pragma unroll
@@ -150,9 +159,9 @@ int xc_point_blocks(int64_t np) { return (int)((np + kBlock - 1) / kBlock); }
 
 cudaError_t launch_xc_point(const double *feat, const double *w, int64_t n_grid, int64_t np,
                             const gdft_functional &fn, const double *ehf, int n_omega, double *coef,
-                            double *epart, double *dens, cudaStream_t st) {
+                            double *epart, double *dens, cudaStream_t st, double *ghf) {
   const int blocks = xc_point_blocks(np);
-  xc_point_kernel<<<blocks, kBlock, 0, st>>>(feat, w, n_grid, np, fn, ehf, n_omega, coef, epart, dens);
+  xc_point_kernel<<<blocks, kBlock, 0, st>>>(feat, w, n_grid, np, fn, ehf, n_omega, coef, epart, dens, ghf);
   return cudaGetLastError();
 }
 

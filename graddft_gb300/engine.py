@@ -138,6 +138,20 @@ class Resident:
                                                    self.ws.numel(), _stream(self.device)))
         return exc, vxc
 
+    def xc_energy_grads_hf(self, rdm1, fn: GdftFunctional, ehf, want_vxc=True):
+        """(E_xc, V_xc, g): g (grid,) = dE_xc/d ehf[w][s][r] of the functional's HF column (the sum of ehf)."""
+        rdm1 = self._rdm1(rdm1)
+        ehf_t = as_device_f64(ehf, self.device)
+        if ehf_t is None or ehf_t.ndim != 3 or ehf_t.shape[1] != 2 or ehf_t.shape[2] != self.n_grid:
+            raise ValueError(f"ehf must be (omega, 2, {self.n_grid})")
+        exc = torch.empty((), dtype=F64, device=self.device)
+        vxc = torch.empty((2, self.n_ao, self.n_ao), dtype=F64, device=self.device) if want_vxc else None
+        ghf = torch.empty(self.n_grid, dtype=F64, device=self.device)
+        check(_lib.load().gdft_xc_energy_grads_hf(ctypes.byref(self.desc), _ptr(rdm1), ctypes.byref(fn), _ptr(ehf_t),
+                                                  ehf_t.shape[0], _ptr(exc), _ptr(vxc), _ptr(ghf), _ptr(self.ws),
+                                                  self.ws.numel(), _stream(self.device)))
+        return exc, vxc, ghf
+
     def vxc_from_potentials(self, pot, vxc_out=None):
         """V_s = sum_r [c0 phi phi + sum_j c_j phi d_j phi + c4 phi lap phi + c5 sum_j d_j phi d_j phi], pot (2, 6, grid)."""
         pot = as_device_f64(pot, self.device)
@@ -322,6 +336,61 @@ def fock(h1e, vj, vxc, clip=1e-30) -> torch.Tensor:
     out = torch.empty_like(vxc)
     check(_lib.load().gdft_fock(n, _ptr(h1e), _ptr(vj), _ptr(vxc.contiguous()), float(clip), _ptr(out),
                                 _stream(dev)))
+    return out
+
+
+def _hf_ws(n_grid: int, n_ao: int, n_omega: int, device) -> torch.Tensor:
+    nbytes = ctypes.c_size_t()
+    check(_lib.load().gdft_hf_workspace_bytes(n_grid, n_ao, n_omega, ctypes.byref(nbytes)))
+    return torch.empty(nbytes.value, dtype=torch.uint8, device=device)
+
+
+def _chi(chi, ao):
+    chi = as_device_f64(chi, ao.device)
+    if chi.ndim != 4 or chi.shape[0] != ao.shape[0] or chi.shape[2] != 2 or chi.shape[3] != ao.shape[1]:
+        raise ValueError(f"chi must be (grid, omega, 2, orbitals) = ({ao.shape[0]}, omega, 2, {ao.shape[1]}), "
+                         f"got {tuple(chi.shape)}")
+    return chi.contiguous()
+
+
+def hf_energy_density(ao, rdm1, chi) -> torch.Tensor:
+    """molecule.py:507-541: ehf (omega, 2, grid) = -1/2 einsum("rwsc,sac,ra->wsr", chi, rdm1, ao)."""
+    dev = require_cuda(ao.device if isinstance(ao, torch.Tensor) and ao.is_cuda else None)
+    ao = as_device_f64(ao, dev).contiguous()
+    rdm1 = as_device_f64(rdm1, dev).contiguous()
+    chi = _chi(chi, ao)
+    n_grid, n_ao = ao.shape
+    n_omega = chi.shape[1]
+    out = torch.empty((n_omega, 2, n_grid), dtype=F64, device=dev)
+    ws = _hf_ws(n_grid, n_ao, n_omega, dev)
+    check(_lib.load().gdft_hf_energy_density(_ptr(ao), _ptr(rdm1), _ptr(chi), n_grid, n_ao, n_omega, _ptr(out),
+                                             _ptr(ws), ws.numel(), _stream(dev)))
+    return out
+
+
+def hf_fock(ao, chi, g) -> torch.Tensor:
+    """sum over omega of molecule.py:545-685: F_s = -1/2 sum_w einsum("rw s b, w s r, r a -> s a b")."""
+    dev = require_cuda(ao.device if isinstance(ao, torch.Tensor) and ao.is_cuda else None)
+    ao = as_device_f64(ao, dev).contiguous()
+    chi = _chi(chi, ao)
+    n_grid, n_ao = ao.shape
+    n_omega = chi.shape[1]
+    g = as_device_f64(g, dev)
+    if tuple(g.shape) != (n_omega, 2, n_grid):
+        raise ValueError(f"g must be (omega, 2, grid) = ({n_omega}, 2, {n_grid}), got {tuple(g.shape)}")
+    g = g.contiguous()
+    out = torch.empty((2, n_ao, n_ao), dtype=F64, device=dev)
+    ws = _hf_ws(n_grid, n_ao, n_omega, dev)
+    check(_lib.load().gdft_hf_fock(_ptr(ao), _ptr(chi), _ptr(g), n_grid, n_ao, n_omega, _ptr(out), _ptr(ws),
+                                   ws.numel(), _stream(dev)))
+    return out
+
+
+def fock_add_hf(fock_, fock_hf, clip=1e-30) -> torch.Tensor:
+    """train.py:200-210: fock = abs_clip(fock + F + F^T) (in place on a copy)."""
+    out = fock_.contiguous().clone()
+    f = as_device_f64(fock_hf, out.device).contiguous()
+    check(_lib.load().gdft_fock_add_hf(_ptr(out), _ptr(f), out.shape[-1], float(clip), _stream(out.device)))
     return out
 
 

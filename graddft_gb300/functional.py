@@ -171,6 +171,22 @@ class Functional:
         fn, ehf = self.spec(params, atoms, clip_cte)
         return atoms.resident().xc_energy_and_grads(atoms._rdm1(), fn, ehf, want_vxc=True)
 
+    def hf_density_gradient(self, params, atoms, ehf, clip_cte: float = CLIP):
+        """dE_xc/d ehf[w][s][r] (grid,) through the densities, the gradient that
+        HF_density_grad_2_Fock takes (molecule.py:598-603): the same for every
+        (omega, spin) because the HF column is their sum (b3lyp_combine)."""
+        cols = energy_density_columns(self.energy_densities) if self.energy_densities is not None else ()
+        hf_cols = getattr(self.combine_densities, "_gdft_hf_cols", None) if self.combine_densities else None
+        if hf_cols != (_lib.COL_HF,):
+            raise NotImplementedError("the HF-density gradient is built for functionals whose HF column is "
+                                      "the sum of ehf over omega and spin (b3lyp_combine)")
+        if self.coefficient_inputs is not None or self.nograd_coefficient_inputs is not None:
+            raise NotImplementedError("coefficient inputs are only supported by NeuralFunctional/DM21")
+        coeffs = _const_row(self.coefficients(self, None))
+        fn = engine.make_functional(cols + tuple(hf_cols), coeffs, clip_cte)
+        _, _, g = atoms.resident().xc_energy_grads_hf(atoms._rdm1(), fn, ehf, want_vxc=False)
+        return g
+
     def energy_xc_only(self, params, atoms, *args, **kwargs):
         fn, ehf = self.spec(params, atoms, kwargs.get("clip_cte", CLIP))
         rdm1 = atoms.rdm1 if isinstance(atoms.rdm1, torch.Tensor) and atoms.rdm1.requires_grad else atoms._rdm1()

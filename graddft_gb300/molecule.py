@@ -133,13 +133,51 @@ class Molecule:
                               want_energy=True)
         return e
 
-    def HF_energy_density(self, omegas, *args, **kwargs):
-        """molecule.py:188-210.  Only the supplied stop-gradient ``ehf`` is available in this build."""
-        if self.ehf is not None:
-            return engine.as_device_f64(self.ehf, self.device)[: len(omegas)]
+    # ------------------------------------------------- exact exchange (chi)
+    def select_HF_omegas(self, omegas):
+        """molecule.py:153-183: chi (grid, omega, spin, orbitals) for the given omegas."""
         if self.chi is None:
             raise ValueError("Precomputed chi tensor has not been loaded.")
-        raise NotImplementedError("the chi-based HF energy density is not built in this version")
+        have = [float(o) for o in (self.omegas.tolist() if hasattr(self.omegas, "tolist") else self.omegas)]
+        for o in omegas:
+            if float(o) not in have:
+                raise ValueError(f"The molecule.chi tensor does not contain omega value {o}, only {self.omegas}")
+        idx = [have.index(float(o)) for o in omegas]
+        chi = engine.as_device_f64(self.chi, self.device)
+        return chi[:, idx].contiguous()
+
+    def HF_energy_density(self, omegas, *args, **kwargs):
+        """molecule.py:185-204: ehf (omega, spin, grid) from chi on the device.
+
+        Without chi, a supplied stop-gradient ``ehf`` (omega, spin, grid) stands in.
+        """
+        if self.chi is not None:
+            return engine.hf_energy_density(engine.as_device_f64(self.ao, self.device), self._rdm1(),
+                                            self.select_HF_omegas(omegas))
+        if self.ehf is not None:
+            return engine.as_device_f64(self.ehf, self.device)[: len(omegas)]
+        raise ValueError("Precomputed chi tensor has not been loaded.")
+
+    def HF_density_grad_2_Fock(self, functional, params, omegas, ehf, coefficient_inputs, densities_wout_hf,
+                               **kwargs):
+        """molecule.py:206-250 -> (omega, spin, orbitals, orbitals).
+
+        F[w,s,a,b] = -1/2 sum_r chi[r,w,s,b] g[w,s,r] ao[r,a] with g = dE_xc/d ehf
+        through the densities (molecule.py:545-613).  The densities are
+        recomputed on the device from rdm1 (they are the ones predict passes).
+        """
+        chi = self.select_HF_omegas(omegas)
+        ehf = engine.as_device_f64(ehf, self.device)
+        g = functional.hf_density_gradient(params, self, ehf, kwargs.get("clip_cte", 1e-30))
+        ao = engine.as_device_f64(self.ao, self.device)
+        g3 = g[None, None, :].expand(1, 2, g.shape[0]).contiguous()
+        return torch.stack([engine.hf_fock(ao, chi[:, w:w + 1], g3) for w in range(chi.shape[1])])
+
+    def HF_coefficient_input_grad_2_Fock(self, functional, params, omegas, ehf, cinputs_wout_hf, densities,
+                                         **kwargs):
+        """molecule.py:252-294: the HF-Fock term through the coefficient inputs (DM21)."""
+        self.select_HF_omegas(omegas)
+        raise NotImplementedError("the HF-Fock term through the network's coefficient inputs is not built yet")
 
     def to_dict(self) -> dict:
         d = {f.name: getattr(self, f.name) for f in dataclasses.fields(self)[1:] if not f.name.startswith("_")}

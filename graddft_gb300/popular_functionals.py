@@ -61,10 +61,9 @@ def b3lyp_nograd_densities(molecule, *_, **__):
 
 
 def b3lyp_hfgrads(functional, params, molecule, ehf, cinputs, densities_wout_hf, omegas=(0.0,)):
-    """popular_functionals.py:352-372 (explicit HF Fock term; needs chi)."""
-    if getattr(molecule, "chi", None) is None:
-        raise ValueError("Precomputed chi tensor has not been loaded.")
-    raise NotImplementedError("the chi-based HF Fock contribution is not built in this version")
+    """popular_functionals.py:352-372: the explicit HF Fock term, summed over omega (needs chi)."""
+    vxc_hf = molecule.HF_density_grad_2_Fock(functional, params, omegas, ehf, cinputs, densities_wout_hf)
+    return vxc_hf.sum(dim=0)
 
 
 def _one(self, *_):

@@ -139,6 +139,26 @@ def make_ehf(n_grid: int, seed: int = 0, rho: np.ndarray | None = None, n_omega:
     return out
 
 
+def make_chi(ao: np.ndarray, rdm1: np.ndarray, n_omega: int = 2, seed: int = 0) -> np.ndarray:
+    """A stand-in chi tensor (grid, omega, spin, orbitals) for the exact-exchange terms.
+
+    chi^{w,s}_c(r) = sum_bd D^s_bd psi_b(r) v^w_cd(r) needs range-separated
+    integrals (``interface/pyscf.py:1067-1126``); here v^w_cd(r) is replaced by a
+    seeded smooth positive factor k_w (1 + 0.3 u_c(r)), so that chi = k_w (1 +
+    0.3 u) (phi D) and ehf = -1/2 chi . (phi D) has the sign and rough size of
+    the exchange energy density.
+    """
+    g = rng(seed, STREAM_EHF + 1)
+    x = np.einsum("ra,sab->rsb", np.asarray(ao, dtype=np.float64), np.asarray(rdm1, dtype=np.float64))
+    n_grid, _, n_ao = x.shape
+    out = np.empty((n_grid, n_omega, 2, n_ao))
+    for w in range(n_omega):
+        k = 1.0 / (1.0 + 0.5 * w)
+        u = g.uniform(-1.0, 1.0, size=(n_grid, 1, n_ao))
+        out[:, w] = k * (1.0 + 0.3 * u) * x
+    return out
+
+
 def glorot_params(layer_widths=(256,) * 6, n_in: int = 11, n_out: int = 3, seed: int = 0) -> dict:
     """Flax-style parameter tree for the DM21 network (``functional.py:797-822``).
 

@@ -12,9 +12,10 @@ def energy_predictor(functional, nlc_functional=None, clip_cte: float = CLIP, **
 
     ``predict(params, atoms) -> (E, F)``: E = E_xc + nonXC and
     F = abs_clip(1/2 (G + G^T)) with G = abs_clip(h1e + J + dE_xc/d rdm1)
-    (train.py:147-163).  The explicit HF Fock terms (train.py:200-213) need a
-    chi tensor: as in the reference, a functional with ``densitygrads`` or
-    ``coefficient_input_grads`` raises ``ValueError`` when the molecule has none.
+    (train.py:147-163), plus the explicit HF Fock terms of ``densitygrads`` /
+    ``coefficient_input_grads`` (train.py:165-213) computed from the
+    molecule's chi tensor; as in the reference, a functional that has them
+    raises ``ValueError`` when the molecule has no chi.
     """
     if nlc_functional is not None:
         raise NotImplementedError("dispersion (nlc) functionals are not part of the XC grid path")
@@ -30,7 +31,18 @@ def energy_predictor(functional, nlc_functional=None, clip_cte: float = CLIP, **
         energy = exc + enonxc
         fock = engine.fock(atoms.h1e, vj, vxc, clip_cte)
         if needs_chi:
-            raise NotImplementedError("the chi-based HF Fock contributions are not built in this version")
+            # train.py:165-213: the explicit HF terms, each added as F + F^T and clipped.
+            grad_densities = functional.energy_densities(atoms) if functional.energy_densities is not None else None
+            nograd_densities = functional.nograd_densities(atoms) if functional.nograd_densities else None
+            cinputs = functional.compute_coefficient_inputs(atoms)
+            if functional.densitygrads is not None:
+                vxc_expl = functional.densitygrads(functional, params, atoms, nograd_densities, cinputs,
+                                                   grad_densities)
+                fock = engine.fock_add_hf(fock, vxc_expl, clip_cte)
+            if functional.coefficient_input_grads is not None:
+                vxc_expl = functional.coefficient_input_grads(functional, params, atoms, nograd_densities, cinputs,
+                                                              grad_densities)
+                fock = engine.fock_add_hf(fock, vxc_expl, clip_cte)
         return energy, fock
 
     return predict

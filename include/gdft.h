@@ -133,6 +133,37 @@ int gdft_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rdm1, con
                              const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc,
                              void *d_ws, size_t ws_bytes, void *stream);
 
+/* gdft_xc_energy_and_grads plus d_ghf (n_grid): dE_xc/d ehf[w][s][r] for a
+ * functional whose HF column (GDFT_COL_HF) is ehf summed over omega and spin
+ * (b3lyp_combine, popular_functionals.py:328-337), the same for every (w, s):
+ * abs_clip(w_r) * [|sum_f c_f e_f(r)| > clip] * c_HF with the other columns
+ * unclipped -- the gradient HF_density_grad_2_Fock takes (molecule.py:598-603)
+ * with the energy densities as predict passes them (train.py:167-178). */
+int gdft_xc_energy_grads_hf(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,
+                            const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc, double *d_ghf,
+                            void *d_ws, size_t ws_bytes, void *stream);
+
+/* Exact-exchange terms from a supplied chi tensor (grid, omega, spin,
+ * orbitals), FP64 device arrays in the reference's layouts; ao is (grid,
+ * orbitals) row-major, rdm1 (2, n, n).  Workspace of
+ * gdft_hf_workspace_bytes bytes (8-byte aligned).
+ *   gdft_hf_energy_density: ehf (omega, 2, grid) =
+ *       -1/2 einsum("rwsc,sac,ra->wsr", chi, rdm1, ao)   (molecule.py:507-541)
+ *   gdft_hf_fock: fock_hf (2, n, n) =
+ *       sum_w -1/2 einsum("rws,wsr,ra->wsab"...), i.e.
+ *       F_s[a][b] = -1/2 sum_w sum_r ao[r][a] g[w][s][r] chi[r][w][s][b]
+ *       with g = dE/d ehf (omega, 2, grid): HF_density_grad_2_Fock /
+ *       HF_coefficient_input_grad_2_Fock (molecule.py:545-685) summed over
+ *       omega as b3lyp_hfgrads and dm21_hfgrads_* do.
+ *   gdft_fock_add_hf: fock (2, n, n) = abs_clip(fock + F + F^T, clip), the
+ *       update of train.py:200-210. */
+int gdft_hf_workspace_bytes(int64_t n_grid, int32_t n_ao, int32_t n_omega, size_t *bytes);
+int gdft_hf_energy_density(const double *d_ao, const double *d_rdm1, const double *d_chi, int64_t n_grid,
+                           int32_t n_ao, int32_t n_omega, double *d_ehf, void *d_ws, size_t ws_bytes, void *stream);
+int gdft_hf_fock(const double *d_ao, const double *d_chi, const double *d_g, int64_t n_grid, int32_t n_ao,
+                 int32_t n_omega, double *d_fock_hf, void *d_ws, size_t ws_bytes, void *stream);
+int gdft_fock_add_hf(double *d_fock, const double *d_fock_hf, int32_t n_ao, double clip, void *stream);
+
 /* The DM21-style coefficient network of a NeuralFunctional (DM21.default_nn,
  * functional.py:797-822, with NeuralFunctional.head :407-419):
  *   h0 = tanh(log(|x| + squash_offset) W0 + b0),

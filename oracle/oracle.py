@@ -29,6 +29,7 @@ __all__ = [
     "dm21_coefficient_inputs", "dm21_densities", "dm21_combine_cinputs", "dm21_combine_densities",
     "densities_generic", "dm21_network", "FUNCTIONALS", "energy_densities", "xc_energy",
     "xc_energy_and_grads", "xc_hvp", "predict_fock", "t64", "features_numpy", "FZETA_PP0",
+    "hf_energy_density", "hf_density_grad_2_fock", "b3lyp_predict_with_chi",
 ]
 
 
@@ -379,8 +380,12 @@ def _features(rdm1, ao, grad_ao, grad2_ao):
     return rho, grad_rho, lapl, tau
 
 
-def energy_densities(name, rho, grad_rho, lapl, tau, ehf=None, clip_cte=CLIP):
-    """Stack the energy-density columns of a named functional, then abs_clip (functional.py:160-185)."""
+def energy_densities(name, rho, grad_rho, lapl, tau, ehf=None, clip_cte=CLIP, clip_output=True):
+    """Stack the energy-density columns of a named functional, then abs_clip (functional.py:160-185).
+
+    ``clip_output=False`` leaves out the final abs_clip: the columns as
+    ``energy_densities`` returns them before compute_densities clips them.
+    """
     cols, _ = FUNCTIONALS[name]
     out = []
     for c in cols:
@@ -404,7 +409,8 @@ def energy_densities(name, rho, grad_rho, lapl, tau, ehf=None, clip_cte=CLIP):
             out.append(ehf.detach()[1].sum(axis=0))
         else:
             raise KeyError(c)
-    return abs_clip(torch.stack(out, axis=1), clip_cte)
+    stacked = torch.stack(out, axis=1)
+    return abs_clip(stacked, clip_cte) if clip_output else stacked
 
 
 def xc_energy(coefficients, densities, weights, clip_cte=CLIP):
@@ -507,6 +513,49 @@ def predict_fock(E_xc, V_xc, h1e, vj, nonxc_energy, clip_cte=CLIP):
     fock = 0.5 * (fock + fock.transpose(1, 2))
     fock = abs_clip(fock, clip_cte)
     return E_xc + nonxc_energy, abs_clip(fock, clip_cte).numpy()
+
+
+# --------------------------------------------------------------------------
+# Exact exchange from a chi tensor (molecule.py:153-300, 504-685; train.py:165-213)
+# --------------------------------------------------------------------------
+def hf_energy_density(rdm1, ao, chi):
+    """molecule.py:507-541: ehf (omega, spin, grid) = -1/2 einsum("rwsc,sac,ra->wsr", chi, rdm1, ao)."""
+    return -0.5 * torch.einsum("rwsc,sac,ra->wsr", t64(chi), t64(rdm1), t64(ao))
+
+
+def hf_density_grad_2_fock(name, rdm1, ao, grad_ao, grad2_ao, weights, chi, ehf, clip_cte=CLIP):
+    """molecule.py:545-613 for a constant-coefficient functional: (omega, spin, n, n).
+
+    gr = d xc_energy / d ehf with the densities as predict passes them
+    (energy_densities unclipped, train.py:167-178, combined with ehf by
+    b3lyp_combine); F[w,s,a,b] = -1/2 sum_r chi[r,w,s,b] gr[w,s,r] ao[r,a].
+    """
+    cols, coeffs = FUNCTIONALS[name]
+    with torch.no_grad():
+        rho, grad_rho, lapl, tau = _features(t64(rdm1), t64(ao), t64(grad_ao),
+                                             None if grad2_ao is None else t64(grad2_ao))
+        raw = energy_densities(name, rho, grad_rho, lapl, tau, t64(ehf), clip_cte, clip_output=False)
+    ehf_v = t64(ehf).clone().requires_grad_(True)
+    dens = torch.cat([raw[:, :-1], ehf_v.sum(axis=(0, 1))[:, None]], axis=1)
+    E = xc_energy(torch.tensor([coeffs], dtype=F64), dens, t64(weights), clip_cte)
+    (gr,) = torch.autograd.grad(E, ehf_v)
+    return -0.5 * torch.einsum("rwsb,wsr,ra->wsab", t64(chi), gr, t64(ao))
+
+
+def b3lyp_predict_with_chi(rdm1, ao, grad_ao, grad2_ao, weights, h1e, eri, chi, omegas, nuclear_repulsion,
+                           clip_cte=CLIP):
+    """energy_predictor(B3LYP) (train.py:124-218) with its HF terms from chi: (E, F)."""
+    i0 = list(np.asarray(omegas)).index(0.0)
+    ehf0 = hf_energy_density(rdm1, ao, t64(chi)[:, i0:i0 + 1])
+    e, v = xc_energy_and_grads("B3LYP", rdm1, ao, grad_ao, grad2_ao, weights, ehf=ehf0, clip_cte=clip_cte)
+    d = np.asarray(rdm1).sum(0)
+    vj = np.einsum("pqrt,rt->pq", eri, d)
+    enonxc = nuclear_repulsion + np.einsum("ij,ij->", d, h1e) + np.einsum("pq,pq->", d, vj) / 2.0
+    E, F = predict_fock(e, v, h1e, vj, enonxc, clip_cte)
+    vexpl = hf_density_grad_2_fock("B3LYP", rdm1, ao, grad_ao, grad2_ao, weights, t64(chi)[:, i0:i0 + 1], ehf0,
+                                   clip_cte).sum(0)
+    F = t64(F) + vexpl + vexpl.transpose(1, 2)
+    return E, abs_clip(F, clip_cte).detach().numpy()
 
 
 def features_numpy(rdm1, ao, grad_ao, grad2_ao):

@@ -300,6 +300,21 @@ class _Sub:
         return typing.Any
 
 
+def vmap(fun, in_axes=0, out_axes=0, **_):
+    """jax.vmap for single-array outputs: a loop over the mapped axis, then a stack."""
+
+    def wrapped(*args):
+        axes = tuple(in_axes) if isinstance(in_axes, (tuple, list)) else (in_axes,) * len(args)
+        n = next(_t(a).shape[ax] for a, ax in zip(args, axes) if ax is not None)
+        outs = []
+        for i in range(n):
+            sl = [_t(a).select(ax, i) if ax is not None else a for a, ax in zip(args, axes)]
+            outs.append(_t(fun(*sl)))
+        return torch.stack(outs, dim=out_axes)
+
+    return wrapped
+
+
 def install():
     """Register the stand-in modules (idempotent)."""
     if "jax" in sys.modules and getattr(sys.modules["jax"], "_is_graddft_shim", False):
@@ -330,9 +345,6 @@ def install():
         return f
 
     jax.jit = jit
-
-    def vmap(*a, **k):
-        raise NotImplementedError("vmap is not part of the XC path stand-in")
 
     jax.vmap = vmap
     jax.custom_vjp = lambda f: f
@@ -424,8 +436,8 @@ def load_reference(root: str):
     utils = types.ModuleType("grad_dft.utils")
     utils.__path__ = []
 
-    def vmap_chunked(*a, **k):
-        raise NotImplementedError("vmap_chunked is outside the XC path stand-in")
+    def vmap_chunked(fun, in_axes=0, out_axes=0, chunk_size=None, **_):
+        return vmap(fun, in_axes=in_axes, out_axes=out_axes)
 
     utils.vmap_chunked = vmap_chunked
     sys.modules["grad_dft.utils"] = utils

@@ -28,13 +28,16 @@ from oracle.ao_numpy import eval_ao_planes  # noqa: E402
 
 F64 = torch.float64
 
-# torch's Tensor.transpose takes two dims; the reference calls transpose(perm) (train.py:157,162).
+# torch's Tensor.transpose takes two dims; the reference calls transpose(perm) (train.py:157,162)
+# and transpose(*axes) (molecule.py:613).
 _orig_transpose = torch.Tensor.transpose
 
 
 def _transpose(self, *dims):
     if len(dims) == 1 and isinstance(dims[0], (tuple, list)):
         return self.permute(*dims[0])
+    if len(dims) > 2:  # jnp's transpose(*axes) (molecule.py:613)
+        return self.permute(*dims)
     return _orig_transpose(self, *dims)
 
 
@@ -43,6 +46,7 @@ CASES = {
     "compact": (512, 20, 4, 11, 6.0, 4.0),
     "tails": (384, 16, 3, 12, 20.0, 12.0),
     "dm21": (256, 16, 3, 13, 6.0, 4.0),
+    "hf": (320, 18, 4, 14, 6.0, 4.0),
 }
 
 
@@ -183,6 +187,29 @@ def main(root):
             else:
                 res[f"dtheta/{k}/{kk}"] = g
     path = os.path.join(HERE, "ref_dm21.npz")
+    np.savez_compressed(path, **res)
+    out_files.append(path)
+    # B3LYP with its exact-exchange terms from a chi tensor (molecule.py:153-300,
+    # popular_functionals.py:345-391, train.py:165-213): predict() runs the
+    # reference's HF_energy_density and HF_density_grad_2_Fock unchanged.
+    wl, ao, g1, g2, h1e, eri = _inputs("hf")
+    mol = _molecule(ref, wl, ao, g1, g2, h1e, eri)
+    omegas = np.array([0.0, 0.4])
+    chi = synthetic.make_chi(ao, wl.rdm1, n_omega=2, seed=15)
+    mol = mol.replace(chi=torch.as_tensor(chi), omegas=torch.as_tensor(omegas))
+    res = dict(ao=ao, grad_ao=g1, grad2_ao=g2, weights=wl.weights, rdm1=wl.rdm1, h1e=h1e, eri=eri, chi=chi,
+               omegas=omegas)
+    with torch.no_grad():
+        res["ehf"] = mol.HF_energy_density(list(omegas)).numpy()
+        res["ehf_w0"] = mol.HF_energy_density([0.0]).numpy()
+    params = {"params": {}}
+    E, F = ref.train.energy_predictor(pop.B3LYP)(params, mol)
+    res["predict_E_B3LYP"] = E.detach().numpy()
+    res["predict_F_B3LYP"] = F.detach().numpy()
+    ehf0 = mol.HF_energy_density([0.0]).detach()
+    vexpl = pop.b3lyp_hfgrads(pop.B3LYP, params, mol, ehf0, None, pop.b3lyp_exhf_densities(mol))
+    res["b3lyp_hfgrads"] = vexpl.detach().numpy()
+    path = os.path.join(HERE, "ref_hf.npz")
     np.savez_compressed(path, **res)
     out_files.append(path)
     torch.Tensor.transpose = _orig_transpose

@@ -1,0 +1,104 @@
+"""GPU parity of the exact-exchange (HF) terms computed from a chi tensor.
+
+HF_energy_density (molecule.py:507-541), the HF Fock term of B3LYP
+(HF_density_grad_2_Fock, molecule.py:545-613, summed over omega by
+b3lyp_hfgrads) and energy_predictor(B3LYP) with those terms (train.py:124-218)
+against fixtures made by running the reference's own source
+(tests/golden/make_golden.py), and the general-omega Fock contraction against
+the oracle.  All FP64: the bar is 1e-11 relative to the largest entry.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from graddft_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-11
+
+
+def _close(a, b, rtol=RTOL, what=""):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, (what, a.shape, b.shape)
+    scale = max(np.max(np.abs(b)), 1e-300)
+    err = np.max(np.abs(a - b))
+    assert err <= rtol * scale, f"{what}: max abs err {err:.3e} vs scale {scale:.3e}"
+
+
+@pytest.fixture(scope="module")
+def G(built_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import graddft_gb300 as G
+
+    return G
+
+
+def _t(x):
+    return torch.as_tensor(np.asarray(x), dtype=torch.float64, device="cuda")
+
+
+def _molecule(G, g, precision="fp64"):
+    grid = G.Grid(coords=None, weights=_t(g["weights"]))
+    return G.Molecule(grid=grid, atom_index=None, nuclear_pos=None, ao=_t(g["ao"]), grad_ao=_t(g["grad_ao"]),
+                      grad_n_ao={2: _t(g["grad2_ao"])}, rdm1=_t(g["rdm1"]), nuclear_repulsion=1.25, h1e=_t(g["h1e"]),
+                      vj=None, mo_coeff=None, mo_occ=None, mo_energy=None, rep_tensor=_t(g["eri"]),
+                      omegas=[float(o) for o in g["omegas"]], chi=_t(g["chi"]), precision=precision)
+
+
+def test_hf_energy_density(G, golden):
+    g = golden("hf")
+    mol = _molecule(G, g)
+    _close(mol.HF_energy_density([0.0, 0.4]), g["ehf"], what="ehf")
+    _close(mol.HF_energy_density([0.0]), g["ehf_w0"], what="ehf w0")
+    # omega order follows the request, as in select_HF_omegas
+    _close(mol.HF_energy_density([0.4, 0.0]), g["ehf"][::-1], what="ehf reversed")
+
+
+def test_b3lyp_hf_fock_term(G, golden):
+    g = golden("hf")
+    mol = _molecule(G, g)
+    ehf0 = mol.HF_energy_density([0.0])
+    v = G.popular_functionals.b3lyp_hfgrads(G.B3LYP, {"params": {}}, mol, ehf0, None, None)
+    _close(v, g["b3lyp_hfgrads"], what="b3lyp_hfgrads")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32x3"])
+def test_b3lyp_predict_with_chi(G, golden, precision):
+    g = golden("hf")
+    mol = _molecule(G, g, precision)
+    E, F = G.energy_predictor(G.B3LYP)({"params": {}}, mol)
+    # The mixed form's E_xc and V_xc carry its ~1e-7 relative error; the HF terms are FP64 in both.
+    rtol = RTOL if precision == "fp64" else 2e-6
+    assert abs(float(E) - float(g["predict_E_B3LYP"])) <= rtol * abs(float(g["predict_E_B3LYP"]))
+    _close(F, g["predict_F_B3LYP"], rtol=rtol, what="F")
+
+
+def test_hf_fock_general_omegas_vs_oracle(G):
+    """Two omegas, omega- and spin-dependent g, ragged sizes."""
+    n_grid, n_ao = 4099, 37
+    wl = synthetic.make_workload(n_grid, n_ao, 5, seed=21, box_angstrom=7.0, centre_box_angstrom=4.0)
+    ao, _, _ = O.eval_ao_planes(wl.basis, wl.coords)
+    chi = synthetic.make_chi(ao, wl.rdm1, n_omega=2, seed=22)
+    rng = np.random.default_rng(23)
+    gw = rng.standard_normal((2, 2, n_grid)) * 1e-3
+    got = G.engine.hf_fock(_t(ao), _t(chi), _t(gw))
+    ref = (-0.5 * np.einsum("rwsb,wsr,ra->sab", chi, gw, ao))
+    _close(got, ref, what="hf_fock")
+    e = G.engine.hf_energy_density(_t(ao), _t(wl.rdm1), _t(chi))
+    _close(e, O.hf_energy_density(wl.rdm1, ao, chi).numpy(), what="ehf")
+
+
+def test_hf_errors(G, golden):
+    g = golden("hf")
+    mol = _molecule(G, g)
+    with pytest.raises(ValueError):
+        mol.HF_energy_density([0.2])  # omega not in molecule.omegas (molecule.py:176-180)
+    with pytest.raises(ValueError):
+        G.engine.hf_energy_density(_t(g["ao"]), _t(g["rdm1"]), _t(g["chi"])[:, :, :, :5])
+    no_chi = mol.replace(chi=None)
+    with pytest.raises(ValueError):
+        no_chi.HF_energy_density([0.0])

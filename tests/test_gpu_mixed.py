@@ -1,10 +1,12 @@
 """GPU parity of the mixed (TF32x3 tensor-core) form.
 
-The mixed form rounds the AO tables and D to hi + lo TF32 pairs (~22 bits)
-and accumulates in FP32 inside bounded windows, FP64 across them.  It is
-checked against the FP64 oracle on small and ragged shapes with the
-tolerances below (relative to the largest entry), and against the GPU FP64
-form at larger sizes.
+The density contraction rounds the AO tables and D to hi + lo TF32 pairs
+(~22 bits) and accumulates in FP32 inside bounded windows, FP64 across them;
+the V_xc contraction runs on block-scaled three-slice operands with exact
+hi*hi chunk sums.  It is checked against the FP64 oracle on small and ragged
+shapes with the tolerances below (relative to the largest entry; the largest
+errors seen are about a third of them), and against the GPU FP64 form at
+n_ao 512 with the absolute bounds the mixed form is specified to meet.
 """
 import numpy as np
 import pytest
@@ -16,9 +18,12 @@ from graddft_gb300 import synthetic
 pytestmark = pytest.mark.gpu
 
 # Mixed-form tolerances, relative to the largest magnitude of the quantity.
-TOL_FEAT = 2e-5
-TOL_E = 1e-6
-TOL_V = 2e-5
+TOL_FEAT = 2e-6
+TOL_E = 5e-7
+TOL_V = 2e-6
+# Absolute bounds of the mixed form against the FP64 form (Ha).
+ABS_DE = 1e-6
+ABS_DV = 1e-7
 
 
 @pytest.fixture(scope="module")
@@ -88,5 +93,5 @@ def test_mixed_vs_fp64_gpu_large(eng):
     de = abs(float(emx) - float(e64))
     dv = float((vmx - v64).abs().max())
     print("E", float(e64), "|dE|", de, "max|V|", float(v64.abs().max()), "max|dV|", dv)
-    assert de <= TOL_E * abs(float(e64))
-    assert dv <= TOL_V * float(v64.abs().max())
+    assert de <= ABS_DE and de <= TOL_E * abs(float(e64))
+    assert dv <= ABS_DV and dv <= TOL_V * float(v64.abs().max())

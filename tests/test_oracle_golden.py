@@ -143,3 +143,16 @@ def test_ao_normalisation():
     ao, _, _ = eval_ao_planes(basis, pts)
     dv = (t[1] - t[0]) ** 3
     np.testing.assert_allclose((ao ** 2).sum(0) * dv, 1.0, rtol=1e-6)
+
+
+def test_hf_exact_exchange_vs_reference(golden):
+    """HF_energy_density, b3lyp_hfgrads and B3LYP predict with a chi tensor (reference fixtures)."""
+    g = golden("hf")
+    _close(O.hf_energy_density(g["rdm1"], g["ao"], g["chi"]).numpy(), g["ehf"])
+    f = O.hf_density_grad_2_fock("B3LYP", g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"],
+                                 g["chi"][:, :1], g["ehf_w0"]).sum(0)
+    _close(f.detach().numpy(), g["b3lyp_hfgrads"])
+    E, F = O.b3lyp_predict_with_chi(g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"], g["h1e"],
+                                    g["eri"], g["chi"], g["omegas"], 1.25)
+    assert abs(E - float(g["predict_E_B3LYP"])) <= 1e-12 * abs(float(g["predict_E_B3LYP"]))
+    _close(F, g["predict_F_B3LYP"])
