@@ -624,6 +624,51 @@ int gdft_neural_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rd
   return run_vxc(mol, coef, d_vxc, ws, st);
 }
 
+int gdft_neural_xc_hf_grads(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net,
+                            const double *d_params, const double *d_ehf, double *d_exc, double *d_g_dens,
+                            double *d_g_cin, void *d_ws, size_t ws_bytes, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_network(net))) return rc;
+  if (net->precision != GDFT_FP64 || net->n_in != kDm21In || net->n_out != kDm21Out) {
+    set_error("gdft_neural_xc_hf_grads: the HF gradients are built for the FP64 DM21 network form "
+              "(11 inputs, 3 outputs)");
+    return GDFT_ERR_INVALID;
+  }
+  const size_t need = neural_ws_bytes(mol, net);
+  if (d_ws == nullptr || ws_bytes < need) {
+    set_error("workspace of %zu bytes is smaller than the %zu bytes required", ws_bytes, need);
+    return GDFT_ERR_WORKSPACE;
+  }
+  if (((uintptr_t)d_ws & 255u) != 0) {
+    set_error("workspace must be 256-byte aligned");
+    return GDFT_ERR_ALIGNMENT;
+  }
+  if (d_rdm1 == nullptr || d_params == nullptr || d_ehf == nullptr || d_exc == nullptr ||
+      (d_g_dens == nullptr && d_g_cin == nullptr)) {
+    set_error("gdft_neural_xc_hf_grads: rdm1, params, ehf, exc and one of g_dens, g_cin are required");
+    return GDFT_ERR_INVALID;
+  }
+  if ((rc = check_aligned8(d_params, "params")) || (rc = check_aligned8(d_ehf, "ehf")) ||
+      (d_g_dens && (rc = check_aligned8(d_g_dens, "g_dens"))) || (d_g_cin && (rc = check_aligned8(d_g_cin, "g_cin"))))
+    return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  const WsLayout W = ws_layout(mol);
+  if ((rc = run_density(mol, d_rdm1, ws, st))) return rc;
+  double *feat = (double *)(ws + W.off_feat);
+  double *coef = (double *)(ws + W.off_coef);
+  double *mws = (double *)(ws + W.bytes);
+  {
+    StageTimer tm(GDFT_STAGE_MLP, st);
+    if ((rc = mlp_run_f64(net_shape(net), d_params, nullptr, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
+                          net->clip, mws, d_exc, coef, st)))
+      return rc;
+  }
+  return check_cuda(launch_dm21_hf_grads(net_shape(net), mol->n_grid, mol->n_grid_pad, mws, d_g_dens, d_g_cin, st),
+                    "dm21_hf_grads");
+}
+
 int gdft_neural_inputs(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net, const double *d_ehf,
                        double *d_cinputs, double *d_dens, void *d_ws, size_t ws_bytes, void *stream) {
   int rc = check_mol(mol);

@@ -346,6 +346,39 @@ cudaError_t launch_dm21_features(const double *feat, const double *ehf, int64_t 
   return cudaGetLastError();
 }
 
+// dE/d ehf[w][s][r] of the DM21 network (for the HF Fock terms, molecule.py:545-685):
+//   through the densities: the HF energy-density column of omega w is the spin
+//   sum of ehf[w] (dm21_combine_densities, functional.py:652-675), so the
+//   gradient is dE/de_{1+w} for both spins;
+//   through the inputs: ehf[w][s] is input 7 + 2 s + w (dm21_combine_cinputs,
+//   functional.py:628-649), entering as log(|x| + offset).
+__global__ void dm21_hf_grads_kernel(const double *__restrict__ x, const double *__restrict__ du,
+                                     const double *__restrict__ de, int64_t n_grid, double off,
+                                     double *__restrict__ g_dens, double *__restrict__ g_cin) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_grid) return;
+#pragma unroll
+  for (int w = 0; w < 2; ++w)
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const size_t o = ((size_t)w * 2 + s) * n_grid + p;
+      if (g_dens) g_dens[o] = de[(size_t)p * 3 + 1 + w];
+      if (g_cin) {
+        const int k = 7 + 2 * s + w;
+        const double xv = x[(size_t)p * kDm21In + k];
+        g_cin[o] = du[(size_t)p * kDm21InPad + k] * (xv >= 0.0 ? 1.0 : -1.0) / (fabs(xv) + off);
+      }
+    }
+}
+
+cudaError_t launch_dm21_hf_grads(const MlpShape &S, int64_t n_grid, int64_t np, const double *ws, double *g_dens,
+                                 double *g_cin, cudaStream_t st) {
+  const MlpLayout L = mlp_layout(S, np);
+  dm21_hf_grads_kernel<<<(unsigned)((n_grid + 255) / 256), 256, 0, st>>>(ws + L.x, ws + L.du, ws + L.de, n_grid,
+                                                                          S.squash_offset, g_dens, g_cin);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_dm21_potentials(const double *feat, const double *x, const double *du, const double *de,
                                    int64_t n_grid, int64_t np, double clip, double off, double *coef,
                                    cudaStream_t st) {

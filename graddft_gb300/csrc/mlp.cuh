@@ -45,6 +45,11 @@ bool mlp_width_supported(int width);
 int mlp_run_f64(const MlpShape &S, const double *params, double *dparams, const double *feat, const double *ehf,
                 const double *w, int64_t n_grid, int64_t np, double clip, double *ws, double *exc, double *coef,
                 cudaStream_t st);
+// After mlp_run_f64 with coef (the backward pass) on the same workspace:
+// g_dens, g_cin (2 omegas, 2 spins, n_grid) = dE/d ehf through the HF
+// energy-density columns and through the HF inputs (either may be null).
+cudaError_t launch_dm21_hf_grads(const MlpShape &S, int64_t n_grid, int64_t np, const double *ws, double *g_dens,
+                                 double *g_cin, cudaStream_t st);
 
 // Scratch of the second-order pass (offsets in doubles).  Primal and tangent
 // activations are stacked as [2][np][width] so one GEMM serves both.

@@ -187,6 +187,22 @@ class Resident:
             _ptr(vxc), _ptr(dp), _ptr(ws), ws.numel(), _stream(self.device)))
         return exc, vxc, dp
 
+    def neural_xc_hf_grads(self, rdm1, net: "Network", flat_params, ehf):
+        """(E_xc, g_dens, g_cin): dE_xc/d ehf (2, 2, grid) through the HF densities and through the HF inputs."""
+        rdm1 = self._rdm1(rdm1)
+        ehf_t = as_device_f64(ehf, self.device)
+        if ehf_t is None or ehf_t.shape != (2, 2, self.n_grid):
+            raise ValueError(f"ehf must be (2, 2, {self.n_grid})")
+        flat = as_device_f64(flat_params, self.device)
+        ws = self._neural_ws(net)
+        exc = torch.empty((), dtype=F64, device=self.device)
+        g_dens = torch.empty((2, 2, self.n_grid), dtype=F64, device=self.device)
+        g_cin = torch.empty((2, 2, self.n_grid), dtype=F64, device=self.device)
+        check(_lib.load().gdft_neural_xc_hf_grads(ctypes.byref(self.desc), _ptr(rdm1), ctypes.byref(net.desc),
+                                                  _ptr(flat), _ptr(ehf_t.contiguous()), _ptr(exc), _ptr(g_dens),
+                                                  _ptr(g_cin), _ptr(ws), ws.numel(), _stream(self.device)))
+        return exc, g_dens, g_cin
+
     def neural_xc_hvp(self, rdm1, net: "Network", flat_params, ehf, tangent, want_value=False, want_drdm1=True,
                       want_dparams=True):
         """Gradients of L = <tangent, V_xc(D, theta)>: (L, dL/dD, dL/dtheta) (second-order adjoint)."""

@@ -172,7 +172,7 @@ class Functional:
         return atoms.resident().xc_energy_and_grads(atoms._rdm1(), fn, ehf, want_vxc=True)
 
     def hf_density_gradient(self, params, atoms, ehf, clip_cte: float = CLIP):
-        """dE_xc/d ehf[w][s][r] (grid,) through the densities, the gradient that
+        """dE_xc/d ehf (omega, spin, grid) through the densities, the gradient that
         HF_density_grad_2_Fock takes (molecule.py:598-603): the same for every
         (omega, spin) because the HF column is their sum (b3lyp_combine)."""
         cols = energy_density_columns(self.energy_densities) if self.energy_densities is not None else ()
@@ -185,7 +185,11 @@ class Functional:
         coeffs = _const_row(self.coefficients(self, None))
         fn = engine.make_functional(cols + tuple(hf_cols), coeffs, clip_cte)
         _, _, g = atoms.resident().xc_energy_grads_hf(atoms._rdm1(), fn, ehf, want_vxc=False)
-        return g
+        return g[None, None, :].expand(ehf.shape[0], 2, g.shape[0]).contiguous()
+
+    def hf_cinput_gradient(self, params, atoms, ehf, clip_cte: float = CLIP):
+        """dE_xc/d ehf through the coefficient inputs: none for constant coefficients."""
+        raise NotImplementedError("the functional's coefficients do not depend on HF inputs")
 
     def energy_xc_only(self, params, atoms, *args, **kwargs):
         fn, ehf = self.spec(params, atoms, kwargs.get("clip_cte", CLIP))

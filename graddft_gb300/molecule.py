@@ -167,17 +167,22 @@ class Molecule:
         recomputed on the device from rdm1 (they are the ones predict passes).
         """
         chi = self.select_HF_omegas(omegas)
-        ehf = engine.as_device_f64(ehf, self.device)
-        g = functional.hf_density_gradient(params, self, ehf, kwargs.get("clip_cte", 1e-30))
+        g = functional.hf_density_gradient(params, self, engine.as_device_f64(ehf, self.device),
+                                           kwargs.get("clip_cte", 1e-30))
+        return self._hf_fock_per_omega(chi, g)
+
+    def _hf_fock_per_omega(self, chi, g):
         ao = engine.as_device_f64(self.ao, self.device)
-        g3 = g[None, None, :].expand(1, 2, g.shape[0]).contiguous()
-        return torch.stack([engine.hf_fock(ao, chi[:, w:w + 1], g3) for w in range(chi.shape[1])])
+        return torch.stack([engine.hf_fock(ao, chi[:, w:w + 1], g[w:w + 1]) for w in range(chi.shape[1])])
 
     def HF_coefficient_input_grad_2_Fock(self, functional, params, omegas, ehf, cinputs_wout_hf, densities,
                                          **kwargs):
-        """molecule.py:252-294: the HF-Fock term through the coefficient inputs (DM21)."""
-        self.select_HF_omegas(omegas)
-        raise NotImplementedError("the HF-Fock term through the network's coefficient inputs is not built yet")
+        """molecule.py:252-294 -> (omega, spin, orbitals, orbitals): as HF_density_grad_2_Fock with
+        g = dE_xc/d ehf through the network's HF inputs (molecule.py:668-673)."""
+        chi = self.select_HF_omegas(omegas)
+        g = functional.hf_cinput_gradient(params, self, engine.as_device_f64(ehf, self.device),
+                                          kwargs.get("clip_cte", 1e-30))
+        return self._hf_fock_per_omega(chi, g)
 
     def to_dict(self) -> dict:
         d = {f.name: getattr(self, f.name) for f in dataclasses.fields(self)[1:] if not f.name.startswith("_")}

@@ -9,9 +9,10 @@ dE_xc/d theta from the hand-written adjoint.  Parameters are the flax tree
 tensors, numpy arrays or DLPack producers.
 
 The HF inputs (``nograd_densities`` / ``nograd_coefficient_inputs``) are
-stop-gradient, as in the reference.  The explicit HF Fock terms
-(``densitygrads`` / ``coefficient_input_grads``, train.py:200-213) need the chi
-tensor and are not part of this path.
+stop-gradient, as in the reference; with a chi tensor on the molecule they come
+from ``Molecule.HF_energy_density`` and the explicit HF Fock terms
+(``densitygrads`` / ``coefficient_input_grads``, train.py:200-213) are built
+from the network's dE/d ehf (FP64 network form).
 """
 from __future__ import annotations
 
@@ -57,18 +58,17 @@ def _neural_inputs(atoms, net: engine.Network, ehf):
     return x, e
 
 
-def dm21_hfgrads_densities(functional, params, atoms, *_, **__):
-    """functional.py:676-716: HF-Fock term from dE/d ehf (densities); needs the chi tensor."""
-    if getattr(atoms, "chi", None) is None:
-        raise ValueError("Precomputed chi tensor has not been loaded.")
-    raise NotImplementedError("the chi-based HF Fock contributions are not part of the XC grid path")
+def dm21_hfgrads_densities(functional, params, atoms, ehf, coefficient_inputs, densities_wout_hf,
+                           omegas=(0.0, 0.4)):
+    """functional.py:677-716: the HF Fock term from dE/d ehf through the HF densities, summed over omega."""
+    return atoms.HF_density_grad_2_Fock(functional, params, omegas, ehf, coefficient_inputs,
+                                        densities_wout_hf).sum(dim=0)
 
 
-def dm21_hfgrads_cinputs(functional, params, atoms, *_, **__):
-    """functional.py:718-757: HF-Fock term from dE/d ehf (coefficient inputs); needs the chi tensor."""
-    if getattr(atoms, "chi", None) is None:
-        raise ValueError("Precomputed chi tensor has not been loaded.")
-    raise NotImplementedError("the chi-based HF Fock contributions are not part of the XC grid path")
+def dm21_hfgrads_cinputs(functional, params, atoms, ehf, cinputs_wout_hf, densities, omegas=(0.0, 0.4)):
+    """functional.py:718-757: the HF Fock term from dE/d ehf through the HF inputs, summed over omega."""
+    return atoms.HF_coefficient_input_grad_2_Fock(functional, params, omegas, ehf, cinputs_wout_hf,
+                                                  densities).sum(dim=0)
 
 
 class _NeuralXc(torch.autograd.Function):
@@ -266,6 +266,23 @@ class NeuralFunctional(Functional):
         rdm1 = atoms.rdm1 if isinstance(atoms.rdm1, torch.Tensor) and atoms.rdm1.requires_grad else atoms._rdm1()
         return _NeuralXcPair.apply(rdm1, flat, r, net, self._ehf(atoms))
 
+    def _hf_grads(self, params, atoms, ehf, clip_cte):
+        self._check_slots()
+        r = atoms.resident()
+        net = self.network(clip_cte)
+        if net.precision != "fp64":
+            raise NotImplementedError("the HF gradients of the network run in its FP64 form (precision='fp64')")
+        _, g_dens, g_cin = r.neural_xc_hf_grads(atoms._rdm1(), net, net.flatten(params, r.device), ehf)
+        return g_dens, g_cin
+
+    def hf_density_gradient(self, params, atoms, ehf, clip_cte: float = CLIP):
+        """dE_xc/d ehf (2, 2, grid) through the HF energy-density columns (molecule.py:598-603)."""
+        return self._hf_grads(params, atoms, ehf, clip_cte)[0]
+
+    def hf_cinput_gradient(self, params, atoms, ehf, clip_cte: float = CLIP):
+        """dE_xc/d ehf (2, 2, grid) through the network's HF inputs (molecule.py:668-673)."""
+        return self._hf_grads(params, atoms, ehf, clip_cte)[1]
+
     def energy_xc_only(self, params, atoms, *args, **kwargs):
         """E_xc as a differentiable torch scalar in rdm1 and in the parameter tensors."""
         self._check_slots()
@@ -283,7 +300,7 @@ class DM21(NeuralFunctional):
     As in the reference, the default ``densitygrads`` / ``coefficient_input_grads``
     need the chi tensor (energy_predictor raises ValueError without it); pass
     ``densitygrads=None, coefficient_input_grads=None`` and stop-gradient
-    ``nograd_*`` inputs to use supplied HF energy densities.
+    ``nograd_*`` inputs to use supplied HF energy densities instead.
     """
 
     coefficients: Callable = None

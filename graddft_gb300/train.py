@@ -34,14 +34,22 @@ def energy_predictor(functional, nlc_functional=None, clip_cte: float = CLIP, **
             # train.py:165-213: the explicit HF terms, each added as F + F^T and clipped.
             grad_densities = functional.energy_densities(atoms) if functional.energy_densities is not None else None
             nograd_densities = functional.nograd_densities(atoms) if functional.nograd_densities else None
-            cinputs = functional.compute_coefficient_inputs(atoms)
+            densities = grad_densities
+            if grad_densities is not None and nograd_densities is not None:
+                densities = functional.combine_densities(grad_densities, nograd_densities)
+            grad_cinputs = functional.coefficient_inputs(atoms) if functional.coefficient_inputs else None
+            nograd_cinputs = (functional.nograd_coefficient_inputs(atoms)
+                              if functional.nograd_coefficient_inputs else None)
+            cinputs = grad_cinputs
+            if grad_cinputs is not None and nograd_cinputs is not None:
+                cinputs = functional.combine_inputs(grad_cinputs, nograd_cinputs)
             if functional.densitygrads is not None:
                 vxc_expl = functional.densitygrads(functional, params, atoms, nograd_densities, cinputs,
                                                    grad_densities)
                 fock = engine.fock_add_hf(fock, vxc_expl, clip_cte)
             if functional.coefficient_input_grads is not None:
-                vxc_expl = functional.coefficient_input_grads(functional, params, atoms, nograd_densities, cinputs,
-                                                              grad_densities)
+                vxc_expl = functional.coefficient_input_grads(functional, params, atoms, nograd_cinputs,
+                                                              grad_cinputs, densities)
                 fock = engine.fock_add_hf(fock, vxc_expl, clip_cte)
         return energy, fock
 

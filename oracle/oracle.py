@@ -29,7 +29,7 @@ __all__ = [
     "dm21_coefficient_inputs", "dm21_densities", "dm21_combine_cinputs", "dm21_combine_densities",
     "densities_generic", "dm21_network", "FUNCTIONALS", "energy_densities", "xc_energy",
     "xc_energy_and_grads", "xc_hvp", "predict_fock", "t64", "features_numpy", "FZETA_PP0",
-    "hf_energy_density", "hf_density_grad_2_fock", "b3lyp_predict_with_chi",
+    "hf_energy_density", "hf_density_grad_2_fock", "b3lyp_predict_with_chi", "dm21_hf_fock_terms",
 ]
 
 
@@ -540,6 +540,32 @@ def hf_density_grad_2_fock(name, rdm1, ao, grad_ao, grad2_ao, weights, chi, ehf,
     E = xc_energy(torch.tensor([coeffs], dtype=F64), dens, t64(weights), clip_cte)
     (gr,) = torch.autograd.grad(E, ehf_v)
     return -0.5 * torch.einsum("rwsb,wsr,ra->wsab", t64(chi), gr, t64(ao))
+
+
+def dm21_hf_fock_terms(rdm1, ao, grad_ao, grad2_ao, weights, params, chi, clip_cte=CLIP):
+    """dm21_hfgrads_densities and dm21_hfgrads_cinputs (functional.py:677-757), omegas 0 and 0.4.
+
+    (F_dens, F_cin), each (spin, n, n) summed over omega: the HF Fock terms
+    with dE/d ehf taken through the HF energy-density columns (the network's
+    inputs held) and through the HF inputs (the densities held), with the
+    local densities unclipped as predict passes them.
+    """
+    with torch.no_grad():
+        rho, grad_rho, _, tau = _features(t64(rdm1), t64(ao), t64(grad_ao), None if grad2_ao is None else t64(grad2_ao))
+        ehf = hf_energy_density(rdm1, ao, chi)
+        dens_wout = dm21_densities(rho, grad_rho, tau, "LDA", clip_cte)
+        cin_wout = dm21_coefficient_inputs(rho, grad_rho, tau, clip_cte)
+    w = t64(weights)
+    p = params["params"] if "params" in params else params
+    params = {"params": {k: {kk: t64(v) for kk, v in d.items()} for k, d in p.items()}}
+    e1 = ehf.clone().requires_grad_(True)
+    c1 = dm21_network(params, dm21_combine_cinputs(cin_wout, ehf)).detach()
+    (g_dens,) = torch.autograd.grad(xc_energy(c1, dm21_combine_densities(dens_wout, e1), w, clip_cte), e1)
+    e2 = ehf.clone().requires_grad_(True)
+    c2 = dm21_network(params, dm21_combine_cinputs(cin_wout, e2))
+    (g_cin,) = torch.autograd.grad(xc_energy(c2, dm21_combine_densities(dens_wout, ehf), w, clip_cte), e2)
+    fock = lambda g: -0.5 * torch.einsum("rwsb,wsr,ra->sab", t64(chi), g, t64(ao))  # noqa: E731
+    return fock(g_dens), fock(g_cin)
 
 
 def b3lyp_predict_with_chi(rdm1, ao, grad_ao, grad2_ao, weights, h1e, eri, chi, omegas, nuclear_repulsion,

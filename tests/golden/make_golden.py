@@ -209,6 +209,23 @@ def main(root):
     ehf0 = mol.HF_energy_density([0.0]).detach()
     vexpl = pop.b3lyp_hfgrads(pop.B3LYP, params, mol, ehf0, None, pop.b3lyp_exhf_densities(mol))
     res["b3lyp_hfgrads"] = vexpl.detach().numpy()
+    # DM21 with its default slots: HF inputs and densities from chi, and both
+    # HF Fock terms (functional.py:677-785) in predict.
+    dm21 = fun.DM21()
+    np_params = synthetic.glorot_params(seed=7)
+    params = {"params": {k: {kk: torch.as_tensor(vv) for kk, vv in v.items()} for k, v in np_params["params"].items()}}
+    E, F = ref.train.energy_predictor(dm21)(params, mol)
+    res["predict_E_DM21"] = E.detach().numpy()
+    res["predict_F_DM21"] = F.detach().numpy()
+    with torch.no_grad():
+        ehf = mol.HF_energy_density(jnp.array([0.0, 0.4]))
+        dens_wout = dm21.energy_densities(mol)
+        cin_wout = dm21.coefficient_inputs(mol)
+    cin = dm21.combine_inputs(cin_wout, ehf)
+    dens = dm21.combine_densities(dens_wout, ehf)
+    res["dm21_hfgrads_densities"] = fun.dm21_hfgrads_densities(dm21, params, mol, ehf, cin, dens_wout).detach().numpy()
+    res["dm21_hfgrads_cinputs"] = fun.dm21_hfgrads_cinputs(dm21, params, mol, ehf, cin_wout, dens).detach().numpy()
+    res["theta_seed"] = np.array(7)
     path = os.path.join(HERE, "ref_hf.npz")
     np.savez_compressed(path, **res)
     out_files.append(path)

@@ -1,9 +1,10 @@
 """GPU parity of the exact-exchange (HF) terms computed from a chi tensor.
 
-HF_energy_density (molecule.py:507-541), the HF Fock term of B3LYP
+HF_energy_density (molecule.py:507-541), the HF Fock terms of B3LYP
 (HF_density_grad_2_Fock, molecule.py:545-613, summed over omega by
-b3lyp_hfgrads) and energy_predictor(B3LYP) with those terms (train.py:124-218)
-against fixtures made by running the reference's own source
+b3lyp_hfgrads) and of DM21 (dm21_hfgrads_densities / dm21_hfgrads_cinputs,
+functional.py:677-757), and energy_predictor with those terms
+(train.py:124-218) against fixtures made by running the reference's own source
 (tests/golden/make_golden.py), and the general-omega Fock contraction against
 the oracle.  All FP64: the bar is 1e-11 relative to the largest entry.
 """
@@ -102,3 +103,24 @@ def test_hf_errors(G, golden):
     no_chi = mol.replace(chi=None)
     with pytest.raises(ValueError):
         no_chi.HF_energy_density([0.0])
+
+
+def test_dm21_hf_terms(G, golden):
+    g = golden("hf")
+    mol = _molecule(G, g)
+    dm21 = G.DM21()
+    params = synthetic.glorot_params(seed=int(g["theta_seed"]))
+    ehf = mol.HF_energy_density([0.0, 0.4])
+    fd = G.neural.dm21_hfgrads_densities(dm21, params, mol, ehf, None, None)
+    fc = G.neural.dm21_hfgrads_cinputs(dm21, params, mol, ehf, None, None)
+    _close(fd, g["dm21_hfgrads_densities"], what="HF term through the densities")
+    _close(fc, g["dm21_hfgrads_cinputs"], what="HF term through the inputs")
+
+
+def test_dm21_predict_with_chi(G, golden):
+    g = golden("hf")
+    mol = _molecule(G, g)
+    params = synthetic.glorot_params(seed=int(g["theta_seed"]))
+    E, F = G.energy_predictor(G.DM21())(params, mol)
+    assert abs(float(E) - float(g["predict_E_DM21"])) <= RTOL * abs(float(g["predict_E_DM21"]))
+    _close(F, g["predict_F_DM21"], what="F")

@@ -156,3 +156,12 @@ def test_hf_exact_exchange_vs_reference(golden):
                                     g["eri"], g["chi"], g["omegas"], 1.25)
     assert abs(E - float(g["predict_E_B3LYP"])) <= 1e-12 * abs(float(g["predict_E_B3LYP"]))
     _close(F, g["predict_F_B3LYP"])
+
+
+def test_dm21_hf_terms_vs_reference(golden):
+    """dm21_hfgrads_densities / dm21_hfgrads_cinputs with a chi tensor (reference fixtures)."""
+    g = golden("hf")
+    params = synthetic.glorot_params(seed=int(g["theta_seed"]))
+    fd, fc = O.dm21_hf_fock_terms(g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"], params, g["chi"])
+    _close(fd.numpy(), g["dm21_hfgrads_densities"])
+    _close(fc.numpy(), g["dm21_hfgrads_cinputs"])
