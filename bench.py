@@ -517,6 +517,74 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_hf(args):
+    """DM21 energy_predictor with its exact-exchange terms from a chi tensor: grid-pts/s of (E, Fock)."""
+    import time
+
+    import torch
+
+    import graddft_gb300 as G
+    import oracle as O
+    from graddft_gb300 import build, synthetic
+
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    n_grid = args.n_grid if args.n_grid != N_GRID else 1 << 17
+    n_ao = args.n_ao if args.n_ao != N_AO else 128
+    wl = synthetic.make_workload(n_grid, n_ao, max(1, n_ao // 8), SEED)
+    t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64, device=dev)  # noqa: E731
+    r = G.engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "fp64", dev)
+    ao = r.ao_planes()[0, :n_grid, :n_ao].contiguous()  # phi as evaluated on the device
+    chi = synthetic.make_chi(ao.cpu().numpy(), wl.rdm1, n_omega=2, seed=SEED)
+    rng = np.random.default_rng(SEED)
+    h = rng.standard_normal((n_ao, n_ao))
+    eri = rng.standard_normal((n_ao, n_ao, n_ao, n_ao)) * (0.01 / n_ao)
+    mol = G.Molecule(grid=G.Grid(coords=None, weights=t(wl.weights)), atom_index=None, nuclear_pos=None, ao=ao,
+                     grad_ao=None, grad_n_ao=None, rdm1=t(wl.rdm1), nuclear_repulsion=1.0, h1e=t(0.5 * (h + h.T)),
+                     vj=None, mo_coeff=None, mo_occ=None, mo_energy=None, rep_tensor=t(eri), omegas=[0.0, 0.4],
+                     chi=t(chi), _resident=r)
+    params = synthetic.glorot_params(seed=SEED)
+    predict = G.energy_predictor(G.DM21())
+    for _ in range(max(1, args.warmup)):
+        predict(params, mol)
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 5))
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            E, F = predict(params, mol)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    line = {
+        "metric": "DM21 predict with exact-exchange terms from chi, grid-pts/s (E, Fock)", "value": n_grid / (ms * 1e-3),
+        "unit": "grid-pts/s", "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded basis, rdm1, stand-in chi tensor, random symmetric h1e and eri)",
+        "config": {"workload": f"DM21 energy_predictor with chi: n_ao {n_ao}, n_grid {n_grid}, omegas (0, 0.4)",
+                   "n_ao": n_ao, "n_grid": n_grid, "network": "DM21 6 x 256, FP64 form",
+                   "l2": "inputs larger than L2 (chi %.2f GiB)" % (chi.nbytes / 2**30)},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        n_s = min(args.cpu_sample, 2048)
+        sl = slice(0, n_s)
+        g1 = O.eval_ao_planes(wl.basis, wl.coords[sl])
+        torch.set_num_threads(os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        O.xc_energy_and_grads("DM21", wl.rdm1, g1[0], g1[1], g1[2], wl.weights[sl], params=params,
+                              ehf=O.hf_energy_density(wl.rdm1, g1[0], chi[sl]))
+        O.dm21_hf_fock_terms(wl.rdm1, g1[0], g1[1], g1[2], wl.weights[sl], params, chi[sl])
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_s / dt, "unit": "grid-pts/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{n_s} grid points of the same workload ({dt:.1f} s), FP64 torch-CPU "
+                                          "restatement of E_xc, V_xc and both HF Fock terms"}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -531,9 +599,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
-    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch"],
+    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch", "hf"],
                     help="xc: B88+LYP contraction benchmark (headline); neural: DM21-style network fwd+bwd; "
-                         "scf: differentiable SCF loop; batch: many molecules per step")
+                         "scf: differentiable SCF loop; batch: many molecules per step; hf: DM21 predict with "
+                         "its exact-exchange terms from a chi tensor")
     ap.add_argument("--n-mol", type=int, default=64, help="molecules (--workload batch)")
     ap.add_argument("--points-per-ao", type=int, default=150, help="grid points per AO (--workload batch)")
     ap.add_argument("--cycles", type=int, default=20, help="SCF iterations (--workload scf)")
@@ -546,6 +615,8 @@ def main():
         return run_scf(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "hf":
+        return run_hf(args)
 
     import torch
 

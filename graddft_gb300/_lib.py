@@ -105,7 +105,7 @@ _SIGS = {
     "gdft_hf_energy_density": ([P, P, P, I64, I32, I32, P, P, SZ, P], ctypes.c_int),
     "gdft_hf_fock": ([P, P, P, I64, I32, I32, P, P, SZ, P], ctypes.c_int),
     "gdft_fock_add_hf": ([P, P, I32, D, P], ctypes.c_int),
-    "gdft_neural_xc_hf_grads": ([PMOL, P, PNET, P, P, P, P, P, P, SZ, P], ctypes.c_int),
+    "gdft_neural_xc_hf_grads": ([PMOL, P, PNET, P, P, P, P, P, P, P, SZ, P], ctypes.c_int),
     "gdft_energy_densities": ([PMOL, P, PFN, P, I32, P, P, SZ, P], ctypes.c_int),
     "gdft_vxc_from_potentials": ([PMOL, P, P, P, SZ, P], ctypes.c_int),
     "gdft_integrate": ([I64, I32, P, I32, P, P, D, P, P, SZ, P], ctypes.c_int),

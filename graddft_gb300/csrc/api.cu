@@ -625,8 +625,8 @@ int gdft_neural_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rd
 }
 
 int gdft_neural_xc_hf_grads(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net,
-                            const double *d_params, const double *d_ehf, double *d_exc, double *d_g_dens,
-                            double *d_g_cin, void *d_ws, size_t ws_bytes, void *stream) {
+                            const double *d_params, const double *d_ehf, double *d_exc, double *d_vxc,
+                            double *d_g_dens, double *d_g_cin, void *d_ws, size_t ws_bytes, void *stream) {
   int rc = check_mol(mol);
   if (rc) return rc;
   if ((rc = check_network(net))) return rc;
@@ -665,8 +665,11 @@ int gdft_neural_xc_hf_grads(const gdft_molecule *mol, const double *d_rdm1, cons
                           net->clip, mws, d_exc, coef, st)))
       return rc;
   }
-  return check_cuda(launch_dm21_hf_grads(net_shape(net), mol->n_grid, mol->n_grid_pad, mws, d_g_dens, d_g_cin, st),
-                    "dm21_hf_grads");
+  if ((rc = check_cuda(launch_dm21_hf_grads(net_shape(net), mol->n_grid, mol->n_grid_pad, mws, d_g_dens, d_g_cin, st),
+                       "dm21_hf_grads")))
+    return rc;
+  if (d_vxc == nullptr) return GDFT_OK;
+  return run_vxc(mol, coef, d_vxc, ws, st);
 }
 
 int gdft_neural_inputs(const gdft_molecule *mol, const double *d_rdm1, const gdft_network *net, const double *d_ehf,

@@ -105,6 +105,14 @@ class Resident:
         torch.cuda.current_stream(dev).synchronize()
         return r
 
+    def ao_planes(self) -> torch.Tensor:
+        """The FP64 form's resident tables as a (5, n_grid_pad, ld) view: phi, d_x, d_y, d_z, lap phi."""
+        if self.precision != "fp64":
+            raise ValueError("the resident tables are FP64 planes only in the FP64 form")
+        np_, ld = int(self.desc.n_grid_pad), int(self.desc.ld)
+        off = (np_ * 8 + 255) // 256 * 256  # after the weights
+        return self.buffer[off:off + 5 * np_ * ld * 8].view(torch.float64).view(5, np_, ld)
+
     # ------------------------------------------------------------------ calls
     def density(self, rdm1, want=("rho", "grad_rho", "lapl", "tau")):
         rdm1 = self._rdm1(rdm1)
@@ -187,8 +195,9 @@ class Resident:
             _ptr(vxc), _ptr(dp), _ptr(ws), ws.numel(), _stream(self.device)))
         return exc, vxc, dp
 
-    def neural_xc_hf_grads(self, rdm1, net: "Network", flat_params, ehf):
-        """(E_xc, g_dens, g_cin): dE_xc/d ehf (2, 2, grid) through the HF densities and through the HF inputs."""
+    def neural_xc_hf_grads(self, rdm1, net: "Network", flat_params, ehf, want_vxc=False):
+        """(E_xc, V_xc or None, g_dens, g_cin) in one network pass: g = dE_xc/d ehf (2, 2, grid) through the
+        HF densities and through the HF inputs."""
         rdm1 = self._rdm1(rdm1)
         ehf_t = as_device_f64(ehf, self.device)
         if ehf_t is None or ehf_t.shape != (2, 2, self.n_grid):
@@ -198,10 +207,12 @@ class Resident:
         exc = torch.empty((), dtype=F64, device=self.device)
         g_dens = torch.empty((2, 2, self.n_grid), dtype=F64, device=self.device)
         g_cin = torch.empty((2, 2, self.n_grid), dtype=F64, device=self.device)
+        vxc = torch.empty((2, self.n_ao, self.n_ao), dtype=F64, device=self.device) if want_vxc else None
         check(_lib.load().gdft_neural_xc_hf_grads(ctypes.byref(self.desc), _ptr(rdm1), ctypes.byref(net.desc),
-                                                  _ptr(flat), _ptr(ehf_t.contiguous()), _ptr(exc), _ptr(g_dens),
-                                                  _ptr(g_cin), _ptr(ws), ws.numel(), _stream(self.device)))
-        return exc, g_dens, g_cin
+                                                  _ptr(flat), _ptr(ehf_t.contiguous()), _ptr(exc), _ptr(vxc),
+                                                  _ptr(g_dens), _ptr(g_cin), _ptr(ws), ws.numel(),
+                                                  _stream(self.device)))
+        return exc, vxc, g_dens, g_cin
 
     def neural_xc_hvp(self, rdm1, net: "Network", flat_params, ehf, tangent, want_value=False, want_drdm1=True,
                       want_dparams=True):

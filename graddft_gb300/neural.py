@@ -17,6 +17,7 @@ from the network's dE/d ehf (FP64 network form).
 from __future__ import annotations
 
 import ctypes
+import weakref
 from dataclasses import dataclass, field
 from typing import Any, Callable, Optional
 
@@ -238,7 +239,20 @@ class NeuralFunctional(Functional):
         return torch.dot(w, e)
 
     def xc_energy_and_grads(self, params, atoms, clip_cte: float = CLIP):
-        """(E_xc, dE_xc/d rdm1) (train.py:86-121)."""
+        """(E_xc, dE_xc/d rdm1) (train.py:86-121).
+
+        With a chi tensor on the molecule and HF Fock terms to come (densitygrads /
+        coefficient_input_grads), the same network pass also makes dE/d ehf for them.
+        """
+        hf_terms = self.densitygrads is not None or self.coefficient_input_grads is not None
+        if hf_terms and getattr(atoms, "chi", None) is not None and self.precision == "fp64":
+            self._check_slots()
+            r = atoms.resident()
+            net = self.network(clip_cte)
+            e, v, g_dens, g_cin = r.neural_xc_hf_grads(atoms._rdm1(), net, net.flatten(params, r.device),
+                                                       self._ehf(atoms), want_vxc=True)
+            self.__dict__["_hf_cache"] = (self._hf_key(params, atoms, clip_cte), (g_dens, g_cin))
+            return e, v
         e, v, _ = self.xc_energy_and_grads_params(params, atoms, clip_cte, want_dparams=False)
         return e, v
 
@@ -266,13 +280,34 @@ class NeuralFunctional(Functional):
         rdm1 = atoms.rdm1 if isinstance(atoms.rdm1, torch.Tensor) and atoms.rdm1.requires_grad else atoms._rdm1()
         return _NeuralXcPair.apply(rdm1, flat, r, net, self._ehf(atoms))
 
+    @staticmethod
+    def _hf_key(params, atoms, clip_cte):
+        rdm1 = atoms.rdm1
+        ver = (rdm1.data_ptr(), rdm1._version) if isinstance(rdm1, torch.Tensor) else None
+        return (weakref.ref(atoms), params, rdm1, ver, clip_cte)
+
+    def _hf_cached(self, params, atoms, clip_cte):
+        cached = self.__dict__.get("_hf_cache")
+        if cached is None:
+            return None
+        (ref, p, rdm1, ver, clip), grads = cached
+        now = self._hf_key(params, atoms, clip_cte)
+        if ref() is atoms and p is params and rdm1 is atoms.rdm1 and ver == now[3] and clip == clip_cte:
+            return grads
+        return None
+
     def _hf_grads(self, params, atoms, ehf, clip_cte):
+        """(g_dens, g_cin), reused from the xc pass of the same predict when it already made them."""
         self._check_slots()
+        cached = self._hf_cached(params, atoms, clip_cte)
+        if cached is not None:
+            return cached
         r = atoms.resident()
         net = self.network(clip_cte)
         if net.precision != "fp64":
             raise NotImplementedError("the HF gradients of the network run in its FP64 form (precision='fp64')")
-        _, g_dens, g_cin = r.neural_xc_hf_grads(atoms._rdm1(), net, net.flatten(params, r.device), ehf)
+        _, _, g_dens, g_cin = r.neural_xc_hf_grads(atoms._rdm1(), net, net.flatten(params, r.device), ehf)
+        self.__dict__["_hf_cache"] = (self._hf_key(params, atoms, clip_cte), (g_dens, g_cin))
         return g_dens, g_cin
 
     def hf_density_gradient(self, params, atoms, ehf, clip_cte: float = CLIP):
