@@ -357,7 +357,9 @@ def run_scf(args):
         f = G.DM21(densitygrads=None, coefficient_input_grads=None, nograd_densities=hf,
                    nograd_coefficient_inputs=hf, precision=prec)
         leaves = {k: {kk: t(v).requires_grad_(True) for kk, v in d.items()} for k, d in params["params"].items()}
-        out = G.diff_simple_scf_loop(f, cycles=cycles, mixing_factor=mix)({"params": leaves}, mol)
+        loop = (G.diff_scf_loop(f, cycles=cycles) if args.loop == "diis"
+                else G.diff_simple_scf_loop(f, cycles=cycles, mixing_factor=mix))
+        out = loop({"params": leaves}, mol)
         out.energy.backward()
         return float(out.energy.detach()), leaves
 
@@ -380,9 +382,11 @@ def run_scf(args):
         "unit": "loops/s", "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup // 3), "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3",
         "data": "synthetic (seeded basis, H, S, density-fitting tensor)",
-        "config": {"workload": SCF_WORKLOAD if (n_grid, n_ao, cycles) == (1 << 19, 256, 20) else
-                   f"differentiable SCF loop, n_ao {n_ao}, n_grid {n_grid}, {cycles} iterations",
-                   "n_ao": n_ao, "n_grid": n_grid, "cycles": cycles, "mixing": mix, "naux": 768,
+        "config": {"workload": (SCF_WORKLOAD if (n_grid, n_ao, cycles, args.loop) == (1 << 19, 256, 20, "simple") else
+                                f"differentiable SCF loop ({'CDIIS' if args.loop == 'diis' else 'linear mixing'}), "
+                                f"n_ao {n_ao}, n_grid {n_grid}, {cycles} iterations"),
+                   "n_ao": n_ao, "n_grid": n_grid, "cycles": cycles, "loop": args.loop,
+                   "mixing": mix if args.loop == "simple" else None, "naux": 768,
                    "eigensolver": "FP64 generalized eigh (cuSOLVER through torch), Lorentzian-broadened reverse"},
         "grid_pts_per_s": n_grid * (cycles + 1) / (ms * 1e-3), "energy": e_tc, "clocks": clk.summary(),
     }
@@ -606,6 +610,8 @@ def main():
     ap.add_argument("--n-mol", type=int, default=64, help="molecules (--workload batch)")
     ap.add_argument("--points-per-ao", type=int, default=150, help="grid points per AO (--workload batch)")
     ap.add_argument("--cycles", type=int, default=20, help="SCF iterations (--workload scf)")
+    ap.add_argument("--loop", default="simple", choices=["simple", "diis"],
+                    help="--workload scf: linear density mixing (diff_simple_scf_loop) or CDIIS (diff_scf_loop)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

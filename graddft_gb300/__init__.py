@@ -31,7 +31,7 @@ from .popular_functionals import (
     vwn_density,
 )
 from .train import energy_predictor
-from .scf import diff_simple_scf_loop, safe_eigh, safe_fock_solver, safe_general_eigh
+from .scf import JittableDiis, diff_scf_loop, diff_simple_scf_loop, safe_eigh, safe_fock_solver, safe_general_eigh
 from .neural import DM21, NeuralFunctional, dm21_coefficient_inputs, dm21_hfgrads_cinputs, dm21_hfgrads_densities
 
 __all__ = [
@@ -40,5 +40,6 @@ __all__ = [
     "stack_densities", "B3LYP", "B88", "BLYP", "LSDA", "LYP", "PW92", "VWN", "b3lyp_combine",
     "b3lyp_exhf_densities", "b88_density", "lsda_density", "lyp_density", "pw92_densities", "vwn_density",
     "energy_predictor", "DM21", "NeuralFunctional", "dm21_coefficient_inputs", "dm21_hfgrads_cinputs",
-    "dm21_hfgrads_densities", "diff_simple_scf_loop", "safe_eigh", "safe_fock_solver", "safe_general_eigh",
+    "dm21_hfgrads_densities", "diff_simple_scf_loop", "diff_scf_loop", "JittableDiis", "safe_eigh",
+    "safe_fock_solver", "safe_general_eigh",
 ]

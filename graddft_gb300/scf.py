@@ -1,10 +1,11 @@
-"""Differentiable SCF loop on the GPU (evaluate.py:256-344) with the safe eigensolver.
+"""Differentiable SCF loops on the GPU (evaluate.py:256-344 and 917-1210) with the safe eigensolver.
 
-Mirrors ``diff_simple_scf_loop``: an initial energy/Fock evaluation, then
-``cycles`` iterations of generalized eigh of the Fock matrix, aufbau
-occupations, the density matrix, linear mixing and a new energy/Fock
-evaluation; the whole loop is differentiable.  The pieces follow the
-reference:
+``diff_simple_scf_loop``: an initial energy/Fock evaluation, then ``cycles``
+iterations of generalized eigh of the Fock matrix, aufbau occupations, the
+density matrix, linear mixing and a new energy/Fock evaluation.
+``diff_scf_loop``: the same with the Fock matrix extrapolated by CDIIS
+(``JittableDiis``) instead of density mixing.  Both are differentiable end to
+end.  The pieces follow the reference:
 
 * ``safe_eigh`` / ``safe_general_eigh`` / ``safe_fock_solver``:
   utils/eigenproblem.py:26-149, including the Lorentzian-broadened reverse rule
@@ -134,20 +135,25 @@ def orbital_grad(mo_coeff, mo_occ, fock):
     return torch.cat(out)
 
 
+def _to_device(atoms):
+    dev = atoms.resident().device
+    t = lambda x: x if isinstance(x, torch.Tensor) and x.device == dev else torch.as_tensor(x, dtype=F64, device=dev)  # noqa: E731
+    atoms = atoms.replace(rdm1=t(atoms.rdm1), h1e=t(atoms.h1e), s1e=t(atoms.s1e),
+                          nuclear_repulsion=t(atoms.nuclear_repulsion), mo_occ=t(atoms.mo_occ))
+    if getattr(atoms, "df_tensor", None) is not None:
+        return atoms.replace(df_tensor=t(atoms.df_tensor))
+    if atoms.rep_tensor is not None:
+        return atoms.replace(rep_tensor=t(atoms.rep_tensor))
+    return atoms
+
+
 def diff_simple_scf_loop(functional, cycles: int = 25, mixing_factor: float = 0.4,
                          clip_cte: float = CLIP) -> Callable:
     """evaluate.py:256-344: returns ``iterator(params, atoms) -> atoms`` with the final
     rdm1, fock, energy, mo_coeff, mo_energy and mo_occ."""
 
     def iterator(params, atoms, *args):
-        dev = atoms.resident().device
-        t = lambda x: x if isinstance(x, torch.Tensor) and x.device == dev else torch.as_tensor(x, dtype=F64, device=dev)  # noqa: E731
-        atoms = atoms.replace(rdm1=t(atoms.rdm1), h1e=t(atoms.h1e), s1e=t(atoms.s1e),
-                              nuclear_repulsion=t(atoms.nuclear_repulsion), mo_occ=t(atoms.mo_occ))
-        if getattr(atoms, "df_tensor", None) is not None:
-            atoms = atoms.replace(df_tensor=t(atoms.df_tensor))
-        elif atoms.rep_tensor is not None:
-            atoms = atoms.replace(rep_tensor=t(atoms.rep_tensor))
+        atoms = _to_device(atoms)
         nelecs = [int(round(float(atoms.mo_occ[s].sum()))) for s in range(2)]
         energy, fock = energy_and_fock(functional, params, atoms, clip_cte)
         atoms = atoms.replace(fock=fock, energy=energy)
@@ -160,5 +166,88 @@ def diff_simple_scf_loop(functional, cycles: int = 25, mixing_factor: float = 0.
             energy, fock = energy_and_fock(functional, params, atoms, clip_cte)
             atoms = atoms.replace(fock=fock, energy=energy)
         return atoms
+
+    return iterator
+
+
+class JittableDiis:
+    """evaluate.py:1041-1210: CDIIS over a fixed history of ``max_diis`` entries, differentiable.
+
+    F_DIIS = A^T (sum_i x_i F_i) A with x from the bordered system of the
+    error inner products, e_i = A F_i D_i S A^T - (...)^T.  The history keeps
+    the reference's indexing: entries are written at position ``cycle`` while
+    cycle < max_diis, the one at cycle == max_diis is dropped (its scatter is
+    out of bounds), and later ones shift the history by one.
+    """
+
+    def __init__(self, overlap_matrix, A, max_diis: int = 8):
+        self.S, self.A, self.max_diis = overlap_matrix, A, int(max_diis)
+
+    def empty(self, n_ao, like):
+        z = lambda *shape: torch.zeros(shape, dtype=like.dtype, device=like.device)  # noqa: E731
+        m = self.max_diis
+        return z(m, 2, n_ao, n_ao), z(m, 2, n_ao, n_ao), z(m), z(m, 2, n_ao, n_ao)
+
+    def _push(self, vec, x, cycle):
+        if cycle > self.max_diis:
+            return torch.cat((vec, x[None]), dim=0)[1:]
+        if cycle < self.max_diis:
+            return torch.cat((vec[:cycle], x[None], vec[cycle + 1:]), dim=0)
+        return vec
+
+    def update(self, new_data, diis_data, cycle):
+        density, fock, energy = new_data
+        dv, fv, ev, errv = diis_data
+        fds = torch.einsum("ij,sjk,skl,lm,mn->sin", self.A, fock, density, self.S, self.A.T)
+        err = fds - fds.transpose(1, 2)
+        return (self._push(dv, density, cycle), self._push(fv, fock, cycle),
+                self._push(ev, energy.reshape(()).to(ev.dtype), cycle), self._push(errv, err, cycle))
+
+    def cdiis_minimize(self, error_vector, cycle):
+        n = error_vector.shape[0]
+        inner = torch.einsum("iskl,jskl->sij", error_vector, error_vector)
+        used = (torch.arange(n, device=inner.device) <= cycle).to(inner.dtype)
+        diag = torch.where(used > 0, torch.diagonal(inner, dim1=1, dim2=2), torch.ones_like(used))
+        core = inner - torch.diag_embed(torch.diagonal(inner, dim1=1, dim2=2)) + torch.diag_embed(diag)
+        border = used.expand(2, n)
+        top = torch.cat((torch.zeros(2, 1, dtype=inner.dtype, device=inner.device), border), dim=1)
+        B = torch.cat((top[:, None, :], torch.cat((border[:, :, None], core), dim=2)), dim=1)
+        C = torch.zeros(n + 1, dtype=inner.dtype, device=inner.device)
+        C[0] = 1.0
+        x = torch.stack([torch.linalg.inv(B[s]) @ C for s in range(2)], dim=0)
+        return x[:, 1:]
+
+    def run(self, new_data, diis_data, cycle=0):
+        diis_data = self.update(new_data, diis_data, cycle)
+        _, fock_vector, _, error_vector = diis_data
+        x = self.cdiis_minimize(error_vector, cycle)
+        F = torch.einsum("si,isjk->sjk", x, fock_vector)
+        return torch.einsum("ji,sjk,kl->sil", self.A, F, self.A), diis_data
+
+
+def diff_scf_loop(functional, cycles: int = 25, clip_cte: float = CLIP, max_diis: int = 10) -> Callable:
+    """evaluate.py:917-1038: ``iterator(params, atoms) -> atoms`` with CDIIS extrapolation of the
+    Fock matrix (A = identity), the final rdm1, fock, energy, mo_coeff, mo_energy and mo_occ."""
+
+    def iterator(params, atoms, *args):
+        atoms = _to_device(atoms)
+        nelecs = [int(round(float(atoms.mo_occ[s].sum()))) for s in range(2)]
+        energy, fock = energy_and_fock(functional, params, atoms, clip_cte)
+        atoms = atoms.replace(fock=fock)
+        n = fock.shape[-1]
+        A = torch.eye(n, dtype=F64, device=fock.device)
+        diis = JittableDiis(atoms.s1e, A, max_diis)
+        diis_data = diis.empty(n, fock)
+        for cycle in range(cycles):
+            fock, diis_data = diis.run((atoms.rdm1, atoms.fock, energy), diis_data, cycle)
+            mo_energy, mo_coeff = safe_fock_solver(fock, atoms.s1e)
+            mo_occ = get_occ(mo_energy, nelecs)
+            atoms = atoms.replace(fock=fock, mo_energy=mo_energy, mo_coeff=mo_coeff, mo_occ=mo_occ,
+                                  rdm1=make_rdm1(mo_coeff, mo_occ))
+            energy, fock = energy_and_fock(functional, params, atoms, clip_cte)
+            atoms = atoms.replace(fock=fock)
+        # The reference then runs one more iteration without DIIS history and
+        # discards it (evaluate.py:1022-1031); the state it returns is this one.
+        return atoms.replace(energy=energy)
 
     return iterator

@@ -52,20 +52,57 @@ def _axis(axis):
     return tuple(axis) if isinstance(axis, (list, tuple)) else axis
 
 
+class _DType:
+    """A jnp scalar type: usable as a dtype and callable (jnp.int64(x))."""
+
+    def __init__(self, dt):
+        self.torch = dt
+
+    def __call__(self, x):
+        return torch.as_tensor(x).to(self.torch)
+
+
+def _dt(d):
+    return d.torch if isinstance(d, _DType) else d
+
+
+class _At:
+    """x.at[idx].set(v) as a copy; updates at out-of-bounds indices are dropped, as JAX drops them."""
+
+    def __init__(self, t):
+        self.t = t
+
+    def __getitem__(self, idx):
+        t = self.t
+
+        class _Set:
+            @staticmethod
+            def set(v):
+                out = t.clone()
+                try:
+                    out[idx] = _t(v).to(out.dtype) if isinstance(v, torch.Tensor) else v
+                except IndexError:
+                    pass
+                return out
+
+        return _Set()
+
+
 def _mk_jnp():
     m = types.ModuleType("jax.numpy")
     m.pi = math.pi
+    m.inf = math.inf
     m.float64 = F64
     m.float32 = torch.float32
-    m.int64 = torch.int64
-    m.int32 = torch.int32
+    m.int64 = _DType(torch.int64)
+    m.int32 = _DType(torch.int32)
     m.ndarray = torch.Tensor
 
     def array(x, dtype=None):
         t = _t(x) if not isinstance(x, (list, tuple)) or not any(isinstance(e, torch.Tensor) for e in x) \
             else torch.stack([_t(e) for e in x])
         if dtype is not None:
-            t = t.to(dtype)
+            t = t.to(_dt(dtype))
         elif t.is_floating_point():
             t = t.to(F64)
         return t
@@ -130,11 +167,19 @@ def _mk_jnp():
         return torch.round(x * factor) / factor
 
     m.round = _round
-    m.empty = lambda shape, dtype=F64: torch.empty(shape, dtype=dtype if dtype is not None else F64)
-    m.zeros = lambda shape, dtype=F64: torch.zeros(shape, dtype=dtype if dtype is not None else F64)
-    m.ones = lambda shape, dtype=F64: torch.ones(shape, dtype=dtype if dtype is not None else F64)
+    m.empty = lambda shape, dtype=F64: torch.empty(shape, dtype=_dt(dtype) if dtype is not None else F64)
+    m.zeros = lambda shape, dtype=F64: torch.zeros(shape, dtype=_dt(dtype) if dtype is not None else F64)
+    m.ones = lambda shape, dtype=F64: torch.ones(shape, dtype=_dt(dtype) if dtype is not None else F64)
     m.zeros_like = lambda x: torch.zeros_like(_t(x))
-    m.identity = lambda n, dtype=F64: torch.eye(n, dtype=dtype)
+    m.identity = lambda n, dtype=F64: torch.eye(n, dtype=_dt(dtype))
+    m.diag = lambda x: torch.diag(_t(x))
+    m.diag_indices_from = lambda x: (torch.arange(_t(x).shape[0]), torch.arange(_t(x).shape[0]))
+    m.divide = lambda a, b: torch.div(_t(a), _t(b))
+    m.multiply = lambda a, b: torch.mul(_t(a), _t(b))
+    m.nan_to_num = lambda x: torch.nan_to_num(_t(x))
+    m.moveaxis = lambda x, a, b: torch.movedim(_t(x), a, b)
+    m.less_equal = lambda a, b: torch.less_equal(_t(a), _t(b))
+    m.vectorize = lambda f, signature=None: f  # called on single matrices here
     m.dot = lambda a, b, precision=None: _t(a) @ _t(b)
     m.tensordot = lambda a, b, axes=2, precision=None: torch.tensordot(_t(a), _t(b), dims=axes)
     m.reshape = lambda x, shape: torch.reshape(_t(x), shape)
@@ -300,6 +345,38 @@ class _Sub:
         return typing.Any
 
 
+class _CustomVjp:
+    """jax.custom_vjp: the primal runs as is; with defvjp, a torch.autograd.Function calls bwd(res, g)."""
+
+    def __init__(self, f):
+        self.f, self.fwd, self.bwd = f, None, None
+
+    def defvjp(self, fwd, bwd):
+        self.fwd, self.bwd = fwd, bwd
+
+    def __call__(self, *args):
+        tensors = [a for a in args if isinstance(a, torch.Tensor)]
+        if self.fwd is None or not torch.is_grad_enabled() or not any(t.requires_grad for t in tensors):
+            return self.f(*args)
+        outer = self
+
+        class _Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, *a):
+                out, res = outer.fwd(*a)
+                ctx.res = res
+                return tuple(out) if isinstance(out, (tuple, list)) else out
+
+            @staticmethod
+            def backward(ctx, *gs):
+                ref = ctx.res[0] if isinstance(ctx.res, tuple) else None
+                gs = tuple(torch.zeros_like(r) if g is None else g
+                           for g, r in zip(gs, ref if isinstance(ref, tuple) else gs))
+                return outer.bwd(ctx.res, gs if len(gs) > 1 else gs[0])
+
+        return _Fn.apply(*args)
+
+
 def vmap(fun, in_axes=0, out_axes=0, **_):
     """jax.vmap for single-array outputs: a loop over the mapped axis, then a stack."""
 
@@ -315,8 +392,27 @@ def vmap(fun, in_axes=0, out_axes=0, **_):
     return wrapped
 
 
+_orig_getitem = torch.Tensor.__getitem__
+
+
+def _clamped_getitem(self, idx):
+    """Indexing that clamps out-of-bounds integer indices, as JAX's gathers do."""
+    try:
+        return _orig_getitem(self, idx)
+    except IndexError:
+        parts = idx if isinstance(idx, tuple) else (idx,)
+        if not all(isinstance(p, (int, slice)) for p in parts):
+            raise
+        fixed = tuple(min(max(p, -self.shape[d]), self.shape[d] - 1) if isinstance(p, int) else p
+                      for d, p in enumerate(parts))
+        return _orig_getitem(self, fixed)
+
+
 def install():
     """Register the stand-in modules (idempotent)."""
+    torch.Tensor.at = property(lambda self: _At(self))
+    torch.Tensor.__getitem__ = _clamped_getitem
+    torch.Tensor.astype = lambda self, dt: self.to(_dt(dt))
     if "jax" in sys.modules and getattr(sys.modules["jax"], "_is_graddft_shim", False):
         return
     jax = types.ModuleType("jax")
@@ -327,14 +423,19 @@ def install():
     lax.Precision = _Precision
     lax.stop_gradient = lambda x: _t(x).detach() if isinstance(x, torch.Tensor) else x
 
-    def fori_loop(lo, hi, body, init):
-        v = init
+    def fori_loop(lo, hi, body=None, init=None, body_fun=None, init_val=None):
+        body = body if body is not None else body_fun
+        v = init if init is not None else init_val
         for i in range(lo, hi):
             v = body(i, v)
         return v
 
     lax.fori_loop = fori_loop
-    lax.cond = lambda p, t, f, operand=None: t(operand) if bool(p) else f(operand)
+    def cond(p, t, f, *operands, operand=None):
+        args = operands if operands else (operand,)
+        return t(*args) if bool(p) else f(*args)
+
+    lax.cond = cond
     jax.lax = lax
     jax.grad = grad
     jax.value_and_grad = value_and_grad
@@ -347,7 +448,7 @@ def install():
     jax.jit = jit
 
     jax.vmap = vmap
-    jax.custom_vjp = lambda f: f
+    jax.custom_vjp = _CustomVjp
     jax.config = types.SimpleNamespace(x64_enabled=True, update=lambda *a, **k: None)
     prof = types.ModuleType("jax.profiler")
     prof.annotate_function = lambda f=None, name=None, **k: (f if f is not None else (lambda g: g))
@@ -475,3 +576,41 @@ def load_reference(root: str):
     train = run("train")
     pkg.energy_predictor = train.energy_predictor
     return types.SimpleNamespace(molecule=mol, functional=fun, popular=pop, train=train)
+
+
+def load_scf(root: str, ref):
+    """Execute utils/eigenproblem.py and evaluate.py (the SCF loops) on top of load_reference.
+
+    evaluate.py's PySCF-facing imports (interface/pyscf.py, scipy-style
+    optimizers) are not used by the differentiable loops and get stand-ins.
+    """
+    import importlib.util
+    import os
+
+    def run(name, fname):
+        spec = importlib.util.spec_from_file_location(name, os.path.join(root, "grad_dft", fname))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+        return mod
+
+    jsc = types.ModuleType("jax.scipy")
+    jsc.special = types.SimpleNamespace(erfc=torch.special.erfc)
+    jsc.optimize = types.SimpleNamespace(minimize=None)
+    sys.modules["jax.scipy"], sys.modules["jax.scipy.special"] = jsc, jsc.special
+    sys.modules["jax.scipy.optimize"] = jsc.optimize
+    sys.modules["jax"].scipy = jsc
+    iface = types.ModuleType("grad_dft.interface")
+    iface.__path__ = []
+    pys = types.ModuleType("grad_dft.interface.pyscf")
+    for n in ("generate_chi_tensor", "mol_from_Molecule", "process_mol"):
+        setattr(pys, n, None)
+    sys.modules["grad_dft.interface"], sys.modules["grad_dft.interface.pyscf"] = iface, pys
+    eig = run("grad_dft.utils.eigenproblem", "utils/eigenproblem.py")
+    utils = sys.modules["grad_dft.utils"]
+    utils.Optimizer = typing.Any
+    for n in ("safe_eigh", "safe_general_eigh", "safe_fock_solver"):
+        setattr(utils, n, getattr(eig, n))
+    ev = run("grad_dft.evaluate", "evaluate.py")
+    ref.eigenproblem, ref.evaluate = eig, ev
+    return ev

@@ -229,6 +229,54 @@ def main(root):
     path = os.path.join(HERE, "ref_hf.npz")
     np.savez_compressed(path, **res)
     out_files.append(path)
+    # diff_scf_loop (evaluate.py:917-1038) with JittableDiis (:1041-1210): the
+    # final energy, density matrix and dE/dtheta through all iterations, DM21
+    # with stop-gradient HF inputs, 12 cycles (past the 10-entry DIIS history).
+    ev = jaxshim.load_scf(root, ref)
+    wl, ao, g1, g2, _, _ = _inputs("dm21")
+    n = wl.n_ao
+    sysm = synthetic.make_scf_system(n, 3, naux=32, seed=17)
+    eri = np.einsum("Ppq,Prs->pqrs", sysm.df_tensor, sysm.df_tensor)
+    mol = _molecule(ref, wl, ao, g1, g2, sysm.h1e, eri)
+    tt = lambda x: torch.as_tensor(np.asarray(x), dtype=F64)  # noqa: E731
+    mol = mol.replace(rdm1=tt(sysm.rdm1), s1e=tt(sysm.s1e), mo_occ=tt(sysm.mo_occ),
+                      nuclear_repulsion=tt(sysm.nuclear_repulsion))
+    rho = np.einsum("sab,ra,rb->rs", sysm.rdm1, ao, ao)
+    ehf_t = torch.as_tensor(synthetic.make_ehf(wl.n_grid, 18, rho, n_omega=2))
+    dm21 = fun.DM21(densitygrads=None, coefficient_input_grads=None,
+                    nograd_densities=lambda atoms, *_, **__: ehf_t,
+                    nograd_coefficient_inputs=lambda atoms, *_, **__: ehf_t)
+    np_params = synthetic.glorot_params(seed=19)
+    params = {"params": {k: {kk: torch.as_tensor(vv) for kk, vv in v.items()} for k, v in np_params["params"].items()}}
+    cycles = 12
+    loop = ev.diff_scf_loop(dm21, cycles=cycles)
+    jax = sys.modules["jax"]
+    out = {}
+
+    def final_energy(p):
+        m = loop(p, mol)
+        out["mol"] = m
+        return m.energy
+
+    dtheta = jax.grad(final_energy)(params)
+    m = out["mol"]
+    res = dict(ao=ao, grad_ao=g1, grad2_ao=g2, weights=wl.weights, ehf=ehf_t.numpy(), h1e=sysm.h1e, s1e=sysm.s1e,
+               df_tensor=sysm.df_tensor, rdm1_init=sysm.rdm1, mo_occ=sysm.mo_occ,
+               nuclear_repulsion=np.array(sysm.nuclear_repulsion), theta_seed=np.array(19), cycles=np.array(cycles),
+               energy=m.energy.detach().numpy(), rdm1=m.rdm1.detach().numpy(), fock=m.fock.detach().numpy())
+    sel = np.random.default_rng(98)
+    for k, d in dtheta["params"].items():
+        for kk, g in d.items():
+            g = g.detach().numpy()
+            if g.size > 4096:
+                idx = np.sort(sel.choice(g.size, 2048, replace=False))
+                res[f"dtheta/{k}/{kk}/idx"] = idx
+                res[f"dtheta/{k}/{kk}"] = g.reshape(-1)[idx]
+            else:
+                res[f"dtheta/{k}/{kk}"] = g
+    path = os.path.join(HERE, "ref_scf_diis.npz")
+    np.savez_compressed(path, **res)
+    out_files.append(path)
     torch.Tensor.transpose = _orig_transpose
     for p in out_files:
         print(p, os.path.getsize(p))
