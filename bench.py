@@ -589,6 +589,101 @@ def run_hf(args):
     print(json.dumps(line))
 
 
+def contracted_basis(n_atoms: int, seed: int = SEED):
+    """A seeded contracted spherical basis: per atom s(6 prim) + 3 s, p(3 prim) + 2 p, 2 d, 1 f (30 AOs),
+    centres uniform in a 12 A box, exponents log-uniform (tight contracted primitives up to 5000 bohr^-2)."""
+    import math
+
+    from graddft_gb300 import basis as B
+    from graddft_gb300 import synthetic
+
+    g = synthetic.rng(seed, 20)
+    half = 0.5 * 12.0 / synthetic.BOHR2ANGSTROM
+    pattern = [(0, 6), (0, 1), (0, 1), (0, 1), (1, 3), (1, 1), (1, 1), (2, 1), (2, 1), (3, 1)]
+    shells = []
+    for _ in range(n_atoms):
+        centre = g.uniform(-half, half, 3)
+        for l, nprim in pattern:
+            top = 5000.0 if nprim > 1 else 20.0
+            e = np.sort(np.exp(g.uniform(math.log(0.1), math.log(top), nprim)))[::-1]
+            shells.append(B.Shell(centre, l, e, B.normalized_contraction(l, e, g.uniform(0.1, 1.0, (nprim, 1)))))
+    return B.ShellBasis(shells)
+
+
+def run_ao(args):
+    """AO evaluation from contracted shells into the resident tables (numint.eval_ao + ao_grads on the device)."""
+    import ctypes
+
+    import torch
+
+    from oracle import shells as OS
+    from graddft_gb300 import _lib, build, engine, synthetic
+
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    n_grid = args.n_grid
+    n_atoms = max(1, args.n_ao // 30)
+    basis = contracted_basis(n_atoms)
+    n_ao = basis.n_ao
+    coords, w = synthetic.make_grid(n_grid, SEED)
+    form = args.form or "fp64"
+    r = engine.Resident(n_grid, n_ao, form, dev)
+    desc, _keep = basis.device_desc(dev)
+    c_d = torch.as_tensor(coords, device=dev)
+    w_d = torch.as_tensor(w, device=dev)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+    sp = engine._stream(dev)
+
+    def step():
+        _lib.check(lib.gdft_molecule_eval_shells(ctypes.byref(r.desc), ctypes.byref(desc), engine._ptr(c_d),
+                                                 engine._ptr(w_d), sp))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(1, args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    np_, ld = int(r.desc.n_grid_pad), int(r.desc.ld)
+    ldk = (n_ao + 127) // 128 * 128
+    # algorithmic bytes written per launch: the resident tables of the form
+    out_bytes = 5 * np_ * ld * 8 if form == "fp64" else (5 * 2 + 4 * 3 + 5) * np_ * ldk * 4
+    hbm, _, src = _peaks()
+    n_exp = sum(len(s.exps) * (2 * s.l + 1) for s in basis.shells)
+    line = {
+        "metric": "AO tables from contracted shells (phi, grad phi, lap phi), grid-pts/s", "value": n_grid / (ms * 1e-3),
+        "unit": "grid-pts/s", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded contracted spherical basis, uniform grid)",
+        "config": {"workload": f"gdft_molecule_eval_shells: {n_atoms} atoms x (4s 3p 2d 1f) = {n_ao} AOs, "
+                               f"n_grid {n_grid}, {form} tables", "n_ao": n_ao, "n_grid": n_grid, "form": form,
+                   "exp_per_point": n_exp, "l2": "output tables larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": out_bytes / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": out_bytes / (ms * 1e-3) / 1e9 / hbm, "traffic": None,
+                     "note": f"bytes written by the table pass over its duration, of {src} copy bandwidth; "
+                             f"{n_exp} FP64 exponentials per point"},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        n_s = min(args.cpu_sample, 1024)
+        spec = [(s.centre, s.l, s.exps, s.coefs, None) for s in basis.shells]
+        t0 = time.perf_counter()
+        OS.eval_shells(spec, coords[:n_s])
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_s / dt, "unit": "grid-pts/s", "cores": 1, "kind": "port",
+                                "sample": f"{n_s} grid points ({dt:.1f} s), numpy restatement (oracle/shells.py) "
+                                          "of phi, grad phi and the diagonal second derivatives"}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -603,10 +698,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
-    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch", "hf"],
+    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch", "hf", "ao"],
                     help="xc: B88+LYP contraction benchmark (headline); neural: DM21-style network fwd+bwd; "
                          "scf: differentiable SCF loop; batch: many molecules per step; hf: DM21 predict with "
-                         "its exact-exchange terms from a chi tensor")
+                         "its exact-exchange terms from a chi tensor; ao: AO tables from contracted shells")
     ap.add_argument("--n-mol", type=int, default=64, help="molecules (--workload batch)")
     ap.add_argument("--points-per-ao", type=int, default=150, help="grid points per AO (--workload batch)")
     ap.add_argument("--cycles", type=int, default=20, help="SCF iterations (--workload scf)")
@@ -623,6 +718,8 @@ def main():
         return run_batch(args)
     if args.workload == "hf":
         return run_hf(args)
+    if args.workload == "ao":
+        return run_ao(args)
 
     import torch
 

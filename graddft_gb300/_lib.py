@@ -30,7 +30,8 @@ MAX_COLS = 8
 # Every symbol include/gdft.h declares.
 EXPORTS = (
     "gdft_abi_version", "gdft_last_error", "gdft_molecule_bytes", "gdft_molecule_init", "gdft_molecule_load",
-    "gdft_molecule_eval_basis", "gdft_workspace_bytes", "gdft_density", "gdft_xc_energy_and_grads",
+    "gdft_molecule_eval_basis", "gdft_eval_ao", "gdft_molecule_eval_shells", "gdft_workspace_bytes",
+    "gdft_density", "gdft_xc_energy_and_grads",
     "gdft_energy_densities", "gdft_vxc_from_potentials", "gdft_integrate", "gdft_integrate_workspace_bytes", "gdft_integrate_noalloc", "gdft_fock", "gdft_coulomb",
     "gdft_profile_enable", "gdft_profile_reset", "gdft_profile_read", "gdft_device_status", "gdft_selftest_umma",
     "gdft_umma_probe", "gdft_network_param_count", "gdft_neural_workspace_bytes",
@@ -86,7 +87,24 @@ _lock = threading.Lock()
 
 P = ctypes.c_void_p
 I32, I64, SZ, D = ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t, ctypes.c_double
+class GdftBasis(ctypes.Structure):
+    _fields_ = [
+        ("n_shell", ctypes.c_int32),
+        ("n_ao", ctypes.c_int32),
+        ("n_prim", ctypes.c_int64),
+        ("n_coef", ctypes.c_int64),
+        ("n_trans", ctypes.c_int64),
+        ("d_shell", ctypes.c_void_p),
+        ("d_centre", ctypes.c_void_p),
+        ("d_exp", ctypes.c_void_p),
+        ("d_coef", ctypes.c_void_p),
+        ("d_ao", ctypes.c_void_p),
+        ("d_trans", ctypes.c_void_p),
+    ]
+
+
 PMOL = ctypes.POINTER(GdftMolecule)
+PBAS = ctypes.POINTER(GdftBasis)
 PFN = ctypes.POINTER(GdftFunctional)
 PNET = ctypes.POINTER(GdftNetwork)
 
@@ -97,6 +115,8 @@ _SIGS = {
     "gdft_molecule_init": ([PMOL, I64, I32, I32, P, SZ], ctypes.c_int),
     "gdft_molecule_load": ([PMOL, P, P, P, P, P], ctypes.c_int),
     "gdft_molecule_eval_basis": ([PMOL, P, P, P, P], ctypes.c_int),
+    "gdft_eval_ao": ([PBAS, P, I64, I32, P, P, P, P], ctypes.c_int),
+    "gdft_molecule_eval_shells": ([PMOL, PBAS, P, P, P], ctypes.c_int),
     "gdft_workspace_bytes": ([PMOL, ctypes.POINTER(SZ)], ctypes.c_int),
     "gdft_density": ([PMOL, P, P, P, P, P, P, SZ, P], ctypes.c_int),
     "gdft_xc_energy_and_grads": ([PMOL, P, PFN, P, I32, P, P, P, SZ, P], ctypes.c_int),

@@ -6,6 +6,7 @@
 // np rows (multiple of 128) and ld columns (multiple of 32).
 #include "common.cuh"
 #include "kernels.cuh"
+#include "shells.cuh"
 
 namespace gdft {
 
@@ -96,7 +97,63 @@ __global__ void eval_basis_kernel(const double *__restrict__ basis, const double
   if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
 }
 
+// Contracted shells -> reference layouts: ao (grid, ao), grad (grid, ao, 3),
+// grad2 (grid, ao, 3) diagonal second derivatives.  One thread per (point, AO),
+// AO fastest, so a warp writes a contiguous run.  An AO whose table entries are
+// out of range gets NaN.
+__global__ void eval_ao_kernel(ShellView B, const double *__restrict__ coords, int64_t n_grid, int deriv,
+                               double *__restrict__ ao, double *__restrict__ g1, double *__restrict__ g2) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)n_grid * B.n_ao) return;
+  const int64_t p = (int64_t)(idx / B.n_ao);
+  const int a = (int)(idx % B.n_ao);
+  double v[7];
+  if (!shell_ao_eval(B, coords[3 * p], coords[3 * p + 1], coords[3 * p + 2], a, v))
+    for (int q = 0; q < 7; ++q) v[q] = __longlong_as_double(0x7ff8000000000000LL);
+  ao[idx] = v[0];
+  if (deriv >= 1)
+    for (int i = 0; i < 3; ++i) g1[3 * idx + i] = v[1 + i];
+  if (deriv >= 2)
+    for (int i = 0; i < 3; ++i) g2[3 * idx + i] = v[4 + i];
+}
+
+// Contracted shells -> the FP64 form's resident planes.
+__global__ void eval_shell_tables_kernel(ShellView B, const double *__restrict__ coords,
+                                         const double *__restrict__ w, int64_t n_grid, int64_t np, int ld,
+                                         double *__restrict__ tab, double *__restrict__ wout) {
+  const size_t pe = (size_t)np * ld;
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= pe) return;
+  const int64_t p = (int64_t)(idx / ld);
+  const int a = (int)(idx % ld);
+  double v[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (p < n_grid && a < B.n_ao &&
+      !shell_ao_eval(B, coords[3 * p], coords[3 * p + 1], coords[3 * p + 2], a, v))
+    for (int q = 0; q < 7; ++q) v[q] = __longlong_as_double(0x7ff8000000000000LL);
+  tab[T_PHI * pe + idx] = v[0];
+  tab[T_DX * pe + idx] = v[1];
+  tab[T_DY * pe + idx] = v[2];
+  tab[T_DZ * pe + idx] = v[3];
+  tab[T_LAP * pe + idx] = (v[4] + v[5]) + v[6];
+  if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
+}
+
 }  // namespace
+
+cudaError_t launch_eval_ao(const ShellView &B, const double *coords, int64_t n_grid, int deriv, double *ao,
+                           double *g1, double *g2, cudaStream_t st) {
+  const size_t total = (size_t)n_grid * B.n_ao;
+  eval_ao_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(B, coords, n_grid, deriv, ao, g1, g2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eval_shell_tables(const ShellView &B, const double *coords, const double *w, int64_t n_grid,
+                                     int64_t np, int ld, double *tab, double *wout, cudaStream_t st) {
+  const size_t total = (size_t)np * ld;
+  eval_shell_tables_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(B, coords, w, n_grid, np, ld, tab,
+                                                                             wout);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_load_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *w,
                                int64_t n_grid, int n_ao, int64_t np, int ld, double *tab, double *wout,

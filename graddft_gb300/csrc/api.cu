@@ -478,6 +478,82 @@ int gdft_molecule_eval_basis(const gdft_molecule *mol, const double *d_basis, co
                     "eval_basis");
 }
 
+static int check_basis(const gdft_basis *b, const char *who, ShellView *out) {
+  if (b == nullptr || b->d_shell == nullptr || b->d_centre == nullptr || b->d_exp == nullptr ||
+      b->d_coef == nullptr || b->d_ao == nullptr || b->d_trans == nullptr) {
+    set_error("%s: the basis and all of its tables are required", who);
+    return GDFT_ERR_INVALID;
+  }
+  if (b->n_shell <= 0 || b->n_ao <= 0 || b->n_prim <= 0 || b->n_coef <= 0 || b->n_trans <= 0) {
+    set_error("%s: basis sizes must be positive (n_shell=%d n_ao=%d)", who, b->n_shell, b->n_ao);
+    return GDFT_ERR_INVALID;
+  }
+  int rc;
+  if ((rc = check_aligned8(b->d_centre, "basis centres")) || (rc = check_aligned8(b->d_exp, "basis exponents")) ||
+      (rc = check_aligned8(b->d_coef, "basis coefficients")) || (rc = check_aligned8(b->d_trans, "basis rows")))
+    return rc;
+  if (((uintptr_t)b->d_shell | (uintptr_t)b->d_ao) & 3u) {
+    set_error("%s: the shell and AO tables must be 4-byte aligned", who);
+    return GDFT_ERR_ALIGNMENT;
+  }
+  *out = ShellView{b->d_shell, b->d_centre, b->d_exp, b->d_coef, b->d_ao, b->d_trans,
+                   b->n_shell, b->n_ao,   b->n_prim, b->n_coef, b->n_trans};
+  return GDFT_OK;
+}
+
+int gdft_eval_ao(const gdft_basis *basis, const double *d_coords, int64_t n_grid, int32_t deriv, double *d_ao,
+                 double *d_grad_ao, double *d_grad2_ao, void *stream) {
+  ShellView B;
+  int rc = check_basis(basis, "gdft_eval_ao", &B);
+  if (rc) return rc;
+  if (d_coords == nullptr || d_ao == nullptr || n_grid <= 0 || deriv < 0 || deriv > 2 ||
+      (deriv >= 1 && d_grad_ao == nullptr) || (deriv >= 2 && d_grad2_ao == nullptr)) {
+    set_error("gdft_eval_ao: coords, ao and the outputs of deriv=%d are required (n_grid=%lld)", deriv,
+              (long long)n_grid);
+    return GDFT_ERR_INVALID;
+  }
+  if ((size_t)n_grid * (size_t)basis->n_ao > ((size_t)1 << 38)) {  // grid of 256-thread blocks within 2^31
+    set_error("gdft_eval_ao: n_grid * n_ao too large");
+    return GDFT_ERR_INVALID;
+  }
+  if ((rc = check_aligned8(d_coords, "coords")) || (rc = check_aligned8(d_ao, "ao")) ||
+      (rc = check_aligned8(d_grad_ao, "grad_ao")) || (rc = check_aligned8(d_grad2_ao, "grad2_ao")))
+    return rc;
+  StageTimer tm(GDFT_STAGE_AO, (cudaStream_t)stream);
+  return check_cuda(launch_eval_ao(B, d_coords, n_grid, deriv, d_ao, deriv >= 1 ? d_grad_ao : nullptr,
+                                   deriv >= 2 ? d_grad2_ao : nullptr, (cudaStream_t)stream),
+                    "eval_ao");
+}
+
+int gdft_molecule_eval_shells(const gdft_molecule *mol, const gdft_basis *basis, const double *d_coords,
+                              const double *d_weights, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  ShellView B;
+  if ((rc = check_basis(basis, "gdft_molecule_eval_shells", &B))) return rc;
+  if (basis->n_ao != mol->n_ao) {
+    set_error("gdft_molecule_eval_shells: the basis has %d AOs, the molecule %d", basis->n_ao, mol->n_ao);
+    return GDFT_ERR_INVALID;
+  }
+  if (d_coords == nullptr || d_weights == nullptr) {
+    set_error("gdft_molecule_eval_shells: coords and weights are required");
+    return GDFT_ERR_INVALID;
+  }
+  if ((rc = check_aligned8(d_coords, "coords")) || (rc = check_aligned8(d_weights, "weights"))) return rc;
+  const MolLayout L = mol_layout(mol->n_grid, mol->n_ao, mol->precision);
+  double *w = (double *)((char *)mol->buffer + L.off_w);
+  StageTimer tm(GDFT_STAGE_AO, (cudaStream_t)stream);
+  if (mol->precision == GDFT_TF32X3)
+    return check_cuda(launch_pack_tables(nullptr, nullptr, nullptr, nullptr, d_coords, d_weights, mol->n_grid,
+                                         mol->n_ao, L.np, L.ldk, (float *)((char *)mol->buffer + L.off_pm),
+                                         (float *)((char *)mol->buffer + L.off_av),
+                                         (float *)((char *)mol->buffer + L.off_af), w, (cudaStream_t)stream, &B),
+                      "pack_tables (shells)");
+  return check_cuda(launch_eval_shell_tables(B, d_coords, d_weights, mol->n_grid, L.np, L.ld,
+                                             (double *)((char *)mol->buffer + L.off_tab), w, (cudaStream_t)stream),
+                    "eval_shell_tables");
+}
+
 int gdft_workspace_bytes(const gdft_molecule *mol, size_t *bytes) {
   int rc = check_mol(mol);
   if (rc) return rc;

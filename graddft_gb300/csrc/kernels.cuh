@@ -2,6 +2,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "shells.cuh"
 
 namespace gdft {
 
@@ -11,6 +12,11 @@ cudaError_t launch_load_tables(const double *ao, const double *grad_ao, const do
                                cudaStream_t st);
 cudaError_t launch_eval_basis(const double *basis, const double *coords, const double *w, int64_t n_grid, int n_ao,
                               int64_t np, int ld, double *tab, double *wout, cudaStream_t st);
+// Contracted shells: reference layouts (eval_ao / ao_grads) and the FP64 planes.
+cudaError_t launch_eval_ao(const ShellView &B, const double *coords, int64_t n_grid, int deriv, double *ao,
+                           double *g1, double *g2, cudaStream_t st);
+cudaError_t launch_eval_shell_tables(const ShellView &B, const double *coords, const double *w, int64_t n_grid,
+                                     int64_t np, int ld, double *tab, double *wout, cudaStream_t st);
 
 // dens_f64.cu: FP64 form of the density contraction -> feat[2][6][np].
 cudaError_t launch_dens_f64(const double *tab, int64_t np, int ld, int n_ao, const double *rdm1, double *feat,
@@ -24,7 +30,8 @@ cudaError_t launch_vxc_f64(const double *tab, int64_t np, int ld, int n_ao, cons
 // tc_pack.cu / dens_tc.cu: TF32x3 form.
 cudaError_t launch_pack_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *basis,
                                const double *coords, const double *w, int64_t n_grid, int n_ao, int64_t np, int ldk,
-                               float *pm, float *av, float *af, double *wout, cudaStream_t st);
+                               float *pm, float *av, float *af, double *wout, cudaStream_t st,
+                               const ShellView *shells = nullptr);
 cudaError_t launch_pack_rdm1(const double *D, int n, int ldk, float *out, cudaStream_t st);
 cudaError_t launch_dens_tc(const float *pm, const float *dpk, int64_t np, int ldk, double *feat, int *err,
                            cudaStream_t st);

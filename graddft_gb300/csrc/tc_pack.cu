@@ -41,25 +41,39 @@ __device__ __forceinline__ void store_split(float *base, size_t blk, uint32_t of
   b[umma::kBlockBytes / 4 + off / 4] = lo;
 }
 
+// Sources of the plane values.
+enum PackSrc { kFromTables = 0, kFromSynthetic = 1, kFromShells = 2 };
+
 // One thread per (point, AO) of the padded tables: computes the five plane
-// values (from reference layouts or from the synthetic basis) and scatters
+// values (from reference layouts, the synthetic basis or contracted shells) and scatters
 // them into the point-major and FP32 layouts.  The AO-major three-slice sets
 // need each AO's maximum over a point chunk first: this pass parks the FP64
 // values of a set, [point (32)][AO (128)], in the set's own first 32 KB and
 // pack_av_kernel splits them in place.
-template <bool kBasis>
+template <int kSrc>
 __global__ void pack_tables_kernel(const double *__restrict__ ao, const double *__restrict__ grad_ao,
                                    const double *__restrict__ grad2_ao, const double *__restrict__ basis,
                                    const double *__restrict__ coords, const double *__restrict__ w, int64_t n_grid,
                                    int n_ao, int64_t np, int ldk, float *__restrict__ pm, float *__restrict__ av,
-                                   float *__restrict__ af, double *__restrict__ wout) {
+                                   float *__restrict__ af, double *__restrict__ wout, ShellView shells) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)np * ldk) return;
   const int64_t p = (int64_t)(idx / ldk);
   const int a = (int)(idx % ldk);
   double v[kPlanes] = {0.0, 0.0, 0.0, 0.0, 0.0};
   if (p < n_grid && a < n_ao) {
-    if (!kBasis) {
+    if (kSrc == kFromShells) {
+      double u[7];
+      if (shell_ao_eval(shells, coords[3 * p], coords[3 * p + 1], coords[3 * p + 2], a, u)) {
+        v[T_PHI] = u[0];
+        v[T_DX] = u[1];
+        v[T_DY] = u[2];
+        v[T_DZ] = u[3];
+        v[T_LAP] = (u[4] + u[5]) + u[6];
+      } else {
+        for (int t = 0; t < kPlanes; ++t) v[t] = __longlong_as_double(0x7ff8000000000000LL);
+      }
+    } else if (kSrc == kFromTables) {
       const size_t r = (size_t)p * n_ao + a;
       v[T_PHI] = ao[r];
       v[T_DX] = grad_ao[3 * r + 0];
@@ -157,15 +171,22 @@ __global__ void pack_rdm1_kernel(const double *__restrict__ D, int n, int ldk, f
 
 cudaError_t launch_pack_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *basis,
                                const double *coords, const double *w, int64_t n_grid, int n_ao, int64_t np, int ldk,
-                               float *pm, float *av, float *af, double *wout, cudaStream_t st) {
+                               float *pm, float *av, float *af, double *wout, cudaStream_t st,
+                               const ShellView *shells) {
   const size_t total = (size_t)np * ldk;
   const unsigned blocks = (unsigned)((total + 255) / 256);
-  if (basis != nullptr)
-    pack_tables_kernel<true><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
-                                                     pm, av, af, wout);
-  else
-    pack_tables_kernel<false><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao, np, ldk,
-                                                      pm, av, af, wout);
+  ShellView sv{};
+  if (shells != nullptr) {
+    sv = *shells;
+    pack_tables_kernel<kFromShells><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao,
+                                                            np, ldk, pm, av, af, wout, sv);
+  } else if (basis != nullptr) {
+    pack_tables_kernel<kFromSynthetic><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid,
+                                                               n_ao, np, ldk, pm, av, af, wout, sv);
+  } else {
+    pack_tables_kernel<kFromTables><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao,
+                                                            np, ldk, pm, av, af, wout, sv);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   pack_av_kernel<<<(unsigned)((size_t)(ldk / 128) * 4 * (np / 32)), 128, 0, st>>>(av);

@@ -105,6 +105,22 @@ class Resident:
         torch.cuda.current_stream(dev).synchronize()
         return r
 
+    @classmethod
+    def from_shells(cls, basis, coords, weights, precision="fp64", device=None) -> "Resident":
+        """Evaluate a contracted Gaussian basis (``graddft_gb300.basis.ShellBasis``) straight into the
+        resident tables: no (grid, ao) reference-layout arrays are formed."""
+        dev = require_cuda(device)
+        coords = as_device_f64(coords, dev)
+        weights = as_device_f64(weights, dev)
+        if coords.ndim != 2 or coords.shape[1] != 3 or weights.shape != (coords.shape[0],):
+            raise ValueError(f"coords {tuple(coords.shape)} / weights {tuple(weights.shape)} must be (grid, 3) / (grid,)")
+        desc, _keep = basis.device_desc(dev)
+        r = cls(coords.shape[0], desc.n_ao, precision, dev)
+        check(_lib.load().gdft_molecule_eval_shells(ctypes.byref(r.desc), ctypes.byref(desc), _ptr(coords),
+                                                    _ptr(weights), _stream(dev)))
+        torch.cuda.current_stream(dev).synchronize()
+        return r
+
     def ao_planes(self) -> torch.Tensor:
         """The FP64 form's resident tables as a (5, n_grid_pad, ld) view: phi, d_x, d_y, d_z, lap phi."""
         if self.precision != "fp64":

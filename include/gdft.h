@@ -114,6 +114,44 @@ int gdft_molecule_load(const gdft_molecule *mol, const double *d_ao, const doubl
 int gdft_molecule_eval_basis(const gdft_molecule *mol, const double *d_basis, const double *d_coords,
                              const double *d_weights, void *stream);
 
+/* A contracted Gaussian basis on the device: the functions numint.eval_ao
+ * evaluates (interface/pyscf.py:849-852).  AO a belongs to shell s = ao[a][0]
+ * and contraction c = ao[a][1]:
+ *   phi_a(r) = sum_p coef[coff_s + c*nprim_s + p] exp(-exp[poff_s + p] |r - R_s|^2)
+ *              * sum_(i,j,k) trans[ao[a][2] + q] x^i y^j z^k,   (x, y, z) = r - R_s,
+ * q running over the (l+1)(l+2)/2 exponents (i, j, k) of degree l = shell[s][0]
+ * in the order i = l..0, then j = l-i..0 (PySCF's cartesian order).  The
+ * angular rows carry the convention (real solid harmonics or cartesians).
+ * All pointers are device pointers; l <= 6.  An AO whose entries fall outside
+ * the tables evaluates to NaN (the kernels never read outside them). */
+typedef struct gdft_basis {
+  int32_t n_shell;
+  int32_t n_ao;
+  int64_t n_prim;          /* length of d_exp                                         */
+  int64_t n_coef;          /* length of d_coef                                        */
+  int64_t n_trans;         /* length of d_trans                                       */
+  const int32_t *d_shell;  /* (n_shell, 4): l, nprim, exponent offset, coefficient offset */
+  const double *d_centre;  /* (n_shell, 3) bohr                                       */
+  const double *d_exp;
+  const double *d_coef;
+  const int32_t *d_ao;     /* (n_ao, 4): shell, contraction, row offset in d_trans, 0   */
+  const double *d_trans;
+} gdft_basis;
+
+/* numint.eval_ao(mol, coords, deriv) for deriv 0 or 1 (interface/pyscf.py:849-852,
+ * the derivative axis moved last as the Molecule stores it) and, for deriv 2,
+ * the diagonal second derivatives of ao_grads(mol, coords, order=2)[2]
+ * (interface/pyscf.py:677-705).  d_coords: (n_grid, 3) bohr; d_ao: (n_grid, n_ao);
+ * d_grad_ao (deriv >= 1), d_grad2_ao (deriv 2): (n_grid, n_ao, 3). */
+int gdft_eval_ao(const gdft_basis *basis, const double *d_coords, int64_t n_grid, int32_t deriv, double *d_ao,
+                 double *d_grad_ao, double *d_grad2_ao, void *stream);
+
+/* Evaluate a contracted basis on the grid directly into the molecule (both
+ * arithmetic forms): phi, its gradient and Laplacian, with no reference-layout
+ * tables in between.  basis->n_ao must equal the molecule's n_ao. */
+int gdft_molecule_eval_shells(const gdft_molecule *mol, const gdft_basis *basis, const double *d_coords,
+                              const double *d_weights, void *stream);
+
 /* Workspace bytes for the calls below on this molecule. */
 int gdft_workspace_bytes(const gdft_molecule *mol, size_t *bytes);
 
