@@ -254,16 +254,17 @@ class ShellBasis:
             e = np.asarray(s.exps, dtype=np.float64)
             c = np.asarray(s.coefs, dtype=np.float64).reshape(e.size, -1)
             rows = self.rows_for(s)
-            shell_t.append([int(s.l), e.size, len(exps), len(coefs)])
+            ncomp, nctr = rows.shape[0], c.shape[1]
+            shell_t.append([int(s.l), e.size, len(exps), len(coefs), len(ao_t), ncomp, nctr, len(trans)])
             centre.append(np.asarray(s.centre, dtype=np.float64))
             exps.extend(e.tolist())
             coefs.extend(c.T.reshape(-1).tolist())  # contraction-major
-            for ic in range(c.shape[1]):
-                for r in rows:
-                    ao_t.append([i, ic, len(trans), 0])
-                    trans.extend(r.tolist())
+            trans.extend(rows.reshape(-1).tolist())
+            for ic in range(nctr):
+                for k in range(ncomp):
+                    ao_t.append([i, ic, k, 0])
         return {
-            "shell": np.asarray(shell_t, dtype=np.int32).reshape(-1, 4),
+            "shell": np.asarray(shell_t, dtype=np.int32).reshape(-1, 8),
             "centre": np.asarray(centre, dtype=np.float64).reshape(-1, 3),
             "exp": np.asarray(exps, dtype=np.float64),
             "coef": np.asarray(coefs, dtype=np.float64),

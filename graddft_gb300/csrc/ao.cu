@@ -97,62 +97,52 @@ __global__ void eval_basis_kernel(const double *__restrict__ basis, const double
   if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
 }
 
-// Contracted shells -> reference layouts: ao (grid, ao), grad (grid, ao, 3),
-// grad2 (grid, ao, 3) diagonal second derivatives.  One thread per (point, AO),
-// AO fastest, so a warp writes a contiguous run.  An AO whose table entries are
-// out of range gets NaN.
-__global__ void eval_ao_kernel(ShellView B, const double *__restrict__ coords, int64_t n_grid, int deriv,
-                               double *__restrict__ ao, double *__restrict__ g1, double *__restrict__ g2) {
-  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (size_t)n_grid * B.n_ao) return;
-  const int64_t p = (int64_t)(idx / B.n_ao);
-  const int a = (int)(idx % B.n_ao);
-  double v[7];
-  if (!shell_ao_eval(B, coords[3 * p], coords[3 * p + 1], coords[3 * p + 2], a, v))
-    for (int q = 0; q < 7; ++q) v[q] = __longlong_as_double(0x7ff8000000000000LL);
-  ao[idx] = v[0];
-  if (deriv >= 1)
-    for (int i = 0; i < 3; ++i) g1[3 * idx + i] = v[1 + i];
-  if (deriv >= 2)
-    for (int i = 0; i < 3; ++i) g2[3 * idx + i] = v[4 + i];
-}
+// Sinks of the shell tiles (shells.cuh).  Reference layouts: ao (grid, ao),
+// grad (grid, ao, 3), grad2 (grid, ao, 3) diagonal second derivatives.
+struct RefSink {
+  double *ao, *g1, *g2;
+  int64_t n_grid;
+  int n_ao, deriv;
+  __device__ void operator()(const double *tile, int t, int ps, int64_t p, int a) const {
+    if (p >= n_grid || a >= n_ao) return;
+    const size_t r = (size_t)p * n_ao + a;
+    ao[r] = tile[t];
+    if (deriv >= 1)
+      for (int i = 0; i < 3; ++i) g1[3 * r + i] = tile[(1 + i) * ps + t];
+    if (deriv >= 2)
+      for (int i = 0; i < 3; ++i) g2[3 * r + i] = tile[(4 + i) * ps + t];
+  }
+};
 
-// Contracted shells -> the FP64 form's resident planes.
-__global__ void eval_shell_tables_kernel(ShellView B, const double *__restrict__ coords,
-                                         const double *__restrict__ w, int64_t n_grid, int64_t np, int ld,
-                                         double *__restrict__ tab, double *__restrict__ wout) {
-  const size_t pe = (size_t)np * ld;
-  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= pe) return;
-  const int64_t p = (int64_t)(idx / ld);
-  const int a = (int)(idx % ld);
-  double v[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  if (p < n_grid && a < B.n_ao &&
-      !shell_ao_eval(B, coords[3 * p], coords[3 * p + 1], coords[3 * p + 2], a, v))
-    for (int q = 0; q < 7; ++q) v[q] = __longlong_as_double(0x7ff8000000000000LL);
-  tab[T_PHI * pe + idx] = v[0];
-  tab[T_DX * pe + idx] = v[1];
-  tab[T_DY * pe + idx] = v[2];
-  tab[T_DZ * pe + idx] = v[3];
-  tab[T_LAP * pe + idx] = (v[4] + v[5]) + v[6];
-  if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
-}
+// The FP64 form's resident planes (zero padding beyond n_grid and n_ao).
+struct PlaneSink {
+  double *tab;
+  const double *w;
+  double *wout;
+  int64_t n_grid;
+  size_t pe;
+  int n_ao, ld;
+  __device__ void operator()(const double *tile, int t, int ps, int64_t p, int a) const {
+    if (a >= ld) return;
+    const bool live = p < n_grid && a < n_ao;
+    const size_t o = (size_t)p * ld + a;
+#pragma unroll
+    for (int q = 0; q < kPlanes; ++q) tab[q * pe + o] = live ? tile[q * ps + t] : 0.0;
+    if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
+  }
+};
 
 }  // namespace
 
 cudaError_t launch_eval_ao(const ShellView &B, const double *coords, int64_t n_grid, int deriv, double *ao,
                            double *g1, double *g2, cudaStream_t st) {
-  const size_t total = (size_t)n_grid * B.n_ao;
-  eval_ao_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(B, coords, n_grid, deriv, ao, g1, g2);
-  return cudaGetLastError();
+  return launch_shell_tiles<7>(B, coords, n_grid, n_grid, B.n_ao, RefSink{ao, g1, g2, n_grid, B.n_ao, deriv}, st);
 }
 
 cudaError_t launch_eval_shell_tables(const ShellView &B, const double *coords, const double *w, int64_t n_grid,
                                      int64_t np, int ld, double *tab, double *wout, cudaStream_t st) {
-  const size_t total = (size_t)np * ld;
-  eval_shell_tables_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(B, coords, w, n_grid, np, ld, tab,
-                                                                             wout);
-  return cudaGetLastError();
+  return launch_shell_tiles<kPlanes>(B, coords, n_grid, np, ld,
+                                     PlaneSink{tab, w, wout, n_grid, (size_t)np * ld, B.n_ao, ld}, st);
 }
 
 cudaError_t launch_load_tables(const double *ao, const double *grad_ao, const double *grad2_ao, const double *w,

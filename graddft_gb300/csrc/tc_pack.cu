@@ -41,8 +41,26 @@ __device__ __forceinline__ void store_split(float *base, size_t blk, uint32_t of
   b[umma::kBlockBytes / 4 + off / 4] = lo;
 }
 
-// Sources of the plane values.
-enum PackSrc { kFromTables = 0, kFromSynthetic = 1, kFromShells = 2 };
+// Sources of the plane values (contracted shells go through the tile sink below).
+enum PackSrc { kFromTables = 0, kFromSynthetic = 1 };
+
+// Scatter the five plane values of (point p, AO a) into the point-major pairs,
+// the parked FP64 values of the AO-major sets and the AO-major FP32 blocks.
+__device__ __forceinline__ void pack_store(float *__restrict__ pm, float *__restrict__ av, float *__restrict__ af,
+                                           int64_t np, int ldk, int64_t p, int a, const double v[kPlanes]) {
+  const int nkc = ldk / 32;
+  const int64_t npc = np / 32;
+  const int64_t tile = p / 128;
+#pragma unroll
+  for (int t = 0; t < kPlanes; ++t) {
+    store_split(pm, pm_block(tile, t, a / 32, nkc), umma::kblock_off((int)(p % 128), a % 32), v[t]);
+    if (t < 4)
+      ((double *)(av + av_set(a / 128, t, p / 32, npc) * 3 * (umma::kBlockBytes / 4)))[(p % 32) * 128 + a % 128] =
+          v[t];
+    af[af_block(a / 128, t, p / 32, npc) * (umma::kBlockBytes / 4) + umma::kblock_off(a % 128, (int)(p % 32)) / 4] =
+        (float)v[t];
+  }
+}
 
 // One thread per (point, AO) of the padded tables: computes the five plane
 // values (from reference layouts, the synthetic basis or contracted shells) and scatters
@@ -55,25 +73,14 @@ __global__ void pack_tables_kernel(const double *__restrict__ ao, const double *
                                    const double *__restrict__ grad2_ao, const double *__restrict__ basis,
                                    const double *__restrict__ coords, const double *__restrict__ w, int64_t n_grid,
                                    int n_ao, int64_t np, int ldk, float *__restrict__ pm, float *__restrict__ av,
-                                   float *__restrict__ af, double *__restrict__ wout, ShellView shells) {
+                                   float *__restrict__ af, double *__restrict__ wout) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)np * ldk) return;
   const int64_t p = (int64_t)(idx / ldk);
   const int a = (int)(idx % ldk);
   double v[kPlanes] = {0.0, 0.0, 0.0, 0.0, 0.0};
   if (p < n_grid && a < n_ao) {
-    if (kSrc == kFromShells) {
-      double u[7];
-      if (shell_ao_eval(shells, coords[3 * p], coords[3 * p + 1], coords[3 * p + 2], a, u)) {
-        v[T_PHI] = u[0];
-        v[T_DX] = u[1];
-        v[T_DY] = u[2];
-        v[T_DZ] = u[3];
-        v[T_LAP] = (u[4] + u[5]) + u[6];
-      } else {
-        for (int t = 0; t < kPlanes; ++t) v[t] = __longlong_as_double(0x7ff8000000000000LL);
-      }
-    } else if (kSrc == kFromTables) {
+    if (kSrc == kFromTables) {
       const size_t r = (size_t)p * n_ao + a;
       v[T_PHI] = ao[r];
       v[T_DX] = grad_ao[3 * r + 0];
@@ -125,20 +132,27 @@ __global__ void pack_tables_kernel(const double *__restrict__ ao, const double *
       v[T_LAP] = (lp[0] + lp[1]) + lp[2];
     }
   }
-  const int nkc = ldk / 32;
-  const int64_t npc = np / 32;
-  const int64_t tile = p / 128;
-#pragma unroll
-  for (int t = 0; t < kPlanes; ++t) {
-    store_split(pm, pm_block(tile, t, a / 32, nkc), umma::kblock_off((int)(p % 128), a % 32), v[t]);
-    if (t < 4)
-      ((double *)(av + av_set(a / 128, t, p / 32, npc) * 3 * (umma::kBlockBytes / 4)))[(p % 32) * 128 + a % 128] =
-          v[t];
-    af[af_block(a / 128, t, p / 32, npc) * (umma::kBlockBytes / 4) + umma::kblock_off(a % 128, (int)(p % 32)) / 4] =
-        (float)v[t];
-  }
+  pack_store(pm, av, af, np, ldk, p, a, v);
   if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
 }
+
+// Sink of the shell tiles (shells.cuh) into the same three layouts.
+struct PackSink {
+  float *pm, *av, *af;
+  const double *w;
+  double *wout;
+  int64_t n_grid, np;
+  int n_ao, ldk;
+  __device__ void operator()(const double *tile, int t, int ps, int64_t p, int a) const {
+    if (a >= ldk) return;
+    const bool live = p < n_grid && a < n_ao;
+    double v[kPlanes];
+#pragma unroll
+    for (int q = 0; q < kPlanes; ++q) v[q] = live ? tile[q * ps + t] : 0.0;
+    pack_store(pm, av, af, np, ldk, p, a, v);
+    if (a == 0) wout[p] = p < n_grid ? w[p] : 0.0;
+  }
+};
 
 // One CTA of 128 threads per AO-major set, one AO row per thread: reads the
 // parked FP64 values, then (after the whole CTA has read) writes hi|lo|lo2 over them.
@@ -173,21 +187,21 @@ cudaError_t launch_pack_tables(const double *ao, const double *grad_ao, const do
                                const double *coords, const double *w, int64_t n_grid, int n_ao, int64_t np, int ldk,
                                float *pm, float *av, float *af, double *wout, cudaStream_t st,
                                const ShellView *shells) {
-  const size_t total = (size_t)np * ldk;
-  const unsigned blocks = (unsigned)((total + 255) / 256);
-  ShellView sv{};
+  cudaError_t e;
   if (shells != nullptr) {
-    sv = *shells;
-    pack_tables_kernel<kFromShells><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao,
-                                                            np, ldk, pm, av, af, wout, sv);
-  } else if (basis != nullptr) {
-    pack_tables_kernel<kFromSynthetic><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid,
-                                                               n_ao, np, ldk, pm, av, af, wout, sv);
+    e = launch_shell_tiles<kPlanes>(*shells, coords, n_grid, np, ldk,
+                                    PackSink{pm, av, af, w, wout, n_grid, np, n_ao, ldk}, st);
   } else {
-    pack_tables_kernel<kFromTables><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao,
-                                                            np, ldk, pm, av, af, wout, sv);
+    const size_t total = (size_t)np * ldk;
+    const unsigned blocks = (unsigned)((total + 255) / 256);
+    if (basis != nullptr)
+      pack_tables_kernel<kFromSynthetic><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid,
+                                                                 n_ao, np, ldk, pm, av, af, wout);
+    else
+      pack_tables_kernel<kFromTables><<<blocks, 256, 0, st>>>(ao, grad_ao, grad2_ao, basis, coords, w, n_grid, n_ao,
+                                                              np, ldk, pm, av, af, wout);
+    e = cudaGetLastError();
   }
-  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   pack_av_kernel<<<(unsigned)((size_t)(ldk / 128) * 4 * (np / 32)), 128, 0, st>>>(av);
   return cudaGetLastError();

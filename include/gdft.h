@@ -115,26 +115,30 @@ int gdft_molecule_eval_basis(const gdft_molecule *mol, const double *d_basis, co
                              const double *d_weights, void *stream);
 
 /* A contracted Gaussian basis on the device: the functions numint.eval_ao
- * evaluates (interface/pyscf.py:849-852).  AO a belongs to shell s = ao[a][0]
- * and contraction c = ao[a][1]:
- *   phi_a(r) = sum_p coef[coff_s + c*nprim_s + p] exp(-exp[poff_s + p] |r - R_s|^2)
- *              * sum_(i,j,k) trans[ao[a][2] + q] x^i y^j z^k,   (x, y, z) = r - R_s,
- * q running over the (l+1)(l+2)/2 exponents (i, j, k) of degree l = shell[s][0]
- * in the order i = l..0, then j = l-i..0 (PySCF's cartesian order).  The
+ * evaluates (interface/pyscf.py:849-852).  Shell s (row s of d_shell: l,
+ * nprim, exponent offset, coefficient offset, first AO, ncomp, nctr, row
+ * offset) owns the nctr * ncomp consecutive AOs from its first AO on,
+ * contraction-major; its AO for contraction c and component k is
+ *   phi(r) = sum_p coef[coff + c*nprim + p] exp(-exp[poff + p] |r - R_s|^2)
+ *            * sum_(i,j,k) trans[roff + k*ncart + q] x^i y^j z^k,   (x, y, z) = r - R_s,
+ * q running over the ncart = (l+1)(l+2)/2 exponents (i, j, k) of degree l in
+ * the order i = l..0, then j = l-i..0 (PySCF's cartesian order).  The
  * angular rows carry the convention (real solid harmonics or cartesians).
- * All pointers are device pointers; l <= 6.  An AO whose entries fall outside
- * the tables evaluates to NaN (the kernels never read outside them). */
+ * Shells follow each other in AO order.  d_ao row a: shell, contraction,
+ * component, 0.  All pointers are device pointers; l <= 6.  An AO whose
+ * entries fall outside the tables evaluates to NaN (the kernels never read
+ * outside them). */
 typedef struct gdft_basis {
   int32_t n_shell;
   int32_t n_ao;
   int64_t n_prim;          /* length of d_exp                                         */
   int64_t n_coef;          /* length of d_coef                                        */
   int64_t n_trans;         /* length of d_trans                                       */
-  const int32_t *d_shell;  /* (n_shell, 4): l, nprim, exponent offset, coefficient offset */
+  const int32_t *d_shell;  /* (n_shell, 8)                                            */
   const double *d_centre;  /* (n_shell, 3) bohr                                       */
   const double *d_exp;
   const double *d_coef;
-  const int32_t *d_ao;     /* (n_ao, 4): shell, contraction, row offset in d_trans, 0   */
+  const int32_t *d_ao;     /* (n_ao, 4): shell, contraction, component, 0               */
   const double *d_trans;
 } gdft_basis;
 

@@ -156,10 +156,12 @@ def test_from_libcint_arrays():
     assert np.allclose(sb.shells[2].centre, [1.4, 0.3, -0.1])
     assert np.allclose(sb.shells[0].coefs, c_s)
     t = sb.host_tables()
-    assert t["shell"].tolist() == [[0, 3, 0, 0], [1, 2, 3, 6], [2, 1, 5, 8]]
+    # l, nprim, exponent offset, coefficient offset, first AO, components, contractions, row offset
+    assert t["shell"].tolist() == [[0, 3, 0, 0, 0, 1, 2, 0], [1, 2, 3, 6, 2, 3, 1, 1], [2, 1, 5, 8, 5, 5, 1, 10]]
     # AO order: contraction-major within a shell
-    assert t["ao"][:, :2].tolist() == [[0, 0], [0, 1], [1, 0], [1, 0], [1, 0]] + [[2, 0]] * 5
-    assert t["trans"].size == 2 * 1 + 3 * 3 + 5 * 6
+    assert t["ao"][:, :3].tolist() == ([[0, 0, 0], [0, 1, 0], [1, 0, 0], [1, 0, 1], [1, 0, 2]]
+                                       + [[2, 0, k] for k in range(5)])
+    assert t["trans"].size == 1 * 1 + 3 * 3 + 5 * 6
     cart = B.ShellBasis.from_libcint(atm, np.asarray(bas, dtype=np.int32), np.asarray(env), cart=True)
     assert cart.n_ao == 2 + 3 + 6
 
