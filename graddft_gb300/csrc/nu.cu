@@ -1,0 +1,619 @@
+// nu.cu - range-separated one-electron integrals on the grid and the chi tensor.
+//
+//   nu_ab(C) = int phi_a(r') phi_b(r') erf(omega |r' - C|) / |r' - C| dr'   (omega = 0: 1/|r' - C|)
+//   chi[r][w][s][a] = sum_(b,d) D_s[b][d] phi_b(r) nu^w_da(r)
+// (_evaluate_nu / _nu_chunk, external/_hf_density.py:17-120, which call PySCF's
+// int1e_grids; generate_chi_tensor, interface/pyscf.py:1067-1126).
+//
+// Integrals by the McMurchie-Davidson scheme.  For primitives of exponents
+// alpha (centre A) and beta (centre B), p = alpha + beta, P = (alpha A + beta B)/p:
+//   G_a G_b = sum_tuv E^x_t E^y_u E^z_v Lambda_tuv(r; p, P)   (Hermite expansion, E^00_0 = exp(-alpha beta/p X_AB^2),
+//     E^(i+1)j_t = E^ij_(t-1)/(2p) + X_PA E^ij_t + (t+1) E^ij_(t+1), likewise in j with X_PB),
+//   int Lambda_tuv(r') erf(omega|r'-C|)/|r'-C| dr' = (2 pi / p) sqrt(mu/p) R_tuv(mu, P - C),
+// with 1/mu = 1/p + 1/omega^2 (mu = p for the plain Coulomb operator): the
+// attenuated operator acts as the Coulomb potential of a Gaussian charge of
+// exponent omega^2, whose convolution with the product Gaussian is a Gaussian of
+// exponent mu.  R^n_000 = (-2 mu)^n F_n(mu |P - C|^2) and
+//   R^n_(t+1)uv = t R^(n+1)_(t-1)uv + X_PC R^(n+1)_tuv  (likewise in u and v).
+// The Boys function F_n(T) = int_0^1 u^(2n) exp(-T u^2) du comes from a table of
+// F_n on T = 0, 0.1, ..., 60 filled on the device from the positive series
+// F_n(T) = exp(-T) sum_k (2T)^k / ((2n+1)(2n+3)...(2n+2k+1)), a 9-term Taylor
+// expansion about the nearest tabulated T (F_n' = -F_(n+1)) for the highest n,
+// and the downward recursion F_n = (2T F_(n+1) + exp(-T)) / (2n+1); beyond T = 60,
+// F_0 = sqrt(pi/T)/2 and F_(n+1) = (2n+1) F_n / (2T).
+//
+// Work layout: one warp per shell pair and 32 grid points (lanes = points), so the
+// shell pair's primitive data (set up once per pair and omega by
+// nu_pair_setup_kernel) are uniform loads; templates on (l_a >= l_b) <= 2.
+#include <vector>
+
+#include "common.cuh"
+#include "mlp_gemm.cuh"
+#include "shells.cuh"
+
+namespace gdft {
+
+namespace {
+
+constexpr int kNuMaxL = 2;                 // shells up to d
+constexpr int kBoysN = 17;                 // F_0 .. F_16 tabulated
+constexpr int kBoysPts = 601;              // T = 0, 0.1, ..., 60
+constexpr double kBoysStep = 0.1;
+constexpr double kBoysTMax = 60.0;
+constexpr int kETab = 3 * 3 * 5;           // E[i][j][t], i, j <= 2, t <= 4 (per dimension)
+constexpr int kPPStride = 8 + 3 * kETab;   // mu, pref, P(3), p, 2 pad, E[x|y|z]
+constexpr double kPi = 3.14159265358979323846;
+
+__global__ void boys_table_kernel(double *__restrict__ tab) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kBoysPts * kBoysN) return;
+  const int pt = i / kBoysN, n = i % kBoysN;
+  const double T = pt * kBoysStep;
+  double term = 1.0 / (2 * n + 1), sum = term;
+  for (int k = 1; k < 1000; ++k) {
+    term *= 2.0 * T / (2 * n + 2 * k + 1);
+    sum += term;
+    if (term < 1e-18 * sum) break;
+  }
+  tab[i] = exp(-T) * sum;
+}
+
+// F_0 .. F_L at T.
+template <int L>
+__device__ __forceinline__ void boys(const double *__restrict__ tab, double T, double F[L + 1]) {
+  if (T < kBoysTMax) {
+    const int i = (int)(T * (1.0 / kBoysStep) + 0.5);
+    const double md = i * kBoysStep - T;  // -(T - T_i)
+    const double *row = tab + i * kBoysN + L;
+    // sum_k F_(L+k)(T_i) (-(T - T_i))^k / k!, Horner from k = 8
+    constexpr double inv_fact[9] = {1.0, 1.0, 1.0 / 2, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040,
+                                    1.0 / 40320};
+    double acc = row[8] * inv_fact[8];
+#pragma unroll
+    for (int k = 7; k >= 0; --k) acc = fma(acc, md, row[k] * inv_fact[k]);
+    F[L] = acc;
+    if (L > 0) {
+      const double e = exp(-T);
+#pragma unroll
+      for (int n = L - 1; n >= 0; --n) F[n] = fma(2.0 * T, F[n + 1], e) * (1.0 / (2 * n + 1));
+    }
+  } else {
+    F[0] = 0.5 * sqrt(kPi / T);
+    const double h = 0.5 / T;
+#pragma unroll
+    for (int n = 0; n < L; ++n) F[n + 1] = F[n] * ((2 * n + 1) * h);
+  }
+}
+
+__device__ __forceinline__ int e_idx(int i, int j, int t) { return (i * 3 + j) * 5 + t; }
+
+// One thread per shell pair: the primitive-pair records (mu, prefactor, P, Hermite E tables).
+__global__ void nu_pair_setup_kernel(ShellView B, const int32_t *__restrict__ pairs, int n_pairs, double omega,
+                                     double *__restrict__ pp, int64_t n_pp) {
+  const int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= n_pairs) return;
+  const int s1 = pairs[4 * ip], s2 = pairs[4 * ip + 1];
+  const int64_t off = pairs[4 * ip + 2];
+  shells_detail::ShellRec r1, r2;
+  if (!shells_detail::load_shell(B, s1, r1) || !shells_detail::load_shell(B, s2, r2)) return;
+  if (r1.l > kNuMaxL || r2.l > kNuMaxL || off < 0 || off + (int64_t)r1.np * r2.np > n_pp) return;
+  const double *A = B.centre + 3 * s1, *Bc = B.centre + 3 * s2;
+  for (int i1 = 0; i1 < r1.np; ++i1) {
+    for (int i2 = 0; i2 < r2.np; ++i2) {
+      double *rec = pp + (off + (int64_t)i1 * r2.np + i2) * kPPStride;
+      const double a = B.exps[r1.poff + i1], b = B.exps[r2.poff + i2];
+      const double p = a + b, ip2 = 0.5 / p;
+      const double mu = omega == 0.0 ? p : p * omega * omega / (p + omega * omega);
+      rec[0] = mu;
+      rec[1] = (2.0 * kPi / p) * sqrt(mu / p);
+      rec[5] = p;
+      for (int d = 0; d < 3; ++d) {
+        const double P = (a * A[d] + b * Bc[d]) / p;
+        rec[2 + d] = P;
+        const double xab = A[d] - Bc[d], xpa = P - A[d], xpb = P - Bc[d];
+        double *E = rec + 8 + d * kETab;
+        for (int q = 0; q < kETab; ++q) E[q] = 0.0;
+        E[e_idx(0, 0, 0)] = exp(-a * b / p * xab * xab);
+        for (int i = 0; i < r1.l; ++i)
+          for (int t = 0; t <= i + 1; ++t)
+            E[e_idx(i + 1, 0, t)] = (t > 0 ? ip2 * E[e_idx(i, 0, t - 1)] : 0.0) + xpa * E[e_idx(i, 0, t)] +
+                                    (t + 1 <= i ? (t + 1) * E[e_idx(i, 0, t + 1)] : 0.0);
+        for (int j = 0; j < r2.l; ++j)
+          for (int i = 0; i <= r1.l; ++i)
+            for (int t = 0; t <= i + j + 1; ++t)
+              E[e_idx(i, j + 1, t)] = (t > 0 ? ip2 * E[e_idx(i, j, t - 1)] : 0.0) + xpb * E[e_idx(i, j, t)] +
+                                      (t + 1 <= i + j ? (t + 1) * E[e_idx(i, j, t + 1)] : 0.0);
+      }
+    }
+  }
+}
+
+template <int L>
+struct CartPow {
+  // exponents of the ncart(L) monomials in PySCF's order
+  static constexpr int n = (L + 1) * (L + 2) / 2;
+  static __device__ __forceinline__ constexpr int x(int q) {
+    int idx = 0;
+    for (int lx = L; lx >= 0; --lx)
+      for (int ly = L - lx; ly >= 0; --ly) {
+        if (idx == q) return lx;
+        ++idx;
+      }
+    return 0;
+  }
+  static __device__ __forceinline__ constexpr int y(int q) {
+    int idx = 0;
+    for (int lx = L; lx >= 0; --lx)
+      for (int ly = L - lx; ly >= 0; --ly) {
+        if (idx == q) return ly;
+        ++idx;
+      }
+    return 0;
+  }
+  static __device__ __forceinline__ constexpr int z(int q) { return L - x(q) - y(q); }
+};
+
+// Hermite Coulomb integrals R^0_tuv, t + u + v <= L.
+template <int L>
+__device__ __forceinline__ void hermite_r(const double F[L + 1], double mu, double X, double Y, double Z,
+                                          double R[L + 1][L + 1][L + 1]) {
+  double nxt[L + 1][L + 1][L + 1];
+  double m2 = 1.0;
+#pragma unroll
+  for (int n = 0; n < L; ++n) m2 *= -2.0 * mu;
+  nxt[0][0][0] = m2 * F[L];
+#pragma unroll
+  for (int n = L - 1; n >= 0; --n) {
+    double cur[L + 1][L + 1][L + 1];
+    const int top = L - n;
+#pragma unroll
+    for (int t = 0; t <= L; ++t)
+#pragma unroll
+      for (int u = 0; u <= L; ++u)
+#pragma unroll
+        for (int v = 0; v <= L; ++v) {
+          if (t + u + v > top) continue;
+          double val;
+          if (t > 0)
+            val = (t > 1 ? (t - 1) * nxt[t > 1 ? t - 2 : 0][u][v] : 0.0) + X * nxt[t - 1][u][v];
+          else if (u > 0)
+            val = (u > 1 ? (u - 1) * nxt[0][u > 1 ? u - 2 : 0][v] : 0.0) + Y * nxt[0][u - 1][v];
+          else if (v > 0)
+            val = (v > 1 ? (v - 1) * nxt[0][0][v > 1 ? v - 2 : 0] : 0.0) + Z * nxt[0][0][v - 1];
+          else {
+            double m = 1.0;
+#pragma unroll
+            for (int k = 0; k < n; ++k) m *= -2.0 * mu;
+            val = m * F[n];
+          }
+          cur[t][u][v] = val;
+        }
+#pragma unroll
+    for (int t = 0; t <= L; ++t)
+#pragma unroll
+      for (int u = 0; u <= L; ++u)
+#pragma unroll
+        for (int v = 0; v <= L; ++v)
+          if (t + u + v <= top) nxt[t][u][v] = cur[t][u][v];
+  }
+#pragma unroll
+  for (int t = 0; t <= L; ++t)
+#pragma unroll
+    for (int u = 0; u <= L; ++u)
+#pragma unroll
+      for (int v = 0; v <= L; ++v)
+        if (t + u + v <= L) R[t][u][v] = nxt[t][u][v];
+}
+
+struct NuOut {
+  double *nu;      // nu[(a * n + b) * s_ab + p * s_p]
+  int64_t s_ab, s_p;
+  int n;
+};
+
+// One warp per shell pair of class (LA, LB), lanes = 32 points from p0.
+template <int LA, int LB>
+__global__ void __launch_bounds__(256) nu_kernel(ShellView B, const int32_t *__restrict__ pairs, int pair_lo,
+                                                 int pair_hi, const double *__restrict__ pp, int64_t n_pp,
+                                                 const double *__restrict__ boys_tab,
+                                                 const double *__restrict__ coords, int64_t p_begin, int64_t n_pts,
+                                                 NuOut out) {
+  constexpr int L = LA + LB;
+  constexpr int NA = CartPow<LA>::n, NB = CartPow<LB>::n;
+  const int lane = threadIdx.x & 31;
+  const int ip = pair_lo + blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (ip >= pair_hi) return;  // whole warps leave together
+  const int64_t pl = (int64_t)blockIdx.x * 32 + lane;  // point within the chunk
+  const bool live = pl < n_pts;
+  double Cx = 0.0, Cy = 0.0, Cz = 0.0;
+  if (live) {
+    const int64_t p = p_begin + pl;
+    Cx = coords[3 * p];
+    Cy = coords[3 * p + 1];
+    Cz = coords[3 * p + 2];
+  }
+  const int s1 = pairs[4 * ip], s2 = pairs[4 * ip + 1];
+  const int64_t off = pairs[4 * ip + 2];
+  shells_detail::ShellRec r1, r2;
+  if (!shells_detail::load_shell(B, s1, r1) || !shells_detail::load_shell(B, s2, r2)) return;
+  if (r1.l != LA || r2.l != LB || off < 0 || off + (int64_t)r1.np * r2.np > n_pp) return;
+  if (r1.ncomp > NA || r2.ncomp > NB) return;
+  for (int c1 = 0; c1 < r1.nctr; ++c1) {
+    for (int c2 = 0; c2 < r2.nctr; ++c2) {
+      double cart[NA][NB];
+#pragma unroll
+      for (int qa = 0; qa < NA; ++qa)
+#pragma unroll
+        for (int qb = 0; qb < NB; ++qb) cart[qa][qb] = 0.0;
+      for (int i1 = 0; i1 < r1.np; ++i1) {
+        const double ca = B.coef[r1.coff + (int64_t)c1 * r1.np + i1];
+        for (int i2 = 0; i2 < r2.np; ++i2) {
+          const double *rec = pp + (off + (int64_t)i1 * r2.np + i2) * kPPStride;
+          const double cc = ca * B.coef[r2.coff + (int64_t)c2 * r2.np + i2] * rec[1];
+          const double mu = rec[0];
+          const double X = rec[2] - Cx, Y = rec[3] - Cy, Z = rec[4] - Cz;
+          double F[L + 1];
+          boys<L>(boys_tab, mu * (X * X + Y * Y + Z * Z), F);
+          double R[L + 1][L + 1][L + 1];
+          hermite_r<L>(F, mu, X, Y, Z, R);
+          const double *Ex = rec + 8, *Ey = rec + 8 + kETab, *Ez = rec + 8 + 2 * kETab;
+#pragma unroll
+          for (int qa = 0; qa < NA; ++qa) {
+            const int ia = CartPow<LA>::x(qa), ka = CartPow<LA>::y(qa), ma = CartPow<LA>::z(qa);
+#pragma unroll
+            for (int qb = 0; qb < NB; ++qb) {
+              const int ib = CartPow<LB>::x(qb), kb = CartPow<LB>::y(qb), mb = CartPow<LB>::z(qb);
+              double s = 0.0;
+#pragma unroll
+              for (int t = 0; t <= L; ++t) {
+                if (t > ia + ib) continue;
+                const double ex = Ex[e_idx(ia, ib, t)];
+#pragma unroll
+                for (int u = 0; u <= L; ++u) {
+                  if (u > ka + kb) continue;
+                  const double exy = ex * Ey[e_idx(ka, kb, u)];
+#pragma unroll
+                  for (int v = 0; v <= L; ++v) {
+                    if (v > ma + mb || t + u + v > L) continue;
+                    s = fma(exy * Ez[e_idx(ma, mb, v)], R[t][u][v], s);
+                  }
+                }
+              }
+              cart[qa][qb] = fma(cc, s, cart[qa][qb]);
+            }
+          }
+        }
+      }
+      // angular rows on both sides, then the symmetric writes
+      const double *T1 = B.trans + r1.toff, *T2 = B.trans + r2.toff;
+      for (int k1 = 0; k1 < r1.ncomp; ++k1) {
+        double h[NB];
+#pragma unroll
+        for (int qb = 0; qb < NB; ++qb) {
+          double acc = 0.0;
+#pragma unroll
+          for (int qa = 0; qa < NA; ++qa) acc = fma(T1[k1 * NA + qa], cart[qa][qb], acc);
+          h[qb] = acc;
+        }
+        const int a = r1.aoff + c1 * r1.ncomp + k1;
+        for (int k2 = 0; k2 < r2.ncomp; ++k2) {
+          double v = 0.0;
+#pragma unroll
+          for (int qb = 0; qb < NB; ++qb) v = fma(T2[k2 * NB + qb], h[qb], v);
+          const int b = r2.aoff + c2 * r2.ncomp + k2;
+          if (live) {
+            out.nu[((int64_t)a * out.n + b) * out.s_ab + pl * out.s_p] = v;
+            out.nu[((int64_t)b * out.n + a) * out.s_ab + pl * out.s_p] = v;
+          }
+        }
+      }
+    }
+  }
+}
+
+// chi[(p * n_omega + w) * 2 + s][a] = sum_d X_s[p][d] nu[d][a][p] for a chunk of points.
+// CTA: 32 points (lanes) x 32 AOs (4 per warp); X staged through shared memory in 32-wide d tiles.
+__global__ void __launch_bounds__(256) chi_kernel(const double *__restrict__ X, const double *__restrict__ nu,
+                                                  int64_t n_pts, int64_t pc, int n, int n_omega, int w,
+                                                  double *__restrict__ chi, int64_t p_begin) {
+  __shared__ double xs[2][32][33];
+  __shared__ double os[32][2][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t p0 = (int64_t)blockIdx.x * 32;
+  const int a0 = blockIdx.y * 32;
+  double acc[4][2];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) acc[j][0] = acc[j][1] = 0.0;
+  for (int d0 = 0; d0 < n; d0 += 32) {
+    for (int i = threadIdx.x; i < 2 * 32 * 32; i += blockDim.x) {
+      const int s = i / (32 * 32), pt = (i / 32) % 32, dd = i % 32;
+      const int64_t p = p0 + pt;
+      xs[s][pt][dd] = (p < n_pts && d0 + dd < n) ? X[((int64_t)s * pc + p) * n + d0 + dd] : 0.0;
+    }
+    __syncthreads();
+    const int dn = min(32, n - d0);
+    const int64_t p = p0 + lane;
+    if (p < n_pts) {
+      for (int dd = 0; dd < dn; ++dd) {
+        const double x0 = xs[0][lane][dd], x1 = xs[1][lane][dd];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int a = a0 + 4 * warp + j;
+          if (a < n) {
+            const double v = nu[((int64_t)(d0 + dd) * n + a) * pc + p];
+            acc[j][0] = fma(x0, v, acc[j][0]);
+            acc[j][1] = fma(x1, v, acc[j][1]);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    os[lane][0][4 * warp + j] = acc[j][0];
+    os[lane][1][4 * warp + j] = acc[j][1];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 32 * 2 * 32; i += blockDim.x) {
+    const int pt = i / 64, s = (i / 32) % 2, aa = i % 32;
+    const int64_t p = p0 + pt;
+    if (p < n_pts && a0 + aa < n) chi[(((p_begin + p) * n_omega + w) * 2 + s) * n + a0 + aa] = os[pt][s][aa];
+  }
+}
+
+size_t al256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Host-side pair list: shell pairs (s1, s2) with l(s1) >= l(s2), each unordered
+// pair once, grouped by class (l1, l2); class_lo[c]..class_lo[c+1] for class c
+// = l1 * (l1 + 1) / 2 + l2.
+struct PairPlan {
+  std::vector<int32_t> pairs;  // (n_pairs, 4): s1, s2, primitive-pair offset, 0
+  int class_lo[7];
+  int64_t n_pp = 0;
+  int max_l = 0;
+};
+
+int make_plan(const gdft_basis *b, PairPlan &plan, const char *who) {
+  std::vector<int32_t> sh((size_t)b->n_shell * kShellCols);
+  cudaError_t e = cudaMemcpy(sh.data(), b->d_shell, sh.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return check_cuda(e, who);
+  std::vector<std::vector<int32_t>> cls(6);
+  for (int i = 0; i < b->n_shell; ++i) {
+    const int li = sh[(size_t)kShellCols * i];
+    if (li < 0 || li > kNuMaxL) {
+      set_error("%s: shell %d has l = %d; the integrals are built for l <= %d", who, i, li, kNuMaxL);
+      return GDFT_ERR_UNSUPPORTED;
+    }
+    plan.max_l = li > plan.max_l ? li : plan.max_l;
+  }
+  for (int i = 0; i < b->n_shell; ++i)
+    for (int j = 0; j <= i; ++j) {
+      int s1 = i, s2 = j;
+      if (sh[(size_t)kShellCols * s1] < sh[(size_t)kShellCols * s2]) {
+        s1 = j;
+        s2 = i;
+      }
+      const int l1 = sh[(size_t)kShellCols * s1], l2 = sh[(size_t)kShellCols * s2];
+      auto &v = cls[l1 * (l1 + 1) / 2 + l2];
+      v.push_back(s1);
+      v.push_back(s2);
+      v.push_back(0);
+      v.push_back(0);
+    }
+  int n = 0;
+  for (int c = 0; c < 6; ++c) {
+    plan.class_lo[c] = n;
+    for (size_t q = 0; q < cls[c].size(); q += 4) {
+      const int s1 = cls[c][q], s2 = cls[c][q + 1];
+      const int64_t np1 = sh[(size_t)kShellCols * s1 + 1], np2 = sh[(size_t)kShellCols * s2 + 1];
+      if (plan.n_pp + np1 * np2 > INT32_MAX) {
+        set_error("%s: too many primitive pairs", who);
+        return GDFT_ERR_INVALID;
+      }
+      plan.pairs.push_back(s1);
+      plan.pairs.push_back(s2);
+      plan.pairs.push_back((int32_t)plan.n_pp);
+      plan.pairs.push_back(0);
+      plan.n_pp += np1 * np2;
+      ++n;
+    }
+  }
+  plan.class_lo[6] = n;
+  return GDFT_OK;
+}
+
+struct NuWs {
+  size_t off_boys, off_pairs, off_pp, off_nu, off_x, bytes;
+};
+
+NuWs nu_ws(const PairPlan &plan, int n_ao, int64_t chunk, bool want_chi) {
+  NuWs W;
+  size_t off = 0;
+  W.off_boys = off;
+  off = al256(off + (size_t)kBoysPts * kBoysN * sizeof(double));
+  W.off_pairs = off;
+  off = al256(off + plan.pairs.size() * sizeof(int32_t));
+  W.off_pp = off;
+  off = al256(off + (size_t)plan.n_pp * kPPStride * sizeof(double));
+  W.off_nu = off;
+  W.off_x = off;
+  if (want_chi) {
+    off = al256(off + (size_t)n_ao * n_ao * chunk * sizeof(double));
+    W.off_x = off;
+    off = al256(off + (size_t)2 * chunk * n_ao * sizeof(double));
+  }
+  W.bytes = off;
+  return W;
+}
+
+int check_nu_basis(const gdft_basis *b, const char *who, ShellView &B) {
+  if (b == nullptr || b->d_shell == nullptr || b->d_centre == nullptr || b->d_exp == nullptr ||
+      b->d_coef == nullptr || b->d_ao == nullptr || b->d_trans == nullptr || b->n_shell <= 0 || b->n_ao <= 0) {
+    set_error("%s: a basis with all of its tables is required", who);
+    return GDFT_ERR_INVALID;
+  }
+  B = ShellView{b->d_shell, b->d_centre, b->d_exp, b->d_coef, b->d_ao, b->d_trans,
+                b->n_shell, b->n_ao,    b->n_prim, b->n_coef, b->n_trans};
+  return GDFT_OK;
+}
+
+// Setup (Boys table, pair list, primitive pairs for omega) and the nu launches for points [p_begin, p_begin + n_pts).
+int run_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, const double *coords,
+           int64_t p_begin, int64_t n_pts, NuOut out, const char *who, cudaStream_t st) {
+  const double *boys_tab = (const double *)(ws + W.off_boys);
+  const int32_t *pairs = (const int32_t *)(ws + W.off_pairs);
+  const double *pp = (const double *)(ws + W.off_pp);
+  const unsigned gx = (unsigned)((n_pts + 31) / 32);
+  int rc;
+#define GDFT_NU_CLASS(LA, LB)                                                                                     \
+  {                                                                                                               \
+    const int c = LA * (LA + 1) / 2 + LB, lo = plan.class_lo[c], hi = plan.class_lo[c + 1];                        \
+    if (hi > lo) {                                                                                                \
+      if ((hi - lo + 7) / 8 > 65535) {                                                                            \
+        set_error("%s: %d shell pairs of one class exceed one launch", who, hi - lo);                            \
+        return GDFT_ERR_UNSUPPORTED;                                                                              \
+      }                                                                                                           \
+      const dim3 grid(gx, (unsigned)((hi - lo + 7) / 8));                                                         \
+      nu_kernel<LA, LB><<<grid, 256, 0, st>>>(B, pairs, lo, hi, pp, plan.n_pp, boys_tab, coords, p_begin, n_pts,  \
+                                              out);                                                               \
+      if ((rc = check_cuda(cudaGetLastError(), who))) return rc;                                                  \
+    }                                                                                                             \
+  }
+  GDFT_NU_CLASS(0, 0)
+  GDFT_NU_CLASS(1, 0)
+  GDFT_NU_CLASS(1, 1)
+  GDFT_NU_CLASS(2, 0)
+  GDFT_NU_CLASS(2, 1)
+  GDFT_NU_CLASS(2, 2)
+#undef GDFT_NU_CLASS
+  return GDFT_OK;
+}
+
+int setup_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, double omega, bool first,
+             const char *who, cudaStream_t st) {
+  int rc;
+  if (first) {
+    boys_table_kernel<<<(kBoysPts * kBoysN + 255) / 256, 256, 0, st>>>((double *)(ws + W.off_boys));
+    if ((rc = check_cuda(cudaGetLastError(), who))) return rc;
+    if ((rc = check_cuda(cudaMemcpyAsync(ws + W.off_pairs, plan.pairs.data(), plan.pairs.size() * sizeof(int32_t),
+                                         cudaMemcpyHostToDevice, st),
+                         who)))
+      return rc;
+  }
+  const int np = (int)(plan.pairs.size() / 4);
+  nu_pair_setup_kernel<<<(np + 127) / 128, 128, 0, st>>>(B, (const int32_t *)(ws + W.off_pairs), np, omega,
+                                                         (double *)(ws + W.off_pp), plan.n_pp);
+  return check_cuda(cudaGetLastError(), who);
+}
+
+}  // namespace
+
+}  // namespace gdft
+
+using namespace gdft;
+
+extern "C" {
+
+int gdft_nu_workspace_bytes(const gdft_basis *basis, int64_t chunk, size_t *bytes) {
+  const char *who = "gdft_nu_workspace_bytes";
+  ShellView B;
+  int rc = check_nu_basis(basis, who, B);
+  if (rc) return rc;
+  if (bytes == nullptr || chunk < 0) {
+    set_error("%s: invalid arguments", who);
+    return GDFT_ERR_INVALID;
+  }
+  PairPlan plan;
+  if ((rc = make_plan(basis, plan, who))) return rc;
+  *bytes = nu_ws(plan, basis->n_ao, chunk, chunk > 0).bytes;
+  return GDFT_OK;
+}
+
+int gdft_nu_integrals(const gdft_basis *basis, const double *d_coords, int64_t n_grid, double omega, double *d_nu,
+                      void *d_ws, size_t ws_bytes, void *stream) {
+  const char *who = "gdft_nu_integrals";
+  ShellView B;
+  int rc = check_nu_basis(basis, who, B);
+  if (rc) return rc;
+  if (d_coords == nullptr || d_nu == nullptr || d_ws == nullptr || n_grid <= 0 || !(omega >= 0.0)) {
+    set_error("%s: coords, nu and the workspace are required, n_grid > 0 and omega >= 0 (got %g)", who, omega);
+    return GDFT_ERR_INVALID;
+  }
+  if ((((uintptr_t)d_coords | (uintptr_t)d_nu) & 7u) || ((uintptr_t)d_ws & 255u)) {
+    set_error("%s: coords and nu must be 8-byte aligned, the workspace 256-byte aligned", who);
+    return GDFT_ERR_ALIGNMENT;
+  }
+  PairPlan plan;
+  if ((rc = make_plan(basis, plan, who))) return rc;
+  const NuWs W = nu_ws(plan, basis->n_ao, 0, false);
+  if (ws_bytes < W.bytes) {
+    set_error("%s: workspace of %zu bytes, %zu needed", who, ws_bytes, W.bytes);
+    return GDFT_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if ((rc = setup_nu(B, plan, W, (char *)d_ws, omega, true, who, st))) return rc;
+  const int n = basis->n_ao;
+  const NuOut out{d_nu, 1, (int64_t)n * n, n};  // (grid, ao, ao)
+  rc = run_nu(B, plan, W, (char *)d_ws, d_coords, 0, n_grid, out, who, st);
+  if (rc) return rc;
+  // the pair list is copied from host memory that goes out of scope here
+  return check_cuda(cudaStreamSynchronize(st), who);
+}
+
+int gdft_chi(const gdft_basis *basis, const double *d_coords, const double *d_ao, const double *d_rdm1,
+             int64_t n_grid, const double *h_omegas, int32_t n_omega, int64_t chunk, double *d_chi, void *d_ws,
+             size_t ws_bytes, void *stream) {
+  const char *who = "gdft_chi";
+  ShellView B;
+  int rc = check_nu_basis(basis, who, B);
+  if (rc) return rc;
+  if (d_coords == nullptr || d_ao == nullptr || d_rdm1 == nullptr || d_chi == nullptr || d_ws == nullptr ||
+      h_omegas == nullptr || n_grid <= 0 || n_omega <= 0 || chunk <= 0) {
+    set_error("%s: coords, ao, rdm1, omegas, chi and the workspace are required; n_grid, n_omega, chunk > 0", who);
+    return GDFT_ERR_INVALID;
+  }
+  for (int w = 0; w < n_omega; ++w)
+    if (!(h_omegas[w] >= 0.0)) {
+      set_error("Range-separated parameter omega must be non-negative!");
+      return GDFT_ERR_INVALID;
+    }
+  if ((((uintptr_t)d_coords | (uintptr_t)d_ao | (uintptr_t)d_rdm1 | (uintptr_t)d_chi) & 7u) ||
+      ((uintptr_t)d_ws & 255u)) {
+    set_error("%s: arrays must be 8-byte aligned, the workspace 256-byte aligned", who);
+    return GDFT_ERR_ALIGNMENT;
+  }
+  PairPlan plan;
+  if ((rc = make_plan(basis, plan, who))) return rc;
+  const int n = basis->n_ao;
+  const int64_t pc = chunk < n_grid ? chunk : n_grid;
+  const NuWs W = nu_ws(plan, n, pc, true);
+  if (ws_bytes < W.bytes) {
+    set_error("%s: workspace of %zu bytes, %zu needed", who, ws_bytes, W.bytes);
+    return GDFT_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  double *nu = (double *)(ws + W.off_nu);
+  double *X = (double *)(ws + W.off_x);
+  for (int w = 0; w < n_omega; ++w) {
+    if ((rc = setup_nu(B, plan, W, ws, h_omegas[w], w == 0, who, st))) return rc;
+    for (int64_t p0 = 0; p0 < n_grid; p0 += pc) {
+      const int64_t np_ = n_grid - p0 < pc ? n_grid - p0 : pc;
+      // X_s = ao[p0 : p0 + np_] D_s
+      for (int s = 0; s < 2; ++s)
+        if ((rc = check_cuda(gemm<kNN>((int)np_, n, n, d_ao + p0 * n, n, d_rdm1 + (size_t)s * n * n, n,
+                                       X + (size_t)s * pc * n, n, 0.0, st),
+                             who)))
+          return rc;
+      const NuOut out{nu, pc, 1, n};  // [a][b][point]
+      if ((rc = run_nu(B, plan, W, ws, d_coords, p0, np_, out, who, st))) return rc;
+      const dim3 grid((unsigned)((np_ + 31) / 32), (unsigned)((n + 31) / 32));
+      chi_kernel<<<grid, 256, 0, st>>>(X, nu, np_, pc, n, n_omega, w, d_chi, p0);
+      if ((rc = check_cuda(cudaGetLastError(), who))) return rc;
+    }
+  }
+  return check_cuda(cudaStreamSynchronize(st), who);
+}
+
+}  // extern "C"

@@ -156,6 +156,28 @@ int gdft_eval_ao(const gdft_basis *basis, const double *d_coords, int64_t n_grid
 int gdft_molecule_eval_shells(const gdft_molecule *mol, const gdft_basis *basis, const double *d_coords,
                               const double *d_weights, void *stream);
 
+/* nu integrals and the chi tensor (range-separated exact exchange inputs).
+ *   nu_ab(r) = int phi_a(r') phi_b(r') erf(omega |r - r'|) / |r - r'| dr'  (omega = 0: 1/|r - r'|),
+ * PySCF's int1e_grids as _evaluate_nu / _nu_chunk call it (external/_hf_density.py:17-120), and
+ *   chi[r][w][s][a] = sum_(b,d) D_s[b][d] phi_b(r) nu^(omega_w)_da(r),
+ * generate_chi_tensor (interface/pyscf.py:1067-1126).  Shells up to l = 2
+ * (GDFT_ERR_UNSUPPORTED beyond).  Both calls read the basis's shell table back
+ * to the host to plan the shell pairs and synchronise `stream` before returning. */
+
+/* Workspace bytes: chunk = 0 for gdft_nu_integrals, the chunk of grid points
+ * for gdft_chi (its nu buffer holds n_ao^2 * chunk doubles). */
+int gdft_nu_workspace_bytes(const gdft_basis *basis, int64_t chunk, size_t *bytes);
+
+/* d_nu: (n_grid, n_ao, n_ao); omega >= 0. */
+int gdft_nu_integrals(const gdft_basis *basis, const double *d_coords, int64_t n_grid, double omega, double *d_nu,
+                      void *d_ws, size_t ws_bytes, void *stream);
+
+/* d_ao: (n_grid, n_ao) phi on the grid; d_rdm1: (2, n_ao, n_ao); h_omegas: n_omega
+ * host values >= 0; d_chi: (n_grid, n_omega, 2, n_ao). */
+int gdft_chi(const gdft_basis *basis, const double *d_coords, const double *d_ao, const double *d_rdm1,
+             int64_t n_grid, const double *h_omegas, int32_t n_omega, int64_t chunk, double *d_chi, void *d_ws,
+             size_t ws_bytes, void *stream);
+
 /* Workspace bytes for the calls below on this molecule. */
 int gdft_workspace_bytes(const gdft_molecule *mol, size_t *bytes);
 
