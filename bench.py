@@ -684,6 +684,73 @@ def run_ao(args):
     print(json.dumps(line))
 
 
+def run_chi(args):
+    """chi for DM21's two omegas (generate_chi_tensor) from an l <= 2 contracted basis: grid-pts/s."""
+    import torch
+
+    from oracle import nu as ONU
+    from oracle import shells as OS
+    from graddft_gb300 import build, chi, synthetic
+    from graddft_gb300 import basis as B
+
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    n_grid = args.n_grid if args.n_grid != N_GRID else 1 << 16
+    n_atoms = max(1, (args.n_ao if args.n_ao != N_AO else 128) // 23)
+    full = contracted_basis(n_atoms)
+    basis = B.ShellBasis([s for s in full.shells if s.l <= 2])  # per atom 4 s, 3 p, 2 d = 23 AOs
+    n_ao = basis.n_ao
+    coords, w = synthetic.make_grid(n_grid, SEED)
+    g = np.random.default_rng(SEED)
+    m = g.standard_normal((2, n_ao, n_ao))
+    rdm1 = np.einsum("sab,scb->sac", m, m) / n_ao
+    c_d = torch.as_tensor(coords, device=dev)
+    ao = B.eval_ao(basis, c_d, deriv=0)
+    rdm1_d = torch.as_tensor(rdm1, device=dev)
+    omegas = [0.0, 0.4]
+    chunk = 4096
+
+    def step():
+        return chi.generate_chi_tensor(rdm1_d, ao, c_d, basis, omegas, chunk_size=chunk)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 3))
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            out = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    n_pp = sum(len(a.exps) * len(b.exps) for i, a in enumerate(basis.shells) for b in basis.shells[:i + 1])
+    line = {
+        "metric": "chi tensor (generate_chi_tensor, omegas 0 and 0.4), grid-pts/s", "value": n_grid / (ms * 1e-3),
+        "unit": "grid-pts/s", "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded contracted basis up to d, random positive semi-definite rdm1, uniform grid)",
+        "config": {"workload": f"generate_chi_tensor: {n_atoms} atoms x (4s 3p 2d) = {n_ao} AOs, n_grid {n_grid}, "
+                               f"omegas (0, 0.4), chunk {chunk}", "n_ao": n_ao, "n_grid": n_grid,
+                   "primitive_pairs": n_pp, "chi_gib": out.numel() * 8 / 2**30},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        n_s = 8
+        spec = [(s.centre, s.l, s.exps, s.coefs, None) for s in basis.shells]
+        t0 = time.perf_counter()
+        a_s, _, _ = OS.eval_shells(spec, coords[:n_s])
+        ONU.generate_chi(rdm1, a_s, [ONU.nu_integrals(spec, coords[:n_s], wv) for wv in omegas])
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_s / dt, "unit": "grid-pts/s", "cores": 1, "kind": "port",
+                                "sample": f"{n_s} grid points ({dt:.1f} s), numpy McMurchie-Davidson restatement "
+                                          "(oracle/nu.py) and the reference's chi einsum"}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -698,10 +765,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
-    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch", "hf", "ao"],
+    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch", "hf", "ao", "chi"],
                     help="xc: B88+LYP contraction benchmark (headline); neural: DM21-style network fwd+bwd; "
                          "scf: differentiable SCF loop; batch: many molecules per step; hf: DM21 predict with "
-                         "its exact-exchange terms from a chi tensor; ao: AO tables from contracted shells")
+                         "its exact-exchange terms from a chi tensor; ao: AO tables from contracted shells; chi: the chi tensor from range-separated integrals")
     ap.add_argument("--n-mol", type=int, default=64, help="molecules (--workload batch)")
     ap.add_argument("--points-per-ao", type=int, default=150, help="grid points per AO (--workload batch)")
     ap.add_argument("--cycles", type=int, default=20, help="SCF iterations (--workload scf)")
@@ -720,6 +787,8 @@ def main():
         return run_hf(args)
     if args.workload == "ao":
         return run_ao(args)
+    if args.workload == "chi":
+        return run_chi(args)
 
     import torch
 

@@ -24,6 +24,7 @@ from . import _lib, engine
 from .basis import ShellBasis
 
 F64 = torch.float64
+MAX_OMEGA = 8
 
 
 def _as_basis(mol) -> ShellBasis:
@@ -74,6 +75,9 @@ def generate_chi_tensor(rdm1, ao, grid_coords, mol, omegas: Sequence[float], chu
         return torch.zeros((0,), dtype=F64, device=dev)
     if any(w < 0 for w in omegas):
         raise ValueError("Range-separated parameter omega must be non-negative!")
+    if len(omegas) > MAX_OMEGA:  # one library call takes up to MAX_OMEGA
+        return torch.cat([generate_chi_tensor(rdm1, ao, grid_coords, mol, omegas[i:i + MAX_OMEGA], chunk_size,
+                                              device=dev) for i in range(0, len(omegas), MAX_OMEGA)], dim=1)
     basis = _as_basis(mol)
     ao = engine.as_device_f64(ao, dev)
     rdm1 = engine.as_device_f64(rdm1, dev)

@@ -36,13 +36,16 @@ namespace gdft {
 namespace {
 
 constexpr int kNuMaxL = 2;                 // shells up to d
+constexpr int kMaxOmega = 8;               // omegas of one gdft_chi call
 constexpr int kBoysN = 17;                 // F_0 .. F_16 tabulated
 constexpr int kBoysPts = 601;              // T = 0, 0.1, ..., 60
 constexpr double kBoysStep = 0.1;
 constexpr double kBoysTMax = 60.0;
 constexpr int kETab = 3 * 3 * 5;           // E[i][j][t], i, j <= 2, t <= 4 (per dimension)
-constexpr int kPPStride = 8 + 3 * kETab;   // mu, pref, P(3), p, 2 pad, E[x|y|z]
+constexpr int kE3Max = 336;                // Hermite products of a d-d primitive pair
+constexpr int kPPStride = 8 + kE3Max;      // mu, screened flag, P(3), p, 2 pad, products
 constexpr double kPi = 3.14159265358979323846;
+constexpr double kScreen = 1e-30;          // product-overlap prefactor below which a primitive pair is skipped
 
 __global__ void boys_table_kernel(double *__restrict__ tab) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -87,7 +90,11 @@ __device__ __forceinline__ void boys(const double *__restrict__ tab, double T, d
 
 __device__ __forceinline__ int e_idx(int i, int j, int t) { return (i * 3 + j) * 5 + t; }
 
-// One thread per shell pair: the primitive-pair records (mu, prefactor, P, Hermite E tables).
+// One thread per shell pair: the primitive-pair records.  Besides mu and P,
+// a record holds, for every pair of cartesian components (qa, qb) in PySCF's
+// order and every (t, u, v) with t <= ia + ib, u <= ka + kb, v <= ma + mb, the
+// product pref * E^x_t E^y_u E^z_v (pref = (2 pi / p) sqrt(mu / p)): the same for
+// all grid points, so the per-point work is one FMA per term.
 __global__ void nu_pair_setup_kernel(ShellView B, const int32_t *__restrict__ pairs, int n_pairs, double omega,
                                      double *__restrict__ pp, int64_t n_pp) {
   const int ip = blockIdx.x * blockDim.x + threadIdx.x;
@@ -104,26 +111,46 @@ __global__ void nu_pair_setup_kernel(ShellView B, const int32_t *__restrict__ pa
       const double a = B.exps[r1.poff + i1], b = B.exps[r2.poff + i2];
       const double p = a + b, ip2 = 0.5 / p;
       const double mu = omega == 0.0 ? p : p * omega * omega / (p + omega * omega);
+      const double pref = (2.0 * kPi / p) * sqrt(mu / p);
       rec[0] = mu;
-      rec[1] = (2.0 * kPi / p) * sqrt(mu / p);
       rec[5] = p;
+      double E[3][kETab];
       for (int d = 0; d < 3; ++d) {
         const double P = (a * A[d] + b * Bc[d]) / p;
         rec[2 + d] = P;
         const double xab = A[d] - Bc[d], xpa = P - A[d], xpb = P - Bc[d];
-        double *E = rec + 8 + d * kETab;
-        for (int q = 0; q < kETab; ++q) E[q] = 0.0;
-        E[e_idx(0, 0, 0)] = exp(-a * b / p * xab * xab);
+        for (int q = 0; q < kETab; ++q) E[d][q] = 0.0;
+        E[d][e_idx(0, 0, 0)] = exp(-a * b / p * xab * xab);
         for (int i = 0; i < r1.l; ++i)
           for (int t = 0; t <= i + 1; ++t)
-            E[e_idx(i + 1, 0, t)] = (t > 0 ? ip2 * E[e_idx(i, 0, t - 1)] : 0.0) + xpa * E[e_idx(i, 0, t)] +
-                                    (t + 1 <= i ? (t + 1) * E[e_idx(i, 0, t + 1)] : 0.0);
+            E[d][e_idx(i + 1, 0, t)] = (t > 0 ? ip2 * E[d][e_idx(i, 0, t - 1)] : 0.0) + xpa * E[d][e_idx(i, 0, t)] +
+                                       (t + 1 <= i ? (t + 1) * E[d][e_idx(i, 0, t + 1)] : 0.0);
         for (int j = 0; j < r2.l; ++j)
           for (int i = 0; i <= r1.l; ++i)
             for (int t = 0; t <= i + j + 1; ++t)
-              E[e_idx(i, j + 1, t)] = (t > 0 ? ip2 * E[e_idx(i, j, t - 1)] : 0.0) + xpb * E[e_idx(i, j, t)] +
-                                      (t + 1 <= i + j ? (t + 1) * E[e_idx(i, j, t + 1)] : 0.0);
+              E[d][e_idx(i, j + 1, t)] = (t > 0 ? ip2 * E[d][e_idx(i, j, t - 1)] : 0.0) +
+                                         xpb * E[d][e_idx(i, j, t)] +
+                                         (t + 1 <= i + j ? (t + 1) * E[d][e_idx(i, j, t + 1)] : 0.0);
       }
+      // screening: a Gaussian product of overlap prefactor below 1e-30 contributes
+      // nothing at double precision to any point's integrals (the Hermite integrals
+      // grow at most like (2 mu)^(L/2), far from closing the gap for l <= 2)
+      rec[1] = E[0][0] * E[1][0] * E[2][0] < kScreen ? 1.0 : 0.0;
+      double *E3 = rec + 8;
+      int idx = 0;
+      for (int ia = r1.l; ia >= 0; --ia)
+        for (int ka = r1.l - ia; ka >= 0; --ka) {
+          const int ma = r1.l - ia - ka;
+          for (int ib = r2.l; ib >= 0; --ib)
+            for (int kb = r2.l - ib; kb >= 0; --kb) {
+              const int mb = r2.l - ib - kb;
+              for (int t = 0; t <= ia + ib; ++t)
+                for (int u = 0; u <= ka + kb; ++u)
+                  for (int v = 0; v <= ma + mb; ++v)
+                    if (idx < kE3Max)
+                      E3[idx++] = pref * E[0][e_idx(ia, ib, t)] * E[1][e_idx(ka, kb, u)] * E[2][e_idx(ma, mb, v)];
+            }
+        }
     }
   }
 }
@@ -249,14 +276,16 @@ __global__ void __launch_bounds__(256) nu_kernel(ShellView B, const int32_t *__r
         const double ca = B.coef[r1.coff + (int64_t)c1 * r1.np + i1];
         for (int i2 = 0; i2 < r2.np; ++i2) {
           const double *rec = pp + (off + (int64_t)i1 * r2.np + i2) * kPPStride;
-          const double cc = ca * B.coef[r2.coff + (int64_t)c2 * r2.np + i2] * rec[1];
+          if (rec[1] != 0.0) continue;  // screened (uniform across the warp)
+          const double cc = ca * B.coef[r2.coff + (int64_t)c2 * r2.np + i2];
           const double mu = rec[0];
           const double X = rec[2] - Cx, Y = rec[3] - Cy, Z = rec[4] - Cz;
           double F[L + 1];
           boys<L>(boys_tab, mu * (X * X + Y * Y + Z * Z), F);
           double R[L + 1][L + 1][L + 1];
           hermite_r<L>(F, mu, X, Y, Z, R);
-          const double *Ex = rec + 8, *Ey = rec + 8 + kETab, *Ez = rec + 8 + 2 * kETab;
+          const double *E3 = rec + 8;
+          int idx = 0;
 #pragma unroll
           for (int qa = 0; qa < NA; ++qa) {
             const int ia = CartPow<LA>::x(qa), ka = CartPow<LA>::y(qa), ma = CartPow<LA>::z(qa);
@@ -267,15 +296,14 @@ __global__ void __launch_bounds__(256) nu_kernel(ShellView B, const int32_t *__r
 #pragma unroll
               for (int t = 0; t <= L; ++t) {
                 if (t > ia + ib) continue;
-                const double ex = Ex[e_idx(ia, ib, t)];
 #pragma unroll
                 for (int u = 0; u <= L; ++u) {
                   if (u > ka + kb) continue;
-                  const double exy = ex * Ey[e_idx(ka, kb, u)];
 #pragma unroll
                   for (int v = 0; v <= L; ++v) {
-                    if (v > ma + mb || t + u + v > L) continue;
-                    s = fma(exy * Ez[e_idx(ma, mb, v)], R[t][u][v], s);
+                    if (v > ma + mb) continue;
+                    s = fma(E3[idx], R[t][u][v], s);
+                    ++idx;
                   }
                 }
               }
@@ -427,7 +455,7 @@ struct NuWs {
   size_t off_boys, off_pairs, off_pp, off_nu, off_x, bytes;
 };
 
-NuWs nu_ws(const PairPlan &plan, int n_ao, int64_t chunk, bool want_chi) {
+NuWs nu_ws(const PairPlan &plan, int n_ao, int64_t chunk, bool want_chi, int n_omega) {
   NuWs W;
   size_t off = 0;
   W.off_boys = off;
@@ -435,7 +463,7 @@ NuWs nu_ws(const PairPlan &plan, int n_ao, int64_t chunk, bool want_chi) {
   W.off_pairs = off;
   off = al256(off + plan.pairs.size() * sizeof(int32_t));
   W.off_pp = off;
-  off = al256(off + (size_t)plan.n_pp * kPPStride * sizeof(double));
+  off = al256(off + (size_t)n_omega * plan.n_pp * kPPStride * sizeof(double));
   W.off_nu = off;
   W.off_x = off;
   if (want_chi) {
@@ -459,11 +487,11 @@ int check_nu_basis(const gdft_basis *b, const char *who, ShellView &B) {
 }
 
 // Setup (Boys table, pair list, primitive pairs for omega) and the nu launches for points [p_begin, p_begin + n_pts).
-int run_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, const double *coords,
+int run_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, int w, const double *coords,
            int64_t p_begin, int64_t n_pts, NuOut out, const char *who, cudaStream_t st) {
   const double *boys_tab = (const double *)(ws + W.off_boys);
   const int32_t *pairs = (const int32_t *)(ws + W.off_pairs);
-  const double *pp = (const double *)(ws + W.off_pp);
+  const double *pp = (const double *)(ws + W.off_pp) + (size_t)w * plan.n_pp * kPPStride;
   const unsigned gx = (unsigned)((n_pts + 31) / 32);
   int rc;
 #define GDFT_NU_CLASS(LA, LB)                                                                                     \
@@ -490,7 +518,7 @@ int run_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, co
   return GDFT_OK;
 }
 
-int setup_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, double omega, bool first,
+int setup_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, int w, double omega, bool first,
              const char *who, cudaStream_t st) {
   int rc;
   if (first) {
@@ -502,8 +530,9 @@ int setup_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, 
       return rc;
   }
   const int np = (int)(plan.pairs.size() / 4);
-  nu_pair_setup_kernel<<<(np + 127) / 128, 128, 0, st>>>(B, (const int32_t *)(ws + W.off_pairs), np, omega,
-                                                         (double *)(ws + W.off_pp), plan.n_pp);
+  nu_pair_setup_kernel<<<(np + 127) / 128, 128, 0, st>>>(
+      B, (const int32_t *)(ws + W.off_pairs), np, omega,
+      (double *)(ws + W.off_pp) + (size_t)w * plan.n_pp * kPPStride, plan.n_pp);
   return check_cuda(cudaGetLastError(), who);
 }
 
@@ -526,7 +555,7 @@ int gdft_nu_workspace_bytes(const gdft_basis *basis, int64_t chunk, size_t *byte
   }
   PairPlan plan;
   if ((rc = make_plan(basis, plan, who))) return rc;
-  *bytes = nu_ws(plan, basis->n_ao, chunk, chunk > 0).bytes;
+  *bytes = nu_ws(plan, basis->n_ao, chunk, chunk > 0, chunk > 0 ? kMaxOmega : 1).bytes;
   return GDFT_OK;
 }
 
@@ -546,16 +575,16 @@ int gdft_nu_integrals(const gdft_basis *basis, const double *d_coords, int64_t n
   }
   PairPlan plan;
   if ((rc = make_plan(basis, plan, who))) return rc;
-  const NuWs W = nu_ws(plan, basis->n_ao, 0, false);
+  const NuWs W = nu_ws(plan, basis->n_ao, 0, false, 1);
   if (ws_bytes < W.bytes) {
     set_error("%s: workspace of %zu bytes, %zu needed", who, ws_bytes, W.bytes);
     return GDFT_ERR_WORKSPACE;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  if ((rc = setup_nu(B, plan, W, (char *)d_ws, omega, true, who, st))) return rc;
+  if ((rc = setup_nu(B, plan, W, (char *)d_ws, 0, omega, true, who, st))) return rc;
   const int n = basis->n_ao;
   const NuOut out{d_nu, 1, (int64_t)n * n, n};  // (grid, ao, ao)
-  rc = run_nu(B, plan, W, (char *)d_ws, d_coords, 0, n_grid, out, who, st);
+  rc = run_nu(B, plan, W, (char *)d_ws, 0, d_coords, 0, n_grid, out, who, st);
   if (rc) return rc;
   // the pair list is copied from host memory that goes out of scope here
   return check_cuda(cudaStreamSynchronize(st), who);
@@ -569,8 +598,9 @@ int gdft_chi(const gdft_basis *basis, const double *d_coords, const double *d_ao
   int rc = check_nu_basis(basis, who, B);
   if (rc) return rc;
   if (d_coords == nullptr || d_ao == nullptr || d_rdm1 == nullptr || d_chi == nullptr || d_ws == nullptr ||
-      h_omegas == nullptr || n_grid <= 0 || n_omega <= 0 || chunk <= 0) {
-    set_error("%s: coords, ao, rdm1, omegas, chi and the workspace are required; n_grid, n_omega, chunk > 0", who);
+      h_omegas == nullptr || n_grid <= 0 || n_omega <= 0 || n_omega > kMaxOmega || chunk <= 0) {
+    set_error("%s: coords, ao, rdm1, omegas, chi and the workspace are required; n_grid, chunk > 0, "
+              "1 <= n_omega <= %d", who, kMaxOmega);
     return GDFT_ERR_INVALID;
   }
   for (int w = 0; w < n_omega; ++w)
@@ -587,7 +617,7 @@ int gdft_chi(const gdft_basis *basis, const double *d_coords, const double *d_ao
   if ((rc = make_plan(basis, plan, who))) return rc;
   const int n = basis->n_ao;
   const int64_t pc = chunk < n_grid ? chunk : n_grid;
-  const NuWs W = nu_ws(plan, n, pc, true);
+  const NuWs W = nu_ws(plan, n, pc, true, n_omega);
   if (ws_bytes < W.bytes) {
     set_error("%s: workspace of %zu bytes, %zu needed", who, ws_bytes, W.bytes);
     return GDFT_ERR_WORKSPACE;
@@ -596,18 +626,19 @@ int gdft_chi(const gdft_basis *basis, const double *d_coords, const double *d_ao
   char *ws = (char *)d_ws;
   double *nu = (double *)(ws + W.off_nu);
   double *X = (double *)(ws + W.off_x);
-  for (int w = 0; w < n_omega; ++w) {
-    if ((rc = setup_nu(B, plan, W, ws, h_omegas[w], w == 0, who, st))) return rc;
-    for (int64_t p0 = 0; p0 < n_grid; p0 += pc) {
-      const int64_t np_ = n_grid - p0 < pc ? n_grid - p0 : pc;
-      // X_s = ao[p0 : p0 + np_] D_s
-      for (int s = 0; s < 2; ++s)
-        if ((rc = check_cuda(gemm<kNN>((int)np_, n, n, d_ao + p0 * n, n, d_rdm1 + (size_t)s * n * n, n,
-                                       X + (size_t)s * pc * n, n, 0.0, st),
-                             who)))
-          return rc;
+  for (int w = 0; w < n_omega; ++w)
+    if ((rc = setup_nu(B, plan, W, ws, w, h_omegas[w], w == 0, who, st))) return rc;
+  for (int64_t p0 = 0; p0 < n_grid; p0 += pc) {
+    const int64_t np_ = n_grid - p0 < pc ? n_grid - p0 : pc;
+    // X_s = ao[p0 : p0 + np_] D_s, shared by the omegas
+    for (int s = 0; s < 2; ++s)
+      if ((rc = check_cuda(gemm<kNN>((int)np_, n, n, d_ao + p0 * n, n, d_rdm1 + (size_t)s * n * n, n,
+                                     X + (size_t)s * pc * n, n, 0.0, st),
+                           who)))
+        return rc;
+    for (int w = 0; w < n_omega; ++w) {
       const NuOut out{nu, pc, 1, n};  // [a][b][point]
-      if ((rc = run_nu(B, plan, W, ws, d_coords, p0, np_, out, who, st))) return rc;
+      if ((rc = run_nu(B, plan, W, ws, w, d_coords, p0, np_, out, who, st))) return rc;
       const dim3 grid((unsigned)((np_ + 31) / 32), (unsigned)((n + 31) / 32));
       chi_kernel<<<grid, 256, 0, st>>>(X, nu, np_, pc, n, n_omega, w, d_chi, p0);
       if ((rc = check_cuda(cudaGetLastError(), who))) return rc;

@@ -165,7 +165,7 @@ int gdft_molecule_eval_shells(const gdft_molecule *mol, const gdft_basis *basis,
  * to the host to plan the shell pairs and synchronise `stream` before returning. */
 
 /* Workspace bytes: chunk = 0 for gdft_nu_integrals, the chunk of grid points
- * for gdft_chi (its nu buffer holds n_ao^2 * chunk doubles). */
+ * for gdft_chi (its nu buffer holds n_ao^2 * chunk doubles; up to 8 omegas). */
 int gdft_nu_workspace_bytes(const gdft_basis *basis, int64_t chunk, size_t *bytes);
 
 /* d_nu: (n_grid, n_ao, n_ao); omega >= 0. */

@@ -88,6 +88,18 @@ def test_random_basis_vs_oracle(G, cart):
                what=f"nu cart={cart} omega={omega}")
 
 
+def test_chi_many_omegas(G, golden):
+    """More omegas than one library call takes: split and concatenated in omega order."""
+    g = golden("chi")
+    basis, spec = _fixture_basis(G, g)
+    sl = slice(0, 40)
+    omegas = [0.0, 0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 1.0]
+    chi = G.chi.generate_chi_tensor(g["rdm1"], g["ao"][sl], g["coords"][sl], basis, omegas, chunk_size=16)
+    assert chi.shape == (40, 10, 2, 30)
+    ref = ONU.generate_chi(g["rdm1"], g["ao"][sl], [ONU.nu_integrals(spec, g["coords"][sl], w) for w in omegas])
+    _close(chi, ref, what="chi 10 omegas")
+
+
 def test_chi_feeds_hf_energy_density(G, golden):
     """chi generated on the device gives the oracle's HF energy density (molecule.py:507-541)."""
     import oracle as O
