@@ -34,6 +34,7 @@ from .train import energy_predictor
 from .scf import JittableDiis, diff_scf_loop, diff_simple_scf_loop, safe_eigh, safe_fock_solver, safe_general_eigh
 from .basis import ShellBasis, eval_ao, molecule_from_basis
 from . import chi
+from .solid import KPointInfo, Solid
 from .chi import generate_chi_tensor
 from .neural import DM21, NeuralFunctional, dm21_coefficient_inputs, dm21_hfgrads_cinputs, dm21_hfgrads_densities
 
@@ -45,5 +46,5 @@ __all__ = [
     "energy_predictor", "DM21", "NeuralFunctional", "dm21_coefficient_inputs", "dm21_hfgrads_cinputs",
     "dm21_hfgrads_densities", "diff_simple_scf_loop", "diff_scf_loop", "JittableDiis", "safe_eigh",
     "safe_fock_solver", "safe_general_eigh", "ShellBasis", "eval_ao", "molecule_from_basis",
-    "generate_chi_tensor",
+    "generate_chi_tensor", "Solid", "KPointInfo",
 ]

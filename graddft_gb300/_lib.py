@@ -31,7 +31,8 @@ MAX_COLS = 8
 EXPORTS = (
     "gdft_abi_version", "gdft_last_error", "gdft_molecule_bytes", "gdft_molecule_init", "gdft_molecule_load",
     "gdft_molecule_eval_basis", "gdft_eval_ao", "gdft_molecule_eval_shells", "gdft_nu_workspace_bytes",
-    "gdft_nu_integrals", "gdft_chi", "gdft_workspace_bytes",
+    "gdft_nu_integrals", "gdft_chi", "gdft_kpoint_workspace_bytes", "gdft_kpoint_density",
+    "gdft_kpoint_xc_energy_and_grads", "gdft_kpoint_coulomb", "gdft_kpoint_fock", "gdft_workspace_bytes",
     "gdft_density", "gdft_xc_energy_and_grads",
     "gdft_energy_densities", "gdft_vxc_from_potentials", "gdft_integrate", "gdft_integrate_workspace_bytes", "gdft_integrate_noalloc", "gdft_fock", "gdft_coulomb",
     "gdft_profile_enable", "gdft_profile_reset", "gdft_profile_read", "gdft_device_status", "gdft_selftest_umma",
@@ -119,6 +120,12 @@ _SIGS = {
     "gdft_eval_ao": ([PBAS, P, I64, I32, P, P, P, P], ctypes.c_int),
     "gdft_molecule_eval_shells": ([PMOL, PBAS, P, P, P], ctypes.c_int),
     "gdft_nu_workspace_bytes": ([PBAS, I64, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_kpoint_workspace_bytes": ([PMOL, I32, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_kpoint_coulomb": ([I32, I32, P, P, P, P, D, P, P, P], ctypes.c_int),
+    "gdft_kpoint_fock": ([I32, I32, P, P, P, D, P, P], ctypes.c_int),
+    "gdft_kpoint_density": ([PMOL, I32, P, ctypes.POINTER(ctypes.c_double), P, P, P, P, P, SZ, P], ctypes.c_int),
+    "gdft_kpoint_xc_energy_and_grads": ([PMOL, I32, P, ctypes.POINTER(ctypes.c_double), PFN, P, P, P, SZ, P],
+                                        ctypes.c_int),
     "gdft_nu_integrals": ([PBAS, P, I64, ctypes.c_double, P, P, SZ, P], ctypes.c_int),
     "gdft_chi": ([PBAS, P, P, P, I64, ctypes.POINTER(ctypes.c_double), I32, I64, P, P, SZ, P], ctypes.c_int),
     "gdft_workspace_bytes": ([PMOL, ctypes.POINTER(SZ)], ctypes.c_int),

@@ -635,6 +635,183 @@ int gdft_xc_energy_grads_hf(const gdft_molecule *mol, const double *d_rdm1, cons
 }
 
 
+// ---- k-points (Solid) ------------------------------------------------------
+// Workspace: one molecule's layout, then the doubled real matrix M, the real
+// V of one k-point and the features summed over k-points.
+struct KptWs {
+  size_t off_m, off_v, off_fsum, bytes;
+};
+
+static KptWs kpt_ws(const gdft_molecule *m) {
+  KptWs K;
+  size_t off = align256(ws_layout(m).bytes);
+  const size_t mat = (size_t)2 * m->n_ao * m->n_ao * sizeof(double);
+  K.off_m = off;
+  off += align256(mat);
+  K.off_v = off;
+  off += align256(mat);
+  K.off_fsum = off;
+  off += align256((size_t)2 * kFeat * m->n_grid_pad * sizeof(double));
+  K.bytes = off;
+  return K;
+}
+
+static int check_kpts(const gdft_molecule *mols, int32_t n_kpt, const double *h_kweights, const char *who) {
+  if (mols == nullptr || n_kpt <= 0 || h_kweights == nullptr) {
+    set_error("%s: k-point molecules and weights are required (n_kpt=%d)", who, n_kpt);
+    return GDFT_ERR_INVALID;
+  }
+  for (int k = 0; k < n_kpt; ++k) {
+    int rc = check_mol(&mols[k]);
+    if (rc) return rc;
+    if (mols[k].n_grid != mols[0].n_grid || mols[k].n_ao != mols[0].n_ao ||
+        mols[k].precision != mols[0].precision || (mols[k].n_ao & 1)) {
+      set_error("%s: every k-point needs the same grid, form and an even n_ao (2 x crystal AOs)", who);
+      return GDFT_ERR_INVALID;
+    }
+  }
+  return GDFT_OK;
+}
+
+// Features summed over k-points into ws + off_fsum.
+static int kpt_density(const gdft_molecule *mols, int32_t K, const double *rdm1c, const double *h_kweights,
+                       char *ws, cudaStream_t st) {
+  const WsLayout W = ws_layout(&mols[0]);
+  const KptWs KW = kpt_ws(&mols[0]);
+  const int n = mols[0].n_ao / 2;
+  double *M = (double *)(ws + KW.off_m), *fsum = (double *)(ws + KW.off_fsum);
+  const size_t nf = (size_t)2 * kFeat * mols[0].n_grid_pad;
+  int rc;
+  for (int k = 0; k < K; ++k) {
+    if ((rc = check_cuda(launch_kpt_build_m(rdm1c, K, k, n, h_kweights[k], M, st), "kpt_build_m"))) return rc;
+    if ((rc = run_density(&mols[k], M, ws, st))) return rc;
+    if ((rc = check_cuda(launch_feat_add((const double *)(ws + W.off_feat), fsum, nf, k == 0, st), "feat_add")))
+      return rc;
+  }
+  return GDFT_OK;
+}
+
+int gdft_kpoint_workspace_bytes(const gdft_molecule *mols, int32_t n_kpt, size_t *bytes) {
+  double one = 1.0;
+  int rc = check_kpts(mols, n_kpt, &one, "gdft_kpoint_workspace_bytes");
+  if (rc) return rc;
+  if (bytes == nullptr) {
+    set_error("gdft_kpoint_workspace_bytes: null output");
+    return GDFT_ERR_INVALID;
+  }
+  *bytes = kpt_ws(&mols[0]).bytes;
+  return GDFT_OK;
+}
+
+static int check_kpt_ws(const gdft_molecule *m, void *ws, size_t ws_bytes) {
+  const size_t need = kpt_ws(m).bytes;
+  if (ws == nullptr || ws_bytes < need) {
+    set_error("workspace of %zu bytes is smaller than the %zu bytes required", ws_bytes, need);
+    return GDFT_ERR_WORKSPACE;
+  }
+  if (((uintptr_t)ws & 255u) != 0) {
+    set_error("workspace must be 256-byte aligned");
+    return GDFT_ERR_ALIGNMENT;
+  }
+  return GDFT_OK;
+}
+
+int gdft_kpoint_density(const gdft_molecule *mols, int32_t n_kpt, const double *d_rdm1, const double *h_kweights,
+                        double *d_rho, double *d_grad_rho, double *d_lapl, double *d_tau, void *d_ws,
+                        size_t ws_bytes, void *stream) {
+  const char *who = "gdft_kpoint_density";
+  int rc = check_kpts(mols, n_kpt, h_kweights, who);
+  if (rc) return rc;
+  if ((rc = check_kpt_ws(&mols[0], d_ws, ws_bytes))) return rc;
+  if (d_rdm1 == nullptr || ((uintptr_t)d_rdm1 & 7)) {
+    set_error("%s: rdm1 (2, n_kpt, n, n) complex is required, 8-byte aligned", who);
+    return GDFT_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  if ((rc = kpt_density(mols, n_kpt, d_rdm1, h_kweights, ws, st))) return rc;
+  StageTimer tm(GDFT_STAGE_REDUCE, st);
+  return check_cuda(launch_feat_to_reference((const double *)(ws + kpt_ws(&mols[0]).off_fsum), mols[0].n_grid,
+                                             mols[0].n_grid_pad, d_rho, d_grad_rho, d_lapl, d_tau, st),
+                    "feat_to_reference");
+}
+
+int gdft_kpoint_xc_energy_and_grads(const gdft_molecule *mols, int32_t n_kpt, const double *d_rdm1,
+                                    const double *h_kweights, const gdft_functional *fn, double *d_exc,
+                                    double *d_vxc, void *d_ws, size_t ws_bytes, void *stream) {
+  const char *who = "gdft_kpoint_xc_energy_and_grads";
+  int rc = check_kpts(mols, n_kpt, h_kweights, who);
+  if (rc) return rc;
+  if ((rc = check_kpt_ws(&mols[0], d_ws, ws_bytes))) return rc;
+  if ((rc = check_functional(fn, nullptr, 0))) return rc;
+  if (d_rdm1 == nullptr || d_exc == nullptr || (((uintptr_t)d_rdm1 | (uintptr_t)d_vxc) & 7)) {
+    set_error("%s: rdm1 and exc are required, 8-byte aligned", who);
+    return GDFT_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *ws = (char *)d_ws;
+  const WsLayout W = ws_layout(&mols[0]);
+  const KptWs KW = kpt_ws(&mols[0]);
+  if ((rc = kpt_density(mols, n_kpt, d_rdm1, h_kweights, ws, st))) return rc;
+  double *coef = d_vxc ? (double *)(ws + W.off_coef) : nullptr;
+  double *epart = (double *)(ws + W.off_epart);
+  {
+    StageTimer tm(GDFT_STAGE_POINT, st);
+    rc = check_cuda(launch_xc_point((const double *)(ws + KW.off_fsum), mol_w(&mols[0]), mols[0].n_grid,
+                                    mols[0].n_grid_pad, *fn, nullptr, 0, coef, epart, nullptr, st),
+                    "xc_point");
+    if (rc) return rc;
+  }
+  {
+    StageTimer tm(GDFT_STAGE_REDUCE, st);
+    if ((rc = check_cuda(launch_energy_reduce(epart, W.n_eblocks, d_exc, st), "energy_reduce"))) return rc;
+  }
+  if (d_vxc == nullptr) return GDFT_OK;
+  const int n = mols[0].n_ao / 2;
+  double *V = (double *)(ws + KW.off_v);
+  for (int k = 0; k < n_kpt; ++k) {
+    if ((rc = run_vxc(&mols[k], coef, V, ws, st))) return rc;
+    if ((rc = check_cuda(launch_kpt_vxc(V, n_kpt, k, n, h_kweights[k], d_vxc, st), "kpt_vxc"))) return rc;
+  }
+  return GDFT_OK;
+}
+
+int gdft_kpoint_coulomb(int32_t n_kpt, int32_t n_ao, const double *d_rep, const double *d_rdm1, const double *d_h1e,
+                        const double *d_kweights, double nuclear_repulsion, double *d_vj, double *d_enonxc,
+                        void *stream) {
+  if (n_kpt <= 0 || n_ao <= 0 || d_rep == nullptr || d_rdm1 == nullptr || d_kweights == nullptr || d_vj == nullptr ||
+      (d_enonxc != nullptr && d_h1e == nullptr)) {
+    set_error("gdft_kpoint_coulomb: rep_tensor, rdm1, k-point weights and vj are required (h1e with the energy)");
+    return GDFT_ERR_INVALID;
+  }
+  if (((uintptr_t)d_rep | (uintptr_t)d_rdm1 | (uintptr_t)d_h1e | (uintptr_t)d_kweights | (uintptr_t)d_vj |
+       (uintptr_t)d_enonxc) &
+      7) {
+    set_error("gdft_kpoint_coulomb: pointers must be 8-byte aligned");
+    return GDFT_ERR_ALIGNMENT;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = check_cuda(launch_kpt_coulomb(d_rep, d_rdm1, d_kweights, n_kpt, n_ao, d_vj, st), "kpt_coulomb");
+  if (rc || d_enonxc == nullptr) return rc;
+  return check_cuda(launch_kpt_nonxc(d_rdm1, d_h1e, d_vj, d_kweights, n_kpt, n_ao, nuclear_repulsion, d_enonxc, st),
+                    "kpt_nonxc");
+}
+
+int gdft_kpoint_fock(int32_t n_kpt, int32_t n_ao, const double *d_h1e, const double *d_vj, const double *d_vxc,
+                     double clip, double *d_fock, void *stream) {
+  if (n_kpt <= 0 || n_ao <= 0 || d_h1e == nullptr || d_vj == nullptr || d_vxc == nullptr || d_fock == nullptr) {
+    set_error("gdft_kpoint_fock: h1e, vj, vxc and fock are required");
+    return GDFT_ERR_INVALID;
+  }
+  if (((uintptr_t)d_h1e | (uintptr_t)d_vj | (uintptr_t)d_vxc | (uintptr_t)d_fock) & 7) {
+    set_error("gdft_kpoint_fock: pointers must be 8-byte aligned");
+    return GDFT_ERR_ALIGNMENT;
+  }
+  return check_cuda(launch_kpt_fock(d_h1e, d_vj, d_vxc, n_kpt, n_ao, (double)n_kpt, clip, d_fock,
+                                    (cudaStream_t)stream),
+                    "kpt_fock");
+}
+
 int gdft_network_param_count(const gdft_network *net, size_t *count) {
   int rc = check_network(net);
   if (rc) return rc;

@@ -43,6 +43,17 @@ cudaError_t launch_vxc_q_tc(const float *av, const float *af, const double *coef
                             int ldk, int n_ao, float *q, int nsplit, double *vpart, double *vxc, int *err,
                             cudaStream_t st);
 
+// kpoint.cu: the doubled real form of a k-point's complex density matrix and gradient.
+cudaError_t launch_kpt_build_m(const double *rdm1c, int K, int k, int n, double wk, double *M, cudaStream_t st);
+cudaError_t launch_feat_add(const double *f, double *sum, size_t count, bool first, cudaStream_t st);
+cudaError_t launch_kpt_vxc(const double *V, int K, int k, int n, double wk, double *vxc, cudaStream_t st);
+cudaError_t launch_kpt_coulomb(const double *rep, const double *rdm1c, const double *w, int K, int n, double *vj,
+                               cudaStream_t st);
+cudaError_t launch_kpt_fock(const double *h1e, const double *vj, const double *vxc, int K, int n, double scale,
+                            double clip, double *fock, cudaStream_t st);
+cudaError_t launch_kpt_nonxc(const double *rdm1c, const double *h1e, const double *vj, const double *w, int K, int n,
+                             double e_nuc, double *out, cudaStream_t st);
+
 // xc_point.cu
 int xc_point_blocks(int64_t np);
 cudaError_t launch_xc_point(const double *feat, const double *w, int64_t n_grid, int64_t np,

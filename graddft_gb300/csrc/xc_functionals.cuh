@@ -37,11 +37,13 @@ __device__ __forceinline__ double fzeta_pp0() { return 4.0 / (9.0 * (pow(2.0, 1.
 // correlation_polarization_correction, functional.py:982-1045.
 //
 // `nan_path` is set when the reference's reverse-mode gradient is NaN: with
-// rho_a + rho_b > clip and zeta exactly +-1, the backward of log2(1 -+ zeta)
-// in fzeta divides a (possibly zero) cotangent by zero, and the NaN reaches
-// rho_a and rho_b through the selected branch of the zeta `where`, whatever
-// the masks further down (jax.grad at train.py:86).  Forward-mode partials
-// would stay finite there, so the caller poisons those inputs explicitly.
+// rho_a + rho_b > clip and |zeta| >= 1 (zeta = +-1 exactly, or beyond when one
+// spin density is negative, as the unconjugated k-point forms of a Solid
+// allow), the backward of 2^(4/3 log2(1 -+ zeta)) in fzeta meets a division of
+// a (possibly zero) cotangent by zero or a NaN forward value, and the NaN
+// reaches rho_a and rho_b through the selected branch of the zeta `where`,
+// whatever the masks further down (jax.grad at train.py:86).  Forward-mode
+// partials would stay finite there, so the caller poisons those inputs.
 template <class T>
 __device__ __forceinline__ T corr_pol(const T &ep0, const T &ep1, const T &r0, const T &r1, double clip,
                                       bool *nan_path = nullptr) {
@@ -49,7 +51,7 @@ __device__ __forceinline__ T corr_pol(const T &ep0, const T &ep1, const T &r0, c
   const T log_rho = xlog2(xclipmin(rs, clip));
   const T log_rs = log2(pow(3.0 / (4.0 * kPi), 1.0 / 3.0)) - log_rho / 3.0;
   const T zeta = xwhere(val(rs) > clip, (r0 - r1) / rs, tconst(rs, 0.0));
-  if (nan_path != nullptr) *nan_path = val(rs) > clip && (1.0 - val(zeta) == 0.0 || 1.0 + val(zeta) == 0.0);
+  if (nan_path != nullptr) *nan_path = val(rs) > clip && !(1.0 - val(zeta) > 0.0 && 1.0 + val(zeta) > 0.0);
   const double A_ = 0.016887, alpha1 = 0.11125, beta1 = 10.357, beta2 = 3.6231, beta3 = 0.88026,
                beta4 = 0.49671;
   const T ars = xexp2(log2(alpha1) + log_rs);

@@ -193,6 +193,8 @@ class Functional:
 
     def energy_xc_only(self, params, atoms, *args, **kwargs):
         fn, ehf = self.spec(params, atoms, kwargs.get("clip_cte", CLIP))
+        if getattr(atoms, "is_solid", False):  # E_xc of the k-points (no autograd through a complex rdm1)
+            return atoms.resident().xc_energy_and_grads(atoms._rdm1(), fn, ehf, want_vxc=False)[0]
         rdm1 = atoms.rdm1 if isinstance(atoms.rdm1, torch.Tensor) and atoms.rdm1.requires_grad else atoms._rdm1()
         return _XcEnergy.apply(rdm1, atoms.resident(), fn, ehf)
 

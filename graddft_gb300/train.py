@@ -22,6 +22,16 @@ def energy_predictor(functional, nlc_functional=None, clip_cte: float = CLIP, **
 
     def predict(params, atoms, *args):
         needs_chi = functional.densitygrads is not None or functional.coefficient_input_grads is not None
+        if getattr(atoms, "is_solid", False):
+            # train.py:147-163 with a Solid: F = h1e + J + n_kpt dE_xc/d rdm1 (complex, jax.grad's
+            # convention), clipped, (F + F^H)/2, clipped; hybrid terms are not available for solids.
+            if needs_chi:
+                atoms.select_HF_omegas(None)
+            exc, vxc = functional.xc_energy_and_grads(params, atoms, clip_cte)
+            r = atoms.resident()
+            vj, enonxc = r.coulomb(atoms.rep_tensor, atoms._rdm1(), atoms.h1e, float(atoms.nuclear_repulsion),
+                                   want_energy=True)
+            return exc + enonxc, r.fock(atoms.h1e, vj, vxc, clip_cte)
         if needs_chi and getattr(atoms, "chi", None) is None:
             raise ValueError("Precomputed chi tensor has not been loaded.")
         exc, vxc = functional.xc_energy_and_grads(params, atoms, clip_cte)

@@ -156,6 +156,47 @@ int gdft_eval_ao(const gdft_basis *basis, const double *d_coords, int64_t n_grid
 int gdft_molecule_eval_shells(const gdft_molecule *mol, const gdft_basis *basis, const double *d_coords,
                               const double *d_weights, void *stream);
 
+/* k-points (the Solid path, solid.py:100-260 and train.py:124-163 with a Solid).
+ * Each k-point is a molecule of 2n "AOs": the real and imaginary parts of the
+ * n crystal AOs, [Re phi_k | Im phi_k] (loaded with gdft_molecule_load from the
+ * (grid, 2n) real and imaginary parts side by side); all k-points share the grid
+ * and the form.  d_rdm1: (2, n_kpt, n, n) complex128 (interleaved re, im);
+ * h_kweights: n_kpt host doubles (KPointInfo.weights).  The densities are the
+ * reference's unconjugated bilinear forms, e.g.
+ * rho = Re sum_k w_k D_k,ab phi_k,a phi_k,b (solid.py:491-632), summed over k. */
+int gdft_kpoint_workspace_bytes(const gdft_molecule *mols, int32_t n_kpt, size_t *bytes);
+
+/* density / grad_density / lapl_density / kinetic_density of a Solid (solid.py:491-632);
+ * outputs as gdft_density (any may be NULL). */
+int gdft_kpoint_density(const gdft_molecule *mols, int32_t n_kpt, const double *d_rdm1, const double *h_kweights,
+                        double *d_rho, double *d_grad_rho, double *d_lapl, double *d_tau, void *d_ws,
+                        size_t ws_bytes, void *stream);
+
+/* xc_energy_and_grads (train.py:86-121) for a Solid and a functional with
+ * constant coefficients: E_xc and d_vxc = jax.grad of E_xc with respect to the
+ * complex rdm1 (JAX's convention dE/dRe - i dE/dIm), (2, n_kpt, n, n) complex128,
+ * or NULL.  Columns needing HF densities are rejected (the reference's Solid
+ * raises NotImplementedError for them, solid.py:228-256). */
+int gdft_kpoint_xc_energy_and_grads(const gdft_molecule *mols, int32_t n_kpt, const double *d_rdm1,
+                                    const double *h_kweights, const gdft_functional *fn, double *d_exc,
+                                    double *d_vxc, void *d_ws, size_t ws_bytes, void *stream);
+
+/* Coulomb potential and non-XC energy of a Solid (solid.py:272-411, complex128 interleaved):
+ *   vj[k][i][j] = w_k sum_(q,l,m) rep[k][q][i][j][l][m] D_q[m][l]   (D = rdm1 summed over spin),
+ *   enonxc = E_nuc + Re sum_k w_k tr(D_k h1e_k) + Re sum_k w_k tr(D_k vj_k) / 2.
+ * d_rep (n_kpt, n_kpt, n, n, n, n); d_rdm1 (2, n_kpt, n, n); d_h1e (n_kpt, n, n);
+ * d_kweights (n_kpt) device doubles; d_vj (n_kpt, n, n); d_enonxc one double or NULL. */
+int gdft_kpoint_coulomb(int32_t n_kpt, int32_t n_ao, const double *d_rep, const double *d_rdm1, const double *d_h1e,
+                        const double *d_kweights, double nuclear_repulsion, double *d_vj, double *d_enonxc,
+                        void *stream);
+
+/* predict's Fock matrix for a Solid (train.py:147-163): F = h1e + vj + n_kpt * vxc
+ * (undoing the 1/n_kpt of the k-point weights in jax.grad), abs_clip, (F + F^H)/2
+ * over the orbital indices, abs_clip.  d_h1e, d_vj (n_kpt, n, n), d_vxc and d_fock
+ * (2, n_kpt, n, n), complex128 interleaved. */
+int gdft_kpoint_fock(int32_t n_kpt, int32_t n_ao, const double *d_h1e, const double *d_vj, const double *d_vxc,
+                     double clip, double *d_fock, void *stream);
+
 /* nu integrals and the chi tensor (range-separated exact exchange inputs).
  *   nu_ab(r) = int phi_a(r') phi_b(r') erf(omega |r - r'|) / |r - r'| dr'  (omega = 0: 1/|r - r'|),
  * PySCF's int1e_grids as _evaluate_nu / _nu_chunk call it (external/_hf_density.py:17-120), and

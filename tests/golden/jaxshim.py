@@ -138,7 +138,10 @@ def _mk_jnp():
     m.logical_and = lambda a, b: torch.logical_and(_t(a), _t(b))
 
     def einsum(subscripts, *ops, precision=None, **_):
-        return torch.einsum(subscripts, *[_t(o) for o in ops])
+        ts = [_t(o) for o in ops]
+        if any(t.is_complex() for t in ts):  # jnp.einsum promotes mixed real/complex operands
+            ts = [t if t.is_complex() else t.to(torch.complex128) for t in ts]
+        return torch.einsum(subscripts, *ts)
 
     m.einsum = einsum
 
@@ -205,7 +208,7 @@ def _tree_prepare(x):
 
         return {k: p[0] for k, p in zip(keys, parts)}, leaves, rebuild
     t = _t(x)
-    if not t.is_floating_point():
+    if not (t.is_floating_point() or t.is_complex()):
         t = t.to(F64)
     if not t.requires_grad:
         t = t.detach().clone().requires_grad_(True)
@@ -237,6 +240,9 @@ def _vg_call(fun, nums, argnums, has_aux, args, kwargs):
         val = out[0] if has_aux else out
         gs = torch.autograd.grad(val, leaves_all, create_graph=True, allow_unused=True)
         gs = [torch.zeros_like(l) if g is None else g for g, l in zip(gs, leaves_all)]
+        # jax.grad of a real function of a complex leaf is dL/dRe - i dL/dIm, the
+        # conjugate of the gradient torch returns
+        gs = [g.conj() if g.is_complex() else g for g in gs]
         res, j = [], 0
         for rb, c in zip(rebuilds, counts):
             res.append(rb(gs[j:j + c]))
@@ -520,7 +526,7 @@ def install():
         sys.modules[name] = mod
 
 
-def load_reference(root: str):
+def load_reference(root: str, with_solid: bool = False):
     """Execute the reference's molecule/functional/popular_functionals/train modules.
 
     ``grad_dft/__init__.py`` is not executed (it imports PySCF, h5py and the
@@ -562,10 +568,15 @@ def load_reference(root: str):
               "coulomb_energy"):
         setattr(pkg, n, getattr(mol, n))
 
-    class Solid:  # the periodic path is outside this stand-in
-        pass
+    if with_solid:
+        sol = run("solid")
+        pkg.Solid, pkg.KPointInfo = sol.Solid, sol.KPointInfo
+    else:
+        class Solid:  # the periodic path is left out unless asked for
+            pass
 
-    pkg.Solid = Solid
+        pkg.Solid = Solid
+        sol = None
     fun = run("functional")
     for n in ("DispersionFunctional", "Functional", "NeuralFunctional", "DM21",
               "correlation_polarization_correction", "exchange_polarization_correction",
@@ -575,7 +586,7 @@ def load_reference(root: str):
     pop = run("popular_functionals")
     train = run("train")
     pkg.energy_predictor = train.energy_predictor
-    return types.SimpleNamespace(molecule=mol, functional=fun, popular=pop, train=train)
+    return types.SimpleNamespace(molecule=mol, functional=fun, popular=pop, train=train, solid=sol)
 
 
 def load_scf(root: str, ref):
