@@ -751,6 +751,84 @@ def run_chi(args):
     print(json.dumps(line))
 
 
+def run_solid(args):
+    """k-point (Solid) E_xc + complex V_xc for B88+LYP: grid-pts/s over all k-points."""
+    import torch
+
+    import oracle.solid as OSd
+    from graddft_gb300 import basis as B
+    from graddft_gb300 import build, engine, synthetic, _lib
+    from graddft_gb300.solid import KPointResident
+
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    n_grid = args.n_grid if args.n_grid != N_GRID else 1 << 17
+    n_ao = args.n_ao if args.n_ao != N_AO else 64
+    n_kpt = 4
+    form = args.form or "tf32x3"
+    wl = synthetic.make_workload(n_grid, n_ao, max(1, n_ao // 8), SEED)
+    sb = B.ShellBasis.from_synthetic(wl.basis)
+    c_d = torch.as_tensor(wl.coords, device=dev)
+    phi, dphi, d2phi = B.eval_ao(sb, c_d, deriv=2)
+    kpts = torch.tensor([[0.0, 0.0, 0.0], [0.02, 0.0, 0.0], [0.0, 0.02, 0.0], [0.0, 0.0, 0.02]],
+                        dtype=torch.float64, device=dev)[:n_kpt]
+    ph = torch.exp(1j * (c_d @ kpts.T)).T[:, :, None]  # Bloch phases (k, grid, 1)
+    kk = kpts[:, None, None, :]
+    ao = phi[None] * ph
+    grad_ao = (dphi[None] + 1j * kk * phi[None, :, :, None]) * ph[..., None]
+    grad2_ao = (d2phi[None] + 2j * kk * dphi[None] - kk * kk * phi[None, :, :, None]) * ph[..., None]
+    del phi, dphi, d2phi
+    g = np.random.default_rng(SEED)
+    rdm1 = np.empty((2, n_kpt, n_ao, n_ao), dtype=np.complex128)
+    for s in range(2):
+        for k in range(n_kpt):
+            q, _ = np.linalg.qr(g.standard_normal((n_ao, n_ao)) + 1j * g.standard_normal((n_ao, n_ao)))
+            c = q[:, :max(1, n_ao // 8)]
+            rdm1[s, k] = c @ c.conj().T
+    kw = np.full(n_kpt, 1.0 / n_kpt)
+    res = KPointResident(ao, grad_ao, grad2_ao, torch.as_tensor(wl.weights, device=dev), kw, form, dev)
+    d_rdm1 = torch.as_tensor(rdm1, device=dev)
+    fn = engine.make_functional([_lib.COL_LSDA, _lib.COL_B88, _lib.COL_LYP], [1.0])
+
+    def step():
+        return res.xc_energy_and_grads(d_rdm1, fn)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(1, args.steps)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            exc, vxc = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    line = {
+        "metric": "Solid E_xc + complex V_xc (all k-points), grid-pts/s", "value": n_grid / (ms * 1e-3),
+        "unit": "grid-pts/s", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "fp64" else "tf32x3",
+        "data": "synthetic (seeded Gaussians with Bloch phases, Hermitian density matrices per k-point)",
+        "config": {"workload": f"k-point XC: {n_kpt} k-points x {n_ao} crystal AOs, n_grid {n_grid}, B88+LYP, "
+                               f"{form} form", "n_kpt": n_kpt, "n_ao": n_ao, "n_grid": n_grid, "form": form},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        n_s = min(args.cpu_sample, 4096)
+        sl = slice(0, n_s)
+        t0 = time.perf_counter()
+        e_ref, _ = OSd.solid_xc_energy_and_grads("BLYP", rdm1, ao[:, sl].cpu().numpy(), grad_ao[:, sl].cpu().numpy(),
+                                                 grad2_ao[:, sl].cpu().numpy(), wl.weights[sl], kw)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_s / dt, "unit": "grid-pts/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{n_s} grid points ({dt:.1f} s), torch-CPU restatement of the k-point "
+                                          "densities, BLYP and the complex jax.grad (oracle/solid.py)"}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -765,10 +843,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
-    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch", "hf", "ao", "chi"],
+    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch", "hf", "ao", "chi", "solid"],
                     help="xc: B88+LYP contraction benchmark (headline); neural: DM21-style network fwd+bwd; "
                          "scf: differentiable SCF loop; batch: many molecules per step; hf: DM21 predict with "
-                         "its exact-exchange terms from a chi tensor; ao: AO tables from contracted shells; chi: the chi tensor from range-separated integrals")
+                         "its exact-exchange terms from a chi tensor; ao: AO tables from contracted shells; chi: the chi tensor from range-separated integrals; solid: k-point XC for a Solid")
     ap.add_argument("--n-mol", type=int, default=64, help="molecules (--workload batch)")
     ap.add_argument("--points-per-ao", type=int, default=150, help="grid points per AO (--workload batch)")
     ap.add_argument("--cycles", type=int, default=20, help="SCF iterations (--workload scf)")
@@ -789,6 +867,8 @@ def main():
         return run_ao(args)
     if args.workload == "chi":
         return run_chi(args)
+    if args.workload == "solid":
+        return run_solid(args)
 
     import torch
 
