@@ -10,7 +10,7 @@ with the range-separated integrals of ``_evaluate_nu`` / ``_nu_chunk``
     nu_(d a)(r) = int phi_d(r') phi_a(r') erf(omega |r - r'|) / |r - r'| dr'   (omega = 0: 1/|r - r'|).
 
 The integrals run in ``libgdft_xc.so`` (McMurchie-Davidson, FP64) for shells
-up to l = 2; chi for a chunk of grid points is contracted from the chunk's
+up to l = 3; chi for a chunk of grid points is contracted from the chunk's
 integrals without leaving the device.
 """
 from __future__ import annotations

@@ -24,28 +24,18 @@
 //
 // Work layout: one warp per shell pair and 32 grid points (lanes = points), so the
 // shell pair's primitive data (set up once per pair and omega by
-// nu_pair_setup_kernel) are uniform loads; templates on (l_a >= l_b) <= 2.
+// nu_pair_setup_kernel) are uniform loads; templates on (l_a >= l_b) <= 3.
 #include <vector>
 
 #include "common.cuh"
 #include "mlp_gemm.cuh"
-#include "shells.cuh"
+#include "nu_kernels.cuh"
 
 namespace gdft {
 
 namespace {
 
-constexpr int kNuMaxL = 2;                 // shells up to d
-constexpr int kMaxOmega = 8;               // omegas of one gdft_chi call
-constexpr int kBoysN = 17;                 // F_0 .. F_16 tabulated
-constexpr int kBoysPts = 601;              // T = 0, 0.1, ..., 60
-constexpr double kBoysStep = 0.1;
-constexpr double kBoysTMax = 60.0;
-constexpr int kETab = 3 * 3 * 5;           // E[i][j][t], i, j <= 2, t <= 4 (per dimension)
-constexpr int kE3Max = 336;                // Hermite products of a d-d primitive pair
-constexpr int kPPStride = 8 + kE3Max;      // mu, screened flag, P(3), p, 2 pad, products
-constexpr double kPi = 3.14159265358979323846;
-constexpr double kScreen = 1e-30;          // product-overlap prefactor below which a primitive pair is skipped
+using namespace nu_detail;
 
 __global__ void boys_table_kernel(double *__restrict__ tab) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,35 +51,6 @@ __global__ void boys_table_kernel(double *__restrict__ tab) {
   tab[i] = exp(-T) * sum;
 }
 
-// F_0 .. F_L at T.
-template <int L>
-__device__ __forceinline__ void boys(const double *__restrict__ tab, double T, double F[L + 1]) {
-  if (T < kBoysTMax) {
-    const int i = (int)(T * (1.0 / kBoysStep) + 0.5);
-    const double md = i * kBoysStep - T;  // -(T - T_i)
-    const double *row = tab + i * kBoysN + L;
-    // sum_k F_(L+k)(T_i) (-(T - T_i))^k / k!, Horner from k = 8
-    constexpr double inv_fact[9] = {1.0, 1.0, 1.0 / 2, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040,
-                                    1.0 / 40320};
-    double acc = row[8] * inv_fact[8];
-#pragma unroll
-    for (int k = 7; k >= 0; --k) acc = fma(acc, md, row[k] * inv_fact[k]);
-    F[L] = acc;
-    if (L > 0) {
-      const double e = exp(-T);
-#pragma unroll
-      for (int n = L - 1; n >= 0; --n) F[n] = fma(2.0 * T, F[n + 1], e) * (1.0 / (2 * n + 1));
-    }
-  } else {
-    F[0] = 0.5 * sqrt(kPi / T);
-    const double h = 0.5 / T;
-#pragma unroll
-    for (int n = 0; n < L; ++n) F[n + 1] = F[n] * ((2 * n + 1) * h);
-  }
-}
-
-__device__ __forceinline__ int e_idx(int i, int j, int t) { return (i * 3 + j) * 5 + t; }
-
 // One thread per shell pair: the primitive-pair records.  Besides mu and P,
 // a record holds, for every pair of cartesian components (qa, qb) in PySCF's
 // order and every (t, u, v) with t <= ia + ib, u <= ka + kb, v <= ma + mb, the
@@ -103,11 +64,13 @@ __global__ void nu_pair_setup_kernel(ShellView B, const int32_t *__restrict__ pa
   const int64_t off = pairs[4 * ip + 2];
   shells_detail::ShellRec r1, r2;
   if (!shells_detail::load_shell(B, s1, r1) || !shells_detail::load_shell(B, s2, r2)) return;
-  if (r1.l > kNuMaxL || r2.l > kNuMaxL || off < 0 || off + (int64_t)r1.np * r2.np > n_pp) return;
+  if (r1.l > kNuMaxL || r2.l > kNuMaxL) return;
+  const int len = rec_len(r1.l, r2.l);
+  if (off < 0 || off + (int64_t)r1.np * r2.np * len > n_pp) return;
   const double *A = B.centre + 3 * s1, *Bc = B.centre + 3 * s2;
   for (int i1 = 0; i1 < r1.np; ++i1) {
     for (int i2 = 0; i2 < r2.np; ++i2) {
-      double *rec = pp + (off + (int64_t)i1 * r2.np + i2) * kPPStride;
+      double *rec = pp + off + ((int64_t)i1 * r2.np + i2) * len;
       const double a = B.exps[r1.poff + i1], b = B.exps[r2.poff + i2];
       const double p = a + b, ip2 = 0.5 / p;
       const double mu = omega == 0.0 ? p : p * omega * omega / (p + omega * omega);
@@ -134,7 +97,7 @@ __global__ void nu_pair_setup_kernel(ShellView B, const int32_t *__restrict__ pa
       }
       // screening: a Gaussian product of overlap prefactor below 1e-30 contributes
       // nothing at double precision to any point's integrals (the Hermite integrals
-      // grow at most like (2 mu)^(L/2), far from closing the gap for l <= 2)
+      // grow at most like (2 mu)^(L/2), far from closing the gap for l <= 3)
       rec[1] = E[0][0] * E[1][0] * E[2][0] < kScreen ? 1.0 : 0.0;
       double *E3 = rec + 8;
       int idx = 0;
@@ -147,194 +110,10 @@ __global__ void nu_pair_setup_kernel(ShellView B, const int32_t *__restrict__ pa
               for (int t = 0; t <= ia + ib; ++t)
                 for (int u = 0; u <= ka + kb; ++u)
                   for (int v = 0; v <= ma + mb; ++v)
-                    if (idx < kE3Max)
+                    if (idx < len - 8)
                       E3[idx++] = pref * E[0][e_idx(ia, ib, t)] * E[1][e_idx(ka, kb, u)] * E[2][e_idx(ma, mb, v)];
             }
         }
-    }
-  }
-}
-
-template <int L>
-struct CartPow {
-  // exponents of the ncart(L) monomials in PySCF's order
-  static constexpr int n = (L + 1) * (L + 2) / 2;
-  static __device__ __forceinline__ constexpr int x(int q) {
-    int idx = 0;
-    for (int lx = L; lx >= 0; --lx)
-      for (int ly = L - lx; ly >= 0; --ly) {
-        if (idx == q) return lx;
-        ++idx;
-      }
-    return 0;
-  }
-  static __device__ __forceinline__ constexpr int y(int q) {
-    int idx = 0;
-    for (int lx = L; lx >= 0; --lx)
-      for (int ly = L - lx; ly >= 0; --ly) {
-        if (idx == q) return ly;
-        ++idx;
-      }
-    return 0;
-  }
-  static __device__ __forceinline__ constexpr int z(int q) { return L - x(q) - y(q); }
-};
-
-// Hermite Coulomb integrals R^0_tuv, t + u + v <= L.
-template <int L>
-__device__ __forceinline__ void hermite_r(const double F[L + 1], double mu, double X, double Y, double Z,
-                                          double R[L + 1][L + 1][L + 1]) {
-  double nxt[L + 1][L + 1][L + 1];
-  double m2 = 1.0;
-#pragma unroll
-  for (int n = 0; n < L; ++n) m2 *= -2.0 * mu;
-  nxt[0][0][0] = m2 * F[L];
-#pragma unroll
-  for (int n = L - 1; n >= 0; --n) {
-    double cur[L + 1][L + 1][L + 1];
-    const int top = L - n;
-#pragma unroll
-    for (int t = 0; t <= L; ++t)
-#pragma unroll
-      for (int u = 0; u <= L; ++u)
-#pragma unroll
-        for (int v = 0; v <= L; ++v) {
-          if (t + u + v > top) continue;
-          double val;
-          if (t > 0)
-            val = (t > 1 ? (t - 1) * nxt[t > 1 ? t - 2 : 0][u][v] : 0.0) + X * nxt[t - 1][u][v];
-          else if (u > 0)
-            val = (u > 1 ? (u - 1) * nxt[0][u > 1 ? u - 2 : 0][v] : 0.0) + Y * nxt[0][u - 1][v];
-          else if (v > 0)
-            val = (v > 1 ? (v - 1) * nxt[0][0][v > 1 ? v - 2 : 0] : 0.0) + Z * nxt[0][0][v - 1];
-          else {
-            double m = 1.0;
-#pragma unroll
-            for (int k = 0; k < n; ++k) m *= -2.0 * mu;
-            val = m * F[n];
-          }
-          cur[t][u][v] = val;
-        }
-#pragma unroll
-    for (int t = 0; t <= L; ++t)
-#pragma unroll
-      for (int u = 0; u <= L; ++u)
-#pragma unroll
-        for (int v = 0; v <= L; ++v)
-          if (t + u + v <= top) nxt[t][u][v] = cur[t][u][v];
-  }
-#pragma unroll
-  for (int t = 0; t <= L; ++t)
-#pragma unroll
-    for (int u = 0; u <= L; ++u)
-#pragma unroll
-      for (int v = 0; v <= L; ++v)
-        if (t + u + v <= L) R[t][u][v] = nxt[t][u][v];
-}
-
-struct NuOut {
-  double *nu;      // nu[(a * n + b) * s_ab + p * s_p]
-  int64_t s_ab, s_p;
-  int n;
-};
-
-// One warp per shell pair of class (LA, LB), lanes = 32 points from p0.
-template <int LA, int LB>
-__global__ void __launch_bounds__(256) nu_kernel(ShellView B, const int32_t *__restrict__ pairs, int pair_lo,
-                                                 int pair_hi, const double *__restrict__ pp, int64_t n_pp,
-                                                 const double *__restrict__ boys_tab,
-                                                 const double *__restrict__ coords, int64_t p_begin, int64_t n_pts,
-                                                 NuOut out) {
-  constexpr int L = LA + LB;
-  constexpr int NA = CartPow<LA>::n, NB = CartPow<LB>::n;
-  const int lane = threadIdx.x & 31;
-  const int ip = pair_lo + blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (ip >= pair_hi) return;  // whole warps leave together
-  const int64_t pl = (int64_t)blockIdx.x * 32 + lane;  // point within the chunk
-  const bool live = pl < n_pts;
-  double Cx = 0.0, Cy = 0.0, Cz = 0.0;
-  if (live) {
-    const int64_t p = p_begin + pl;
-    Cx = coords[3 * p];
-    Cy = coords[3 * p + 1];
-    Cz = coords[3 * p + 2];
-  }
-  const int s1 = pairs[4 * ip], s2 = pairs[4 * ip + 1];
-  const int64_t off = pairs[4 * ip + 2];
-  shells_detail::ShellRec r1, r2;
-  if (!shells_detail::load_shell(B, s1, r1) || !shells_detail::load_shell(B, s2, r2)) return;
-  if (r1.l != LA || r2.l != LB || off < 0 || off + (int64_t)r1.np * r2.np > n_pp) return;
-  if (r1.ncomp > NA || r2.ncomp > NB) return;
-  for (int c1 = 0; c1 < r1.nctr; ++c1) {
-    for (int c2 = 0; c2 < r2.nctr; ++c2) {
-      double cart[NA][NB];
-#pragma unroll
-      for (int qa = 0; qa < NA; ++qa)
-#pragma unroll
-        for (int qb = 0; qb < NB; ++qb) cart[qa][qb] = 0.0;
-      for (int i1 = 0; i1 < r1.np; ++i1) {
-        const double ca = B.coef[r1.coff + (int64_t)c1 * r1.np + i1];
-        for (int i2 = 0; i2 < r2.np; ++i2) {
-          const double *rec = pp + (off + (int64_t)i1 * r2.np + i2) * kPPStride;
-          if (rec[1] != 0.0) continue;  // screened (uniform across the warp)
-          const double cc = ca * B.coef[r2.coff + (int64_t)c2 * r2.np + i2];
-          const double mu = rec[0];
-          const double X = rec[2] - Cx, Y = rec[3] - Cy, Z = rec[4] - Cz;
-          double F[L + 1];
-          boys<L>(boys_tab, mu * (X * X + Y * Y + Z * Z), F);
-          double R[L + 1][L + 1][L + 1];
-          hermite_r<L>(F, mu, X, Y, Z, R);
-          const double *E3 = rec + 8;
-          int idx = 0;
-#pragma unroll
-          for (int qa = 0; qa < NA; ++qa) {
-            const int ia = CartPow<LA>::x(qa), ka = CartPow<LA>::y(qa), ma = CartPow<LA>::z(qa);
-#pragma unroll
-            for (int qb = 0; qb < NB; ++qb) {
-              const int ib = CartPow<LB>::x(qb), kb = CartPow<LB>::y(qb), mb = CartPow<LB>::z(qb);
-              double s = 0.0;
-#pragma unroll
-              for (int t = 0; t <= L; ++t) {
-                if (t > ia + ib) continue;
-#pragma unroll
-                for (int u = 0; u <= L; ++u) {
-                  if (u > ka + kb) continue;
-#pragma unroll
-                  for (int v = 0; v <= L; ++v) {
-                    if (v > ma + mb) continue;
-                    s = fma(E3[idx], R[t][u][v], s);
-                    ++idx;
-                  }
-                }
-              }
-              cart[qa][qb] = fma(cc, s, cart[qa][qb]);
-            }
-          }
-        }
-      }
-      // angular rows on both sides, then the symmetric writes
-      const double *T1 = B.trans + r1.toff, *T2 = B.trans + r2.toff;
-      for (int k1 = 0; k1 < r1.ncomp; ++k1) {
-        double h[NB];
-#pragma unroll
-        for (int qb = 0; qb < NB; ++qb) {
-          double acc = 0.0;
-#pragma unroll
-          for (int qa = 0; qa < NA; ++qa) acc = fma(T1[k1 * NA + qa], cart[qa][qb], acc);
-          h[qb] = acc;
-        }
-        const int a = r1.aoff + c1 * r1.ncomp + k1;
-        for (int k2 = 0; k2 < r2.ncomp; ++k2) {
-          double v = 0.0;
-#pragma unroll
-          for (int qb = 0; qb < NB; ++qb) v = fma(T2[k2 * NB + qb], h[qb], v);
-          const int b = r2.aoff + c2 * r2.ncomp + k2;
-          if (live) {
-            out.nu[((int64_t)a * out.n + b) * out.s_ab + pl * out.s_p] = v;
-            out.nu[((int64_t)b * out.n + a) * out.s_ab + pl * out.s_p] = v;
-          }
-        }
-      }
     }
   }
 }
@@ -397,8 +176,8 @@ size_t al256(size_t x) { return (x + 255) / 256 * 256; }
 // = l1 * (l1 + 1) / 2 + l2.
 struct PairPlan {
   std::vector<int32_t> pairs;  // (n_pairs, 4): s1, s2, primitive-pair offset, 0
-  int class_lo[7];
-  int64_t n_pp = 0;
+  int class_lo[11];
+  int64_t n_pp = 0;  // doubles of the primitive-pair records of one omega
   int max_l = 0;
 };
 
@@ -406,7 +185,7 @@ int make_plan(const gdft_basis *b, PairPlan &plan, const char *who) {
   std::vector<int32_t> sh((size_t)b->n_shell * kShellCols);
   cudaError_t e = cudaMemcpy(sh.data(), b->d_shell, sh.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return check_cuda(e, who);
-  std::vector<std::vector<int32_t>> cls(6);
+  std::vector<std::vector<int32_t>> cls(10);
   for (int i = 0; i < b->n_shell; ++i) {
     const int li = sh[(size_t)kShellCols * i];
     if (li < 0 || li > kNuMaxL) {
@@ -430,12 +209,13 @@ int make_plan(const gdft_basis *b, PairPlan &plan, const char *who) {
       v.push_back(0);
     }
   int n = 0;
-  for (int c = 0; c < 6; ++c) {
+  for (int c = 0; c < 10; ++c) {
     plan.class_lo[c] = n;
     for (size_t q = 0; q < cls[c].size(); q += 4) {
       const int s1 = cls[c][q], s2 = cls[c][q + 1];
       const int64_t np1 = sh[(size_t)kShellCols * s1 + 1], np2 = sh[(size_t)kShellCols * s2 + 1];
-      if (plan.n_pp + np1 * np2 > INT32_MAX) {
+      const int64_t len = rec_len(sh[(size_t)kShellCols * s1], sh[(size_t)kShellCols * s2]);
+      if (plan.n_pp + np1 * np2 * len > INT32_MAX) {
         set_error("%s: too many primitive pairs", who);
         return GDFT_ERR_INVALID;
       }
@@ -443,11 +223,11 @@ int make_plan(const gdft_basis *b, PairPlan &plan, const char *who) {
       plan.pairs.push_back(s2);
       plan.pairs.push_back((int32_t)plan.n_pp);
       plan.pairs.push_back(0);
-      plan.n_pp += np1 * np2;
+      plan.n_pp += np1 * np2 * len;
       ++n;
     }
   }
-  plan.class_lo[6] = n;
+  plan.class_lo[10] = n;
   return GDFT_OK;
 }
 
@@ -463,7 +243,7 @@ NuWs nu_ws(const PairPlan &plan, int n_ao, int64_t chunk, bool want_chi, int n_o
   W.off_pairs = off;
   off = al256(off + plan.pairs.size() * sizeof(int32_t));
   W.off_pp = off;
-  off = al256(off + (size_t)n_omega * plan.n_pp * kPPStride * sizeof(double));
+  off = al256(off + (size_t)n_omega * plan.n_pp * sizeof(double));
   W.off_nu = off;
   W.off_x = off;
   if (want_chi) {
@@ -491,8 +271,7 @@ int run_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, in
            int64_t p_begin, int64_t n_pts, NuOut out, const char *who, cudaStream_t st) {
   const double *boys_tab = (const double *)(ws + W.off_boys);
   const int32_t *pairs = (const int32_t *)(ws + W.off_pairs);
-  const double *pp = (const double *)(ws + W.off_pp) + (size_t)w * plan.n_pp * kPPStride;
-  const unsigned gx = (unsigned)((n_pts + 31) / 32);
+  const double *pp = (const double *)(ws + W.off_pp) + (size_t)w * plan.n_pp;
   int rc;
 #define GDFT_NU_CLASS(LA, LB)                                                                                     \
   {                                                                                                               \
@@ -502,10 +281,11 @@ int run_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, in
         set_error("%s: %d shell pairs of one class exceed one launch", who, hi - lo);                            \
         return GDFT_ERR_UNSUPPORTED;                                                                              \
       }                                                                                                           \
-      const dim3 grid(gx, (unsigned)((hi - lo + 7) / 8));                                                         \
-      nu_kernel<LA, LB><<<grid, 256, 0, st>>>(B, pairs, lo, hi, pp, plan.n_pp, boys_tab, coords, p_begin, n_pts,  \
-                                              out);                                                               \
-      if ((rc = check_cuda(cudaGetLastError(), who))) return rc;                                                  \
+      const cudaError_t e = LA < 3 ? launch_nu_class<(LA < 3 ? LA : 0), (LA < 3 ? LB : 0)>(                      \
+                                         B, pairs, lo, hi, pp, plan.n_pp, boys_tab, coords, p_begin, n_pts, out, st) \
+                                   : launch_nu_f_class(LA, LB, B, pairs, lo, hi, pp, plan.n_pp, boys_tab, coords,    \
+                                                       p_begin, n_pts, out, st);                                  \
+      if ((rc = check_cuda(e, who))) return rc;                                                                   \
     }                                                                                                             \
   }
   GDFT_NU_CLASS(0, 0)
@@ -514,6 +294,10 @@ int run_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, in
   GDFT_NU_CLASS(2, 0)
   GDFT_NU_CLASS(2, 1)
   GDFT_NU_CLASS(2, 2)
+  GDFT_NU_CLASS(3, 0)
+  GDFT_NU_CLASS(3, 1)
+  GDFT_NU_CLASS(3, 2)
+  GDFT_NU_CLASS(3, 3)
 #undef GDFT_NU_CLASS
   return GDFT_OK;
 }
@@ -532,7 +316,7 @@ int setup_nu(const ShellView &B, const PairPlan &plan, const NuWs &W, char *ws, 
   const int np = (int)(plan.pairs.size() / 4);
   nu_pair_setup_kernel<<<(np + 127) / 128, 128, 0, st>>>(
       B, (const int32_t *)(ws + W.off_pairs), np, omega,
-      (double *)(ws + W.off_pp) + (size_t)w * plan.n_pp * kPPStride, plan.n_pp);
+      (double *)(ws + W.off_pp) + (size_t)w * plan.n_pp, plan.n_pp);
   return check_cuda(cudaGetLastError(), who);
 }
 

@@ -1,0 +1,15 @@
+// nu_fd.cu - the f-d integral class in a translation unit of its own (816
+// unrolled Hermite products per primitive pair).
+#include "nu_kernels.cuh"
+
+namespace gdft {
+namespace nu_detail {
+
+cudaError_t launch_nu_fd(const ShellView &B, const int32_t *pairs, int lo, int hi, const double *pp, int64_t n_pp,
+                         const double *boys_tab, const double *coords, int64_t p_begin, int64_t n_pts, NuOut out,
+                         cudaStream_t st) {
+  return launch_nu_class<3, 2>(B, pairs, lo, hi, pp, n_pp, boys_tab, coords, p_begin, n_pts, out, st);
+}
+
+}  // namespace nu_detail
+}  // namespace gdft

@@ -201,7 +201,7 @@ int gdft_kpoint_fock(int32_t n_kpt, int32_t n_ao, const double *d_h1e, const dou
  *   nu_ab(r) = int phi_a(r') phi_b(r') erf(omega |r - r'|) / |r - r'| dr'  (omega = 0: 1/|r - r'|),
  * PySCF's int1e_grids as _evaluate_nu / _nu_chunk call it (external/_hf_density.py:17-120), and
  *   chi[r][w][s][a] = sum_(b,d) D_s[b][d] phi_b(r) nu^(omega_w)_da(r),
- * generate_chi_tensor (interface/pyscf.py:1067-1126).  Shells up to l = 2
+ * generate_chi_tensor (interface/pyscf.py:1067-1126).  Shells up to l = 3
  * (GDFT_ERR_UNSUPPORTED beyond).  Both calls read the basis's shell table back
  * to the host to plan the shell pairs and synchronise `stream` before returning. */
 

@@ -74,7 +74,7 @@ def test_random_basis_vs_oracle(G, cart):
     shells = []
     for _ in range(4):
         c = rng.uniform(-2.0, 2.0, 3)
-        for l in (0, 1, 2):
+        for l in (0, 1, 2, 3):
             nprim = int(rng.integers(1, 4))
             nctr = int(rng.integers(1, 3))
             e = np.sort(np.exp(rng.uniform(math.log(0.1), math.log(30.0), nprim)))[::-1]
@@ -116,9 +116,9 @@ def test_chi_feeds_hf_energy_density(G, golden):
 def test_errors(G):
     from graddft_gb300 import basis as B
 
-    f_shell = B.ShellBasis([B.Shell(np.zeros(3), 3, np.array([1.0]), np.array([[1.0]]))])
+    g_shell = B.ShellBasis([B.Shell(np.zeros(3), 4, np.array([1.0]), np.array([[1.0]]))])
     with pytest.raises(NotImplementedError):
-        G.chi.nu_integrals(f_shell, np.zeros((4, 3)), 0.0)
+        G.chi.nu_integrals(g_shell, np.zeros((4, 3)), 0.0)
     s_shell = B.ShellBasis([B.Shell(np.zeros(3), 0, np.array([1.0]), np.array([[1.0]]))])
     with pytest.raises(ValueError):
         G.chi.nu_integrals(s_shell, np.zeros((4, 3)), -0.1)

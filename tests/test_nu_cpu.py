@@ -78,7 +78,7 @@ def _quadrature_nu(shells, C, omega, n_r=140, n_t=48, n_p=96, s_max=11.0):
 def test_integrals_against_quadrature(omega):
     g = np.random.default_rng(5)
     shells = []
-    for l in (0, 1, 2):
+    for l in (0, 1, 2, 3):
         e = [1.1, 0.55] if l == 0 else [0.8]
         c = OS.normalise_contraction(l, e, np.ones((len(e), 1)))
         shells.append((g.uniform(-0.6, 0.6, 3), l, np.asarray(e), c, None))
