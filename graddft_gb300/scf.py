@@ -147,12 +147,67 @@ def _to_device(atoms):
     return atoms
 
 
+# ---------------------------------------------------------------- solids
+def solid_fock_solver(fock, s1e):
+    """safe_fock_solver (utils/eigenproblem.py:110-149) as the reference applies it to a Solid's
+    k-point batches: B = L L^H, C = L^-1 F L^-T (no conjugation), eigh of C's lower triangle,
+    eigenvectors L^-T C'.  fock (2, n_kpt, n, n), s1e (n_kpt, n, n): (mo_energy, mo_coeff)."""
+    L_inv = torch.linalg.inv(torch.linalg.cholesky(s1e))
+    es, cs = [], []
+    for s in range(2):
+        e, v = torch.linalg.eigh(L_inv @ fock[s] @ L_inv.transpose(-1, -2))
+        es.append(e)
+        cs.append(L_inv.transpose(-1, -2) @ v)
+    return torch.stack(es), torch.stack(cs)
+
+
+def solid_get_occ(mo_energy, nelecs):
+    """solid.py:438-487: the nelec lowest orbitals of each spin and k-point."""
+    occ = torch.zeros(mo_energy.shape, dtype=F64, device=mo_energy.device)
+    idx = torch.argsort(mo_energy, dim=-1)
+    for s in range(2):
+        occ[s].scatter_(-1, idx[s, :, :int(nelecs[s])], 1.0)
+    return occ
+
+
+def solid_make_rdm1(mo_coeff, mo_occ):
+    """solid.py:413-435: D[s,k] = C diag(occ) C^H."""
+    return torch.einsum("skij,skj,sklj->skil", mo_coeff, mo_occ.to(mo_coeff.dtype), mo_coeff.conj())
+
+
+def _solid_scf(functional, params, atoms, cycles, mixing_factor, clip_cte):
+    """diff_simple_scf_loop (evaluate.py:256-344) with a Solid: linear mixing around the k-point predict.
+    With constant-coefficient functionals nothing depends on parameters, so the loop runs forward."""
+    from .train import energy_predictor
+
+    predict = energy_predictor(functional, clip_cte=clip_cte)
+    dev = atoms.device
+    c = lambda x: torch.as_tensor(x).to(device=dev, dtype=torch.complex128)  # noqa: E731
+    atoms = atoms.replace(rdm1=c(atoms.rdm1), s1e=c(atoms.s1e))
+    mo_occ0 = torch.as_tensor(atoms.mo_occ)
+    nelecs = [int(round(float(mo_occ0[s, 0].sum()))) for s in range(2)]
+    energy, fock = predict(params, atoms)
+    atoms = atoms.replace(fock=fock, energy=energy)
+    for _ in range(cycles):
+        old_rdm1 = atoms.rdm1
+        mo_energy, mo_coeff = solid_fock_solver(atoms.fock, atoms.s1e)
+        mo_occ = solid_get_occ(mo_energy, nelecs)
+        rdm1 = (1.0 - mixing_factor) * old_rdm1 + mixing_factor * solid_make_rdm1(mo_coeff, mo_occ)
+        atoms = atoms.replace(mo_energy=mo_energy, mo_coeff=mo_coeff, mo_occ=mo_occ, rdm1=rdm1.resolve_conj())
+        energy, fock = predict(params, atoms)
+        atoms = atoms.replace(fock=fock, energy=energy)
+    return atoms
+
+
 def diff_simple_scf_loop(functional, cycles: int = 25, mixing_factor: float = 0.4,
                          clip_cte: float = CLIP) -> Callable:
     """evaluate.py:256-344: returns ``iterator(params, atoms) -> atoms`` with the final
-    rdm1, fock, energy, mo_coeff, mo_energy and mo_occ."""
+    rdm1, fock, energy, mo_coeff, mo_energy and mo_occ (a Molecule, or a Solid with
+    k-points for constant-coefficient functionals)."""
 
     def iterator(params, atoms, *args):
+        if getattr(atoms, "is_solid", False):
+            return _solid_scf(functional, params, atoms, cycles, mixing_factor, clip_cte)
         atoms = _to_device(atoms)
         nelecs = [int(round(float(atoms.mo_occ[s].sum()))) for s in range(2)]
         energy, fock = energy_and_fock(functional, params, atoms, clip_cte)
@@ -230,6 +285,12 @@ def diff_scf_loop(functional, cycles: int = 25, clip_cte: float = CLIP, max_diis
     Fock matrix (A = identity), the final rdm1, fock, energy, mo_coeff, mo_energy and mo_occ."""
 
     def iterator(params, atoms, *args):
+        if getattr(atoms, "is_solid", False):
+            # the reference's DIIS loops do not take k-points either: scf_loop rejects a Solid
+            # (evaluate.py:402-403) and diff_scf_loop's A = identity(s1e.shape[0]) (evaluate.py:972)
+            # does not fit k-point overlaps
+            raise NotImplementedError("Solids with full BZ zampling not yet supported. Use simple_scf_loop or "
+                                      "diff_simple_scf_loop instead.")
         atoms = _to_device(atoms)
         nelecs = [int(round(float(atoms.mo_occ[s].sum()))) for s in range(2)]
         energy, fock = energy_and_fock(functional, params, atoms, clip_cte)

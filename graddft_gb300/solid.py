@@ -49,7 +49,7 @@ def _as_c128(x, dev) -> torch.Tensor:
         return None
     if not isinstance(x, torch.Tensor):
         x = torch.as_tensor(x)
-    return x.to(device=dev, dtype=C128).contiguous()
+    return x.to(device=dev, dtype=C128).resolve_conj().contiguous()
 
 
 def _real_tables(x: torch.Tensor) -> torch.Tensor:
@@ -242,6 +242,21 @@ class Solid:
         _, e = self.resident().coulomb(self.rep_tensor, self._rdm1(), self.h1e, float(self.nuclear_repulsion),
                                        want_energy=True)
         return e
+
+    # ------------------------------------------------------------- SCF
+    def make_rdm1(self, *args, **kwargs):
+        """solid.py:158-165 / 413-435."""
+        from .scf import solid_make_rdm1
+
+        return solid_make_rdm1(_as_c128(self.mo_coeff, self.device), torch.as_tensor(self.mo_occ).to(self.device))
+
+    def get_occ(self):
+        """solid.py:167-177 / 438-487 (electrons per spin from the first k-point of mo_occ)."""
+        from .scf import solid_get_occ
+
+        mo_occ = torch.as_tensor(self.mo_occ)
+        nelecs = [int(round(float(mo_occ[s, 0].sum()))) for s in range(2)]
+        return solid_get_occ(torch.as_tensor(self.mo_energy).to(self.device), nelecs)
 
     # ------------------------------------------------- exact exchange
     def select_HF_omegas(self, omegas):

@@ -78,3 +78,49 @@ def solid_predict(name, rdm1, ao, grad_ao, grad2_ao, weights, kweights, h1e, rep
     F = 0.5 * (F + F.transpose(-1, -2).conj().resolve_conj())
     F = cabs_clip(F, clip_cte)
     return exc + solid_nonxc(rdm1, h1e, rep, nuclear_repulsion, kweights), F.numpy()
+
+
+def solid_fock_solver(fock, s1e):
+    """safe_fock_solver (utils/eigenproblem.py:110-149) on k-point batches, as the reference runs it for
+    a Solid: C = L^-1 F L^-T (no conjugation) with B = L L^H, eigh of its lower triangle, L^-T C'."""
+    L = torch.linalg.cholesky(_c(s1e))
+    L_inv = torch.linalg.inv(L)
+    out_e, out_c = [], []
+    for s in range(2):
+        C = L_inv @ _c(fock[s]) @ L_inv.transpose(-1, -2)
+        e, v = torch.linalg.eigh(C)
+        out_e.append(e)
+        out_c.append(L_inv.transpose(-1, -2) @ v)
+    return torch.stack(out_e), torch.stack(out_c)
+
+
+def solid_get_occ(mo_energy, nelecs):
+    """solid.py:438-487: per spin and k-point, the nelec lowest orbitals."""
+    occ = torch.zeros(mo_energy.shape, dtype=torch.float64)
+    for s in range(2):
+        for k in range(mo_energy.shape[1]):
+            idx = torch.argsort(mo_energy[s, k])
+            occ[s, k, idx[:int(nelecs[s])]] = 1.0
+    return occ
+
+
+def solid_make_rdm1(mo_coeff, mo_occ):
+    """solid.py:413-435."""
+    return torch.einsum("skij,skj,sklj->skil", mo_coeff, mo_occ.to(C128), mo_coeff.conj())
+
+
+def solid_scf_loop(name, rdm1, mo_occ, ao, grad_ao, grad2_ao, weights, kweights, h1e, s1e, rep, nuclear_repulsion,
+                   cycles, mixing_factor=0.4, clip_cte=CLIP):
+    """diff_simple_scf_loop (evaluate.py:256-344) with a Solid: (energy, rdm1, fock, mo_energy)."""
+    nelecs = [int(round(float(np.asarray(mo_occ)[s, 0].sum()))) for s in range(2)]
+    D = _c(rdm1)
+    E, F = solid_predict(name, D.numpy(), ao, grad_ao, grad2_ao, weights, kweights, h1e, rep, nuclear_repulsion,
+                         clip_cte)
+    mo_e = None
+    for _ in range(cycles):
+        mo_e, mo_c = solid_fock_solver(F, s1e)
+        occ = solid_get_occ(mo_e, nelecs)
+        D = (1 - mixing_factor) * D + mixing_factor * solid_make_rdm1(mo_c, occ)
+        E, F = solid_predict(name, D.resolve_conj().numpy(), ao, grad_ao, grad2_ao, weights, kweights, h1e, rep,
+                             nuclear_repulsion, clip_cte)
+    return E, D.resolve_conj().numpy(), F, mo_e.numpy()

@@ -84,7 +84,42 @@ def main(root):
     ref = jaxshim.load_reference(root, with_solid=True)
     for case, kpts in KPTS.items():
         make_case(ref, case, solid_inputs(kpts=kpts))
+    make_scf_case(ref, root)
     torch.Tensor.transpose = _orig_transpose
+
+
+def make_scf_case(ref, root, cycles=4):
+    """diff_simple_scf_loop (evaluate.py:256-344) on a Solid: linear mixing with the k-point predict."""
+    ev = jaxshim.load_scf(root, ref)
+    sol = ref.solid
+    inp = solid_inputs(kpts=KPTS["solid_small_k"])
+    g = np.random.default_rng(77)
+    K, n = inp["rdm1"].shape[1], inp["rdm1"].shape[2]
+    s1e = np.empty((K, n, n), dtype=np.complex128)
+    for k in range(K):
+        m = g.standard_normal((n, n)) + 1j * g.standard_normal((n, n))
+        s1e[k] = np.eye(n) + 0.05 * (m @ m.conj().T) / n
+    mo_occ = np.zeros((2, K, n))
+    mo_occ[:, :, :2] = 1.0
+    c = lambda x: torch.as_tensor(x, dtype=torch.complex128)  # noqa: E731
+    f = lambda x: torch.as_tensor(x, dtype=torch.float64)  # noqa: E731
+    kinfo = sol.KPointInfo(kpts_abs=f(inp["kpts"]), kpts_scaled=f(inp["kpts"]), weights=f(inp["kweights"]))
+    solid = sol.Solid(grid=sol.Grid(coords=f(inp["coords"]), weights=f(inp["weights"])), kpt_info=kinfo,
+                      atom_index=torch.tensor([1, 1]), lattice_vectors=f(np.eye(3) * 3.6),
+                      nuclear_pos=f(np.zeros((2, 3))), ao=c(inp["ao"]), grad_ao=c(inp["grad_ao"]),
+                      grad_n_ao={2: c(inp["grad2_ao"])}, rdm1=c(inp["rdm1"]),
+                      nuclear_repulsion=f(inp["nuclear_repulsion"]), h1e=c(inp["h1e"]), vj=None, mo_coeff=None,
+                      mo_occ=f(mo_occ), mo_energy=None, rep_tensor=c(inp["rep"]), s1e=c(s1e))
+    out = dict(inp, s1e=s1e, mo_occ_init=mo_occ, cycles=np.array(cycles))
+    for name in ("LSDA", "B88"):
+        final = ev.diff_simple_scf_loop(getattr(ref.popular, name), cycles=cycles)({"params": {}}, solid)
+        out[f"energy_{name}"] = np.asarray(final.energy.detach())
+        out[f"rdm1_{name}"] = final.rdm1.detach().resolve_conj().numpy()
+        out[f"fock_{name}"] = final.fock.detach().resolve_conj().numpy()
+        out[f"mo_energy_{name}"] = final.mo_energy.detach().numpy()
+    path = os.path.join(HERE, "ref_solid_scf.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path))
 
 
 def make_case(ref, case, inp):

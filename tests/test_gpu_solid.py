@@ -86,5 +86,22 @@ def test_energy_and_errors(G, golden, case="solid_small_k"):
         s.select_HF_omegas([0.0])
     with pytest.raises(NotImplementedError):
         G.energy_predictor(G.B3LYP)({"params": {}}, s)
+    with pytest.raises(NotImplementedError):
+        G.diff_scf_loop(G.LSDA, cycles=2)({"params": {}}, s)
     with pytest.raises(ValueError):
         s.replace(rdm1=torch.zeros((2, 2, 2, 2), dtype=torch.complex128, device="cuda")).density()
+
+
+@pytest.mark.parametrize("name", ["LSDA", "B88"])
+@pytest.mark.parametrize("precision,rtol_e,rtol_m", [("fp64", 1e-11, 1e-9), ("tf32x3", 1e-6, 1e-5)])
+def test_scf_loop(G, golden, name, precision, rtol_e, rtol_m):
+    """diff_simple_scf_loop with a Solid (evaluate.py:256-344) against the reference's own loop."""
+    g = golden("solid_scf")
+    s = _solid(G, g, precision).replace(s1e=torch.as_tensor(g["s1e"], device="cuda"),
+                                        mo_occ=torch.as_tensor(g["mo_occ_init"]))
+    final = G.diff_simple_scf_loop(getattr(G, name), cycles=int(g["cycles"]))({"params": {}}, s)
+    ref_e = float(g[f"energy_{name}"])
+    assert abs(float(final.energy) - ref_e) <= rtol_e * abs(ref_e)
+    _close(final.rdm1, g[f"rdm1_{name}"], rtol_m, "rdm1")
+    _close(final.fock, g[f"fock_{name}"], rtol_m, "fock")
+    _close(final.mo_energy, g[f"mo_energy_{name}"], rtol_m, "mo_energy")

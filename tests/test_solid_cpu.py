@@ -43,3 +43,16 @@ def test_predict(golden, name, case):
                              g["h1e"], g["rep"], float(g["nuclear_repulsion"]))
     assert abs(E - float(g[f"E_{name}"])) <= 1e-13 * abs(float(g[f"E_{name}"]))
     _same(F, g[f"F_{name}"])
+
+
+@pytest.mark.parametrize("name", ["LSDA", "B88"])
+def test_scf_loop(golden, name):
+    """diff_simple_scf_loop with a Solid (evaluate.py:256-344), run by the reference for the fixture."""
+    g = golden("solid_scf")
+    E, D, F, mo_e = OSd.solid_scf_loop(name, g["rdm1"], g["mo_occ_init"], g["ao"], g["grad_ao"], g["grad2_ao"],
+                                       g["weights"], g["kweights"], g["h1e"], g["s1e"], g["rep"],
+                                       float(g["nuclear_repulsion"]), int(g["cycles"]))
+    assert abs(E - float(g[f"energy_{name}"])) <= 1e-12 * abs(float(g[f"energy_{name}"]))
+    _same(D, g[f"rdm1_{name}"], 1e-10)
+    _same(F, g[f"fock_{name}"], 1e-10)
+    _same(mo_e, g[f"mo_energy_{name}"], 1e-10)
