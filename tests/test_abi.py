@@ -95,3 +95,22 @@ def test_network_layout_host_side(built_lib):
     assert lib.gdft_network_param_count(ctypes.byref(wrong.desc), ctypes.byref(n)) == _lib.GDFT_ERR_INVALID
     with pytest.raises(ValueError):
         net.flatten({"params": {"Dense_0": params["params"]["Dense_0"]}}, "cpu")
+
+
+def test_host_only_argument_checks_new_entries(built_lib):
+    """Basis, chi and k-point entries reject bad arguments before any device work."""
+    from graddft_gb300 import _lib
+
+    lib = _lib.load(built_lib)
+    nbytes = ctypes.c_size_t()
+    assert lib.gdft_eval_ao(None, None, 10, 1, None, None, None, None) == _lib.GDFT_ERR_INVALID
+    assert lib.gdft_molecule_eval_shells(None, None, None, None, None) == _lib.GDFT_ERR_INVALID
+    assert lib.gdft_nu_workspace_bytes(None, 0, ctypes.byref(nbytes)) == _lib.GDFT_ERR_INVALID
+    assert lib.gdft_nu_integrals(None, None, 10, 0.0, None, None, 0, None) == _lib.GDFT_ERR_INVALID
+    assert lib.gdft_chi(None, None, None, None, 10, None, 1, 8, None, None, 0, None) == _lib.GDFT_ERR_INVALID
+    assert lib.gdft_kpoint_workspace_bytes(None, 1, ctypes.byref(nbytes)) == _lib.GDFT_ERR_INVALID
+    assert lib.gdft_kpoint_fock(0, 4, None, None, None, 1e-30, None, None) == _lib.GDFT_ERR_INVALID
+    assert lib.gdft_kpoint_coulomb(0, 4, None, None, None, None, 0.0, None, None, None) == _lib.GDFT_ERR_INVALID
+    basis = _lib.GdftBasis()  # empty tables
+    assert lib.gdft_eval_ao(ctypes.byref(basis), None, 10, 1, None, None, None, None) == _lib.GDFT_ERR_INVALID
+    assert b"basis" in lib.gdft_last_error()
