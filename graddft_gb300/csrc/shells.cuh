@@ -63,6 +63,9 @@ __device__ __forceinline__ void poly(const double *__restrict__ t, double x, dou
     for (int ly = L - lx; ly >= 0; --ly) {
       const int lz = L - lx - ly;
       const double c = t[idx++];
+      // the lanes of a warp evaluate the same AO row (warp-uniform branch): solid-harmonic
+      // rows are mostly zero, and a zero term adds nothing
+      if (c == 0.0) continue;
       const double X0 = xp[lx], Y0 = yp[ly], Z0 = zp[lz];
       const double X1 = lx > 0 ? lx * xp[lx > 0 ? lx - 1 : 0] : 0.0;
       const double Y1 = ly > 0 ? ly * yp[ly > 0 ? ly - 1 : 0] : 0.0;
