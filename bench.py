@@ -538,8 +538,11 @@ def run_hf(args):
     n_ao = args.n_ao if args.n_ao != N_AO else 128
     wl = synthetic.make_workload(n_grid, n_ao, max(1, n_ao // 8), SEED)
     t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64, device=dev)  # noqa: E731
+    form = args.form or "fp64"
     r = G.engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "fp64", dev)
     ao = r.ao_planes()[0, :n_grid, :n_ao].contiguous()  # phi as evaluated on the device
+    if form == "tf32x3":  # contractions and network in the mixed form; exact exchange stays FP64
+        r = G.engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "tf32x3", dev)
     chi = synthetic.make_chi(ao.cpu().numpy(), wl.rdm1, n_omega=2, seed=SEED)
     rng = np.random.default_rng(SEED)
     h = rng.standard_normal((n_ao, n_ao))
@@ -547,9 +550,9 @@ def run_hf(args):
     mol = G.Molecule(grid=G.Grid(coords=None, weights=t(wl.weights)), atom_index=None, nuclear_pos=None, ao=ao,
                      grad_ao=None, grad_n_ao=None, rdm1=t(wl.rdm1), nuclear_repulsion=1.0, h1e=t(0.5 * (h + h.T)),
                      vj=None, mo_coeff=None, mo_occ=None, mo_energy=None, rep_tensor=t(eri), omegas=[0.0, 0.4],
-                     chi=t(chi), _resident=r)
+                     chi=t(chi), precision=form, _resident=r)
     params = synthetic.glorot_params(seed=SEED)
-    predict = G.energy_predictor(G.DM21())
+    predict = G.energy_predictor(G.DM21(precision=form))
     for _ in range(max(1, args.warmup)):
         predict(params, mol)
     torch.cuda.synchronize()
@@ -566,10 +569,12 @@ def run_hf(args):
     line = {
         "metric": "DM21 predict with exact-exchange terms from chi, grid-pts/s (E, Fock)", "value": n_grid / (ms * 1e-3),
         "unit": "grid-pts/s", "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup), "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "fp64" else form,
         "data": "synthetic (seeded basis, rdm1, stand-in chi tensor, random symmetric h1e and eri)",
         "config": {"workload": f"DM21 energy_predictor with chi: n_ao {n_ao}, n_grid {n_grid}, omegas (0, 0.4)",
-                   "n_ao": n_ao, "n_grid": n_grid, "network": "DM21 6 x 256, FP64 form",
+                   "n_ao": n_ao, "n_grid": n_grid,
+                   "network": "DM21 6 x 256, " + ("FP64 form" if form == "fp64" else "TF32x3 tensor-core form"),
+                   "form": form,
                    "l2": "inputs larger than L2 (chi %.2f GiB)" % (chi.nbytes / 2**30)},
         "clocks": clk.summary(),
     }

@@ -883,9 +883,8 @@ int gdft_neural_xc_hf_grads(const gdft_molecule *mol, const double *d_rdm1, cons
   int rc = check_mol(mol);
   if (rc) return rc;
   if ((rc = check_network(net))) return rc;
-  if (net->precision != GDFT_FP64 || net->n_in != kDm21In || net->n_out != kDm21Out) {
-    set_error("gdft_neural_xc_hf_grads: the HF gradients are built for the FP64 DM21 network form "
-              "(11 inputs, 3 outputs)");
+  if (net->n_in != kDm21In || net->n_out != kDm21Out) {
+    set_error("gdft_neural_xc_hf_grads: the HF gradients are built for the DM21 network (11 inputs, 3 outputs)");
     return GDFT_ERR_INVALID;
   }
   const size_t need = neural_ws_bytes(mol, net);
@@ -914,13 +913,26 @@ int gdft_neural_xc_hf_grads(const gdft_molecule *mol, const double *d_rdm1, cons
   double *mws = (double *)(ws + W.bytes);
   {
     StageTimer tm(GDFT_STAGE_MLP, st);
-    if ((rc = mlp_run_f64(net_shape(net), d_params, nullptr, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
-                          net->clip, mws, d_exc, coef, st)))
-      return rc;
+    if (net->precision == GDFT_TF32X3)
+      rc = mlp_run_tc(net_shape(net), d_params, nullptr, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
+                      net->clip, ws + W.bytes, d_exc, coef, (int *)(ws + W.off_err), st);
+    else
+      rc = mlp_run_f64(net_shape(net), d_params, nullptr, feat, d_ehf, mol_w(mol), mol->n_grid, mol->n_grid_pad,
+                       net->clip, mws, d_exc, coef, st);
+    if (rc) return rc;
   }
-  if ((rc = check_cuda(launch_dm21_hf_grads(net_shape(net), mol->n_grid, mol->n_grid_pad, mws, d_g_dens, d_g_cin, st),
-                       "dm21_hf_grads")))
-    return rc;
+  if (net->precision == GDFT_TF32X3) {
+    const MlpTcLayout T = mlp_tc_layout(net_shape(net), mol->n_grid_pad);
+    const char *nws = ws + W.bytes;
+    rc = check_cuda(launch_dm21_hf_grads_from((const double *)(nws + T.x), (const double *)(nws + T.du),
+                                              (const double *)(nws + T.de), mol->n_grid, net->squash_offset,
+                                              d_g_dens, d_g_cin, st),
+                    "dm21_hf_grads");
+  } else {
+    rc = check_cuda(launch_dm21_hf_grads(net_shape(net), mol->n_grid, mol->n_grid_pad, mws, d_g_dens, d_g_cin, st),
+                    "dm21_hf_grads");
+  }
+  if (rc) return rc;
   if (d_vxc == nullptr) return GDFT_OK;
   return run_vxc(mol, coef, d_vxc, ws, st);
 }

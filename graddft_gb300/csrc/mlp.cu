@@ -374,8 +374,13 @@ __global__ void dm21_hf_grads_kernel(const double *__restrict__ x, const double 
 cudaError_t launch_dm21_hf_grads(const MlpShape &S, int64_t n_grid, int64_t np, const double *ws, double *g_dens,
                                  double *g_cin, cudaStream_t st) {
   const MlpLayout L = mlp_layout(S, np);
-  dm21_hf_grads_kernel<<<(unsigned)((n_grid + 255) / 256), 256, 0, st>>>(ws + L.x, ws + L.du, ws + L.de, n_grid,
-                                                                          S.squash_offset, g_dens, g_cin);
+  return launch_dm21_hf_grads_from(ws + L.x, ws + L.du, ws + L.de, n_grid, S.squash_offset, g_dens, g_cin, st);
+}
+
+cudaError_t launch_dm21_hf_grads_from(const double *x, const double *du, const double *de, int64_t n_grid,
+                                      double squash_offset, double *g_dens, double *g_cin, cudaStream_t st) {
+  dm21_hf_grads_kernel<<<(unsigned)((n_grid + 255) / 256), 256, 0, st>>>(x, du, de, n_grid, squash_offset, g_dens,
+                                                                          g_cin);
   return cudaGetLastError();
 }
 

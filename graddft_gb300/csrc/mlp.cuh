@@ -50,6 +50,10 @@ int mlp_run_f64(const MlpShape &S, const double *params, double *dparams, const 
 // energy-density columns and through the HF inputs (either may be null).
 cudaError_t launch_dm21_hf_grads(const MlpShape &S, int64_t n_grid, int64_t np, const double *ws, double *g_dens,
                                  double *g_cin, cudaStream_t st);
+// The same from the network pass's FP64 inputs x [np][11], input gradients du
+// [np][16] and energy-density gradients de [np][3] (either network form).
+cudaError_t launch_dm21_hf_grads_from(const double *x, const double *du, const double *de, int64_t n_grid,
+                                      double squash_offset, double *g_dens, double *g_cin, cudaStream_t st);
 
 // Scratch of the second-order pass (offsets in doubles).  Primal and tangent
 // activations are stacked as [2][np][width] so one GEMM serves both.

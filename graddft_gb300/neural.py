@@ -245,7 +245,7 @@ class NeuralFunctional(Functional):
         coefficient_input_grads), the same network pass also makes dE/d ehf for them.
         """
         hf_terms = self.densitygrads is not None or self.coefficient_input_grads is not None
-        if hf_terms and getattr(atoms, "chi", None) is not None and self.precision == "fp64":
+        if hf_terms and getattr(atoms, "chi", None) is not None:
             self._check_slots()
             r = atoms.resident()
             net = self.network(clip_cte)
@@ -304,8 +304,6 @@ class NeuralFunctional(Functional):
             return cached
         r = atoms.resident()
         net = self.network(clip_cte)
-        if net.precision != "fp64":
-            raise NotImplementedError("the HF gradients of the network run in its FP64 form (precision='fp64')")
         _, _, g_dens, g_cin = r.neural_xc_hf_grads(atoms._rdm1(), net, net.flatten(params, r.device), ehf)
         self.__dict__["_hf_cache"] = (self._hf_key(params, atoms, clip_cte), (g_dens, g_cin))
         return g_dens, g_cin

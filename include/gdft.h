@@ -310,7 +310,7 @@ int gdft_neural_xc_energy_and_grads(const gdft_molecule *mol, const double *d_rd
                                     const double *d_params, const double *d_ehf, double *d_exc, double *d_vxc,
                                     double *d_dparams, void *d_ws, size_t ws_bytes, void *stream);
 
-/* DM21 network (FP64 form, omegas 0 and 0.4) in one pass: E_xc into d_exc,
+/* DM21 network (either network form, omegas 0 and 0.4) in one pass: E_xc into d_exc,
  * optionally V_xc = dE_xc/d rdm1 into d_vxc, and dE_xc/d ehf[w][s][r]
  * (2, 2, n_grid) through the HF energy-density columns (d_g_dens: the
  * gradient of HF_density_grad_2_Fock, molecule.py:598-603) and through the HF

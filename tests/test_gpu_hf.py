@@ -124,3 +124,20 @@ def test_dm21_predict_with_chi(G, golden):
     E, F = G.energy_predictor(G.DM21())(params, mol)
     assert abs(float(E) - float(g["predict_E_DM21"])) <= RTOL * abs(float(g["predict_E_DM21"]))
     _close(F, g["predict_F_DM21"], what="F")
+
+
+def test_dm21_hf_terms_and_predict_mixed_network(G, golden):
+    """The same with the tensor-core (TF32x3) network: E to 1e-6 relative, the HF terms and F to 2e-5 of
+    their largest entries (the network's FP32 activations; the exchange contractions stay FP64)."""
+    g = golden("hf")
+    mol = _molecule(G, g)
+    params = synthetic.glorot_params(seed=int(g["theta_seed"]))
+    dm21 = G.DM21(precision="tf32x3")
+    ehf = mol.HF_energy_density([0.0, 0.4])
+    fd = G.neural.dm21_hfgrads_densities(dm21, params, mol, ehf, None, None)
+    fc = G.neural.dm21_hfgrads_cinputs(dm21, params, mol, ehf, None, None)
+    _close(fd, g["dm21_hfgrads_densities"], rtol=2e-5, what="HF term through the densities (mixed network)")
+    _close(fc, g["dm21_hfgrads_cinputs"], rtol=2e-5, what="HF term through the inputs (mixed network)")
+    E, F = G.energy_predictor(dm21)(params, mol)
+    assert abs(float(E) - float(g["predict_E_DM21"])) <= 1e-6 * abs(float(g["predict_E_DM21"]))
+    _close(F, g["predict_F_DM21"], rtol=2e-5, what="F (mixed network)")
