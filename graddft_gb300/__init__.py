@@ -31,7 +31,8 @@ from .popular_functionals import (
     vwn_density,
 )
 from .train import energy_predictor
-from .scf import JittableDiis, diff_scf_loop, diff_simple_scf_loop, safe_eigh, safe_fock_solver, safe_general_eigh
+from .scf import (JittableDiis, diff_scf_loop, diff_simple_scf_loop, non_scf_predictor, safe_eigh, safe_fock_solver,
+                  safe_general_eigh, simple_scf_loop)
 from .basis import ShellBasis, eval_ao, molecule_from_basis
 from . import chi
 from .solid import KPointInfo, Solid
@@ -46,5 +47,5 @@ __all__ = [
     "energy_predictor", "DM21", "NeuralFunctional", "dm21_coefficient_inputs", "dm21_hfgrads_cinputs",
     "dm21_hfgrads_densities", "diff_simple_scf_loop", "diff_scf_loop", "JittableDiis", "safe_eigh",
     "safe_fock_solver", "safe_general_eigh", "ShellBasis", "eval_ao", "molecule_from_basis",
-    "generate_chi_tensor", "Solid", "KPointInfo",
+    "generate_chi_tensor", "Solid", "KPointInfo", "simple_scf_loop", "non_scf_predictor",
 ]

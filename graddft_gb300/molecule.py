@@ -121,6 +121,22 @@ class Molecule:
         """molecule.py:144-151 -> (grid, spin)."""
         return self.resident().density(self._rdm1(), want=("tau",))["tau"]
 
+    # ------------------------------------------------------------- orbitals
+    def make_rdm1(self, *args, **kwargs):
+        """molecule.py:816-846: D_s = C_s diag(occ_s) C_s^T."""
+        from .scf import make_rdm1
+
+        dev = self.device
+        return make_rdm1(engine.as_device_f64(self.mo_coeff, dev), engine.as_device_f64(self.mo_occ, dev))
+
+    def get_occ(self):
+        """molecule.py:848-889: the nelec lowest orbitals of each spin, nelec from mo_occ."""
+        from .scf import get_occ
+
+        mo_occ = torch.as_tensor(self.mo_occ)
+        nelecs = [int(round(float(mo_occ[s].sum()))) for s in range(2)]
+        return get_occ(engine.as_device_f64(self.mo_energy, self.device), nelecs)
+
     # --------------------------------------------------------- non-XC parts
     def get_coulomb_potential(self, *args, **kwargs):
         """molecule.py:110-115: J from rep_tensor and rdm1 summed over spin."""

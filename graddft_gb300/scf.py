@@ -29,6 +29,7 @@ from typing import Callable
 
 import torch
 
+from . import engine
 from .functional import CLIP
 
 DEGEN_TOL = 1e-6
@@ -197,6 +198,70 @@ def _solid_scf(functional, params, atoms, cycles, mixing_factor, clip_cte):
         energy, fock = predict(params, atoms)
         atoms = atoms.replace(fock=fock, energy=energy)
     return atoms
+
+
+def non_scf_predictor(functional, chunk_size: int = 1024, **kwargs) -> Callable:
+    """evaluate.py:88-126: ``predictor(params, atoms) -> atoms`` with the energy and Fock matrix of
+    ``energy_predictor`` at the given density (``chunk_size`` is accepted for signature compatibility)."""
+    from .train import energy_predictor
+
+    predict = energy_predictor(functional, **kwargs)
+
+    def non_scf_predictor(params, atoms, *args):
+        energy, fock = predict(params, atoms, *args)
+        return atoms.replace(fock=fock, energy=energy)
+
+    return non_scf_predictor
+
+
+def simple_scf_loop(functional, mixing_factor: float = 0.4, chunk_size: int = 1024, cycles: int = 50,
+                    start_cycle: int = 0, e_conv: float = 1e-5, g_conv: float = 1e-5, verbose: int = 0,
+                    **kwargs) -> Callable:
+    """evaluate.py:131-254: the non-jitted linear-mixing loop, as the reference runs it.
+
+    Cycle 0 takes the incoming orbitals (no diagonalisation), occupies them and
+    keeps their density matrix as the one to mix with, while the energy and
+    Fock matrix are evaluated at the incoming rdm1; later cycles diagonalise the
+    previous Fock matrix and mix.  Every cycle checks that the grid integral of
+    the density matches atom_index.sum() - charge to 1e-3 (AssertionError
+    otherwise).  All ``cycles`` run (``e_conv`` and ``g_conv`` are unused, as in
+    the reference); ``chunk_size``, ``start_cycle`` and ``verbose`` are accepted
+    for signature compatibility.
+    """
+    from .train import energy_predictor
+
+    predict = energy_predictor(functional, **kwargs)
+
+    def simple_scf_iterator(params, atoms, clip_cte=CLIP, *args):
+        solid = getattr(atoms, "is_solid", False)
+        dev = atoms.device
+        nelectron = float(torch.as_tensor(atoms.atom_index).sum()) - float(atoms.charge)
+        fock = atoms.fock
+        old_rdm1 = None
+        predicted_e = None
+        for cycle in range(cycles):
+            if cycle > 0:
+                if solid:
+                    mo_energy, mo_coeff = solid_fock_solver(fock, torch.as_tensor(atoms.s1e).to(dev, torch.complex128))
+                else:
+                    mo_energy, mo_coeff = safe_fock_solver(fock, engine.as_device_f64(atoms.s1e, dev))
+                atoms = atoms.replace(mo_coeff=mo_coeff, mo_energy=mo_energy)
+            atoms = atoms.replace(mo_occ=atoms.get_occ())
+            if cycle == 0:
+                old_rdm1 = atoms.make_rdm1()
+            else:
+                rdm1 = (1 - mixing_factor) * old_rdm1 + mixing_factor * atoms.make_rdm1()
+                atoms = atoms.replace(rdm1=rdm1)
+                old_rdm1 = rdm1
+            w = engine.as_device_f64(atoms.grid.weights, dev)
+            computed_charge = float(torch.einsum("r,rs->", w, atoms.density()))
+            assert abs(nelectron - computed_charge) <= 1e-3 + 1e-5 * abs(computed_charge), (
+                "Total charge is not conserved. given electrons: %.3f, computed electrons: %.3f"
+                % (nelectron, computed_charge))
+            predicted_e, fock = predict(params, atoms, *args)
+        return atoms.replace(fock=fock, energy=predicted_e)
+
+    return simple_scf_iterator
 
 
 def diff_simple_scf_loop(functional, cycles: int = 25, mixing_factor: float = 0.4,

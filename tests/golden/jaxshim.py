@@ -137,6 +137,9 @@ def _mk_jnp():
     m.less = lambda a, b: torch.less(_t(a), _t(b))
     m.logical_and = lambda a, b: torch.logical_and(_t(a), _t(b))
 
+    m.isclose = lambda a, b, rtol=1e-05, atol=1e-08, equal_nan=False: torch.isclose(
+        _t(a).to(F64), _t(b).to(F64), rtol=rtol, atol=atol, equal_nan=equal_nan)
+
     def einsum(subscripts, *ops, precision=None, **_):
         ts = [_t(o) for o in ops]
         if any(t.is_complex() for t in ts):  # jnp.einsum promotes mixed real/complex operands

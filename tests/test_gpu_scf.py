@@ -244,3 +244,44 @@ def test_diis_scf_loop_vs_reference(G, golden, precision):
         worst = max(worst, err)
         assert err <= g_tol, (key, err)
     print(precision, "max rel d(dE/dtheta) per leaf", worst)
+
+
+def _simple_scf_molecule(G, g, precision):
+    t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64, device="cuda")  # noqa: E731
+    return G.Molecule(grid=G.Grid(coords=t(g["coords"]), weights=t(g["weights"])),
+                      atom_index=torch.as_tensor(g["atom_index"]), nuclear_pos=None, ao=t(g["ao"]),
+                      grad_ao=t(g["grad_ao"]), grad_n_ao={2: t(g["grad2_ao"])}, rdm1=t(g["rdm1"]),
+                      nuclear_repulsion=float(g["nuclear_repulsion"]), h1e=t(g["h1e"]), vj=None,
+                      mo_coeff=t(g["mo_coeff"]), mo_occ=t(g["mo_occ"]), mo_energy=t(g["mo_energy"]),
+                      s1e=t(g["s1e"]), rep_tensor=t(g["eri"]), fock=t(np.zeros_like(g["h1e"])), charge=0,
+                      precision=precision)
+
+
+@pytest.mark.parametrize("name", ["B88", "LSDA"])
+@pytest.mark.parametrize("precision,rtol_e,rtol_m", [("fp64", 1e-11, 1e-9), ("tf32x3", 1e-6, 2e-5)])
+def test_simple_scf_loop_and_non_scf_predictor_vs_reference(G, golden, name, precision, rtol_e, rtol_m):
+    """simple_scf_loop (evaluate.py:131-254) and non_scf_predictor (evaluate.py:88-126) against the
+    reference's own functions (tests/golden/make_golden_simple_scf.py)."""
+    g = golden("simple_scf")
+    mol = _simple_scf_molecule(G, g, precision)
+    fn = getattr(G, name)
+    final = G.simple_scf_loop(fn, mixing_factor=float(g["mixing_factor"]), cycles=int(g["cycles"]))(
+        {"params": {}}, mol)
+    ref_e = float(g[f"energy_{name}"])
+    assert abs(float(final.energy) - ref_e) <= rtol_e * abs(ref_e)
+    for key, got in (("rdm1", final.rdm1), ("fock", final.fock), ("mo_energy", final.mo_energy)):
+        ref = g[f"{key}_{name}"]
+        err = float(np.max(np.abs(got.detach().cpu().numpy() - ref)))
+        assert err <= rtol_m * float(np.max(np.abs(ref))), (key, err)
+    nsp = G.non_scf_predictor(fn)({"params": {}}, mol)
+    assert abs(float(nsp.energy) - float(g[f"nonscf_energy_{name}"])) <= rtol_e * abs(float(g[f"nonscf_energy_{name}"]))
+    err = float(np.max(np.abs(nsp.fock.detach().cpu().numpy() - g[f"nonscf_fock_{name}"])))
+    assert err <= rtol_m * float(np.max(np.abs(g[f"nonscf_fock_{name}"])))
+
+
+def test_simple_scf_loop_charge_check(G, golden):
+    """The loop's charge assertion (evaluate.py:212-220) fires when the electron count does not match."""
+    g = golden("simple_scf")
+    mol = _simple_scf_molecule(G, g, "fp64").replace(charge=1)
+    with pytest.raises(AssertionError):
+        G.simple_scf_loop(G.LSDA, cycles=2)({"params": {}}, mol)
