@@ -90,6 +90,26 @@ class _XcEnergy(torch.autograd.Function):
         return g * vxc, None, None, None
 
 
+class _XcEnergyPotential(torch.autograd.Function):
+    """(E_xc, V_xc) from one device pass; E_xc is differentiable in rdm1 (its gradient is V_xc).  A
+    gradient flowing into V_xc would need the functional's second derivative, which is built for the
+    DM21 network (NeuralFunctional) only."""
+
+    @staticmethod
+    def forward(ctx, rdm1, resident, fn, ehf):
+        exc, vxc = resident.xc_energy_and_grads(rdm1.detach(), fn, ehf, want_vxc=True)
+        ctx.save_for_backward(vxc)
+        return exc, vxc
+
+    @staticmethod
+    def backward(ctx, g_exc, g_vxc):
+        (vxc,) = ctx.saved_tensors
+        if g_vxc is not None and bool(torch.any(g_vxc != 0)):
+            raise NotImplementedError("second derivatives of constant-coefficient functionals are not built; "
+                                      "differentiate through V_xc with a NeuralFunctional (DM21)")
+        return (None if g_exc is None else g_exc * vxc), None, None, None
+
+
 @dataclass
 class Functional:
     """functional.py:48-342."""
@@ -170,6 +190,13 @@ class Functional:
         """(E_xc, dE_xc/d rdm1) through the fused device path (train.py:86-121)."""
         fn, ehf = self.spec(params, atoms, clip_cte)
         return atoms.resident().xc_energy_and_grads(atoms._rdm1(), fn, ehf, want_vxc=True)
+
+    def xc_energy_and_potential(self, params, atoms, clip_cte: float = CLIP):
+        """(E_xc, V_xc) of one device pass, E_xc differentiable in rdm1 (as the energies of the SCF
+        loops and the orbital optimisers need); V_xc is a constant of the autograd graph."""
+        fn, ehf = self.spec(params, atoms, clip_cte)
+        rdm1 = atoms.rdm1 if isinstance(atoms.rdm1, torch.Tensor) and atoms.rdm1.requires_grad else atoms._rdm1()
+        return _XcEnergyPotential.apply(rdm1, atoms.resident(), fn, ehf)
 
     def hf_density_gradient(self, params, atoms, ehf, clip_cte: float = CLIP):
         """dE_xc/d ehf (omega, spin, grid) through the densities, the gradient that

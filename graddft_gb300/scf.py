@@ -377,3 +377,101 @@ def diff_scf_loop(functional, cycles: int = 25, clip_cte: float = CLIP, max_diis
         return atoms.replace(energy=energy)
 
     return iterator
+
+
+# ------------------------------------------------------ orbital optimisers
+def canonical_eigvec_signs(v: torch.Tensor) -> torch.Tensor:
+    """Eigenvectors (columns) with their largest-magnitude component made positive."""
+    idx = torch.argmax(v.abs(), dim=-2, keepdim=True)
+    sign = torch.sign(torch.gather(v, -2, idx))
+    return v * torch.where(sign == 0, torch.ones_like(sign), sign)
+
+
+def _whitening(s1e, whitening: str):
+    """evaluate.py:723-735: D with C = Q D for orthogonal Q (PCA, Cholesky or ZCA).
+
+    PCA's D = diag(w^-1/2) v^T depends on the signs of the eigenvectors, which
+    eigensolvers choose freely (the reference's result changes with its LAPACK);
+    here each eigenvector is made to have its largest-magnitude component positive."""
+    if whitening == "PCA":
+        w, v = torch.linalg.eigh(s1e)
+        return torch.diag(torch.sqrt(1.0 / w)) @ canonical_eigvec_signs(v).T
+    if whitening == "Cholesky":
+        return torch.linalg.cholesky(torch.linalg.inv(s1e)).T
+    if whitening == "ZCA":
+        w, v = torch.linalg.eigh(s1e)
+        return v @ torch.diag(torch.sqrt(1.0 / w)) @ v.T
+    raise ValueError(f"whitening must be 'PCA', 'Cholesky' or 'ZCA', got {whitening!r}")
+
+
+def _orbital_energy(functional, params, atoms, W, D, clip_cte):
+    """evaluate.py:640-692: E(W) with Q = qr(W_s), C = Q D, rdm1 = C occ C^T (differentiable in W)."""
+    Q = torch.stack([torch.linalg.qr(W[0])[0], torch.linalg.qr(W[1])[0]])
+    C = torch.einsum("sij,jk->ski", Q, D)
+    rdm1 = make_rdm1(C, atoms.mo_occ)
+    energy, _ = energy_and_fock(functional, params, atoms.replace(rdm1=rdm1, mo_coeff=C), clip_cte)
+    return energy
+
+
+def _orbital_setup(functional, params, atoms, clip_cte, whitening):
+    if getattr(atoms, "is_solid", False):
+        raise NotImplementedError("Solids with full BZ zampling not yet supported. Use simple_scf_loop instead.")
+    atoms = _to_device(atoms)
+    atoms = atoms.replace(mo_coeff=engine.as_device_f64(atoms.mo_coeff, atoms.device))
+    with torch.no_grad():
+        energy, _ = energy_and_fock(functional, params, atoms, clip_cte)
+    D = _whitening(atoms.s1e, whitening)
+    W = torch.einsum("sji,jk->sik", atoms.mo_coeff, torch.linalg.inv(D))  # C transposed
+    return atoms, energy, D, W
+
+
+def _orbital_step(functional, params, atoms, W, D, tx, opt_state, clip_cte):
+    from .optim import apply_updates
+
+    Wg = W.detach().requires_grad_(True)
+    with torch.enable_grad():
+        energy = _orbital_energy(functional, params, atoms, Wg, D, clip_cte)
+        (grads,) = torch.autograd.grad(energy, [Wg])
+    updates, opt_state = tx.update(grads, opt_state, W)
+    return energy.detach(), apply_updates(W, updates), opt_state
+
+
+def mol_orb_optimizer(fxc, tx, chunk_size: int = 1024, cycles: int = 500, e_conv: float = 1e-7,
+                      whitening: str = "PCA", precision=None, verbose: int = 0, clip_cte: float = CLIP,
+                      **kwargs) -> Callable:
+    """evaluate.py:595-780: minimise the predicted energy over the density matrix generated by
+    orthogonal orbitals C = qr(W) D (D4FT, Li et al., ICLR 2023), with the optax-protocol
+    optimiser ``tx`` (``graddft_gb300.optim.adam``), until |dE| in kcal/mol <= e_conv or ``cycles``.
+
+    As in the reference, the returned molecule carries the last evaluated energy (that of W
+    before its final update) and keeps its other fields."""
+    HARTREE2KCALMOL = 627.50947
+
+    def neural_iterator(params, molecule, *args):
+        atoms, predicted_e, D, W = _orbital_setup(fxc, params, molecule, clip_cte, whitening)
+        old_e = float("inf")
+        opt_state = tx.init(W)
+        cycle = 0
+        while abs(float(predicted_e) - old_e) * HARTREE2KCALMOL > e_conv and cycle < cycles:
+            old_e = float(predicted_e)
+            predicted_e, W, opt_state = _orbital_step(fxc, params, atoms, W, D, tx, opt_state, clip_cte)
+            cycle += 1
+            if verbose > 1:
+                print(f"cycle: {cycle}, predicted energy: {float(predicted_e):.7e}, "
+                      f"energy difference: {abs(float(predicted_e) - old_e):.4e}")
+        return molecule.replace(energy=predicted_e)
+
+    return neural_iterator
+
+
+def jitted_mol_orb_optimizer(functional, tx, cycles: int = 500, clip_cte: float = CLIP, **kwargs) -> Callable:
+    """evaluate.py:783-915: the same with PCA whitening and exactly ``cycles`` steps."""
+
+    def neural_iterator(params, molecule, *args):
+        atoms, predicted_e, D, W = _orbital_setup(functional, params, molecule, clip_cte, "PCA")
+        opt_state = tx.init(W)
+        for _ in range(cycles):
+            predicted_e, W, opt_state = _orbital_step(functional, params, atoms, W, D, tx, opt_state, clip_cte)
+        return molecule.replace(energy=predicted_e)
+
+    return neural_iterator

@@ -191,7 +191,8 @@ def _mk_jnp():
     m.reshape = lambda x, shape: torch.reshape(_t(x), shape)
     m.argsort = lambda x: torch.argsort(_t(x))
     m.linalg = types.SimpleNamespace(norm=lambda x: torch.linalg.norm(_t(x)), inv=torch.linalg.inv,
-                                     eigh=torch.linalg.eigh, cholesky=torch.linalg.cholesky)
+                                     eigh=torch.linalg.eigh, cholesky=torch.linalg.cholesky,
+                                     qr=lambda x: torch.linalg.qr(_t(x)))
     return m
 
 
@@ -510,7 +511,27 @@ def install():
     optax = types.ModuleType("optax")
     optax.OptState = object
     optax.GradientTransformation = object
-    optax.apply_updates = lambda p, u: p
+    optax.apply_updates = lambda p, u: p + u
+
+    class _Adam:
+        """optax.adam (scale_by_adam with bias correction, then scale by -learning_rate), for the
+        orbital-optimiser fixtures; optax itself is not installed."""
+
+        def __init__(self, learning_rate, b1=0.9, b2=0.999, eps=1e-8, eps_root=0.0):
+            self.lr, self.b1, self.b2, self.eps, self.eps_root = learning_rate, b1, b2, eps, eps_root
+
+        def init(self, params):
+            return (0, torch.zeros_like(params), torch.zeros_like(params))
+
+        def update(self, grads, state, params=None):
+            count, mu, nu = state
+            mu = self.b1 * mu + (1 - self.b1) * grads
+            nu = self.b2 * nu + (1 - self.b2) * grads * grads
+            count += 1
+            mu_hat, nu_hat = mu / (1 - self.b1 ** count), nu / (1 - self.b2 ** count)
+            return -self.lr * mu_hat / (torch.sqrt(nu_hat + self.eps_root) + self.eps), (count, mu, nu)
+
+    optax.adam = _Adam
     orbax = types.ModuleType("orbax")
     ock = types.ModuleType("orbax.checkpoint")
     ock.Checkpointer = object

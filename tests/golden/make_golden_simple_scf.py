@@ -1,4 +1,5 @@
-"""Golden fixture of simple_scf_loop and non_scf_predictor, made by running the reference's own code.
+"""Golden fixture of simple_scf_loop, non_scf_predictor and the orbital optimisers, made by running
+the reference's own code.
 
 Usage (needs the reference checkout; this is not run by the tests):
 
@@ -70,10 +71,35 @@ def system():
                 nuclear_repulsion=np.array(3.1), atom_index=np.array([2 * N_OCC]))
 
 
+def orbital_system(inp, seed=SEED + 1):
+    """The system in the basis phi M (M SPD, eigenvalues in [0.7, 1.4]): S = M^T S M, h and the ERIs
+    transformed alike, orbitals M^-1 C (so C^T S C is unchanged) and D = M^-1 D M^-T."""
+    g = np.random.default_rng(seed)
+    q, _ = np.linalg.qr(g.standard_normal((N_AO, N_AO)))
+    M = (q * np.linspace(0.7, 1.4, N_AO)) @ q.T
+    Mi = np.linalg.inv(M)
+    return dict(ao=inp["ao"] @ M, grad_ao=np.einsum("rai,ab->rbi", inp["grad_ao"], M),
+                grad2_ao=np.einsum("rai,ab->rbi", inp["grad2_ao"], M), s1e=M.T @ inp["s1e"] @ M,
+                h1e=M.T @ inp["h1e"] @ M, eri=np.einsum("abcd,ap,bq,cr,ds->pqrs", inp["eri"], M, M, M, M),
+                mo_coeff=np.einsum("ab,sbj->saj", Mi, inp["mo_coeff"]),
+                rdm1=np.einsum("ab,sbc,dc->sad", Mi, inp["rdm1"], Mi))
+
+
+def _eigh_canonical(a):
+    """torch.linalg.eigh with each eigenvector's largest-magnitude component positive: PCA whitening
+    (evaluate.py:723-727) depends on eigenvector signs, which LAPACK builds choose differently; the
+    library fixes the same convention.  Everything else the loops compute is invariant to it."""
+    w, v = torch.linalg.eigh(a)
+    idx = torch.argmax(v.abs(), dim=-2, keepdim=True)
+    sign = torch.sign(torch.gather(v, -2, idx))
+    return w, v * torch.where(sign == 0, torch.ones_like(sign), sign)
+
+
 def main(root):
     torch.Tensor.transpose = _transpose
     ref = jaxshim.load_reference(root)
     ev = jaxshim.load_scf(root, ref)
+    sys.modules["jax.numpy"].linalg.eigh = _eigh_canonical
     inp = system()
     t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64)  # noqa: E731
     mol = ref.molecule.Molecule(
@@ -94,6 +120,21 @@ def main(root):
         nsp = ev.non_scf_predictor(fn)({"params": {}}, mol)
         out[f"nonscf_energy_{name}"] = np.asarray(nsp.energy.detach())
         out[f"nonscf_fock_{name}"] = nsp.fock.detach().numpy()
+    # orbital optimisers (evaluate.py:595-915) with optax.adam(1e-2), 3 steps, B88, on the same system in
+    # a non-orthonormal basis (AOs times an SPD matrix M with spread eigenvalues): PCA whitening needs
+    # distinct overlap eigenvalues, and the orthonormalised system's overlap is the identity
+    orb = orbital_system(inp)
+    mol2 = mol.replace(ao=t(orb["ao"]), grad_ao=t(orb["grad_ao"]), grad_n_ao={2: t(orb["grad2_ao"])},
+                       s1e=t(orb["s1e"]), h1e=t(orb["h1e"]), rep_tensor=t(orb["eri"]), mo_coeff=t(orb["mo_coeff"]),
+                       rdm1=t(orb["rdm1"]))
+    out.update({f"orb/{k}": v for k, v in orb.items()})
+    optax = sys.modules["optax"]
+    for whitening in ("PCA", "Cholesky", "ZCA"):
+        m = ev.mol_orb_optimizer(ref.popular.B88, optax.adam(1e-2), cycles=3, whitening=whitening)({"params": {}},
+                                                                                                    mol2)
+        out[f"orb_energy_{whitening}"] = np.asarray(m.energy.detach())
+    m = ev.jitted_mol_orb_optimizer(ref.popular.B88, optax.adam(1e-2), cycles=3)({"params": {}}, mol2)
+    out["orb_energy_jitted"] = np.asarray(m.energy.detach())
     torch.Tensor.transpose = _orig_transpose
     path = os.path.join(HERE, "ref_simple_scf.npz")
     np.savez_compressed(path, **out)

@@ -285,3 +285,22 @@ def test_simple_scf_loop_charge_check(G, golden):
     mol = _simple_scf_molecule(G, g, "fp64").replace(charge=1)
     with pytest.raises(AssertionError):
         G.simple_scf_loop(G.LSDA, cycles=2)({"params": {}}, mol)
+
+
+@pytest.mark.parametrize("precision,rtol", [("fp64", 1e-9), ("tf32x3", 1e-5)])
+def test_orbital_optimizers_vs_reference(G, golden, precision, rtol):
+    """mol_orb_optimizer (PCA / Cholesky / ZCA whitening) and jitted_mol_orb_optimizer
+    (evaluate.py:595-915) with adam(1e-2), 3 steps, against the reference's own functions."""
+    g = golden("simple_scf")
+    t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64, device="cuda")  # noqa: E731
+    mol = _simple_scf_molecule(G, g, precision)
+    mol = mol.replace(ao=t(g["orb/ao"]), grad_ao=t(g["orb/grad_ao"]), grad_n_ao={2: t(g["orb/grad2_ao"])},
+                      s1e=t(g["orb/s1e"]), h1e=t(g["orb/h1e"]), rep_tensor=t(g["orb/eri"]),
+                      mo_coeff=t(g["orb/mo_coeff"]), rdm1=t(g["orb/rdm1"]))
+    for whitening in ("PCA", "Cholesky", "ZCA"):
+        m = G.mol_orb_optimizer(G.B88, G.optim.adam(1e-2), cycles=3, whitening=whitening)({"params": {}}, mol)
+        ref = float(g[f"orb_energy_{whitening}"])
+        assert abs(float(m.energy) - ref) <= rtol * abs(ref), (whitening, float(m.energy), ref)
+    m = G.jitted_mol_orb_optimizer(G.B88, G.optim.adam(1e-2), cycles=3)({"params": {}}, mol)
+    ref = float(g["orb_energy_jitted"])
+    assert abs(float(m.energy) - ref) <= rtol * abs(ref)
