@@ -31,7 +31,7 @@ from .popular_functionals import (
     vwn_density,
 )
 from .train import energy_predictor
-from .scf import (JittableDiis, diff_scf_loop, diff_simple_scf_loop, jitted_mol_orb_optimizer, mol_orb_optimizer,
+from .scf import (Diis, JittableDiis, diff_scf_loop, scf_loop, diff_simple_scf_loop, jitted_mol_orb_optimizer, mol_orb_optimizer,
                   non_scf_predictor, safe_eigh, safe_fock_solver, safe_general_eigh, simple_scf_loop)
 from . import optim
 from .basis import ShellBasis, eval_ao, molecule_from_basis
@@ -49,5 +49,5 @@ __all__ = [
     "dm21_hfgrads_densities", "diff_simple_scf_loop", "diff_scf_loop", "JittableDiis", "safe_eigh",
     "safe_fock_solver", "safe_general_eigh", "ShellBasis", "eval_ao", "molecule_from_basis",
     "generate_chi_tensor", "Solid", "KPointInfo", "simple_scf_loop", "non_scf_predictor",
-    "mol_orb_optimizer", "jitted_mol_orb_optimizer", "optim",
+    "mol_orb_optimizer", "jitted_mol_orb_optimizer", "optim", "scf_loop", "Diis",
 ]

@@ -137,6 +137,14 @@ class Molecule:
         nelecs = [int(round(float(mo_occ[s].sum()))) for s in range(2)]
         return get_occ(engine.as_device_f64(self.mo_energy, self.device), nelecs)
 
+    def get_mo_grads(self, *args, **kwargs):
+        """molecule.py:258-266 / 344-381: the orbital gradient as the reference computes it."""
+        from .scf import mo_grads
+
+        dev = self.device
+        return mo_grads(engine.as_device_f64(self.mo_coeff, dev), engine.as_device_f64(self.mo_occ, dev),
+                        engine.as_device_f64(self.fock, dev))
+
     # --------------------------------------------------------- non-XC parts
     def get_coulomb_potential(self, *args, **kwargs):
         """molecule.py:110-115: J from rep_tensor and rdm1 summed over spin."""

@@ -475,3 +475,140 @@ def jitted_mol_orb_optimizer(functional, tx, cycles: int = 500, clip_cte: float 
         return molecule.replace(energy=predicted_e)
 
     return neural_iterator
+
+
+# ------------------------------------------------------------ scf_loop
+def mo_grads(mo_coeff, mo_occ, fock):
+    """molecule.py:344-381 (orbital_grad as computed): sum over spins of C_vir^T F C_occ, with the
+    columns of C zeroed where the orbital is (un)occupied; (n, n)."""
+    c_occ = torch.where((mo_occ > 0)[:, None, :], mo_coeff, torch.zeros((), dtype=mo_coeff.dtype, device=mo_coeff.device))
+    c_vir = torch.where((mo_occ == 0)[:, None, :], mo_coeff, torch.zeros((), dtype=mo_coeff.dtype, device=mo_coeff.device))
+    return torch.einsum("sab,sac,scd->bd", c_vir, fock, c_occ)
+
+
+def damping(s, d, f, factor):
+    """evaluate.py:1477-1503 (PySCF's damping): f - (f0 + f0^T) factor / (factor + 1), f0 = (1 - s d) f d s."""
+    f0 = (torch.eye(s.shape[0], dtype=s.dtype, device=s.device) - s @ d) @ f @ d @ s
+    return f - (f0 + f0.T) * (factor / (factor + 1.0))
+
+
+def level_shift(s, d, f, factor):
+    """evaluate.py:1506-1545 (PySCF's level shift of the virtual space): f + (s - s d s) factor."""
+    return f + (s - s @ d @ s) * factor
+
+
+class Diis:
+    """evaluate.py:1212-1386, the CDIIS branch: a history growing to ``max_diis`` entries (the
+    oldest dropped beyond), error e_i = A F_i D_i S A^T - (...)^T, coefficients from the bordered
+    matrix [[0, 1], [1, <e_i|e_j>]] inverted through its eigendecomposition, F = A^T (sum x_i F_i) A."""
+
+    def __init__(self, overlap_matrix, A, max_diis: int = 8, diis_method: str = "CDIIS"):
+        if diis_method != "CDIIS":
+            raise NotImplementedError("only CDIIS is built: the reference's EDIIS/ADIIS minimise with "
+                                      "jax.scipy.optimize.minimize")
+        self.S, self.A, self.max_diis = overlap_matrix, A, int(max_diis)
+
+    def update(self, new_data, diis_data):
+        density, fock, energy = new_data
+        dv, fv, ev, errv = diis_data
+        fds = torch.einsum("ij,sjk,skl,lm,mn->sin", self.A, fock, density, self.S, self.A.T)
+        err = fds - fds.transpose(1, 2)
+        dv, fv = torch.cat((dv, density[None]), 0), torch.cat((fv, fock[None]), 0)
+        ev, errv = torch.cat((ev, energy.reshape(1).to(ev.dtype))), torch.cat((errv, err[None]), 0)
+        if errv.shape[0] > self.max_diis:
+            dv, fv, ev, errv = dv[1:], fv[1:], ev[1:], errv[1:]
+        return dv, fv, ev, errv
+
+    def cdiis_minimize(self, error_vector):
+        n = error_vector.shape[0]
+        inner = torch.einsum("iskl,jskl->sij", error_vector, error_vector)
+        B = torch.zeros((2, n + 1, n + 1), dtype=inner.dtype, device=inner.device)
+        B[:, 1:, 1:] = inner
+        B[:, 0, 1:] = 1.0
+        B[:, 1:, 0] = 1.0
+        xs = []
+        for s in range(2):
+            w, v = torch.linalg.eigh(B[s])
+            xs.append(v @ torch.diag(1.0 / w) @ v.T[:, 0])  # B^-1 (1, 0, ..., 0)
+        x = torch.stack(xs)
+        if bool(torch.isnan(x).any()):
+            raise AssertionError("DIIS coefficients are NaN")
+        return x[:, 1:]
+
+    def run(self, new_data, diis_data, cycle=0):
+        diis_data = self.update(new_data, diis_data)
+        fv, errv = diis_data[1], diis_data[3]
+        if errv.shape[0] == 1:
+            return fv[0], diis_data
+        x = self.cdiis_minimize(errv)
+        F = torch.einsum("si,isjk->sjk", x, fv)
+        return torch.einsum("ji,sjk,kl->sil", self.A, F, self.A), diis_data
+
+
+def scf_loop(functional, level_shift_factor=(0.0, 0.0), damp_factor=(0.0, 0.0), chunk_size: int = 1024,
+             cycles: int = 50, diis_start_cycle: int = 0, e_conv: float = 1e-5, g_conv: float = 1e-5,
+             diis_method: str = "CDIIS", smearing=None, smearing_sigma: float = 0.0, verbose: int = 0,
+             **kwargs) -> Callable:
+    """evaluate.py:355-592: the non-jitted SCF loop with CDIIS, damping and level shifting, until
+    |dE| in kcal/mol <= e_conv and |orbital gradient| <= g_conv or ``cycles``; on convergence one more
+    diagonalisation without level shift.  Every cycle checks the grid charge (AssertionError).
+    Not built: EDIIS/ADIIS (``jax.scipy.optimize.minimize`` in the reference), smearing (the reference's
+    smearing branch cannot run: it applies Python's min to a (2, n) array and stores a flattened
+    occupation vector), and chi regeneration for omegas (the reference reads an undefined ``mf``)."""
+    from .train import energy_predictor
+
+    if smearing:
+        raise NotImplementedError("smearing is not built (the reference's smearing branch cannot run as written)")
+    predict = energy_predictor(functional, **kwargs)
+    HARTREE2KCALMOL = 627.50947
+
+    def _diag_occ_rdm1(molecule, fock, nelecs):
+        mo_energy, mo_coeff = safe_fock_solver(fock, molecule.s1e)
+        mo_occ = get_occ(mo_energy, nelecs)
+        return molecule.replace(mo_coeff=mo_coeff, mo_energy=mo_energy, mo_occ=mo_occ,
+                                rdm1=make_rdm1(mo_coeff, mo_occ))
+
+    def scf_iterator(params, molecule, *args):
+        if getattr(molecule, "is_solid", False):
+            raise NotImplementedError("Solids with full BZ zampling not yet supported. Use simple_scf_loop or "
+                                      "diff_simple_scf_loop instead.")
+        if getattr(molecule, "omegas", None):
+            raise NotImplementedError("chi regeneration inside scf_loop is not built")
+        molecule = _to_device(molecule)
+        dev = molecule.device
+        nelectron = float(torch.as_tensor(molecule.atom_index).sum()) - float(molecule.charge)
+        nelecs = [int(round(float(molecule.mo_occ[s].sum()))) for s in range(2)]
+        old_e, norm_gorb, cycle = float("inf"), float("inf"), 0
+        predicted_e, fock = predict(params, molecule, *args)
+        n = molecule.s1e.shape[0]
+        A = torch.eye(n, dtype=F64, device=dev)
+        diis = Diis(molecule.s1e, A, max_diis=10, diis_method=diis_method)
+        z = torch.zeros((0, 2, n, n), dtype=F64, device=dev)
+        diis_data = (z, z, torch.zeros(0, dtype=F64, device=dev), z)
+        while ((abs(float(predicted_e) - old_e) * HARTREE2KCALMOL > e_conv or norm_gorb > g_conv)
+               and cycle < cycles):
+            old_e = float(predicted_e)
+            if 0 <= cycle < diis_start_cycle - 1 and abs(damp_factor[0]) + abs(damp_factor[1]) > 1e-4:
+                fock = torch.stack([damping(molecule.s1e, molecule.rdm1[s], fock[s], damp_factor[s]) for s in range(2)])
+            if cycle >= diis_start_cycle:
+                fock, diis_data = diis.run((molecule.rdm1, fock, predicted_e), diis_data, cycle)
+            if abs(level_shift_factor[0]) + abs(level_shift_factor[1]) > 1e-4:
+                fock = torch.stack([level_shift(molecule.s1e, molecule.rdm1[s], fock[s], level_shift_factor[s])
+                                    for s in range(2)])
+            molecule = _diag_occ_rdm1(molecule, fock, nelecs)
+            w = engine.as_device_f64(molecule.grid.weights, dev)
+            computed_charge = float(torch.einsum("r,rs->", w, molecule.density()))
+            assert abs(nelectron - computed_charge) <= 1e-3 + 1e-5 * abs(computed_charge), \
+                "Total charge is not conserved"
+            predicted_e, fock = predict(params, molecule, *args)
+            norm_gorb = float(torch.linalg.norm(mo_grads(molecule.mo_coeff, molecule.mo_occ, fock)))
+            if verbose > 1:
+                print(f"cycle: {cycle}, energy: {float(predicted_e):.7e}, "
+                      f"energy difference: {abs(float(predicted_e) - old_e):.4e}, norm_gradient_orbitals: {norm_gorb:.2e}")
+            cycle += 1
+        if abs(float(predicted_e) - old_e) * HARTREE2KCALMOL < e_conv and norm_gorb < g_conv:
+            molecule = _diag_occ_rdm1(molecule, fock, nelecs)  # once more, without the level shift
+            predicted_e, fock = predict(params, molecule, *args)
+        return molecule.replace(fock=fock, energy=predicted_e)
+
+    return scf_iterator

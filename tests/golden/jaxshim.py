@@ -137,6 +137,10 @@ def _mk_jnp():
     m.less = lambda a, b: torch.less(_t(a), _t(b))
     m.logical_and = lambda a, b: torch.logical_and(_t(a), _t(b))
 
+    m.eye = lambda n, dtype=None: torch.eye(int(n), dtype=F64)
+    if not hasattr(m, "dot"):
+        m.dot = lambda a, b: torch.matmul(_t(a), _t(b))
+    m.any = lambda x, axis=None: torch.any(_t(x)) if axis is None else torch.any(_t(x), dim=axis)
     m.isclose = lambda a, b, rtol=1e-05, atol=1e-08, equal_nan=False: torch.isclose(
         _t(a).to(F64), _t(b).to(F64), rtol=rtol, atol=atol, equal_nan=equal_nan)
 
@@ -638,8 +642,11 @@ def load_scf(root: str, ref):
     iface = types.ModuleType("grad_dft.interface")
     iface.__path__ = []
     pys = types.ModuleType("grad_dft.interface.pyscf")
-    for n in ("generate_chi_tensor", "mol_from_Molecule", "process_mol"):
-        setattr(pys, n, None)
+    pys.generate_chi_tensor = None
+    # scf_loop builds PySCF objects up front only to regenerate chi when the molecule has omegas
+    # (evaluate.py:404-408, 509-521); without omegas placeholders do
+    pys.mol_from_Molecule = lambda molecule, *a, **k: None
+    pys.process_mol = lambda *a, **k: (None, None)
     sys.modules["grad_dft.interface"], sys.modules["grad_dft.interface.pyscf"] = iface, pys
     eig = run("grad_dft.utils.eigenproblem", "utils/eigenproblem.py")
     utils = sys.modules["grad_dft.utils"]

@@ -1,5 +1,5 @@
-"""Golden fixture of simple_scf_loop, non_scf_predictor and the orbital optimisers, made by running
-the reference's own code.
+"""Golden fixture of simple_scf_loop, non_scf_predictor, scf_loop and the orbital optimisers, made by
+running the reference's own code.
 
 Usage (needs the reference checkout; this is not run by the tests):
 
@@ -38,6 +38,8 @@ _orig_transpose = torch.Tensor.transpose
 def _transpose(self, *dims):
     if len(dims) == 1 and isinstance(dims[0], (tuple, list)):
         return self.permute(*dims[0])
+    if len(dims) > 2:  # transpose(*axes), as the Diis error matrix is built (evaluate.py:1300)
+        return self.permute(*dims)
     return _orig_transpose(self, *dims)
 
 
@@ -120,6 +122,17 @@ def main(root):
         nsp = ev.non_scf_predictor(fn)({"params": {}}, mol)
         out[f"nonscf_energy_{name}"] = np.asarray(nsp.energy.detach())
         out[f"nonscf_fock_{name}"] = nsp.fock.detach().numpy()
+    # scf_loop (evaluate.py:355-592, CDIIS): all cycles, with damping + level shift, and to convergence
+    runs = {"plain": dict(cycles=6, e_conv=1e-14, g_conv=1e-14),
+            "shifted": dict(cycles=6, e_conv=1e-14, g_conv=1e-14, level_shift_factor=(0.1, 0.1),
+                            damp_factor=(0.3, 0.3), diis_start_cycle=3),
+            "converged": dict(cycles=60)}
+    for key, kw in runs.items():
+        final = ev.scf_loop(ref.popular.B88, **kw)({"params": {}}, mol)
+        out[f"scf_{key}_energy"] = np.asarray(final.energy.detach())
+        out[f"scf_{key}_rdm1"] = final.rdm1.detach().numpy()
+        out[f"scf_{key}_fock"] = final.fock.detach().numpy()
+
     # orbital optimisers (evaluate.py:595-915) with optax.adam(1e-2), 3 steps, B88, on the same system in
     # a non-orthonormal basis (AOs times an SPD matrix M with spread eigenvalues): PCA whitening needs
     # distinct overlap eigenvalues, and the orthonormalised system's overlap is the identity

@@ -304,3 +304,25 @@ def test_orbital_optimizers_vs_reference(G, golden, precision, rtol):
     m = G.jitted_mol_orb_optimizer(G.B88, G.optim.adam(1e-2), cycles=3)({"params": {}}, mol)
     ref = float(g["orb_energy_jitted"])
     assert abs(float(m.energy) - ref) <= rtol * abs(ref)
+
+
+@pytest.mark.parametrize("precision,rtol_e,rtol_m", [("fp64", 1e-10, 1e-7), ("tf32x3", 1e-6, 2e-5)])
+def test_scf_loop_vs_reference(G, golden, precision, rtol_e, rtol_m):
+    """scf_loop (evaluate.py:355-592) with CDIIS: all cycles, with damping and level shift, and to
+    convergence (with the final extra diagonalisation), against the reference's own loop."""
+    g = golden("simple_scf")
+    mol = _simple_scf_molecule(G, g, precision)
+    runs = {"plain": dict(cycles=6, e_conv=1e-14, g_conv=1e-14),
+            "shifted": dict(cycles=6, e_conv=1e-14, g_conv=1e-14, level_shift_factor=(0.1, 0.1),
+                            damp_factor=(0.3, 0.3), diis_start_cycle=3),
+            "converged": dict(cycles=60)}
+    for key, kw in runs.items():
+        final = G.scf_loop(G.B88, **kw)({"params": {}}, mol)
+        ref_e = float(g[f"scf_{key}_energy"])
+        assert abs(float(final.energy) - ref_e) <= rtol_e * abs(ref_e), (key, float(final.energy), ref_e)
+        for part in ("rdm1", "fock"):
+            ref = g[f"scf_{key}_{part}"]
+            err = float(np.max(np.abs(getattr(final, part).detach().cpu().numpy() - ref)))
+            assert err <= rtol_m * float(np.max(np.abs(ref))), (key, part, err)
+    with pytest.raises(NotImplementedError):
+        G.scf_loop(G.B88, diis_method="EDIIS")({"params": {}}, mol)
