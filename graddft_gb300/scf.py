@@ -127,15 +127,6 @@ def energy_and_fock(functional, params, atoms, clip_cte: float = CLIP):
     return energy, _abs_clip(fock, clip_cte)
 
 
-def orbital_grad(mo_coeff, mo_occ, fock):
-    """molecule.py:344-383: 2 C_vir^T F C_occ per spin, concatenated."""
-    out = []
-    for s in range(2):
-        occ = mo_occ[s] > 0
-        out.append((2.0 * mo_coeff[s][:, ~occ].T @ fock[s] @ mo_coeff[s][:, occ]).reshape(-1))
-    return torch.cat(out)
-
-
 def _to_device(atoms):
     dev = atoms.resident().device
     t = lambda x: x if isinstance(x, torch.Tensor) and x.device == dev else torch.as_tensor(x, dtype=F64, device=dev)  # noqa: E731
