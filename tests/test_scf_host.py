@@ -1,5 +1,7 @@
 """Host-side pieces of the SCF loop (no GPU): the safe eigensolver's reverse
 rule, occupations and the density matrix, against plain torch on the CPU."""
+import numpy as np
+import pytest
 import torch
 
 from graddft_gb300 import scf
@@ -45,3 +47,75 @@ def test_general_eigh_and_occupations():
     assert occ[1, -2:].sum() == 2 and occ[1, :-2].sum() == 0
     d = scf.make_rdm1(torch.stack([c, c]), occ)
     assert torch.allclose(torch.einsum("ij,ji->", d[0], s), torch.tensor(3.0, dtype=torch.float64))
+
+
+def test_adam_matches_its_definition():
+    """graddft_gb300.optim.adam: optax's Adam (bias-corrected moments, eps outside the square root)."""
+    from graddft_gb300 import optim
+
+    tx = optim.adam(0.05)
+    w = torch.tensor([1.0, -2.0, 0.5], dtype=torch.float64)
+    st = tx.init(w)
+    m = v = torch.zeros(3, dtype=torch.float64)
+    for k in range(1, 5):
+        g = torch.tensor([0.3 * k, -0.1, 2.0 / k], dtype=torch.float64)
+        u, st = tx.update(g, st, w)
+        m = 0.9 * m + (1 - 0.9) * g
+        v = 0.999 * v + (1 - 0.999) * g * g
+        ref = -0.05 * (m / (1 - 0.9 ** k)) / (torch.sqrt(v / (1 - 0.999 ** k)) + 1e-8)
+        assert torch.allclose(u, ref, rtol=1e-14, atol=0)
+        w = optim.apply_updates(w, u)
+    u, _ = optim.sgd(0.1).update(torch.ones(3, dtype=torch.float64), None)
+    assert torch.equal(u, -0.1 * torch.ones(3, dtype=torch.float64))
+
+
+def test_damping_level_shift_and_cdiis():
+    """evaluate.py:1477-1545 (PySCF's damping and level shift) and the CDIIS coefficients
+    (evaluate.py:1365-1385): B^-1 (1, 0, ...) by eigendecomposition equals a direct solve."""
+    from graddft_gb300 import scf
+
+    g = np.random.default_rng(3)
+    n = 5
+    a = g.standard_normal((n, n))
+    s = torch.as_tensor(np.eye(n) + 0.1 * (a @ a.T) / n)
+    d = torch.as_tensor(0.2 * np.eye(n))
+    f = torch.as_tensor(g.standard_normal((n, n)))
+    f = 0.5 * (f + f.T)
+    f0 = (torch.eye(n, dtype=torch.float64) - s @ d) @ f @ d @ s
+    assert torch.allclose(scf.damping(s, d, f, 0.25), f - (f0 + f0.T) * 0.2, rtol=1e-14, atol=1e-14)
+    assert torch.allclose(scf.level_shift(s, d, f, 0.3), f + (s - s @ d @ s) * 0.3, rtol=1e-14, atol=1e-14)
+    diis = scf.Diis(s, torch.eye(n, dtype=torch.float64), max_diis=3)
+    errs = torch.as_tensor(g.standard_normal((3, 2, n, n)))
+    x = diis.cdiis_minimize(errs)
+    for sp in range(2):
+        inner = torch.einsum("ikl,jkl->ij", errs[:, sp], errs[:, sp])
+        B = torch.zeros((4, 4), dtype=torch.float64)
+        B[1:, 1:] = inner
+        B[0, 1:] = B[1:, 0] = 1.0
+        rhs = torch.zeros(4, dtype=torch.float64)
+        rhs[0] = 1.0
+        assert torch.allclose(x[sp], torch.linalg.solve(B, rhs)[1:], rtol=1e-10, atol=1e-12)
+        assert abs(float(x[sp].sum()) - 1.0) < 1e-12  # the constraint row
+    with pytest.raises(NotImplementedError):
+        scf.Diis(s, torch.eye(n, dtype=torch.float64), diis_method="EDIIS")
+
+
+def test_canonical_eigvec_signs_and_mo_grads():
+    from graddft_gb300 import scf
+
+    g = np.random.default_rng(4)
+    a = torch.as_tensor(g.standard_normal((6, 6)))
+    w, v = torch.linalg.eigh(a @ a.T)
+    c = scf.canonical_eigvec_signs(v)
+    assert torch.allclose(c.abs(), v.abs())
+    assert bool((torch.gather(c, 0, c.abs().argmax(0, keepdim=True)) > 0).all())
+    assert torch.allclose(scf.canonical_eigvec_signs(-v), c)
+    # mo_grads: C_vir^T F C_occ summed over spin, zeros outside the (vir, occ) block
+    C = torch.as_tensor(g.standard_normal((2, 6, 6)))
+    F = torch.as_tensor(g.standard_normal((2, 6, 6)))
+    occ = torch.zeros((2, 6), dtype=torch.float64)
+    occ[:, :2] = 1.0
+    G = scf.mo_grads(C, occ, F)
+    ref = sum(C[s][:, 2:].T @ F[s] @ C[s][:, :2] for s in range(2))
+    assert torch.allclose(G[2:, :2], ref, rtol=1e-13, atol=1e-13)
+    assert float(G[:2].abs().max()) == 0.0 and float(G[:, 2:].abs().max()) == 0.0
