@@ -541,7 +541,7 @@ def run_hf(args):
     form = args.form or "fp64"
     r = G.engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "fp64", dev)
     ao = r.ao_planes()[0, :n_grid, :n_ao].contiguous()  # phi as evaluated on the device
-    if form == "tf32x3":  # contractions and network in the mixed form; exact exchange stays FP64
+    if form == "tf32x3":  # density, V_xc, exchange contractions and network in the mixed form
         r = G.engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "tf32x3", dev)
     chi = synthetic.make_chi(ao.cpu().numpy(), wl.rdm1, n_omega=2, seed=SEED)
     rng = np.random.default_rng(SEED)
@@ -574,6 +574,8 @@ def run_hf(args):
         "config": {"workload": f"DM21 energy_predictor with chi: n_ao {n_ao}, n_grid {n_grid}, omegas (0, 0.4)",
                    "n_ao": n_ao, "n_grid": n_grid,
                    "network": "DM21 6 x 256, " + ("FP64 form" if form == "fp64" else "TF32x3 tensor-core form"),
+                   "exchange": ("FP64 GEMMs" if form == "fp64" else
+                                "block-scaled three-slice tcgen05 GEMMs (ao.[D0|D1], ao^T [B0|B1])"),
                    "form": form,
                    "l2": "inputs larger than L2 (chi %.2f GiB)" % (chi.nbytes / 2**30)},
         "clocks": clk.summary(),

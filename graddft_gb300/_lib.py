@@ -41,7 +41,8 @@ EXPORTS = (
     "gdft_network_apply", "gdft_neural_hvp_workspace_bytes", "gdft_neural_xc_hvp", "gdft_tc_gemm_probe",
     "gdft_tc_gemm3_probe", "gdft_neural_batch_workspace_bytes", "gdft_neural_batch_xc",
     "gdft_xc_energy_grads_hf", "gdft_hf_workspace_bytes", "gdft_hf_energy_density", "gdft_hf_fock",
-    "gdft_fock_add_hf", "gdft_neural_xc_hf_grads",
+    "gdft_fock_add_hf", "gdft_neural_xc_hf_grads", "gdft_hf_workspace_bytes_form", "gdft_hf_energy_density_form",
+    "gdft_hf_fock_form", "gdft_hf_device_status",
 )
 STAGE_AO, STAGE_DENSITY, STAGE_POINT, STAGE_VXC, STAGE_REDUCE, STAGE_MLP = range(6)
 
@@ -136,6 +137,10 @@ _SIGS = {
     "gdft_hf_energy_density": ([P, P, P, I64, I32, I32, P, P, SZ, P], ctypes.c_int),
     "gdft_hf_fock": ([P, P, P, I64, I32, I32, P, P, SZ, P], ctypes.c_int),
     "gdft_fock_add_hf": ([P, P, I32, D, P], ctypes.c_int),
+    "gdft_hf_workspace_bytes_form": ([I64, I32, I32, I32, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_hf_energy_density_form": ([P, P, P, I64, I32, I32, I32, P, P, SZ, P], ctypes.c_int),
+    "gdft_hf_fock_form": ([P, P, P, I64, I32, I32, I32, P, P, SZ, P], ctypes.c_int),
+    "gdft_hf_device_status": ([P, SZ, ctypes.POINTER(I32), P], ctypes.c_int),
     "gdft_neural_xc_hf_grads": ([PMOL, P, PNET, P, P, P, P, P, P, P, SZ, P], ctypes.c_int),
     "gdft_energy_densities": ([PMOL, P, PFN, P, I32, P, P, SZ, P], ctypes.c_int),
     "gdft_vxc_from_potentials": ([PMOL, P, P, P, SZ, P], ctypes.c_int),

@@ -382,10 +382,23 @@ def fock(h1e, vj, vxc, clip=1e-30) -> torch.Tensor:
     return out
 
 
-def _hf_ws(n_grid: int, n_ao: int, n_omega: int, device) -> torch.Tensor:
+def _hf_form(form) -> int:
+    if form not in PRECISIONS:
+        raise ValueError(f"unknown form {form!r}; expected one of {sorted(PRECISIONS)}")
+    return PRECISIONS[form]
+
+
+def _hf_ws(n_grid: int, n_ao: int, n_omega: int, form: int, device) -> torch.Tensor:
     nbytes = ctypes.c_size_t()
-    check(_lib.load().gdft_hf_workspace_bytes(n_grid, n_ao, n_omega, ctypes.byref(nbytes)))
+    check(_lib.load().gdft_hf_workspace_bytes_form(n_grid, n_ao, n_omega, form, ctypes.byref(nbytes)))
     return torch.empty(nbytes.value, dtype=torch.uint8, device=device)
+
+
+def _hf_status(ws: torch.Tensor, form: int) -> None:
+    """The bounded-wait error word of a mixed-form exchange call (synchronises the stream)."""
+    if form == _lib.GDFT_TF32X3:
+        status = ctypes.c_int32()
+        check(_lib.load().gdft_hf_device_status(_ptr(ws), ws.numel(), ctypes.byref(status), _stream(ws.device)))
 
 
 def _chi(chi, ao):
@@ -396,24 +409,30 @@ def _chi(chi, ao):
     return chi.contiguous()
 
 
-def hf_energy_density(ao, rdm1, chi) -> torch.Tensor:
-    """molecule.py:507-541: ehf (omega, 2, grid) = -1/2 einsum("rwsc,sac,ra->wsr", chi, rdm1, ao)."""
+def hf_energy_density(ao, rdm1, chi, form: str = "fp64") -> torch.Tensor:
+    """molecule.py:507-541: ehf (omega, 2, grid) = -1/2 einsum("rwsc,sac,ra->wsr", chi, rdm1, ao).
+
+    ``form`` "fp64" contracts on the FP64 GEMM, "tf32x3" on the block-scaled three-slice tensor-core GEMM.
+    """
     dev = require_cuda(ao.device if isinstance(ao, torch.Tensor) and ao.is_cuda else None)
+    code = _hf_form(form)
     ao = as_device_f64(ao, dev).contiguous()
     rdm1 = as_device_f64(rdm1, dev).contiguous()
     chi = _chi(chi, ao)
     n_grid, n_ao = ao.shape
     n_omega = chi.shape[1]
     out = torch.empty((n_omega, 2, n_grid), dtype=F64, device=dev)
-    ws = _hf_ws(n_grid, n_ao, n_omega, dev)
-    check(_lib.load().gdft_hf_energy_density(_ptr(ao), _ptr(rdm1), _ptr(chi), n_grid, n_ao, n_omega, _ptr(out),
-                                             _ptr(ws), ws.numel(), _stream(dev)))
+    ws = _hf_ws(n_grid, n_ao, n_omega, code, dev)
+    check(_lib.load().gdft_hf_energy_density_form(_ptr(ao), _ptr(rdm1), _ptr(chi), n_grid, n_ao, n_omega, code,
+                                                  _ptr(out), _ptr(ws), ws.numel(), _stream(dev)))
+    _hf_status(ws, code)
     return out
 
 
-def hf_fock(ao, chi, g) -> torch.Tensor:
+def hf_fock(ao, chi, g, form: str = "fp64") -> torch.Tensor:
     """sum over omega of molecule.py:545-685: F_s = -1/2 sum_w einsum("rw s b, w s r, r a -> s a b")."""
     dev = require_cuda(ao.device if isinstance(ao, torch.Tensor) and ao.is_cuda else None)
+    code = _hf_form(form)
     ao = as_device_f64(ao, dev).contiguous()
     chi = _chi(chi, ao)
     n_grid, n_ao = ao.shape
@@ -423,9 +442,10 @@ def hf_fock(ao, chi, g) -> torch.Tensor:
         raise ValueError(f"g must be (omega, 2, grid) = ({n_omega}, 2, {n_grid}), got {tuple(g.shape)}")
     g = g.contiguous()
     out = torch.empty((2, n_ao, n_ao), dtype=F64, device=dev)
-    ws = _hf_ws(n_grid, n_ao, n_omega, dev)
-    check(_lib.load().gdft_hf_fock(_ptr(ao), _ptr(chi), _ptr(g), n_grid, n_ao, n_omega, _ptr(out), _ptr(ws),
-                                   ws.numel(), _stream(dev)))
+    ws = _hf_ws(n_grid, n_ao, n_omega, code, dev)
+    check(_lib.load().gdft_hf_fock_form(_ptr(ao), _ptr(chi), _ptr(g), n_grid, n_ao, n_omega, code, _ptr(out),
+                                        _ptr(ws), ws.numel(), _stream(dev)))
+    _hf_status(ws, code)
     return out
 
 

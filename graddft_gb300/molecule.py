@@ -177,7 +177,7 @@ class Molecule:
         """
         if self.chi is not None:
             return engine.hf_energy_density(engine.as_device_f64(self.ao, self.device), self._rdm1(),
-                                            self.select_HF_omegas(omegas))
+                                            self.select_HF_omegas(omegas), form=self.precision)
         if self.ehf is not None:
             return engine.as_device_f64(self.ehf, self.device)[: len(omegas)]
         raise ValueError("Precomputed chi tensor has not been loaded.")
@@ -197,7 +197,8 @@ class Molecule:
 
     def _hf_fock_per_omega(self, chi, g):
         ao = engine.as_device_f64(self.ao, self.device)
-        return torch.stack([engine.hf_fock(ao, chi[:, w:w + 1], g[w:w + 1]) for w in range(chi.shape[1])])
+        return torch.stack([engine.hf_fock(ao, chi[:, w:w + 1], g[w:w + 1], form=self.precision)
+                            for w in range(chi.shape[1])])
 
     def HF_coefficient_input_grad_2_Fock(self, functional, params, omegas, ehf, cinputs_wout_hf, densities,
                                          **kwargs):

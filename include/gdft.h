@@ -268,6 +268,23 @@ int gdft_hf_energy_density(const double *d_ao, const double *d_rdm1, const doubl
 int gdft_hf_fock(const double *d_ao, const double *d_chi, const double *d_g, int64_t n_grid, int32_t n_ao,
                  int32_t n_omega, double *d_fock_hf, void *d_ws, size_t ws_bytes, void *stream);
 int gdft_fock_add_hf(double *d_fock, const double *d_fock_hf, int32_t n_ao, double clip, void *stream);
+/* The same two contractions in either arithmetic form (the three entries above
+ * are the GDFT_FP64 form).  GDFT_TF32X3 runs both on the block-scaled
+ * three-slice tcgen05 GEMM (FP64 inputs and outputs; the products are exact
+ * in their high slices and compensated in the rest, about 1e-9 relative to
+ * the largest term); it needs n_grid <= 2^30, a 256-byte aligned workspace of
+ * gdft_hf_workspace_bytes_form bytes, and gdft_hf_device_status on that
+ * workspace after the call to learn whether a bounded device wait expired. */
+int gdft_hf_workspace_bytes_form(int64_t n_grid, int32_t n_ao, int32_t n_omega, int32_t form, size_t *bytes);
+int gdft_hf_energy_density_form(const double *d_ao, const double *d_rdm1, const double *d_chi, int64_t n_grid,
+                                int32_t n_ao, int32_t n_omega, int32_t form, double *d_ehf, void *d_ws,
+                                size_t ws_bytes, void *stream);
+int gdft_hf_fock_form(const double *d_ao, const double *d_chi, const double *d_g, int64_t n_grid, int32_t n_ao,
+                      int32_t n_omega, int32_t form, double *d_fock_hf, void *d_ws, size_t ws_bytes, void *stream);
+/* Reads (synchronising the stream) the device error word of a workspace last
+ * used by a GDFT_TF32X3 exact-exchange call: GDFT_ERR_DEVICE with *status the
+ * code when a bounded wait expired. */
+int gdft_hf_device_status(void *d_ws, size_t ws_bytes, int32_t *status, void *stream);
 
 /* The DM21-style coefficient network of a NeuralFunctional (DM21.default_nn,
  * functional.py:797-822, with NeuralFunctional.head :407-419):

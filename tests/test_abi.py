@@ -114,3 +114,29 @@ def test_host_only_argument_checks_new_entries(built_lib):
     basis = _lib.GdftBasis()  # empty tables
     assert lib.gdft_eval_ao(ctypes.byref(basis), None, 10, 1, None, None, None, None) == _lib.GDFT_ERR_INVALID
     assert b"basis" in lib.gdft_last_error()
+
+
+def test_host_only_checks_exchange_forms(built_lib):
+    """The form-taking exchange entries: workspace sizes per form, unknown forms, missing pointers."""
+    from graddft_gb300 import _lib
+
+    lib = _lib.load(built_lib)
+    fp64, mixed = ctypes.c_size_t(), ctypes.c_size_t()
+    assert lib.gdft_hf_workspace_bytes_form(4099, 37, 2, _lib.GDFT_FP64, ctypes.byref(fp64)) == _lib.GDFT_OK
+    legacy = ctypes.c_size_t()
+    assert lib.gdft_hf_workspace_bytes(4099, 37, 2, ctypes.byref(legacy)) == _lib.GDFT_OK
+    assert legacy.value == fp64.value
+    assert lib.gdft_hf_workspace_bytes_form(4099, 37, 2, _lib.GDFT_TF32X3, ctypes.byref(mixed)) == _lib.GDFT_OK
+    # error word + the larger of (ao sets, D sets, X) and (ao^T sets, B sets, split partials)
+    set3, a256 = 3 * 128 * 32 * 4, (lambda x: (x + 255) // 256 * 256)
+    energy = a256(33 * 2 * set3) + a256(1 * 2 * set3) + a256(4099 * 74 * 8)
+    rch = (4099 + 31) // 32
+    fock = a256(rch * set3) + a256(rch * set3) + a256(rch * 37 * 74 * 8)  # one split per K chunk here
+    assert mixed.value == 256 + max(energy, fock)
+    assert lib.gdft_hf_workspace_bytes_form(4099, 37, 2, 7, ctypes.byref(mixed)) == _lib.GDFT_ERR_INVALID
+    assert lib.gdft_hf_energy_density_form(None, None, None, 10, 4, 1, _lib.GDFT_TF32X3, None, None, 0,
+                                           None) == _lib.GDFT_ERR_INVALID
+    assert lib.gdft_hf_fock_form(None, None, None, 10, 4, 1, 9, None, None, 0, None) == _lib.GDFT_ERR_INVALID
+    assert b"form" in lib.gdft_last_error()
+    status = ctypes.c_int32()
+    assert lib.gdft_hf_device_status(None, 0, ctypes.byref(status), None) == _lib.GDFT_ERR_INVALID

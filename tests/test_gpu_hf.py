@@ -6,7 +6,8 @@ b3lyp_hfgrads) and of DM21 (dm21_hfgrads_densities / dm21_hfgrads_cinputs,
 functional.py:677-757), and energy_predictor with those terms
 (train.py:124-218) against fixtures made by running the reference's own source
 (tests/golden/make_golden.py), and the general-omega Fock contraction against
-the oracle.  All FP64: the bar is 1e-11 relative to the largest entry.
+the oracle.  FP64 form: the bar is 1e-11 relative to the largest entry; the
+mixed form's exchange contractions (three-slice tensor-core GEMM): 2e-8.
 """
 import numpy as np
 import pytest
@@ -72,7 +73,7 @@ def test_b3lyp_predict_with_chi(G, golden, precision):
     g = golden("hf")
     mol = _molecule(G, g, precision)
     E, F = G.energy_predictor(G.B3LYP)({"params": {}}, mol)
-    # The mixed form's E_xc and V_xc carry its ~1e-7 relative error; the HF terms are FP64 in both.
+    # The mixed form's E_xc and V_xc carry its ~1e-7 relative error; its exchange terms about 1e-9.
     rtol = RTOL if precision == "fp64" else 2e-6
     assert abs(float(E) - float(g["predict_E_B3LYP"])) <= rtol * abs(float(g["predict_E_B3LYP"]))
     _close(F, g["predict_F_B3LYP"], rtol=rtol, what="F")
@@ -93,6 +94,40 @@ def test_hf_fock_general_omegas_vs_oracle(G):
     _close(e, O.hf_energy_density(wl.rdm1, ao, chi).numpy(), what="ehf")
 
 
+MIXED_RTOL = 2e-8  # three-slice operands: about 2^-31 of each row's largest entry per element
+
+
+@pytest.mark.parametrize("n_grid,n_ao,n_omega", [(4099, 37, 2), (1000, 130, 3), (31, 5, 1)])
+def test_hf_mixed_form_vs_oracle(G, n_grid, n_ao, n_omega):
+    """The tensor-core (TF32x3) exact-exchange contractions on ragged sizes: partial point tiles and
+    K chunks, both spins in one GEMM with a spin boundary inside a column tile (n_ao = 130), a single
+    partial tile (31 points x 5 orbitals); numpy emulation of the six-product form: 4e-10 (F), 1e-9 (ehf)."""
+    wl = synthetic.make_workload(n_grid, n_ao, max(1, min(5, n_ao // 2)), seed=21, box_angstrom=7.0,
+                                 centre_box_angstrom=4.0)
+    ao, _, _ = O.eval_ao_planes(wl.basis, wl.coords)
+    chi = synthetic.make_chi(ao, wl.rdm1, n_omega=n_omega, seed=22)
+    rng = np.random.default_rng(23)
+    gw = rng.standard_normal((n_omega, 2, n_grid)) * 1e-3
+    ref_f = -0.5 * np.einsum("rwsb,wsr,ra->sab", chi, gw, ao)
+    ref_e = O.hf_energy_density(wl.rdm1, ao, chi).numpy()
+    got_f = G.engine.hf_fock(_t(ao), _t(chi), _t(gw), form="tf32x3")
+    _close(got_f, ref_f, rtol=MIXED_RTOL, what="hf_fock (mixed)")
+    got_e = G.engine.hf_energy_density(_t(ao), _t(wl.rdm1), _t(chi), form="tf32x3")
+    _close(got_e, ref_e, rtol=MIXED_RTOL, what="ehf (mixed)")
+    # the FP64 form of the same call stays at FP64 rounding
+    _close(G.engine.hf_fock(_t(ao), _t(chi), _t(gw), form="fp64"), ref_f, what="hf_fock (fp64)")
+
+
+def test_hf_mixed_form_golden(G, golden):
+    """ehf and the B3LYP HF Fock term in the mixed form against the reference's own outputs."""
+    g = golden("hf")
+    mol = _molecule(G, g, precision="tf32x3")
+    _close(mol.HF_energy_density([0.0, 0.4]), g["ehf"], rtol=MIXED_RTOL, what="ehf (mixed)")
+    ehf0 = mol.HF_energy_density([0.0])
+    v = G.popular_functionals.b3lyp_hfgrads(G.B3LYP, {"params": {}}, mol, ehf0, None, None)
+    _close(v, g["b3lyp_hfgrads"], rtol=1e-6, what="b3lyp_hfgrads (mixed densities and exchange)")
+
+
 def test_hf_errors(G, golden):
     g = golden("hf")
     mol = _molecule(G, g)
@@ -103,6 +138,8 @@ def test_hf_errors(G, golden):
     no_chi = mol.replace(chi=None)
     with pytest.raises(ValueError):
         no_chi.HF_energy_density([0.0])
+    with pytest.raises(ValueError):
+        G.engine.hf_energy_density(_t(g["ao"]), _t(g["rdm1"]), _t(g["chi"]), form="bf16")
 
 
 def test_dm21_hf_terms(G, golden):
@@ -126,11 +163,13 @@ def test_dm21_predict_with_chi(G, golden):
     _close(F, g["predict_F_DM21"], what="F")
 
 
-def test_dm21_hf_terms_and_predict_mixed_network(G, golden):
+@pytest.mark.parametrize("mol_form", ["fp64", "tf32x3"])
+def test_dm21_hf_terms_and_predict_mixed_network(G, golden, mol_form):
     """The same with the tensor-core (TF32x3) network: E to 1e-6 relative, the HF terms and F to 2e-5 of
-    their largest entries (the network's FP32 activations; the exchange contractions stay FP64)."""
+    their largest entries (the network's FP32 activations), with the molecule's densities, V_xc and
+    exchange contractions in either form."""
     g = golden("hf")
-    mol = _molecule(G, g)
+    mol = _molecule(G, g, mol_form)
     params = synthetic.glorot_params(seed=int(g["theta_seed"]))
     dm21 = G.DM21(precision="tf32x3")
     ehf = mol.HF_energy_density([0.0, 0.4])
