@@ -168,6 +168,8 @@ class Molecule:
                 raise ValueError(f"The molecule.chi tensor does not contain omega value {o}, only {self.omegas}")
         idx = [have.index(float(o)) for o in omegas]
         chi = engine.as_device_f64(self.chi, self.device)
+        if idx == list(range(chi.shape[1])) and chi.is_contiguous():
+            return chi  # every omega in stored order: no gather (callers only read chi)
         return chi[:, idx].contiguous()
 
     def HF_energy_density(self, omegas, *args, **kwargs):
