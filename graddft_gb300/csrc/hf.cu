@@ -96,7 +96,7 @@ struct FetchDensity {  // row j = s n + c, K = a: D_s[a][c]
     return d[(s * n + a) * n + c];
   }
 };
-struct FetchHfB {  // row j = s n + b, K = r: B_s[r][b] = -1/2 sum_w g[w][s][r] chi[r][w][s][b]
+struct FetchHfB {  // row j = s n + b, K = r: sum_w g[w][s][r] chi[r][w][s][b] (the packer scales by -1/2)
   const double *chi, *g;
   int64_t n_grid, n;
   int n_omega;
@@ -105,16 +105,53 @@ struct FetchHfB {  // row j = s n + b, K = r: B_s[r][b] = -1/2 sum_w g[w][s][r] 
     double acc = 0.0;
     for (int w = 0; w < n_omega; ++w)
       acc = fma(g[((size_t)w * 2 + s) * n_grid + r], chi[(((size_t)r * n_omega + w) * 2 + s) * n + b], acc);
-    return -0.5 * acc;
+    return acc;
   }
 };
 
+// One row (32 K values) of a three-slice block set [hi | lo | lo2] from FP64
+// values times a power of two, with one FP64 subtraction and three conversions
+// per value (the FP64 pipe bounds these packers): xf = x rounded to FP32 and
+// xl = (x - xf) rounded, so xf + xl = x to 2^-47 |x|; hi = xf on the row's
+// quantum (as umma::quant takes it from the row maximum), r = xf - hi and
+// e = r - tf32(r) exact in FP32, lo = tf32(r), lo2 = tf32(e + xl).  The
+// representation error stays within about 2^-31 of the row maximum, the bound
+// of umma::store_row3.
+__device__ __forceinline__ void store_row3_scaled(float *blk3, int row, const double (&v)[32], float scale) {
+  float xf[32], xl[32];
+  float m = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    const float f = (float)v[k];
+    xl[k] = (float)(v[k] - (double)f) * scale;
+    xf[k] = f * scale;
+    m = fmaxf(m, fabsf(xf[k]));
+  }
+  const umma::Quant u = umma::quant(m);
+#pragma unroll
+  for (int k4 = 0; k4 < 8; ++k4) {
+    float h[4], l[4], l2[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float x = xf[4 * k4 + i];
+      h[i] = rintf(x * u.inv) * u.q;
+      const float r = x - h[i];
+      l[i] = umma::tf32_rn(r);
+      l2[i] = umma::tf32_rn((r - l[i]) + xl[4 * k4 + i]);
+    }
+    const uint32_t off = umma::kblock_off(row, 4 * k4) / 4;
+    *(float4 *)(blk3 + off) = make_float4(h[0], h[1], h[2], h[3]);
+    *(float4 *)(blk3 + umma::kBlockBytes / 4 + off) = make_float4(l[0], l[1], l[2], l[3]);
+    *(float4 *)(blk3 + umma::kBlockBytes / 2 + off) = make_float4(l2[0], l2[1], l2[2], l2[3]);
+  }
+}
+
 // Block (tile, kc) of a three-slice operand: rows tile*128 + m, K indices
-// kc*32 + k, zero outside rows x kdim, written as umma::store_row3 lays it out
-// (the block sets the three-slice GEMM streams).  One thread per row.
+// kc*32 + k, scale * f(m, k), zero outside rows x kdim, in the block layout the
+// three-slice GEMM streams.  One thread per row.
 template <class Fetch>
 __global__ void __launch_bounds__(128) hf_pack3_kernel(Fetch f, int64_t rows, int64_t kdim, int64_t kchunks,
-                                                       float *__restrict__ out) {
+                                                       float scale, float *__restrict__ out) {
   const int64_t t = blockIdx.x / kchunks, kc = blockIdx.x % kchunks;
   const int64_t m = t * 128 + threadIdx.x;
   double v[32];
@@ -123,7 +160,7 @@ __global__ void __launch_bounds__(128) hf_pack3_kernel(Fetch f, int64_t rows, in
     const int64_t kk = kc * 32 + k;
     v[k] = (m < rows && kk < kdim) ? f(m, kk) : 0.0;
   }
-  umma::store_row3(out + (size_t)blockIdx.x * 3 * (umma::kBlockBytes / 4), (int)threadIdx.x, v);
+  store_row3_scaled(out + (size_t)blockIdx.x * 3 * (umma::kBlockBytes / 4), (int)threadIdx.x, v, scale);
 }
 
 // F[s][a][b] = sum_z part[z][a][s n + b], the splits in order.
@@ -250,9 +287,9 @@ int hf_energy_density_tc(const double *ao, const double *rdm1, const double *chi
   double *X = (double *)(ws + L.off_x);
   if ((rc = check_cuda(cudaMemsetAsync(err, 0, sizeof(int), st), "hf err clear"))) return rc;
   hf_pack3_kernel<FetchRows><<<(unsigned)(L.tiles_g * L.kc_ao), 128, 0, st>>>(FetchRows{ao, n}, n_grid, n, L.kc_ao,
-                                                                               pa);
+                                                                               1.0f, pa);
   hf_pack3_kernel<FetchDensity><<<(unsigned)(L.tiles_j * L.kc_ao), 128, 0, st>>>(FetchDensity{rdm1, n}, 2 * n, n,
-                                                                                  L.kc_ao, pb);
+                                                                                  L.kc_ao, 1.0f, pb);
   if ((rc = check_cuda(cudaGetLastError(), "hf pack ao, D"))) return rc;
   TcgArgs a{};
   a.a = pa;
@@ -281,9 +318,9 @@ int hf_fock_tc(const double *ao, const double *chi, const double *g, int64_t n_g
   double *part = (double *)(ws + L.off_part);
   if ((rc = check_cuda(cudaMemsetAsync(err, 0, sizeof(int), st), "hf err clear"))) return rc;
   hf_pack3_kernel<FetchCols><<<(unsigned)(L.tiles_ao * L.rchunks), 128, 0, st>>>(FetchCols{ao, n}, n, n_grid,
-                                                                                  L.rchunks, fa);
+                                                                                  L.rchunks, 1.0f, fa);
   hf_pack3_kernel<FetchHfB><<<(unsigned)(L.tiles_j * L.rchunks), 128, 0, st>>>(
-      FetchHfB{chi, g, n_grid, n, n_omega}, 2 * n, n_grid, L.rchunks, fb);
+      FetchHfB{chi, g, n_grid, n, n_omega}, 2 * n, n_grid, L.rchunks, -0.5f, fb);
   if ((rc = check_cuda(cudaGetLastError(), "hf pack ao^T, B"))) return rc;
   TcgArgs a{};
   a.a = fa;

@@ -250,25 +250,27 @@ class Resident:
                                              ws.numel(), _stream(self.device)))
         return val, hd, hp
 
-    def _hvp_ws(self, net: "Network") -> torch.Tensor:
-        key = net.key
-        cached = getattr(self, "_hws", None)
-        if cached is None or cached[0] != key:
+    # Workspaces of the network passes, one per network shape and form: callers that mix networks (the
+    # DM21 inputs of the default network beside a functional's own, say) would otherwise reallocate and
+    # zero a workspace of gigabytes on every switch.
+    _WS_KEEP = 4
+
+    def _cached_ws(self, name: str, net: "Network", size_fn) -> torch.Tensor:
+        cache = self.__dict__.setdefault(name, {})
+        ws = cache.get(net.key)
+        if ws is None:
             nbytes = ctypes.c_size_t()
-            check(_lib.load().gdft_neural_hvp_workspace_bytes(ctypes.byref(self.desc), ctypes.byref(net.desc),
-                                                              ctypes.byref(nbytes)))
-            self._hws = (key, torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device))
-        return self._hws[1]
+            check(size_fn(ctypes.byref(self.desc), ctypes.byref(net.desc), ctypes.byref(nbytes)))
+            if len(cache) >= self._WS_KEEP:
+                cache.pop(next(iter(cache)))
+            ws = cache[net.key] = torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device)  # error word 0
+        return ws
+
+    def _hvp_ws(self, net: "Network") -> torch.Tensor:
+        return self._cached_ws("_hws", net, _lib.load().gdft_neural_hvp_workspace_bytes)
 
     def _neural_ws(self, net: "Network") -> torch.Tensor:
-        key = net.key
-        cached = getattr(self, "_nws", None)
-        if cached is None or cached[0] != key:
-            nbytes = ctypes.c_size_t()
-            check(_lib.load().gdft_neural_workspace_bytes(ctypes.byref(self.desc), ctypes.byref(net.desc),
-                                                          ctypes.byref(nbytes)))
-            self._nws = (key, torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device))
-        return self._nws[1]
+        return self._cached_ws("_nws", net, _lib.load().gdft_neural_workspace_bytes)
 
     def status(self) -> int:
         """Synchronise and raise if a kernel recorded an expired bounded wait since the last query."""
@@ -276,9 +278,8 @@ class Resident:
         check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(self.ws), self.ws.numel(),
                                              ctypes.byref(st), _stream(self.device)))
         for name in ("_nws", "_hws"):
-            cached = getattr(self, name, None)
-            if cached is not None:
-                check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(cached[1]), cached[1].numel(),
+            for ws in self.__dict__.get(name, {}).values():
+                check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(ws), ws.numel(),
                                                      ctypes.byref(st), _stream(self.device)))
         return st.value
 
