@@ -72,6 +72,12 @@ def dm21_hfgrads_cinputs(functional, params, atoms, ehf, cinputs_wout_hf, densit
                                                   densities).sum(dim=0)
 
 
+# Both terms take dE_xc/d ehf from the functional's device pass (cached by xc_energy_and_grads); of
+# their arguments they read ehf alone, and only when that pass has not run for the molecule.
+dm21_hfgrads_densities._gdft_reads_ehf_only = True
+dm21_hfgrads_cinputs._gdft_reads_ehf_only = True
+
+
 class _NeuralXc(torch.autograd.Function):
     """E_xc(D, theta) with the hand-written adjoint: backward returns g * V_xc and g * dE/dtheta."""
 

@@ -40,7 +40,16 @@ def energy_predictor(functional, nlc_functional=None, clip_cte: float = CLIP, **
                                     want_energy=True)
         energy = exc + enonxc
         fock = engine.fock(atoms.h1e, vj, vxc, clip_cte)
-        if needs_chi:
+        if needs_chi and _cached_library_hf_terms(functional, params, atoms):
+            # The library's DM21 HF terms take dE_xc/d ehf from the network pass just made; they read
+            # none of the densities, inputs or ehf that train.py:165-196 builds for other terms.
+            if functional.densitygrads is not None:
+                vxc_expl = functional.densitygrads(functional, params, atoms, None, None, None)
+                fock = engine.fock_add_hf(fock, vxc_expl, clip_cte)
+            if functional.coefficient_input_grads is not None:
+                vxc_expl = functional.coefficient_input_grads(functional, params, atoms, None, None, None)
+                fock = engine.fock_add_hf(fock, vxc_expl, clip_cte)
+        elif needs_chi:
             # train.py:165-213: the explicit HF terms, each added as F + F^T and clipped.
             grad_densities = functional.energy_densities(atoms) if functional.energy_densities is not None else None
             nograd_densities = functional.nograd_densities(atoms) if functional.nograd_densities else None
@@ -64,3 +73,14 @@ def energy_predictor(functional, nlc_functional=None, clip_cte: float = CLIP, **
         return energy, fock
 
     return predict
+
+
+def _cached_library_hf_terms(functional, params, atoms) -> bool:
+    """True when every HF Fock term of ``functional`` is one of the library's DM21 terms (marked
+    ``_gdft_reads_ehf_only``) and their dE_xc/d ehf is cached for this molecule, parameters and the
+    clip they look it up with."""
+    slots = [f for f in (functional.densitygrads, functional.coefficient_input_grads) if f is not None]
+    if not slots or not all(getattr(f, "_gdft_reads_ehf_only", False) for f in slots):
+        return False
+    cached = getattr(functional, "_hf_cached", None)
+    return cached is not None and cached(params, atoms, CLIP) is not None

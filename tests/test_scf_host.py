@@ -119,3 +119,38 @@ def test_canonical_eigvec_signs_and_mo_grads():
     ref = sum(C[s][:, 2:].T @ F[s] @ C[s][:, :2] for s in range(2))
     assert torch.allclose(G[2:, :2], ref, rtol=1e-13, atol=1e-13)
     assert float(G[:2].abs().max()) == 0.0 and float(G[:, 2:].abs().max()) == 0.0
+
+
+def test_predict_takes_cached_library_hf_terms_only():
+    """predict skips the densities and inputs of train.py:165-196 only for the library's DM21 HF terms
+    with dE/d ehf cached from the same predict's network pass (at the clip those terms look it up with)."""
+    from graddft_gb300 import neural
+    from graddft_gb300.functional import CLIP
+    from graddft_gb300.train import _cached_library_hf_terms
+
+    class Fn:
+        densitygrads = neural.dm21_hfgrads_densities
+        coefficient_input_grads = neural.dm21_hfgrads_cinputs
+
+        def __init__(self, hit):
+            self.hit, self.asked = hit, []
+
+        def _hf_cached(self, params, atoms, clip):
+            self.asked.append(clip)
+            return ("g_dens", "g_cin") if self.hit else None
+
+    hit = Fn(True)
+    assert _cached_library_hf_terms(hit, {}, object()) and hit.asked == [CLIP]
+    assert not _cached_library_hf_terms(Fn(False), {}, object())
+    user = Fn(True)
+    user.densitygrads = lambda *a: None  # a user-supplied term reads the arguments predict builds
+    assert not _cached_library_hf_terms(user, {}, object())
+    only_one = Fn(True)
+    only_one.coefficient_input_grads = None
+    assert _cached_library_hf_terms(only_one, {}, object())
+
+    class NoCache:
+        densitygrads = neural.dm21_hfgrads_densities
+        coefficient_input_grads = None
+
+    assert not _cached_library_hf_terms(NoCache(), {}, object())
