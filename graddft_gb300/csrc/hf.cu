@@ -257,15 +257,6 @@ int check_hf_args(const char *who, int form, const void *ao, const void *chi, in
   return GDFT_OK;
 }
 
-}  // namespace
-
-}  // namespace gdft
-
-using namespace gdft;
-
-namespace gdft {
-namespace {
-
 // Launch-size limits of the mixed form (grid x of each packer and GEMM).
 int check_tc_sizes(const char *who, const HfTcLayout &L) {
   const int64_t lim = (int64_t)INT32_MAX;
@@ -340,7 +331,10 @@ int hf_fock_tc(const double *ao, const double *chi, const double *g, int64_t n_g
 }
 
 }  // namespace
+
 }  // namespace gdft
+
+using namespace gdft;
 
 extern "C" {
 
