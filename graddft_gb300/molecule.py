@@ -202,6 +202,11 @@ class Molecule:
         return torch.stack([engine.hf_fock(ao, chi[:, w:w + 1], g[w:w + 1], form=self.precision)
                             for w in range(chi.shape[1])])
 
+    def _hf_fock_omega_sum(self, chi, g):
+        """The omega sum of ``_hf_fock_per_omega`` as one contraction (B = -1/2 sum_w g chi before the GEMM),
+        on the stored chi without per-omega copies."""
+        return engine.hf_fock(engine.as_device_f64(self.ao, self.device), chi, g, form=self.precision)
+
     def HF_coefficient_input_grad_2_Fock(self, functional, params, omegas, ehf, cinputs_wout_hf, densities,
                                          **kwargs):
         """molecule.py:252-294 -> (omega, spin, orbitals, orbitals): as HF_density_grad_2_Fock with

@@ -25,6 +25,7 @@ import torch
 
 from . import _lib, engine
 from .functional import CLIP, Functional, dm21_combine_cinputs, dm21_combine_densities, dm21_densities
+from .molecule import Molecule
 
 F64 = torch.float64
 
@@ -59,17 +60,30 @@ def _neural_inputs(atoms, net: engine.Network, ehf):
     return x, e
 
 
+def _omega_summed_hf_term(atoms, method, gradient, functional, params, omegas, ehf, *args):
+    """sum over omega of atoms.<method>(functional, params, omegas, ehf, *args), as functional.py:677-757
+    sum what the molecule returns.  With the library's own Molecule method the sum is one exchange
+    contraction over all omegas (g and chi summed inside B) instead of one per omega."""
+    if getattr(type(atoms), method, None) is not getattr(Molecule, method):
+        return getattr(atoms, method)(functional, params, omegas, ehf, *args).sum(dim=0)
+    chi = atoms.select_HF_omegas(omegas)
+    g = getattr(functional, gradient)(params, atoms, engine.as_device_f64(ehf, atoms.device), CLIP)
+    return atoms._hf_fock_omega_sum(chi, g)
+
+
 def dm21_hfgrads_densities(functional, params, atoms, ehf, coefficient_inputs, densities_wout_hf,
                            omegas=(0.0, 0.4)):
-    """functional.py:677-716: the HF Fock term from dE/d ehf through the HF densities, summed over omega."""
-    return atoms.HF_density_grad_2_Fock(functional, params, omegas, ehf, coefficient_inputs,
-                                        densities_wout_hf).sum(dim=0)
+    """functional.py:677-716: the HF Fock term from dE/d ehf through the HF densities, summed over omega
+    (Molecule.HF_density_grad_2_Fock summed)."""
+    return _omega_summed_hf_term(atoms, "HF_density_grad_2_Fock", "hf_density_gradient", functional, params,
+                                 omegas, ehf, coefficient_inputs, densities_wout_hf)
 
 
 def dm21_hfgrads_cinputs(functional, params, atoms, ehf, cinputs_wout_hf, densities, omegas=(0.0, 0.4)):
-    """functional.py:718-757: the HF Fock term from dE/d ehf through the HF inputs, summed over omega."""
-    return atoms.HF_coefficient_input_grad_2_Fock(functional, params, omegas, ehf, cinputs_wout_hf,
-                                                  densities).sum(dim=0)
+    """functional.py:718-757: the HF Fock term from dE/d ehf through the HF inputs, summed over omega
+    (Molecule.HF_coefficient_input_grad_2_Fock summed)."""
+    return _omega_summed_hf_term(atoms, "HF_coefficient_input_grad_2_Fock", "hf_cinput_gradient", functional,
+                                 params, omegas, ehf, cinputs_wout_hf, densities)
 
 
 # Both terms take dE_xc/d ehf from the functional's device pass (cached by xc_energy_and_grads); of

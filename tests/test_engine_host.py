@@ -47,3 +47,54 @@ def test_network_workspaces_cached_per_key():
         nets[id(n.desc)] = n
         r._cached_ws("_nws", n, size_fn)
     assert len(r._nws) == engine.Resident._WS_KEEP and ("a",) not in r._nws
+
+
+def test_dm21_hf_terms_sum_omegas_in_one_contraction(monkeypatch):
+    """dm21_hfgrads_* return the omega sum of the molecule's per-omega HF Fock terms; with the library's
+    Molecule they take it as one contraction over both omegas, a Molecule subclass keeps its own method."""
+    import numpy as np
+
+    from graddft_gb300 import molecule, neural
+
+    calls = []
+
+    def hf_fock(ao, chi, g, form="fp64"):  # F_s = -1/2 sum_w sum_r ao_ra g_wsr chi_rwsb
+        calls.append(chi.shape[1])
+        return -0.5 * torch.einsum("rwsb,wsr,ra->sab", chi, g, ao)
+
+    monkeypatch.setattr(engine, "require_cuda", lambda device=None: torch.device("cpu"))
+    monkeypatch.setattr(engine, "hf_fock", hf_fock)
+    rng = np.random.default_rng(3)
+    n_grid, n = 50, 6
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64)  # noqa: E731
+    mol = molecule.Molecule(grid=molecule.Grid(coords=None, weights=t(rng.random(n_grid))), atom_index=None,
+                            nuclear_pos=None, ao=t(rng.standard_normal((n_grid, n))), grad_ao=None, grad_n_ao=None,
+                            rdm1=t(rng.standard_normal((2, n, n))), nuclear_repulsion=0.0, h1e=None, vj=None,
+                            mo_coeff=None, mo_occ=None, mo_energy=None, omegas=[0.0, 0.4],
+                            chi=t(rng.standard_normal((n_grid, 2, 2, n))))
+    g = {"hf_density_gradient": t(rng.standard_normal((2, 2, n_grid))),
+         "hf_cinput_gradient": t(rng.standard_normal((2, 2, n_grid)))}
+
+    class Fn:
+        def hf_density_gradient(self, params, atoms, ehf, clip):
+            return g["hf_density_gradient"]
+
+        def hf_cinput_gradient(self, params, atoms, ehf, clip):
+            return g["hf_cinput_gradient"]
+
+    for term, method in ((neural.dm21_hfgrads_densities, "HF_density_grad_2_Fock"),
+                         (neural.dm21_hfgrads_cinputs, "HF_coefficient_input_grad_2_Fock")):
+        calls.clear()
+        got = term(Fn(), {}, mol, None, None, None)
+        assert calls == [2]  # both omegas in one contraction
+        per_omega = getattr(mol, method)(Fn(), {}, (0.0, 0.4), None, None, None)
+        assert per_omega.shape == (2, 2, n, n)
+        torch.testing.assert_close(got, per_omega.sum(0), rtol=0, atol=1e-12)
+
+    class Custom(molecule.Molecule):
+        def HF_density_grad_2_Fock(self, *args, **kwargs):
+            return torch.ones((2, 2, n, n), dtype=torch.float64)
+
+    custom = Custom(**{f.name: getattr(mol, f.name) for f in __import__("dataclasses").fields(mol)})
+    assert torch.equal(neural.dm21_hfgrads_densities(Fn(), {}, custom, None, None, None),
+                       torch.full((2, n, n), 2.0, dtype=torch.float64))
