@@ -11,6 +11,7 @@ from .functional import (
     canonicalize_inputs,
     dm21_combine_cinputs,
     dm21_combine_densities,
+    densities,
     dm21_densities,
     stack_densities,
 )
@@ -43,7 +44,7 @@ from .neural import DM21, NeuralFunctional, dm21_coefficient_inputs, dm21_hfgrad
 __all__ = [
     "Grid", "Molecule", "abs_clip", "density", "grad_density", "lapl_density", "kinetic_density",
     "Functional", "canonicalize_inputs", "dm21_combine_cinputs", "dm21_combine_densities", "dm21_densities",
-    "stack_densities", "B3LYP", "B88", "BLYP", "LSDA", "LYP", "PW92", "VWN", "b3lyp_combine",
+    "densities", "stack_densities", "B3LYP", "B88", "BLYP", "LSDA", "LYP", "PW92", "VWN", "b3lyp_combine",
     "b3lyp_exhf_densities", "b88_density", "lsda_density", "lyp_density", "pw92_densities", "vwn_density",
     "energy_predictor", "DM21", "NeuralFunctional", "dm21_coefficient_inputs", "dm21_hfgrads_cinputs",
     "dm21_hfgrads_densities", "diff_simple_scf_loop", "diff_scf_loop", "JittableDiis", "safe_eigh",

@@ -21,11 +21,25 @@ GDFT_ERR_CUDA = 4
 GDFT_ERR_DEVICE = 5
 GDFT_ERR_UNSUPPORTED = 6
 
+GDFT_WAIT_EXPIRY_PROBE = 99
+
 GDFT_FP64 = 0
 GDFT_TF32X3 = 1
 
-COL_LSDA, COL_B88, COL_VWN, COL_LYP, COL_PW92, COL_HF, COL_DM21_LDA, COL_HF_W0, COL_HF_W1 = range(9)
-MAX_COLS = 8
+ABI_VERSION = 2
+
+COL_LSDA, COL_B88, COL_VWN, COL_LYP, COL_PW92, COL_HF, COL_DM21_LDA, COL_HF_W0, COL_HF_W1, COL_ZERO = range(10)
+MAX_COLS = 16
+
+
+def col_dm21_uw(i: int, j: int) -> int:
+    """GDFT_COL_DM21_UW(i, j): dm21_densities' u^i w^j term summed over spin (functional.py:616-624)."""
+    return 0x100 | (i << 4) | j
+
+
+def col_dens_x(spin: int, i: int, j: int) -> int:
+    """GDFT_COL_DENS_X(s, i, j): densities()' exchange term u^i w^j of one spin (functional.py:1130-1134)."""
+    return 0x200 | (spin << 8) | (i << 4) | j
 
 # Every symbol include/gdft.h declares.
 EXPORTS = (
@@ -42,7 +56,7 @@ EXPORTS = (
     "gdft_tc_gemm3_probe", "gdft_neural_batch_workspace_bytes", "gdft_neural_batch_xc",
     "gdft_xc_energy_grads_hf", "gdft_hf_workspace_bytes", "gdft_hf_energy_density", "gdft_hf_fock",
     "gdft_fock_add_hf", "gdft_neural_xc_hf_grads", "gdft_hf_workspace_bytes_form", "gdft_hf_energy_density_form",
-    "gdft_hf_fock_form", "gdft_hf_device_status",
+    "gdft_hf_fock_form", "gdft_hf_device_status", "gdft_selftest_wait_expiry",
 )
 STAGE_AO, STAGE_DENSITY, STAGE_POINT, STAGE_VXC, STAGE_REDUCE, STAGE_MLP = range(6)
 
@@ -150,6 +164,7 @@ _SIGS = {
     "gdft_fock": ([I32, P, P, P, D, P, P], ctypes.c_int),
     "gdft_coulomb": ([I32, P, P, P, D, P, P, P], ctypes.c_int),
     "gdft_device_status": ([PMOL, P, SZ, ctypes.POINTER(I32), P], ctypes.c_int),
+    "gdft_selftest_wait_expiry": ([PMOL, P, SZ, I32, P], ctypes.c_int),
     "gdft_selftest_umma": ([ctypes.POINTER(D)], ctypes.c_int),
     "gdft_umma_probe": ([P, P, P], ctypes.c_int),
     "gdft_network_param_count": ([PNET, ctypes.POINTER(SZ)], ctypes.c_int),
@@ -186,7 +201,7 @@ def load(path: str | None = None):
             fn = getattr(lib, name)
             fn.argtypes = args
             fn.restype = res
-        if lib.gdft_abi_version() != 1:
+        if lib.gdft_abi_version() != ABI_VERSION:
             raise ImportError("libgdft_xc.so ABI version mismatch")
         _lib = lib
         return lib

@@ -168,7 +168,8 @@ static int check_functional(const gdft_functional *fn, const double *ehf, int n_
   }
   for (int i = 0; i < fn->n_cols; ++i) {
     const int c = fn->cols[i];
-    if (c < GDFT_COL_LSDA || c > GDFT_COL_HF_W1) {
+    const bool uw = (c & ~0xff) == 0x100 || (c & ~0x1ff) == 0x200;  // GDFT_COL_DM21_UW / GDFT_COL_DENS_X
+    if (!uw && (c < GDFT_COL_LSDA || c > GDFT_COL_ZERO)) {
       set_error("unknown energy-density column %d", c);
       return GDFT_ERR_INVALID;
     }
@@ -1196,6 +1197,19 @@ int gdft_device_status(const gdft_molecule *mol, void *d_ws, size_t ws_bytes, in
   return GDFT_OK;
 }
 
+int gdft_selftest_wait_expiry(const gdft_molecule *mol, void *d_ws, size_t ws_bytes, int32_t limit, void *stream) {
+  int rc = check_mol(mol);
+  if (rc) return rc;
+  if ((rc = check_ws(mol, d_ws, ws_bytes))) return rc;
+  if (limit < 1 || limit > 65536) {
+    set_error("gdft_selftest_wait_expiry: limit %d outside 1..65536 polls", limit);
+    return GDFT_ERR_INVALID;
+  }
+  int *err = (int *)((char *)d_ws + ws_layout(mol).off_err);
+  return check_cuda(launch_wait_expiry_probe(err, (uint32_t)limit, GDFT_WAIT_EXPIRY_PROBE, (cudaStream_t)stream),
+                    "wait expiry probe");
+}
+
 int gdft_energy_densities(const gdft_molecule *mol, const double *d_rdm1, const gdft_functional *fn,
                           const double *d_ehf, int32_t n_omega, double *d_dens, void *d_ws, size_t ws_bytes,
                           void *stream) {
@@ -1216,8 +1230,11 @@ int gdft_energy_densities(const gdft_molecule *mol, const double *d_rdm1, const 
                     "xc_point");
 }
 
+// Largest grid whose block count (n_grid + 255) / 256 fits the int of integrate_blocks.
+static constexpr int64_t kIntegrateMaxGrid = (int64_t)INT32_MAX * 256 - 255;
+
 int gdft_integrate_workspace_bytes(int64_t n_grid, size_t *bytes) {
-  if (n_grid <= 0 || bytes == nullptr) {
+  if (n_grid <= 0 || n_grid > kIntegrateMaxGrid || bytes == nullptr) {
     set_error("gdft_integrate_workspace_bytes: invalid arguments");
     return GDFT_ERR_INVALID;
   }
@@ -1230,6 +1247,11 @@ int gdft_integrate(int64_t n_grid, int32_t n_cols, const double *h_coeffs, int32
   if (n_grid <= 0 || n_cols < 1 || !(n_coeffs == 1 || n_coeffs == n_cols) || n_coeffs > GDFT_MAX_COLS ||
       h_coeffs == nullptr || d_dens == nullptr || d_weights == nullptr || d_exc == nullptr) {
     set_error("gdft_integrate: invalid arguments (n_cols=%d, n_coeffs=%d)", n_cols, n_coeffs);
+    return GDFT_ERR_INVALID;
+  }
+  if (n_grid > kIntegrateMaxGrid) {  // block counts are int: checked before they are formed
+    set_error("gdft_integrate: n_grid=%lld is beyond the supported %lld", (long long)n_grid,
+              (long long)kIntegrateMaxGrid);
     return GDFT_ERR_INVALID;
   }
   const size_t need = align256((size_t)integrate_blocks(n_grid) * sizeof(double));

@@ -60,6 +60,9 @@ cudaError_t launch_xc_point(const double *feat, const double *w, int64_t n_grid,
                             const gdft_functional &fn, const double *ehf, int n_omega, double *coef,
                             double *epart, double *dens, cudaStream_t st, double *ghf = nullptr);
 
+// tc_selftest.cu: a bounded wait that runs out on purpose (failure-detection test).
+cudaError_t launch_wait_expiry_probe(int *err, uint32_t limit, int code, cudaStream_t st);
+
 // reduce.cu
 int integrate_blocks(int64_t n_grid);
 cudaError_t launch_pad_potentials(const double *pot, int64_t n_grid, int64_t np, double *coef, cudaStream_t st);

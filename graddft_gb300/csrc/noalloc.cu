@@ -35,7 +35,9 @@ double *g_partials_addr[kMaxDevices] = {nullptr};
 
 // Device address of the scratch on the current device.  In host code the
 // array's name is only a host-side stand-in, so the address comes from
-// cudaGetSymbolAddress, once per device, with that device current.
+// cudaGetSymbolAddress, once per device, with that device current.  The
+// address belongs to the device's primary context; a cudaDeviceReset ends it,
+// which is why gdft.h rules out this entry after a reset.
 int partials_on_current_device(double **out) {
   int dev = 0;
   int rc = check_cuda(cudaGetDevice(&dev), "integrate_noalloc: cudaGetDevice");
@@ -68,13 +70,14 @@ extern "C" int gdft_integrate_noalloc(int64_t n_grid, int32_t n_cols, const doub
     set_error("gdft_integrate_noalloc: invalid arguments (n_cols=%d, n_coeffs=%d)", n_cols, n_coeffs);
     return GDFT_ERR_INVALID;
   }
-  const int blocks = integrate_blocks(n_grid);
-  if (n_grid > (int64_t)kNoAllocMaxBlocks * 256 || blocks > kNoAllocMaxBlocks) {
+  // The size check comes before any block arithmetic, so no grid size can overflow it.
+  if (n_grid > (int64_t)kNoAllocMaxBlocks * 256) {
     set_error("gdft_integrate_noalloc: n_grid=%lld exceeds the fixed scratch limit of %lld grid points; "
               "use gdft_integrate with a caller workspace",
               (long long)n_grid, (long long)kNoAllocMaxBlocks * 256);
     return GDFT_ERR_INVALID;
   }
+  const int blocks = integrate_blocks(n_grid);
   double *partials = nullptr;
   int rc = partials_on_current_device(&partials);
   if (rc) return rc;

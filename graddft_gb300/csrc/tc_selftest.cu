@@ -71,7 +71,27 @@ __global__ void __launch_bounds__(128) umma_selftest_kernel(const float *__restr
   if (warp == 0) umma::tmem_dealloc(tbase, 128);
 }
 
+// Waits on an mbarrier that nothing arrives on, with a short poll limit, so
+// that the bounded wait every pipeline kernel uses runs out: the thread
+// records `code` in the error word and the CTA returns.  Nothing else is in
+// flight (no bulk copy, no MMA, no TMEM held), so the context stays usable.
+__global__ void wait_expiry_probe_kernel(int *__restrict__ err, uint32_t limit, int code) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    umma::mbar_init(&bar, 1);
+    umma::fence_barrier_init();
+    if (!umma::mbar_wait_n(&bar, 0, limit)) atomicCAS(err, 0, code);
+    umma::mbar_inval(&bar);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_wait_expiry_probe(int *err, uint32_t limit, int code, cudaStream_t st) {
+  wait_expiry_probe_kernel<<<1, 32, 0, st>>>(err, limit, code);
+  return cudaGetLastError();
+}
+
 }  // namespace gdft
 
 using namespace gdft;

@@ -47,13 +47,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // far fewer iterations.
 constexpr uint32_t kWaitLimit = 1u << 22;
 
-// Returns false when the limit is exceeded.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+// Returns false when `limit` polls pass without the phase completing.
+__device__ __forceinline__ bool mbar_wait_n(uint64_t *bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     if (i > 64) __nanosleep(64);
   }
   return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) { return mbar_wait_n(bar, parity, kWaitLimit); }
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // Warp-uniform bounded wait: lane 0 polls, the result is broadcast, and every

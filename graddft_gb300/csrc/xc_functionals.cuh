@@ -175,6 +175,48 @@ __device__ __forceinline__ T lyp_c_e(const T rho_in[2], const T s[2], const T la
   return -a * xwhere(big, gamma / (1.0 + d * rhom1_3) * (rsum + braket), zero);
 }
 
+// One spin's u^i w^j feature term, 2^(4/3 log rho + i log u + j log w), of
+// dm21_densities (functional.py:588-624) and of densities() (:1104-1134):
+//   log rho = log2(clip(rho)),  log x = log2(clip(|grad rho|^2))/2 - 4/3 log rho,
+//   log u   = where(log rho > log2 clip, log x - log2(1 + beta 2^log x) + log2 beta, 0),
+//   log 1/t = -(5/3 log rho - log tau + 2/3 log2(6 pi^2) + log2(3/5))   (dm21_densities, :601-603)
+//           = log tau - 5/3 log rho                                      (densities(), :1119),
+//   log w   = where(log rho > log2 clip, log 1/t - log2(1 + beta 2^log 1/t) + log2 beta, 0),
+// with clip(v) = clip(v, a_min=clip_cte) and beta = 1/1024.  A zero power
+// adds 0 * (a finite log u or log w) to the exponent in the reference, so the
+// term is skipped (2^(e + 0) = 2^e).
+template <class T>
+__device__ __forceinline__ T uw_term(const T &rho, const T &sig, const T &tau, int i, int j, bool dm21_form,
+                                     double clip) {
+  const double beta = 1.0 / 1024.0;
+  const double lbeta = log2(beta);
+  const T log_rho = xlog2(xclipmin(rho, clip));
+  const bool above = val(log_rho) > log2(clip);
+  T ex = 4.0 / 3.0 * log_rho;
+  if (i != 0) {
+    const T log_x = xlog2(xclipmin(sig, clip)) / 2.0 - 4.0 / 3.0 * log_rho;
+    const T log_u = above ? (log_x - xlog2(1.0 + beta * xexp2(log_x))) + lbeta : tconst(rho, 0.0);
+    ex = ex + (double)i * log_u;
+  }
+  if (j != 0) {
+    const T log_tau = xlog2(xclipmin(tau, clip));
+    const T log_1t = dm21_form ? -(((5.0 / 3.0 * log_rho - log_tau) + 2.0 / 3.0 * log2(6.0 * (kPi * kPi))) +
+                                   log2(3.0 / 5.0))
+                               : log_tau - 5.0 / 3.0 * log_rho;
+    const T log_w = above ? (log_1t - xlog2(1.0 + beta * xexp2(log_1t))) + lbeta : tconst(rho, 0.0);
+    ex = ex + (double)j * log_w;
+  }
+  return xexp2(ex);
+}
+
+// dm21_densities' column for (i, j): the spin sum of uw_term, times the
+// Dirac exchange constant -2 pi (3/(4 pi))^(4/3) for i = j = 0 (functional.py:616-624).
+template <class T>
+__device__ __forceinline__ T dm21_uw(const T rho[2], const T sig[2], const T tau[2], int i, int j, double clip) {
+  const T s = uw_term(rho[0], sig[0], tau[0], i, j, true, clip) + uw_term(rho[1], sig[1], tau[1], i, j, true, clip);
+  return (i == 0 && j == 0) ? s * (-2.0 * kPi * pow(3.0 / (4.0 * kPi), 4.0 / 3.0)) : s;
+}
+
 // dm21_densities(functional_type="LDA"), functional.py:534-626: one column.
 template <class T>
 __device__ __forceinline__ T dm21_lda(const T rho[2], double clip) {

@@ -27,21 +27,36 @@ namespace {
 
 constexpr int kBlock = 256;
 
-// Dual variable indices for the classical functionals: rho_a, rho_b,
-// |grad rho_a|^2, |grad rho_b|^2, lap_a, lap_b.
-constexpr int KV = 6;
-enum { V_R0 = 0, V_R1 = 1, V_S0 = 2, V_S1 = 3, V_L0 = 4, V_L1 = 5 };
+// Dual variable indices: rho_a, rho_b, |grad rho_a|^2, |grad rho_b|^2, lap_a,
+// lap_b and, for columns that read it (the w powers of the feature columns),
+// tau_a, tau_b.  The kernel runs with K = 6 unless a column depends on tau.
+enum { V_R0 = 0, V_R1 = 1, V_S0 = 2, V_S1 = 3, V_L0 = 4, V_L1 = 5, V_T0 = 6, V_T1 = 7 };
 
 template <int K>
 __device__ __forceinline__ Dual<K> seed(double v, int idx) {
   Dual<K> r = dconst<K>(v);
-  r.d[idx] = 1.0;
+  if (idx < K) r.d[idx] = 1.0;
   return r;
 }
 
+// Fields of a GDFT_COL_DM21_UW / GDFT_COL_DENS_X code.
+__host__ __device__ __forceinline__ bool is_uw_col(int col) { return (col & ~0xff) == 0x100 || (col & ~0x1ff) == 0x200; }
+__host__ __device__ __forceinline__ int uw_i(int col) { return (col >> 4) & 15; }
+__host__ __device__ __forceinline__ int uw_j(int col) { return col & 15; }
+
+// The feature-power columns out of line: inlined beside the classical
+// functionals they would raise every functional's register pressure.
 template <class T>
-__device__ __forceinline__ T column(int col, const T rho[2], const T s[2], const T lap[2], double hf,
+__device__ __noinline__ T uw_column(int col, const T rho[2], const T s[2], const T tau[2], double clip) {
+  if ((col & ~0xff) == 0x100) return dm21_uw(rho, s, tau, uw_i(col), uw_j(col), clip);
+  const int sp = (col >> 8) & 1;  // densities(): one spin's exchange term
+  return uw_term(rho[sp], s[sp], tau[sp], uw_i(col), uw_j(col), false, clip);
+}
+
+template <class T>
+__device__ __forceinline__ T column(int col, const T rho[2], const T s[2], const T lap[2], const T tau[2], double hf,
                                     double hf0, double hf1, double clip, unsigned *poison) {
+  if (is_uw_col(col)) return uw_column(col, rho, s, tau, clip);
   switch (col) {
     case GDFT_COL_LSDA: return lsda_x_e(rho, clip);
     case GDFT_COL_B88: return b88_x_e(rho, s, clip);
@@ -52,10 +67,11 @@ __device__ __forceinline__ T column(int col, const T rho[2], const T s[2], const
     case GDFT_COL_HF: return tconst(rho[0], hf);
     case GDFT_COL_HF_W0: return tconst(rho[0], hf0);
     case GDFT_COL_HF_W1: return tconst(rho[0], hf1);
-    default: return tconst(rho[0], 0.0);
+    default: return tconst(rho[0], 0.0);  // GDFT_COL_ZERO
   }
 }
 
+template <int KV>
 __global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restrict__ feat, const double *__restrict__ w,
                                                           int64_t n_grid, int64_t np, gdft_functional fn,
                                                           const double *__restrict__ ehf, int n_omega,
@@ -76,7 +92,7 @@ __global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restri
       for (int s = 0; s < 2; ++s)
 #pragma unroll
         for (int k = 0; k < kFeat; ++k) f[s][k] = feat[((size_t)s * kFeat + k) * np + p];
-      Dual<KV> rho[2], sg[2], lap[2];
+      Dual<KV> rho[2], sg[2], lap[2], tau[2];
 #pragma unroll
       for (int s = 0; s < 2; ++s) {
         rho[s] = seed<KV>(f[s][F_RHO], V_R0 + s);
@@ -84,6 +100,7 @@ __global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restri
         const double sv = (f[s][F_GX] * f[s][F_GX] + f[s][F_GY] * f[s][F_GY]) + f[s][F_GZ] * f[s][F_GZ];
         sg[s] = seed<KV>(sv, V_S0 + s);
         lap[s] = seed<KV>(f[s][F_LAP], V_L0 + s);
+        tau[s] = seed<KV>(f[s][F_TAU], V_T0 + s);  // a constant when KV = 6 (no column reads tau)
       }
       double hf = 0.0, hf0 = 0.0, hf1 = 0.0;
       if (ehf != nullptr) {
@@ -101,7 +118,7 @@ __global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restri
       double e_raw = 0.0, c_hf = 0.0;  // unclipped columns' sum; coefficient of the HF column
       unsigned poison = 0;  // spins whose rho gradient is NaN in the reference (see corr_pol)
       for (int i = 0; i < fn.n_cols; ++i) {
-        Dual<KV> e = column<Dual<KV>>(fn.cols[i], rho, sg, lap, hf, hf0, hf1, clip, &poison);
+        Dual<KV> e = column<Dual<KV>>(fn.cols[i], rho, sg, lap, tau, hf, hf0, hf1, clip, &poison);
         if (dens != nullptr) dens[(size_t)p * fn.n_cols + i] = e.v;
         const double ci = fn.n_coeffs == 1 ? fn.coeffs[0] : fn.coeffs[i];
         e_raw += ci * e.v;
@@ -127,7 +144,8 @@ __global__ void __launch_bounds__(kBlock) xc_point_kernel(const double *__restri
         c[s][C_GY] = 2.0 * (2.0 * f[s][F_GY] * dsig);
         c[s][C_GZ] = 2.0 * (2.0 * f[s][F_GZ] * dsig);
         c[s][C_LAP] = 2.0 * dlap;
-        c[s][C_KIN] = 2.0 * dlap;  // + 1/2 dE/dtau (no tau dependence in these columns)
+        c[s][C_KIN] = 2.0 * dlap;
+        if (KV > V_T0 + s) c[s][C_KIN] += 0.5 * dv[(KV > V_T0 + s) ? V_T0 + s : 0];  // tau = 1/2 sum_j D d_j phi d_j phi
         if (poison & (1u << s)) c[s][C_RHO] = __longlong_as_double(0x7ff8000000000000ll);
       }
     }
@@ -161,7 +179,12 @@ cudaError_t launch_xc_point(const double *feat, const double *w, int64_t n_grid,
                             const gdft_functional &fn, const double *ehf, int n_omega, double *coef,
                             double *epart, double *dens, cudaStream_t st, double *ghf) {
   const int blocks = xc_point_blocks(np);
-  xc_point_kernel<<<blocks, kBlock, 0, st>>>(feat, w, n_grid, np, fn, ehf, n_omega, coef, epart, dens, ghf);
+  bool reads_tau = false;
+  for (int i = 0; i < fn.n_cols; ++i) reads_tau |= is_uw_col(fn.cols[i]) && uw_j(fn.cols[i]) != 0;
+  if (reads_tau)
+    xc_point_kernel<8><<<blocks, kBlock, 0, st>>>(feat, w, n_grid, np, fn, ehf, n_omega, coef, epart, dens, ghf);
+  else
+    xc_point_kernel<6><<<blocks, kBlock, 0, st>>>(feat, w, n_grid, np, fn, ehf, n_omega, coef, epart, dens, ghf);
   return cudaGetLastError();
 }
 

@@ -252,19 +252,31 @@ class Resident:
 
     # Workspaces of the network passes, one per network shape and form: callers that mix networks (the
     # DM21 inputs of the default network beside a functional's own, say) would otherwise reallocate and
-    # zero a workspace of gigabytes on every switch.
+    # zero a workspace of gigabytes on every switch.  The cache drops its least recently used entry.
     _WS_KEEP = 4
 
     def _cached_ws(self, name: str, net: "Network", size_fn) -> torch.Tensor:
         cache = self.__dict__.setdefault(name, {})
-        ws = cache.get(net.key)
+        ws = cache.pop(net.key, None)  # re-inserted last: the dict's order is least recently used first
         if ws is None:
             nbytes = ctypes.c_size_t()
             check(size_fn(ctypes.byref(self.desc), ctypes.byref(net.desc), ctypes.byref(nbytes)))
             if len(cache) >= self._WS_KEEP:
-                cache.pop(next(iter(cache)))
-            ws = cache[net.key] = torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device)  # error word 0
+                self._retire_ws(cache.pop(next(iter(cache))))
+            ws = torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device)  # error word 0
+        cache[net.key] = ws
         return ws
+
+    def _retire_ws(self, ws: torch.Tensor) -> None:
+        """Read a dropped workspace's error word before it goes: an expired bounded wait recorded there
+        is kept and reported by the next status()."""
+        st = ctypes.c_int32()
+        rc = _lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(ws), ws.numel(), ctypes.byref(st),
+                                            _stream(self.device))
+        if rc == _lib.GDFT_ERR_DEVICE:
+            self.__dict__["_sticky_status"] = st.value
+        else:
+            check(rc)
 
     def _hvp_ws(self, net: "Network") -> torch.Tensor:
         return self._cached_ws("_hws", net, _lib.load().gdft_neural_hvp_workspace_bytes)
@@ -273,7 +285,8 @@ class Resident:
         return self._cached_ws("_nws", net, _lib.load().gdft_neural_workspace_bytes)
 
     def status(self) -> int:
-        """Synchronise and raise if a kernel recorded an expired bounded wait since the last query."""
+        """Synchronise and raise if a kernel recorded an expired bounded wait since the last query
+        (including one recorded in a network workspace the cache has since dropped)."""
         st = ctypes.c_int32()
         check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(self.ws), self.ws.numel(),
                                              ctypes.byref(st), _stream(self.device)))
@@ -281,6 +294,10 @@ class Resident:
             for ws in self.__dict__.get(name, {}).values():
                 check(_lib.load().gdft_device_status(ctypes.byref(self.desc), _ptr(ws), ws.numel(),
                                                      ctypes.byref(st), _stream(self.device)))
+        sticky = self.__dict__.pop("_sticky_status", 0)
+        if sticky:
+            raise _lib.GdftError(f"a device-side wait expired (code {sticky}) in a network workspace since "
+                                 "dropped from the cache; results of the calls before it are invalid")
         return st.value
 
     def _rdm1(self, rdm1) -> torch.Tensor:

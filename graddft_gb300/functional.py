@@ -9,6 +9,7 @@ to columns of the fused device kernels; an unknown callable raises
 """
 from __future__ import annotations
 
+import functools
 from dataclasses import dataclass
 from typing import Any, Callable, Optional, Sequence
 
@@ -21,6 +22,19 @@ CLIP = 1e-30
 
 
 def energy_density_columns(fn) -> tuple:
+    """The device columns of a known energy-density callable.
+
+    ``functools.partial(dm21_densities, functional_type=...)`` and the same of
+    ``densities`` (how the reference's examples select the feature set, e.g.
+    examples/article_experiments/train_atoms.py:93) resolve through the bound
+    keywords."""
+    if isinstance(fn, functools.partial) and getattr(fn.func, "_gdft_cols_of", None) is not None:
+        if fn.args:
+            raise NotImplementedError(f"{fn.func.__name__}: bind functional_type / clip_cte as keywords")
+        kw = dict(fn.keywords)
+        if float(kw.pop("clip_cte", CLIP)) != CLIP:
+            raise NotImplementedError(f"{fn.func.__name__}: energy densities evaluate with clip_cte={CLIP}")
+        return tuple(fn.func._gdft_cols_of(**kw))
     cols = getattr(fn, "_gdft_cols", None)
     if cols is None:
         raise NotImplementedError(
@@ -248,12 +262,68 @@ def dm21_combine_densities(densities, ehf):
     return torch.cat(parts, dim=1)
 
 
-@tag_columns(_lib.COL_DM21_LDA)
+def _uw_ranges(functional_type):
+    """u_range / w_range of dm21_densities and densities (functional.py:575-585, 1089-1099).
+
+    A dict {'u_range': ..., 'w_range': ...} follows the documented meaning
+    (functional.py:548-556); the reference's own code binds the ranges only
+    for a string and raises UnboundLocalError for a dict."""
+    if isinstance(functional_type, str):
+        if functional_type in ("LDA", "DM21"):
+            return range(0, 1), range(0, 1)
+        if functional_type == "GGA":
+            return range(0, 2), range(0, 1)
+        if functional_type == "MGGA":
+            return range(0, 2), range(0, 2)
+        raise ValueError(f"Functional type {functional_type} not recognized, must be one of LDA, GGA, MGGA.")
+    if isinstance(functional_type, dict) and set(functional_type) == {"u_range", "w_range"}:
+        u, w = list(functional_type["u_range"]), list(functional_type["w_range"])
+        if not all(isinstance(k, int) and 0 <= k <= 15 for k in u + w):
+            raise NotImplementedError("u_range / w_range powers must be integers in 0..15")
+        return u, w
+    raise ValueError(f"Functional type {functional_type} not recognized, must be one of LDA, GGA, MGGA "
+                     "or a dict with u_range and w_range")
+
+
+def _dm21_cols(functional_type="LDA"):
+    u, w = _uw_ranges(functional_type)
+    return tuple(_lib.COL_DM21_LDA if (i, j) == (0, 0) else _lib.col_dm21_uw(i, j) for i in u for j in w)
+
+
+def _densities_cols(functional_type="LDA"):
+    u, w = _uw_ranges(functional_type)
+    ex = tuple(_lib.col_dens_x(s, i, j) for i in u for j in w for s in (0, 1))
+    return ex + (_lib.COL_ZERO,) * (2 * len(u) * len(w))
+
+
+def _check_cols(cols, fname):
+    if len(cols) > _lib.MAX_COLS:
+        raise NotImplementedError(f"{fname}: {len(cols)} columns; the device functional holds {_lib.MAX_COLS}")
+    return cols
+
+
 def dm21_densities(atoms, functional_type="LDA", clip_cte: float = CLIP, *_, **__):
-    """functional.py:534-626 (the 'LDA'/'DM21' feature set used by DM21)."""
-    if functional_type not in ("LDA", "DM21"):
-        raise NotImplementedError(f"dm21_densities functional_type={functional_type!r} is not built")
-    return molecule_energy_densities(atoms, (_lib.COL_DM21_LDA,), clip_cte)
+    """functional.py:534-626: one column per (i, j) in u_range x w_range, sum over spin of
+    2^(4/3 log rho + i log u + j log w), the (0, 0) column scaled to DM21's LDA exchange."""
+    cols = _check_cols(_dm21_cols(functional_type), "dm21_densities")
+    return molecule_energy_densities(atoms, cols, clip_cte)
+
+
+dm21_densities._gdft_cols = (_lib.COL_DM21_LDA,)
+dm21_densities._gdft_cols_of = _dm21_cols
+
+
+def densities(atoms, functional_type="LDA", clip_cte: float = CLIP, *_, **__):
+    """functional.py:1048-1202: per (i, j) the two spins' exchange terms 2^(4/3 log rho + i log u + j log w)
+    (log 1/t = log tau - 5/3 log rho), then per (i, j) the two correlation features.  Those are
+    where(round(e_PW92, int(log10(clip_cte))) > clip_cte, ..., 0) (:1188-1197): e_PW92 is negative and
+    clip_cte positive, so they are zero for every input, with zero gradient."""
+    cols = _check_cols(_densities_cols(functional_type), "densities")
+    return molecule_energy_densities(atoms, cols, clip_cte)
+
+
+densities._gdft_cols = _densities_cols("LDA")
+densities._gdft_cols_of = _densities_cols
 
 
 def dm21_combine_cinputs(cinputs, ehf):

@@ -16,6 +16,8 @@ import torch
 from . import engine
 
 _AO_FIELDS = ("grid", "ao", "grad_ao", "grad_n_ao", "precision")
+# clip_cte of the HF Fock-term gradients when the caller passes none (molecule.py:206-294 default).
+HF_GRAD_CLIP = 1e-30
 
 
 @dataclass(frozen=True)
@@ -194,7 +196,7 @@ class Molecule:
         """
         chi = self.select_HF_omegas(omegas)
         g = functional.hf_density_gradient(params, self, engine.as_device_f64(ehf, self.device),
-                                           kwargs.get("clip_cte", 1e-30))
+                                           kwargs.get("clip_cte", HF_GRAD_CLIP))
         return self._hf_fock_per_omega(chi, g)
 
     def _hf_fock_per_omega(self, chi, g):
@@ -213,7 +215,7 @@ class Molecule:
         g = dE_xc/d ehf through the network's HF inputs (molecule.py:668-673)."""
         chi = self.select_HF_omegas(omegas)
         g = functional.hf_cinput_gradient(params, self, engine.as_device_f64(ehf, self.device),
-                                          kwargs.get("clip_cte", 1e-30))
+                                          kwargs.get("clip_cte", HF_GRAD_CLIP))
         return self._hf_fock_per_omega(chi, g)
 
     def to_dict(self) -> dict:

@@ -25,7 +25,7 @@ import torch
 
 from . import _lib, engine
 from .functional import CLIP, Functional, dm21_combine_cinputs, dm21_combine_densities, dm21_densities
-from .molecule import Molecule
+from .molecule import HF_GRAD_CLIP, Molecule
 
 F64 = torch.float64
 
@@ -64,10 +64,14 @@ def _omega_summed_hf_term(atoms, method, gradient, functional, params, omegas, e
     """sum over omega of atoms.<method>(functional, params, omegas, ehf, *args), as functional.py:677-757
     sum what the molecule returns.  With the library's own Molecule method the sum is one exchange
     contraction over all omegas (g and chi summed inside B) instead of one per omega."""
-    if getattr(type(atoms), method, None) is not getattr(Molecule, method):
+    own = all(getattr(type(atoms), m, None) is getattr(Molecule, m)
+              for m in (method, "select_HF_omegas", "_hf_fock_per_omega", "_hf_fock_omega_sum"))
+    if not own:  # a Molecule subclass that changes any step keeps its own per-omega method
         return getattr(atoms, method)(functional, params, omegas, ehf, *args).sum(dim=0)
     chi = atoms.select_HF_omegas(omegas)
-    g = getattr(functional, gradient)(params, atoms, engine.as_device_f64(ehf, atoms.device), CLIP)
+    # The reference calls the molecule method without clip_cte (functional.py:711-713, 752-754), so the
+    # method's default applies.
+    g = getattr(functional, gradient)(params, atoms, engine.as_device_f64(ehf, atoms.device), HF_GRAD_CLIP)
     return atoms._hf_fock_omega_sum(chi, g)
 
 
@@ -228,6 +232,11 @@ class NeuralFunctional(Functional):
         return ehf
 
     def _check_slots(self):
+        from .functional import energy_density_columns
+
+        if self.energy_densities is not None and energy_density_columns(self.energy_densities) != (_lib.COL_DM21_LDA,):
+            raise NotImplementedError("the device network pass takes dm21_densities' LDA column as its "
+                                      "local energy density")
         if getattr(self.combine_inputs, "__name__", "") != "dm21_combine_cinputs" and self.combine_inputs is not None:
             raise NotImplementedError("combine_inputs must be dm21_combine_cinputs")
         if self.combine_densities is not None and getattr(self.combine_densities, "_gdft_hf_cols", None) is None:

@@ -38,8 +38,9 @@ def shard_molecule(mol, rank: int, world: int):
     elif g2 is not None:
         g2 = g2[a:b]
     ehf = None if mol.ehf is None else mol.ehf[..., a:b]
+    chi = None if getattr(mol, "chi", None) is None else mol.chi[a:b]  # chi is (grid, omega, spin, orbitals)
     return dataclasses.replace(mol, grid=grid, ao=mol.ao[a:b], grad_ao=mol.grad_ao[a:b], grad_n_ao=g2, ehf=ehf,
-                               _resident=None)
+                               chi=chi, _resident=None)
 
 
 def allreduce_sum(tensors: Sequence[torch.Tensor], group=None) -> list:
@@ -54,3 +55,23 @@ def allreduce_sum(tensors: Sequence[torch.Tensor], group=None) -> list:
         t.copy_(flat[off:off + n].view_as(t))
         off += n
     return list(tensors)
+
+
+def xc_energy_and_grads_sharded(functional, params, molecule, want_dparams: bool = False, group=None):
+    """(E_xc, V_xc[, dE_xc/dtheta]) of the whole grid: this rank evaluates its slice
+    (shard_molecule), one all-reduce sums the parts.  ``molecule`` is the full,
+    replicated description; its per-point arrays are sliced, never copied whole
+    to the device.  With ``want_dparams`` the functional is a NeuralFunctional
+    and the parameter gradient tree (views of one flat vector) is summed too."""
+    import torch.distributed as dist
+
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    part = shard_molecule(molecule, rank, world)
+    if want_dparams:
+        e, v, dp = functional.xc_energy_and_grads_params(params, part)
+        leaves = [t for mod in dp["params"].values() for t in mod.values()]
+        allreduce_sum([e.reshape(1), v] + leaves, group)
+        return e, v, dp
+    e, v = functional.xc_energy_and_grads(params, part)
+    allreduce_sum([e.reshape(1), v], group)
+    return e, v

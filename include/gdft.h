@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GDFT_ABI_VERSION 1
+#define GDFT_ABI_VERSION 2
 
 /* Status codes (the Python layer maps them to ValueError/TypeError/RuntimeError,
  * as the reference raises ValueError at functional.py:583, molecule.py:174-180). */
@@ -59,10 +59,24 @@ enum {
   GDFT_COL_HF = 5,       /* sum_{omega,spin} ehf   popular_functionals.py:328-334 */
   GDFT_COL_DM21_LDA = 6, /* dm21_densities 'LDA'   functional.py:534-626          */
   GDFT_COL_HF_W0 = 7,    /* sum_spin ehf[0]        functional.py:652-675          */
-  GDFT_COL_HF_W1 = 8     /* sum_spin ehf[1]        functional.py:652-675          */
+  GDFT_COL_HF_W1 = 8,    /* sum_spin ehf[1]        functional.py:652-675          */
+  GDFT_COL_ZERO = 9      /* the correlation features of densities() (functional.py:1146-1200):
+                            e_PW92 < 0 is rounded to a multiple of 10^(-int(log10 clip)) and
+                            compared with clip > 0 (:1188-1197), so they are identically 0 and
+                            carry no gradient                                           */
 };
 
-#define GDFT_MAX_COLS 8
+/* Feature-power columns u^i w^j of dm21_densities and densities() for any
+ * u_range / w_range (functional.py:534-626, 1048-1142), 0 <= i, j <= 15:
+ *  - GDFT_COL_DM21_UW(i, j): sum over spin of 2^(4/3 log rho + i log u + j log w),
+ *    times -2 pi (3/(4 pi))^(4/3) for i = j = 0 (dm21_densities, :616-624);
+ *  - GDFT_COL_DENS_X(s, i, j): the same term for spin s alone with the MGGA
+ *    variable of densities() (log 1/t = log tau - 5/3 log rho, :1119),
+ *    unscaled (:1130-1134). */
+#define GDFT_COL_DM21_UW(i, j) (0x100 | ((i) << 4) | (j))
+#define GDFT_COL_DENS_X(s, i, j) (0x200 | ((s) << 8) | ((i) << 4) | (j))
+
+#define GDFT_MAX_COLS 16
 
 /* A functional with constant coefficients: Functional(coefficients=lambda: c,
  * energy_densities=stack of columns) (functional.py:128-141, popular_functionals.py:375-393).
@@ -425,8 +439,10 @@ int gdft_integrate_workspace_bytes(int64_t n_grid, size_t *bytes);
  * every GPU that loads the library until exit), so n_grid is limited to
  * 33,554,432 points; larger grids are rejected with GDFT_ERR_INVALID.  The
  * first call on a device looks up the array's device address (make it before
- * any stream capture).  Calls share the array: calls that overlap on the GPU
- * race.  Allocates nothing. */
+ * any stream capture) and keeps it for the life of the process: do not use
+ * this entry on a device after cudaDeviceReset, whose new context has the
+ * array at another address.  Calls share the array: calls that overlap on the
+ * GPU race.  Allocates nothing. */
 int gdft_integrate_noalloc(int64_t n_grid, int32_t n_cols, const double *h_coeffs, int32_t n_coeffs,
                            const double *d_dens, const double *d_weights, double clip, double *d_exc, void *stream);
 
@@ -449,6 +465,15 @@ int gdft_coulomb(int32_t n_ao, const double *d_eri, const double *d_rdm1, const 
  * the code in *status) if set, and clears it.  No counterpart in the
  * reference (its errors are Python exceptions). */
 int gdft_device_status(const gdft_molecule *mol, void *d_ws, size_t ws_bytes, int32_t *status, void *stream);
+
+/* Test of the failure path above: one kernel waits on an mbarrier that
+ * nothing arrives on, with `limit` (1..65536) polls instead of the pipeline
+ * kernels' limit, so the wait runs out; it records GDFT_WAIT_EXPIRY_PROBE in
+ * the workspace's error word and returns (no trap; nothing else is in flight,
+ * the context stays usable).  The next gdft_device_status reports it.  No
+ * counterpart in the reference. */
+#define GDFT_WAIT_EXPIRY_PROBE 99
+int gdft_selftest_wait_expiry(const gdft_molecule *mol, void *d_ws, size_t ws_bytes, int32_t limit, void *stream);
 
 /* Self-test of the tensor-core building blocks (TMA bulk copy, tcgen05.mma
  * kind::tf32, TMEM load) on one 128 x 128 x 32 product of small integers;

@@ -30,6 +30,7 @@ __all__ = [
     "densities_generic", "dm21_network", "FUNCTIONALS", "energy_densities", "xc_energy",
     "xc_energy_and_grads", "xc_hvp", "predict_fock", "t64", "features_numpy", "FZETA_PP0",
     "hf_energy_density", "hf_density_grad_2_fock", "b3lyp_predict_with_chi", "dm21_hf_fock_terms",
+    "DM21_GGA_COEFFS", "DM21_MGGA_COEFFS", "DENS_GGA_COEFFS", "DENS_MGGA_COEFFS",
 ]
 
 
@@ -227,6 +228,11 @@ def dm21_coefficient_inputs(rho, grad_rho, tau, clip_cte=CLIP):
 
 
 def _uw_ranges(functional_type):
+    """functional.py:575-585 (and :1089-1099).  A dict {'u_range', 'w_range'} takes the meaning the
+    docstring gives it (:548-556); the reference's code itself binds the ranges only for strings, so a
+    dict raises UnboundLocalError there (recorded by tests/golden/make_golden.py)."""
+    if isinstance(functional_type, dict):
+        return functional_type["u_range"], functional_type["w_range"]
     if functional_type in ("LDA", "DM21"):
         return range(0, 1), range(0, 1)
     if functional_type == "GGA":
@@ -358,6 +364,11 @@ def dm21_network(params: dict, x, n_layers: int | None = None, squash_offset=1e-
 # Functionals (popular_functionals.py:271-393) and the energy (functional.py:160-342)
 # --------------------------------------------------------------------------
 B3LYP_COEFFS = [1 - 0.2, 0.72, 1 - 0.81, 0.81, 0.2]  # popular_functionals.py:336-343
+# Test coefficients of the feature-power functionals (any constant rows serve; these mix signs).
+DM21_GGA_COEFFS = [0.9, 1.1]
+DM21_MGGA_COEFFS = [1.0, 0.5, -0.3, 0.2]
+DENS_GGA_COEFFS = [-0.7, -0.6, 0.3, 0.2, 0.5, 0.4, 0.3, 0.2]
+DENS_MGGA_COEFFS = [-0.7, -0.6, 0.3, 0.2, -0.2, -0.1, 0.1, 0.05, 0.5, 0.4, 0.3, 0.2, 0.1, 0.1, 0.1, 0.1]
 
 FUNCTIONALS = {
     # name: (energy-density columns, constant coefficient row or None for neural)
@@ -369,6 +380,12 @@ FUNCTIONALS = {
     "BLYP": (("lsda", "b88", "lyp"), [1.0]),
     "B3LYP": (("lsda", "b88", "vwn", "lyp", "hf"), B3LYP_COEFFS),
     "DM21": (("dm21_lda", "hf_w0", "hf_w1"), None),
+    # Constant-coefficient functionals on the feature powers of dm21_densities / densities
+    # (functional.py:534-626, 1048-1202), selected as energy_densities=partial(..., functional_type=...).
+    "DM21_GGA": ((("dm21", "GGA"),), DM21_GGA_COEFFS),
+    "DM21_MGGA": ((("dm21", "MGGA"),), DM21_MGGA_COEFFS),
+    "DENS_GGA": ((("dens", "GGA"),), DENS_GGA_COEFFS),
+    "DENS_MGGA": ((("dens", "MGGA"),), DENS_MGGA_COEFFS),
 }
 
 
@@ -407,6 +424,10 @@ def energy_densities(name, rho, grad_rho, lapl, tau, ehf=None, clip_cte=CLIP, cl
             out.append(ehf.detach()[0].sum(axis=0))
         elif c == "hf_w1":
             out.append(ehf.detach()[1].sum(axis=0))
+        elif isinstance(c, tuple) and c[0] == "dm21":
+            out.extend(dm21_densities(rho, grad_rho, tau, c[1], clip_cte).unbind(1))
+        elif isinstance(c, tuple) and c[0] == "dens":
+            out.extend(densities_generic(rho, grad_rho, tau, c[1], clip_cte).unbind(1))
         else:
             raise KeyError(c)
     stacked = torch.stack(out, axis=1)

@@ -12,6 +12,7 @@ reference computes from them is written to ``tests/golden/*.npz``.
 """
 from __future__ import annotations
 
+import functools
 import os
 import sys
 
@@ -25,6 +26,7 @@ sys.path.insert(0, HERE)
 import jaxshim  # noqa: E402
 from graddft_gb300 import synthetic  # noqa: E402
 from oracle.ao_numpy import eval_ao_planes  # noqa: E402
+from oracle import oracle as O  # noqa: E402  (test coefficient rows only)
 
 F64 = torch.float64
 
@@ -122,6 +124,16 @@ def main(root):
             res["dm21_densities_lda"] = fun.dm21_densities(mol, "LDA").numpy()
             res["dm21_densities_mgga"] = fun.dm21_densities(mol, "MGGA").numpy()
             res["densities_mgga"] = fun.densities(mol, "MGGA").numpy()
+            res["dm21_densities_gga"] = fun.dm21_densities(mol, "GGA").numpy()
+            res["densities_lda"] = fun.densities(mol, "LDA").numpy()
+            res["densities_gga"] = fun.densities(mol, "GGA").numpy()
+        # The documented dict functional_type (functional.py:548-556): the reference's code binds
+        # u_range / w_range only for a string (:575-585), so it raises for a dict.
+        try:
+            fun.dm21_densities(mol, {"u_range": range(0, 2), "w_range": range(0, 2)})
+            res["dict_type_raises"] = np.array(0)
+        except UnboundLocalError:
+            res["dict_type_raises"] = np.array(1)
         ehf = synthetic.make_ehf(wl.n_grid, 5, rho.numpy(), n_omega=2)
         res["ehf"] = ehf
         params = {"params": {}}
@@ -136,6 +148,15 @@ def main(root):
                                     nograd_densities=lambda m, *a, **k: torch.as_tensor(ehf[:1]),
                                     combine_densities=pop.b3lyp_combine),
         }
+        # Constant rows on the feature powers, selected as the reference's examples select them
+        # (energy_densities=partial(dm21_densities, functional_type=...)).
+        for name, fn_, ftype, coeffs in (("DM21_GGA", fun.dm21_densities, "GGA", O.DM21_GGA_COEFFS),
+                                         ("DM21_MGGA", fun.dm21_densities, "MGGA", O.DM21_MGGA_COEFFS),
+                                         ("DENS_GGA", fun.densities, "GGA", O.DENS_GGA_COEFFS),
+                                         ("DENS_MGGA", fun.densities, "MGGA", O.DENS_MGGA_COEFFS)):
+            functionals[name] = fun.Functional(
+                coefficients=(lambda c: (lambda self, *_: jnp.array([c])))(list(coeffs)),
+                energy_densities=functools.partial(fn_, functional_type=ftype))
         for name, f in functionals.items():
             e, v = _raw_xc(ref, f, params, mol)
             res[f"exc_{name}"] = e

@@ -27,7 +27,7 @@ def test_host_only_calls(built_lib):
     from graddft_gb300 import _lib
 
     lib = _lib.load(built_lib)
-    assert lib.gdft_abi_version() == 1
+    assert lib.gdft_abi_version() == _lib.ABI_VERSION == 2
     nbytes = ctypes.c_size_t()
     assert lib.gdft_molecule_bytes(1000, 40, _lib.GDFT_FP64, ctypes.byref(nbytes)) == 0
     # five FP64 planes of 1024 x 64 plus the weights

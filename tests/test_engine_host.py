@@ -42,11 +42,40 @@ def test_network_workspaces_cached_per_key():
         assert r._cached_ws("_nws", b, size_fn) is wb
     assert calls == [("a",), ("b",)]
     assert wa.numel() == 64 and int(wa.sum()) == 0 and wb.numel() == 32
-    extra = [_Net((f"n{i}",), 8) for i in range(engine.Resident._WS_KEEP)]
+    retired = []
+    r._retire_ws = retired.append
+    r._cached_ws("_nws", a, size_fn)  # a is now the most recently used: b goes first
+    extra = [_Net((f"n{i}",), 8) for i in range(engine.Resident._WS_KEEP - 1)]
     for n in extra:
         nets[id(n.desc)] = n
         r._cached_ws("_nws", n, size_fn)
-    assert len(r._nws) == engine.Resident._WS_KEEP and ("a",) not in r._nws
+    assert len(r._nws) == engine.Resident._WS_KEEP and ("b",) not in r._nws and ("a",) in r._nws
+    assert retired == [wb]
+
+
+def test_dropped_workspace_error_word_is_reported(monkeypatch):
+    """A bounded wait that expired in a network workspace the cache drops is still reported: the dropped
+    workspace's error word is read on the way out and the next status() raises."""
+    import pytest
+
+    from graddft_gb300 import _lib
+
+    bad = torch.zeros(16, dtype=torch.uint8)
+
+    class FakeLib:
+        def gdft_device_status(self, desc, ws, nbytes, status, stream):
+            code = 7 if ws.value == bad.data_ptr() else 0
+            status._obj.value = code
+            return _lib.GDFT_ERR_DEVICE if code else _lib.GDFT_OK
+
+    monkeypatch.setattr(_lib, "load", lambda *a, **k: FakeLib())
+    monkeypatch.setattr(engine, "_stream", lambda device: None)
+    r = _resident()
+    r.ws = torch.zeros(16, dtype=torch.uint8)
+    r._retire_ws(bad)
+    with pytest.raises(_lib.GdftError, match="code 7"):
+        r.status()
+    assert r.status() == 0  # reported once
 
 
 def test_dm21_hf_terms_sum_omegas_in_one_contraction(monkeypatch):
@@ -98,3 +127,59 @@ def test_dm21_hf_terms_sum_omegas_in_one_contraction(monkeypatch):
     custom = Custom(**{f.name: getattr(mol, f.name) for f in __import__("dataclasses").fields(mol)})
     assert torch.equal(neural.dm21_hfgrads_densities(Fn(), {}, custom, None, None, None),
                        torch.full((2, n, n), 2.0, dtype=torch.float64))
+
+
+def test_feature_power_columns_host_side():
+    """energy_densities=partial(dm21_densities | densities, functional_type=...) resolve to device columns
+    on the host: the reference's order (i over u_range, j over w_range; densities() spin-major exchange
+    terms, then the zero correlation features), dict ranges, and the reference's ValueError."""
+    import functools
+
+    import pytest
+
+    import graddft_gb300 as G
+    from graddft_gb300 import _lib
+    from graddft_gb300.functional import energy_density_columns as cols
+
+    assert cols(G.dm21_densities) == (_lib.COL_DM21_LDA,)
+    assert cols(functools.partial(G.dm21_densities, functional_type="GGA")) == (
+        _lib.COL_DM21_LDA, _lib.col_dm21_uw(1, 0))
+    assert cols(functools.partial(G.dm21_densities, functional_type="MGGA")) == (
+        _lib.COL_DM21_LDA, _lib.col_dm21_uw(0, 1), _lib.col_dm21_uw(1, 0), _lib.col_dm21_uw(1, 1))
+    dens = cols(functools.partial(G.densities, functional_type="MGGA"))
+    assert len(dens) == 16 and dens[8:] == (_lib.COL_ZERO,) * 8
+    assert dens[:4] == (_lib.col_dens_x(0, 0, 0), _lib.col_dens_x(1, 0, 0), _lib.col_dens_x(0, 0, 1),
+                        _lib.col_dens_x(1, 0, 1))
+    d = {"u_range": range(0, 2), "w_range": range(0, 2)}
+    assert cols(functools.partial(G.dm21_densities, functional_type=d)) == cols(
+        functools.partial(G.dm21_densities, functional_type="MGGA"))
+    with pytest.raises(ValueError):
+        cols(functools.partial(G.dm21_densities, functional_type="XGGA"))
+    with pytest.raises(NotImplementedError):  # 2 * 3 * 3 * 2 columns exceed the device functional
+        G.densities(None, {"u_range": range(0, 3), "w_range": range(0, 3)})
+    with pytest.raises(NotImplementedError):
+        cols(functools.partial(G.dm21_densities, functional_type="GGA", clip_cte=1e-20))
+    # the codes the C ABI documents (GDFT_COL_DM21_UW / GDFT_COL_DENS_X)
+    assert _lib.col_dm21_uw(1, 1) == 0x111 and _lib.col_dens_x(1, 1, 0) == 0x310
+
+
+def test_dlpack_producer_is_accepted_on_the_host():
+    """as_device_f64 takes an object that offers only __dlpack__ / __dlpack_device__ (a jax.Array's view
+    of the protocol), here wrapping a CPU tensor and a numpy array."""
+    import numpy as np
+
+    class DLPackOnly:
+        def __init__(self, a):
+            self._a = a
+
+        def __dlpack__(self, *args, **kwargs):
+            return self._a.__dlpack__(*args, **kwargs)
+
+        def __dlpack_device__(self):
+            return self._a.__dlpack_device__()
+
+    a = np.arange(12, dtype=np.float32).reshape(3, 4)
+    for src in (torch.as_tensor(a), a):
+        got = engine.as_device_f64(DLPackOnly(src), "cpu")
+        assert got.dtype == torch.float64 and got.is_contiguous()
+        assert torch.equal(got, torch.as_tensor(a, dtype=torch.float64))

@@ -95,3 +95,32 @@ def test_mixed_vs_fp64_gpu_large(eng):
     print("E", float(e64), "|dE|", de, "max|V|", float(v64.abs().max()), "max|dV|", dv)
     assert de <= ABS_DE and de <= TOL_E * abs(float(e64))
     assert dv <= ABS_DV and dv <= TOL_V * float(v64.abs().max())
+
+
+@pytest.mark.parametrize("case", ["compact", "tails"])
+@pytest.mark.parametrize("name,fname,ftype", [("DM21_GGA", "dm21_densities", "GGA"),
+                                              ("DM21_MGGA", "dm21_densities", "MGGA"),
+                                              ("DENS_MGGA", "densities", "MGGA")])
+def test_mixed_feature_functionals_vs_reference(eng, golden, case, name, fname, ftype):
+    """The feature-power functionals (tau enters V through the kinetic term) in the mixed form against
+    the reference's own E and V_xc, at the mixed form's tolerances."""
+    import functools
+
+    import graddft_gb300 as G
+
+    g = golden(case)
+    t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64, device="cuda")  # noqa: E731
+    mol = G.Molecule(grid=G.Grid(coords=None, weights=t(g["weights"])), atom_index=None, nuclear_pos=None,
+                     ao=t(g["ao"]), grad_ao=t(g["grad_ao"]), grad_n_ao={2: t(g["grad2_ao"])}, rdm1=t(g["rdm1"]),
+                     nuclear_repulsion=1.25, h1e=None, vj=None, mo_coeff=None, mo_occ=None, mo_energy=None,
+                     rep_tensor=None, precision="tf32x3")
+    row = torch.tensor([getattr(O, name + "_COEFFS")], dtype=torch.float64)
+    f = G.Functional(coefficients=lambda self, *_: row,
+                     energy_densities=functools.partial(getattr(G, fname), functional_type=ftype))
+    exc, vxc = f.xc_energy_and_grads({"params": {}}, mol)
+    assert mol.resident().status() == 0
+    e_ref = float(g[f"exc_{name}"])
+    de = abs(float(exc) - e_ref) / abs(e_ref)
+    dv = _rel(vxc, g[f"vxc_{name}"])
+    print(case, name, "dE", de, "dV", dv)
+    assert de <= TOL_E and dv <= TOL_V

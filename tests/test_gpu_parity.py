@@ -14,7 +14,14 @@ from graddft_gb300 import synthetic
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-11
-FUNCTIONALS = ["LSDA", "B88", "VWN", "LYP", "PW92", "BLYP", "B3LYP"]
+FUNCTIONALS = ["LSDA", "B88", "VWN", "LYP", "PW92", "BLYP", "B3LYP", "DM21_GGA", "DM21_MGGA", "DENS_GGA",
+               "DENS_MGGA"]
+# Feature-power functionals as the reference's examples build them:
+# energy_densities=partial(dm21_densities | densities, functional_type=...) with a constant row.
+FEATURE_FUNCTIONALS = {"DM21_GGA": ("dm21_densities", "GGA", O.DM21_GGA_COEFFS),
+                       "DM21_MGGA": ("dm21_densities", "MGGA", O.DM21_MGGA_COEFFS),
+                       "DENS_GGA": ("densities", "GGA", O.DENS_GGA_COEFFS),
+                       "DENS_MGGA": ("densities", "MGGA", O.DENS_MGGA_COEFFS)}
 
 
 def _close(a, b, rtol=RTOL, what=""):
@@ -50,6 +57,13 @@ def _molecule(G, g, precision="fp64", ehf=None):
 
 
 def _functional(G, name):
+    if name in FEATURE_FUNCTIONALS:
+        import functools
+
+        fname, ftype, coeffs = FEATURE_FUNCTIONALS[name]
+        row = torch.tensor([coeffs], dtype=torch.float64)
+        return G.Functional(coefficients=lambda self, *_: row,
+                            energy_densities=functools.partial(getattr(G, fname), functional_type=ftype))
     if name == "B3LYP":  # HF column from the supplied stop-gradient ehf (no chi tensor)
         return G.Functional(coefficients=G.popular_functionals.b3lyp_coefficients,
                             energy_densities=G.b3lyp_exhf_densities,
@@ -90,6 +104,33 @@ def test_energy_density_columns(G, golden, case):
     _close(G.pw92_densities(mol), g["ed_pw92"], what="pw92")
     _close(G.b3lyp_exhf_densities(mol), g["ed_b3lyp_exhf"], what="b3lyp_exhf")
     _close(G.dm21_densities(mol), g["dm21_densities_lda"], what="dm21 lda")
+    for ftype in ("LDA", "GGA", "MGGA"):
+        if ftype != "LDA":
+            _close(G.dm21_densities(mol, ftype), g[f"dm21_densities_{ftype.lower()}"], what=f"dm21 {ftype}")
+        _close(G.densities(mol, ftype), g[f"densities_{ftype.lower()}"], what=f"densities {ftype}")
+
+
+@pytest.mark.parametrize("case", ["compact", "tails"])
+def test_feature_type_dict(G, golden, case):
+    """The documented dict functional_type (the reference's code raises for it): the MGGA ranges give
+    the MGGA features; other ranges agree with the oracle; the E/V path takes them through a partial."""
+    import functools
+
+    g = golden(case)
+    mol = _molecule(G, g)
+    d = {"u_range": range(0, 2), "w_range": range(0, 2)}
+    _close(G.dm21_densities(mol, d), g["dm21_densities_mgga"], what="dm21 dict")
+    _close(G.densities(mol, d), g["densities_mgga"], what="densities dict")
+    d3 = {"u_range": range(0, 3), "w_range": range(1, 3)}
+    rho, grad_rho, lapl, tau = (O.t64(x) for x in O.features_numpy(g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"]))
+    _close(G.dm21_densities(mol, d3), O.dm21_densities(rho, grad_rho, tau, d3).numpy(), what="dm21 dict ranges")
+    f = G.Functional(coefficients=lambda self, *_: torch.tensor([[1.0, 0.5, -0.3, 0.2]], dtype=torch.float64),
+                     energy_densities=functools.partial(G.dm21_densities, functional_type=d))
+    exc, vxc = f.xc_energy_and_grads({"params": {}}, mol)
+    assert abs(float(exc) - float(g["exc_DM21_MGGA"])) <= RTOL * abs(float(g["exc_DM21_MGGA"]))
+    _close(vxc, g["vxc_DM21_MGGA"], what="V dict")
+    with pytest.raises(ValueError):
+        G.dm21_densities(mol, "XGGA")
 
 
 @pytest.mark.parametrize("name", ["LSDA", "B88", "BLYP"])

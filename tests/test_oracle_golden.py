@@ -12,7 +12,8 @@ import oracle as O
 from graddft_gb300 import synthetic
 
 RTOL = 1e-12
-FUNCTIONALS = ["LSDA", "B88", "VWN", "LYP", "PW92", "BLYP", "B3LYP"]
+FUNCTIONALS = ["LSDA", "B88", "VWN", "LYP", "PW92", "BLYP", "B3LYP", "DM21_GGA", "DM21_MGGA", "DENS_GGA",
+               "DENS_MGGA"]
 
 
 def _close(a, b, rtol=RTOL):
@@ -59,6 +60,24 @@ def test_energy_density_columns(golden, case):
     _close(O.dm21_densities(rho, grad_rho, tau, "LDA").numpy(), g["dm21_densities_lda"])
     _close(O.dm21_densities(rho, grad_rho, tau, "MGGA").numpy(), g["dm21_densities_mgga"])
     _close(O.densities_generic(rho, grad_rho, tau, "MGGA").numpy(), g["densities_mgga"])
+    _close(O.dm21_densities(rho, grad_rho, tau, "GGA").numpy(), g["dm21_densities_gga"])
+    _close(O.densities_generic(rho, grad_rho, tau, "LDA").numpy(), g["densities_lda"])
+    _close(O.densities_generic(rho, grad_rho, tau, "GGA").numpy(), g["densities_gga"])
+
+
+@pytest.mark.parametrize("case", ["compact", "tails"])
+def test_feature_type_dict(golden, case):
+    """A dict functional_type: the reference raises (it binds the ranges for strings only), the oracle
+    follows the documented meaning, which for the MGGA ranges is the MGGA feature set; the correlation
+    features of densities() are zero for every input (round to a multiple of 1e30, then > clip)."""
+    g = golden(case)
+    assert int(g["dict_type_raises"]) == 1
+    rho, grad_rho, lapl, tau = (O.t64(x) for x in O.features_numpy(g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"]))
+    d = {"u_range": range(0, 2), "w_range": range(0, 2)}
+    _close(O.dm21_densities(rho, grad_rho, tau, d).numpy(), g["dm21_densities_mgga"])
+    _close(O.densities_generic(rho, grad_rho, tau, d).numpy(), g["densities_mgga"])
+    for key, n in (("densities_lda", 1), ("densities_gga", 2), ("densities_mgga", 4)):
+        assert np.all(g[key][:, 2 * n:] == 0.0)
 
 
 @pytest.mark.parametrize("name", ["LSDA", "B88", "BLYP"])
