@@ -72,15 +72,16 @@ MolLayout mol_layout(int64_t n_grid, int n_ao, int precision) {
   if (precision == GDFT_FP64) {
     off = align256(off + (size_t)kPlanes * L.plane_elems() * sizeof(double));
   } else {
-    // Point-major hi/lo of the five planes, AO-major block-scaled hi/lo/lo2 of
-    // four planes, and AO-major FP32 of the five planes.
+    // Point-major hi/lo of the five planes, AO-major block-scaled hi/lo/lo2
+    // of four planes, and AO-major FP32 pairs (hi = fp32(x), lo = fp32(x - hi))
+    // of the five planes.
     const size_t plane = (size_t)L.np * L.ldk * sizeof(float);
     L.off_pm = off;
     off = align256(off + kPlanes * 2 * plane);
     L.off_av = off;
     off = align256(off + 4 * 3 * plane);
     L.off_af = off;
-    off = align256(off + kPlanes * plane);
+    off = align256(off + kPlanes * 2 * plane);
   }
   L.bytes = off;
   return L;

@@ -11,8 +11,9 @@
 //     block-scaled three-slice sets (umma::store_row3: hi quantised per AO and
 //     point chunk, hi + lo + lo2 ~= x to about 2^-33 of the chunk's largest value)
 //     (A operand of the V_xc contraction, contracted over points)
-//   AO-major FP32 [AO tile (128)][plane][point chunk (32)] : the same blocks as single
-//     FP32 values (inputs of the B operand that is built per call)
+//   AO-major FP32 pairs [AO tile (128)][plane][point chunk (32)][hi|lo] : the same
+//     blocks as hi = fp32(x), lo = fp32(x - hi) (together about 2^-48 of x; the
+//     inputs of the B operand that is built per call in double-float arithmetic)
 // The density matrix is packed per call as the B operand of the density
 // contraction: [spin][column tile (128)][k chunk (32)][hi|lo], element (c, k) = D[k][c].
 #include "common.cuh"
@@ -30,7 +31,7 @@ __device__ __forceinline__ size_t av_set(int atile, int plane, int64_t pc, int64
   return (size_t)(atile * 4 + plane) * npc + pc;  // in units of three-block sets (48 KB)
 }
 __device__ __forceinline__ size_t af_block(int atile, int plane, int64_t pc, int64_t npc) {
-  return (size_t)(atile * kPlanes + plane) * npc + pc;
+  return ((size_t)(atile * kPlanes + plane) * npc + pc) * 2;  // in units of 16 KB blocks (hi; lo = +1)
 }
 
 __device__ __forceinline__ void store_split(float *base, size_t blk, uint32_t off, double v) {
@@ -45,7 +46,7 @@ __device__ __forceinline__ void store_split(float *base, size_t blk, uint32_t of
 enum PackSrc { kFromTables = 0, kFromSynthetic = 1 };
 
 // Scatter the five plane values of (point p, AO a) into the point-major pairs,
-// the parked FP64 values of the AO-major sets and the AO-major FP32 blocks.
+// the parked FP64 values of the AO-major sets and the AO-major FP32 pairs.
 __device__ __forceinline__ void pack_store(float *__restrict__ pm, float *__restrict__ av, float *__restrict__ af,
                                            int64_t np, int ldk, int64_t p, int a, const double v[kPlanes]) {
   const int nkc = ldk / 32;
@@ -57,8 +58,11 @@ __device__ __forceinline__ void pack_store(float *__restrict__ pm, float *__rest
     if (t < 4)
       ((double *)(av + av_set(a / 128, t, p / 32, npc) * 3 * (umma::kBlockBytes / 4)))[(p % 32) * 128 + a % 128] =
           v[t];
-    af[af_block(a / 128, t, p / 32, npc) * (umma::kBlockBytes / 4) + umma::kblock_off(a % 128, (int)(p % 32)) / 4] =
-        (float)v[t];
+    float *afb = af + af_block(a / 128, t, p / 32, npc) * (umma::kBlockBytes / 4) +
+                 umma::kblock_off(a % 128, (int)(p % 32)) / 4;
+    const float hi = (float)v[t];
+    afb[0] = hi;
+    afb[umma::kBlockBytes / 4] = (float)(v[t] - (double)hi);
   }
 }
 
