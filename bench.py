@@ -151,12 +151,15 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     n_sample = args.cpu_sample
-    value, _, _ = cpu_baseline(n_sample, threads, args.warmup, args.steps)
+    value, _, (_, _, e_o, v_o) = cpu_baseline(n_sample, threads, args.warmup, args.steps, args.n_grid, args.n_ao)
+    if args.dump:  # the sample's oracle E_xc and V_xc, for the GPU arm's accuracy check
+        np.savez(args.dump, exc=np.array(e_o), vxc=v_o)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n_sample / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_ao": N_AO, "n_grid": N_GRID, "functional": "B88+LYP"},
+        "config": {"workload": _workload(args.n_grid, args.n_ao), "n_ao": args.n_ao, "n_grid": args.n_grid,
+                   "functional": "B88+LYP"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{n_sample} of the 2^20 grid points (same basis, D, weights), "
                                    "FP64 torch-CPU restatement with autograd for V_xc; median of "
@@ -853,6 +856,7 @@ def main():
                     help="grid points of the FP64-form measurement (its rate is per point)")
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--seeds", type=int, default=3, help="seeded workloads of the mixed-vs-FP64 accuracy check")
+    ap.add_argument("--dump", default=None, help="--impl reference: write the sample's oracle E_xc, V_xc here")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
     ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch", "hf", "ao", "chi", "solid"],
@@ -1087,12 +1091,23 @@ def main():
         "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(), **other,
     }
     if rank == 0 and not args.no_cpu:
-        v, dt, (wl_c, idx, e_o, v_o) = cpu_baseline(args.cpu_sample, os.cpu_count() or 1, 2, 5, args.n_grid,
-                                                   args.n_ao)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{args.cpu_sample} grid points of the same workload (median "
-                                          f"{dt:.2f} s of 5 calls after 2 warm-ups), FP64 torch-CPU restatement "
-                                          "with autograd"}
+        # The CPU baseline is the reference arm itself, run in a fresh interpreter (no CUDA context, no
+        # GPU-side threads), so the two report one measurement protocol: median of 5 calls after 2 warm-ups.
+        import tempfile
+
+        dump = os.path.join(tempfile.mkdtemp(), "oracle_sample.npz")
+        env = {k: v for k, v in os.environ.items() if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE")}
+        ref = subprocess.run([sys.executable, os.path.abspath(__file__), "--impl", "reference", "--steps", "5",
+                              "--warmup", "2", "--cpu-sample", str(args.cpu_sample), "--n-grid", str(args.n_grid),
+                              "--n-ao", str(args.n_ao), "--dump", dump], capture_output=True, text=True, env=env,
+                             check=True)
+        ref_line = json.loads(ref.stdout.strip().splitlines()[-1])
+        line["cpu_baseline"] = {**ref_line["cpu_baseline"], "sample": ref_line["cpu_baseline"]["sample"] +
+                                " (the --impl reference arm, run as a child process)"}
+        got = np.load(dump)
+        e_o, v_o = float(got["exc"]), got["vxc"]
+        wl_c = synthetic.make_workload(args.n_grid, args.n_ao, N_OCC, SEED)
+        idx = slice(0, args.cpu_sample)
         # Both forms against the oracle on that sample (the same points, basis and D at the full n_ao).
         vs_oracle = {"points": args.cpu_sample}
         for prec in ("fp64", form) if form != "fp64" else ("fp64",):
