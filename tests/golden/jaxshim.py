@@ -115,9 +115,16 @@ def _mk_jnp():
         setattr(m, name, (lambda f: (lambda x: f(_t(x))))(fn))
 
     def clip(a, a_min=None, a_max=None, min=None, max=None):  # noqa: A002
+        # jnp.clip is maximum(a_min, x) then minimum(a_max, .): at an exact tie the gradient is split in
+        # half, as torch.maximum / torch.minimum split it (torch.clamp would pass all of it).
         lo = a_min if a_min is not None else min
         hi = a_max if a_max is not None else max
-        return torch.clamp(_t(a), min=lo, max=hi)
+        x = _t(a)
+        if lo is not None:
+            x = torch.maximum(x, torch.as_tensor(lo, dtype=x.dtype))
+        if hi is not None:
+            x = torch.minimum(x, torch.as_tensor(hi, dtype=x.dtype))
+        return x
 
     m.clip = clip
 

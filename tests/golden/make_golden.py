@@ -250,6 +250,27 @@ def main(root):
     path = os.path.join(HERE, "ref_hf.npz")
     np.savez_compressed(path, **res)
     out_files.append(path)
+    # Config 1's stand-in (its PySCF H2O / def2-TZVP inputs are not available): unrestricted B3LYP evaluated
+    # non-self-consistently on a fixed D at n_ao = 43 (popular_functionals.py:384-391), its HF column from a
+    # chi tensor: E_xc and V_xc of xc_energy_and_grads (train.py:86-121) and the explicit HF Fock term
+    # (popular_functionals.py:352-372).  The inputs are regenerated from seeds (oracle/cases.py), so only
+    # the reference's outputs are stored.
+    from oracle.cases import b3lyp43_inputs
+
+    wl, ao, g1, g2, chi, omegas = b3lyp43_inputs()
+    n = wl.n_ao
+    mol = _molecule(ref, wl, ao, g1, g2, np.zeros((n, n)), np.zeros((1, 1, 1, 1)))
+    mol = mol.replace(chi=torch.as_tensor(chi), omegas=torch.as_tensor(omegas))
+    params = {"params": {}}
+    e, v = _raw_xc(ref, pop.B3LYP, params, mol)
+    with torch.no_grad():
+        ehf0 = mol.HF_energy_density([0.0])
+    vexpl = pop.b3lyp_hfgrads(pop.B3LYP, params, mol, ehf0.detach(), None, pop.b3lyp_exhf_densities(mol))
+    res = dict(exc=e, vxc=v, ehf=ehf0.numpy(), b3lyp_hfgrads=vexpl.detach().numpy(), n_ao=np.array(n),
+               n_grid=np.array(wl.n_grid))
+    path = os.path.join(HERE, "ref_b3lyp43.npz")
+    np.savez_compressed(path, **res)
+    out_files.append(path)
     # diff_scf_loop (evaluate.py:917-1038) with JittableDiis (:1041-1210): the
     # final energy, density matrix and dE/dtheta through all iterations, DM21
     # with stop-gradient HF inputs, 12 cycles (past the 10-entry DIIS history).

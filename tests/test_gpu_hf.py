@@ -180,3 +180,27 @@ def test_dm21_hf_terms_and_predict_mixed_network(G, golden, mol_form):
     E, F = G.energy_predictor(dm21)(params, mol)
     assert abs(float(E) - float(g["predict_E_DM21"])) <= 1e-6 * abs(float(g["predict_E_DM21"]))
     _close(F, g["predict_F_DM21"], rtol=2e-5, what="F (mixed network)")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32x3"])
+def test_b3lyp_n43_config1_stand_in(G, golden, precision):
+    """Config 1's stand-in (n_ao 43, unrestricted B3LYP on a fixed D, HF column from chi): E_xc, V_xc and
+    the explicit HF Fock term against the reference's own outputs (inputs regenerated from seeds)."""
+    from oracle.cases import b3lyp43_inputs
+
+    g = golden("b3lyp43")
+    wl, ao, g1, g2, chi, omegas = b3lyp43_inputs()
+    mol = G.Molecule(grid=G.Grid(coords=None, weights=_t(wl.weights)), atom_index=None, nuclear_pos=None,
+                     ao=_t(ao), grad_ao=_t(g1), grad_n_ao={2: _t(g2)}, rdm1=_t(wl.rdm1), nuclear_repulsion=0.0,
+                     h1e=None, vj=None, mo_coeff=None, mo_occ=None, mo_energy=None, rep_tensor=None,
+                     omegas=[float(o) for o in omegas], chi=_t(chi), precision=precision)
+    exc, vxc = G.B3LYP.xc_energy_and_grads({"params": {}}, mol)
+    ehf0 = mol.HF_energy_density([0.0])
+    vhf = G.popular_functionals.b3lyp_hfgrads(G.B3LYP, {"params": {}}, mol, ehf0, None, None)
+    # Mixed form: E_xc and V_xc at the mixed tolerances; the exchange terms' three-slice GEMMs at 2e-8.
+    rtol_e, rtol_v, rtol_hf = (RTOL, RTOL, RTOL) if precision == "fp64" else (5e-7, 2e-6, 2e-8)
+    ref = float(g["exc"])
+    assert abs(float(exc) - ref) <= rtol_e * abs(ref), (float(exc), ref)
+    _close(vxc, g["vxc"], rtol=rtol_v, what="V_xc")
+    _close(ehf0, g["ehf"], rtol=rtol_hf, what="ehf")
+    _close(vhf, g["b3lyp_hfgrads"], rtol=max(rtol_hf, 2e-6 if precision != "fp64" else RTOL), what="HF Fock term")

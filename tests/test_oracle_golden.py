@@ -184,3 +184,19 @@ def test_dm21_hf_terms_vs_reference(golden):
     fd, fc = O.dm21_hf_fock_terms(g["rdm1"], g["ao"], g["grad_ao"], g["grad2_ao"], g["weights"], params, g["chi"])
     _close(fd.numpy(), g["dm21_hfgrads_densities"])
     _close(fc.numpy(), g["dm21_hfgrads_cinputs"])
+
+
+def test_b3lyp_n43_config1_stand_in(golden):
+    """The oracle on config 1's stand-in (n_ao 43 B3LYP with the HF column from chi) against the reference's
+    outputs; the inputs are regenerated from seeds."""
+    from oracle.cases import b3lyp43_inputs
+
+    g = golden("b3lyp43")
+    wl, ao, g1, g2, chi, _ = b3lyp43_inputs()
+    ehf0 = O.hf_energy_density(wl.rdm1, ao, chi)
+    _close(ehf0.numpy(), g["ehf"])
+    e, v = O.xc_energy_and_grads("B3LYP", wl.rdm1, ao, g1, g2, wl.weights, ehf=ehf0)
+    assert abs(e - float(g["exc"])) <= RTOL * abs(float(g["exc"]))
+    _close(v, g["vxc"])
+    f = O.hf_density_grad_2_fock("B3LYP", wl.rdm1, ao, g1, g2, wl.weights, chi, ehf0).sum(0)
+    _close(f.numpy(), g["b3lyp_hfgrads"])
