@@ -56,7 +56,8 @@ EXPORTS = (
     "gdft_tc_gemm3_probe", "gdft_neural_batch_workspace_bytes", "gdft_neural_batch_xc",
     "gdft_xc_energy_grads_hf", "gdft_hf_workspace_bytes", "gdft_hf_energy_density", "gdft_hf_fock",
     "gdft_fock_add_hf", "gdft_neural_xc_hf_grads", "gdft_hf_workspace_bytes_form", "gdft_hf_energy_density_form",
-    "gdft_hf_fock_form", "gdft_hf_device_status", "gdft_selftest_wait_expiry",
+    "gdft_hf_fock_form", "gdft_hf_device_status", "gdft_selftest_wait_expiry", "gdft_chunked_workspace_bytes",
+    "gdft_xc_energy_and_grads_chunked", "gdft_neural_xc_energy_and_grads_chunked", "gdft_chunked_status",
 )
 STAGE_AO, STAGE_DENSITY, STAGE_POINT, STAGE_VXC, STAGE_REDUCE, STAGE_MLP = range(6)
 
@@ -165,6 +166,12 @@ _SIGS = {
     "gdft_coulomb": ([I32, P, P, P, D, P, P, P], ctypes.c_int),
     "gdft_device_status": ([PMOL, P, SZ, ctypes.POINTER(I32), P], ctypes.c_int),
     "gdft_selftest_wait_expiry": ([PMOL, P, SZ, I32, P], ctypes.c_int),
+    "gdft_chunked_workspace_bytes": ([I32, I64, I32, PNET, ctypes.POINTER(SZ)], ctypes.c_int),
+    "gdft_xc_energy_and_grads_chunked": ([PBAS, P, I32, P, P, I64, I64, I32, P, PFN, P, I32, P, P, P, SZ, P],
+                                         ctypes.c_int),
+    "gdft_neural_xc_energy_and_grads_chunked": ([PBAS, P, I32, P, P, I64, I64, I32, P, PNET, P, P, P, P, P, P, SZ,
+                                                 P], ctypes.c_int),
+    "gdft_chunked_status": ([P, SZ, ctypes.POINTER(I32), P], ctypes.c_int),
     "gdft_selftest_umma": ([ctypes.POINTER(D)], ctypes.c_int),
     "gdft_umma_probe": ([P, P, P], ctypes.c_int),
     "gdft_network_param_count": ([PNET, ctypes.POINTER(SZ)], ctypes.c_int),

@@ -325,7 +325,7 @@ def eval_ao(basis: ShellBasis, coords, deriv: int = 1, device=None):
 
 
 def molecule_from_basis(basis: ShellBasis, coords, weights, rdm1, precision: str = "fp64", device=None,
-                        with_tables: bool = False, **fields):
+                        with_tables: bool = False, recompute_chunk: Optional[int] = None, **fields):
     """A Molecule whose AO tables are evaluated on the device from ``basis``.
 
     The stand-in for building ``ao``, ``grad_ao`` and ``grad_n_ao`` with PySCF
@@ -333,6 +333,8 @@ def molecule_from_basis(basis: ShellBasis, coords, weights, rdm1, precision: str
     tables the XC path reads are filled straight from the shells.  With
     ``with_tables`` the reference-layout arrays are evaluated as well (the HF
     exact-exchange terms take ``ao`` from there); otherwise those fields are None.
+    With ``recompute_chunk`` the tables are never held for the whole grid: each
+    evaluation recomputes them chunk by chunk (``engine.ChunkedResident``).
     """
     from . import engine
     from .molecule import Grid, Molecule
@@ -340,7 +342,10 @@ def molecule_from_basis(basis: ShellBasis, coords, weights, rdm1, precision: str
     dev = engine.require_cuda(device)
     coords = engine.as_device_f64(coords, dev)
     weights = engine.as_device_f64(weights, dev)
-    r = engine.Resident.from_shells(basis, coords, weights, precision, dev)
+    if recompute_chunk is not None:
+        r = engine.ChunkedResident(basis, coords, weights, precision, int(recompute_chunk), dev)
+    else:
+        r = engine.Resident.from_shells(basis, coords, weights, precision, dev)
     ao = grad_ao = grad_n_ao = None
     if with_tables:
         ao, grad_ao, g2 = eval_ao(basis, coords, 2, dev)

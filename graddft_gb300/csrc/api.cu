@@ -1293,3 +1293,256 @@ int gdft_coulomb(int32_t n_ao, const double *d_eri, const double *d_rdm1, const 
 }
 
 }  // extern "C"
+
+// ---- grid-chunked evaluation: phi recomputed per chunk ----------------------
+// The AO tables of one chunk of grid points are evaluated from the basis into a
+// chunk buffer, read by that chunk's density, point and V_xc stages, and
+// overwritten by the next chunk: phi is recomputed where it is needed instead
+// of being held for the whole grid.  E_xc, V_xc (and dE/dtheta) accumulate over
+// the chunks on the device.  Workspace: [persistent error word (256 B)][chunk
+// molecule buffer][chunk workspace][ehf slice][chunk E][chunk V][chunk dtheta].
+constexpr int kChunkMaxOmega = 4;
+
+struct ChunkWs {
+  size_t off_mol, mol_bytes, off_ws, ws_bytes, off_ehf, off_e, off_v, off_dp, bytes;
+};
+
+static ChunkWs chunk_ws(int32_t n_ao, int64_t chunk, int32_t precision, const gdft_network *net) {
+  ChunkWs C;
+  size_t off = 256;  // the persistent error word
+  const MolLayout L = mol_layout(chunk, n_ao, precision);
+  C.off_mol = off;
+  C.mol_bytes = L.bytes;
+  off += align256(L.bytes);
+  gdft_molecule m{chunk, L.np, n_ao, L.ld, precision, 0, nullptr, L.bytes};
+  C.ws_bytes = net ? neural_ws_bytes(&m, net) : ws_layout(&m).bytes;
+  C.off_ws = off;
+  off += align256(C.ws_bytes);
+  C.off_ehf = off;
+  off += align256((size_t)kChunkMaxOmega * 2 * chunk * sizeof(double));
+  C.off_e = off;
+  off += 256;
+  C.off_v = off;
+  off += align256((size_t)2 * n_ao * n_ao * sizeof(double));
+  C.off_dp = off;
+  off += net ? align256(mlp_param_count(net_shape(net)) * sizeof(double)) : 0;
+  C.bytes = off;
+  return C;
+}
+
+static int check_chunked(const gdft_basis *shells, const double *rows, int32_t n_ao, const double *coords,
+                         const double *weights, int64_t n_grid, int64_t chunk, int32_t precision, void *ws,
+                         const char *who, ShellView *B) {
+  if ((shells == nullptr) == (rows == nullptr)) {
+    set_error("%s: give exactly one of a contracted basis and synthetic basis rows", who);
+    return GDFT_ERR_INVALID;
+  }
+  int rc;
+  if (shells != nullptr) {
+    if ((rc = check_basis(shells, who, B))) return rc;
+    if (shells->n_ao != n_ao) {
+      set_error("%s: the basis has %d AOs, n_ao is %d", who, shells->n_ao, n_ao);
+      return GDFT_ERR_INVALID;
+    }
+  }
+  if (n_ao <= 0 || n_grid <= 0 || chunk < 128 || chunk % 256 != 0 || coords == nullptr || weights == nullptr ||
+      !(precision == GDFT_FP64 || precision == GDFT_TF32X3)) {
+    set_error("%s: n_ao %d, n_grid %lld, chunk %lld (a multiple of 256), precision %d", who, n_ao,
+              (long long)n_grid, (long long)chunk, precision);
+    return GDFT_ERR_INVALID;
+  }
+  if ((rc = check_aligned8(coords, "coords")) || (rc = check_aligned8(weights, "weights"))) return rc;
+  if (((uintptr_t)ws & 255u) != 0) {
+    set_error("%s: workspace must be 256-byte aligned", who);
+    return GDFT_ERR_ALIGNMENT;
+  }
+  return GDFT_OK;
+}
+
+// AO tables of points [off, off + len) into the chunk molecule.
+static int chunk_tables(const gdft_molecule *m, const ShellView *B, const double *rows, const double *coords,
+                        const double *weights, int64_t off, cudaStream_t st) {
+  const MolLayout L = mol_layout(m->n_grid, m->n_ao, m->precision);
+  char *buf = (char *)m->buffer;
+  double *w = (double *)(buf + L.off_w);
+  const double *c = coords + 3 * off, *wt = weights + off;
+  StageTimer tm(GDFT_STAGE_AO, st);
+  if (m->precision == GDFT_TF32X3)
+    return check_cuda(launch_pack_tables(nullptr, nullptr, nullptr, rows, c, wt, m->n_grid, m->n_ao, L.np, L.ldk,
+                                         (float *)(buf + L.off_pm), (float *)(buf + L.off_av),
+                                         (float *)(buf + L.off_af), w, st, B),
+                      "chunk tables");
+  if (B != nullptr)
+    return check_cuda(launch_eval_shell_tables(*B, c, wt, m->n_grid, L.np, L.ld, (double *)(buf + L.off_tab), w, st),
+                      "chunk tables");
+  return check_cuda(launch_eval_basis(rows, c, wt, m->n_grid, m->n_ao, L.np, L.ld, (double *)(buf + L.off_tab), w,
+                                      st),
+                    "chunk tables");
+}
+
+// One chunk's stages; `net` selects the network pass, `fn` the constant-coefficient one.
+static int chunk_pass(const gdft_molecule *m, char *ws, const ChunkWs &C, char *base, const double *rdm1,
+                      const gdft_functional *fn, const gdft_network *net, const double *params, const double *ehf,
+                      int n_omega, int64_t n_grid, int64_t off, bool first, double *exc, double *vxc,
+                      double *dparams, cudaStream_t st) {
+  const WsLayout W = ws_layout(m);
+  int rc;
+  // A shorter (last) chunk's layout puts its error word where the full chunks kept other data.
+  if ((rc = check_cuda(cudaMemsetAsync(ws + W.off_err, 0, sizeof(int), st), "chunk status clear"))) return rc;
+  if ((rc = run_density(m, rdm1, ws, st))) return rc;
+  const double *ehf_c = nullptr;
+  if (ehf != nullptr) {  // this chunk's columns of ehf (omega, spin, grid)
+    double *dst = (double *)(base + C.off_ehf);
+    if ((rc = check_cuda(cudaMemcpy2DAsync(dst, (size_t)m->n_grid * 8, ehf + off, (size_t)n_grid * 8,
+                                           (size_t)m->n_grid * 8, (size_t)2 * n_omega, cudaMemcpyDeviceToDevice, st),
+                         "chunk ehf")))
+      return rc;
+    ehf_c = dst;
+  }
+  double *feat = (double *)(ws + W.off_feat);
+  double *coef = vxc ? (double *)(ws + W.off_coef) : nullptr;
+  double *e_c = (double *)(base + C.off_e);
+  double *dp_c = dparams ? (double *)(base + C.off_dp) : nullptr;
+  if (net != nullptr) {
+    StageTimer tm(GDFT_STAGE_MLP, st);
+    if (net->precision == GDFT_TF32X3)
+      rc = mlp_run_tc(net_shape(net), params, dp_c, feat, ehf_c, mol_w(m), m->n_grid, m->n_grid_pad, net->clip,
+                      ws + W.bytes, e_c, coef, (int *)(ws + W.off_err), st);
+    else
+      rc = mlp_run_f64(net_shape(net), params, dp_c, feat, ehf_c, mol_w(m), m->n_grid, m->n_grid_pad, net->clip,
+                       (double *)(ws + W.bytes), e_c, coef, st);
+    if (rc) return rc;
+  } else {
+    double *epart = (double *)(ws + W.off_epart);
+    {
+      StageTimer tm(GDFT_STAGE_POINT, st);
+      if ((rc = check_cuda(launch_xc_point(feat, mol_w(m), m->n_grid, m->n_grid_pad, *fn, ehf_c, n_omega, coef,
+                                           epart, nullptr, st),
+                           "xc_point")))
+        return rc;
+    }
+    StageTimer tm(GDFT_STAGE_REDUCE, st);
+    if ((rc = check_cuda(launch_energy_reduce(epart, W.n_eblocks, e_c, st), "energy_reduce"))) return rc;
+  }
+  {
+    StageTimer tm(GDFT_STAGE_REDUCE, st);
+    if ((rc = check_cuda(launch_feat_add(e_c, exc, 1, first, st), "chunk E"))) return rc;
+    if (dparams &&
+        (rc = check_cuda(launch_feat_add(dp_c, dparams, mlp_param_count(net_shape(net)), first, st), "chunk dtheta")))
+      return rc;
+  }
+  if (vxc != nullptr) {
+    double *v_c = (double *)(base + C.off_v);
+    if ((rc = run_vxc(m, coef, v_c, ws, st))) return rc;
+    StageTimer tm(GDFT_STAGE_REDUCE, st);
+    if ((rc = check_cuda(launch_feat_add(v_c, vxc, (size_t)2 * m->n_ao * m->n_ao, first, st), "chunk V")))
+      return rc;
+  }
+  return check_cuda(launch_err_fold((int *)base, (int *)(ws + W.off_err), st), "chunk status");
+}
+
+static int run_chunked(const char *who, const gdft_basis *shells, const double *rows, int32_t n_ao,
+                       const double *coords, const double *weights, int64_t n_grid, int64_t chunk, int32_t precision,
+                       const double *rdm1, const gdft_functional *fn, const gdft_network *net, const double *params,
+                       const double *ehf, int32_t n_omega, double *exc, double *vxc, double *dparams, void *d_ws,
+                       size_t ws_bytes, void *stream) {
+  ShellView B;
+  int rc = check_chunked(shells, rows, n_ao, coords, weights, n_grid, chunk, precision, d_ws, who, &B);
+  if (rc) return rc;
+  const ChunkWs C = chunk_ws(n_ao, chunk, precision, net);
+  if (d_ws == nullptr || ws_bytes < C.bytes) {
+    set_error("%s: workspace of %zu bytes is smaller than the %zu bytes required", who, ws_bytes, C.bytes);
+    return GDFT_ERR_WORKSPACE;
+  }
+  if (rdm1 == nullptr || exc == nullptr) {
+    set_error("%s: rdm1 and exc are required", who);
+    return GDFT_ERR_INVALID;
+  }
+  if (ehf != nullptr && (n_omega < 1 || n_omega > kChunkMaxOmega)) {
+    set_error("%s: n_omega %d outside 1..%d", who, n_omega, kChunkMaxOmega);
+    return GDFT_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *base = (char *)d_ws;
+  for (int64_t off = 0; off < n_grid; off += chunk) {
+    const int64_t len = n_grid - off < chunk ? n_grid - off : chunk;
+    gdft_molecule m;
+    if ((rc = gdft_molecule_init(&m, len, n_ao, precision, base + C.off_mol, C.mol_bytes))) return rc;
+    if ((rc = chunk_tables(&m, shells ? &B : nullptr, rows, coords, weights, off, st))) return rc;
+    if ((rc = chunk_pass(&m, base + C.off_ws, C, base, rdm1, fn, net, params, ehf, n_omega, n_grid, off, off == 0,
+                         exc, vxc, dparams, st)))
+      return rc;
+  }
+  return GDFT_OK;
+}
+
+extern "C" {
+
+int gdft_chunked_workspace_bytes(int32_t n_ao, int64_t chunk, int32_t precision, const gdft_network *net,
+                                 size_t *bytes) {
+  if (bytes == nullptr || n_ao <= 0 || chunk < 128 || chunk % 256 != 0 ||
+      !(precision == GDFT_FP64 || precision == GDFT_TF32X3)) {
+    set_error("gdft_chunked_workspace_bytes: n_ao %d, chunk %lld (a multiple of 256), precision %d", n_ao,
+              (long long)chunk, precision);
+    return GDFT_ERR_INVALID;
+  }
+  if (net != nullptr) {
+    int rc = check_network(net);
+    if (rc) return rc;
+  }
+  *bytes = chunk_ws(n_ao, chunk, precision, net).bytes;
+  return GDFT_OK;
+}
+
+int gdft_xc_energy_and_grads_chunked(const gdft_basis *shells, const double *d_basis_rows, int32_t n_ao,
+                                     const double *d_coords, const double *d_weights, int64_t n_grid, int64_t chunk,
+                                     int32_t precision, const double *d_rdm1, const gdft_functional *fn,
+                                     const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc, void *d_ws,
+                                     size_t ws_bytes, void *stream) {
+  int rc = check_functional(fn, d_ehf, n_omega);
+  if (rc) return rc;
+  return run_chunked("gdft_xc_energy_and_grads_chunked", shells, d_basis_rows, n_ao, d_coords, d_weights, n_grid,
+                     chunk, precision, d_rdm1, fn, nullptr, nullptr, d_ehf, n_omega, d_exc, d_vxc, nullptr, d_ws,
+                     ws_bytes, stream);
+}
+
+int gdft_neural_xc_energy_and_grads_chunked(const gdft_basis *shells, const double *d_basis_rows, int32_t n_ao,
+                                            const double *d_coords, const double *d_weights, int64_t n_grid,
+                                            int64_t chunk, int32_t precision, const double *d_rdm1,
+                                            const gdft_network *net, const double *d_params, const double *d_ehf,
+                                            double *d_exc, double *d_vxc, double *d_dparams, void *d_ws,
+                                            size_t ws_bytes, void *stream) {
+  int rc = check_network(net);
+  if (rc) return rc;
+  if (d_params == nullptr || d_ehf == nullptr) {
+    set_error("gdft_neural_xc_energy_and_grads_chunked: params and ehf (2, 2, grid) are required");
+    return GDFT_ERR_INVALID;
+  }
+  if ((rc = check_aligned8(d_params, "params")) || (rc = check_aligned8(d_ehf, "ehf")) ||
+      (d_dparams && (rc = check_aligned8(d_dparams, "dparams"))))
+    return rc;
+  return run_chunked("gdft_neural_xc_energy_and_grads_chunked", shells, d_basis_rows, n_ao, d_coords, d_weights,
+                     n_grid, chunk, precision, d_rdm1, nullptr, net, d_params, d_ehf, 2, d_exc, d_vxc, d_dparams,
+                     d_ws, ws_bytes, stream);
+}
+
+int gdft_chunked_status(void *d_ws, size_t ws_bytes, int32_t *status, void *stream) {
+  if (d_ws == nullptr || ws_bytes < 256 || status == nullptr) {
+    set_error("gdft_chunked_status: invalid arguments");
+    return GDFT_ERR_INVALID;
+  }
+  int h = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc;
+  if ((rc = check_cuda(cudaMemcpyAsync(&h, d_ws, sizeof(int), cudaMemcpyDeviceToHost, st), "status read"))) return rc;
+  if ((rc = check_cuda(cudaStreamSynchronize(st), "status sync"))) return rc;
+  if ((rc = check_cuda(cudaMemsetAsync(d_ws, 0, sizeof(int), st), "status clear"))) return rc;
+  *status = h;
+  if (h != 0) {
+    set_error("a device-side wait expired (code %d); results of the last calls are invalid", h);
+    return GDFT_ERR_DEVICE;
+  }
+  return GDFT_OK;
+}
+
+}  // extern "C"

@@ -69,6 +69,7 @@ cudaError_t launch_pad_potentials(const double *pot, int64_t n_grid, int64_t np,
 cudaError_t launch_integrate(int64_t n_grid, int n_cols, const gdft_functional &fn, const double *dens,
                              const double *w, double *epart, cudaStream_t st);
 cudaError_t launch_energy_reduce(const double *epart, int n, double *exc, cudaStream_t st);
+cudaError_t launch_err_fold(int *dst, int *src, cudaStream_t st);
 cudaError_t launch_vxc_reduce(const double *vpart, int nsplit, int n_ao, double *vxc, cudaStream_t st);
 cudaError_t launch_feat_to_reference(const double *feat, int64_t n_grid, int64_t np, double *rho, double *grad_rho,
                                      double *lapl, double *tau, cudaStream_t st);

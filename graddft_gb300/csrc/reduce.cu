@@ -158,6 +158,18 @@ cudaError_t launch_integrate(int64_t n_grid, int n_cols, const gdft_functional &
   return cudaGetLastError();
 }
 
+// Move a per-call error word into a persistent one (the first code recorded wins) and clear it.
+__global__ void err_fold_kernel(int *__restrict__ dst, int *__restrict__ src) {
+  const int e = *src;
+  if (e != 0) atomicCAS(dst, 0, e);
+  *src = 0;
+}
+
+cudaError_t launch_err_fold(int *dst, int *src, cudaStream_t st) {
+  err_fold_kernel<<<1, 1, 0, st>>>(dst, src);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_energy_reduce(const double *epart, int n, double *exc, cudaStream_t st) {
   energy_reduce_kernel<<<1, 256, 0, st>>>(epart, n, exc);
   return cudaGetLastError();

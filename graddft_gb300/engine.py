@@ -307,6 +307,124 @@ class Resident:
         return rdm1
 
 
+class ChunkedResident:
+    """A molecule whose AO tables are never held for the whole grid.
+
+    The grid is processed in chunks of ``chunk`` points; each chunk's AO tables
+    are evaluated from the basis into a chunk buffer and contracted at once
+    (gdft_xc_energy_and_grads_chunked): phi is recomputed per chunk instead of
+    stored, so the device memory is the basis, the grid and one chunk's tables
+    and workspace (a few GB where the resident tables of 2^20 points x 512 AOs
+    take 64 GiB plus the 48 GiB V_xc operand).  The same calls as ``Resident``
+    for the functional and network passes.
+    """
+
+    def __init__(self, basis, coords, weights, precision: str = "fp64", chunk: int = 1 << 16, device=None):
+        self.device = require_cuda(device)
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, got {precision!r}")
+        if chunk < 256 or chunk % 256:
+            raise ValueError(f"chunk must be a positive multiple of 256 grid points, got {chunk}")
+        self.precision, self.chunk = precision, int(chunk)
+        self.coords = as_device_f64(coords, self.device)
+        self.weights = as_device_f64(weights, self.device)
+        if self.coords.ndim != 2 or self.coords.shape[1] != 3 or self.weights.shape != (self.coords.shape[0],):
+            raise ValueError(f"coords {tuple(self.coords.shape)} / weights {tuple(self.weights.shape)} must be "
+                             "(grid, 3) / (grid,)")
+        self.n_grid = int(self.coords.shape[0])
+        if hasattr(basis, "device_desc"):  # a contracted ShellBasis
+            self._desc, self._keep = basis.device_desc(self.device)
+            self._rows = None
+            self.n_ao = int(self._desc.n_ao)
+        else:  # the synthetic rows of gdft_molecule_eval_basis, (n_ao, 8)
+            self._desc, self._keep = None, None
+            self._rows = as_device_f64(basis, self.device)
+            if self._rows.ndim != 2 or self._rows.shape[1] != 8:
+                raise ValueError(f"basis rows must be (n_ao, 8), got {tuple(self._rows.shape)}")
+            self.n_ao = int(self._rows.shape[0])
+        self._ws = {}
+
+    def _basis_args(self):
+        return (None if self._desc is None else ctypes.byref(self._desc)), _ptr(self._rows)
+
+    def workspace(self, net: Optional["Network"] = None) -> torch.Tensor:
+        key = None if net is None else net.key
+        ws = self._ws.get(key)
+        if ws is None:
+            nbytes = ctypes.c_size_t()
+            check(_lib.load().gdft_chunked_workspace_bytes(self.n_ao, self.chunk, PRECISIONS[self.precision],
+                                                           None if net is None else ctypes.byref(net.desc),
+                                                           ctypes.byref(nbytes)))
+            ws = self._ws[key] = torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device)
+        return ws
+
+    @property
+    def nbytes(self) -> int:
+        return sum(ws.numel() for ws in self._ws.values())
+
+    def _rdm1(self, rdm1) -> torch.Tensor:
+        rdm1 = as_device_f64(rdm1, self.device)
+        if rdm1.shape != (2, self.n_ao, self.n_ao):
+            raise ValueError(f"rdm1 must be (2, {self.n_ao}, {self.n_ao}), got {tuple(rdm1.shape)}")
+        return rdm1
+
+    def xc_energy_and_grads(self, rdm1, fn: GdftFunctional, ehf=None, want_vxc=True, exc_out=None, vxc_out=None):
+        rdm1 = self._rdm1(rdm1)
+        ehf_t = as_device_f64(ehf, self.device)
+        n_omega = 0
+        if ehf_t is not None:
+            if ehf_t.ndim != 3 or ehf_t.shape[1] != 2 or ehf_t.shape[2] != self.n_grid:
+                raise ValueError(f"ehf must be (omega, 2, {self.n_grid}), got {tuple(ehf_t.shape)}")
+            n_omega = ehf_t.shape[0]
+        exc = exc_out if exc_out is not None else torch.empty((), dtype=F64, device=self.device)
+        vxc = None
+        if want_vxc:
+            vxc = vxc_out if vxc_out is not None else torch.empty((2, self.n_ao, self.n_ao), dtype=F64,
+                                                                   device=self.device)
+        ws = self.workspace()
+        shells, rows = self._basis_args()
+        check(_lib.load().gdft_xc_energy_and_grads_chunked(
+            shells, rows, self.n_ao, _ptr(self.coords), _ptr(self.weights), self.n_grid, self.chunk,
+            PRECISIONS[self.precision], _ptr(rdm1), ctypes.byref(fn), _ptr(ehf_t), n_omega, _ptr(exc), _ptr(vxc),
+            _ptr(ws), ws.numel(), _stream(self.device)))
+        return exc, vxc
+
+    def neural_xc_energy_and_grads(self, rdm1, net: "Network", flat_params, ehf, want_vxc=True,
+                                   want_dparams=False, exc_out=None, vxc_out=None, dparams_out=None):
+        rdm1 = self._rdm1(rdm1)
+        ehf_t = as_device_f64(ehf, self.device)
+        if ehf_t is None or ehf_t.shape != (2, 2, self.n_grid):
+            raise ValueError(f"ehf must be (2, 2, {self.n_grid}) for the DM21 inputs")
+        flat = as_device_f64(flat_params, self.device)
+        if flat.ndim != 1 or flat.numel() != net.n_params:
+            raise ValueError(f"flat parameters must hold {net.n_params} values, got {tuple(flat.shape)}")
+        exc = exc_out if exc_out is not None else torch.empty((), dtype=F64, device=self.device)
+        vxc = (vxc_out if vxc_out is not None else torch.empty((2, self.n_ao, self.n_ao), dtype=F64,
+                                                               device=self.device)) if want_vxc else None
+        dp = (dparams_out if dparams_out is not None else torch.empty(net.n_params, dtype=F64, device=self.device)
+              ) if want_dparams else None
+        ws = self.workspace(net)
+        shells, rows = self._basis_args()
+        check(_lib.load().gdft_neural_xc_energy_and_grads_chunked(
+            shells, rows, self.n_ao, _ptr(self.coords), _ptr(self.weights), self.n_grid, self.chunk,
+            PRECISIONS[self.precision], _ptr(rdm1), ctypes.byref(net.desc), _ptr(flat), _ptr(ehf_t.contiguous()),
+            _ptr(exc), _ptr(vxc), _ptr(dp), _ptr(ws), ws.numel(), _stream(self.device)))
+        return exc, vxc, dp
+
+    def status(self) -> int:
+        """Synchronise and raise if a kernel recorded an expired bounded wait since the last query."""
+        st = ctypes.c_int32()
+        for ws in self._ws.values():
+            check(_lib.load().gdft_chunked_status(_ptr(ws), ws.numel(), ctypes.byref(st), _stream(self.device)))
+        return st.value
+
+    def __getattr__(self, name):
+        if name in ("density", "vxc_from_potentials", "neural_xc_hf_grads", "neural_xc_hvp", "xc_energy_grads_hf"):
+            raise NotImplementedError(f"{name} needs the AO tables of the whole grid; build the molecule with "
+                                      "resident tables (molecule_from_basis without recompute_chunk)")
+        raise AttributeError(name)
+
+
 class Network:
     """Shape and constants of a DM21-style coefficient network, and its flat parameter layout.
 

@@ -466,6 +466,41 @@ int gdft_coulomb(int32_t n_ao, const double *d_eri, const double *d_rdm1, const 
  * reference (its errors are Python exceptions). */
 int gdft_device_status(const gdft_molecule *mol, void *d_ws, size_t ws_bytes, int32_t *status, void *stream);
 
+/* Grid-chunked evaluation: phi recomputed per chunk instead of held for the
+ * whole grid.  Replaces holding Molecule.ao / grad_ao / grad_n_ao for all grid
+ * points (interface/pyscf.py:849-852, molecule.py:72-106) when the basis is
+ * known: the grid is processed in chunks of `chunk` points (a multiple of 256);
+ * for each chunk the AO tables are evaluated from the basis (a contracted
+ * gdft_basis, or the synthetic rows of gdft_molecule_eval_basis: exactly one
+ * of the two) into a chunk buffer inside the workspace, then the density,
+ * point and V_xc stages run on them and E_xc, V_xc (and dE/dtheta)
+ * accumulate over the chunks on the device.  The result is
+ * xc_energy_and_grads (train.py:86-121) of the whole grid; only the
+ * summation order over grid points differs from the resident path.
+ * d_coords (n_grid, 3) bohr, d_weights (n_grid,); d_ehf (omega, 2, n_grid)
+ * with n_omega <= 4 where the functional reads it (the network: (2, 2,
+ * n_grid)).  Workspace bytes from gdft_chunked_workspace_bytes (net NULL for
+ * a constant-coefficient functional); an expired bounded wait is reported by
+ * gdft_chunked_status. */
+int gdft_chunked_workspace_bytes(int32_t n_ao, int64_t chunk, int32_t precision, const gdft_network *net,
+                                 size_t *bytes);
+int gdft_xc_energy_and_grads_chunked(const gdft_basis *shells, const double *d_basis_rows, int32_t n_ao,
+                                     const double *d_coords, const double *d_weights, int64_t n_grid, int64_t chunk,
+                                     int32_t precision, const double *d_rdm1, const gdft_functional *fn,
+                                     const double *d_ehf, int32_t n_omega, double *d_exc, double *d_vxc, void *d_ws,
+                                     size_t ws_bytes, void *stream);
+/* The same for the DM21-style network (gdft_neural_xc_energy_and_grads per chunk; d_dparams may be NULL). */
+int gdft_neural_xc_energy_and_grads_chunked(const gdft_basis *shells, const double *d_basis_rows, int32_t n_ao,
+                                            const double *d_coords, const double *d_weights, int64_t n_grid,
+                                            int64_t chunk, int32_t precision, const double *d_rdm1,
+                                            const gdft_network *net, const double *d_params, const double *d_ehf,
+                                            double *d_exc, double *d_vxc, double *d_dparams, void *d_ws,
+                                            size_t ws_bytes, void *stream);
+/* Status of the chunked calls made with this workspace since the last query
+ * (as gdft_device_status: synchronises, returns GDFT_ERR_DEVICE with the code,
+ * clears).  No counterpart in the reference. */
+int gdft_chunked_status(void *d_ws, size_t ws_bytes, int32_t *status, void *stream);
+
 /* Test of the failure path above: one kernel waits on an mbarrier that
  * nothing arrives on, with `limit` (1..65536) polls instead of the pipeline
  * kernels' limit, so the wait runs out; it records GDFT_WAIT_EXPIRY_PROBE in

@@ -140,3 +140,20 @@ def test_host_only_checks_exchange_forms(built_lib):
     assert b"form" in lib.gdft_last_error()
     status = ctypes.c_int32()
     assert lib.gdft_hf_device_status(None, 0, ctypes.byref(status), None) == _lib.GDFT_ERR_INVALID
+
+
+def test_chunked_workspace_is_bounded_by_the_chunk(built_lib):
+    """The chunked path's workspace depends on the chunk, not on the grid (host-only call)."""
+    from graddft_gb300 import _lib
+
+    lib = _lib.load(built_lib)
+    small, big = ctypes.c_size_t(), ctypes.c_size_t()
+    assert lib.gdft_chunked_workspace_bytes(512, 1 << 16, _lib.GDFT_TF32X3, None, ctypes.byref(small)) == 0
+    assert lib.gdft_chunked_workspace_bytes(512, 1 << 17, _lib.GDFT_TF32X3, None, ctypes.byref(big)) == 0
+    assert 1.9 < big.value / small.value < 2.1
+    full = ctypes.c_size_t()
+    mol = _lib.GdftMolecule()
+    assert lib.gdft_molecule_bytes(1 << 20, 512, _lib.GDFT_TF32X3, ctypes.byref(full)) == 0
+    assert small.value < full.value / 8  # 2^16-point chunks against the resident 2^20-point tables
+    assert lib.gdft_chunked_workspace_bytes(512, 1000, _lib.GDFT_FP64, None, ctypes.byref(small)) == \
+        _lib.GDFT_ERR_INVALID  # chunks are multiples of 256 points

@@ -1,0 +1,139 @@
+"""The grid-chunked path (phi recomputed per chunk, never held for the whole grid) against the
+resident-table path and the oracle.
+
+Both paths evaluate the same AO values and run the same kernels; only the
+summation order over grid points differs (per-chunk energy and V_xc sums
+added on the device), so the FP64 form agrees to 1e-12 relative.  The mixed
+form is held to its own tolerances against the FP64 form.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from graddft_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+TOL_E, TOL_V = 5e-7, 2e-6  # the mixed form's tolerances (relative to the largest entry)
+
+
+@pytest.fixture(scope="module")
+def G(built_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import graddft_gb300 as G
+
+    return G
+
+
+def _rel(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = b.detach().cpu().numpy() if isinstance(b, torch.Tensor) else np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def _blyp(G):
+    from graddft_gb300 import _lib, engine
+
+    return engine.make_functional([_lib.COL_LSDA, _lib.COL_B88, _lib.COL_LYP], [1.0])
+
+
+@pytest.mark.parametrize("n_grid,chunk", [(2000, 512), (4096, 1024), (777, 256)])
+def test_chunked_matches_resident_fp64(G, n_grid, chunk):
+    from graddft_gb300 import engine
+
+    wl = synthetic.make_workload(n_grid, 60, 7, seed=n_grid, box_angstrom=8.0, centre_box_angstrom=5.0)
+    fn = _blyp(G)
+    r = engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "fp64")
+    e0, v0 = r.xc_energy_and_grads(wl.rdm1, fn)
+    c = engine.ChunkedResident(wl.basis.packed(), wl.coords, wl.weights, "fp64", chunk)
+    e1, v1 = c.xc_energy_and_grads(wl.rdm1, fn)
+    assert c.status() == 0
+    assert abs(float(e1) - float(e0)) <= RTOL * abs(float(e0))
+    assert _rel(v1, v0) <= RTOL
+    # and against the oracle on the same tables
+    ao, g1, g2 = O.eval_ao_planes(wl.basis, wl.coords)
+    e_ref, v_ref = O.xc_energy_and_grads("BLYP", wl.rdm1, ao, g1, g2, wl.weights)
+    assert abs(float(e1) - e_ref) <= 1e-11 * abs(e_ref) and _rel(v1, v_ref) <= 1e-11
+
+
+def test_chunked_mixed_form(G):
+    from graddft_gb300 import engine
+
+    wl = synthetic.make_workload(3000, 130, 16, seed=7, box_angstrom=8.0, centre_box_angstrom=5.0)
+    fn = _blyp(G)
+    e64, v64 = engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "fp64").xc_energy_and_grads(
+        wl.rdm1, fn)
+    c = engine.ChunkedResident(wl.basis.packed(), wl.coords, wl.weights, "tf32x3", 1024)
+    e1, v1 = c.xc_energy_and_grads(wl.rdm1, fn)
+    assert c.status() == 0
+    de = abs(float(e1) - float(e64)) / abs(float(e64))
+    dv = _rel(v1, v64)
+    print("chunked mixed: dE", de, "dV", dv)
+    assert de <= TOL_E and dv <= TOL_V
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32x3"])
+def test_chunked_contracted_shells_through_the_functional_api(G, precision):
+    """molecule_from_basis(..., recompute_chunk=...) behind the Functional API, HF column from ehf."""
+    from graddft_gb300 import basis as B
+
+    g = np.random.default_rng(5)
+    shells = []
+    for _ in range(4):
+        for l in range(3):
+            nprim = int(g.integers(1, 5))
+            e = np.sort(np.exp(g.uniform(math.log(0.1), math.log(30.0), nprim)))[::-1]
+            shells.append(B.Shell(g.uniform(-2.0, 2.0, 3), l, e,
+                                  B.normalized_contraction(l, e, g.uniform(0.1, 1.0, (nprim, 1)))))
+    basis = B.ShellBasis(shells)
+    wl = synthetic.make_workload(2300, basis.n_ao, 4, seed=9, box_angstrom=7.0, centre_box_angstrom=4.0)
+    rho = np.full((wl.n_grid, 2), 1e-2)
+    ehf = synthetic.make_ehf(wl.n_grid, 3, rho, n_omega=1)
+    ref = B.molecule_from_basis(basis, wl.coords, wl.weights, wl.rdm1, "fp64", ehf=torch.as_tensor(ehf).cuda())
+    mol = B.molecule_from_basis(basis, wl.coords, wl.weights, wl.rdm1, precision, recompute_chunk=512,
+                                ehf=torch.as_tensor(ehf).cuda())
+    f = G.Functional(coefficients=G.popular_functionals.b3lyp_coefficients,
+                     energy_densities=G.b3lyp_exhf_densities,
+                     nograd_densities=lambda m, *a, **k: m.HF_energy_density([0.0]),
+                     combine_densities=G.b3lyp_combine)
+    e0, v0 = f.xc_energy_and_grads({"params": {}}, ref)
+    e1, v1 = f.xc_energy_and_grads({"params": {}}, mol)
+    assert mol.resident().status() == 0
+    tol_e, tol_v = (RTOL, RTOL) if precision == "fp64" else (TOL_E, TOL_V)
+    assert abs(float(e1) - float(e0)) <= tol_e * abs(float(e0))
+    assert _rel(v1, v0) <= tol_v
+    with pytest.raises(NotImplementedError):
+        mol.density()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32x3"])
+def test_chunked_neural(G, precision):
+    """E_xc, V_xc and dE/dtheta of the DM21-style network, chunk by chunk, against the resident pass."""
+    from graddft_gb300 import engine
+
+    wl = synthetic.make_workload(2600, 64, 8, seed=3, box_angstrom=7.0, centre_box_angstrom=4.0)
+    ao, _, _ = O.eval_ao_planes(wl.basis, wl.coords)
+    rho = np.einsum("sab,ra,rb->rs", wl.rdm1, ao, ao)
+    ehf = synthetic.make_ehf(wl.n_grid, 4, rho, n_omega=2)
+    width = 128
+    net = engine.Network(n_layers=2, width=width, precision=precision)
+    params = synthetic.glorot_params(layer_widths=(width,) * 2, seed=4)
+    flat = net.flatten({"params": {k: {kk: torch.as_tensor(v) for kk, v in d.items()}
+                                   for k, d in params["params"].items()}}, torch.device("cuda"))
+    r = engine.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "fp64")
+    net64 = engine.Network(n_layers=2, width=width, precision="fp64")
+    e0, v0, d0 = r.neural_xc_energy_and_grads(wl.rdm1, net64, flat, ehf, want_vxc=True, want_dparams=True)
+    c = engine.ChunkedResident(wl.basis.packed(), wl.coords, wl.weights, precision, 768)
+    e1, v1, d1 = c.neural_xc_energy_and_grads(wl.rdm1, net, flat, ehf, want_vxc=True, want_dparams=True)
+    assert c.status() == 0
+    if precision == "fp64":
+        assert abs(float(e1) - float(e0)) <= 1e-11 * abs(float(e0))
+        assert _rel(v1, v0) <= 1e-11 and _rel(d1, d0) <= 1e-10
+    else:
+        assert abs(float(e1) - float(e0)) <= 1e-6 * abs(float(e0))
+        assert _rel(v1, v0) <= 1e-5 and _rel(d1, d0) <= 1e-5
