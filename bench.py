@@ -528,6 +528,139 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_stream(args):
+    """Config 2 with the AO tables recomputed per grid chunk (never resident): grid-pts/s and device memory."""
+    import ctypes
+
+    import torch
+
+    from graddft_gb300 import _lib, build, engine, synthetic
+
+    build.build()
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    form = args.form or "tf32x3"
+    wl = synthetic.make_workload(args.n_grid, args.n_ao, N_OCC, SEED)
+    fn = engine.make_functional([_lib.COL_LSDA, _lib.COL_B88, _lib.COL_LYP], [1.0])
+    rdm1 = torch.as_tensor(wl.rdm1, device=dev)
+    c = engine.ChunkedResident(wl.basis.packed(), wl.coords, wl.weights, form,
+                               args.chunk if args.chunk else "auto", dev)
+    exc = torch.empty((), dtype=torch.float64, device=dev)
+    vxc = torch.empty((2, args.n_ao, args.n_ao), dtype=torch.float64, device=dev)
+    for _ in range(args.warmup):
+        c.xc_energy_and_grads(rdm1, fn, None, True, exc, vxc)
+    torch.cuda.synchronize()
+    c.status()
+    lib.gdft_profile_reset()
+    lib.gdft_profile_enable(1)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            c.xc_energy_and_grads(rdm1, fn, None, True, exc, vxc)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    lib.gdft_profile_enable(0)
+    c.status()
+    ms = e0.elapsed_time(e1) / args.steps
+    stage = {}
+    for name, sid in (("ao", _lib.STAGE_AO), ("density", _lib.STAGE_DENSITY), ("point", _lib.STAGE_POINT),
+                      ("vxc", _lib.STAGE_VXC), ("reduce", _lib.STAGE_REDUCE)):
+        t, n = ctypes.c_double(), ctypes.c_int64()
+        _lib.check(lib.gdft_profile_read(sid, ctypes.byref(t), ctypes.byref(n)))
+        stage[name] = t.value / args.steps
+    mol_bytes, ws_bytes = ctypes.c_size_t(), ctypes.c_size_t()
+    _lib.check(lib.gdft_molecule_bytes(args.n_grid, args.n_ao, engine.PRECISIONS[form], ctypes.byref(mol_bytes)))
+    desc = _lib.GdftMolecule()
+    desc.n_grid, desc.n_ao, desc.precision = args.n_grid, args.n_ao, engine.PRECISIONS[form]
+    line = {
+        "metric": "E_xc fwd+bwd grid-pts/s with the AO tables recomputed per grid chunk", "value": args.n_grid / (ms * 1e-3),
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": form,
+        "data": "synthetic (seeded Gaussian basis, evaluated per chunk on the device)",
+        "config": {"workload": _workload(args.n_grid, args.n_ao) + ", AO tables recomputed per chunk",
+                   "n_ao": args.n_ao, "n_grid": args.n_grid, "chunk": c.chunk, "form": form},
+        "device_bytes": {"chunked_workspace": c.nbytes, "resident_tables": mol_bytes.value},
+        "stage_ms_per_step": stage, "clocks": clk.summary(),
+        "e_xc": float(exc),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_batch_full(args):
+    """Config 4 at its stated grid, N = 1500 n_ao (rounded to 128): 64 molecules, n_ao ~ U[24, 400], the DM21
+    network (6 x 256), loss sum_m (E_m - E_ref)^2; each molecule's AO tables recomputed per grid chunk (one
+    workspace shared by all molecules, chunk size from the autotuner); E, V_xc and dE/dtheta per molecule."""
+    import torch
+
+    from graddft_gb300 import build, engine, synthetic
+
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(SEED)
+    n_mol = args.n_mol
+    naos = rng.integers(24, 401, size=n_mol)
+    pool = {}
+    mols = []
+    for i, n_ao in enumerate(naos):
+        n_grid = int(round(args.points_per_ao * n_ao / 128.0)) * 128
+        wl = synthetic.make_workload(n_grid, int(n_ao), max(1, int(n_ao) // 8), seed=SEED + 1 + i)
+        r = engine.ChunkedResident(wl.basis.packed(), wl.coords, wl.weights, "tf32x3",
+                                   args.chunk if args.chunk else "auto", dev, workspace_pool=pool)
+        mols.append((r, torch.as_tensor(wl.rdm1, device=dev),
+                     torch.as_tensor(synthetic.make_ehf(n_grid, SEED + 100 + i, None, 2), device=dev)))
+    net = engine.Network(precision="tf32x3")
+    p = synthetic.glorot_params(seed=SEED)
+    flat = net.flatten({"params": {k: {kk: torch.as_tensor(v) for kk, v in d.items()}
+                                   for k, d in p["params"].items()}}, dev)
+    exc = torch.empty(n_mol, dtype=torch.float64, device=dev)
+    vx = [torch.empty((2, r.n_ao, r.n_ao), dtype=torch.float64, device=dev) for r, _, _ in mols]
+    dps = torch.empty((n_mol, net.n_params), dtype=torch.float64, device=dev)
+    e_ref = torch.zeros(n_mol, dtype=torch.float64, device=dev)
+
+    def step():
+        for i, (r, d, ehf) in enumerate(mols):
+            r.neural_xc_energy_and_grads(d, net, flat, ehf, want_vxc=True, want_dparams=True, exc_out=exc[i],
+                                         vxc_out=vx[i], dparams_out=dps[i])
+        # The caller's loss: dloss/dtheta = sum_m 2 (E_m - E_ref,m) dE_m/dtheta, dloss/dD_m = 2 (E_m - E_ref,m) V_m.
+        g = 2.0 * (exc - e_ref)
+        return (g[:, None] * dps).sum(0)
+
+    step()  # tunes the chunk size per AO bucket (timed once, cached on disk)
+    e_ref = exc + 0.01 * torch.randn(n_mol, dtype=torch.float64, generator=torch.Generator().manual_seed(SEED)).to(dev)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    for r, _, _ in mols:
+        r.status()
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    n_pts = sum(r.n_grid for r, _, _ in mols)
+    line = {
+        "metric": "batched training step molecules/s at the full config-4 grid (AO tables recomputed per chunk)",
+        "value": n_mol / (ms * 1e-3), "unit": "molecules/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "tf32x3", "data": "synthetic (seeded basis per molecule)",
+        "config": {"workload": f"batched step, {n_mol} molecules, n_ao ~ U[24, 400], n_grid = "
+                               f"{args.points_per_ao} n_ao, DM21 network 6 x 256", "n_mol": n_mol,
+                   "n_ao_range": [int(naos.min()), int(naos.max())], "grid_points_total": n_pts,
+                   "chunks": sorted({int(r.chunk) for r, _, _ in mols})},
+        "grid_pts_per_s": n_pts / (ms * 1e-3), "device_bytes_workspace": sum(w.numel() for w in pool.values()),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_hf(args):
     """DM21 energy_predictor with its exact-exchange terms from a chi tensor: grid-pts/s of (E, Fock)."""
     import time
@@ -859,11 +992,14 @@ def main():
     ap.add_argument("--dump", default=None, help="--impl reference: write the sample's oracle E_xc, V_xc here")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form run (rate and accuracy)")
-    ap.add_argument("--workload", default="xc", choices=["xc", "neural", "scf", "batch", "hf", "ao", "chi", "solid"],
+    ap.add_argument("--workload", default="xc",
+                    choices=["xc", "neural", "scf", "batch", "batch_full", "stream", "hf", "ao", "chi", "solid"],
                     help="xc: B88+LYP contraction benchmark (headline); neural: DM21-style network fwd+bwd; "
                          "scf: differentiable SCF loop; batch: many molecules per step; hf: DM21 predict with "
                          "its exact-exchange terms from a chi tensor; ao: AO tables from contracted shells; chi: the chi tensor from range-separated integrals; solid: k-point XC for a Solid")
     ap.add_argument("--n-mol", type=int, default=64, help="molecules (--workload batch)")
+    ap.add_argument("--chunk", type=int, default=None,
+                    help="grid points per chunk of --workload stream / batch_full (default: the autotuner's choice)")
     ap.add_argument("--points-per-ao", type=int, default=150, help="grid points per AO (--workload batch)")
     ap.add_argument("--cycles", type=int, default=20, help="SCF iterations (--workload scf)")
     ap.add_argument("--loop", default="simple", choices=["simple", "diis"],
@@ -877,6 +1013,12 @@ def main():
         return run_scf(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "batch_full":
+        if args.points_per_ao == 150:
+            args.points_per_ao = 1500
+        return run_batch_full(args)
+    if args.workload == "stream":
+        return run_stream(args)
     if args.workload == "hf":
         return run_hf(args)
     if args.workload == "ao":

@@ -319,13 +319,18 @@ class ChunkedResident:
     for the functional and network passes.
     """
 
-    def __init__(self, basis, coords, weights, precision: str = "fp64", chunk: int = 1 << 16, device=None):
+    def __init__(self, basis, coords, weights, precision: str = "fp64", chunk=1 << 16, device=None,
+                 workspace_pool: Optional[dict] = None):
+        """``chunk``: grid points per chunk (a multiple of 256), or "auto" to let ``autotune`` pick it on
+        the first call (timed once per problem bucket and cached on disk).  ``workspace_pool``: a dict
+        shared by several molecules evaluated one after another, so that they reuse one workspace per
+        network shape (grown to the largest molecule) instead of holding one each."""
         self.device = require_cuda(device)
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, got {precision!r}")
-        if chunk < 256 or chunk % 256:
-            raise ValueError(f"chunk must be a positive multiple of 256 grid points, got {chunk}")
-        self.precision, self.chunk = precision, int(chunk)
+        if chunk != "auto" and (int(chunk) < 256 or int(chunk) % 256):
+            raise ValueError(f"chunk must be a positive multiple of 256 grid points or 'auto', got {chunk}")
+        self.precision, self.chunk = precision, (chunk if chunk == "auto" else int(chunk))
         self.coords = as_device_f64(coords, self.device)
         self.weights = as_device_f64(weights, self.device)
         if self.coords.ndim != 2 or self.coords.shape[1] != 3 or self.weights.shape != (self.coords.shape[0],):
@@ -342,21 +347,45 @@ class ChunkedResident:
             if self._rows.ndim != 2 or self._rows.shape[1] != 8:
                 raise ValueError(f"basis rows must be (n_ao, 8), got {tuple(self._rows.shape)}")
             self.n_ao = int(self._rows.shape[0])
-        self._ws = {}
+        self._ws = workspace_pool if workspace_pool is not None else {}
 
     def _basis_args(self):
         return (None if self._desc is None else ctypes.byref(self._desc)), _ptr(self._rows)
 
+    def workspace_bytes(self, chunk: int, net: Optional["Network"] = None) -> int:
+        nbytes = ctypes.c_size_t()
+        check(_lib.load().gdft_chunked_workspace_bytes(self.n_ao, int(chunk), PRECISIONS[self.precision],
+                                                       None if net is None else ctypes.byref(net.desc),
+                                                       ctypes.byref(nbytes)))
+        return nbytes.value
+
     def workspace(self, net: Optional["Network"] = None) -> torch.Tensor:
         key = None if net is None else net.key
+        need = self.workspace_bytes(self.chunk, net)
         ws = self._ws.get(key)
-        if ws is None:
-            nbytes = ctypes.c_size_t()
-            check(_lib.load().gdft_chunked_workspace_bytes(self.n_ao, self.chunk, PRECISIONS[self.precision],
-                                                           None if net is None else ctypes.byref(net.desc),
-                                                           ctypes.byref(nbytes)))
-            ws = self._ws[key] = torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device)
+        if ws is None or ws.numel() < need:
+            if ws is not None:  # report what the smaller workspace recorded before it goes
+                st = ctypes.c_int32()
+                check(_lib.load().gdft_chunked_status(_ptr(ws), ws.numel(), ctypes.byref(st), _stream(self.device)))
+            self._ws.pop(key, None)
+            ws = self._ws[key] = torch.zeros(need, dtype=torch.uint8, device=self.device)  # error word 0
         return ws
+
+    def _resolve_chunk(self, net: Optional["Network"], call) -> None:
+        """Pick the chunk size with the autotuner when it was left to "auto" (the first call times the
+        candidates with the caller's own arguments)."""
+        if self.chunk != "auto":
+            return
+        from . import autotune
+
+        key = autotune.bucket_key(self.n_ao, self.precision, None if net is None else net.key, self.device)
+
+        def run(c):
+            self.chunk = c
+            call()
+
+        self.chunk = autotune.choose(key, run, lambda c: self.workspace_bytes(c, net), self.n_grid, self.device)
+        self._ws.pop(None if net is None else net.key, None)  # the timing may have grown it past the chosen size
 
     @property
     def nbytes(self) -> int:
@@ -381,6 +410,7 @@ class ChunkedResident:
         if want_vxc:
             vxc = vxc_out if vxc_out is not None else torch.empty((2, self.n_ao, self.n_ao), dtype=F64,
                                                                    device=self.device)
+        self._resolve_chunk(None, lambda: self.xc_energy_and_grads(rdm1, fn, ehf, want_vxc, exc, vxc))
         ws = self.workspace()
         shells, rows = self._basis_args()
         check(_lib.load().gdft_xc_energy_and_grads_chunked(
@@ -403,6 +433,8 @@ class ChunkedResident:
                                                                device=self.device)) if want_vxc else None
         dp = (dparams_out if dparams_out is not None else torch.empty(net.n_params, dtype=F64, device=self.device)
               ) if want_dparams else None
+        self._resolve_chunk(net, lambda: self.neural_xc_energy_and_grads(rdm1, net, flat, ehf_t, want_vxc,
+                                                                         want_dparams, exc, vxc, dp))
         ws = self.workspace(net)
         shells, rows = self._basis_args()
         check(_lib.load().gdft_neural_xc_energy_and_grads_chunked(

@@ -183,3 +183,24 @@ def test_dlpack_producer_is_accepted_on_the_host():
         got = engine.as_device_f64(DLPackOnly(src), "cpu")
         assert got.dtype == torch.float64 and got.is_contiguous()
         assert torch.equal(got, torch.as_tensor(a, dtype=torch.float64))
+
+
+def test_chunk_autotuner_times_once_and_caches(monkeypatch, tmp_path):
+    """The autotuner keeps the smallest chunk within the tolerance of the fastest, skips sizes over the memory
+    budget or the grid, and answers from its on-disk cache afterwards."""
+    from graddft_gb300 import autotune
+
+    monkeypatch.setenv("GDFT_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    ms = {1 << 14: 10.0, 1 << 15: 8.0, 1 << 16: 7.9, 1 << 17: 7.7, 1 << 18: 7.6}
+    timed = []
+    monkeypatch.setattr(autotune, "time_call", lambda fn, device, reps=2: (fn(), ms.get(timed[-1], 5.0))[1])
+    run = lambda c: timed.append(c)  # noqa: E731
+    ws = lambda c: c * 1000  # noqa: E731
+    got = autotune.choose("k", run, ws, n_grid=1 << 20, device=None, budget_bytes=(1 << 17) * 1000, tol=0.03)
+    assert got == 1 << 16 and sorted(set(timed)) == [1 << 14, 1 << 15, 1 << 16, 1 << 17]
+    timed.clear()
+    assert autotune.choose("k", run, ws, n_grid=1 << 20, device=None, budget_bytes=1) == 1 << 16 and not timed
+    # sizes above the grid collapse to the grid rounded up to 256
+    timed.clear()
+    assert autotune.choose("small", run, ws, n_grid=5000, device=None, budget_bytes=1 << 40) == 5120
+    assert set(timed) == {5120}
