@@ -124,3 +124,66 @@ def test_mixed_feature_functionals_vs_reference(eng, golden, case, name, fname, 
     dv = _rel(vxc, g[f"vxc_{name}"])
     print(case, name, "dE", de, "dV", dv)
     assert de <= TOL_E and dv <= TOL_V
+
+
+def _decode_tables(r, n_grid, n_ao):
+    """The mixed form's resident tables read back: point-major hi + lo, AO-major three-slice sums and
+    FP32-pair sums, each as (5 or 4, n_grid, n_ao) float64 arrays (the layouts of tc_pack.cu)."""
+    np_, ldk = int(r.desc.n_grid_pad), -(-n_ao // 128) * 128
+    buf = r.buffer.cpu().numpy()
+    a256 = lambda x: (x + 255) // 256 * 256  # noqa: E731
+    plane = np_ * ldk * 4
+    off_pm = a256(np_ * 8)
+    off_av = a256(off_pm + 5 * 2 * plane)
+    off_af = a256(off_av + 4 * 3 * plane)
+    f = lambda off, n: buf[off:off + 4 * n].view(np.float32).astype(np.float64)  # noqa: E731
+    pm, av, af = f(off_pm, 5 * 2 * np_ * ldk), f(off_av, 4 * 3 * np_ * ldk), f(off_af, 5 * 2 * np_ * ldk)
+    p = np.arange(n_grid)[:, None]
+    a = np.arange(n_ao)[None, :]
+
+    def koff(row, k):
+        return (((row >> 3) * 8 + (k >> 2)) * 128 + (row & 7) * 16 + (k & 3) * 4) // 4
+
+    blk = 128 * 32
+    nkc, npc = ldk // 32, np_ // 32
+    out_pm, out_av, out_af = np.empty((5, n_grid, n_ao)), np.empty((4, n_grid, n_ao)), np.empty((5, n_grid, n_ao))
+    for t in range(5):
+        b = ((p // 128 * 5 + t) * nkc + a // 32) * 2
+        i = b * blk + koff(p % 128, a % 32)
+        out_pm[t] = pm[i] + pm[i + blk]
+        b = ((a // 128 * 5 + t) * npc + p // 32) * 2
+        i = b * blk + koff(a % 128, p % 32)
+        out_af[t] = af[i] + af[i + blk]
+        if t < 4:
+            b = ((a // 128 * 4 + t) * npc + p // 32) * 3
+            i = b * blk + koff(a % 128, p % 32)
+            out_av[t] = (av[i] + av[i + blk]) + av[i + 2 * blk]
+    return out_pm, out_av, out_af
+
+
+@pytest.mark.parametrize("source", ["basis", "tables"])
+def test_packed_tables_against_fp64(eng, source):
+    """The mixed form's tables, built in double-float arithmetic, against FP64 values: the FP32 pairs to
+    1e-10 of each AO's largest value over its 32-point chunk (about 2^-44 of the terms, which cancel in
+    the gradient and Laplacian planes), the three-slice sets to 2^-31 of it, the
+    point-major TF32 pairs to 2^-21 of each value.  Values below 1e-20 are measured against 1e-20: FP32
+    pairs lose their low part near FP32's range (exponentials below e^-70) and flush under it."""
+    n_grid, n_ao = 1000, 130
+    wl = synthetic.make_workload(n_grid, n_ao, 16, seed=17, box_angstrom=8.0, centre_box_angstrom=5.0)
+    ao, g1, g2 = O.eval_ao_planes(wl.basis, wl.coords)
+    if source == "basis":
+        r = eng.Resident.from_basis(wl.basis.packed(), wl.coords, wl.weights, "tf32x3")
+    else:
+        r = eng.Resident.from_tables(ao, g1, g2, wl.weights, "tf32x3")
+    torch.cuda.synchronize()
+    ref = np.stack([ao, g1[..., 0], g1[..., 1], g1[..., 2], g2.sum(-1)])
+    pm, av, af = _decode_tables(r, n_grid, n_ao)
+    # the largest magnitude of each AO over each 32-point chunk (the quantisation scale)
+    pad = (-n_grid) % 32
+    refp = np.pad(np.abs(ref), ((0, 0), (0, pad), (0, 0)))
+    scale = np.maximum(np.repeat(refp.reshape(5, -1, 32, n_ao).max(axis=2), 32, axis=1)[:, :n_grid], 1e-20)
+    err_af = np.max(np.abs(af - ref) / scale)
+    err_av = np.max(np.abs(av - ref[:4]) / scale[:4])
+    err_pm = np.max(np.abs(pm - ref) / np.maximum(np.abs(ref), 1e-20))
+    print(source, "af", err_af, "av", err_av, "pm", err_pm)
+    assert err_af <= 1e-10 and err_av <= 2.0 ** -31 and err_pm <= 2.0 ** -21, (err_af, err_av, err_pm)
