@@ -27,47 +27,260 @@ constexpr size_t kBlk = 2 * (umma::kBlockBytes / 4);  // floats in one packed hi
 // (GB300's FP64 rate is a small fraction of its FP32 rate, and the activations
 // are FP32); long accumulations over grid points and the energy stay FP64.
 
-// z = zW + b (stored back); h = tanh(z).
-__global__ void l0_fwd_kernel(float *__restrict__ Z, const float *__restrict__ b, size_t total, int width,
-                              float *__restrict__ H) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= total) return;
-  const float z = Z[i] + b[i % width];
-  Z[i] = z;
-  H[i] = tanhf(z);
+// ---------------------------------------------------------------- row tiles
+// The fused row kernels below take 32 grid points at a time: each warp handles
+// 4 of them (one row per warp at a time), the 32 x W activation tile is staged in
+// shared memory (row stride W + 4) and then written in both packed operand
+// layouts of the next GEMMs, so neither packing pass re-reads it from memory:
+//   rt (row tiles, A of z = h W and dh = dz W^T): block (r / 128, c / 32)
+//   ct (column tiles, A / B of dW = h^T dz):      block (c / 128, r / 32)
+// A warp's 16-byte stores cover 512 contiguous bytes of a block in both.
+constexpr int kRowTile = 32;
+
+// hi = tf32(x), lo = tf32(x - hi) of four values.
+__device__ __forceinline__ void split_f4(const float (&v)[4], float4 &h, float4 &l) {
+  umma::split_tf32f(v[0], h.x, l.x);
+  umma::split_tf32f(v[1], h.y, l.y);
+  umma::split_tf32f(v[2], h.z, l.z);
+  umma::split_tf32f(v[3], h.w, l.w);
 }
 
-// z = zW + b + h_prev (stored back into Z); h = elu(LayerNorm(z)) (in place of h_prev).
-// Mean and variance are taken in two passes over the row held in registers.
 template <int PL>
-__global__ void layer_fwd_kernel(float *__restrict__ Z, const float *__restrict__ b, float *__restrict__ H,
-                                 const float *__restrict__ gam, const float *__restrict__ bet, double eps,
-                                 int64_t rows) {
-  constexpr int W = 32 * PL;
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (r >= rows) return;
-  float *z = Z + (size_t)r * W, *h = H + (size_t)r * W;
-  float v[PL], s1 = 0.0f;
+__device__ __forceinline__ void store_tile_packs(const float *tile, int64_t r0, float *__restrict__ rt_out,
+                                                 float *__restrict__ ct_out, int64_t rchunks) {
+  constexpr int W = 32 * PL, LD = W + 4, KC = W / 32, FT = W / 128;
+  const int u = threadIdx.x;
+  if (rt_out) {
+    const int64_t t = r0 / 128;
+    const int rb = (int)(r0 % 128);
+    const int row = (u >> 6) * 8 + (u & 7), kg = (u >> 3) & 7;
+    const uint32_t off = umma::kblock_off(rb + row, kg * 4) / 4;
+#pragma unroll
+    for (int kc = 0; kc < KC; ++kc) {
+      const float4 v = *(const float4 *)(tile + row * LD + kc * 32 + kg * 4);
+      const float a[4] = {v.x, v.y, v.z, v.w};
+      float4 h, l;
+      split_f4(a, h, l);
+      float *blk = rt_out + ((size_t)t * KC + kc) * kBlk;
+      *(float4 *)(blk + off) = h;
+      *(float4 *)(blk + umma::kBlockBytes / 4 + off) = l;
+    }
+  }
+  if (ct_out) {
+    const int64_t rc = r0 / 32;
+#pragma unroll
+    for (int ft = 0; ft < FT; ++ft) {
+      float *blk = ct_out + ((size_t)ft * rchunks + rc) * kBlk;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int v = u + 256 * i;
+        const int f = (v >> 6) * 8 + (v & 7), pg = (v >> 3) & 7;
+        const float *col = tile + ft * 128 + f;
+        const float a[4] = {col[(pg * 4 + 0) * LD], col[(pg * 4 + 1) * LD], col[(pg * 4 + 2) * LD],
+                            col[(pg * 4 + 3) * LD]};
+        float4 h, l;
+        split_f4(a, h, l);
+        const uint32_t off = umma::kblock_off(f, pg * 4) / 4;
+        *(float4 *)(blk + off) = h;
+        *(float4 *)(blk + umma::kBlockBytes / 4 + off) = l;
+      }
+    }
+  }
+}
+
+// Forward row pass fused with the packing of its output h:
+//   L0:    z = zW + b (stored back), h = tanh(z)
+//   else:  z = zW + b + h_prev (stored back), h = elu(LayerNorm(z)) (in place of h_prev)
+// h is written to H and, where the pointers are given, packed as the rt
+// operand of the next dense layer and the ct operand of its weight gradient.
+// rows is a multiple of 32.
+template <int PL, bool L0>
+__global__ void __launch_bounds__(256) layer_fwd_pack_kernel(float *__restrict__ Z, const float *__restrict__ b,
+                                                             float *__restrict__ H, const float *__restrict__ gam,
+                                                             const float *__restrict__ bet, double eps, int64_t rows,
+                                                             float *__restrict__ rt_out, float *__restrict__ ct_out) {
+  constexpr int W = 32 * PL, LD = W + 4;
+  __shared__ __align__(16) float tile[kRowTile * LD];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float bf[PL], gf[PL], ef[PL];
 #pragma unroll
   for (int k = 0; k < PL; ++k) {
     const int c = lane + 32 * k;
-    v[k] = (z[c] + b[c]) + h[c];
-    s1 += v[k];
+    bf[k] = b[c];
+    gf[k] = L0 ? 0.0f : gam[c];
+    ef[k] = L0 ? 0.0f : bet[c];
   }
-  const float mean = warp_sumf(s1) * (1.0f / W);
-  float s2 = 0.0f;
+  for (int64_t r0 = (int64_t)blockIdx.x * kRowTile; r0 < rows; r0 += (int64_t)gridDim.x * kRowTile) {
+    // All four rows' loads first (Z and H are written below).
+    float v[4][PL];
 #pragma unroll
-  for (int k = 0; k < PL; ++k) {
-    const float d = v[k] - mean;
-    s2 += d * d;
+    for (int i = 0; i < 4; ++i) {
+      const size_t base = (size_t)(r0 + wid * 4 + i) * W;
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const int c = lane + 32 * k;
+        v[i][k] = L0 ? Z[base + c] + bf[k] : (Z[base + c] + bf[k]) + H[base + c];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int rr = wid * 4 + i;
+      const size_t base = (size_t)(r0 + rr) * W;
+      float mean = 0.0f, rs = 1.0f;
+      if (!L0) {
+        float s1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PL; ++k) s1 += v[i][k];
+        mean = warp_sumf(s1) * (1.0f / W);
+        float s2 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PL; ++k) {
+          const float d = v[i][k] - mean;
+          s2 += d * d;
+        }
+        rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
+      }
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const int c = lane + 32 * k;
+        const float h = L0 ? tanhf(v[i][k]) : eluf((v[i][k] - mean) * (rs * gf[k]) + ef[k]);
+        Z[base + c] = v[i][k];
+        H[base + c] = h;
+        tile[rr * LD + c] = h;
+      }
+    }
+    __syncthreads();
+    store_tile_packs<PL>(tile, r0, rt_out, ct_out, rows / 32);
+    __syncthreads();
   }
-  const float rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
+}
+
+// Reverse of a residual layer fused with the packing of dE/dz as the rt
+// operand of dh = dz W^T and the ct operand of dW = h^T dz.  The incoming
+// dE/dh is dy W_out^T (last layer: dy != null) or dhp + gres (the GEMM output
+// plus the residual branch of the layer above).  Writes dE/dz (FP32) and
+// per-block partial sums [block][3][W] of dE/dgamma, dE/dbeta and dE/db
+// (= sum dz): FP32 over 16 rows of a warp at a time, then FP64.
+// rows is a multiple of 32; part has gridDim.x blocks of [3][W].
+template <int PL>
+constexpr size_t bwd_pack_smem() {
+  return sizeof(double) * 8 * 3 * (32 * PL) + sizeof(float) * kRowTile * (32 * PL + 4);
+}
+
+template <int PL>
+__global__ void __launch_bounds__(256, 2) layer_bwd_pack_kernel(
+    const float *__restrict__ dhp, const float *__restrict__ gres, const double *__restrict__ dy,
+    const float *__restrict__ Wo, const float *__restrict__ Z, const float *__restrict__ gam,
+    const float *__restrict__ bet, double eps, int64_t rows, float *__restrict__ gz, double *__restrict__ part,
+    float *__restrict__ rt_out, float *__restrict__ ct_out) {
+  constexpr int W = 32 * PL, LD = W + 4;
+  // Dynamic shared memory (bwd_pack_smem<PL>() bytes): per-warp FP64 sums of
+  // dgamma, dbeta, db, then the row tile.
+  extern __shared__ __align__(16) unsigned char bwd_smem[];
+  double(*sacc)[3][W] = reinterpret_cast<double(*)[3][W]>(bwd_smem);
+  float *tile = reinterpret_cast<float *>(bwd_smem + sizeof(double) * 8 * 3 * W);
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float gmf[PL], btf[PL];
 #pragma unroll
   for (int k = 0; k < PL; ++k) {
     const int c = lane + 32 * k;
-    z[c] = v[k];
-    h[c] = eluf((v[k] - mean) * (rs * gam[c]) + bet[c]);
+    gmf[k] = gam[c];
+    btf[k] = bet[c];
+    sacc[wid][0][c] = sacc[wid][1][c] = sacc[wid][2][c] = 0.0;
+  }
+  float fg[PL], fb[PL], fd[PL];
+#pragma unroll
+  for (int k = 0; k < PL; ++k) fg[k] = fb[k] = fd[k] = 0.0f;
+  int ntile = 0;
+  for (int64_t r0 = (int64_t)blockIdx.x * kRowTile; r0 < rows; r0 += (int64_t)gridDim.x * kRowTile) {
+#pragma unroll 1
+    for (int i2 = 0; i2 < 4; i2 += 2) {
+      float zv[2][PL], gh[2][PL];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int64_t r = r0 + wid * 4 + i2 + i;
+        const size_t base = (size_t)r * W;
+        float dy0 = 0.0f, dy1 = 0.0f, dy2 = 0.0f;
+        if (dy) {
+          dy0 = (float)dy[r * 3 + 0];
+          dy1 = (float)dy[r * 3 + 1];
+          dy2 = (float)dy[r * 3 + 2];
+        }
+#pragma unroll
+        for (int k = 0; k < PL; ++k) {
+          const int c = lane + 32 * k;
+          zv[i][k] = Z[base + c];
+          gh[i][k] = dy ? fmaf(dy0, __ldg(Wo + c * 3), fmaf(dy1, __ldg(Wo + c * 3 + 1), dy2 * __ldg(Wo + c * 3 + 2)))
+                        : dhp[base + c] + gres[base + c];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int rr = wid * 4 + i2 + i;
+        const size_t base = (size_t)(r0 + rr) * W;
+        float s1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PL; ++k) s1 += zv[i][k];
+        const float mean = warp_sumf(s1) * (1.0f / W);
+        float s2 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PL; ++k) {
+          const float d = zv[i][k] - mean;
+          s2 += d * d;
+        }
+        const float rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
+        float g[PL], xh[PL], m1 = 0.0f, m2 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PL; ++k) {
+          xh[k] = (zv[i][k] - mean) * rs;
+          const float a = xh[k] * gmf[k] + btf[k];
+          const float da = gh[i][k] * (a > 0.0f ? 1.0f : expf(a));
+          fg[k] = fmaf(da, xh[k], fg[k]);
+          fb[k] += da;
+          g[k] = da * gmf[k];
+          m1 += g[k];
+          m2 += g[k] * xh[k];
+        }
+        const float mm1 = warp_sumf(m1) * (1.0f / W), mm2 = warp_sumf(m2) * (1.0f / W);
+#pragma unroll
+        for (int k = 0; k < PL; ++k) {
+          const int c = lane + 32 * k;
+          const float d = rs * (g[k] - mm1 - xh[k] * mm2);
+          fd[k] += d;
+          gz[base + c] = d;
+          tile[rr * LD + c] = d;
+        }
+      }
+    }
+    if (++ntile == 4) {  // 16 rows per warp: FP32 partials into the FP64 sums
+      ntile = 0;
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const int c = lane + 32 * k;
+        sacc[wid][0][c] += fg[k];
+        sacc[wid][1][c] += fb[k];
+        sacc[wid][2][c] += fd[k];
+        fg[k] = fb[k] = fd[k] = 0.0f;
+      }
+    }
+    __syncthreads();
+    store_tile_packs<PL>(tile, r0, rt_out, ct_out, rows / 32);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < PL; ++k) {
+    const int c = lane + 32 * k;
+    sacc[wid][0][c] += fg[k];
+    sacc[wid][1][c] += fb[k];
+    sacc[wid][2][c] += fd[k];
+  }
+  __syncthreads();
+  double *out = part + (size_t)blockIdx.x * 3 * W;
+  for (int c = threadIdx.x; c < 3 * W; c += blockDim.x) {
+    const int q = c / W, cc = c % W;
+    double sum = 0.0;
+    for (int w8 = 0; w8 < 8; ++w8) sum += sacc[w8][q][cc];
+    out[c] = sum;
   }
 }
 
@@ -145,112 +358,6 @@ __global__ void __launch_bounds__(256) head_kernel(const float *__restrict__ H, 
     double t = 0.0;
     for (int i = 0; i < 8; ++i) t += red[i];
     epart[blockIdx.x] = t;
-  }
-}
-
-// Reverse of a residual layer, one warp per row.  The incoming dE/dh is
-// dy W_out^T (last layer: dy != null) or dhp + gres (the GEMM output plus the
-// residual branch of the layer above).  Writes dE/dz (FP32) and per-block
-// partial sums [block][3][W] of dE/dgamma, dE/dbeta and dE/db (= sum dz),
-// accumulated in FP64 over the rows.
-template <int PL>
-__global__ void __launch_bounds__(256) layer_bwd_kernel(const float *__restrict__ dhp, const float *__restrict__ gres,
-                                                        const double *__restrict__ dy, const float *__restrict__ Wo,
-                                                        const float *__restrict__ Z, const float *__restrict__ gam,
-                                                        const float *__restrict__ bet, double eps, int64_t rows,
-                                                        float *__restrict__ gz, double *__restrict__ part) {
-  constexpr int W = 32 * PL;
-  __shared__ double sacc[8][3][W];
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float gmf[PL], btf[PL], wo[PL][3];
-#pragma unroll
-  for (int k = 0; k < PL; ++k) {
-    const int c = lane + 32 * k;
-    gmf[k] = gam[c];
-    btf[k] = bet[c];
-#pragma unroll
-    for (int f = 0; f < 3; ++f) wo[k][f] = dy ? Wo[c * 3 + f] : 0.0f;
-  }
-  // Parameter-gradient sums: FP32 over 16 rows at a time, then FP64.
-  double pg[PL], pb[PL], pd[PL];
-  float fg[PL], fb[PL], fd[PL];
-#pragma unroll
-  for (int k = 0; k < PL; ++k) {
-    pg[k] = pb[k] = pd[k] = 0.0;
-    fg[k] = fb[k] = fd[k] = 0.0f;
-  }
-  int nrow = 0;
-  for (int64_t r = (int64_t)blockIdx.x * 8 + wid; r < rows; r += (int64_t)gridDim.x * 8) {
-    const float *z = Z + (size_t)r * W;
-    float zv[PL], gh[PL], s1 = 0.0f;
-    float dy0 = 0.0f, dy1 = 0.0f, dy2 = 0.0f;
-    if (dy) {
-      dy0 = (float)dy[r * 3 + 0];
-      dy1 = (float)dy[r * 3 + 1];
-      dy2 = (float)dy[r * 3 + 2];
-    }
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      const int c = lane + 32 * k;
-      zv[k] = z[c];
-      s1 += zv[k];
-      gh[k] = dy ? fmaf(dy0, wo[k][0], fmaf(dy1, wo[k][1], dy2 * wo[k][2]))
-                 : dhp[(size_t)r * W + c] + gres[(size_t)r * W + c];
-    }
-    const float mean = warp_sumf(s1) * (1.0f / W);
-    float s2 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      const float d = zv[k] - mean;
-      s2 += d * d;
-    }
-    const float rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
-    float g[PL], xh[PL], m1 = 0.0f, m2 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      xh[k] = (zv[k] - mean) * rs;
-      const float a = xh[k] * gmf[k] + btf[k];
-      const float da = gh[k] * (a > 0.0f ? 1.0f : expf(a));
-      fg[k] = fmaf(da, xh[k], fg[k]);
-      fb[k] += da;
-      g[k] = da * gmf[k];
-      m1 += g[k];
-      m2 += g[k] * xh[k];
-    }
-    const float mm1 = warp_sumf(m1) * (1.0f / W), mm2 = warp_sumf(m2) * (1.0f / W);
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      const float d = rs * (g[k] - mm1 - xh[k] * mm2);
-      fd[k] += d;
-      gz[(size_t)r * W + lane + 32 * k] = d;
-    }
-    if (++nrow == 16) {
-      nrow = 0;
-#pragma unroll
-      for (int k = 0; k < PL; ++k) {
-        pg[k] += fg[k];
-        pb[k] += fb[k];
-        pd[k] += fd[k];
-        fg[k] = fb[k] = fd[k] = 0.0f;
-      }
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < PL; ++k) {
-    pg[k] += fg[k];
-    pb[k] += fb[k];
-    pd[k] += fd[k];
-    sacc[wid][0][lane + 32 * k] = pg[k];
-    sacc[wid][1][lane + 32 * k] = pb[k];
-    sacc[wid][2][lane + 32 * k] = pd[k];
-  }
-  __syncthreads();
-  double *out = part + (size_t)blockIdx.x * 3 * W;
-  for (int c = threadIdx.x; c < 3 * W; c += blockDim.x) {
-    const int q = c / W, cc = c % W;
-    double s = 0.0;
-    for (int w8 = 0; w8 < 8; ++w8) s += sacc[w8][q][cc];
-    out[c] = s;
   }
 }
 
@@ -392,16 +499,21 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
   // ---- forward ----
   GDFT_CK(launch_dm21_features(feat, ehf, n_grid, np, clip, S.squash_offset, x, u, e, st), "mlp_tc features");
   GDFT_CK(launch_pack_rt<double>(u, np, S.n_in, kDm21InPad, rt, 1, PU, st), "mlp_tc pack u");
+  // Each row pass also packs its h for the next dense layer (rt) and, with
+  // dparams, for that layer's weight gradient (ct).
   GDFT_CK(gemm_act(PU, 1, WTi(0), 1, 1, ZF), "mlp_tc dense_0");
-  l0_fwd_kernel<<<eblocks, 256, 0, st>>>(ZF, b0f, act, Wd, HF);
+  layer_fwd_pack_kernel<PL, true><<<kLnBlocks, 256, 0, st>>>(ZF, b0f, HF, nullptr, nullptr, 0.0, np,
+                                                             S.n_layers > 0 ? PH : nullptr,
+                                                             (dparams && S.n_layers > 0) ? CHi(0) : nullptr);
   GDFT_CK(cudaGetLastError(), "mlp_tc tanh");
   for (int i = 1; i <= S.n_layers; ++i) {
     const float *Wif = pf + tc_layer_offset(S, i - 1), *bi = Wif + (size_t)Wd * Wd, *gi = bi + Wd, *bei = gi + Wd;
-    GDFT_CK(launch_pack_rt<float>(HF, np, Wd, Wd, rt, kcw, PH, st), "mlp_tc pack h");
-    if (dparams) GDFT_CK(launch_pack_ct<float>(HF, np, Wd, Wd, ft, rc, CHi(i - 1), st), "mlp_tc pack h^T");
     float *Zi = ZF + (size_t)i * act;
     GDFT_CK(gemm_act(PH, kcw, WTi(i), kcw, kcw, Zi), "mlp_tc dense_i");
-    layer_fwd_kernel<PL><<<wblocks, 256, 0, st>>>(Zi, bi, HF, gi, bei, S.ln_eps, np);
+    const bool more = i < S.n_layers;
+    layer_fwd_pack_kernel<PL, false><<<kLnBlocks, 256, 0, st>>>(Zi, bi, HF, gi, bei, S.ln_eps, np,
+                                                                more ? PH : nullptr,
+                                                                (dparams && more) ? CHi(i) : nullptr);
     GDFT_CK(cudaGetLastError(), "mlp_tc layernorm");
   }
   const unsigned hblocks = (unsigned)((np + 255) / 256);
@@ -428,18 +540,19 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
     GDFT_CK(cudaGetLastError(), "mlp_tc head wgrad");
   }
   float *gz_cur = GZ, *gz_prev = GZ + act;
+  GDFT_CK(cudaFuncSetAttribute(layer_bwd_pack_kernel<PL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)bwd_pack_smem<PL>()),
+          "mlp_tc layernorm bwd smem");
   for (int i = S.n_layers; i >= 1; --i) {
     const float *Wif = pf + tc_layer_offset(S, i - 1), *gi = Wif + (size_t)Wd * Wd + Wd, *bei = gi + Wd;
     const float *Zi = ZF + (size_t)i * act;
     const bool last = i == S.n_layers;
-    layer_bwd_kernel<PL><<<kLnBlocks, 256, 0, st>>>(last ? nullptr : DHP, last ? nullptr : gz_prev,
-                                                    last ? dy : nullptr, Wof, Zi, gi, bei, S.ln_eps, np, gz_cur,
-                                                    lnpart);
+    layer_bwd_pack_kernel<PL><<<kLnBlocks, 256, bwd_pack_smem<PL>(), st>>>(last ? nullptr : DHP, last ? nullptr : gz_prev,
+                                                         last ? dy : nullptr, Wof, Zi, gi, bei, S.ln_eps, np,
+                                                         gz_cur, lnpart, PG, dparams ? CG : nullptr);
     GDFT_CK(cudaGetLastError(), "mlp_tc layernorm bwd");
-    GDFT_CK(launch_pack_rt<float>(gz_cur, np, Wd, Wd, rt, kcw, PG, st), "mlp_tc pack dz");
     if (dparams) {
       double *dWi = dparams + tc_layer_offset(S, i - 1);
-      GDFT_CK(launch_pack_ct<float>(gz_cur, np, Wd, Wd, ft, rc, CG, st), "mlp_tc pack dz^T");
       GDFT_CK(gemm_wgrad(CHi(i - 1), ft, Wd, CG, dWi), "mlp_tc dW_i");
       // [dgamma | dbeta | db] partials -> db, then (dgamma, dbeta) in the flat order (db, gamma, beta).
       colsum_final_kernel<<<(3 * Wd + 255) / 256, 256, 0, st>>>(lnpart, kLnBlocks, 3 * Wd, colpart2);

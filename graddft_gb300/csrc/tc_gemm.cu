@@ -58,6 +58,11 @@ constexpr uint32_t kScol = 384;
 
 __device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, code); }
 
+// Persistent over output tiles: CTA x takes tiles x, x + gridDim.x, ... of its
+// K split (blockIdx.y) with one continuous operand pipeline, so barrier and
+// TMEM set-up, pipeline fill and the drain of a tile's result overlap the next
+// tile's MMAs (the network's activation GEMMs have K = width, a few stages per
+// tile).
 __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -65,10 +70,10 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
   __shared__ uint32_t tmem_base;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int mt = blockIdx.x % A.m_tiles, nt = blockIdx.x / A.m_tiles;
+  const int ntiles = A.m_tiles * A.n_tiles;
   const int64_t c0 = (int64_t)blockIdx.y * A.chunks_per_split;
   const int64_t c1 = c0 + A.chunks_per_split < A.k_chunks ? c0 + A.chunks_per_split : A.k_chunks;
-  const int64_t nst = c1 > c0 ? c1 - c0 : 0;
+  const int64_t nst = c1 > c0 ? c1 - c0 : 0;  // K stages per tile
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -87,24 +92,30 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
   __syncthreads();
   umma::tc_fence_after();
   const uint32_t tbase = tmem_base;
-  const float *a_tile = A.a + (size_t)mt * A.a_chunks * (kOpBytes / 4);
-  const float *b_tile = A.b + (size_t)nt * A.b_chunks * (kOpBytes / 4);
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     // One thread issues the copies; its waits are bounded and single-threaded.
     if (lane == 0) {
       int64_t it = 0;
-      for (; it < nst; ++it) {
-        const int s = (int)(it % kStages);
-        if (!umma::mbar_wait(&empty[s], ((it / kStages) & 1) ^ 1)) {
-          flag(A.err, 41);
-          break;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int mt = tile % A.m_tiles, nt = tile / A.m_tiles;
+        const float *a_tile = A.a + (size_t)mt * A.a_chunks * (kOpBytes / 4);
+        const float *b_tile = A.b + (size_t)nt * A.b_chunks * (kOpBytes / 4);
+        for (int64_t k = 0; k < nst; ++k, ++it) {
+          const int s = (int)(it % kStages);
+          if (!umma::mbar_wait(&empty[s], ((it / kStages) & 1) ^ 1)) {
+            flag(A.err, 41);
+            ok = false;
+            break;
+          }
+          const int64_t kc = c0 + k;
+          umma::mbar_arrive_expect_tx(&full[s], kStageBytes);
+          umma::bulk_g2s(smem + s * kStageBytes, a_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
+          umma::bulk_g2s(smem + s * kStageBytes + kOpBytes, b_tile + (size_t)kc * (kOpBytes / 4), kOpBytes,
+                         &full[s]);
         }
-        const int64_t kc = c0 + it;
-        umma::mbar_arrive_expect_tx(&full[s], kStageBytes);
-        umma::bulk_g2s(smem + s * kStageBytes, a_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
-        umma::bulk_g2s(smem + s * kStageBytes + kOpBytes, b_tile + (size_t)kc * (kOpBytes / 4), kOpBytes, &full[s]);
       }
       // Our own copies land before the CTA can release shared memory.
       for (int64_t i = it > kStages ? it - kStages : 0; i < it; ++i)
@@ -124,28 +135,33 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
       const uint64_t dalo0 = umma::sdesc(sa0 + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
       const uint64_t dbhi0 = umma::sdesc(sa0 + kOpBytes, umma::kBlockLBO, umma::kBlockSBO);
       const uint64_t dblo0 = umma::sdesc(sa0 + kOpBytes + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
-      for (int64_t it = 0; it < nst; ++it) {
-        const int s = (int)(it % kStages);
-        const int buf = (int)(it % kWBufs);
-        if (!umma::mbar_wait(&wempty[buf], ((it / kWBufs) & 1) ^ 1) ||
-            !umma::mbar_wait(&full[s], (it / kStages) & 1)) {
-          flag(A.err, 43);
-          break;
+      int64_t it = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        for (int64_t k = 0; k < nst; ++k, ++it) {
+          const int s = (int)(it % kStages);
+          const int buf = (int)(it % kWBufs);
+          if (!umma::mbar_wait(&wempty[buf], ((it / kWBufs) & 1) ^ 1) ||
+              !umma::mbar_wait(&full[s], (it / kStages) & 1)) {
+            flag(A.err, 43);
+            ok = false;
+            break;
+          }
+          umma::tc_fence_after();
+          const uint32_t d = tbase + buf * 128;
+          const uint64_t so = (uint64_t)s * (kStageBytes >> 4);  // slot offset in the address field
+          const uint64_t ahi = dahi0 + so, alo = dalo0 + so, bhi = dbhi0 + so, blo = dblo0 + so;
+          // Products from the smallest up, the hi*hi ones last (the accumulator's
+          // truncation is relative to its size at each instruction).
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+            umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, kk == 0 ? 0u : 1u),
+                umma::mma_tf32(d, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(d, ahi + 16 * kk, bhi + 16 * kk, idesc, 1u);
+          umma::mma_commit(&empty[s]);
+          umma::mma_commit(&wfull[buf]);
         }
-        umma::tc_fence_after();
-        const uint32_t d = tbase + buf * 128;
-        const uint64_t so = (uint64_t)s * (kStageBytes >> 4);  // slot offset in the address field
-        const uint64_t ahi = dahi0 + so, alo = dalo0 + so, bhi = dbhi0 + so, blo = dblo0 + so;
-        // Products from the smallest up, the hi*hi ones last (the accumulator's
-        // truncation is relative to its size at each instruction).
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
-          umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, kk == 0 ? 0u : 1u),
-              umma::mma_tf32(d, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(d, ahi + 16 * kk, bhi + 16 * kk, idesc, 1u);
-        umma::mma_commit(&empty[s]);
-        umma::mma_commit(&wfull[buf]);
       }
       umma::mma_commit(&drain);
       if (!umma::mbar_wait(&drain, 0)) flag(A.err, 45);
@@ -153,63 +169,89 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
     __syncwarp();
   } else {
     // -------------------------------------------------------------- drains
+    // Per tile: every K stage's W is folded into the running sum S (TMEM) with
+    // Kahan compensation C in registers; after the tile's last stage S - C is
+    // written out and the next tile starts over.
     const int q = warp & 3, half = (warp - 2) >> 2;
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16) + half * 64;
-    float C[64];
-#pragma unroll
-    for (int i = 0; i < 64; ++i) C[i] = 0.0f;
     int64_t it = 0;
-    for (; it < nst; ++it) {
-      const int buf = (int)(it % kWBufs);
-      if (!umma::warp_wait(&wfull[buf], (it / kWBufs) & 1)) {
-        if (lane == 0) flag(A.err, 46);
-        break;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      const int mt = tile % A.m_tiles, nt = tile / A.m_tiles;
+      float C[64];
+#pragma unroll
+      for (int i = 0; i < 64; ++i) C[i] = 0.0f;
+      int64_t k = 0;
+      for (; k < nst; ++k, ++it) {
+        const int buf = (int)(it % kWBufs);
+        if (!umma::warp_wait(&wfull[buf], (it / kWBufs) & 1)) {
+          if (lane == 0) flag(A.err, 46);
+          ok = false;
+          break;
+        }
+        umma::tc_fence_after();
+#pragma unroll
+        for (int c = 0; c < 64; c += 16) {
+          uint32_t wr[16], sr[16];
+          umma::tmem_ld16_nowait(tl + buf * 128 + c, wr);
+          if (k > 0) umma::tmem_ld16_nowait(tl + kScol + c, sr);
+          umma::tmem_ld_wait(wr, sr);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            if (k == 0) {
+              sr[i] = wr[i];
+            } else {  // Kahan: S + (w - C)
+              const float sp = __uint_as_float(sr[i]);
+              const float y = __uint_as_float(wr[i]) - C[c + i];
+              const float t = sp + y;
+              C[c + i] = (t - sp) - y;
+              sr[i] = __float_as_uint(t);
+            }
+          }
+          umma::tmem_st16(tl + kScol + c, sr);
+        }
+        umma::tmem_st_wait();
+        umma::tc_fence_before();
+        umma::mbar_arrive(&wempty[buf]);
       }
-      umma::tc_fence_after();
+      const bool have = ok && k == nst && nst > 0;
+      const int m = mt * 128 + q * 32 + lane;
+      const int n0 = nt * 128 + half * 64;
 #pragma unroll
       for (int c = 0; c < 64; c += 32) {
-        uint32_t wr[32], sr[32];
-        umma::tmem_ld32_nowait(tl + buf * 128 + c, wr);
-        if (it > 0) umma::tmem_ld32_nowait(tl + kScol + c, sr);
-        umma::tmem_ld_wait(wr, sr);
         float sv[32];
+        if (have) umma::tmem_ld32(tl + kScol + c, sv);
+        if (m < A.m_valid) {
+          // Each lane owns one output row: whole 16-byte pieces where the row
+          // segment is in range and aligned (a lane's 32 values are 128 bytes).
+          if (A.out32) {
+            float *row = A.out32 + (size_t)m * A.ldo + n0 + c;
+            if (n0 + c + 32 <= A.n_valid && (A.ldo & 3) == 0) {
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const float w = __uint_as_float(wr[i]);
-          if (it == 0) {
-            sv[i] = w;
-          } else {  // Kahan: S + (w - C)
-            const float sp = __uint_as_float(sr[i]);
-            const float y = w - C[c + i];
-            const float t = sp + y;
-            C[c + i] = (t - sp) - y;
-            sv[i] = t;
+              for (int i = 0; i < 32; i += 4)
+                *reinterpret_cast<float4 *>(row + i) =
+                    have ? make_float4(sv[i] - C[c + i], sv[i + 1] - C[c + i + 1], sv[i + 2] - C[c + i + 2],
+                                       sv[i + 3] - C[c + i + 3])
+                         : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            } else {
+#pragma unroll
+              for (int i = 0; i < 32; ++i)
+                if (n0 + c + i < A.n_valid) row[i] = have ? sv[i] - C[c + i] : 0.0f;
+            }
+          } else {
+            double *row = A.out64 + ((size_t)blockIdx.y * A.m_valid + m) * A.n_valid + n0 + c;
+            if (n0 + c + 32 <= A.n_valid && (A.n_valid & 1) == 0) {
+#pragma unroll
+              for (int i = 0; i < 32; i += 2)
+                *reinterpret_cast<double2 *>(row + i) =
+                    have ? make_double2((double)sv[i] - (double)C[c + i], (double)sv[i + 1] - (double)C[c + i + 1])
+                         : make_double2(0.0, 0.0);
+            } else {
+#pragma unroll
+              for (int i = 0; i < 32; ++i)
+                if (n0 + c + i < A.n_valid) row[i] = have ? (double)sv[i] - (double)C[c + i] : 0.0;
+            }
           }
-        }
-        umma::tmem_st32(tl + kScol + c, sv);
-      }
-      umma::tmem_st_wait();
-      umma::tc_fence_before();
-      umma::mbar_arrive(&wempty[buf]);
-    }
-    const bool have = it == nst && nst > 0;
-    const int m = mt * 128 + q * 32 + lane;
-    const int n0 = nt * 128 + half * 64;
-#pragma unroll
-    for (int c = 0; c < 64; c += 32) {
-      float sv[32];
-      if (have) umma::tmem_ld32(tl + kScol + c, sv);
-      if (m < A.m_valid) {
-        if (A.out32) {
-          float *row = A.out32 + (size_t)m * A.ldo + n0 + c;
-#pragma unroll
-          for (int i = 0; i < 32; ++i)
-            if (n0 + c + i < A.n_valid) row[i] = have ? sv[i] - C[c + i] : 0.0f;
-        } else {
-          double *row = A.out64 + ((size_t)blockIdx.y * A.m_valid + m) * A.n_valid + n0 + c;
-#pragma unroll
-          for (int i = 0; i < 32; ++i)
-            if (n0 + c + i < A.n_valid) row[i] = have ? (double)sv[i] - (double)C[c + i] : 0.0;
         }
       }
     }
@@ -410,7 +452,18 @@ cudaError_t launch_tcg(const TcgArgs &a, int nsplit, cudaStream_t st) {
   if (a.m_tiles <= 0 || a.n_tiles <= 0 || nsplit <= 0 || (a.out32 == nullptr) == (a.out64 == nullptr) ||
       (a.out32 && nsplit != 1) || a.k_chunks > a.a_chunks || a.k_chunks > a.b_chunks)
     return cudaErrorInvalidValue;
-  dim3 grid(a.m_tiles * a.n_tiles, nsplit);
+  // One CTA per SM in all (each holds all 512 TMEM columns); the tiles of a split are shared out.
+  static int n_sm = 0;
+  if (n_sm == 0) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+  }
+  const int tiles = a.m_tiles * a.n_tiles;
+  int gx = n_sm / nsplit;
+  gx = gx < 1 ? 1 : (gx > tiles ? tiles : gx);
+  dim3 grid(gx, nsplit);
   tcg_kernel<<<grid, kThreads, kSmemBytes, st>>>(a);
   return cudaGetLastError();
 }
