@@ -469,15 +469,18 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
     a.m_tiles = m_tiles;
     a.n_tiles = ft;
     a.a_chunks = a.b_chunks = a.k_chunks = rc;
-    a.chunks_per_split = (rc + L.nsplit - 1) / L.nsplit;
+    // L.nsplit CTAs in all: the output tiles of one K range run side by side
+    // and share its operand chunks through L2.
+    const int ns = L.nsplit / (m_tiles * ft) > 1 ? L.nsplit / (m_tiles * ft) : 1;
+    a.chunks_per_split = (rc + ns - 1) / ns;
     a.out64 = kpart;
     a.m_valid = m_valid;
     a.n_valid = Wd;
     a.err = err;
-    cudaError_t r = launch_tcg(a, L.nsplit, st);
+    cudaError_t r = launch_tcg(a, ns, st);
     if (r != cudaSuccess) return r;
     const size_t total = (size_t)m_valid * Wd;
-    sum_splits_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(kpart, L.nsplit, total, out);
+    sum_splits_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(kpart, ns, total, out);
     return cudaGetLastError();
   };
   const unsigned wblocks = (unsigned)((np * 32 + 255) / 256);  // one warp per row

@@ -62,7 +62,9 @@ __device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, cod
 // K split (blockIdx.y) with one continuous operand pipeline, so barrier and
 // TMEM set-up, pipeline fill and the drain of a tile's result overlap the next
 // tile's MMAs (the network's activation GEMMs have K = width, a few stages per
-// tile).
+// tile).  Tile t is (m = t / n_tiles, n = t % n_tiles): the column tiles of one
+// row tile run on neighbouring CTAs at about the same time and read its A
+// chunks once from memory, the second time from L2.
 __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -100,7 +102,7 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
       int64_t it = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int mt = tile % A.m_tiles, nt = tile / A.m_tiles;
+        const int mt = tile / A.n_tiles, nt = tile % A.n_tiles;
         const float *a_tile = A.a + (size_t)mt * A.a_chunks * (kOpBytes / 4);
         const float *b_tile = A.b + (size_t)nt * A.b_chunks * (kOpBytes / 4);
         for (int64_t k = 0; k < nst; ++k, ++it) {
@@ -177,7 +179,7 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
     int64_t it = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      const int mt = tile % A.m_tiles, nt = tile / A.m_tiles;
+      const int mt = tile / A.n_tiles, nt = tile % A.n_tiles;
       float C[64];
 #pragma unroll
       for (int i = 0; i < 64; ++i) C[i] = 0.0f;
