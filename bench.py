@@ -175,8 +175,8 @@ NEURAL_WORKLOAD = ("synthetic neural functional (DM21-style network, 6 x 256, 11
 
 def _neural_launches(n_layers: int) -> int:
     """Kernels one mixed neural step launches (the sequence in mlp_tc.cu plus the two contractions):
-    weight packing 2 + 2n, forward 6 + 2n, backward 11 + 5n, density 2 and V_xc 3."""
-    return (2 + 2 * n_layers) + (6 + 2 * n_layers) + (11 + 5 * n_layers) + 5
+    weight packing 2 + 2n, forward 6 + 2n, backward 5 + 5n, density 2 and V_xc 3."""
+    return (2 + 2 * n_layers) + (6 + 2 * n_layers) + (5 + 5 * n_layers) + 5
 
 
 def run_neural(args):

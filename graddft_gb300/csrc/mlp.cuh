@@ -77,7 +77,7 @@ int mlp_hvp_f64(const MlpShape &S, const double *params, double *dparams, const 
 struct MlpTcLayout {
   size_t bytes;
   size_t x, u, e, dy, de, du, epart, kpart, lnpart, colpart, colpart2;            // FP64 regions (byte offsets)
-  size_t pf, dyf, pu, cu, wt, wr, zf, hf, ph, ch, gz, dhp, pg, cg;               // FP32 regions (byte offsets)
+  size_t pf, dyf, pu, wt, wr, zf, hf, ph, ch, gz, dhp, pg, cg;                   // FP32 regions (byte offsets)
   int nsplit;
 };
 MlpTcLayout mlp_tc_layout(const MlpShape &s, int64_t np);

@@ -111,12 +111,27 @@ __global__ void colsum_part_kernel(const double *__restrict__ X, int64_t rows, i
   }
 }
 
-__global__ void colsum_final_kernel(const double *__restrict__ part, int nparts, int ncols, double *__restrict__ out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncols) return;
+// out[c] = sum over b of part[b][c]: one block of 8 warps per 32 columns, each
+// warp sums an interleaved slice of the parts, warp 0 adds the eight in order.
+__global__ void __launch_bounds__(256) colsum_final_kernel(const double *__restrict__ part, int nparts, int ncols,
+                                                           double *__restrict__ out) {
+  __shared__ double ws[8][32];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * 32 + lane;
   double s = 0.0;
-  for (int b = 0; b < nparts; ++b) s += part[(size_t)b * ncols + c];
-  out[c] = s;
+  if (c < ncols)
+    for (int b = wid; b < nparts; b += 8) s += part[(size_t)b * ncols + c];
+  ws[wid][lane] = s;
+  __syncthreads();
+  if (wid == 0 && c < ncols) {
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t += ws[w][lane];
+    out[c] = t;
+  }
+}
+inline void launch_colsum_final(const double *part, int nparts, int ncols, double *out, cudaStream_t st) {
+  colsum_final_kernel<<<(ncols + 31) / 32, 256, 0, st>>>(part, nparts, ncols, out);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -151,7 +166,7 @@ inline cudaError_t gemm_tn_split(int M, int N, int64_t K, const double *A, int l
 inline cudaError_t col_sums(const double *X, int64_t rows, int ncols, int ld, double *out, double *part, int nparts,
                             cudaStream_t st) {
   colsum_part_kernel<<<nparts, 256, 0, st>>>(X, rows, ncols, ld, part);
-  colsum_final_kernel<<<(ncols + 255) / 256, 256, 0, st>>>(part, nparts, ncols, out);
+  launch_colsum_final(part, nparts, ncols, out, st);
   return cudaGetLastError();
 }
 
@@ -195,12 +210,24 @@ __global__ void head_wgrad_part_kernel(const float *__restrict__ H, const float 
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     for (int64_t rb = r0; rb < r1; rb += 16) {  // FP32 over 16 rows, FP64 across
       float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
-      const int64_t re = rb + 16 < r1 ? rb + 16 : r1;
-      for (int64_t r = rb; r < re; ++r) {
-        const float hv = H[(size_t)r * width + c];
-        f0 = fmaf(hv, dyf[r * 3 + 0], f0);
-        f1 = fmaf(hv, dyf[r * 3 + 1], f1);
-        f2 = fmaf(hv, dyf[r * 3 + 2], f2);
+      if (rb + 16 <= r1) {  // all 16 rows' loads issued together
+        float hv[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) hv[j] = H[(size_t)(rb + j) * width + c];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int64_t r = rb + j;
+          f0 = fmaf(hv[j], dyf[r * 3 + 0], f0);
+          f1 = fmaf(hv[j], dyf[r * 3 + 1], f1);
+          f2 = fmaf(hv[j], dyf[r * 3 + 2], f2);
+        }
+      } else {
+        for (int64_t r = rb; r < r1; ++r) {
+          const float hv = H[(size_t)r * width + c];
+          f0 = fmaf(hv, dyf[r * 3 + 0], f0);
+          f1 = fmaf(hv, dyf[r * 3 + 1], f1);
+          f2 = fmaf(hv, dyf[r * 3 + 2], f2);
+        }
       }
       a0 += f0;
       a1 += f1;

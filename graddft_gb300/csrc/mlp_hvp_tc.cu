@@ -447,8 +447,7 @@ int run_hvp_tc(const MlpShape &S, const double *params, double *dparams, const d
   // ---- reverse of the augmented graph ----
   if (dparams) {
     head_wgrad_part_kernel<<<kColBlocks, 256, 0, st>>>(H, GYf, GY, rows2, np, Wd, colpart);
-    colsum_final_kernel<<<(3 * Wd + 3 + 255) / 256, 256, 0, st>>>(colpart, kColBlocks, 3 * Wd + 3,
-                                                                  dparams + head_off);
+    launch_colsum_final(colpart, kColBlocks, 3 * Wd + 3, dparams + head_off, st);
     GDFT_CK(cudaGetLastError(), "hvp_tc head wgrad");
   }
   float *gz_cur = GZ, *gz_prev = GZ + act2;
@@ -465,7 +464,7 @@ int run_hvp_tc(const MlpShape &S, const double *params, double *dparams, const d
       double *dWi = dparams + hvp_tc_layer_offset(S, i - 1);
       GDFT_CK(launch_pack_ct<float>(gz_cur, rows2, Wd, Wd, ft, rc2, CG, st), "hvp_tc pack dz^T");
       GDFT_CK(gemm_wgrad(CHi(i - 1), ft, Wd, CG, dWi), "hvp_tc dW_i");
-      colsum_final_kernel<<<(3 * Wd + 255) / 256, 256, 0, st>>>(lnpart, kLnBlocks, 3 * Wd, colpart2);
+      launch_colsum_final(lnpart, kLnBlocks, 3 * Wd, colpart2, st);
       GDFT_CK(cudaGetLastError(), "hvp_tc ln sums");
       GDFT_CK(cudaMemcpyAsync(dWi + (size_t)Wd * Wd, colpart2 + 2 * Wd, Wd * sizeof(double),
                               cudaMemcpyDeviceToDevice, st),
@@ -486,7 +485,7 @@ int run_hvp_tc(const MlpShape &S, const double *params, double *dparams, const d
     GDFT_CK(launch_pack_ct<float>(gz_cur, rows2, Wd, Wd, ft, rc2, CG, st), "hvp_tc pack dz0^T");
     GDFT_CK(gemm_wgrad(CU, 1, S.n_in, CG, dparams), "hvp_tc dW_0");
     colsum_f32_part_kernel<<<kColBlocks, 256, 0, st>>>(gz_cur, np, Wd, colpart);
-    colsum_final_kernel<<<(Wd + 255) / 256, 256, 0, st>>>(colpart, kColBlocks, Wd, dparams + (size_t)S.n_in * Wd);
+    launch_colsum_final(colpart, kColBlocks, Wd, dparams + (size_t)S.n_in * Wd, st);
     GDFT_CK(cudaGetLastError(), "hvp_tc db0");
   }
   if (coef) {

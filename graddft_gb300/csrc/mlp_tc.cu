@@ -361,13 +361,102 @@ __global__ void __launch_bounds__(256) head_kernel(const float *__restrict__ H, 
   }
 }
 
-// Layer 0 reverse: dz0 = (dhp + gres) (1 - tanh(z0)^2), FP32.
-__global__ void l0_bwd_kernel(const float *__restrict__ dhp, const float *__restrict__ gres,
-                              const float *__restrict__ Z0, size_t total, float *__restrict__ gz) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= total) return;
-  const float h = tanhf(Z0[i]);
-  gz[i] = (dhp[i] + gres[i]) * (1.0f - h * h);
+// Layer 0 reverse fused with everything that consumes it.  dz0 = (dhp + gres)
+// (1 - tanh(z0)^2) (FP32; the residual layer above passes dhp = dz_1 W_1^T and
+// gres = dz_1) is formed per 32-row tile and not stored; from it
+//   du[r][j] = sum_c dz0[r][c] W0[j][c]            (du != null; FP32 lane
+//                                                   products, FP64 warp sums)
+//   part[block][j][c] = sum_r u[r][j] dz0[r][c]    (j < n_in: dW0)
+//   part[block][n_in][c] = sum_r dz0[r][c]         (db0)
+// with the parameter sums in FP32 over 16 rows, then FP64, one thread per
+// column.  Dynamic shared memory: l0_bwd_smem<PL>() bytes.
+template <int PL>
+constexpr size_t l0_bwd_smem() {
+  return sizeof(float) * (kRowTile * (32 * PL + 4) + kRowTile * kDm21InPad + kDm21InPad * 32 * PL);
+}
+
+template <int PL>
+__global__ void __launch_bounds__(256, 2) l0_bwd_fused_kernel(const float *__restrict__ dhp,
+                                                           const float *__restrict__ gres,
+                                                           const float *__restrict__ Z0, const double *__restrict__ u,
+                                                           const float *__restrict__ W0, int n_in, int64_t rows,
+                                                           double *__restrict__ du, double *__restrict__ part) {
+  constexpr int W = 32 * PL, LD = W + 4, NJ = kDm21InPad + 1;
+  extern __shared__ __align__(16) unsigned char l0_smem[];
+  float *tile = reinterpret_cast<float *>(l0_smem);  // [32][LD] dz0
+  float *uf = tile + kRowTile * LD;                   // [32][kDm21InPad] u (FP32)
+  float *w0s = uf + kRowTile * kDm21InPad;            // [kDm21InPad][W] W0, zero rows past n_in
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < kDm21InPad * W; i += blockDim.x) w0s[i] = i / W < n_in ? W0[i] : 0.0f;
+  const int c = threadIdx.x;  // column of the parameter sums (c < W)
+  double acc[NJ];
+  float fac[NJ];
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) acc[j] = fac[j] = 0.0f;
+  __syncthreads();
+  for (int64_t r0 = (int64_t)blockIdx.x * kRowTile; r0 < rows; r0 += (int64_t)gridDim.x * kRowTile) {
+    float g[4][PL], z[4][PL];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const size_t base = (size_t)(r0 + wid * 4 + i) * W;
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const int cc = lane + 32 * k;
+        g[i][k] = dhp[base + cc] + gres[base + cc];
+        z[i][k] = Z0[base + cc];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int rr = wid * 4 + i;
+      const int64_t r = r0 + rr;
+      float d[PL];
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const float h = tanhf(z[i][k]);
+        d[k] = g[i][k] * (1.0f - h * h);
+        tile[rr * LD + lane + 32 * k] = d[k];
+      }
+      if (lane < kDm21InPad) uf[rr * kDm21InPad + lane] = lane < n_in ? (float)u[r * kDm21InPad + lane] : 0.0f;
+      if (du) {
+        for (int j = 0; j < kDm21InPad; ++j) {
+          double sj = 0.0;
+          if (j < n_in) {
+            float sf = 0.0f;
+#pragma unroll
+            for (int k = 0; k < PL; ++k) sf = fmaf(d[k], w0s[j * W + lane + 32 * k], sf);
+            sj = (double)warp_sumf(sf);
+          }
+          if (lane == 0) du[(size_t)r * kDm21InPad + j] = sj;
+        }
+      }
+    }
+    __syncthreads();
+    if (part && c < W) {
+#pragma unroll 4
+      for (int rr = 0; rr < kRowTile; ++rr) {
+        const float gv = tile[rr * LD + c];
+#pragma unroll
+        for (int j = 0; j < kDm21InPad; ++j) fac[j] = fmaf(uf[rr * kDm21InPad + j], gv, fac[j]);
+        fac[kDm21InPad] += gv;
+        if ((rr & 15) == 15) {
+#pragma unroll
+          for (int j = 0; j < NJ; ++j) {
+            acc[j] += fac[j];
+            fac[j] = 0.0f;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (part && c < W) {
+    double *out = part + (size_t)blockIdx.x * (n_in + 1) * W;
+#pragma unroll
+    for (int j = 0; j < kDm21InPad; ++j)
+      if (j < n_in) out[(size_t)j * W + c] = acc[j];
+    out[(size_t)n_in * W + c] = acc[kDm21InPad];
+  }
 }
 
 // Per-segment energies from the 256-row energy partials (Kahan), the loss and
@@ -424,7 +513,7 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
   double *x = d64(L.x), *u = d64(L.u), *e = d64(L.e), *dy = d64(L.dy), *de = d64(L.de), *du = d64(L.du);
   double *epart = d64(L.epart), *kpart = d64(L.kpart), *lnpart = d64(L.lnpart), *colpart = d64(L.colpart);
   double *colpart2 = d64(L.colpart2);
-  float *PU = f32(L.pu), *CU = f32(L.cu), *WT = f32(L.wt), *WR = f32(L.wr), *ZF = f32(L.zf), *HF = f32(L.hf);
+  float *PU = f32(L.pu), *WT = f32(L.wt), *WR = f32(L.wr), *ZF = f32(L.zf), *HF = f32(L.hf);
   float *PH = f32(L.ph), *CH = f32(L.ch), *GZ = f32(L.gz), *DHP = f32(L.dhp), *PG = f32(L.pg), *CG = f32(L.cg);
   const size_t act = (size_t)np * Wd;
   const int64_t rt = np / kPointTile, rc = np / 32;  // row tiles, row chunks
@@ -483,8 +572,6 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
     sum_splits_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(kpart, ns, total, out);
     return cudaGetLastError();
   };
-  const unsigned wblocks = (unsigned)((np * 32 + 255) / 256);  // one warp per row
-  const unsigned eblocks = (unsigned)((act + 255) / 256);
 
   // ---- weights: packed once per call ----
   {
@@ -538,8 +625,7 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
   // ---- backward ----
   if (dparams) {
     head_wgrad_part_kernel<<<kColBlocks, 256, 0, st>>>(HF, dyf, dy, np, np, Wd, colpart);
-    colsum_final_kernel<<<(3 * Wd + 3 + 255) / 256, 256, 0, st>>>(colpart, kColBlocks, 3 * Wd + 3,
-                                                                  dparams + head_off);
+    launch_colsum_final(colpart, kColBlocks, 3 * Wd + 3, dparams + head_off, st);
     GDFT_CK(cudaGetLastError(), "mlp_tc head wgrad");
   }
   float *gz_cur = GZ, *gz_prev = GZ + act;
@@ -558,7 +644,7 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
       double *dWi = dparams + tc_layer_offset(S, i - 1);
       GDFT_CK(gemm_wgrad(CHi(i - 1), ft, Wd, CG, dWi), "mlp_tc dW_i");
       // [dgamma | dbeta | db] partials -> db, then (dgamma, dbeta) in the flat order (db, gamma, beta).
-      colsum_final_kernel<<<(3 * Wd + 255) / 256, 256, 0, st>>>(lnpart, kLnBlocks, 3 * Wd, colpart2);
+      launch_colsum_final(lnpart, kLnBlocks, 3 * Wd, colpart2, st);
       GDFT_CK(cudaGetLastError(), "mlp_tc ln sums");
       GDFT_CK(cudaMemcpyAsync(dWi + (size_t)Wd * Wd, colpart2 + 2 * Wd, Wd * sizeof(double),
                               cudaMemcpyDeviceToDevice, st),
@@ -572,23 +658,22 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
     gz_cur = gz_prev;
     gz_prev = t;
   }
-  // Layer 0: gz_prev holds dE/dz_1, DHP its product with W_1^T.
-  l0_bwd_kernel<<<eblocks, 256, 0, st>>>(DHP, gz_prev, ZF, act, gz_cur);
+  // Layer 0: gz_prev holds dE/dz_1, DHP its product with W_1^T.  One pass
+  // gives du and the FP64 partials of [dW0 | db0] (kpart is free by now and
+  // holds kLnBlocks x (n_in + 1) x W doubles: 4 (n_in + 1) <= W).
+  GDFT_CK(cudaFuncSetAttribute(l0_bwd_fused_kernel<PL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)l0_bwd_smem<PL>()),
+          "mlp_tc tanh bwd smem");
+  l0_bwd_fused_kernel<PL><<<kLnBlocks, 256, l0_bwd_smem<PL>(), st>>>(DHP, gz_prev, ZF, u, W0f, S.n_in, np,
+                                                                    coef ? du : nullptr, dparams ? kpart : nullptr);
   GDFT_CK(cudaGetLastError(), "mlp_tc tanh bwd");
   if (dparams) {
-    GDFT_CK(launch_pack_ct<double>(u, np, S.n_in, kDm21InPad, 1, rc, CU, st), "mlp_tc pack u^T");
-    GDFT_CK(launch_pack_ct<float>(gz_cur, np, Wd, Wd, ft, rc, CG, st), "mlp_tc pack dz0^T");
-    GDFT_CK(gemm_wgrad(CU, 1, S.n_in, CG, dparams), "mlp_tc dW_0");
-    colsum_f32_part_kernel<<<kColBlocks, 256, 0, st>>>(gz_cur, np, Wd, colpart);
-    colsum_final_kernel<<<(Wd + 255) / 256, 256, 0, st>>>(colpart, kColBlocks, Wd, dparams + (size_t)S.n_in * Wd);
-    GDFT_CK(cudaGetLastError(), "mlp_tc db0");
+    launch_colsum_final(kpart, kLnBlocks, (S.n_in + 1) * Wd, dparams, st);
+    GDFT_CK(cudaGetLastError(), "mlp_tc dW_0");
   }
-  if (coef) {
-    du_kernel<PL><<<wblocks, 256, 0, st>>>(gz_cur, W0f, S.n_in, np, du);
-    GDFT_CK(cudaGetLastError(), "mlp_tc du");
+  if (coef)
     GDFT_CK(launch_dm21_potentials(feat, x, du, de, n_grid, np, clip, S.squash_offset, coef, st),
             "mlp_tc potentials");
-  }
 #undef GDFT_CK
   return GDFT_OK;
 }
@@ -624,7 +709,6 @@ MlpTcLayout mlp_tc_layout(const MlpShape &s, int64_t np) {
   L.pf = take(mlp_param_count(s) * 4);
   L.dyf = take((size_t)np * 3 * 4);
   L.pu = take((size_t)rt * kBlk * 4);
-  L.cu = take((size_t)rc * kBlk * 4);
   L.wt = take(((size_t)ft * kBlk + (size_t)s.n_layers * ft * kcw * kBlk) * 4);
   L.wr = take((size_t)(s.n_layers > 0 ? s.n_layers : 1) * ft * kcw * kBlk * 4);
   L.zf = take(act * (s.n_layers + 1) * 4);
