@@ -160,11 +160,20 @@ __global__ void __launch_bounds__(256) layer_fwd_pack_kernel(float *__restrict__
 // dE/dh is dy W_out^T (last layer: dy != null) or dhp + gres (the GEMM output
 // plus the residual branch of the layer above).  Writes dE/dz (FP32) and
 // per-block partial sums [block][3][W] of dE/dgamma, dE/dbeta and dE/db
-// (= sum dz): FP32 over 16 rows of a warp at a time, then FP64.
+// (= sum dz): FP32 over 16 rows of a warp at a time, then Kahan-compensated
+// FP32 per warp, FP64 across the block's warps.
 // rows is a multiple of 32; part has gridDim.x blocks of [3][W].
 template <int PL>
 constexpr size_t bwd_pack_smem() {
-  return sizeof(double) * 8 * 3 * (32 * PL) + sizeof(float) * kRowTile * (32 * PL + 4);
+  return sizeof(float2) * 8 * 3 * (32 * PL) + sizeof(float) * kRowTile * (32 * PL + 4);
+}
+
+// Kahan step on a (total, compensation) pair: total + (v - compensation).
+__device__ __forceinline__ void kahan_add(float2 &a, float v) {
+  const float y = v - a.y;
+  const float t = a.x + y;
+  a.y = (t - a.x) - y;
+  a.x = t;
 }
 
 template <int PL>
@@ -174,11 +183,12 @@ __global__ void __launch_bounds__(256, 2) layer_bwd_pack_kernel(
     const float *__restrict__ bet, double eps, int64_t rows, float *__restrict__ gz, double *__restrict__ part,
     float *__restrict__ rt_out, float *__restrict__ ct_out) {
   constexpr int W = 32 * PL, LD = W + 4;
-  // Dynamic shared memory (bwd_pack_smem<PL>() bytes): per-warp FP64 sums of
-  // dgamma, dbeta, db, then the row tile.
+  // Dynamic shared memory (bwd_pack_smem<PL>() bytes): per-warp Kahan sums
+  // (total, compensation) of dgamma, dbeta, db in FP32 (GB300's FP64 rate is a
+  // small fraction of its FP32 rate), then the row tile.
   extern __shared__ __align__(16) unsigned char bwd_smem[];
-  double(*sacc)[3][W] = reinterpret_cast<double(*)[3][W]>(bwd_smem);
-  float *tile = reinterpret_cast<float *>(bwd_smem + sizeof(double) * 8 * 3 * W);
+  float2(*sacc)[3][W] = reinterpret_cast<float2(*)[3][W]>(bwd_smem);
+  float *tile = reinterpret_cast<float *>(bwd_smem + sizeof(float2) * 8 * 3 * W);
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float gmf[PL], btf[PL];
 #pragma unroll
@@ -186,7 +196,7 @@ __global__ void __launch_bounds__(256, 2) layer_bwd_pack_kernel(
     const int c = lane + 32 * k;
     gmf[k] = gam[c];
     btf[k] = bet[c];
-    sacc[wid][0][c] = sacc[wid][1][c] = sacc[wid][2][c] = 0.0;
+    sacc[wid][0][c] = sacc[wid][1][c] = sacc[wid][2][c] = make_float2(0.0f, 0.0f);
   }
   float fg[PL], fb[PL], fd[PL];
 #pragma unroll
@@ -252,14 +262,14 @@ __global__ void __launch_bounds__(256, 2) layer_bwd_pack_kernel(
         }
       }
     }
-    if (++ntile == 4) {  // 16 rows per warp: FP32 partials into the FP64 sums
+    if (++ntile == 4) {  // 16 rows per warp: FP32 partials into the Kahan sums
       ntile = 0;
 #pragma unroll
       for (int k = 0; k < PL; ++k) {
         const int c = lane + 32 * k;
-        sacc[wid][0][c] += fg[k];
-        sacc[wid][1][c] += fb[k];
-        sacc[wid][2][c] += fd[k];
+        kahan_add(sacc[wid][0][c], fg[k]);
+        kahan_add(sacc[wid][1][c], fb[k]);
+        kahan_add(sacc[wid][2][c], fd[k]);
         fg[k] = fb[k] = fd[k] = 0.0f;
       }
     }
@@ -270,16 +280,16 @@ __global__ void __launch_bounds__(256, 2) layer_bwd_pack_kernel(
 #pragma unroll
   for (int k = 0; k < PL; ++k) {
     const int c = lane + 32 * k;
-    sacc[wid][0][c] += fg[k];
-    sacc[wid][1][c] += fb[k];
-    sacc[wid][2][c] += fd[k];
+    kahan_add(sacc[wid][0][c], fg[k]);
+    kahan_add(sacc[wid][1][c], fb[k]);
+    kahan_add(sacc[wid][2][c], fd[k]);
   }
   __syncthreads();
   double *out = part + (size_t)blockIdx.x * 3 * W;
   for (int c = threadIdx.x; c < 3 * W; c += blockDim.x) {
     const int q = c / W, cc = c % W;
     double sum = 0.0;
-    for (int w8 = 0; w8 < 8; ++w8) sum += sacc[w8][q][cc];
+    for (int w8 = 0; w8 < 8; ++w8) sum += (double)sacc[w8][q][cc].x - (double)sacc[w8][q][cc].y;
     out[c] = sum;
   }
 }
@@ -368,8 +378,9 @@ __global__ void __launch_bounds__(256) head_kernel(const float *__restrict__ H, 
 //                                                   products, FP64 warp sums)
 //   part[block][j][c] = sum_r u[r][j] dz0[r][c]    (j < n_in: dW0)
 //   part[block][n_in][c] = sum_r dz0[r][c]         (db0)
-// with the parameter sums in FP32 over 16 rows, then FP64, one thread per
-// column.  Dynamic shared memory: l0_bwd_smem<PL>() bytes.
+// with the parameter sums in FP32 over 16 rows, then Kahan-compensated FP32
+// per block (FP64 partials out), one thread per column.  Dynamic shared
+// memory: l0_bwd_smem<PL>() bytes.
 template <int PL>
 constexpr size_t l0_bwd_smem() {
   return sizeof(float) * (kRowTile * (32 * PL + 4) + kRowTile * kDm21InPad + kDm21InPad * 32 * PL);
@@ -389,10 +400,11 @@ __global__ void __launch_bounds__(256, 2) l0_bwd_fused_kernel(const float *__res
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i < kDm21InPad * W; i += blockDim.x) w0s[i] = i / W < n_in ? W0[i] : 0.0f;
   const int c = threadIdx.x;  // column of the parameter sums (c < W)
-  double acc[NJ];
-  float fac[NJ];
+  // FP32 sums over 16 rows (fac) folded into Kahan-compensated FP32 totals
+  // (acc, comp): GB300's FP64 rate is a small fraction of its FP32 rate.
+  float acc[NJ], comp[NJ], fac[NJ];
 #pragma unroll
-  for (int j = 0; j < NJ; ++j) acc[j] = fac[j] = 0.0f;
+  for (int j = 0; j < NJ; ++j) acc[j] = comp[j] = fac[j] = 0.0f;
   __syncthreads();
   for (int64_t r0 = (int64_t)blockIdx.x * kRowTile; r0 < rows; r0 += (int64_t)gridDim.x * kRowTile) {
     float g[4][PL], z[4][PL];
@@ -420,14 +432,14 @@ __global__ void __launch_bounds__(256, 2) l0_bwd_fused_kernel(const float *__res
       if (lane < kDm21InPad) uf[rr * kDm21InPad + lane] = lane < n_in ? (float)u[r * kDm21InPad + lane] : 0.0f;
       if (du) {
         for (int j = 0; j < kDm21InPad; ++j) {
-          double sj = 0.0;
+          float sj = 0.0f;
           if (j < n_in) {
             float sf = 0.0f;
 #pragma unroll
             for (int k = 0; k < PL; ++k) sf = fmaf(d[k], w0s[j * W + lane + 32 * k], sf);
-            sj = (double)warp_sumf(sf);
+            sj = warp_sumf(sf);
           }
-          if (lane == 0) du[(size_t)r * kDm21InPad + j] = sj;
+          if (lane == 0) du[(size_t)r * kDm21InPad + j] = (double)sj;
         }
       }
     }
@@ -441,8 +453,11 @@ __global__ void __launch_bounds__(256, 2) l0_bwd_fused_kernel(const float *__res
         fac[kDm21InPad] += gv;
         if ((rr & 15) == 15) {
 #pragma unroll
-          for (int j = 0; j < NJ; ++j) {
-            acc[j] += fac[j];
+          for (int j = 0; j < NJ; ++j) {  // Kahan: acc + (fac - comp)
+            const float y = fac[j] - comp[j];
+            const float t = acc[j] + y;
+            comp[j] = (t - acc[j]) - y;
+            acc[j] = t;
             fac[j] = 0.0f;
           }
         }
@@ -454,8 +469,8 @@ __global__ void __launch_bounds__(256, 2) l0_bwd_fused_kernel(const float *__res
     double *out = part + (size_t)blockIdx.x * (n_in + 1) * W;
 #pragma unroll
     for (int j = 0; j < kDm21InPad; ++j)
-      if (j < n_in) out[(size_t)j * W + c] = acc[j];
-    out[(size_t)n_in * W + c] = acc[kDm21InPad];
+      if (j < n_in) out[(size_t)j * W + c] = (double)acc[j] - (double)comp[j];
+    out[(size_t)n_in * W + c] = (double)acc[kDm21InPad] - (double)comp[kDm21InPad];
   }
 }
 

@@ -180,9 +180,12 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
       const int mt = tile / A.n_tiles, nt = tile % A.n_tiles;
-      float C[64];
+      // Compensations of this thread's 64 columns as 32 packed FP32 pairs: the
+      // fold runs on add/sub.rn.f32x2, two columns per instruction, each
+      // rounded exactly like the scalar operation.
+      uint64_t C2[32];
 #pragma unroll
-      for (int i = 0; i < 64; ++i) C[i] = 0.0f;
+      for (int i = 0; i < 32; ++i) C2[i] = 0ull;
       int64_t k = 0;
       for (; k < nst; ++k, ++it) {
         const int buf = (int)(it % kWBufs);
@@ -198,25 +201,33 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
           umma::tmem_ld16_nowait(tl + buf * 128 + c, wr);
           if (k > 0) umma::tmem_ld16_nowait(tl + kScol + c, sr);
           umma::tmem_ld_wait(wr, sr);
+          if (k > 0) {
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            if (k == 0) {
-              sr[i] = wr[i];
-            } else {  // Kahan: S + (w - C)
-              const float sp = __uint_as_float(sr[i]);
-              const float y = __uint_as_float(wr[i]) - C[c + i];
-              const float t = sp + y;
-              C[c + i] = (t - sp) - y;
-              sr[i] = __float_as_uint(t);
+            for (int i = 0; i < 16; i += 2) {  // Kahan: S + (w - C)
+              const uint64_t sp = umma::pk2(sr[i], sr[i + 1]);
+              const uint64_t y = umma::sub2(umma::pk2(wr[i], wr[i + 1]), C2[(c + i) / 2]);
+              const uint64_t t = umma::add2(sp, y);
+              C2[(c + i) / 2] = umma::sub2(umma::sub2(t, sp), y);
+              umma::unpk2(t, sr[i], sr[i + 1]);
             }
+            umma::tmem_st16(tl + kScol + c, sr);
+          } else {
+            umma::tmem_st16(tl + kScol + c, wr);
           }
-          umma::tmem_st16(tl + kScol + c, sr);
         }
         umma::tmem_st_wait();
         umma::tc_fence_before();
         umma::mbar_arrive(&wempty[buf]);
       }
       const bool have = ok && k == nst && nst > 0;
+      float C[64];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        uint32_t lo, hi;
+        umma::unpk2(C2[i], lo, hi);
+        C[2 * i] = __uint_as_float(lo);
+        C[2 * i + 1] = __uint_as_float(hi);
+      }
       const int m = mt * 128 + q * 32 + lane;
       const int n0 = nt * 128 + half * 64;
 #pragma unroll
