@@ -53,7 +53,7 @@ EXPORTS = (
     "gdft_umma_probe", "gdft_network_param_count", "gdft_neural_workspace_bytes",
     "gdft_neural_xc_energy_and_grads", "gdft_neural_inputs", "gdft_network_apply_workspace_bytes",
     "gdft_network_apply", "gdft_neural_hvp_workspace_bytes", "gdft_neural_xc_hvp", "gdft_tc_gemm_probe",
-    "gdft_tc_gemm3_probe", "gdft_neural_batch_workspace_bytes", "gdft_neural_batch_xc",
+    "gdft_tc_gemm3_probe", "gdft_neural_batch_workspace_bytes", "gdft_neural_batch_xc", "gdft_neural_batch_status",
     "gdft_xc_energy_grads_hf", "gdft_hf_workspace_bytes", "gdft_hf_energy_density", "gdft_hf_fock",
     "gdft_fock_add_hf", "gdft_neural_xc_hf_grads", "gdft_hf_workspace_bytes_form", "gdft_hf_energy_density_form",
     "gdft_hf_fock_form", "gdft_hf_device_status", "gdft_selftest_wait_expiry", "gdft_chunked_workspace_bytes",
@@ -186,6 +186,7 @@ _SIGS = {
     "gdft_tc_gemm3_probe": ([I32, I32, I32, I32, P, P, P], ctypes.c_int),
     "gdft_neural_batch_workspace_bytes": ([I32, P, PNET, ctypes.POINTER(SZ)], ctypes.c_int),
     "gdft_neural_batch_xc": ([I32, P, P, P, PNET, P, P, P, P, P, P, P, SZ, P], ctypes.c_int),
+    "gdft_neural_batch_status": ([P, SZ, ctypes.POINTER(I32), P], ctypes.c_int),
     "gdft_profile_enable": ([I32], ctypes.c_int),
     "gdft_profile_reset": ([], ctypes.c_int),
     "gdft_profile_read": ([I32, ctypes.POINTER(D), ctypes.POINTER(I64)], ctypes.c_int),

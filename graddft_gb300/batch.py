@@ -51,12 +51,7 @@ class NeuralBatch:
         nbytes = ctypes.c_size_t()
         check(_lib.load().gdft_neural_batch_workspace_bytes(n, self.descs, ctypes.byref(self.net.desc),
                                                             ctypes.byref(nbytes)))
-        self.ws = torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device)
-        # Each molecule's own workspace sits at the running sum of the workspace sizes.
-        self._ws_off, off = [], 0
-        for r in self.residents:
-            self._ws_off.append(off)
-            off += r.ws.numel()
+        self.ws = torch.zeros(nbytes.value, dtype=torch.uint8, device=self.device)  # error word 0
         ptrs = lambda ts: (ctypes.c_void_p * n)(*[t.data_ptr() for t in ts])  # noqa: E731
         self._h_rdm1, self._h_ehf, self._h_vxc = ptrs(self.rdm1), ptrs(self.ehf), ptrs(self.vxc)
         self.use_eref = False
@@ -107,10 +102,9 @@ class NeuralBatch:
         return self.loss, self.energies, self.vxc, self.dparams
 
     def status(self) -> int:
-        """Synchronise and raise if a kernel of the batch recorded an expired bounded wait."""
+        """Synchronise and raise if a kernel of the batch recorded an expired bounded wait (the batch
+        workspace's persistent error word, where every molecule's stages and the network fold theirs)."""
         st = ctypes.c_int32()
-        base = self.ws.data_ptr()
-        for r, off in zip(self.residents, self._ws_off):
-            check(_lib.load().gdft_device_status(ctypes.byref(r.desc), ctypes.c_void_p(base + off), r.ws.numel(),
-                                                 ctypes.byref(st), engine._stream(self.device)))
+        check(_lib.load().gdft_neural_batch_status(engine._ptr(self.ws), self.ws.numel(), ctypes.byref(st),
+                                                   engine._stream(self.device)))
         return st.value

@@ -267,11 +267,14 @@ __global__ void write_seg_kernel(const SegTable t, int n, int64_t *__restrict__ 
 
 // Batch workspace: each molecule's own workspace, then the concatenated point
 // arrays (segments padded to 256 rows) and the network scratch.
+// Batch workspace: [256 B persistent error word][one molecule region, sized
+// for the largest molecule and used by each molecule in turn: the density and
+// V_xc stages run one molecule after another on the caller's stream][joint
+// features, weights, ehf, coefficients, segments, cotangents][network].
 struct BatchLayout {
-  size_t mol_off[kBatchMax];
   int64_t seg[kBatchMax + 1];
   int64_t npt;
-  size_t off_feat, off_w, off_ehf, off_coef, off_seg, off_cot, off_net, bytes;
+  size_t off_mol, off_feat, off_w, off_ehf, off_coef, off_seg, off_cot, off_net, bytes;
 };
 
 static int batch_layout(int n_mol, const gdft_molecule *mols, const gdft_network *net, BatchLayout *B) {
@@ -279,16 +282,18 @@ static int batch_layout(int n_mol, const gdft_molecule *mols, const gdft_network
     set_error("batch of %d molecules (1..%d supported)", n_mol, kBatchMax);
     return GDFT_ERR_INVALID;
   }
-  size_t off = 0;
+  size_t off = 256, mol_bytes = 0;
   int64_t npt = 0;
   for (int m = 0; m < n_mol; ++m) {
     int rc = check_mol(&mols[m]);
     if (rc) return rc;
-    B->mol_off[m] = off;
-    off += align256(ws_layout(&mols[m]).bytes);
+    const size_t b = align256(ws_layout(&mols[m]).bytes);
+    mol_bytes = b > mol_bytes ? b : mol_bytes;
     B->seg[m] = npt;
     npt += round_up(mols[m].n_grid_pad, 256);
   }
+  B->off_mol = off;
+  off += mol_bytes;
   B->seg[n_mol] = npt;
   B->npt = npt;
   B->off_feat = off;
@@ -353,6 +358,27 @@ static int run_vxc(const gdft_molecule *mol, const double *coef, double *d_vxc, 
                                     mol->n_ao, (float *)(ws + W.off_q), W.n_vsplit, vpart, d_vxc,
                                     (int *)(ws + W.off_err), st),
                     "vxc_q_tc");
+}
+
+// The error word at the start of a chunked or batch workspace: read, cleared,
+// reported.
+static int persistent_status(const char *name, void *d_ws, size_t ws_bytes, int32_t *status, void *stream) {
+  if (d_ws == nullptr || ws_bytes < 256 || status == nullptr) {
+    set_error("%s: invalid arguments", name);
+    return GDFT_ERR_INVALID;
+  }
+  int h = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc;
+  if ((rc = check_cuda(cudaMemcpyAsync(&h, d_ws, sizeof(int), cudaMemcpyDeviceToHost, st), "status read"))) return rc;
+  if ((rc = check_cuda(cudaStreamSynchronize(st), "status sync"))) return rc;
+  if ((rc = check_cuda(cudaMemsetAsync(d_ws, 0, sizeof(int), st), "status clear"))) return rc;
+  *status = h;
+  if (h != 0) {
+    set_error("a device-side wait expired (code %d); results of the last calls are invalid", h);
+    return GDFT_ERR_DEVICE;
+  }
+  return GDFT_OK;
 }
 
 extern "C" {
@@ -1116,12 +1142,19 @@ int gdft_neural_batch_xc(int32_t n_mol, const gdft_molecule *mols, const double 
       (rc = check_cuda(cudaMemsetAsync(w, 0, (size_t)npt * 8, st), "batch clear")) ||
       (rc = check_cuda(cudaMemsetAsync(ehf, 0, (size_t)4 * npt * 8, st), "batch clear")))
     return rc;
+  int *batch_err = (int *)ws;
+  char *wsm = ws + B.off_mol;  // the shared molecule region
+  // A molecule's error word sits where its own layout puts it in the shared
+  // region: cleared before the molecule's stage (a previous molecule's data may
+  // lie there) and folded into the batch's word after it.
+  auto mol_err = [&](const gdft_molecule *mol) { return (int *)(wsm + ws_layout(mol).off_err); };
   for (int m = 0; m < n_mol; ++m) {
     const gdft_molecule *mol = &mols[m];
-    char *wsm = ws + B.mol_off[m];
     const WsLayout W = ws_layout(mol);
     const int64_t np = mol->n_grid_pad, off = B.seg[m];
+    if ((rc = check_cuda(cudaMemsetAsync(mol_err(mol), 0, sizeof(int), st), "batch error word"))) return rc;
     if ((rc = run_density(mol, h_rdm1[m], wsm, st))) return rc;
+    if ((rc = check_cuda(launch_err_fold(batch_err, mol_err(mol), st), "batch error fold"))) return rc;
     if ((rc = check_cuda(cudaMemcpy2DAsync(feat + off, (size_t)npt * 8, wsm + W.off_feat, (size_t)np * 8,
                                            (size_t)np * 8, 2 * kFeat, cudaMemcpyDeviceToDevice, st),
                          "batch features")) ||
@@ -1136,22 +1169,27 @@ int gdft_neural_batch_xc(int32_t n_mol, const gdft_molecule *mols, const double 
   {
     StageTimer tm(GDFT_STAGE_MLP, st);
     rc = mlp_run_tc(net_shape(net), d_params, d_dparams, feat, ehf, w, npt, npt, net->clip, ws + B.off_net, nullptr,
-                    coef, (int *)(ws + B.mol_off[0] + ws_layout(&mols[0]).off_err), st, &sg);
+                    coef, batch_err, st, &sg);
     if (rc) return rc;
   }
   for (int m = 0; m < n_mol; ++m) {
     if (h_vxc == nullptr || h_vxc[m] == nullptr) continue;
     const gdft_molecule *mol = &mols[m];
-    char *wsm = ws + B.mol_off[m];
     const WsLayout W = ws_layout(mol);
     const int64_t np = mol->n_grid_pad, off = B.seg[m];
-    if ((rc = check_cuda(cudaMemcpy2DAsync(wsm + W.off_coef, (size_t)np * 8, coef + off, (size_t)npt * 8,
+    if ((rc = check_cuda(cudaMemsetAsync(mol_err(mol), 0, sizeof(int), st), "batch error word")) ||
+        (rc = check_cuda(cudaMemcpy2DAsync(wsm + W.off_coef, (size_t)np * 8, coef + off, (size_t)npt * 8,
                                            (size_t)np * 8, 2 * kFeat, cudaMemcpyDeviceToDevice, st),
                          "batch coefficients")))
       return rc;
     if ((rc = run_vxc(mol, (const double *)(wsm + W.off_coef), h_vxc[m], wsm, st))) return rc;
+    if ((rc = check_cuda(launch_err_fold(batch_err, mol_err(mol), st), "batch error fold"))) return rc;
   }
   return GDFT_OK;
+}
+
+int gdft_neural_batch_status(void *d_ws, size_t ws_bytes, int32_t *status, void *stream) {
+  return persistent_status("gdft_neural_batch_status", d_ws, ws_bytes, status, stream);
 }
 
 int gdft_vxc_from_potentials(const gdft_molecule *mol, const double *d_pot, double *d_vxc, void *d_ws,
@@ -1527,22 +1565,7 @@ int gdft_neural_xc_energy_and_grads_chunked(const gdft_basis *shells, const doub
 }
 
 int gdft_chunked_status(void *d_ws, size_t ws_bytes, int32_t *status, void *stream) {
-  if (d_ws == nullptr || ws_bytes < 256 || status == nullptr) {
-    set_error("gdft_chunked_status: invalid arguments");
-    return GDFT_ERR_INVALID;
-  }
-  int h = 0;
-  cudaStream_t st = (cudaStream_t)stream;
-  int rc;
-  if ((rc = check_cuda(cudaMemcpyAsync(&h, d_ws, sizeof(int), cudaMemcpyDeviceToHost, st), "status read"))) return rc;
-  if ((rc = check_cuda(cudaStreamSynchronize(st), "status sync"))) return rc;
-  if ((rc = check_cuda(cudaMemsetAsync(d_ws, 0, sizeof(int), st), "status clear"))) return rc;
-  *status = h;
-  if (h != 0) {
-    set_error("a device-side wait expired (code %d); results of the last calls are invalid", h);
-    return GDFT_ERR_DEVICE;
-  }
-  return GDFT_OK;
+  return persistent_status("gdft_chunked_status", d_ws, ws_bytes, status, stream);
 }
 
 }  // extern "C"

@@ -367,7 +367,10 @@ int gdft_neural_xc_hvp(const gdft_molecule *mol, const double *d_rdm1, const gdf
                        const double *d_params, const double *d_ehf, const double *d_tangent, double *d_value,
                        double *d_hrdm1, double *d_hparams, void *d_ws, size_t ws_bytes, void *stream);
 
-/* Workspace bytes of gdft_neural_batch_xc for these molecules. */
+/* Workspace bytes of gdft_neural_batch_xc for these molecules: a persistent
+ * error word, ONE molecule region sized for the largest molecule (the
+ * molecules' density and V_xc stages run one after another on the stream and
+ * share it), the joint per-point arrays and the network's scratch. */
 int gdft_neural_batch_workspace_bytes(int32_t n_mol, const gdft_molecule *mols, const gdft_network *net,
                                       size_t *bytes);
 
@@ -387,6 +390,12 @@ int gdft_neural_batch_xc(int32_t n_mol, const gdft_molecule *mols, const double 
                          const double *const *h_ehf, const gdft_network *net, const double *d_params,
                          const double *d_eref, double *d_energies, double *d_loss, double *const *h_vxc,
                          double *d_dparams, void *d_ws, size_t ws_bytes, void *stream);
+
+/* Synchronises the stream and reads (then clears) the batch workspace's
+ * persistent error word, where every molecule's and the network's expired
+ * bounded waits of gdft_neural_batch_xc calls are folded; GDFT_ERR_DEVICE with
+ * *status = the first code if one expired.  No counterpart in the reference. */
+int gdft_neural_batch_status(void *d_ws, size_t ws_bytes, int32_t *status, void *stream);
 
 /* The DM21 network inputs and energy densities of a molecule: d_cinputs
  * (grid, 11) = dm21_combine_cinputs(dm21_coefficient_inputs(...), ehf)

@@ -88,3 +88,30 @@ def test_batch_graph_replay(G):
     assert all(torch.equal(a, c) for a, c in zip(v_graph, v_eager))
     assert torch.equal(d_graph, d_eager)
     assert b.status() == 0
+
+
+def test_batch_status_reports_a_recorded_expiry(G):
+    """The batch's persistent error word: a code recorded there (planted from the host, as an expired
+    bounded wait would leave it) is reported once by status() and then cleared."""
+    from graddft_gb300 import _lib
+    from graddft_gb300.batch import NeuralBatch
+
+    mols = _molecules(G, SHAPES[:2])
+    f = _dm21(G)
+    b = NeuralBatch(mols, f)
+    b.step(f.init(5))
+    assert b.status() == 0
+    b.ws[:4].copy_(torch.tensor([46, 0, 0, 0], dtype=torch.uint8))
+    with pytest.raises(_lib.GdftError):
+        b.status()
+    assert b.status() == 0
+    # The shared molecule region is the largest molecule's, not the sum over the batch.
+    import ctypes
+
+    one = []
+    for r in b.residents:
+        nb = ctypes.c_size_t()
+        _lib.check(_lib.load().gdft_neural_batch_workspace_bytes(1, ctypes.byref(r.desc), ctypes.byref(b.net.desc),
+                                                                 ctypes.byref(nb)))
+        one.append(nb.value)
+    assert b.ws.numel() < sum(one)
