@@ -274,6 +274,176 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
   if (warp == 1) umma::tmem_dealloc(tbase, kTmemCols);
 }
 
+// ------------------------------------------------------------- tcgw_kernel
+// Single-split FP32-output form for an even number of column tiles (the
+// network's activation GEMMs, K = width): a CTA owns a 128 x 256 output tile
+// (column tiles 2p, 2p + 1), so each stage copies the A chunk once for both
+// halves (A hi|lo + two B hi|lo = 96 KB, two stages) and issues 24 MMAs.
+// TMEM holds two W buffers per half (all 512 columns); the running sum of each
+// drain thread's 128 columns stays in registers and takes each stage's W with
+// a round-to-nearest FP32 add (unbiased; at K = width the few folds keep it
+// within the FP32 rounding of the stored activations, while the tensor core's
+// truncating accumulation still never spans more than one 32-wide K chunk).
+// Drain warps 2-5 take half 0, warps 6-9 half 1 (TMEM lane quadrant warp % 4).
+constexpr int kStagesW = 2;
+constexpr uint32_t kStageWBytes = 3 * kOpBytes;  // A, B half 0, B half 1 (hi|lo each)
+constexpr int kSmemWBytes = kStagesW * kStageWBytes + 1024;
+
+__global__ void __launch_bounds__(kThreads, 1) tcgw_kernel(const TcgArgs A) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full[kStagesW], empty[kStagesW], wfull[2][2], wempty[2][2], drain;
+  __shared__ uint32_t tmem_base;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int npairs = A.n_tiles / 2;
+  const int ntiles = A.m_tiles * npairs;
+  const int64_t nst = A.k_chunks;  // K stages per tile
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStagesW; ++s) {
+      umma::mbar_init(&full[s], 1);
+      umma::mbar_init(&empty[s], 1);
+    }
+    for (int h = 0; h < 2; ++h)
+      for (int b = 0; b < 2; ++b) {
+        umma::mbar_init(&wfull[h][b], 1);
+        umma::mbar_init(&wempty[h][b], 128);
+      }
+    umma::mbar_init(&drain, 1);
+    umma::fence_barrier_init();
+  }
+  if (warp == 1) umma::tmem_alloc(&tmem_base, kTmemCols);
+  umma::tc_fence_before();
+  __syncthreads();
+  umma::tc_fence_after();
+  const uint32_t tbase = tmem_base;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      int64_t it = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int mt = tile / npairs, np2 = tile % npairs;
+        const float *a_tile = A.a + (size_t)mt * A.a_chunks * (kOpBytes / 4);
+        const float *b_tile = A.b + (size_t)(2 * np2) * A.b_chunks * (kOpBytes / 4);
+        for (int64_t k = 0; k < nst; ++k, ++it) {
+          const int s = (int)(it % kStagesW);
+          if (!umma::mbar_wait(&empty[s], ((it / kStagesW) & 1) ^ 1)) {
+            flag(A.err, 51);
+            ok = false;
+            break;
+          }
+          unsigned char *slot = smem + s * kStageWBytes;
+          umma::mbar_arrive_expect_tx(&full[s], kStageWBytes);
+          umma::bulk_g2s(slot, a_tile + (size_t)k * (kOpBytes / 4), kOpBytes, &full[s]);
+          umma::bulk_g2s(slot + kOpBytes, b_tile + (size_t)k * (kOpBytes / 4), kOpBytes, &full[s]);
+          umma::bulk_g2s(slot + 2 * kOpBytes, b_tile + (size_t)(A.b_chunks + k) * (kOpBytes / 4), kOpBytes,
+                         &full[s]);
+        }
+      }
+      for (int64_t i = it > kStagesW ? it - kStagesW : 0; i < it; ++i)
+        if (!umma::mbar_wait(&full[i % kStagesW], (i / kStagesW) & 1)) flag(A.err, 52);
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------------------------------------------------- MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = umma::idesc_tf32(128, 128);
+      const uint32_t sa0 = umma::smem_u32(smem);
+      const uint64_t dahi0 = umma::sdesc(sa0, umma::kBlockLBO, umma::kBlockSBO);
+      const uint64_t dalo0 = umma::sdesc(sa0 + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
+      int64_t it = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        for (int64_t k = 0; k < nst; ++k, ++it) {
+          const int s = (int)(it % kStagesW), buf = (int)(it & 1);
+          if (!umma::mbar_wait(&full[s], (it / kStagesW) & 1)) {
+            flag(A.err, 53);
+            ok = false;
+            break;
+          }
+          const uint64_t so = (uint64_t)s * (kStageWBytes >> 4);  // slot offset in the address field
+          const uint64_t ahi = dahi0 + so, alo = dalo0 + so;
+          for (int h = 0; h < 2 && ok; ++h) {
+            if (!umma::mbar_wait(&wempty[h][buf], ((it >> 1) & 1) ^ 1)) {
+              flag(A.err, 54);
+              ok = false;
+              break;
+            }
+            umma::tc_fence_after();
+            const uint32_t sb = sa0 + s * kStageWBytes + (1 + h) * kOpBytes;
+            const uint64_t bhi = umma::sdesc(sb, umma::kBlockLBO, umma::kBlockSBO);
+            const uint64_t blo = umma::sdesc(sb + umma::kBlockBytes, umma::kBlockLBO, umma::kBlockSBO);
+            const uint32_t d = tbase + (2 * h + buf) * 128;
+            // Products from the smallest up, the hi*hi ones last.
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+              umma::mma_tf32(d, ahi + 16 * kk, blo + 16 * kk, idesc, kk == 0 ? 0u : 1u),
+                  umma::mma_tf32(d, alo + 16 * kk, bhi + 16 * kk, idesc, 1u);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) umma::mma_tf32(d, ahi + 16 * kk, bhi + 16 * kk, idesc, 1u);
+            umma::mma_commit(&wfull[h][buf]);
+          }
+          umma::mma_commit(&empty[s]);
+        }
+      }
+      umma::mma_commit(&drain);
+      if (!umma::mbar_wait(&drain, 0)) flag(A.err, 55);
+    }
+    __syncwarp();
+  } else {
+    // -------------------------------------------------------------- drains
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16) + 2 * h * 128;
+    int64_t it = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      const int mt = tile / npairs, np2 = tile % npairs;
+      float S[128];
+      int64_t k = 0;
+      for (; k < nst; ++k, ++it) {
+        const int buf = (int)(it & 1);
+        if (!umma::warp_wait(&wfull[h][buf], (it >> 1) & 1)) {
+          if (lane == 0) flag(A.err, 56);
+          ok = false;
+          break;
+        }
+        umma::tc_fence_after();
+#pragma unroll
+        for (int c = 0; c < 128; c += 16) {
+          uint32_t wr[16];
+          umma::tmem_ld16_nowait(tl + buf * 128 + c, wr);
+          umma::tmem_ld_wait(wr);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) S[c + i] = k == 0 ? __uint_as_float(wr[i]) : S[c + i] + __uint_as_float(wr[i]);
+        }
+        umma::tc_fence_before();
+        umma::mbar_arrive(&wempty[h][buf]);
+      }
+      if (!ok || k != nst) break;
+      const int m = mt * 128 + q * 32 + lane;
+      const int n0 = (2 * np2 + h) * 128;
+      if (m < A.m_valid) {
+        float *row = A.out32 + (size_t)m * A.ldo + n0;
+        if (n0 + 128 <= A.n_valid && (A.ldo & 3) == 0) {
+#pragma unroll
+          for (int i = 0; i < 128; i += 4)
+            *reinterpret_cast<float4 *>(row + i) = make_float4(S[i], S[i + 1], S[i + 2], S[i + 3]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 128; ++i)
+            if (n0 + i < A.n_valid) row[i] = S[i];
+        }
+      }
+    }
+  }
+  umma::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) umma::tmem_dealloc(tbase, kTmemCols);
+}
+
 __global__ void __launch_bounds__(kThreads, 1) tcg3_kernel(const TcgArgs A) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -472,6 +642,17 @@ cudaError_t launch_tcg(const TcgArgs &a, int nsplit, cudaStream_t st) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
+  }
+  if (a.out32 && a.n_tiles % 2 == 0 && a.k_chunks > 0) {  // 128 x 256 output tiles, sums in registers
+    static bool attr_w = false;
+    if (!attr_w) {
+      cudaError_t e = cudaFuncSetAttribute(tcgw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemWBytes);
+      if (e != cudaSuccess) return e;
+      attr_w = true;
+    }
+    const int wtiles = a.m_tiles * (a.n_tiles / 2);
+    tcgw_kernel<<<wtiles < n_sm ? wtiles : n_sm, kThreads, kSmemWBytes, st>>>(a);
+    return cudaGetLastError();
   }
   const int tiles = a.m_tiles * a.n_tiles;
   int gx = n_sm / nsplit;
