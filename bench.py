@@ -592,8 +592,9 @@ def run_stream(args):
 
 def run_batch_full(args):
     """Config 4 at its stated grid, N = 1500 n_ao (rounded to 128): 64 molecules, n_ao ~ U[24, 400], the DM21
-    network (6 x 256), loss sum_m (E_m - E_ref)^2; each molecule's AO tables recomputed per grid chunk (one
-    workspace shared by all molecules, chunk size from the autotuner); E, V_xc and dE/dtheta per molecule."""
+    network (6 x 256), loss sum_m (E_m - E_ref)^2; each molecule's AO tables recomputed per grid chunk (chunk
+    size from the autotuner); E, V_xc and dE/dtheta per molecule.  Timed one molecule at a time (one workspace
+    shared by all) and side by side on --streams CUDA streams (the reported value)."""
     import torch
 
     from graddft_gb300 import build, engine, synthetic
@@ -622,7 +623,7 @@ def run_batch_full(args):
     dps = torch.empty((n_mol, net.n_params), dtype=torch.float64, device=dev)
     e_ref = torch.zeros(n_mol, dtype=torch.float64, device=dev)
 
-    def step():
+    def step_one_at_a_time():
         for i, (r, d, ehf) in enumerate(mols):
             r.neural_xc_energy_and_grads(d, net, flat, ehf, want_vxc=True, want_dparams=True, exc_out=exc[i],
                                          vxc_out=vx[i], dparams_out=dps[i])
@@ -630,22 +631,43 @@ def run_batch_full(args):
         g = 2.0 * (exc - e_ref)
         return (g[:, None] * dps).sum(0)
 
-    step()  # tunes the chunk size per AO bucket (timed once, cached on disk)
+    step_one_at_a_time()  # tunes the chunk size per AO bucket (timed once, cached on disk)
     e_ref = exc + 0.01 * torch.randn(n_mol, dtype=torch.float64, generator=torch.Generator().manual_seed(SEED)).to(dev)
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    for r, _, _ in mols:
-        r.status()
     stream = torch.cuda.current_stream(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with Clocks(0) as clk:
+
+    def timed(step, clk=None):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(args.steps):
             step()
         e1.record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+        return e0.elapsed_time(e1) / args.steps
+
+    ms_one = timed(step_one_at_a_time)
+    for r, _, _ in mols:
+        r.status()
+    # The same molecules side by side on CUDA streams, longest first to the least-loaded stream, one
+    # workspace pool per stream (graddft_gb300.batch.ChunkedBatch).
+    from graddft_gb300.batch import ChunkedBatch
+
+    pool.clear()  # the one-at-a-time workspace; each stream gets its own
+    torch.cuda.empty_cache()
+    batch = ChunkedBatch([r for r, _, _ in mols], n_streams=args.streams)
+    rdm1s, ehfs = [d for _, d, _ in mols], [e for _, _, e in mols]
+
+    def step():
+        batch.neural_xc_energy_and_grads(rdm1s, net, flat, ehfs, exc, vx, dps)
+        g = 2.0 * (exc - e_ref)
+        return (g[:, None] * dps).sum(0)
+
+    with Clocks(0) as clk:
+        ms = timed(step)
+    batch.status()
+    pool = {i: w for i, p in enumerate(batch.pools) for w in p.values()}
     n_pts = sum(r.n_grid for r, _, _ in mols)
     line = {
         "metric": "batched training step molecules/s at the full config-4 grid (AO tables recomputed per chunk)",
@@ -655,8 +677,11 @@ def run_batch_full(args):
         "config": {"workload": f"batched step, {n_mol} molecules, n_ao ~ U[24, 400], n_grid = "
                                f"{args.points_per_ao} n_ao, DM21 network 6 x 256", "n_mol": n_mol,
                    "n_ao_range": [int(naos.min()), int(naos.max())], "grid_points_total": n_pts,
-                   "chunks": sorted({int(r.chunk) for r, _, _ in mols})},
+                   "chunks": sorted({int(r.chunk) for r, _, _ in mols}), "streams": len(batch.streams)},
         "grid_pts_per_s": n_pts / (ms * 1e-3), "device_bytes_workspace": sum(w.numel() for w in pool.values()),
+        "one_at_a_time": {"ms_per_step": ms_one, "molecules_per_s": n_mol / (ms_one * 1e-3),
+                          "grid_pts_per_s": n_pts / (ms_one * 1e-3)},
+        "streams_over_one_at_a_time": ms_one / ms,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -1002,6 +1027,7 @@ def main():
     ap.add_argument("--chunk", type=int, default=None,
                     help="grid points per chunk of --workload stream / batch_full (default: the autotuner's choice)")
     ap.add_argument("--points-per-ao", type=int, default=150, help="grid points per AO (--workload batch)")
+    ap.add_argument("--streams", type=int, default=3, help="CUDA streams of --workload batch_full")
     ap.add_argument("--cycles", type=int, default=20, help="SCF iterations (--workload scf)")
     ap.add_argument("--loop", default="simple", choices=["simple", "diis"],
                     help="--workload scf: linear density mixing (diff_simple_scf_loop) or CDIIS (diff_scf_loop)")

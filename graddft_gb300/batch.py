@@ -1,4 +1,6 @@
-"""Batches of molecules of different sizes in one device call, capturable in a CUDA graph.
+"""Batches of molecules of different sizes: in one device call, capturable in a CUDA graph
+(``NeuralBatch``, resident AO tables), or side by side on several CUDA streams with the AO
+tables recomputed per grid chunk (``ChunkedBatch``).
 
 A training step over a dataset (train.py:34-218 applied to every molecule,
 loss sum_m (E_m - E_ref_m)^2) becomes one ``gdft_neural_batch_xc`` call: each
@@ -108,3 +110,81 @@ class NeuralBatch:
         check(_lib.load().gdft_neural_batch_status(engine._ptr(self.ws), self.ws.numel(), ctypes.byref(st),
                                                    engine._stream(self.device)))
         return st.value
+
+
+class ChunkedBatch:
+    """Molecules whose AO tables are recomputed per grid chunk (``engine.ChunkedResident``), evaluated side
+    by side on several CUDA streams.
+
+    One molecule at a time leaves most SMs idle for the small ones (the chunk of a 24-AO molecule is a few
+    dozen 128-point tiles per contraction).  The molecules are dealt longest first (cost n_grid * n_ao^2,
+    the contractions' work) to the stream with the least cost queued so far; the molecules of one stream
+    run one after another there and share that stream's workspace pool.  A step makes every stream wait
+    for the caller's stream first and the caller's stream wait for all of them at the end, so it orders
+    like any single-stream call.  Molecules whose chunk size is still "auto" are tuned on the caller's
+    stream the first time (their timing must not overlap other work).
+    """
+
+    def __init__(self, residents: Sequence[engine.ChunkedResident], n_streams: int = 3):
+        if not residents:
+            raise ValueError("a batch needs at least one molecule")
+        if n_streams < 1:
+            raise ValueError(f"n_streams must be positive, got {n_streams}")
+        self.residents = list(residents)
+        self.device = self.residents[0].device
+        n_streams = min(n_streams, len(self.residents))
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(n_streams)]
+        self.pools = [{} for _ in range(n_streams)]
+        self.assignment = schedule_longest_first([r.n_grid * r.n_ao ** 2 for r in self.residents], n_streams)
+        for s, idxs in enumerate(self.assignment):
+            for i in idxs:
+                self.residents[i].use_workspace_pool(self.pools[s])
+
+    def neural_xc_energy_and_grads(self, rdm1s, net: engine.Network, flat_params, ehfs, exc_out: torch.Tensor,
+                                   vxc_outs=None, dparams_out: Optional[torch.Tensor] = None):
+        """E_m into exc_out[m], V_xc of molecule m into vxc_outs[m] (or none), dE_m/dtheta into row m of
+        dparams_out (or none), for every molecule, on the streams."""
+        n = len(self.residents)
+        if exc_out.shape != (n,):
+            raise ValueError(f"exc_out must be ({n},), got {tuple(exc_out.shape)}")
+        want_v, want_d = vxc_outs is not None, dparams_out is not None
+
+        def call(i):
+            self.residents[i].neural_xc_energy_and_grads(
+                rdm1s[i], net, flat_params, ehfs[i], want_vxc=want_v, want_dparams=want_d, exc_out=exc_out[i],
+                vxc_out=vxc_outs[i] if want_v else None, dparams_out=dparams_out[i] if want_d else None)
+
+        done = set()
+        for i, r in enumerate(self.residents):  # chunk sizes still to tune: alone, on the caller's stream
+            if r.chunk == "auto":
+                call(i)
+                done.add(i)
+        caller = torch.cuda.current_stream(self.device)
+        for stream, idxs in zip(self.streams, self.assignment):
+            stream.wait_stream(caller)
+            with torch.cuda.stream(stream):
+                for i in idxs:
+                    if i not in done:
+                        call(i)
+        for stream in self.streams:
+            caller.wait_stream(stream)
+        return exc_out, vxc_outs, dparams_out
+
+    def status(self) -> int:
+        """Synchronise and raise if a kernel of any molecule recorded an expired bounded wait."""
+        st = 0
+        for r in self.residents:
+            st = r.status() or st
+        return st
+
+
+def schedule_longest_first(costs: Sequence[float], n_streams: int) -> list:
+    """Indices dealt to n_streams queues: longest first, each to the queue with the least cost so far (ties to
+    the lowest queue), the order within a queue the dealing order."""
+    queues = [[] for _ in range(n_streams)]
+    load = [0.0] * n_streams
+    for i in sorted(range(len(costs)), key=lambda j: (-costs[j], j)):
+        q = min(range(n_streams), key=lambda k: (load[k], k))
+        queues[q].append(i)
+        load[q] += costs[i]
+    return queues

@@ -352,6 +352,11 @@ class ChunkedResident:
     def _basis_args(self):
         return (None if self._desc is None else ctypes.byref(self._desc)), _ptr(self._rows)
 
+    def use_workspace_pool(self, pool: dict) -> None:
+        """Take workspaces from ``pool`` from now on (molecules that share a pool must run one after another
+        on one stream; ``batch.ChunkedBatch`` gives each of its streams its own)."""
+        self._ws = pool
+
     def workspace_bytes(self, chunk: int, net: Optional["Network"] = None) -> int:
         nbytes = ctypes.c_size_t()
         check(_lib.load().gdft_chunked_workspace_bytes(self.n_ao, int(chunk), PRECISIONS[self.precision],

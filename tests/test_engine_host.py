@@ -204,3 +204,14 @@ def test_chunk_autotuner_times_once_and_caches(monkeypatch, tmp_path):
     timed.clear()
     assert autotune.choose("small", run, ws, n_grid=5000, device=None, budget_bytes=1 << 40) == 5120
     assert set(timed) == {5120}
+
+
+def test_longest_first_schedule():
+    from graddft_gb300.batch import schedule_longest_first
+
+    q = schedule_longest_first([5, 1, 3, 3, 2, 8], 2)
+    assert q == [[5, 3], [0, 2, 4, 1]]
+    assert schedule_longest_first([1.0], 3) == [[0], [], []]
+    costs = [float(c) for c in range(1, 40)]
+    loads = [sum(costs[i] for i in qq) for qq in schedule_longest_first(costs, 4)]
+    assert max(loads) - min(loads) <= max(costs)

@@ -137,3 +137,38 @@ def test_chunked_neural(G, precision):
     else:
         assert abs(float(e1) - float(e0)) <= 1e-6 * abs(float(e0))
         assert _rel(v1, v0) <= 1e-5 and _rel(d1, d0) <= 1e-5
+
+
+def test_chunked_batch_on_streams_matches_one_at_a_time(G):
+    """ChunkedBatch runs molecules side by side on several CUDA streams, each stream with its own workspace
+    pool: every molecule's E, V_xc and dE/dtheta equal the one-at-a-time results bit for bit."""
+    from graddft_gb300 import engine
+    from graddft_gb300.batch import ChunkedBatch
+
+    width = 128
+    net = engine.Network(n_layers=2, width=width, precision="tf32x3")
+    params = synthetic.glorot_params(layer_widths=(width,) * 2, seed=6)
+    flat = net.flatten({"params": {k: {kk: torch.as_tensor(v) for kk, v in d.items()}
+                                   for k, d in params["params"].items()}}, torch.device("cuda"))
+    shapes = [(24, 1280), (64, 2560), (40, 1792), (96, 3072), (30, 1024)]
+    mols, rdm1s, ehfs = [], [], []
+    for i, (n_ao, n_grid) in enumerate(shapes):
+        wl = synthetic.make_workload(n_grid, n_ao, max(1, n_ao // 8), seed=200 + i, box_angstrom=7.0,
+                                     centre_box_angstrom=4.0)
+        mols.append(engine.ChunkedResident(wl.basis.packed(), wl.coords, wl.weights, "tf32x3", 768))
+        rdm1s.append(torch.as_tensor(wl.rdm1, device="cuda"))
+        ehfs.append(torch.as_tensor(synthetic.make_ehf(n_grid, 300 + i, None, 2), device="cuda"))
+    one = [m.neural_xc_energy_and_grads(d, net, flat, e, want_vxc=True, want_dparams=True)
+           for m, d, e in zip(mols, rdm1s, ehfs)]
+    b = ChunkedBatch(mols, n_streams=3)
+    assert sorted(i for q in b.assignment for i in q) == list(range(len(mols)))
+    exc = torch.empty(len(mols), dtype=torch.float64, device="cuda")
+    vx = [torch.empty((2, m.n_ao, m.n_ao), dtype=torch.float64, device="cuda") for m in mols]
+    dp = torch.empty((len(mols), net.n_params), dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        b.neural_xc_energy_and_grads(rdm1s, net, flat, ehfs, exc, vx, dp)
+    torch.cuda.synchronize()
+    assert b.status() == 0
+    for i, (e, v, d) in enumerate(one):
+        assert float(exc[i]) == float(e), i
+        assert torch.equal(vx[i], v) and torch.equal(dp[i], d), i
