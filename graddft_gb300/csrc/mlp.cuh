@@ -117,7 +117,7 @@ cudaError_t launch_hvp_potentials(const double *featp, const double *featt, cons
 struct MlpHvpTcLayout {
   size_t bytes;
   size_t featp, x, xt, u, e, et, gy, ge, gu, lpart, kpart, lnpart, colpart, colpart2;  // FP64 (byte offsets)
-  size_t pf, gyf, pu, cu, wt, wr, z, h, ph, ch, gz, dhp, pg, cg;                    // FP32 (byte offsets)
+  size_t pf, gyf, pu, wt, wr, z, h, ph, ch, gz, dhp, pg, cg;                        // FP32 (byte offsets)
   int nsplit;
 };
 MlpHvpTcLayout mlp_hvp_tc_layout(const MlpShape &s, int64_t np);

@@ -14,6 +14,7 @@
 #include "kernels.cuh"
 #include "mlp.cuh"
 #include "mlp_gemm.cuh"
+#include "mlp_rows.cuh"
 #include "tc_gemm.cuh"
 #include "umma.cuh"
 
@@ -22,67 +23,6 @@ namespace gdft {
 namespace {
 
 constexpr size_t kBlk = 2 * (umma::kBlockBytes / 4);
-
-// Layer 0: z = zW + b (stored), h = tanh(z), h~ = (1 - h^2) z~.
-__global__ void tanh_tan_tc_kernel(float *__restrict__ Z, const float *__restrict__ b, size_t act, int width,
-                                   float *__restrict__ H) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= act) return;
-  const float z = Z[i] + b[i % width];
-  Z[i] = z;
-  const float h = tanhf(z);
-  H[i] = h;
-  H[act + i] = (1.0f - h * h) * Z[act + i];
-}
-
-// Residual layer with tangents (stacked rows r and np + r), one warp per row.
-template <int PL>
-__global__ void tan_fwd_tc_kernel(float *__restrict__ Z, const float *__restrict__ b, float *__restrict__ H,
-                                  const float *__restrict__ gam, const float *__restrict__ bet, double eps,
-                                  int64_t rows) {
-  constexpr int W = 32 * PL;
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (r >= rows) return;
-  const size_t act = (size_t)rows * W;
-  float *z = Z + (size_t)r * W, *zt = Z + act + (size_t)r * W;
-  float *h = H + (size_t)r * W, *ht = H + act + (size_t)r * W;
-  float v[PL], vt[PL], s1 = 0.0f;
-#pragma unroll
-  for (int k = 0; k < PL; ++k) {
-    const int c = lane + 32 * k;
-    v[k] = (z[c] + b[c]) + h[c];
-    vt[k] = zt[c] + ht[c];
-    s1 += v[k];
-  }
-  const float mean = warp_sumf(s1) * (1.0f / W);
-  float s2 = 0.0f;
-#pragma unroll
-  for (int k = 0; k < PL; ++k) {
-    const float d = v[k] - mean;
-    s2 += d * d;
-  }
-  const float rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
-  float xh[PL], m1 = 0.0f, m2 = 0.0f;
-#pragma unroll
-  for (int k = 0; k < PL; ++k) {
-    xh[k] = (v[k] - mean) * rs;
-    m1 += vt[k];
-    m2 += xh[k] * vt[k];
-  }
-  m1 = warp_sumf(m1) * (1.0f / W);
-  m2 = warp_sumf(m2) * (1.0f / W);
-#pragma unroll
-  for (int k = 0; k < PL; ++k) {
-    const int c = lane + 32 * k;
-    z[c] = v[k];
-    zt[c] = vt[k];
-    const float a = xh[k] * gam[c] + bet[c];
-    const float at = gam[c] * (rs * (vt[k] - m1 - xh[k] * m2));
-    h[c] = eluf(a);
-    ht[c] = (a > 0.0f ? 1.0f : expf(a)) * at;
-  }
-}
 
 // Head with tangents: each warp takes 32 rows; y, y~ (FP32 row sums) of row i
 // land in lane i, which evaluates the FP64 head of head_tan_kernel (mlp_hvp.cu):
@@ -184,156 +124,374 @@ __global__ void __launch_bounds__(256) head_tan_tc_kernel(const float *__restric
   }
 }
 
-// Reverse of a residual layer with tangents, one warp per row.  Incoming
-// [dL/dh; dL/dh~] is GY W_out^T (last layer) or dhp + gres (stacked); writes
-// [dL/dz; dL/dz~] (FP32) and per-block partials [block][3][W] of dL/dgamma,
-// dL/dbeta and dL/db (primal dz), FP32 over 16 rows then FP64.
+// ------------------------------------------------------- fused row passes
+// Row passes with the operand packing folded in (as the network's first-order
+// pass does, mlp_tc.cu): per 32-row tile of primal rows r0.. and its tangent
+// rows np + r0.., each warp takes 4 row pairs, and the primal and then the
+// tangent activations go through one shared-memory tile into the rt and ct
+// packs over the stacked 2 np rows.
+
+// Forward, stacked rows r (primal) and np + r (tangent):
+//   L0:   z = zW + b (stored), h = tanh(z), h~ = (1 - h^2) z~
+//   else: z = zW + b + h (stored), z~ = z~W + h~ (stored); h = elu(LN(z)),
+//         h~ = elu'(a) gamma rs (z~ - mean(z~) - xh mean(xh z~)), a = LN(z)
+// (h, h~ in place of the previous layer's).  np is a multiple of 32.
+template <int PL, bool L0>
+__global__ void __launch_bounds__(256) tan_fwd_pack_kernel(float *__restrict__ Z, const float *__restrict__ b,
+                                                           float *__restrict__ H, const float *__restrict__ gam,
+                                                           const float *__restrict__ bet, double eps, int64_t np,
+                                                           float *__restrict__ rt_out, float *__restrict__ ct_out) {
+  constexpr int W = 32 * PL, LD = W + 4;
+  __shared__ __align__(16) float tile[kRowTile * LD];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t act = (size_t)np * W;
+  const int64_t rchunks = 2 * np / 32;
+  float bf[PL], gf[PL], ef[PL];
+#pragma unroll
+  for (int k = 0; k < PL; ++k) {
+    const int c = lane + 32 * k;
+    bf[k] = b[c];
+    gf[k] = L0 ? 0.0f : gam[c];
+    ef[k] = L0 ? 0.0f : bet[c];
+  }
+  for (int64_t r0 = (int64_t)blockIdx.x * kRowTile; r0 < np; r0 += (int64_t)gridDim.x * kRowTile) {
+    float ht[4][PL];
+#pragma unroll 1
+    for (int i = 0; i < 4; ++i) {
+      const int rr = wid * 4 + i;
+      const size_t base = (size_t)(r0 + rr) * W;
+      float v[PL], vt[PL];
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const int c = lane + 32 * k;
+        if (L0) {
+          v[k] = Z[base + c] + bf[k];
+          vt[k] = Z[act + base + c];
+        } else {
+          v[k] = (Z[base + c] + bf[k]) + H[base + c];
+          vt[k] = Z[act + base + c] + H[act + base + c];
+        }
+      }
+      if (L0) {
+#pragma unroll
+        for (int k = 0; k < PL; ++k) {
+          const int c = lane + 32 * k;
+          const float h = tanhf(v[k]);
+          Z[base + c] = v[k];
+          H[base + c] = h;
+          ht[i][k] = (1.0f - h * h) * vt[k];
+          H[act + base + c] = ht[i][k];
+          tile[rr * LD + c] = h;
+        }
+      } else {
+        float s1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PL; ++k) s1 += v[k];
+        const float mean = warp_sumf(s1) * (1.0f / W);
+        float s2 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PL; ++k) {
+          const float d = v[k] - mean;
+          s2 += d * d;
+        }
+        const float rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
+        float xh[PL], m1 = 0.0f, m2 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PL; ++k) {
+          xh[k] = (v[k] - mean) * rs;
+          m1 += vt[k];
+          m2 += xh[k] * vt[k];
+        }
+        m1 = warp_sumf(m1) * (1.0f / W);
+        m2 = warp_sumf(m2) * (1.0f / W);
+#pragma unroll
+        for (int k = 0; k < PL; ++k) {
+          const int c = lane + 32 * k;
+          Z[base + c] = v[k];
+          Z[act + base + c] = vt[k];
+          const float a = xh[k] * gf[k] + ef[k];
+          const float at = gf[k] * (rs * (vt[k] - m1 - xh[k] * m2));
+          const float h = eluf(a);
+          H[base + c] = h;
+          ht[i][k] = (a > 0.0f ? 1.0f : expf(a)) * at;
+          H[act + base + c] = ht[i][k];
+          tile[rr * LD + c] = h;
+        }
+      }
+    }
+    __syncthreads();
+    store_tile_packs<PL>(tile, r0, rt_out, ct_out, rchunks);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int k = 0; k < PL; ++k) tile[(wid * 4 + i) * LD + lane + 32 * k] = ht[i][k];
+    __syncthreads();
+    store_tile_packs<PL>(tile, np + r0, rt_out, ct_out, rchunks);
+    __syncthreads();
+  }
+}
+
+// Reverse of a residual layer with tangents.  Incoming [dL/dh; dL/dh~] is
+// GY W_out^T (last layer) or dhp + gres (stacked); writes [dL/dz; dL/dz~]
+// (FP32), their rt and ct packs, and per-block partials [block][3][W] of
+// dL/dgamma, dL/dbeta and dL/db (primal dz): FP32 per 16 rows of a warp, then
+// Kahan-compensated FP32 per warp, FP64 across the block's warps.  The
+// LayerNorm's second-order term follows mlp_hvp.cu.  Dynamic shared memory:
+// bwd_pack_smem<PL>() bytes.
 template <int PL>
-__global__ void __launch_bounds__(256) tan_bwd_tc_kernel(const float *__restrict__ dhp, const float *__restrict__ gres,
-                                                         const float *__restrict__ GYf, const float *__restrict__ Wo,
-                                                         const float *__restrict__ Z, const float *__restrict__ gam,
-                                                         const float *__restrict__ bet, double eps, int64_t rows,
-                                                         float *__restrict__ gz, double *__restrict__ part) {
-  constexpr int W = 32 * PL;
-  __shared__ double sacc[8][3][W];
+__global__ void __launch_bounds__(256, 2) tan_bwd_pack_kernel(
+    const float *__restrict__ dhp, const float *__restrict__ gres, const float *__restrict__ GYf,
+    const float *__restrict__ Wo, const float *__restrict__ Z, const float *__restrict__ gam,
+    const float *__restrict__ bet, double eps, int64_t rows, float *__restrict__ gz, double *__restrict__ part,
+    float *__restrict__ rt_out, float *__restrict__ ct_out) {
+  constexpr int W = 32 * PL, LD = W + 4;
+  extern __shared__ __align__(16) unsigned char tbwd_smem[];
+  float2(*sacc)[3][W] = reinterpret_cast<float2(*)[3][W]>(tbwd_smem);
+  float *tile = reinterpret_cast<float *>(tbwd_smem + sizeof(float2) * 8 * 3 * W);
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t act = (size_t)rows * W;
-  float gmf[PL], btf[PL], wo[PL][3];
+  const int64_t rchunks = 2 * rows / 32;
+  float gmf[PL], btf[PL];
 #pragma unroll
   for (int k = 0; k < PL; ++k) {
     const int c = lane + 32 * k;
     gmf[k] = gam[c];
     btf[k] = bet[c];
-#pragma unroll
-    for (int f = 0; f < 3; ++f) wo[k][f] = GYf ? Wo[c * 3 + f] : 0.0f;
+    sacc[wid][0][c] = sacc[wid][1][c] = sacc[wid][2][c] = make_float2(0.0f, 0.0f);
   }
-  double pg[PL], pb[PL], pd[PL];
   float fg[PL], fb[PL], fd[PL];
 #pragma unroll
-  for (int k = 0; k < PL; ++k) {
-    pg[k] = pb[k] = pd[k] = 0.0;
-    fg[k] = fb[k] = fd[k] = 0.0f;
-  }
-  int nrow = 0;
-  for (int64_t r = (int64_t)blockIdx.x * 8 + wid; r < rows; r += (int64_t)gridDim.x * 8) {
-    const float *z = Z + (size_t)r * W, *zt = Z + act + (size_t)r * W;
-    float v[PL], vt[PL], gh[PL], ght[PL], s1 = 0.0f;
-    float y0 = 0.0f, y1 = 0.0f, y2 = 0.0f, t0 = 0.0f, t1 = 0.0f, t2 = 0.0f;
-    if (GYf) {
-      y0 = GYf[r * 3 + 0];
-      y1 = GYf[r * 3 + 1];
-      y2 = GYf[r * 3 + 2];
-      t0 = GYf[(rows + r) * 3 + 0];
-      t1 = GYf[(rows + r) * 3 + 1];
-      t2 = GYf[(rows + r) * 3 + 2];
-    }
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      const int c = lane + 32 * k;
-      v[k] = z[c];
-      vt[k] = zt[c];
-      s1 += v[k];
+  for (int k = 0; k < PL; ++k) fg[k] = fb[k] = fd[k] = 0.0f;
+  int ntile = 0;
+  for (int64_t r0 = (int64_t)blockIdx.x * kRowTile; r0 < rows; r0 += (int64_t)gridDim.x * kRowTile) {
+#pragma unroll 1
+    for (int i = 0; i < 4; ++i) {
+      const int rr = wid * 4 + i;
+      const int64_t r = r0 + rr;
+      const size_t base = (size_t)r * W;
+      float v[PL], vt[PL], gh[PL], ght[PL], s1 = 0.0f;
+      float y0 = 0.0f, y1 = 0.0f, y2 = 0.0f, t0 = 0.0f, t1 = 0.0f, t2 = 0.0f;
       if (GYf) {
-        gh[k] = fmaf(y0, wo[k][0], fmaf(y1, wo[k][1], y2 * wo[k][2]));
-        ght[k] = fmaf(t0, wo[k][0], fmaf(t1, wo[k][1], t2 * wo[k][2]));
-      } else {
-        gh[k] = dhp[(size_t)r * W + c] + gres[(size_t)r * W + c];
-        ght[k] = dhp[act + (size_t)r * W + c] + gres[act + (size_t)r * W + c];
+        y0 = GYf[r * 3 + 0];
+        y1 = GYf[r * 3 + 1];
+        y2 = GYf[r * 3 + 2];
+        t0 = GYf[(rows + r) * 3 + 0];
+        t1 = GYf[(rows + r) * 3 + 1];
+        t2 = GYf[(rows + r) * 3 + 2];
       }
-    }
-    const float mean = warp_sumf(s1) * (1.0f / W);
-    float s2 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      const float d = v[k] - mean;
-      s2 += d * d;
-    }
-    const float rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
-    float xh[PL], m1 = 0.0f, m2 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      xh[k] = (v[k] - mean) * rs;
-      m1 += vt[k];
-      m2 += xh[k] * vt[k];
-    }
-    m1 = warp_sumf(m1) * (1.0f / W);
-    m2 = warp_sumf(m2) * (1.0f / W);
-    float gp[PL], gt[PL], xht[PL];
-    float sgp = 0.0f, sgpx = 0.0f, sgt = 0.0f, sgtx = 0.0f, sgtz = 0.0f;
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      xht[k] = rs * (vt[k] - m1 - xh[k] * m2);
-      const float a = gmf[k] * xh[k] + btf[k];
-      const float at = gmf[k] * xht[k];
-      const float ea = expf(a);
-      const float e1 = a > 0.0f ? 1.0f : ea;
-      const float e2 = a > 0.0f ? 0.0f : ea;
-      const float gat = ght[k] * e1;
-      const float ga = gh[k] * e1 + ght[k] * at * e2;
-      fg[k] = fmaf(ga, xh[k], fmaf(gat, xht[k], fg[k]));
-      fb[k] += ga;
-      gp[k] = ga * gmf[k];
-      gt[k] = gat * gmf[k];
-      sgp += gp[k];
-      sgpx += gp[k] * xh[k];
-      sgt += gt[k];
-      sgtx += gt[k] * xh[k];
-      sgtz += gt[k] * vt[k];
-    }
-    const float mgp = warp_sumf(sgp) * (1.0f / W), mgpx = warp_sumf(sgpx) * (1.0f / W);
-    const float mgt = warp_sumf(sgt) * (1.0f / W), mgtx = warp_sumf(sgtx) * (1.0f / W);
-    const float mgtz = warp_sumf(sgtz) * (1.0f / W);
-    const float r2 = rs * rs;
-#pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      const int c = lane + 32 * k;
-      const float second =
-          -r2 * (xh[k] * (mgtz - mgt * m1 - 3.0f * m2 * mgtx) + mgtx * (vt[k] - m1) + m2 * (gt[k] - mgt));
-      const float d = rs * (gp[k] - mgp - xh[k] * mgpx) + second;
-      fd[k] += d;
-      gz[(size_t)r * W + c] = d;
-      gz[act + (size_t)r * W + c] = rs * (gt[k] - mgt - xh[k] * mgtx);
-    }
-    if (++nrow == 16) {
-      nrow = 0;
 #pragma unroll
       for (int k = 0; k < PL; ++k) {
-        pg[k] += fg[k];
-        pb[k] += fb[k];
-        pd[k] += fd[k];
+        const int c = lane + 32 * k;
+        v[k] = Z[base + c];
+        vt[k] = Z[act + base + c];
+        s1 += v[k];
+        if (GYf) {
+          const float w0 = __ldg(Wo + c * 3), w1 = __ldg(Wo + c * 3 + 1), w2 = __ldg(Wo + c * 3 + 2);
+          gh[k] = fmaf(y0, w0, fmaf(y1, w1, y2 * w2));
+          ght[k] = fmaf(t0, w0, fmaf(t1, w1, t2 * w2));
+        } else {
+          gh[k] = dhp[base + c] + gres[base + c];
+          ght[k] = dhp[act + base + c] + gres[act + base + c];
+        }
+      }
+      const float mean = warp_sumf(s1) * (1.0f / W);
+      float s2 = 0.0f;
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const float d = v[k] - mean;
+        s2 += d * d;
+      }
+      const float rs = 1.0f / sqrtf(warp_sumf(s2) * (1.0f / W) + (float)eps);
+      float xh[PL], m1 = 0.0f, m2 = 0.0f;
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        xh[k] = (v[k] - mean) * rs;
+        m1 += vt[k];
+        m2 += xh[k] * vt[k];
+      }
+      m1 = warp_sumf(m1) * (1.0f / W);
+      m2 = warp_sumf(m2) * (1.0f / W);
+      float gp[PL], gt[PL], xht[PL];
+      float sgp = 0.0f, sgpx = 0.0f, sgt = 0.0f, sgtx = 0.0f, sgtz = 0.0f;
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        xht[k] = rs * (vt[k] - m1 - xh[k] * m2);
+        const float a = gmf[k] * xh[k] + btf[k];
+        const float at = gmf[k] * xht[k];
+        const float ea = expf(a);
+        const float e1 = a > 0.0f ? 1.0f : ea;
+        const float e2 = a > 0.0f ? 0.0f : ea;
+        const float gat = ght[k] * e1;
+        const float ga = gh[k] * e1 + ght[k] * at * e2;
+        fg[k] = fmaf(ga, xh[k], fmaf(gat, xht[k], fg[k]));
+        fb[k] += ga;
+        gp[k] = ga * gmf[k];
+        gt[k] = gat * gmf[k];
+        sgp += gp[k];
+        sgpx += gp[k] * xh[k];
+        sgt += gt[k];
+        sgtx += gt[k] * xh[k];
+        sgtz += gt[k] * vt[k];
+      }
+      const float mgp = warp_sumf(sgp) * (1.0f / W), mgpx = warp_sumf(sgpx) * (1.0f / W);
+      const float mgt = warp_sumf(sgt) * (1.0f / W), mgtx = warp_sumf(sgtx) * (1.0f / W);
+      const float mgtz = warp_sumf(sgtz) * (1.0f / W);
+      const float r2 = rs * rs;
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const int c = lane + 32 * k;
+        const float second =
+            -r2 * (xh[k] * (mgtz - mgt * m1 - 3.0f * m2 * mgtx) + mgtx * (vt[k] - m1) + m2 * (gt[k] - mgt));
+        const float d = rs * (gp[k] - mgp - xh[k] * mgpx) + second;
+        fd[k] += d;
+        gz[base + c] = d;
+        gz[act + base + c] = rs * (gt[k] - mgt - xh[k] * mgtx);
+        tile[rr * LD + c] = d;
+      }
+    }
+    if (++ntile == 4) {  // 16 rows per warp: FP32 partials into the Kahan sums
+      ntile = 0;
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const int c = lane + 32 * k;
+        kahan_add(sacc[wid][0][c], fg[k]);
+        kahan_add(sacc[wid][1][c], fb[k]);
+        kahan_add(sacc[wid][2][c], fd[k]);
         fg[k] = fb[k] = fd[k] = 0.0f;
       }
     }
+    __syncthreads();
+    store_tile_packs<PL>(tile, r0, rt_out, ct_out, rchunks);
+    __syncthreads();
+    // The tangent rows this thread wrote above, back through the tile.
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const int rr = wid * 4 + i, c = lane + 32 * k;
+        tile[rr * LD + c] = gz[act + (size_t)(r0 + rr) * W + c];
+      }
+    __syncthreads();
+    store_tile_packs<PL>(tile, rows + r0, rt_out, ct_out, rchunks);
+    __syncthreads();
   }
 #pragma unroll
   for (int k = 0; k < PL; ++k) {
-    pg[k] += fg[k];
-    pb[k] += fb[k];
-    pd[k] += fd[k];
-    sacc[wid][0][lane + 32 * k] = pg[k];
-    sacc[wid][1][lane + 32 * k] = pb[k];
-    sacc[wid][2][lane + 32 * k] = pd[k];
+    const int c = lane + 32 * k;
+    kahan_add(sacc[wid][0][c], fg[k]);
+    kahan_add(sacc[wid][1][c], fb[k]);
+    kahan_add(sacc[wid][2][c], fd[k]);
   }
   __syncthreads();
   double *out = part + (size_t)blockIdx.x * 3 * W;
   for (int c = threadIdx.x; c < 3 * W; c += blockDim.x) {
     const int q = c / W, cc = c % W;
-    double s = 0.0;
-    for (int w8 = 0; w8 < 8; ++w8) s += sacc[w8][q][cc];
-    out[c] = s;
+    double sum = 0.0;
+    for (int w8 = 0; w8 < 8; ++w8) sum += (double)sacc[w8][q][cc].x - (double)sacc[w8][q][cc].y;
+    out[c] = sum;
   }
 }
 
-// Layer 0 reverse with tangents: incoming g = dhp + gres (stacked);
-// dz0 = g s - 2 h s z0~ g~, dz0~ = g~ s with h = tanh(z0), s = 1 - h^2.
-__global__ void tanh_tan_bwd_tc_kernel(const float *__restrict__ dhp, const float *__restrict__ gres,
-                                       const float *__restrict__ Z0, size_t act, float *__restrict__ gz) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= act) return;
-  const float h = tanhf(Z0[i]), s = 1.0f - h * h;
-  const float g = dhp[i] + gres[i], gt = dhp[act + i] + gres[act + i];
-  gz[act + i] = gt * s;
-  gz[i] = g * s - 2.0f * h * s * Z0[act + i] * gt;
+// Layer-0 reverse with tangents, g = dhp + gres (stacked), h = tanh(z0),
+// s = 1 - h^2: dz0 = g s - 2 h s z0~ g~, dz0~ = g~ s; with everything that
+// consumes [dz0; dz0~], per 32-row tile: GU[row][j] = sum_c dz0[row][c] W0[j][c]
+// over the stacked rows, part[block][j][c] = sum over the stacked
+// rows of U[row][j] dz0[row][c] (dW0), part[block][n_in][c] = sum over the
+// primal rows of dz0 (db0); parameter sums FP32 per 16 rows, Kahan FP32 per
+// block.  Dynamic shared memory: l0_tan_bwd_smem<PL>() bytes.
+template <int PL>
+constexpr size_t l0_tan_bwd_smem() {
+  return sizeof(float) * (2 * kRowTile * (32 * PL + 4) + 2 * kRowTile * kDm21InPad + kDm21InPad * 32 * PL);
+}
+
+template <int PL>
+__global__ void __launch_bounds__(256) tanh_tan_bwd_fused_kernel(
+    const float *__restrict__ dhp, const float *__restrict__ gres, const float *__restrict__ Z0,
+    const double *__restrict__ U, const float *__restrict__ W0, int n_in, int64_t np, double *__restrict__ GU,
+    double *__restrict__ part) {
+  constexpr int W = 32 * PL, LD = W + 4, NJ = kDm21InPad + 1;
+  extern __shared__ __align__(16) unsigned char l0t_smem[];
+  float *tp = reinterpret_cast<float *>(l0t_smem);  // [32][LD] dz0, primal rows
+  float *tt = tp + kRowTile * LD;                    // [32][LD] dz0~, tangent rows
+  float *up = tt + kRowTile * LD;                    // [32][kDm21InPad] u, primal rows
+  float *ut = up + kRowTile * kDm21InPad;            // [32][kDm21InPad] u~, tangent rows
+  float *w0s = ut + kRowTile * kDm21InPad;           // [kDm21InPad][W] W0, zero rows past n_in
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t act = (size_t)np * W;
+  for (int i = threadIdx.x; i < kDm21InPad * W; i += blockDim.x) w0s[i] = i / W < n_in ? W0[i] : 0.0f;
+  const int c = threadIdx.x;
+  float acc[NJ], comp[NJ], fac[NJ];
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) acc[j] = comp[j] = fac[j] = 0.0f;
+  __syncthreads();
+  auto du_row = [&](const float (&d)[PL], int64_t row) {
+    if (GU == nullptr) return;
+    for (int j = 0; j < kDm21InPad; ++j) {
+      float sj = 0.0f;
+      if (j < n_in) {
+        float sf = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PL; ++k) sf = fmaf(d[k], w0s[j * W + lane + 32 * k], sf);
+        sj = warp_sumf(sf);
+      }
+      if (lane == 0) GU[(size_t)row * kDm21InPad + j] = (double)sj;
+    }
+  };
+  for (int64_t r0 = (int64_t)blockIdx.x * kRowTile; r0 < np; r0 += (int64_t)gridDim.x * kRowTile) {
+#pragma unroll 1
+    for (int i = 0; i < 4; ++i) {
+      const int rr = wid * 4 + i;
+      const int64_t r = r0 + rr;
+      const size_t base = (size_t)r * W;
+      float d[PL], dt[PL];
+#pragma unroll
+      for (int k = 0; k < PL; ++k) {
+        const size_t e = base + lane + 32 * k;
+        const float h = tanhf(Z0[e]), sv = 1.0f - h * h;
+        const float g = dhp[e] + gres[e], gt = dhp[act + e] + gres[act + e];
+        dt[k] = gt * sv;
+        d[k] = g * sv - 2.0f * h * sv * Z0[act + e] * gt;
+        tp[rr * LD + lane + 32 * k] = d[k];
+        tt[rr * LD + lane + 32 * k] = dt[k];
+      }
+      if (lane < kDm21InPad) {
+        up[rr * kDm21InPad + lane] = lane < n_in ? (float)U[(size_t)r * kDm21InPad + lane] : 0.0f;
+        ut[rr * kDm21InPad + lane] = lane < n_in ? (float)U[(size_t)(np + r) * kDm21InPad + lane] : 0.0f;
+      }
+      du_row(d, r);
+      du_row(dt, np + r);
+    }
+    __syncthreads();
+    if (part && c < W) {
+#pragma unroll 2
+      for (int rr = 0; rr < kRowTile; ++rr) {
+        const float gp = tp[rr * LD + c], gt = tt[rr * LD + c];
+#pragma unroll
+        for (int j = 0; j < kDm21InPad; ++j)
+          fac[j] = fmaf(ut[rr * kDm21InPad + j], gt, fmaf(up[rr * kDm21InPad + j], gp, fac[j]));
+        fac[kDm21InPad] += gp;
+        if ((rr & 15) == 15) {
+#pragma unroll
+          for (int j = 0; j < NJ; ++j) {  // Kahan: acc + (fac - comp)
+            const float y = fac[j] - comp[j];
+            const float t = acc[j] + y;
+            comp[j] = (t - acc[j]) - y;
+            acc[j] = t;
+            fac[j] = 0.0f;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (part && c < W) {
+    double *out = part + (size_t)blockIdx.x * (n_in + 1) * W;
+#pragma unroll
+    for (int j = 0; j < kDm21InPad; ++j)
+      if (j < n_in) out[(size_t)j * W + c] = (double)acc[j] - (double)comp[j];
+    out[(size_t)n_in * W + c] = (double)acc[kDm21InPad] - (double)comp[kDm21InPad];
+  }
 }
 
 size_t hvp_tc_layer_offset(const MlpShape &S, int i) {
@@ -351,7 +509,7 @@ int run_hvp_tc(const MlpShape &S, const double *params, double *dparams, const d
   double *x = d64(L.x), *xt = d64(L.xt), *U = d64(L.u), *e = d64(L.e), *et = d64(L.et), *GY = d64(L.gy);
   double *GE = d64(L.ge), *GU = d64(L.gu), *lpart = d64(L.lpart), *kpart = d64(L.kpart);
   double *lnpart = d64(L.lnpart), *colpart = d64(L.colpart), *colpart2 = d64(L.colpart2);
-  float *pf = f32(L.pf), *GYf = f32(L.gyf), *PU = f32(L.pu), *CU = f32(L.cu), *WT = f32(L.wt), *WR = f32(L.wr);
+  float *pf = f32(L.pf), *GYf = f32(L.gyf), *PU = f32(L.pu), *WT = f32(L.wt), *WR = f32(L.wr);
   float *Z = f32(L.z), *H = f32(L.h), *PH = f32(L.ph), *CH = f32(L.ch), *GZ = f32(L.gz), *DHP = f32(L.dhp);
   float *PG = f32(L.pg), *CG = f32(L.cg);
   const int64_t rows2 = 2 * np;
@@ -406,8 +564,6 @@ int run_hvp_tc(const MlpShape &S, const double *params, double *dparams, const d
     sum_splits_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(kpart, ns, total, out);
     return cudaGetLastError();
   };
-  const unsigned wblocks = (unsigned)((np * 32 + 255) / 256);
-  const unsigned eblocks = (unsigned)((act + 255) / 256);
   const unsigned pblocks = (unsigned)((np + 255) / 256);
 
   {
@@ -426,17 +582,22 @@ int run_hvp_tc(const MlpShape &S, const double *params, double *dparams, const d
   GDFT_CK(launch_features_tan(featp, featt, ehf, n_grid, np, clip, S.squash_offset, x, xt, U, e, et, st),
           "hvp_tc features");
   GDFT_CK(launch_pack_rt<double>(U, rows2, S.n_in, kDm21InPad, rt2, 1, PU, st), "hvp_tc pack u");
+  // Each row pass also packs [h; h~] for the next dense layer (rt) and, with
+  // dparams, for that layer's weight gradient (ct).
   GDFT_CK(gemm_act(PU, 1, WTi(0), Z), "hvp_tc dense_0");
-  tanh_tan_tc_kernel<<<eblocks, 256, 0, st>>>(Z, b0f, act, Wd, H);
+  tan_fwd_pack_kernel<PL, true><<<kLnBlocks, 256, 0, st>>>(Z, b0f, H, nullptr, nullptr, 0.0, np,
+                                                           S.n_layers > 0 ? PH : nullptr,
+                                                           (dparams && S.n_layers > 0) ? CHi(0) : nullptr);
   GDFT_CK(cudaGetLastError(), "hvp_tc tanh");
   for (int i = 1; i <= S.n_layers; ++i) {
     const float *Wif = pf + hvp_tc_layer_offset(S, i - 1), *bi = Wif + (size_t)Wd * Wd, *gi = bi + Wd,
                 *bei = gi + Wd;
-    GDFT_CK(launch_pack_rt<float>(H, rows2, Wd, Wd, rt2, kcw, PH, st), "hvp_tc pack h");
-    if (dparams) GDFT_CK(launch_pack_ct<float>(H, rows2, Wd, Wd, ft, rc2, CHi(i - 1), st), "hvp_tc pack h^T");
     float *Zi = Z + (size_t)i * act2;
     GDFT_CK(gemm_act(PH, kcw, WTi(i), Zi), "hvp_tc dense_i");
-    tan_fwd_tc_kernel<PL><<<wblocks, 256, 0, st>>>(Zi, bi, H, gi, bei, S.ln_eps, np);
+    const bool more = i < S.n_layers;
+    tan_fwd_pack_kernel<PL, false><<<kLnBlocks, 256, 0, st>>>(Zi, bi, H, gi, bei, S.ln_eps, np,
+                                                              more ? PH : nullptr,
+                                                              (dparams && more) ? CHi(i) : nullptr);
     GDFT_CK(cudaGetLastError(), "hvp_tc layernorm");
   }
   head_tan_tc_kernel<PL><<<pblocks, 256, 0, st>>>(H, Wof, bo, e, et, w, n_grid, np, clip, S.sigmoid_scale, GY, GYf,
@@ -451,18 +612,19 @@ int run_hvp_tc(const MlpShape &S, const double *params, double *dparams, const d
     GDFT_CK(cudaGetLastError(), "hvp_tc head wgrad");
   }
   float *gz_cur = GZ, *gz_prev = GZ + act2;
+  GDFT_CK(cudaFuncSetAttribute(tan_bwd_pack_kernel<PL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)bwd_pack_smem<PL>()),
+          "hvp_tc layernorm bwd smem");
   for (int i = S.n_layers; i >= 1; --i) {
     const float *Wif = pf + hvp_tc_layer_offset(S, i - 1), *gi = Wif + (size_t)Wd * Wd + Wd, *bei = gi + Wd;
     const float *Zi = Z + (size_t)i * act2;
     const bool last = i == S.n_layers;
-    tan_bwd_tc_kernel<PL><<<kLnBlocks, 256, 0, st>>>(last ? nullptr : DHP, last ? nullptr : gz_prev,
-                                                     last ? GYf : nullptr, Wof, Zi, gi, bei, S.ln_eps, np, gz_cur,
-                                                     lnpart);
+    tan_bwd_pack_kernel<PL><<<kLnBlocks, 256, bwd_pack_smem<PL>(), st>>>(
+        last ? nullptr : DHP, last ? nullptr : gz_prev, last ? GYf : nullptr, Wof, Zi, gi, bei, S.ln_eps, np, gz_cur,
+        lnpart, PG, dparams ? CG : nullptr);
     GDFT_CK(cudaGetLastError(), "hvp_tc layernorm bwd");
-    GDFT_CK(launch_pack_rt<float>(gz_cur, rows2, Wd, Wd, rt2, kcw, PG, st), "hvp_tc pack dz");
     if (dparams) {
       double *dWi = dparams + hvp_tc_layer_offset(S, i - 1);
-      GDFT_CK(launch_pack_ct<float>(gz_cur, rows2, Wd, Wd, ft, rc2, CG, st), "hvp_tc pack dz^T");
       GDFT_CK(gemm_wgrad(CHi(i - 1), ft, Wd, CG, dWi), "hvp_tc dW_i");
       launch_colsum_final(lnpart, kLnBlocks, 3 * Wd, colpart2, st);
       GDFT_CK(cudaGetLastError(), "hvp_tc ln sums");
@@ -478,22 +640,22 @@ int run_hvp_tc(const MlpShape &S, const double *params, double *dparams, const d
     gz_cur = gz_prev;
     gz_prev = t;
   }
-  tanh_tan_bwd_tc_kernel<<<eblocks, 256, 0, st>>>(DHP, gz_prev, Z, act, gz_cur);
+  // Layer 0: gz_prev holds [dL/dz_1; dL/dz_1~], DHP its product with W_1^T.
+  // One pass gives GU and the FP64 partials of [dW0 | db0] (kpart is free by
+  // now and holds kLnBlocks x (n_in + 1) x W doubles: 4 (n_in + 1) <= W).
+  GDFT_CK(cudaFuncSetAttribute(tanh_tan_bwd_fused_kernel<PL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)l0_tan_bwd_smem<PL>()),
+          "hvp_tc tanh bwd smem");
+  tanh_tan_bwd_fused_kernel<PL><<<kLnBlocks, 256, l0_tan_bwd_smem<PL>(), st>>>(
+      DHP, gz_prev, Z, U, W0f, S.n_in, np, coef ? GU : nullptr, dparams ? kpart : nullptr);
   GDFT_CK(cudaGetLastError(), "hvp_tc tanh bwd");
   if (dparams) {
-    GDFT_CK(launch_pack_ct<double>(U, rows2, S.n_in, kDm21InPad, 1, rc2, CU, st), "hvp_tc pack u^T");
-    GDFT_CK(launch_pack_ct<float>(gz_cur, rows2, Wd, Wd, ft, rc2, CG, st), "hvp_tc pack dz0^T");
-    GDFT_CK(gemm_wgrad(CU, 1, S.n_in, CG, dparams), "hvp_tc dW_0");
-    colsum_f32_part_kernel<<<kColBlocks, 256, 0, st>>>(gz_cur, np, Wd, colpart);
-    launch_colsum_final(colpart, kColBlocks, Wd, dparams + (size_t)S.n_in * Wd, st);
-    GDFT_CK(cudaGetLastError(), "hvp_tc db0");
+    launch_colsum_final(kpart, kLnBlocks, (S.n_in + 1) * Wd, dparams, st);
+    GDFT_CK(cudaGetLastError(), "hvp_tc dW_0");
   }
-  if (coef) {
-    du_kernel<PL><<<(unsigned)((rows2 * 32 + 255) / 256), 256, 0, st>>>(gz_cur, W0f, S.n_in, rows2, GU);
-    GDFT_CK(cudaGetLastError(), "hvp_tc du");
+  if (coef)
     GDFT_CK(launch_hvp_potentials(featp, featt, x, xt, GU, GE, n_grid, np, clip, S.squash_offset, coef, st),
             "hvp_tc potentials");
-  }
 #undef GDFT_CK
   return GDFT_OK;
 }
@@ -532,7 +694,6 @@ MlpHvpTcLayout mlp_hvp_tc_layout(const MlpShape &s, int64_t np) {
   L.pf = take(mlp_param_count(s) * 4);
   L.gyf = take((size_t)rows2 * 3 * 4);
   L.pu = take((size_t)rt2 * kBlk * 4);
-  L.cu = take((size_t)rc2 * kBlk * 4);
   L.wt = take(((size_t)ft * kBlk + (size_t)s.n_layers * ft * kcw * kBlk) * 4);
   L.wr = take((size_t)nl * ft * kcw * kBlk * 4);
   L.z = take(act2 * (s.n_layers + 1) * 4);
