@@ -128,6 +128,7 @@ class _NeuralXcPair(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, rdm1, flat, resident, net, ehf):
+        ctx.set_materialize_grads(False)  # an output nothing reads has no cotangent: no second-order pass for it
         exc, vxc, dp = resident.neural_xc_energy_and_grads(rdm1.detach(), net, flat.detach(), ehf, want_vxc=True,
                                                            want_dparams=ctx.needs_input_grad[1])
         ctx.save_for_backward(rdm1.detach(), flat.detach(), vxc, *(t for t in (dp,) if t is not None))
@@ -145,7 +146,7 @@ class _NeuralXcPair(torch.autograd.Function):
             d_rdm1 = g_e * vxc if g_e is not None else torch.zeros_like(vxc)
         if want_p:
             d_flat = g_e * dp if g_e is not None else torch.zeros_like(flat)
-        if g_v is not None and bool((g_v != 0).any()):
+        if g_v is not None:
             _, hd, hp = ctx.resident.neural_xc_hvp(rdm1, ctx.net, flat, ctx.ehf, g_v.contiguous(), want_value=False,
                                                    want_drdm1=want_d, want_dparams=want_p)
             if want_d:

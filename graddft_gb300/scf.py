@@ -37,12 +37,30 @@ BROADENING = 1e-10
 F64 = torch.float64
 
 
+# The linear algebra of the SCF loop runs without torch's error checks: each
+# check copies the solver's info code to the host, a synchronisation per call
+# that left the GPU idle between the iterations' kernels (about 180 per
+# 20-cycle loop).  JAX's solvers, which the reference uses, do not check
+# either: a failed factorisation gives NaN, not an exception.
+def _eigh(A):
+    op = getattr(torch, "_linalg_eigh", None)  # torch.linalg.eigh without its info check
+    return op(A, "L", True) if op is not None else torch.linalg.eigh(A)
+
+
+def _inv(A):
+    return torch.linalg.inv_ex(A).inverse
+
+
+def _cholesky(A):
+    return torch.linalg.cholesky_ex(A).L
+
+
 class _SafeEigh(torch.autograd.Function):
     """eigh with the reverse rule of utils/eigenproblem.py:41-107."""
 
     @staticmethod
     def forward(ctx, A):
-        evals, evecs = torch.linalg.eigh(A)
+        evals, evecs = _eigh(A)
         ctx.save_for_backward(evals, evecs)
         return evals, evecs
 
@@ -61,7 +79,7 @@ class _SafeEigh(torch.autograd.Function):
         Fm = 0.5 * torch.where(degen, broadened, regular)
         Fm = Fm - torch.diag_embed(torch.diagonal(Fm, dim1=-2, dim2=-1))
         inner = 0.5 * torch.diag_embed(g_evals) + Fm * (vt @ g_evecs)
-        grad = torch.linalg.inv(vt) @ inner @ vt
+        grad = _inv(vt) @ inner @ vt
         return grad + grad.transpose(-1, -2)
 
 
@@ -72,8 +90,8 @@ def safe_eigh(A):
 
 def safe_general_eigh(A, B):
     """A C = B C E via Cholesky of B (eigenproblem.py:110-131)."""
-    L = torch.linalg.cholesky(B)
-    L_inv = torch.linalg.inv(L)
+    L = _cholesky(B)
+    L_inv = _inv(L)
     C = L_inv @ A @ L_inv.transpose(-1, -2)
     evals, evecs_t = safe_eigh(C)
     return evals, L_inv.transpose(-1, -2) @ evecs_t
@@ -325,7 +343,7 @@ class JittableDiis:
         B = torch.cat((top[:, None, :], torch.cat((border[:, :, None], core), dim=2)), dim=1)
         C = torch.zeros(n + 1, dtype=inner.dtype, device=inner.device)
         C[0] = 1.0
-        x = torch.stack([torch.linalg.inv(B[s]) @ C for s in range(2)], dim=0)
+        x = torch.stack([_inv(B[s]) @ C for s in range(2)], dim=0)
         return x[:, 1:]
 
     def run(self, new_data, diis_data, cycle=0):
