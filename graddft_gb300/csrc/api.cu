@@ -274,7 +274,9 @@ __global__ void write_seg_kernel(const SegTable t, int n, int64_t *__restrict__ 
 struct BatchLayout {
   int64_t seg[kBatchMax + 1];
   int64_t npt;
-  size_t off_mol, off_feat, off_w, off_ehf, off_coef, off_seg, off_cot, off_net, bytes;
+  bool ragged;                  // every molecule in the mixed form: one ragged density launch
+  size_t off_dpk[kBatchMax];    // ragged: each molecule's packed rdm1
+  size_t off_mol, off_feat, off_w, off_ehf, off_coef, off_seg, off_cot, off_net, off_queue, bytes;
 };
 
 static int batch_layout(int n_mol, const gdft_molecule *mols, const gdft_network *net, BatchLayout *B) {
@@ -295,6 +297,17 @@ static int batch_layout(int n_mol, const gdft_molecule *mols, const gdft_network
   B->off_mol = off;
   off += mol_bytes;
   B->seg[n_mol] = npt;
+  B->ragged = true;
+  for (int m = 0; m < n_mol; ++m) B->ragged = B->ragged && mols[m].precision == GDFT_TF32X3;
+  if (B->ragged) {
+    for (int m = 0; m < n_mol; ++m) {
+      const size_t ldk = (size_t)round_up(mols[m].n_ao, 128);
+      B->off_dpk[m] = off;
+      off += align256(2 * ldk * ldk * 2 * sizeof(float));
+    }
+    B->off_queue = off;
+    off += align256(dens_ragged_scratch_bytes(n_mol));
+  }
   B->npt = npt;
   B->off_feat = off;
   off += align256((size_t)2 * kFeat * npt * 8);
@@ -1148,10 +1161,37 @@ int gdft_neural_batch_xc(int32_t n_mol, const gdft_molecule *mols, const double 
   // region: cleared before the molecule's stage (a previous molecule's data may
   // lie there) and folded into the batch's word after it.
   auto mol_err = [&](const gdft_molecule *mol) { return (int *)(wsm + ws_layout(mol).off_err); };
+  if (B.ragged) {
+    // Every molecule's density in one persistent launch over all their tiles,
+    // straight into the joint feature array.
+    DensMol dm[kBatchMax];
+    {
+      StageTimer tm(GDFT_STAGE_REDUCE, st);
+      for (int m = 0; m < n_mol; ++m) {
+        const gdft_molecule *mol = &mols[m];
+        const int ldk = (int)round_up(mol->n_ao, 128);
+        float *dpk = (float *)(ws + B.off_dpk[m]);
+        if ((rc = check_cuda(launch_pack_rdm1(h_rdm1[m], mol->n_ao, ldk, dpk, st), "batch pack_rdm1"))) return rc;
+        dm[m] = DensMol{mol_pm(mol), dpk, mol->n_grid_pad, ldk, feat + B.seg[m], npt};
+      }
+    }
+    StageTimer tm(GDFT_STAGE_DENSITY, st);
+    if ((rc = check_cuda(launch_dens_tc_ragged(dm, n_mol, ws + B.off_queue, batch_err, st), "batch dens_tc")))
+      return rc;
+  }
   for (int m = 0; m < n_mol; ++m) {
     const gdft_molecule *mol = &mols[m];
     const WsLayout W = ws_layout(mol);
     const int64_t np = mol->n_grid_pad, off = B.seg[m];
+    if (B.ragged) {
+      if ((rc = check_cuda(cudaMemcpyAsync(w + off, mol_w(mol), (size_t)np * 8, cudaMemcpyDeviceToDevice, st),
+                           "batch weights")) ||
+          (rc = check_cuda(cudaMemcpy2DAsync(ehf + off, (size_t)npt * 8, h_ehf[m], (size_t)mol->n_grid * 8,
+                                             (size_t)mol->n_grid * 8, 4, cudaMemcpyDeviceToDevice, st),
+                           "batch ehf")))
+        return rc;
+      continue;
+    }
     if ((rc = check_cuda(cudaMemsetAsync(mol_err(mol), 0, sizeof(int), st), "batch error word"))) return rc;
     if ((rc = run_density(mol, h_rdm1[m], wsm, st))) return rc;
     if ((rc = check_cuda(launch_err_fold(batch_err, mol_err(mol), st), "batch error fold"))) return rc;

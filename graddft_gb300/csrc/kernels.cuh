@@ -35,6 +35,20 @@ cudaError_t launch_pack_tables(const double *ao, const double *grad_ao, const do
 cudaError_t launch_pack_rdm1(const double *D, int n, int ldk, float *out, cudaStream_t st);
 cudaError_t launch_dens_tc(const float *pm, const float *dpk, int64_t np, int ldk, double *feat, int *err,
                            cudaStream_t st);
+// One persistent launch of the same kernel over several molecules' 128-point
+// tiles (a device work queue, the molecules with the largest n_ao first): each
+// molecule's features go to feat with row stride ldf.  d_scratch holds
+// dens_ragged_scratch_bytes(n_mol) bytes (256-byte aligned).
+struct DensMol {
+  const float *pm;   // point-major resident tables
+  const float *dpk;  // packed rdm1 (launch_pack_rdm1)
+  int64_t np;        // padded grid points (multiple of 128)
+  int ldk;           // n_ao rounded up to 128
+  double *feat;      // [2][6][ldf]
+  int64_t ldf;
+};
+size_t dens_ragged_scratch_bytes(int n_mol);
+cudaError_t launch_dens_tc_ragged(const DensMol *mols, int n_mol, void *d_scratch, int *err, cudaStream_t st);
 
 // vxc_q.cu: mixed V_xc as Q pre-pass + block-scaled three-slice tensor-core GEMM.
 int vxc_q_splits(int64_t np, int n_ao);
