@@ -28,31 +28,35 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                : "memory");
 }
+// One bounded wait step: the thread suspends until the phase completes or
+// kWaitHintNs nanoseconds pass (the suspend-time hint of try_wait), then
+// reports whether the phase completed.
+constexpr uint32_t kWaitHintNs = 1000;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n"
       ".reg .pred p;\n"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
       "selp.u32 %0, 1, 0, p;\n"
       "}\n"
       : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(kWaitHintNs)
       : "memory");
   return ok != 0;
 }
 
-// Iteration limit of every wait (each try_wait itself blocks for a bounded,
-// hardware-defined interval): a healthy pipeline completes any single wait in
-// far fewer iterations.
-constexpr uint32_t kWaitLimit = 1u << 22;
+// Iteration limit of every wait: with each step suspending for up to
+// kWaitHintNs, about a second before a wait gives up; a healthy pipeline's
+// hand-offs complete within microseconds.  (An earlier form polled and slept
+// 64 ns between polls after the 64th: the wake-up latency cost 1-2 % of the
+// tensor-core kernels' time.)
+constexpr uint32_t kWaitLimit = 1u << 20;
 
-// Returns false when `limit` polls pass without the phase completing.
+// Returns false when `limit` steps pass without the phase completing.
 __device__ __forceinline__ bool mbar_wait_n(uint64_t *bar, uint32_t parity, uint32_t limit) {
-  for (uint32_t i = 0; i < limit; ++i) {
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
-    if (i > 64) __nanosleep(64);
-  }
   return false;
 }
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) { return mbar_wait_n(bar, parity, kWaitLimit); }
