@@ -64,15 +64,10 @@ __device__ __forceinline__ void mbar_inval(uint64_t *bar) {
   asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Warp-uniform bounded wait: lane 0 polls, the result is broadcast, and every
-// lane then observes the (already completed) phase itself so that each lane
-// has acquire ordering.  All lanes return the same value.
+// Warp-uniform bounded wait: every lane waits on the phase itself (and so has
+// acquire ordering); all lanes return the same value.
 __device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity) {
-  const int lane = threadIdx.x & 31;
-  bool ok = true;
-  if (lane == 0) ok = mbar_wait(bar, parity);
-  ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-  if (ok) ok = mbar_wait(bar, parity);
+  const bool ok = mbar_wait(bar, parity);
   return __all_sync(0xffffffffu, ok) != 0;
 }
 
