@@ -185,18 +185,6 @@ __global__ void to_f32_kernel(const double *__restrict__ x, size_t n, float *__r
   if (i < n) y[i] = (float)x[i];
 }
 
-// Column sums of an FP32 matrix (FP64 accumulation), first pass per block.
-__global__ void colsum_f32_part_kernel(const float *__restrict__ X, int64_t rows, int ncols,
-                                       double *__restrict__ part) {
-  const int64_t chunk = (rows + gridDim.x - 1) / gridDim.x;
-  const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = r0 + chunk < rows ? r0 + chunk : rows;
-  for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
-    double s = 0.0;
-    for (int64_t r = r0; r < r1; ++r) s += (double)X[(size_t)r * ncols + c];
-    part[(size_t)blockIdx.x * ncols + c] = s;
-  }
-}
-
 // Head weight gradients: part[block][c][0..2] = sum_r h[r][c] dy[r][f] over the
 // block's row range, part[block][W*3 + f] = sum of dy[r][f] over its rows below
 // rows_bias (the bias sees only primal rows); one thread per column.
@@ -241,30 +229,6 @@ __global__ void head_wgrad_part_kernel(const float *__restrict__ H, const float 
     double s = 0.0;
     for (int64_t r = r0; r < (r1 < rows_bias ? r1 : rows_bias); ++r) s += dy[r * 3 + threadIdx.x];
     pb[3 * width + threadIdx.x] = s;
-  }
-}
-
-// du[r][k] = sum_c dz0[r][c] W0[k][c] for the n_in inputs, one warp per row
-// (FP32 products per lane, FP64 warp sums).
-template <int PL>
-__global__ void du_kernel(const float *__restrict__ gz, const float *__restrict__ W0, int n_in, int64_t rows,
-                          double *__restrict__ du) {
-  constexpr int W = 32 * PL;
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (r >= rows) return;
-  float g[PL];
-#pragma unroll
-  for (int k = 0; k < PL; ++k) g[k] = gz[(size_t)r * W + lane + 32 * k];
-  for (int j = 0; j < kDm21InPad; ++j) {
-    double s = 0.0;
-    if (j < n_in) {
-      float sf = 0.0f;
-#pragma unroll
-      for (int k = 0; k < PL; ++k) sf = fmaf(g[k], W0[(size_t)j * W + lane + 32 * k], sf);
-      s = (double)warp_sumf(sf);
-    }
-    if (lane == 0) du[(size_t)r * kDm21InPad + j] = s;
   }
 }
 
