@@ -14,6 +14,9 @@ constexpr int kDm21Out = 3;
 constexpr int kLnBlocks = 592;  // 4 x 148 SMs
 // Blocks of the column-sum (bias gradient) first pass.
 constexpr int kColBlocks = 296;
+// Blocks of the head weight-gradient pass of the tensor-core forms (more row
+// slices in flight: one thread per column walks its slice's rows).
+constexpr int kHeadBlocks = 4 * kColBlocks;
 
 struct MlpShape {
   int n_in, width, n_layers, n_out;

@@ -566,8 +566,8 @@ int run_tc(const MlpShape &S, const double *params, double *dparams, const doubl
 
   // ---- backward ----
   if (dparams) {
-    head_wgrad_part_kernel<<<kColBlocks, 256, 0, st>>>(HF, dyf, dy, np, np, Wd, colpart);
-    launch_colsum_final(colpart, kColBlocks, 3 * Wd + 3, dparams + head_off, st);
+    head_wgrad_part_kernel<<<kHeadBlocks, 256, 0, st>>>(HF, dyf, dy, np, np, Wd, colpart);
+    launch_colsum_final(colpart, kHeadBlocks, 3 * Wd + 3, dparams + head_off, st);
     GDFT_CK(cudaGetLastError(), "mlp_tc head wgrad");
   }
   float *gz_cur = GZ, *gz_prev = GZ + act;
@@ -646,7 +646,7 @@ MlpTcLayout mlp_tc_layout(const MlpShape &s, int64_t np) {
   L.epart = take((size_t)((np + 255) / 256) * 8);
   L.kpart = take((size_t)L.nsplit * W * W * 8);
   L.lnpart = take((size_t)kLnBlocks * 3 * W * 8);
-  L.colpart = take((size_t)kColBlocks * (3 * W + 3) * 8);
+  L.colpart = take((size_t)kHeadBlocks * (3 * W + 3) * 8);
   L.colpart2 = take((size_t)3 * W * 8);
   L.pf = take(mlp_param_count(s) * 4);
   L.dyf = take((size_t)np * 3 * 4);
