@@ -427,7 +427,8 @@ __global__ void __launch_bounds__(256) tanh_tan_bwd_fused_kernel(
   __syncthreads();
   auto du_row = [&](const float (&d)[PL], int64_t row) {
     if (GU == nullptr) return;
-    for (int j = 0; j < kDm21InPad; ++j) {
+#pragma unroll
+    for (int j = 0; j < kDm21InPad; ++j) {  // independent warp sums: unrolled so they overlap
       float sj = 0.0f;
       if (j < n_in) {
         float sf = 0.0f;

@@ -242,20 +242,26 @@ __global__ void __launch_bounds__(256) head_kernel(const float *__restrict__ H, 
 #pragma unroll
     for (int f = 0; f < 3; ++f) wo[k][f] = Wo[(lane + 32 * k) * 3 + f];
   float my[3] = {0.0f, 0.0f, 0.0f};
-  for (int i = 0; i < 32; ++i) {
-    const int64_t r = base + i;
-    if (r >= rows) break;
-    float yf[3] = {0.0f, 0.0f, 0.0f};
+  for (int i0 = 0; i0 < 32; i0 += 4) {  // four rows' loads in flight at a time
+    float hv[4][PL];
 #pragma unroll
-    for (int k = 0; k < PL; ++k) {
-      const float hv = H[(size_t)r * W + lane + 32 * k];
+    for (int i = 0; i < 4; ++i) {
+      const int64_t r = base + i0 + i;
 #pragma unroll
-      for (int f = 0; f < 3; ++f) yf[f] = fmaf(hv, wo[k][f], yf[f]);
+      for (int k = 0; k < PL; ++k) hv[i][k] = r < rows ? H[(size_t)r * W + lane + 32 * k] : 0.0f;
     }
 #pragma unroll
-    for (int f = 0; f < 3; ++f) {
-      const float t = warp_sumf(yf[f]);
-      if (lane == i) my[f] = t;
+    for (int i = 0; i < 4; ++i) {
+      float yf[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int k = 0; k < PL; ++k)
+#pragma unroll
+        for (int f = 0; f < 3; ++f) yf[f] = fmaf(hv[i][k], wo[k][f], yf[f]);
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        const float t = warp_sumf(yf[f]);
+        if (lane == i0 + i) my[f] = t;
+      }
     }
   }
   const int64_t r = base + lane;
@@ -358,7 +364,8 @@ __global__ void __launch_bounds__(256, 2) l0_bwd_fused_kernel(const float *__res
       }
       if (lane < kDm21InPad) uf[rr * kDm21InPad + lane] = lane < n_in ? (float)u[r * kDm21InPad + lane] : 0.0f;
       if (du) {
-        for (int j = 0; j < kDm21InPad; ++j) {
+#pragma unroll
+        for (int j = 0; j < kDm21InPad; ++j) {  // independent warp sums: unrolled so they overlap
           float sj = 0.0f;
           if (j < n_in) {
             float sf = 0.0f;
