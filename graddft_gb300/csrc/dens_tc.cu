@@ -326,11 +326,10 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
 // Ragged form of dens_tc_kernel (same roles and arithmetic per tile): a
 // persistent grid takes (molecule, tile) items from the queue; the operand
 // pipeline, the barriers' phases and TMEM carry over from item to item, and
-// the CTA's warps meet at each item boundary.  (kRagged = false, one tile per
-// CTA, is the single-molecule case; dens_tc_kernel keeps that form on its own
-// code path, which measured 9 % faster than this one.)
-template <bool kRagged>
-__global__ void __launch_bounds__(kThreads, 1) dens_tc_ragged_kernel(const DensArgs A0, const DensQueue Q) {
+// the CTA's warps meet at each item boundary.  (The single-molecule case keeps
+// dens_tc_kernel, one tile per CTA: this form, run that way, measured 9 %
+// slower there.)
+__global__ void __launch_bounds__(kThreads, 1) dens_tc_ragged_kernel(const DensQueue Q) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full[kStages], empty[kStages], wfull[2], wempty[2], drain;
@@ -340,7 +339,7 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_ragged_kernel(const DensA
   __shared__ volatile int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int *const err0 = kRagged ? Q.err : A0.err;
+  int *const err0 = Q.err;
 
   if (threadIdx.x == 0) {
     s_abort = 0;
@@ -363,33 +362,29 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_ragged_kernel(const DensA
   uint32_t p_it = 0;              // producer: stages issued
   uint32_t m_it = 0, m_sub = 0;   // MMA issuer: stages consumed, W buffers filled
   uint32_t e_sub = 0;             // epilogue: W buffers folded
-  for (int round = 0;; ++round) {
+  for (;;) {
     __syncthreads();  // every role is done with the previous item
     if (threadIdx.x == 0) {
       int64_t item = INT64_MAX;
       if (!s_abort) {
-        if (kRagged) {
-          item = atomicAdd(Q.counter, 1);
-          if (item < Q.n_items) {
-            int lo = 0, hi = Q.n_mol;  // first[lo] <= item < first[hi]
-            while (hi - lo > 1) {
-              const int mid = (lo + hi) >> 1;
-              if (Q.first[mid] <= item) lo = mid; else hi = mid;
-            }
-            s_mol = lo;
-          } else {
-            item = INT64_MAX;
+        item = atomicAdd(Q.counter, 1);
+        if (item < Q.n_items) {
+          int lo = 0, hi = Q.n_mol;  // first[lo] <= item < first[hi]
+          while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (Q.first[mid] <= item) lo = mid; else hi = mid;
           }
-        } else if (round == 0) {
-          item = blockIdx.x;
+          s_mol = lo;
+        } else {
+          item = INT64_MAX;
         }
       }
       s_item = item;
     }
     __syncthreads();
     if (s_item == INT64_MAX) break;
-    const DensArgs A = kRagged ? Q.mols[s_mol] : A0;
-    const int64_t tile = kRagged ? s_item - Q.first[s_mol] : s_item;
+    const DensArgs A = Q.mols[s_mol];
+    const int64_t tile = s_item - Q.first[s_mol];
     const int nkc = A.ldk / 32, ncb = A.ldk / kBN;
     const int njobs = 4 * ncb;
     const int nkq = A.ldk / kSubK, kc_per_sub = kSubK / 32;
@@ -648,7 +643,7 @@ size_t dens_ragged_scratch_bytes(int n_mol) {
 cudaError_t launch_dens_tc_ragged(const DensMol *mols, int n_mol, void *d_scratch, int *err, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(dens_tc_ragged_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    cudaError_t e = cudaFuncSetAttribute(dens_tc_ragged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     if (e != cudaSuccess) return e;
     attr = true;
   }
@@ -698,7 +693,7 @@ cudaError_t launch_dens_tc_ragged(const DensMol *mols, int n_mol, void *d_scratc
     if (e != cudaSuccess) return e;
   }
   const DensQueue q{d_mols, d_first, n_mol, items, d_counter, err};
-  dens_tc_ragged_kernel<true><<<(unsigned)(items < n_sm ? items : n_sm), kThreads, kSmemBytes, st>>>(DensArgs{}, q);
+  dens_tc_ragged_kernel<<<(unsigned)(items < n_sm ? items : n_sm), kThreads, kSmemBytes, st>>>(q);
   return cudaGetLastError();
 }
 
