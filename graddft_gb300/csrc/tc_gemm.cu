@@ -11,8 +11,9 @@
 // products per term (hi*hi + hi*lo + lo*hi).  Each 32-wide K chunk is
 // accumulated in one of three TMEM buffers W (the MMA runs up to two chunks
 // ahead of the drains), correction products first, and the drains fold it into
-// a Kahan-compensated FP32 running sum: S in TMEM (columns 384-511), the
-// compensation C in registers.  A single split may write FP32 output instead.
+// a Kahan-compensated FP32 running sum, the sum S and the compensation C both
+// in registers (packed pairs), so a chunk's fold reads W once from TMEM.  A
+// single split may write FP32 output instead.
 //
 // tcg3_kernel (block-scaled, six products): blocks [tile][K chunk][hi|lo|lo2]
 // written by umma::store_row3, whose hi slices are quantised per row and K
@@ -53,8 +54,7 @@ constexpr int kStages3 = 2;
 constexpr int kSmem3Bytes = kStages3 * kStage3Bytes + 1024;
 constexpr int kThreads = 320;
 constexpr int kWBufs = 3;
-constexpr uint32_t kTmemCols = 512;  // tcg: W0..W2 [0, 384), S [384, 512); tcg3: (Y, X) x 2
-constexpr uint32_t kScol = 384;
+constexpr uint32_t kTmemCols = 512;  // tcg: W0..W2 [0, 384); tcgw: 2 x 2 W buffers; tcg3: (Y, X) x 2
 
 __device__ __forceinline__ void flag(int *err, int code) { atomicCAS(err, 0, code); }
 
@@ -171,9 +171,9 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
     __syncwarp();
   } else {
     // -------------------------------------------------------------- drains
-    // Per tile: every K stage's W is folded into the running sum S (TMEM) with
-    // Kahan compensation C in registers; after the tile's last stage S - C is
-    // written out and the next tile starts over.
+    // Per tile: every K stage's W is folded into the running sum S with Kahan
+    // compensation C, both in registers (one TMEM read of W per stage); after
+    // the tile's last stage S - C is written out and the next tile starts over.
     const int q = warp & 3, half = (warp - 2) >> 2;
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16) + half * 64;
     int64_t it = 0;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
       // Compensations of this thread's 64 columns as 32 packed FP32 pairs: the
       // fold runs on add/sub.rn.f32x2, two columns per instruction, each
       // rounded exactly like the scalar operation.
-      uint64_t C2[32];
+      uint64_t S2[32], C2[32];  // running sums and compensations, column pairs, in registers
 #pragma unroll
       for (int i = 0; i < 32; ++i) C2[i] = 0ull;
       int64_t k = 0;
@@ -197,72 +197,84 @@ __global__ void __launch_bounds__(kThreads, 1) tcg_kernel(const TcgArgs A) {
         umma::tc_fence_after();
 #pragma unroll
         for (int c = 0; c < 64; c += 16) {
-          uint32_t wr[16], sr[16];
+          uint32_t wr[16];
           umma::tmem_ld16_nowait(tl + buf * 128 + c, wr);
-          if (k > 0) umma::tmem_ld16_nowait(tl + kScol + c, sr);
-          umma::tmem_ld_wait(wr, sr);
-          if (k > 0) {
+          umma::tmem_ld_wait(wr);
 #pragma unroll
-            for (int i = 0; i < 16; i += 2) {  // Kahan: S + (w - C)
-              const uint64_t sp = umma::pk2(sr[i], sr[i + 1]);
-              const uint64_t y = umma::sub2(umma::pk2(wr[i], wr[i + 1]), C2[(c + i) / 2]);
+          for (int i = 0; i < 16; i += 2) {
+            const uint64_t w2 = umma::pk2(wr[i], wr[i + 1]);
+            if (k > 0) {  // Kahan: S + (w - C)
+              const uint64_t sp = S2[(c + i) / 2];
+              const uint64_t y = umma::sub2(w2, C2[(c + i) / 2]);
               const uint64_t t = umma::add2(sp, y);
               C2[(c + i) / 2] = umma::sub2(umma::sub2(t, sp), y);
-              umma::unpk2(t, sr[i], sr[i + 1]);
+              S2[(c + i) / 2] = t;
+            } else {
+              S2[(c + i) / 2] = w2;
             }
-            umma::tmem_st16(tl + kScol + c, sr);
-          } else {
-            umma::tmem_st16(tl + kScol + c, wr);
           }
         }
-        umma::tmem_st_wait();
         umma::tc_fence_before();
         umma::mbar_arrive(&wempty[buf]);
       }
       const bool have = ok && k == nst && nst > 0;
-      float C[64];
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        uint32_t lo, hi;
-        umma::unpk2(C2[i], lo, hi);
-        C[2 * i] = __uint_as_float(lo);
-        C[2 * i + 1] = __uint_as_float(hi);
-      }
       const int m = mt * 128 + q * 32 + lane;
       const int n0 = nt * 128 + half * 64;
+      // Output S - C, one column pair at a time from the packed registers.
+      auto pair = [&](int i, float &x, float &y) {
+        uint32_t s0, s1, c0, c1;
+        umma::unpk2(S2[i], s0, s1);
+        umma::unpk2(C2[i], c0, c1);
+        x = __uint_as_float(s0) - __uint_as_float(c0);
+        y = __uint_as_float(s1) - __uint_as_float(c1);
+      };
+      auto pair64 = [&](int i, double &x, double &y) {
+        uint32_t s0, s1, c0, c1;
+        umma::unpk2(S2[i], s0, s1);
+        umma::unpk2(C2[i], c0, c1);
+        x = (double)__uint_as_float(s0) - (double)__uint_as_float(c0);
+        y = (double)__uint_as_float(s1) - (double)__uint_as_float(c1);
+      };
+      if (m < A.m_valid) {
+        // Each lane owns one output row: whole 16-byte pieces where the row
+        // segment is in range and aligned (a lane's 64 values are 256 bytes).
+        if (A.out32) {
+          float *row = A.out32 + (size_t)m * A.ldo + n0;
+          if (n0 + 64 <= A.n_valid && (A.ldo & 3) == 0) {
 #pragma unroll
-      for (int c = 0; c < 64; c += 32) {
-        float sv[32];
-        if (have) umma::tmem_ld32(tl + kScol + c, sv);
-        if (m < A.m_valid) {
-          // Each lane owns one output row: whole 16-byte pieces where the row
-          // segment is in range and aligned (a lane's 32 values are 128 bytes).
-          if (A.out32) {
-            float *row = A.out32 + (size_t)m * A.ldo + n0 + c;
-            if (n0 + c + 32 <= A.n_valid && (A.ldo & 3) == 0) {
-#pragma unroll
-              for (int i = 0; i < 32; i += 4)
-                *reinterpret_cast<float4 *>(row + i) =
-                    have ? make_float4(sv[i] - C[c + i], sv[i + 1] - C[c + i + 1], sv[i + 2] - C[c + i + 2],
-                                       sv[i + 3] - C[c + i + 3])
-                         : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            } else {
-#pragma unroll
-              for (int i = 0; i < 32; ++i)
-                if (n0 + c + i < A.n_valid) row[i] = have ? sv[i] - C[c + i] : 0.0f;
+            for (int i = 0; i < 64; i += 4) {
+              float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+              if (have) {
+                pair(i / 2, v.x, v.y);
+                pair(i / 2 + 1, v.z, v.w);
+              }
+              *reinterpret_cast<float4 *>(row + i) = v;
             }
           } else {
-            double *row = A.out64 + ((size_t)blockIdx.y * A.m_valid + m) * A.n_valid + n0 + c;
-            if (n0 + c + 32 <= A.n_valid && (A.n_valid & 1) == 0) {
 #pragma unroll
-              for (int i = 0; i < 32; i += 2)
-                *reinterpret_cast<double2 *>(row + i) =
-                    have ? make_double2((double)sv[i] - (double)C[c + i], (double)sv[i + 1] - (double)C[c + i + 1])
-                         : make_double2(0.0, 0.0);
-            } else {
+            for (int i = 0; i < 64; i += 2) {
+              float x = 0.0f, y = 0.0f;
+              if (have) pair(i / 2, x, y);
+              if (n0 + i < A.n_valid) row[i] = x;
+              if (n0 + i + 1 < A.n_valid) row[i + 1] = y;
+            }
+          }
+        } else {
+          double *row = A.out64 + ((size_t)blockIdx.y * A.m_valid + m) * A.n_valid + n0;
+          if (n0 + 64 <= A.n_valid && (A.n_valid & 1) == 0) {
 #pragma unroll
-              for (int i = 0; i < 32; ++i)
-                if (n0 + c + i < A.n_valid) row[i] = have ? (double)sv[i] - (double)C[c + i] : 0.0;
+            for (int i = 0; i < 64; i += 2) {
+              double x = 0.0, y = 0.0;
+              if (have) pair64(i / 2, x, y);
+              *reinterpret_cast<double2 *>(row + i) = make_double2(x, y);
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 64; i += 2) {
+              double x = 0.0, y = 0.0;
+              if (have) pair64(i / 2, x, y);
+              if (n0 + i < A.n_valid) row[i] = x;
+              if (n0 + i + 1 < A.n_valid) row[i + 1] = y;
             }
           }
         }
