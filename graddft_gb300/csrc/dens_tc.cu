@@ -29,6 +29,11 @@
 // per (TMEM lane quadrant = warp % 4, spin).  Three 64 KB smem stages.  Every wait is
 // bounded (umma::mbar_wait); on expiry the CTA records an error word, waits
 // for its own copies and MMAs to land and releases TMEM.
+//
+// Two launch forms: dens_tc_kernel, one CTA per 128-point tile of one
+// molecule; dens_tc_ragged_kernel, a persistent grid over several molecules'
+// tiles taken from a device work queue (launch_dens_tc_ragged: the batch of
+// molecules in one launch, largest n_ao first).
 #include "common.cuh"
 #include "kernels.cuh"
 #include "umma.cuh"
