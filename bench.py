@@ -1134,7 +1134,10 @@ def main():
         t, n = ctypes.c_double(), ctypes.c_int64()
         _lib.check(lib.gdft_profile_read(sid, ctypes.byref(t), ctypes.byref(n)))
         stage[name] = (t.value, n.value)
-    launches = sum(n for _, n in stage.values())
+    # Kernels per step of the library's XC call (the stage timers count regions, some of which hold
+    # several kernels): mixed pack_rdm1, dens_tc, xc_point, energy_reduce, build_q, tcg3, vxc_q_reduce;
+    # FP64 dens_f64, xc_point, energy_reduce, vxc_f64, vxc_reduce.
+    launches = (7 if form == "tf32x3" else 5) * args.steps
     if world > 1:
         import torch.distributed as dist
 
