@@ -155,6 +155,20 @@ __device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ double xasinh(double x) { return asinh(x); }
 __device__ __forceinline__ double xatan(double x) { return atan(x); }
 __device__ __forceinline__ double xpow(double x, double p) { return pow(x, p); }
+__device__ __forceinline__ double xpow3(double x, int n) {
+  if (!(x >= 0.0)) return pow(x, n / 3.0);  // NaN for negative or NaN x, as pow
+  if (n == -1) return rcbrt(x);
+  if (n == -5) {
+    const double r = rcbrt(x);
+    return (r * r) / x;
+  }
+  if (n == 4) return x * cbrt(x);
+  if (n == 8) {
+    const double c = cbrt(x);
+    return (x * x) * (c * c);
+  }
+  return pow(x, n / 3.0);
+}
 __device__ __forceinline__ double xsq(double x) { return x * x; }
 __device__ __forceinline__ double xclipmin(double x, double c) { return isnan(x) ? x : fmax(c, x); }
 __device__ __forceinline__ double xabs(double x) { return fabs(x); }
@@ -197,6 +211,16 @@ __device__ __forceinline__ Dual<K> xatan(const Dual<K> &x) {
 template <int K>
 __device__ __forceinline__ Dual<K> xpow(const Dual<K> &x, double p) {
   return chain(x, pow(x.v, p), p * pow(x.v, p - 1.0));
+}
+// x ** (n/3) with an integer n from CUDA's cube roots (cbrt and rcbrt are
+// within 1 ulp; pow evaluates a logarithm and an exponential): n = -1, -5, 4
+// and 8, the powers of LYP and B88, to within a few ulp (pow for x < 0 or NaN);
+// partial (n/3) f / x (elsewhere than at finite x > 0 the pow form, p x ** (p - 1)).
+template <int K>
+__device__ __forceinline__ Dual<K> xpow3(const Dual<K> &x, int n) {
+  const double f = xpow3(x.v, n);
+  const double df = x.v > 0.0 && isfinite(f) ? (n / 3.0) * f / x.v : (n / 3.0) * pow(x.v, n / 3.0 - 1.0);
+  return chain(x, f, df);
 }
 // x ** 2 with an integer exponent (jax integer_pow JVP: 2 x).
 template <int K>

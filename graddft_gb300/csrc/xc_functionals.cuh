@@ -3,6 +3,8 @@
 // Each function restates one reference function for a single grid point,
 // keeping its evaluation order, clip and where semantics; it is a template
 // over the scalar type (double for values, Dual<K> for values plus partials).
+// Powers of a third come from cube roots (xpow3), within a few ulp of pow, and
+// B88 is evaluated without its logarithms (see b88_x_e).
 // Inputs per point: rho[2], s[2] = |grad rho_sigma|^2, st = |grad rho_a +
 // grad rho_b|^2, lap[2], tau[2].
 #pragma once
@@ -78,6 +80,12 @@ __device__ __forceinline__ T lsda_x_e(const T rho_in[2], double clip) {
 }
 
 // b88_x_e, popular_functionals.py:52-103 (gradient correction, summed over spin).
+// The reference works in base-2 logarithms: with g = |grad rho_s| (its squared
+// norm clipped), log x = log2 g - 4/3 log2 rho and the term
+// beta 2^(4/3 log2 rho + 2 log x - log2 D), D = 1 + 6 beta x asinh(x).  Since
+// 4/3 log2 rho + 2 log x = log2(g x), the term is beta g x / D with
+// x = g / rho^(4/3): the same function (and the same clips) without the four
+// logarithms and exponentials per spin.
 template <class T>
 __device__ __forceinline__ T b88_x_e(const T rho_in[2], const T s[2], double clip) {
   const double beta = 0.0042;
@@ -85,11 +93,9 @@ __device__ __forceinline__ T b88_x_e(const T rho_in[2], const T s[2], double cli
 #pragma unroll
   for (int sp = 0; sp < 2; ++sp) {
     const T rho = xclipmin(rho_in[sp], clip);
-    const T log_rho = xlog2(xclipmin(rho, clip));
-    const T log_g = xlog2(xclipmin(s[sp], clip)) / 2.0;
-    const T log_x = log_g - 4.0 / 3.0 * log_rho;
-    const T x = xexp2(log_x);
-    const T term = beta * xexp2(4.0 * log_rho / 3.0 + 2.0 * log_x - xlog2(1.0 + 6.0 * beta * x * xasinh(x)));
+    const T g = xsqrt(xclipmin(s[sp], clip));
+    const T x = g / xpow3(xclipmin(rho, clip), 4);
+    const T term = beta * (g * x) / (1.0 + 6.0 * beta * x * xasinh(x));
     out = sp == 0 ? term : out + term;
   }
   return -out;
@@ -166,9 +172,9 @@ __device__ __forceinline__ T lyp_c_e(const T rho_in[2], const T s[2], const T la
   const T rhos_ts = rsum * (t0 + t1);
   const T rho_t = r0 * t0 + r1 * t1;
   const T rho_grad2rho = r0 * lap[0] + r1 * lap[1];
-  const T rhom1_3 = xpow(rsum, -1.0 / 3.0);
-  const T rho8_3 = xpow(r0, 8.0 / 3.0) + xpow(r1, 8.0 / 3.0);
-  const T rhom5_3 = xpow(rsum, -5.0 / 3.0);
+  const T rhom1_3 = xpow3(rsum, -1);
+  const T rho8_3 = xpow3(r0, 8) + xpow3(r1, 8);
+  const T rhom5_3 = xpow3(rsum, -5);
   const T exp_factor = xwhere(val(rsum) > 0.0, xexp(-c * rhom1_3), zero);
   const T parenthesis = pow(2.0, 2.0 / 3.0) * CF * rho8_3 - rhos_ts + rho_t / 9.0 + rho_grad2rho / 18.0;
   const T braket = xwhere(big, 2.0 * b * rhom5_3 * parenthesis * exp_factor, zero);
