@@ -10,7 +10,9 @@
 // against the AO planes exactly as the FP64 form (dens_f64.cu) does:
 //   t = phi : rho, grad rho (x2), and the phi*lap part of the Laplacian
 //   t = d_j : the d_j phi . d_j phi part of the Laplacian and tau.
-// Row reductions use FP32 FMA chains of 8 products summed in FP64.
+// Row reductions use FP32 FMA chains of 8 products whose four chains per unit
+// and the units of a feature are summed as FP32 pairs (TwoSum; about 2^-44 of
+// the terms): GB300 runs FP64 conversions and adds at 1/64 of the FP32 rate.
 //
 // Accumulation: the tensor cores truncate every MMA's products to the
 // accumulator's ulp grid, so long FP32 accumulation chains drift towards
@@ -35,6 +37,7 @@
 // tiles taken from a device work queue (launch_dens_tc_ragged: the batch of
 // molecules in one launch, largest n_ao first).
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "kernels.cuh"
 #include "umma.cuh"
 
@@ -214,9 +217,9 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
     const int sp = (warp - 2) >> 2;  // spin handled by this warp
     const int row = q * 32 + lane;
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16) + sp * kBN;  // this spin's 64 columns
-    double F[6];
+    df::DF F[6];  // per-feature sums as FP32 pairs
 #pragma unroll
-    for (int k = 0; k < 6; ++k) F[k] = 0.0;
+    for (int k = 0; k < 6; ++k) F[k] = df::of(0.0f);
     // Row-reduction unit u of job jr: plane k, columns 32 (u % 2) .. + 31 of the job's block.
     auto unit_plane = [&](int jr, int u) { return (jr / ncb == 0 ? 0 : jr / ncb) + (u >> 1); };
     auto unit_blk = [&](int jr, int u) {
@@ -245,15 +248,15 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
         a[2] = fmaf(x[4 * g + 2], ph[g].z + pl[g].z, a[2]);
         a[3] = fmaf(x[4 * g + 3], ph[g].w + pl[g].w, a[3]);
       }
-      const double d = ((double)a[0] + (double)a[1]) + ((double)a[2] + (double)a[3]);
+      const df::DF d = df::add(df::two_sum(a[0], a[1]), df::two_sum(a[2], a[3]));
       const int k = unit_plane(jr, u);
       switch (jr / ncb == 0 ? k : 5) {
-        case 0: F[0] += d; break;
-        case 1: F[1] += d; break;
-        case 2: F[2] += d; break;
-        case 3: F[3] += d; break;
-        case 4: F[4] += d; break;
-        default: F[5] += d; break;
+        case 0: F[0] = df::add(F[0], d); break;
+        case 1: F[1] = df::add(F[1], d); break;
+        case 2: F[2] = df::add(F[2], d); break;
+        case 3: F[3] = df::add(F[3], d); break;
+        case 4: F[4] = df::add(F[4], d); break;
+        default: F[5] = df::add(F[5], d); break;
       }
     };
     int pj = -1, pu = 0;  // pending unit (job, index), issued but not consumed
@@ -316,12 +319,15 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_kernel(const DensArgs A) 
     }
     const int64_t p = tile * 128 + row;
     double *fs = A.feat + (size_t)sp * kFeat * A.ldf;
-    fs[F_RHO * A.ldf + p] = F[T_PHI];
-    fs[F_GX * A.ldf + p] = 2.0 * F[T_DX];
-    fs[F_GY * A.ldf + p] = 2.0 * F[T_DY];
-    fs[F_GZ * A.ldf + p] = 2.0 * F[T_DZ];
-    fs[F_LAP * A.ldf + p] = 2.0 * F[5] + 2.0 * F[T_LAP];
-    fs[F_TAU * A.ldf + p] = 0.5 * F[5];
+    double Fd[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) Fd[k] = (double)F[k].s + (double)F[k].c;
+    fs[F_RHO * A.ldf + p] = Fd[T_PHI];
+    fs[F_GX * A.ldf + p] = 2.0 * Fd[T_DX];
+    fs[F_GY * A.ldf + p] = 2.0 * Fd[T_DY];
+    fs[F_GZ * A.ldf + p] = 2.0 * Fd[T_DZ];
+    fs[F_LAP * A.ldf + p] = 2.0 * Fd[5] + 2.0 * Fd[T_LAP];
+    fs[F_TAU * A.ldf + p] = 0.5 * Fd[5];
   }
   umma::tc_fence_before();
   __syncthreads();
@@ -493,9 +499,9 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_ragged_kernel(const DensQ
     const int sp = (warp - 2) >> 2;  // spin handled by this warp
     const int row = q * 32 + lane;
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16) + sp * kBN;  // this spin's 64 columns
-    double F[6];
+    df::DF F[6];  // per-feature sums as FP32 pairs
 #pragma unroll
-    for (int k = 0; k < 6; ++k) F[k] = 0.0;
+    for (int k = 0; k < 6; ++k) F[k] = df::of(0.0f);
     // Row-reduction unit u of job jr: plane k, columns 32 (u % 2) .. + 31 of the job's block.
     auto unit_plane = [&](int jr, int u) { return (jr / ncb == 0 ? 0 : jr / ncb) + (u >> 1); };
     auto unit_blk = [&](int jr, int u) {
@@ -524,15 +530,15 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_ragged_kernel(const DensQ
         a[2] = fmaf(x[4 * g + 2], ph[g].z + pl[g].z, a[2]);
         a[3] = fmaf(x[4 * g + 3], ph[g].w + pl[g].w, a[3]);
       }
-      const double d = ((double)a[0] + (double)a[1]) + ((double)a[2] + (double)a[3]);
+      const df::DF d = df::add(df::two_sum(a[0], a[1]), df::two_sum(a[2], a[3]));
       const int k = unit_plane(jr, u);
       switch (jr / ncb == 0 ? k : 5) {
-        case 0: F[0] += d; break;
-        case 1: F[1] += d; break;
-        case 2: F[2] += d; break;
-        case 3: F[3] += d; break;
-        case 4: F[4] += d; break;
-        default: F[5] += d; break;
+        case 0: F[0] = df::add(F[0], d); break;
+        case 1: F[1] = df::add(F[1], d); break;
+        case 2: F[2] = df::add(F[2], d); break;
+        case 3: F[3] = df::add(F[3], d); break;
+        case 4: F[4] = df::add(F[4], d); break;
+        default: F[5] = df::add(F[5], d); break;
       }
     };
     int pj = -1, pu = 0;  // pending unit (job, index), issued but not consumed
@@ -599,12 +605,15 @@ __global__ void __launch_bounds__(kThreads, 1) dens_tc_ragged_kernel(const DensQ
     if (ok) {
       const int64_t p = tile * 128 + row;
       double *fs = A.feat + (size_t)sp * kFeat * A.ldf;
-      fs[F_RHO * A.ldf + p] = F[T_PHI];
-      fs[F_GX * A.ldf + p] = 2.0 * F[T_DX];
-      fs[F_GY * A.ldf + p] = 2.0 * F[T_DY];
-      fs[F_GZ * A.ldf + p] = 2.0 * F[T_DZ];
-      fs[F_LAP * A.ldf + p] = 2.0 * F[5] + 2.0 * F[T_LAP];
-      fs[F_TAU * A.ldf + p] = 0.5 * F[5];
+      double Fd[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) Fd[k] = (double)F[k].s + (double)F[k].c;
+      fs[F_RHO * A.ldf + p] = Fd[T_PHI];
+      fs[F_GX * A.ldf + p] = 2.0 * Fd[T_DX];
+      fs[F_GY * A.ldf + p] = 2.0 * Fd[T_DY];
+      fs[F_GZ * A.ldf + p] = 2.0 * Fd[T_DZ];
+      fs[F_LAP * A.ldf + p] = 2.0 * Fd[5] + 2.0 * Fd[T_LAP];
+      fs[F_TAU * A.ldf + p] = 0.5 * Fd[5];
     }
   }
   }  // items
