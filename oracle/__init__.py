@@ -1,7 +1,7 @@
 """CPU oracle for the XC grid path (test infrastructure only).
 
-This package is the checker: ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` may call it.  The product path in
+The oracle checks the CUDA path: only ``tests/``, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` may call it.  The product path in
 ``graddft_gb300`` never imports it.
 """
 from .oracle import *  # noqa: F401,F403
